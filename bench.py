@@ -1,0 +1,341 @@
+"""Benchmark of the Wilson-clover Dirac operator / MG solve path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload dslash|cg] [--impl ours|reference]
+
+Prints ONE JSON line (rank 0).  A step is one pass of the hot path over one
+batch of seeded synthetic input (theta ~ N(0, 1/beta) links, Gaussian
+sources), timed with CUDA events on the library's stream between a barrier and
+a device synchronize, max over ranks.  Workloads:
+
+* dslash — FP32 D applied to 32 right-hand sides on the 512 x 512 lattice
+  (beta = 6, m = -0.05, c_sw = 1), the fine-operator configuration of the
+  multi-RHS MG benchmark.  Inputs (134 MB) and outputs exceed the 129 MB L2.
+  value = algorithmic HBM GB/s.
+* cg     — FP64 CG on D^dag D to ||r||/||b|| <= 1e-10 on the 32 x 32 lattice
+  (beta = 2, m = 0.1, c_sw = 1).  value = solves/s.
+
+`--impl reference` times the reference's CPU implementation of the same
+workload on this machine's host cores (the C restatement, oracle/), and prints
+the same line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Dslash HBM GB/s; MG-GCR solves/s to 1e-10, mixed+batched vs plain FP64"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device),
+                 "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        try:
+            self.path.unlink()
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median([r[0] for r in rows])), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# --------------------------------------------------------------------- workloads
+DSLASH = dict(L=512, nrhs=32, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20240)
+CG = dict(L=32, beta=2.0, m=0.1, r=1.0, csw=1.0, mu=0.0, seed=31, tol=1e-10, max_iter=10000)
+
+
+def dslash_bytes_f32(L, nrhs):
+    """Compulsory HBM bytes of one FP32 D application to nrhs right-hand sides:
+    spinor in + out (2 x 16 B per site per rhs), 2 complex64 links (16 B) and
+    the clover shift (4 B) per site."""
+    return L * L * (32 * nrhs + 20)
+
+
+def dslash_bytes_f64_single(L):
+    """13 x 8 B per site for one FP64 single-RHS application (in 32, out 32, links 32, clover 8)."""
+    return L * L * 104
+
+
+def run_ours(args, ws, rank, local):
+    import ctypes as Cc
+
+    import torch
+
+    import schwinger_mg_gb300 as smg
+
+    torch.cuda.set_device(local)
+    ctx = smg.Context(local)
+    lib = smg.lib()
+    peak, peak_kind = peaks()
+    out = {"metric": METRIC, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "scaling": "weak",
+           "vs_baseline": None, "data": "synthetic (seeded theta ~ N(0,1/beta) links, Gaussian sources)"}
+    dp = Cc.POINTER(Cc.c_double)
+
+    def timed(step, n):
+        """Device milliseconds per step on the library's stream, max over ranks."""
+        ctx.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        ctx.timer_begin()
+        for _ in range(n):
+            step()
+        ms = ctx.timer_end() / n
+        return max_over_ranks(ms, ws)
+
+    if args.workload == "dslash":
+        c = DSLASH
+        L, nrhs = c["L"], c["nrhs"]
+        U = smg.gauge_normal(L, c["beta"], c["seed"])
+        lat = smg.Lattice(L)
+        g = smg.GaugeField(lat, U, ctx)
+        D = smg.DiracOp(lat, g, c["m"], c["r"], c["csw"], c["mu"])
+        srcs = np.stack([smg.random_vec(lat.ndof, c["seed"] + 1 + j) for j in range(nrhs)])
+        fs = smg.Field(lat, nrhs, "f32", ctx, data=srcs)
+        fd = smg.Field(lat, nrhs, "f32", ctx)
+        bytes_step = dslash_bytes_f32(L, nrhs)
+
+        def step():
+            smg._lib.check(lib.smg_dirac_apply(D.h, 0, fs.h, fd.h), "dirac_apply", ctx.h)
+
+        for _ in range(args.warmup):
+            step()
+        l0 = ctx.kernel_launches
+        with Clocks(local) as clk:
+            ms = timed(step, args.steps)
+        launches = ctx.kernel_launches - l0
+        value = ws * bytes_step / (ms * 1e-3) / 1e9
+        achieved = bytes_step / (ms * 1e-3) / 1e9
+
+        # end to end through the C ABI with pinned host buffers, every step
+        host_in = torch.empty(srcs.size * 2, dtype=torch.float64).pin_memory()
+        host_in.numpy()[:] = srcs.reshape(-1).view(np.float64)
+        host_out = torch.empty_like(host_in).pin_memory()
+        pin, pout = Cc.cast(host_in.data_ptr(), dp), Cc.cast(host_out.data_ptr(), dp)
+
+        def e2e_step():
+            smg._lib.check(lib.smg_field_upload_async(fs.h, pin), "upload", ctx.h)
+            step()
+            smg._lib.check(lib.smg_field_download_async(fd.h, pout), "download", ctx.h)
+
+        for _ in range(2):
+            e2e_step()
+        e2e_ms = timed(e2e_step, args.steps)
+        got = host_out.numpy().view(np.complex128).reshape(nrhs, -1)
+        hb = srcs.size * 16
+        out.update({
+            "value": value, "unit": "GB/s", "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
+            "config": {"workload": "FP32 Wilson-clover D on 32 RHS, L=512 (beta=6, m=-0.05, c_sw=1)",
+                       "L": L, "nrhs": nrhs, "bytes_per_step": bytes_step,
+                       "l2": "inputs and outputs (268 MB) exceed the 129 MB L2; no flush"},
+            "e2e": {"value": ws * bytes_step / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
+                    "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb, "ms_per_step": e2e_ms,
+                    "finite": bool(np.isfinite(got).all())},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "kernel": "k_dslash<float,false,0>", "peak_source": peak_kind},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+        })
+    elif args.workload == "cg":
+        c = CG
+        L = c["L"]
+        U = smg.gauge_normal(L, c["beta"], c["seed"])
+        lat = smg.Lattice(L)
+        g = smg.GaugeField(lat, U, ctx)
+        D = smg.DiracOp(lat, g, c["m"], c["r"], c["csw"], c["mu"])
+        b = smg.random_vec(lat.ndof, c["seed"] + 1)
+        fb = smg.Field(lat, 1, "f64", ctx, data=b)
+        fx = smg.Field(lat, 1, "f64", ctx)
+        res = smg._lib.SolveResult()
+
+        def step():
+            st = lib.smg_cg_solve(D.h, fb.h, fx.h, c["max_iter"], c["tol"], Cc.byref(res))
+            smg._lib.check(st, "cg_solve", ctx.h)
+
+        for _ in range(args.warmup):
+            step()
+        l0 = ctx.kernel_launches
+        with Clocks(local) as clk:
+            ms = timed(step, args.steps)
+        launches = ctx.kernel_launches - l0
+        bh = b.copy()
+        xh = np.empty_like(bh)
+        pb, px = bh.view(np.float64).ctypes.data_as(dp), xh.view(np.float64).ctypes.data_as(dp)
+
+        def e2e_step():
+            smg._lib.check(lib.smg_field_upload(fb.h, pb), "upload", ctx.h)
+            step()
+            smg._lib.check(lib.smg_field_download(fx.h, px), "download", ctx.h)
+
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        e2e_ms = max_over_ranks(e2e_ms, ws)
+        out.update({"value": ws * 1e3 / ms, "unit": "solves/s", "ms_per_step": ms, "higher_is_better": True,
+                    "dtype": "f64",
+                    "config": {"workload": "FP64 CG on D^dag D, L=32 (beta=2, m=0.1, c_sw=1) to 1e-10",
+                               "iterations": res.iterations, "true_residual": res.true_residual,
+                               "l2": "working set is L2-resident within a solve"},
+                    "e2e": {"value": ws * 1e3 / e2e_ms, "unit": "solves/s", "h2d_bytes_per_step": bh.nbytes,
+                            "d2h_bytes_per_step": xh.nbytes, "ms_per_step": e2e_ms},
+                    "gpu_launches": int(launches), "clocks": clk.summary()})
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args.workload)
+    return out
+
+
+def max_over_ranks(v: float, ws: int) -> float:
+    if ws == 1:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(workload: str, threads: int | None = None):
+    """The oracle (C restatement of the reference's CPU path) on this host's cores, bounded sample."""
+    from oracle import oracle as O
+
+    import schwinger_mg_gb300 as smg
+
+    port = O.port()
+    n_threads = threads or os.cpu_count() or 1
+    port.set_threads(n_threads)
+    if workload == "dslash":
+        c = DSLASH
+        L, nrhs = c["L"], 8
+        U = smg.gauge_normal(L, c["beta"], c["seed"])
+        srcs = np.stack([smg.random_vec(2 * L * L, c["seed"] + 1 + j) for j in range(nrhs)])
+        port.time_dirac(U, c["m"], c["r"], c["csw"], c["mu"], 0, srcs[:1], 1)  # warm
+        t, _ = port.time_dirac(U, c["m"], c["r"], c["csw"], c["mu"], 0, srcs, 2)
+        gbs = 2 * nrhs * dslash_bytes_f64_single(L) / t / 1e9
+        return {"value": gbs, "unit": "GB/s", "cores": n_threads, "kind": "port",
+                "sample": f"FP64 D on {nrhs} RHS x 2 reps at L={L} (the reference computes one RHS at a time "
+                          "in FP64; 104 B/site per application)", "seconds": t}
+    c = CG
+    U = smg.gauge_normal(c["L"], c["beta"], c["seed"])
+    b = smg.random_vec(2 * c["L"] ** 2, c["seed"] + 1)
+    reps, tot = 0, 0.0
+    while tot < 5.0 and reps < 200:
+        t, _, it = port.time_cg(U, c["m"], c["r"], c["csw"], c["mu"], b, c["max_iter"], c["tol"])
+        tot += t
+        reps += 1
+    return {"value": reps / tot, "unit": "solves/s", "cores": n_threads, "kind": "port",
+            "sample": f"{reps} FP64 CG solves at L={c['L']} ({it} iterations each)", "seconds": tot}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return None
+    base = cpu_baseline(args.workload)
+    val = base["value"]
+    line = {"metric": METRIC, "impl": "reference", "value": val, "unit": base["unit"], "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": args.workload},
+            "cpu_baseline": {"kind": base["kind"], "cores": base["cores"], "sample": base["sample"], "value": val},
+            "e2e": {"value": val, "unit": base["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--workload", default="dslash", choices=["dslash", "cg"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        line = run_reference(args, ws, rank)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    if ws > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    line = run_ours(args, ws, rank, local)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

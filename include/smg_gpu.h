@@ -1,0 +1,214 @@
+/*
+ * smg_gpu.h — C ABI of the GB300 (sm_103a) Wilson-clover Dirac operator and
+ * multigrid solve path for the 2D U(1) lattice Schwinger model.
+ *
+ * Every entry point takes plain pointers and sizes; no C++ or torch types
+ * cross this boundary.  Objects are opaque handles with explicit
+ * create/destroy.  Device memory belongs to the library; host arrays passed
+ * in are read (or written) before the call returns and are never retained.
+ *
+ * Host array conventions (identical to the reference's `Vec`/`GaugeField`):
+ *   - complex numbers are interleaved (re, im) doubles;
+ *   - a spinor is `v[2*s + spin]` with lexicographic site s = x + L*y
+ *     (reference src/types.h:8, src/lattice.h:19), i.e. 2*V complex = 4*V
+ *     doubles; a multi-RHS field is nrhs such spinors back to back;
+ *   - gauge links are `U[mu][s]`, mu = 0 (x) then 1 (y)
+ *     (reference src/gauge.h:12), i.e. 2*V complex = 4*V doubles;
+ *   - a force / momentum field is `F[mu][s]` real, 2*V doubles
+ *     (reference src/hmc.h:34).
+ *
+ * Each function returns an smg_status; SMG_OK is 0.  The reference signals
+ * failure through asserts, std::cerr warnings and early loop exits
+ * (reference src/prolongator.h:38, src/solvers.cpp:765, src/coarse_op.h:533);
+ * here every such condition maps to a status code, and
+ * smg_last_error() gives the message of the last failure in a context.
+ *
+ * Threading: one smg_context per host thread (or per CUDA stream); objects of
+ * distinct contexts may be used concurrently.  All work of a context is
+ * enqueued on that context's stream; calls that return host data synchronise
+ * that stream.
+ */
+#ifndef SMG_GPU_H
+#define SMG_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SMG_API __attribute__((visibility("default")))
+
+typedef enum {
+    SMG_OK = 0,
+    SMG_NOT_CONVERGED = 1,  /* iteration limit reached above tolerance      */
+    SMG_BREAKDOWN = 2,      /* zero / tiny denominator in a Krylov step      */
+    SMG_NONFINITE = 3,      /* NaN or Inf met in a residual or input         */
+    SMG_BAD_ARG = 4,        /* invalid size, null pointer or mismatch        */
+    SMG_DEVICE_ERROR = 5,   /* a CUDA call failed                            */
+    SMG_TIMEOUT = 6,        /* a bounded device-side wait ran out            */
+    SMG_NO_MEMORY = 7,      /* device allocation failed                      */
+    SMG_UNSUPPORTED = 8     /* configuration not built in this library       */
+} smg_status;
+
+typedef enum {
+    SMG_F64 = 0,   /* complex128 storage and arithmetic                      */
+    SMG_F32 = 1,   /* complex64 storage, FP32 arithmetic                     */
+    SMG_F16 = 2    /* FP16 storage with one FP32 scale per site, FP32 math   */
+} smg_precision;
+
+/* Operators a Dirac handle can apply (reference src/dirac.h:115-152). */
+typedef enum {
+    SMG_OP_D = 0,       /* DiracOp::apply        dirac.h:115 */
+    SMG_OP_DDAG = 1,    /* DiracOp::apply_dag    dirac.h:120 */
+    SMG_OP_DDAGD = 2,   /* DiracOp::apply_DdagD  dirac.h:136 */
+    SMG_OP_G5D = 3      /* DiracOp::apply_g5D    dirac.h:145 */
+} smg_operator;
+
+typedef struct smg_context smg_context;
+typedef struct smg_gauge smg_gauge;
+typedef struct smg_dirac smg_dirac;
+typedef struct smg_field smg_field;
+typedef struct smg_mg smg_mg;
+
+/* Result of a Krylov solve; mirrors CGResult / FCGResult
+ * (reference src/solvers.h:25-35).  final_residual is the solver's own
+ * (recursive) relative residual as the reference reports it; true_residual
+ * is ||b - A x|| / ||b|| recomputed in FP64 after the solve.  For a
+ * multi-RHS solve the fields hold the worst right-hand side. */
+typedef struct {
+    int iterations;
+    double final_residual;
+    double true_residual;
+    int operator_applications;  /* fine-grid A applications (D^dag D) */
+} smg_solve_result;
+
+/* ---------------------------------------------------------------- context */
+
+/* Creates a context on CUDA device `device`, enqueuing all work on `stream`
+ * (a cudaStream_t; NULL = the library creates its own non-blocking stream).
+ * No reference counterpart: the reference is a single-threaded CPU library
+ * with process globals (reference src/linalg.cpp:5-6). */
+SMG_API smg_status smg_context_create(int device, void* stream, smg_context** out);
+SMG_API smg_status smg_context_destroy(smg_context* ctx);
+SMG_API smg_status smg_context_synchronize(smg_context* ctx);
+SMG_API smg_status smg_context_set_stream(smg_context* ctx, void* stream);
+SMG_API void* smg_context_stream(smg_context* ctx);
+SMG_API const char* smg_last_error(smg_context* ctx);
+SMG_API const char* smg_status_string(smg_status s);
+/* Number of kernels this context has launched since creation (a counter the
+ * benchmark reads to report launches inside a timed region). */
+SMG_API uint64_t smg_context_kernel_launches(smg_context* ctx);
+/* Library version string, e.g. "smg-gb300 0.1 sm_103a". */
+SMG_API const char* smg_version(void);
+/* Stream-ordered timing on the context's stream: smg_timer_begin records a
+ * CUDA event, smg_timer_end records a second one, waits for it and returns
+ * the elapsed device time in milliseconds.  No reference counterpart (the
+ * reference times with std::chrono, e.g. src/mode_studies.cpp:1554). */
+SMG_API smg_status smg_timer_begin(smg_context* ctx);
+SMG_API smg_status smg_timer_end(smg_context* ctx, double* ms);
+
+/* ------------------------------------------------------------ gauge field */
+
+/* GaugeField (reference src/gauge.h:10-36).  L must be even and >= 4.
+ * U is 2*V complex, U[mu][s]. */
+SMG_API smg_status smg_gauge_create(smg_context* ctx, int L, const double* U, smg_gauge** out);
+SMG_API smg_status smg_gauge_destroy(smg_gauge* g);
+SMG_API smg_status smg_gauge_set(smg_gauge* g, const double* U);
+SMG_API smg_status smg_gauge_get(smg_gauge* g, double* U);
+SMG_API int smg_gauge_L(const smg_gauge* g);
+/* GaugeField::avg_plaq (reference src/gauge.h:32-36). */
+SMG_API smg_status smg_gauge_avg_plaq(smg_gauge* g, double* out);
+/* gauge_action = -beta * sum_s Re P(s) (reference src/hmc_forces.cpp:80-86). */
+SMG_API smg_status smg_gauge_action(smg_gauge* g, double beta, double* out);
+/* gauge_force (reference src/hmc_forces.cpp:88-111): force is 2*V doubles. */
+SMG_API smg_status smg_gauge_force(smg_gauge* g, double beta, double* force);
+
+/* ---------------------------------------------------------- Dirac operator */
+
+/* DiracOp(lat, gauge, mass, r, c_sw, mu_t) (reference src/dirac.h:17-22).
+ * Computes the clover field F01 on the device when c_sw != 0
+ * (reference src/dirac.h:26-52).  The Dirac handle reads the gauge handle's
+ * links at every apply; after smg_gauge_set call smg_dirac_refresh so the
+ * clover term follows the new links. */
+SMG_API smg_status smg_dirac_create(smg_gauge* g, double mass, double r, double c_sw,
+                                    double mu_t, smg_dirac** out);
+SMG_API smg_status smg_dirac_destroy(smg_dirac* d);
+SMG_API smg_status smg_dirac_refresh(smg_dirac* d);
+/* DiracOp::clover_field, V doubles (reference src/dirac.h:15). */
+SMG_API smg_status smg_dirac_get_clover(smg_dirac* d, double* F01);
+/* dst = op(src) for every right-hand side (reference src/dirac.h:115-152).
+ * src and dst must have the same L, nrhs and precision and be distinct. */
+SMG_API smg_status smg_dirac_apply(smg_dirac* d, smg_operator op, const smg_field* src,
+                                   smg_field* dst);
+
+/* ---------------------------------------------------------- spinor fields */
+
+/* A field holds nrhs spinors of an L x L lattice in the given precision.
+ * Device layout is even-odd, site-major, right-hand side innermost. */
+SMG_API smg_status smg_field_create(smg_context* ctx, int L, int nrhs, smg_precision prec,
+                                    smg_field** out);
+SMG_API smg_status smg_field_destroy(smg_field* f);
+/* host: nrhs * 2V complex in the reference's Vec layout. */
+SMG_API smg_status smg_field_upload(smg_field* f, const double* host);
+SMG_API smg_status smg_field_download(const smg_field* f, double* host);
+/* Same as upload/download but from/to page-locked host memory without an
+ * intermediate staging copy; `host` must be pinned (cudaHostAlloc). */
+SMG_API smg_status smg_field_upload_async(smg_field* f, const double* host);
+SMG_API smg_status smg_field_download_async(const smg_field* f, double* host);
+SMG_API smg_status smg_field_zero(smg_field* f);
+/* dst = src with precision conversion (same L and nrhs). */
+SMG_API smg_status smg_field_copy(const smg_field* src, smg_field* dst);
+SMG_API int smg_field_nrhs(const smg_field* f);
+SMG_API int smg_field_L(const smg_field* f);
+SMG_API smg_precision smg_field_precision(const smg_field* f);
+/* Raw device pointer and byte size of the field's storage. */
+SMG_API void* smg_field_device_ptr(smg_field* f);
+SMG_API size_t smg_field_bytes(const smg_field* f);
+
+/* ------------------------------------------------------------------ BLAS-1 */
+
+/* dot(a,b) = sum conj(a) b per right-hand side, out = nrhs complex
+ * (reference src/linalg.cpp:8-18). Reductions accumulate in FP64. */
+SMG_API smg_status smg_blas_dot(const smg_field* a, const smg_field* b, double* out);
+/* norm(v) per right-hand side, out = nrhs doubles (reference src/linalg.cpp:20). */
+SMG_API smg_status smg_blas_norm(const smg_field* a, double* out);
+/* y += alpha x, alpha = nrhs complex (reference src/linalg.cpp:22-26). */
+SMG_API smg_status smg_blas_axpy(const double* alpha, const smg_field* x, smg_field* y);
+/* v *= alpha, alpha = nrhs complex (reference src/linalg.cpp:35-39). */
+SMG_API smg_status smg_blas_scale(const double* alpha, smg_field* v);
+
+/* ---------------------------------------------------------------- solvers */
+
+/* cg_solve on A = D^dag D (reference src/solvers.cpp:16-78): unpreconditioned
+ * CG from x = 0, stopping when the recursive ||r||/||b|| < tol.  Runs in the
+ * precision of the fields (F64 or F32); every right-hand side is solved
+ * independently and stops on its own. */
+SMG_API smg_status smg_cg_solve(smg_dirac* d, const smg_field* rhs, smg_field* x,
+                                int max_iter, double tol, smg_solve_result* res);
+
+/* ------------------------------------------------------------------ forces */
+
+/* fermion_force (reference src/hmc_forces.cpp:134-194 and 198-495): with
+ * chi = D X recomputed on the device and never stored, force[mu][s] =
+ * -dS/dtheta_mu(s) for S = phi^dag (D^dag D)^-1 phi, X = (D^dag D)^-1 phi.
+ * X is a single-RHS F64 field; force is 2*V doubles on the host. */
+SMG_API smg_status smg_fermion_force(smg_dirac* d, const smg_field* X, double* force);
+
+/* -------------------------------------------------------- host utilities */
+
+/* Seeded synthetic inputs drawn with the C++ standard library generators the
+ * reference uses (std::mt19937 + std::normal_distribution<double>), so the
+ * same seed gives the reference's own numbers.
+ * Gauge: theta_mu(s) ~ N(0, 1/beta) i.i.d. drawn mu-major then site order,
+ * U = exp(i theta).  Vector: the order of random_vec as GCC on x86-64
+ * compiles it (reference src/linalg.cpp:44-48), which draws each entry's
+ * imaginary part before its real part. */
+SMG_API smg_status smg_host_gauge_normal(int L, double beta, uint32_t seed, double* U);
+SMG_API smg_status smg_host_random_vec(int64_t n_complex, uint32_t seed, double* v);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SMG_GPU_H */

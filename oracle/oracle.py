@@ -1,0 +1,343 @@
+"""ORACLE TEST INFRASTRUCTURE — not part of the product.
+
+ctypes loaders for the two CPU checkers:
+
+* ``port()`` — oracle/_build/libsmg_oracle.so, the plain-C restatement of the
+  reference path (smg_oracle.c).  Builds anywhere gcc and OpenMP exist, so it
+  is the checker on the GPU machine and the CPU baseline of bench.py.
+* ``ref()``  — oracle/_ref/libsmg_ref.so, the reference's own C++ sources
+  compiled by oracle/Makefile with the ref_shim.cpp entry points.  Exists only
+  where the reference tree was present at build time; ``ref()`` returns None
+  otherwise.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module.  Arrays are numpy complex128 in the reference layouts
+(spinor v[2*s+spin], links U[mu][s], force F[mu][s]).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+PORT_SO = HERE / "_build" / "libsmg_oracle.so"
+REF_SO = HERE / "_ref" / "libsmg_ref.so"
+REF_SRC = Path(os.environ.get("SMG_REFERENCE_SRC", "/root/reference/src"))
+
+_dp = C.POINTER(C.c_double)
+
+
+def build(ref: bool | None = None) -> None:
+    """Compiles the C restatement and, when the reference tree exists, the reference shim."""
+    targets = ["oracle"]
+    if ref is None:
+        ref = (REF_SRC / "dirac.h").exists()
+    if ref:
+        targets.append("ref")
+    subprocess.run(["make", "-s", "-j8", "-C", str(HERE), f"REF={REF_SRC}", *targets], check=True)
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+def _c(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+class RefMGParams(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("levels", "block_size", "k_null", "coarse_block", "null_iters", "w_cycle",
+                                         "pre_smooth", "post_smooth", "n_defl")]
+
+
+class OrcMG2Params(C.Structure):
+    _fields_ = [("L", C.c_int), ("bs", C.c_int), ("k", C.c_int), ("m", C.c_double), ("r", C.c_double),
+                ("csw", C.c_double), ("mu", C.c_double), ("pre_smooth", C.c_int), ("post_smooth", C.c_int),
+                ("coarse_max_iter", C.c_int), ("coarse_tol", C.c_double)]
+
+
+class _Lib:
+    """Common numpy-facing wrappers; `prefix` is 'orc_' (port) or 'ref_' (reference)."""
+
+    def __init__(self, path: Path, prefix: str):
+        self.lib = C.CDLL(str(path))
+        self.prefix = prefix
+        self.is_ref = prefix == "ref_"
+        f = self._f
+        f("clover").restype = None
+        f("avg_plaq").restype = C.c_double
+        f("dirac").restype = None
+        f("cg").restype = C.c_int
+        f("gauge_force").restype = None
+        f("gauge_action").restype = C.c_double
+        f("fermion_force").restype = None
+        f("mr_smooth").restype = None
+        f("near_null_space").restype = None
+        f("prolongator_build").restype = None
+        f("prolong").restype = None
+        f("restrict").restype = None
+        f("sparse_coarse_build").restype = None
+        f("sparse_coarse_apply").restype = None
+
+    def _f(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+    # -- geometry helpers
+    @staticmethod
+    def _L(U):
+        V = U.size // 2
+        L = int(round(V ** 0.5))
+        assert L * L == V
+        return L
+
+    def clover(self, U):
+        U = _c(U)
+        L = self._L(U)
+        out = np.empty(L * L)
+        self._f("clover")(C.c_int(L), _p(U), _p(out))
+        return out
+
+    def avg_plaq(self, U):
+        U = _c(U)
+        return self._f("avg_plaq")(C.c_int(self._L(U)), _p(U))
+
+    def dirac(self, U, m, r, csw, mu, op, src):
+        U = _c(U)
+        src = _c(src)
+        dst = np.empty_like(src)
+        self._f("dirac")(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                         C.c_double(mu), C.c_int(op), _p(src), _p(dst))
+        return dst
+
+    def cg(self, U, m, r, csw, mu, b, max_iter, tol):
+        U = _c(U)
+        b = _c(b)
+        x = np.empty_like(b)
+        res = C.c_double(0)
+        it = self._f("cg")(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                           C.c_double(mu), _p(b), _p(x), C.c_int(max_iter), C.c_double(tol), C.byref(res))
+        return x, it, res.value
+
+    def gauge_force(self, U, beta):
+        U = _c(U)
+        F = np.empty(U.size)
+        self._f("gauge_force")(C.c_int(self._L(U)), _p(U), C.c_double(beta), _p(F))
+        return F
+
+    def gauge_action(self, U, beta):
+        U = _c(U)
+        return self._f("gauge_action")(C.c_int(self._L(U)), _p(U), C.c_double(beta))
+
+    def fermion_force(self, U, m, r, csw, mu, X):
+        U = _c(U)
+        X = _c(X)
+        F = np.empty(U.size)
+        self._f("fermion_force")(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                                 C.c_double(mu), _p(X), _p(F))
+        return F
+
+    def mr_smooth(self, U, m, r, csw, mu, b, x0, niter):
+        U = _c(U)
+        b = _c(b)
+        x = _c(x0).copy()
+        self._f("mr_smooth")(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                             C.c_double(mu), _p(b), _p(x), C.c_int(niter))
+        return x
+
+    def prolongator_build(self, L, bs, k, null_vecs):
+        nv = _c(null_vecs)
+        nb = (L // bs) ** 2
+        out = np.empty(nb * k * 2 * bs * bs, dtype=np.complex128)
+        self._f("prolongator_build")(C.c_int(L), C.c_int(bs), C.c_int(k), _p(nv), _p(out))
+        return out
+
+    def prolong(self, L, bs, k, bv, coarse):
+        bv = _c(bv)
+        coarse = _c(coarse)
+        fine = np.empty(2 * L * L, dtype=np.complex128)
+        self._f("prolong")(C.c_int(L), C.c_int(bs), C.c_int(k), _p(bv), _p(coarse), _p(fine))
+        return fine
+
+    def restrict(self, L, bs, k, bv, fine):
+        bv = _c(bv)
+        fine = _c(fine)
+        coarse = np.empty((L // bs) ** 2 * k, dtype=np.complex128)
+        self._f("restrict")(C.c_int(L), C.c_int(bs), C.c_int(k), _p(bv), _p(fine), _p(coarse))
+        return coarse
+
+    def sparse_coarse_build(self, U, m, r, csw, mu, bs, k, bv):
+        U = _c(U)
+        bv = _c(bv)
+        L = self._L(U)
+        nb = (L // bs) ** 2
+        links = np.empty(nb * 9 * k * k, dtype=np.complex128)
+        self._f("sparse_coarse_build")(C.c_int(L), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                                       C.c_double(mu), C.c_int(bs), C.c_int(k), _p(bv), _p(links))
+        return links
+
+    def sparse_coarse_apply(self, nbx, nby, k, links, src):
+        links = _c(links)
+        src = _c(src)
+        dst = np.empty_like(src)
+        self._f("sparse_coarse_apply")(C.c_int(nbx), C.c_int(nby), C.c_int(k), _p(links), _p(src), _p(dst))
+        return dst
+
+
+class Port(_Lib):
+    def __init__(self):
+        super().__init__(PORT_SO, "orc_")
+        self.lib.orc_get_threads.restype = C.c_int
+        self.lib.orc_mg2_gcr.restype = C.c_int
+        self.lib.orc_sparse_coarse_cg.restype = C.c_int
+
+    def time_dirac(self, U, m, r, csw, mu, op, srcs, reps):
+        """Seconds for `reps` applications of op to every row of srcs (nrhs x 2V)."""
+        U = _c(U)
+        srcs = _c(srcs)
+        nrhs = srcs.size // (U.size)
+        dst = np.empty_like(srcs)
+        self.lib.orc_time_dirac.restype = C.c_double
+        t = self.lib.orc_time_dirac(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                                    C.c_double(mu), C.c_int(op), C.c_int(nrhs), _p(srcs), _p(dst), C.c_int(reps))
+        return t, dst
+
+    def time_cg(self, U, m, r, csw, mu, b, max_iter, tol):
+        U, b = _c(U), _c(b)
+        x = np.empty_like(b)
+        it = C.c_int(0)
+        self.lib.orc_time_cg.restype = C.c_double
+        t = self.lib.orc_time_cg(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                                 C.c_double(mu), _p(b), _p(x), C.c_int(max_iter), C.c_double(tol), C.byref(it))
+        return t, x, it.value
+
+    def set_threads(self, n: int) -> None:
+        self.lib.orc_set_threads(C.c_int(n))
+
+    def threads(self) -> int:
+        return self.lib.orc_get_threads()
+
+    def near_null_space(self, U, m, r, csw, mu, k, iters, init):
+        U = _c(U)
+        init = _c(init)
+        out = np.empty_like(init)
+        self.lib.orc_near_null_space(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                                     C.c_double(mu), C.c_int(k), C.c_int(iters), _p(init), _p(out))
+        return out
+
+    def sparse_coarse_cg(self, nbx, nby, k, links, b, max_iter, tol):
+        links = _c(links)
+        b = _c(b)
+        x = np.empty_like(b)
+        it = self.lib.orc_sparse_coarse_cg(C.c_int(nbx), C.c_int(nby), C.c_int(k), _p(links), _p(b), _p(x),
+                                           C.c_int(max_iter), C.c_double(tol))
+        return x, it
+
+    @staticmethod
+    def mg2_params(L, bs, k, m, r, csw, mu, pre, post, coarse_max_iter, coarse_tol):
+        return OrcMG2Params(L, bs, k, m, r, csw, mu, pre, post, coarse_max_iter, coarse_tol)
+
+    def mg2_precondition(self, p, U, bv, links, b):
+        U, bv, links, b = _c(U), _c(bv), _c(links), _c(b)
+        out = np.empty_like(b)
+        self.lib.orc_mg2_precondition(C.byref(p), _p(U), _p(bv), _p(links), _p(b), _p(out))
+        return out
+
+    def mg2_gcr(self, p, U, bv, links, b, max_iter, tol, trunc, ref_coeff=False):
+        U, bv, links, b = _c(U), _c(bv), _c(links), _c(b)
+        x = np.empty_like(b)
+        res = C.c_double(0)
+        it = self.lib.orc_mg2_gcr(C.byref(p), _p(U), _p(bv), _p(links), _p(b), _p(x), C.c_int(max_iter),
+                                  C.c_double(tol), C.c_int(trunc), C.c_int(int(ref_coeff)), C.byref(res))
+        return x, it, res.value
+
+
+class Ref(_Lib):
+    def __init__(self):
+        super().__init__(REF_SO, "ref_")
+        self.lib.ref_verify_forces.restype = C.c_int
+        self.lib.ref_mg_gcr.restype = C.c_int
+        self.lib.ref_set_verbosity(C.c_int(0))
+
+    def random_vecs(self, k, n, seed):
+        out = np.empty(k * n, dtype=np.complex128)
+        self.lib.ref_random_vecs(C.c_int(k), C.c_int(n), C.c_uint(seed), _p(out))
+        return out
+
+    def near_null_space(self, U, m, r, csw, mu, k, iters, seed):
+        U = _c(U)
+        L = self._L(U)
+        out = np.empty(k * 2 * L * L, dtype=np.complex128)
+        self.lib.ref_near_null_space(C.c_int(L), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                                     C.c_double(mu), C.c_int(k), C.c_int(iters), C.c_uint(seed), _p(out))
+        return out
+
+    def dense_coarse_build(self, U, m, r, csw, mu, bs, k, bv):
+        U, bv = _c(U), _c(bv)
+        L = self._L(U)
+        dim = (L // bs) ** 2 * k
+        mat = np.empty(dim * dim, dtype=np.complex128)
+        self.lib.ref_dense_coarse_build(C.c_int(L), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                                        C.c_double(mu), C.c_int(bs), C.c_int(k), _p(bv), _p(mat))
+        return mat.reshape(dim, dim).T  # stored column-major
+
+    def verify_forces(self, U, beta, m, r, csw, mu, max_iter, tol, use_eo=False):
+        U = _c(U)
+        return self.lib.ref_verify_forces(C.c_int(self._L(U)), _p(U), C.c_double(beta), C.c_double(m),
+                                          C.c_double(r), C.c_double(csw), C.c_double(mu), C.c_int(max_iter),
+                                          C.c_double(tol), C.c_int(int(use_eo))) == 1
+
+    def mg_precondition(self, U, m, r, csw, mu, params: RefMGParams, seed, b, warm=None):
+        U, b = _c(U), _c(b)
+        out = np.empty_like(b)
+        wp = _p(_c(warm)) if warm is not None else None
+        keep = _c(warm) if warm is not None else None
+        if keep is not None:
+            wp = _p(keep)
+        self.lib.ref_mg_precondition(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                                     C.c_double(mu), C.byref(params), C.c_uint(seed), wp, _p(b), _p(out))
+        return out
+
+    def mg_gcr(self, U, m, r, csw, mu, params: RefMGParams, seed, b, max_iter, tol, trunc, warm=None):
+        U, b = _c(U), _c(b)
+        x = np.empty_like(b)
+        res = C.c_double(0)
+        keep = _c(warm) if warm is not None else None
+        wp = _p(keep) if keep is not None else None
+        it = self.lib.ref_mg_gcr(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                                 C.c_double(mu), C.byref(params), C.c_uint(seed), wp, _p(b), _p(x),
+                                 C.c_int(max_iter), C.c_double(tol), C.c_int(trunc), C.byref(res))
+        return x, it, res.value
+
+    def pseudofermion(self, U, m, r, csw, mu, seed):
+        U = _c(U)
+        L = self._L(U)
+        phi = np.empty(2 * L * L, dtype=np.complex128)
+        self.lib.ref_pseudofermion(C.c_int(L), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                                   C.c_double(mu), C.c_uint(seed), _p(phi))
+        return phi
+
+
+_port = None
+_ref = None
+
+
+def port() -> Port:
+    global _port
+    if _port is None:
+        if not PORT_SO.exists():
+            build(ref=False)
+        _port = Port()
+    return _port
+
+
+def ref() -> Ref | None:
+    global _ref
+    if _ref is None:
+        if not REF_SO.exists():
+            return None
+        _ref = Ref()
+    return _ref

@@ -1,0 +1,313 @@
+// ORACLE TEST INFRASTRUCTURE — not part of the product.
+//
+// A thin extern "C" shim over the reference's own C++ sources, compiled from
+// the reference tree (see oracle/Makefile) into oracle/_ref/libsmg_ref.so.
+// Tests and the benchmark's CPU-baseline leg call it through ctypes to obtain
+// the reference's results on the same seeded inputs as the GPU path.  Every
+// function below constructs the reference objects (Lattice, GaugeField,
+// DiracOp, MGHierarchy, ...) and calls the reference routine named in its
+// comment; nothing here re-implements reference arithmetic.
+//
+// Array conventions: complex numbers are interleaved doubles; a gauge field
+// is U[mu][s] (2*V complex), a spinor is v[2*s+spin] (2*V complex), a force
+// is F[mu][s] (2*V doubles).
+#include <array>
+#include <complex>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "types.h"
+#include "lattice.h"
+#include "gauge.h"
+#include "dirac.h"
+#include "linalg.h"
+#include "smoother.h"
+#include "prolongator.h"
+#include "coarse_op.h"
+#include "multigrid.h"
+#include "mg_builder.h"
+#include "solvers.h"
+#include "hmc.h"
+
+namespace {
+
+struct World {
+    Lattice lat;
+    GaugeField g;
+    World(int L, const double* U) : lat(L), g(lat) {
+        for (int mu = 0; mu < 2; ++mu)
+            for (int s = 0; s < lat.V; ++s) g.U[mu][s] = cx(U[2 * (mu * lat.V + s)], U[2 * (mu * lat.V + s) + 1]);
+    }
+};
+
+Vec to_vec(const double* p, int n) {
+    Vec v(n);
+    for (int i = 0; i < n; ++i) v[i] = cx(p[2 * i], p[2 * i + 1]);
+    return v;
+}
+void from_vec(const Vec& v, double* p) {
+    for (size_t i = 0; i < v.size(); ++i) {
+        p[2 * i] = v[i].real();
+        p[2 * i + 1] = v[i].imag();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+void ref_set_verbosity(int v) { g_verbosity = v; }
+
+// random_vec (src/linalg.cpp:44-48): k vectors drawn one after another from
+// one std::mt19937(seed)
+void ref_random_vecs(int k, int n, unsigned seed, double* out) {
+    std::mt19937 rng(seed);
+    for (int i = 0; i < k; ++i) from_vec(random_vec(n, rng), out + (size_t)2 * n * i);
+}
+
+// DiracOp::compute_clover_field (src/dirac.h:26-52)
+void ref_clover(int L, const double* U, double* F01) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, 0.0, 1.0, 1.0, 0.0);
+    for (int s = 0; s < w.lat.V; ++s) F01[s] = D.clover_field[s];
+}
+
+// GaugeField::avg_plaq (src/gauge.h:32-36)
+double ref_avg_plaq(int L, const double* U) {
+    World w(L, U);
+    return w.g.avg_plaq();
+}
+
+// op: 0 apply (dirac.h:115), 1 apply_dag (:120), 2 apply_DdagD (:136), 3 apply_g5D (:145)
+void ref_dirac(int L, const double* U, double m, double r, double csw, double mu, int op, const double* src,
+               double* dst) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    Vec s = to_vec(src, w.lat.ndof), d(w.lat.ndof);
+    switch (op) {
+        case 0: D.apply(s, d); break;
+        case 1: D.apply_dag(s, d); break;
+        case 2: D.apply_DdagD(s, d); break;
+        default: D.apply_g5D(s, d); break;
+    }
+    from_vec(d, dst);
+}
+
+// cg_solve on D^dag D (src/solvers.cpp:75-78)
+int ref_cg(int L, const double* U, double m, double r, double csw, double mu, const double* b, double* x,
+           int max_iter, double tol, double* final_res) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    OpApply A = [&D](const Vec& s, Vec& d) { D.apply_DdagD(s, d); };
+    CGResult res = cg_solve(A, w.lat.ndof, to_vec(b, w.lat.ndof), max_iter, tol);
+    from_vec(res.solution, x);
+    if (final_res) *final_res = res.final_residual;
+    return res.iterations;
+}
+
+// gauge_force / gauge_action (src/hmc_forces.cpp:80-111)
+void ref_gauge_force(int L, const double* U, double beta, double* F) {
+    World w(L, U);
+    std::array<RVec, 2> f;
+    gauge_force(w.g, beta, f);
+    for (int mu = 0; mu < 2; ++mu) std::memcpy(F + (size_t)mu * w.lat.V, f[mu].data(), sizeof(double) * w.lat.V);
+}
+double ref_gauge_action(int L, const double* U, double beta) {
+    World w(L, U);
+    return gauge_action(w.g, beta);
+}
+
+// fermion_force (src/hmc_forces.cpp:134-139)
+void ref_fermion_force(int L, const double* U, double m, double r, double csw, double mu, const double* X,
+                       double* F) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    std::array<RVec, 2> f;
+    fermion_force(D, to_vec(X, w.lat.ndof), f);
+    for (int mu_ = 0; mu_ < 2; ++mu_) std::memcpy(F + (size_t)mu_ * w.lat.V, f[mu_].data(), sizeof(double) * w.lat.V);
+}
+
+// verify_forces (src/hmc_forces.cpp:869-981); returns 1 on PASS
+int ref_verify_forces(int L, const double* U, double beta, double m, double r, double csw, double mu, int max_iter,
+                      double tol, int use_eo) {
+    World w(L, U);
+    return verify_forces(w.g, beta, m, r, max_iter, tol, csw, use_eo != 0, 1e-4, mu) ? 1 : 0;
+}
+
+// mr_smooth (src/smoother.cpp:9-23): x is updated in place
+void ref_mr_smooth(int L, const double* U, double m, double r, double csw, double mu, const double* b, double* x,
+                   int niter) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    Vec xv = to_vec(x, w.lat.ndof);
+    mr_smooth(D, xv, to_vec(b, w.lat.ndof), niter);
+    from_vec(xv, x);
+}
+
+// compute_near_null_space (src/multigrid.cpp:435-484), rng = std::mt19937(seed)
+void ref_near_null_space(int L, const double* U, double m, double r, double csw, double mu, int k, int iters,
+                         unsigned seed, double* out) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    std::mt19937 rng(seed);
+    auto nv = compute_near_null_space(D, k, iters, rng);
+    for (int i = 0; i < k; ++i) from_vec(nv[i], out + (size_t)2 * w.lat.ndof * i);
+}
+
+// Prolongator::build_from_vectors (src/prolongator.h:133-141); block_vecs out
+// as [b][k][2*bx*by] complex
+void ref_prolongator_build(int L, int bs, int k, const double* null_vecs, double* block_vecs) {
+    Lattice lat(L);
+    Prolongator P(lat, bs, bs, k);
+    std::vector<Vec> nv(k);
+    for (int i = 0; i < k; ++i) nv[i] = to_vec(null_vecs + (size_t)2 * lat.ndof * i, lat.ndof);
+    P.build_from_vectors(nv);
+    int bd = P.block_fine_dim();
+    for (int b = 0; b < P.nblocks; ++b)
+        for (int i = 0; i < k; ++i) from_vec(P.block_vecs[b][i], block_vecs + (size_t)2 * bd * (b * k + i));
+}
+
+static Prolongator make_P(const Lattice& lat, int bs, int k, const double* block_vecs) {
+    Prolongator P(lat, bs, bs, k);
+    int bd = P.block_fine_dim();
+    for (int b = 0; b < P.nblocks; ++b)
+        for (int i = 0; i < k; ++i) P.block_vecs[b][i] = to_vec(block_vecs + (size_t)2 * bd * (b * k + i), bd);
+    return P;
+}
+
+// Prolongator::prolong / restrict_vec (src/prolongator.h:77-108)
+void ref_prolong(int L, int bs, int k, const double* block_vecs, const double* coarse, double* fine) {
+    Lattice lat(L);
+    Prolongator P = make_P(lat, bs, k, block_vecs);
+    from_vec(P.prolong(to_vec(coarse, P.coarse_dim)), fine);
+}
+void ref_restrict(int L, int bs, int k, const double* block_vecs, const double* fine, double* coarse) {
+    Lattice lat(L);
+    Prolongator P = make_P(lat, bs, k, block_vecs);
+    from_vec(P.restrict_vec(to_vec(fine, lat.ndof)), coarse);
+}
+
+// SparseCoarseOp::build with A = D^dag D (src/coarse_op.h:241-279); links out as
+// [block][dir][ki*k + kj] complex
+void ref_sparse_coarse_build(int L, const double* U, double m, double r, double csw, double mu, int bs, int k,
+                             const double* block_vecs, double* links) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    Prolongator P = make_P(w.lat, bs, k, block_vecs);
+    SparseCoarseOp Ac;
+    OpApply A = [&D](const Vec& s, Vec& d) { D.apply_DdagD(s, d); };
+    Ac.build(P, A, w.lat.ndof);
+    for (int b = 0; b < Ac.nblocks; ++b)
+        for (int d = 0; d < SparseCoarseOp::N_DIR; ++d)
+            from_vec(Ac.link[b][d], links + (size_t)2 * k * k * (b * SparseCoarseOp::N_DIR + d));
+}
+
+// SparseCoarseOp::apply_to (src/coarse_op.h:282-297)
+void ref_sparse_coarse_apply(int nbx, int nby, int k, const double* links, const double* src, double* dst) {
+    SparseCoarseOp Ac;
+    Ac.nbx = nbx;
+    Ac.nby = nby;
+    Ac.nblocks = nbx * nby;
+    Ac.k_vec = k;
+    Ac.dim = Ac.nblocks * k;
+    Ac.link.resize(Ac.nblocks);
+    for (int b = 0; b < Ac.nblocks; ++b)
+        for (int d = 0; d < SparseCoarseOp::N_DIR; ++d)
+            Ac.link[b][d] = to_vec(links + (size_t)2 * k * k * (b * SparseCoarseOp::N_DIR + d), k * k);
+    Vec out;
+    Ac.apply_to(to_vec(src, Ac.dim), out);
+    from_vec(out, dst);
+}
+
+// CoarseOp::build (dense Galerkin by probing, src/coarse_op.h:40-43); mat out
+// column-major [j][i] complex
+void ref_dense_coarse_build(int L, const double* U, double m, double r, double csw, double mu, int bs, int k,
+                            const double* block_vecs, double* mat) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    Prolongator P = make_P(w.lat, bs, k, block_vecs);
+    CoarseOp Ac;
+    Ac.build(D, P);
+    for (int j = 0; j < Ac.dim; ++j) from_vec(Ac.mat[j], mat + (size_t)2 * Ac.dim * j);
+}
+
+struct RefMGParams {
+    int levels, block_size, k_null, coarse_block, null_iters, w_cycle, pre_smooth, post_smooth, n_defl;
+};
+
+static MGHierarchy ref_build(const DiracOp& D, const RefMGParams& p, unsigned seed,
+                             const std::vector<Vec>* warm) {
+    MGConfig mc;
+    mc.mg_levels = p.levels;
+    mc.block_size = p.block_size;
+    mc.k_null = p.k_null;
+    mc.coarse_block = p.coarse_block;
+    mc.w_cycle = p.w_cycle != 0;
+    mc.pre_smooth = p.pre_smooth;
+    mc.post_smooth = p.post_smooth;
+    std::mt19937 rng(seed);
+    MGHierarchy mg = build_mg_hierarchy(D, p.levels, p.block_size, p.k_null, mc.resolved_coarse_block(),
+                                        p.null_iters, rng, mc.w_cycle, p.pre_smooth, p.post_smooth, false, warm);
+    if (p.n_defl > 0) {
+        OpApply A = [&D](const Vec& s, Vec& d) { D.apply_DdagD(s, d); };
+        mg.setup_sparse_coarse(A, D.lat.ndof, p.n_defl, 1e-12, 200, "trlm", 0.0);
+    }
+    mg.rebind_prolongator_lambdas();
+    return mg;
+}
+
+// MGHierarchy::precondition (src/multigrid.cpp:155-157) of a hierarchy built by
+// build_mg_hierarchy (:595-687).  With warm != nullptr and null_iters = 0 the
+// hierarchy uses exactly those level-0 null vectors (after normalisation and
+// the final Gram-Schmidt pass, :473-481).
+void ref_mg_precondition(int L, const double* U, double m, double r, double csw, double mu, const RefMGParams* p,
+                         unsigned seed, const double* warm_vecs, const double* b, double* out) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    std::vector<Vec> warm;
+    if (warm_vecs)
+        for (int i = 0; i < p->k_null; ++i) warm.push_back(to_vec(warm_vecs + (size_t)2 * w.lat.ndof * i, w.lat.ndof));
+    MGHierarchy mg = ref_build(D, *p, seed, warm_vecs ? &warm : nullptr);
+    from_vec(mg.precondition(to_vec(b, w.lat.ndof)), out);
+}
+
+// fcg_solve_mg (src/solvers.cpp:803-811): GCR on D^dag D preconditioned by the
+// MG hierarchy; returns the iteration count
+int ref_mg_gcr(int L, const double* U, double m, double r, double csw, double mu, const RefMGParams* p,
+               unsigned seed, const double* warm_vecs, const double* b, double* x, int max_iter, double tol, int trunc,
+               double* final_res) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    std::vector<Vec> warm;
+    if (warm_vecs)
+        for (int i = 0; i < p->k_null; ++i) warm.push_back(to_vec(warm_vecs + (size_t)2 * w.lat.ndof * i, w.lat.ndof));
+    MGHierarchy mg = ref_build(D, *p, seed, warm_vecs ? &warm : nullptr);
+    OpApply A = [&D](const Vec& s, Vec& d) { D.apply_DdagD(s, d); };
+    FCGResult res = fcg_solve_mg(A, w.lat.ndof, to_vec(b, w.lat.ndof), mg, max_iter, tol, trunc);
+    from_vec(res.solution, x);
+    if (final_res) *final_res = res.final_residual;
+    return res.iterations;
+}
+
+// null vectors actually used by a hierarchy (MGHierarchy::null_vecs_l0)
+void ref_mg_null_vectors(int L, const double* U, double m, double r, double csw, double mu, const RefMGParams* p,
+                         unsigned seed, double* out) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    MGHierarchy mg = ref_build(D, *p, seed, nullptr);
+    for (int i = 0; i < p->k_null; ++i) from_vec(mg.null_vecs_l0[i], out + (size_t)2 * w.lat.ndof * i);
+}
+
+// generate_pseudofermion (src/hmc_trajectory.cpp:32-36) with mt19937(seed)
+void ref_pseudofermion(int L, const double* U, double m, double r, double csw, double mu, unsigned seed,
+                       double* phi) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    std::mt19937 rng(seed);
+    Vec p;
+    generate_pseudofermion(D, rng, p);
+    from_vec(p, phi);
+}
+
+}  // extern "C"

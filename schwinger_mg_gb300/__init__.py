@@ -1,0 +1,28 @@
+"""GB300-native (sm_103a) Wilson-clover Dirac operator and multigrid solve path
+for the 2D U(1) lattice Schwinger model, behind the operator and solver API of
+cpviolator/Schwinger_MG.
+
+The compute runs in libsmg_gpu.so (hand-written CUDA for sm_103a, C ABI in
+include/smg_gpu.h); this package is the Python mirror of that API.
+"""
+from ._lib import SmgError, SmgLibraryError, lib  # noqa: F401
+from .api import (  # noqa: F401
+    CGResult,
+    Context,
+    DiracOp,
+    Field,
+    GaugeField,
+    Lattice,
+    axpy,
+    cg_solve,
+    dot,
+    fermion_force,
+    gauge_action,
+    gauge_force,
+    gauge_normal,
+    norm,
+    random_vec,
+    scale,
+)
+
+__version__ = "0.1.0"

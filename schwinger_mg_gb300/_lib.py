@@ -1,0 +1,128 @@
+"""ctypes binding of libsmg_gpu.so (the C ABI declared in include/smg_gpu.h).
+
+The library is loaded from this package directory only.  There is no CPU
+fallback: if the shared object is missing or fails to load, every call raises
+``SmgLibraryError`` naming the cause.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libsmg_gpu.so"
+
+# smg_status codes (include/smg_gpu.h)
+OK, NOT_CONVERGED, BREAKDOWN, NONFINITE, BAD_ARG, DEVICE_ERROR, TIMEOUT, NO_MEMORY, UNSUPPORTED = range(9)
+F64, F32, F16 = 0, 1, 2
+OP_D, OP_DDAG, OP_DDAGD, OP_G5D = 0, 1, 2, 3
+
+
+class SmgLibraryError(RuntimeError):
+    pass
+
+
+class SmgError(RuntimeError):
+    def __init__(self, status: int, where: str, msg: str):
+        super().__init__(f"{where}: {msg} (status {status})")
+        self.status = status
+
+
+class SolveResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("final_residual", C.c_double), ("true_residual", C.c_double),
+                ("operator_applications", C.c_int)]
+
+
+_vp = C.c_void_p
+_dp = C.POINTER(C.c_double)
+_st = C.c_int
+
+_SIGS = {
+    "smg_version": (C.c_char_p, []),
+    "smg_status_string": (C.c_char_p, [C.c_int]),
+    "smg_context_create": (_st, [C.c_int, _vp, C.POINTER(_vp)]),
+    "smg_context_destroy": (_st, [_vp]),
+    "smg_context_synchronize": (_st, [_vp]),
+    "smg_context_set_stream": (_st, [_vp, _vp]),
+    "smg_context_stream": (_vp, [_vp]),
+    "smg_last_error": (C.c_char_p, [_vp]),
+    "smg_context_kernel_launches": (C.c_uint64, [_vp]),
+    "smg_timer_begin": (_st, [_vp]),
+    "smg_timer_end": (_st, [_vp, _dp]),
+    "smg_gauge_create": (_st, [_vp, C.c_int, _dp, C.POINTER(_vp)]),
+    "smg_gauge_destroy": (_st, [_vp]),
+    "smg_gauge_set": (_st, [_vp, _dp]),
+    "smg_gauge_get": (_st, [_vp, _dp]),
+    "smg_gauge_L": (C.c_int, [_vp]),
+    "smg_gauge_avg_plaq": (_st, [_vp, _dp]),
+    "smg_gauge_action": (_st, [_vp, C.c_double, _dp]),
+    "smg_gauge_force": (_st, [_vp, C.c_double, _dp]),
+    "smg_dirac_create": (_st, [_vp, C.c_double, C.c_double, C.c_double, C.c_double, C.POINTER(_vp)]),
+    "smg_dirac_destroy": (_st, [_vp]),
+    "smg_dirac_refresh": (_st, [_vp]),
+    "smg_dirac_get_clover": (_st, [_vp, _dp]),
+    "smg_dirac_apply": (_st, [_vp, C.c_int, _vp, _vp]),
+    "smg_field_create": (_st, [_vp, C.c_int, C.c_int, C.c_int, C.POINTER(_vp)]),
+    "smg_field_destroy": (_st, [_vp]),
+    "smg_field_upload": (_st, [_vp, _dp]),
+    "smg_field_download": (_st, [_vp, _dp]),
+    "smg_field_upload_async": (_st, [_vp, _dp]),
+    "smg_field_download_async": (_st, [_vp, _dp]),
+    "smg_field_zero": (_st, [_vp]),
+    "smg_field_copy": (_st, [_vp, _vp]),
+    "smg_field_nrhs": (C.c_int, [_vp]),
+    "smg_field_L": (C.c_int, [_vp]),
+    "smg_field_precision": (C.c_int, [_vp]),
+    "smg_field_device_ptr": (_vp, [_vp]),
+    "smg_field_bytes": (C.c_size_t, [_vp]),
+    "smg_blas_dot": (_st, [_vp, _vp, _dp]),
+    "smg_blas_norm": (_st, [_vp, _dp]),
+    "smg_blas_axpy": (_st, [_dp, _vp, _vp]),
+    "smg_blas_scale": (_st, [_dp, _vp]),
+    "smg_cg_solve": (_st, [_vp, _vp, _vp, C.c_int, C.c_double, C.POINTER(SolveResult)]),
+    "smg_fermion_force": (_st, [_vp, _vp, _dp]),
+    "smg_host_gauge_normal": (_st, [C.c_int, C.c_double, C.c_uint32, _dp]),
+    "smg_host_random_vec": (_st, [C.c_int64, C.c_uint32, _dp]),
+}
+
+_lib = None
+_load_error: str | None = None
+
+
+def exported_symbols() -> list[str]:
+    return sorted(_SIGS)
+
+
+def lib():
+    """Returns the loaded library, raising SmgLibraryError if it is unavailable."""
+    global _lib, _load_error
+    if _lib is not None:
+        return _lib
+    if _load_error is not None:
+        raise SmgLibraryError(_load_error)
+    if not LIB_PATH.exists():
+        _load_error = (f"{LIB_PATH} is missing: build it with `python -c \"import __graft_entry__ as g; g.build()\"` "
+                       "(there is no CPU fallback)")
+        raise SmgLibraryError(_load_error)
+    try:
+        L = C.CDLL(str(LIB_PATH))
+    except OSError as e:
+        _load_error = f"loading {LIB_PATH} failed: {e}"
+        raise SmgLibraryError(_load_error) from e
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status: int, where: str, ctx=None) -> int:
+    if status == OK:
+        return status
+    L = lib()
+    msg = L.smg_status_string(status).decode()
+    if ctx is not None:
+        detail = L.smg_last_error(ctx).decode()
+        if detail:
+            msg = f"{msg}: {detail}"
+    raise SmgError(status, where, msg)

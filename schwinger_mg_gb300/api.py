@@ -1,0 +1,332 @@
+"""Python mirror of the reference's operator and solver API over libsmg_gpu.
+
+Names, argument meaning and result fields follow the reference
+(cpviolator/Schwinger_MG): ``Lattice`` (src/lattice.h), ``GaugeField``
+(src/gauge.h), ``DiracOp`` (src/dirac.h), ``cg_solve`` and ``CGResult``
+(src/solvers.h), ``fermion_force`` / ``gauge_force`` / ``gauge_action``
+(src/hmc.h).  Host vectors are numpy complex128 arrays in the reference's
+layout (spinor ``v[2*s+spin]``, links ``U[mu][s]``); every computation runs on
+the GPU through the C ABI, and a failure raises ``SmgError`` instead of the
+reference's asserts and warnings.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as _L
+
+_dp = C.POINTER(C.c_double)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_dp)
+
+
+def _as_c128(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+PRECISIONS = {"f64": _L.F64, "f32": _L.F32, "f16": _L.F16}
+
+
+class Context:
+    """One CUDA device + stream; all objects made from it enqueue on that stream."""
+
+    _default: "Context | None" = None
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        lib = _L.lib()
+        h = C.c_void_p()
+        _L.check(lib.smg_context_create(device, C.c_void_p(stream) if stream else None, C.byref(h)),
+                 "smg_context_create")
+        self.h = h
+        self.device = device
+
+    @classmethod
+    def default(cls) -> "Context":
+        if cls._default is None:
+            cls._default = Context(0)
+        return cls._default
+
+    def synchronize(self) -> None:
+        _L.check(_L.lib().smg_context_synchronize(self.h), "smg_context_synchronize", self.h)
+
+    def set_stream(self, stream: int) -> None:
+        _L.check(_L.lib().smg_context_set_stream(self.h, C.c_void_p(stream)), "smg_context_set_stream", self.h)
+
+    def timer_begin(self) -> None:
+        _L.check(_L.lib().smg_timer_begin(self.h), "smg_timer_begin", self.h)
+
+    def timer_end(self) -> float:
+        """Milliseconds of device time on this context's stream since timer_begin."""
+        v = C.c_double()
+        _L.check(_L.lib().smg_timer_end(self.h, C.byref(v)), "smg_timer_end", self.h)
+        return v.value
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(_L.lib().smg_context_kernel_launches(self.h))
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            _L.lib().smg_context_destroy(self.h)
+            self.h = None
+
+
+class Lattice:
+    """Geometry and even-odd maps (reference src/lattice.h:4-42), computed on the host."""
+
+    def __init__(self, L: int):
+        self.L = L
+        self.V = L * L
+        self.ndof = 2 * L * L
+        self.V_half = L * L // 2
+        s = np.arange(self.V)
+        par = ((s % L) + (s // L)) % 2
+        self.even_sites = s[par == 0].astype(np.int32)
+        self.odd_sites = s[par == 1].astype(np.int32)
+        self.eo_index = np.empty(self.V, dtype=np.int32)
+        self.eo_index[self.even_sites] = np.arange(self.even_sites.size, dtype=np.int32)
+        self.eo_index[self.odd_sites] = np.arange(self.odd_sites.size, dtype=np.int32)
+
+    def idx(self, x, y):
+        L = self.L
+        return ((x % L + L) % L) + L * ((y % L + L) % L)
+
+    def xp(self, s):
+        return self.idx(s % self.L + 1, s // self.L)
+
+    def xm(self, s):
+        return self.idx(s % self.L - 1, s // self.L)
+
+    def yp(self, s):
+        return self.idx(s % self.L, s // self.L + 1)
+
+    def ym(self, s):
+        return self.idx(s % self.L, s // self.L - 1)
+
+    def parity(self, s):
+        return ((s % self.L) + (s // self.L)) % 2
+
+
+class GaugeField:
+    """U(1) links U[mu][s] resident on the device (reference src/gauge.h:10-36)."""
+
+    def __init__(self, lat: Lattice, U=None, ctx: Context | None = None):
+        self.lat = lat
+        self.ctx = ctx or Context.default()
+        if U is None:
+            U = np.ones(2 * lat.V, dtype=np.complex128)
+        U = _as_c128(U).reshape(-1)
+        if U.size != 2 * lat.V:
+            raise ValueError("U must hold 2*V complex links")
+        h = C.c_void_p()
+        _L.check(_L.lib().smg_gauge_create(self.ctx.h, lat.L, _ptr(U.view(np.float64)), C.byref(h)),
+                 "smg_gauge_create", self.ctx.h)
+        self.h = h
+
+    @property
+    def U(self) -> np.ndarray:
+        out = np.empty(2 * self.lat.V, dtype=np.complex128)
+        _L.check(_L.lib().smg_gauge_get(self.h, _ptr(out.view(np.float64))), "smg_gauge_get", self.ctx.h)
+        return out.reshape(2, self.lat.V)
+
+    def set_links(self, U) -> None:
+        U = _as_c128(U).reshape(-1)
+        _L.check(_L.lib().smg_gauge_set(self.h, _ptr(U.view(np.float64))), "smg_gauge_set", self.ctx.h)
+
+    def avg_plaq(self) -> float:
+        v = C.c_double()
+        _L.check(_L.lib().smg_gauge_avg_plaq(self.h, C.byref(v)), "smg_gauge_avg_plaq", self.ctx.h)
+        return v.value
+
+    def __del__(self):
+        if getattr(self, "h", None) and _L._lib is not None:
+            _L.lib().smg_gauge_destroy(self.h)
+            self.h = None
+
+
+class Field:
+    """nrhs spinors of an L x L lattice resident on the device."""
+
+    def __init__(self, lat: Lattice, nrhs: int = 1, precision: str = "f64", ctx: Context | None = None, data=None):
+        self.lat = lat
+        self.nrhs = nrhs
+        self.precision = precision
+        self.ctx = ctx or Context.default()
+        h = C.c_void_p()
+        _L.check(_L.lib().smg_field_create(self.ctx.h, lat.L, nrhs, PRECISIONS[precision], C.byref(h)),
+                 "smg_field_create", self.ctx.h)
+        self.h = h
+        if data is not None:
+            self.upload(data)
+
+    def upload(self, data) -> "Field":
+        a = _as_c128(data).reshape(-1)
+        if a.size != self.nrhs * self.lat.ndof:
+            raise ValueError(f"expected {self.nrhs * self.lat.ndof} complex values, got {a.size}")
+        _L.check(_L.lib().smg_field_upload(self.h, _ptr(a.view(np.float64))), "smg_field_upload", self.ctx.h)
+        return self
+
+    def download(self) -> np.ndarray:
+        out = np.empty(self.nrhs * self.lat.ndof, dtype=np.complex128)
+        _L.check(_L.lib().smg_field_download(self.h, _ptr(out.view(np.float64))), "smg_field_download", self.ctx.h)
+        return out if self.nrhs == 1 else out.reshape(self.nrhs, self.lat.ndof)
+
+    def zero(self) -> None:
+        _L.check(_L.lib().smg_field_zero(self.h), "smg_field_zero", self.ctx.h)
+
+    def copy_from(self, other: "Field") -> None:
+        _L.check(_L.lib().smg_field_copy(other.h, self.h), "smg_field_copy", self.ctx.h)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _L._lib is not None:
+            _L.lib().smg_field_destroy(self.h)
+            self.h = None
+
+
+def dot(a: Field, b: Field) -> np.ndarray:
+    """sum conj(a) b per right-hand side (reference src/linalg.cpp:8-18)."""
+    out = np.empty(2 * a.nrhs)
+    _L.check(_L.lib().smg_blas_dot(a.h, b.h, _ptr(out)), "smg_blas_dot", a.ctx.h)
+    return out[0::2] + 1j * out[1::2]
+
+
+def norm(a: Field) -> np.ndarray:
+    out = np.empty(a.nrhs)
+    _L.check(_L.lib().smg_blas_norm(a.h, _ptr(out)), "smg_blas_norm", a.ctx.h)
+    return out
+
+
+def axpy(alpha, x: Field, y: Field) -> None:
+    al = np.broadcast_to(np.asarray(alpha, dtype=np.complex128), (x.nrhs,)).copy()
+    _L.check(_L.lib().smg_blas_axpy(_ptr(al.view(np.float64)), x.h, y.h), "smg_blas_axpy", x.ctx.h)
+
+
+def scale(v: Field, alpha) -> None:
+    al = np.broadcast_to(np.asarray(alpha, dtype=np.complex128), (v.nrhs,)).copy()
+    _L.check(_L.lib().smg_blas_scale(_ptr(al.view(np.float64)), v.h), "smg_blas_scale", v.ctx.h)
+
+
+class DiracOp:
+    """Wilson-clover Dirac operator (reference src/dirac.h:8-183) on the device."""
+
+    def __init__(self, lat: Lattice, gauge: GaugeField, mass: float, r: float = 1.0, c_sw: float = 0.0,
+                 mu_t: float = 0.0):
+        self.lat = lat
+        self.gauge = gauge
+        self.mass, self.r, self.c_sw, self.mu_t = mass, r, c_sw, mu_t
+        self.ctx = gauge.ctx
+        h = C.c_void_p()
+        _L.check(_L.lib().smg_dirac_create(gauge.h, mass, r, c_sw, mu_t, C.byref(h)), "smg_dirac_create",
+                 self.ctx.h)
+        self.h = h
+
+    def refresh(self) -> None:
+        """Recomputes the clover term after the gauge links changed."""
+        _L.check(_L.lib().smg_dirac_refresh(self.h), "smg_dirac_refresh", self.ctx.h)
+
+    @property
+    def clover_field(self) -> np.ndarray:
+        out = np.empty(self.lat.V)
+        _L.check(_L.lib().smg_dirac_get_clover(self.h, _ptr(out)), "smg_dirac_get_clover", self.ctx.h)
+        return out
+
+    def apply_op(self, op: int, src, dst=None):
+        """Applies op to a Field (device in, device out) or to host arrays."""
+        if isinstance(src, Field):
+            if dst is None:
+                dst = Field(self.lat, src.nrhs, src.precision, self.ctx)
+            _L.check(_L.lib().smg_dirac_apply(self.h, op, src.h, dst.h), "smg_dirac_apply", self.ctx.h)
+            return dst
+        a = _as_c128(src)
+        nrhs = a.size // self.lat.ndof
+        fs = Field(self.lat, nrhs, "f64", self.ctx, data=a)
+        fd = Field(self.lat, nrhs, "f64", self.ctx)
+        _L.check(_L.lib().smg_dirac_apply(self.h, op, fs.h, fd.h), "smg_dirac_apply", self.ctx.h)
+        out = fd.download().reshape(a.shape)
+        if dst is not None:
+            dst[...] = out
+            return dst
+        return out
+
+    def apply(self, src, dst=None):
+        return self.apply_op(_L.OP_D, src, dst)
+
+    def apply_dag(self, src, dst=None):
+        return self.apply_op(_L.OP_DDAG, src, dst)
+
+    def apply_DdagD(self, src, dst=None):
+        return self.apply_op(_L.OP_DDAGD, src, dst)
+
+    def apply_g5D(self, src, dst=None):
+        return self.apply_op(_L.OP_G5D, src, dst)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _L._lib is not None:
+            _L.lib().smg_dirac_destroy(self.h)
+            self.h = None
+
+
+@dataclass
+class CGResult:
+    """Mirrors CGResult / FCGResult (reference src/solvers.h:25-35) plus the FP64 true residual."""
+    solution: np.ndarray
+    iterations: int
+    final_residual: float
+    true_residual: float = float("nan")
+
+
+def cg_solve(A: DiracOp, n: int, rhs, max_iter: int, tol: float, precision: str = "f64",
+             raise_on_failure: bool = False) -> CGResult:
+    """CG on D^dag D from x = 0 (reference src/solvers.cpp:75-78); `A` is the DiracOp."""
+    b = _as_c128(rhs)
+    nrhs = b.size // A.lat.ndof
+    if n != A.lat.ndof:
+        raise ValueError("n must equal 2*V")
+    fb = Field(A.lat, nrhs, precision, A.ctx, data=b)
+    fx = Field(A.lat, nrhs, precision, A.ctx)
+    res = _L.SolveResult()
+    st = _L.lib().smg_cg_solve(A.h, fb.h, fx.h, max_iter, tol, C.byref(res))
+    if st != _L.OK and (raise_on_failure or st not in (_L.NOT_CONVERGED,)):
+        _L.check(st, "smg_cg_solve", A.ctx.h)
+    return CGResult(fx.download().reshape(b.shape), res.iterations, res.final_residual, res.true_residual)
+
+
+def fermion_force(D: DiracOp, X) -> np.ndarray:
+    """F[mu][s] = -dS/dtheta for S = phi^dag (D^dag D)^-1 phi at X = (D^dag D)^-1 phi
+    (reference src/hmc_forces.cpp:134-495)."""
+    fx = X if isinstance(X, Field) else Field(D.lat, 1, "f64", D.ctx, data=X)
+    out = np.empty(2 * D.lat.V)
+    _L.check(_L.lib().smg_fermion_force(D.h, fx.h, _ptr(out)), "smg_fermion_force", D.ctx.h)
+    return out.reshape(2, D.lat.V)
+
+
+def gauge_force(g: GaugeField, beta: float) -> np.ndarray:
+    out = np.empty(2 * g.lat.V)
+    _L.check(_L.lib().smg_gauge_force(g.h, beta, _ptr(out)), "smg_gauge_force", g.ctx.h)
+    return out.reshape(2, g.lat.V)
+
+
+def gauge_action(g: GaugeField, beta: float) -> float:
+    v = C.c_double()
+    _L.check(_L.lib().smg_gauge_action(g.h, beta, C.byref(v)), "smg_gauge_action", g.ctx.h)
+    return v.value
+
+
+# ---------------------------------------------------------------- host inputs
+def gauge_normal(L: int, beta: float, seed: int) -> np.ndarray:
+    """U = exp(i theta), theta ~ N(0, 1/beta) from std::mt19937(seed); shape (2, V)."""
+    out = np.empty(2 * L * L, dtype=np.complex128)
+    _L.check(_L.lib().smg_host_gauge_normal(L, beta, seed, _ptr(out.view(np.float64))), "smg_host_gauge_normal")
+    return out.reshape(2, L * L)
+
+
+def random_vec(n: int, seed: int) -> np.ndarray:
+    """random_vec(n, std::mt19937(seed)) (reference src/linalg.cpp:44-48)."""
+    out = np.empty(n, dtype=np.complex128)
+    _L.check(_L.lib().smg_host_random_vec(n, seed, _ptr(out.view(np.float64))), "smg_host_random_vec")
+    return out

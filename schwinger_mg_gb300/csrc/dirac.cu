@@ -1,0 +1,334 @@
+// Wilson-clover Dirac operator on the device (reference src/dirac.h:8-183).
+//
+// One kernel applies D or D^dag to every right-hand side of a field:
+//   D = (2r + m) + C(x) sigma3 + i mu sigma3
+//       - 1/2 sum_mu [ (r - sigma_mu) U_mu(x) delta_{x+mu} + (r + sigma_mu) U_mu^dag(x-mu) delta_{x-mu} ]
+// with sigma_0 -> sigma1, sigma_1 -> sigma2 as in accumulate_hops
+// (dirac.h:58-89) and C = c_sw F01 / 2 (dirac.h:102).  D^dag = g5 D(-mu) g5
+// (dirac.h:120-134) only flips the sign of the spin off-diagonal hopping
+// terms and of mu, so it is the same kernel with DAG = true.  Optional
+// epilogues fuse the reductions a solver step needs: ||out||^2 (CG's
+// <p, D^dag D p> = ||D p||^2) and, for the MR smoother, <out, w> and ||out||^2.
+#include "smg_internal.h"
+#include "reduce.cuh"
+
+namespace {
+
+enum { EPI_NONE = 0, EPI_NORM = 1, EPI_MR = 2 };
+
+template <typename T>
+struct DslashArgs {
+    const cx<T>* __restrict__ src;
+    cx<T>* __restrict__ dst;
+    const cx<T>* __restrict__ U;   // [mu][parity][cb]
+    const T* __restrict__ C;       // clover shift per site or nullptr
+    const cx<T>* __restrict__ w;   // EPI_MR second field
+    Geom g;
+    int nrhs;
+    T diag, mu_eff, r;
+    double* partials;
+    unsigned int* ticket;
+    double* out;
+};
+
+template <typename T, bool DAG, int EPI>
+__global__ void __launch_bounds__(256) k_dslash(DslashArgs<T> a) {
+    constexpr int K = EPI == EPI_MR ? 3 : 1;
+    const T half = T(0.5);
+    const T sgn = DAG ? T(-1) : T(1);
+    const int nrhs = a.nrhs;
+    const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
+    const Geom g = a.g;
+    double v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = 0.0;
+
+    if (rhs < nrhs) {
+        for (int q = blockIdx.x * blockDim.y + threadIdx.y; q < g.V; q += gridDim.x * blockDim.y) {
+            int x, y, p;
+            site_coords(g, q, x, y, p);
+            const int op = (1 - p) * g.Vh;
+            const int xp = x + 1 == g.L ? 0 : x + 1;
+            const int xm = x == 0 ? g.L - 1 : x - 1;
+            const int yp = y + 1 == g.L ? 0 : y + 1;
+            const int ym = y == 0 ? g.L - 1 : y - 1;
+            const int q_xp = op + ((xp + g.L * y) >> 1);
+            const int q_xm = op + ((xm + g.L * y) >> 1);
+            const int q_yp = op + ((x + g.L * yp) >> 1);
+            const int q_ym = op + ((x + g.L * ym) >> 1);
+
+            const cx<T> u0f = a.U[q];
+            const cx<T> u0b = a.U[q_xm];
+            const cx<T> u1f = a.U[g.V + q];
+            const cx<T> u1b = a.U[g.V + q_ym];
+
+            auto ld = [&](int qq, int sp) { return a.src[((int64_t)qq * 2 + sp) * nrhs + rhs]; };
+            const cx<T> s0 = ld(q, 0), s1 = ld(q, 1);
+            const cx<T> a0x = u0f * ld(q_xp, 0), a1x = u0f * ld(q_xp, 1);
+            const cx<T> b0x = cmulc(u0b, ld(q_xm, 0)), b1x = cmulc(u0b, ld(q_xm, 1));
+            const cx<T> a0y = u1f * ld(q_yp, 0), a1y = u1f * ld(q_yp, 1);
+            const cx<T> b0y = cmulc(u1b, ld(q_ym, 0)), b1y = cmulc(u1b, ld(q_ym, 1));
+
+            const T Cq = a.C ? a.C[q] : T(0);
+            const cx<T> dg0 = mk<T>(a.diag + Cq, a.mu_eff);
+            const cx<T> dg1 = mk<T>(a.diag - Cq, -a.mu_eff);
+
+            const cx<T> sr0 = (a0x + b0x) + (a0y + b0y);
+            const cx<T> sr1 = (a1x + b1x) + (a1y + b1y);
+            const cx<T> off0 = (b1x - a1x) + times_i(a1y - b1y);
+            const cx<T> off1 = (b0x - a0x) - times_i(a0y - b0y);
+
+            const cx<T> d0 = dg0 * s0 - half * (a.r * sr0 + sgn * off0);
+            const cx<T> d1 = dg1 * s1 - half * (a.r * sr1 + sgn * off1);
+            a.dst[((int64_t)q * 2 + 0) * nrhs + rhs] = d0;
+            a.dst[((int64_t)q * 2 + 1) * nrhs + rhs] = d1;
+
+            if (EPI == EPI_NORM) {
+                v[0] += (double)(norm2(d0) + norm2(d1));
+            } else if (EPI == EPI_MR) {
+                const cx<T> w0 = a.w[((int64_t)q * 2 + 0) * nrhs + rhs];
+                const cx<T> w1 = a.w[((int64_t)q * 2 + 1) * nrhs + rhs];
+                const cx<T> c = cmulc(d0, w0) + cmulc(d1, w1);
+                v[0] += (double)c.re;
+                v[1] += (double)c.im;
+                v[2] += (double)(norm2(d0) + norm2(d1));
+            }
+        }
+    }
+    if (EPI != EPI_NONE) block_reduce_finalise<K>(v, a.partials, a.ticket, nrhs, FinStore{a.out, K});
+}
+
+// F01(s) = Im(P_ur + P_ul + P_ll + P_lr) / 4   (dirac.h:26-52)
+__device__ __forceinline__ cx<double> lkd(const cx<double>* __restrict__ U, const Geom& g, int mu, int x, int y) {
+    return U[(int64_t)mu * g.V + site_q(g, wrap(x, g.L), wrap(y, g.L))];
+}
+
+__global__ void k_clover(const cx<double>* __restrict__ U, Geom g, double c_sw, double* __restrict__ F01,
+                         double* __restrict__ C64, float* __restrict__ C32) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= g.V) return;
+    int x, y, p;
+    site_coords(g, q, x, y, p);
+    cx<double> P_ur = lkd(U, g, 0, x, y) * lkd(U, g, 1, x + 1, y) * conj(lkd(U, g, 0, x, y + 1)) * conj(lkd(U, g, 1, x, y));
+    cx<double> P_ul = lkd(U, g, 1, x, y) * conj(lkd(U, g, 0, x - 1, y + 1)) * conj(lkd(U, g, 1, x - 1, y)) *
+                      lkd(U, g, 0, x - 1, y);
+    cx<double> P_ll = conj(lkd(U, g, 0, x - 1, y)) * conj(lkd(U, g, 1, x - 1, y - 1)) * lkd(U, g, 0, x - 1, y - 1) *
+                      lkd(U, g, 1, x, y - 1);
+    cx<double> P_lr = conj(lkd(U, g, 1, x, y - 1)) * lkd(U, g, 0, x, y - 1) * lkd(U, g, 1, x + 1, y - 1) *
+                      conj(lkd(U, g, 0, x, y));
+    cx<double> Q = P_ur + P_ul + P_ll + P_lr;
+    double f = Q.im / 4.0;
+    F01[q] = f;
+    double c = 0.5 * c_sw * f;
+    C64[q] = c;
+    C32[q] = (float)c;
+}
+
+__global__ void k_f01_out(const double* __restrict__ F01, Geom g, double* __restrict__ host) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= g.V) return;
+    host[s] = F01[site_q(g, s % g.L, s / g.L)];
+}
+
+template <typename T>
+__global__ void k_gamma5(cx<T>* __restrict__ v, int nsites, int nrhs) {
+    int rhs = blockIdx.y * blockDim.x + threadIdx.x;
+    int q = blockIdx.x * blockDim.y + threadIdx.y;
+    if (rhs >= nrhs || q >= nsites) return;
+    int64_t i = ((int64_t)q * 2 + 1) * nrhs + rhs;
+    v[i] = -v[i];
+}
+
+template <typename T>
+smg_status launch_dslash(smg_dirac* d, bool dag, int epi, const smg_field* src, smg_field* dst, const smg_field* w,
+                         double* out_dev) {
+    smg_context* ctx = src->ctx;
+    DslashArgs<T> a;
+    a.src = (const cx<T>*)src->data;
+    a.dst = (cx<T>*)dst->data;
+    if (sizeof(T) == 8) {
+        a.U = (const cx<T>*)d->gauge->U64;
+        a.C = (const T*)d->C64;
+    } else {
+        a.U = (const cx<T>*)d->gauge->U32;
+        a.C = (const T*)d->C32;
+    }
+    a.w = w ? (const cx<T>*)w->data : nullptr;
+    a.g = src->g;
+    a.nrhs = src->nrhs;
+    a.diag = (T)(2.0 * d->r + d->mass);
+    a.mu_eff = (T)(dag ? -d->mu_t : d->mu_t);
+    a.r = (T)d->r;
+    a.partials = ctx->red.partials;
+    a.ticket = ctx->red.tickets;
+    a.out = out_dev;
+    dim3 grid, block;
+    if (epi == EPI_NONE) {
+        SiteLaunch sl = site_launch(src->g.V, src->nrhs);
+        // the kernel needs power-of-two lanes only for reductions
+        grid = sl.grid;
+        block = sl.block;
+    } else {
+        ReduceLaunch rl = reduce_launch(src->g.V, src->nrhs);
+        SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * src->nrhs * 3));
+        a.partials = ctx->red.partials;
+        grid = rl.grid;
+        block = rl.block;
+    }
+#define SMG_DS(DAG, EPI) k_dslash<T, DAG, EPI><<<grid, block, 0, ctx->stream>>>(a)
+    if (dag) {
+        if (epi == EPI_NONE) SMG_DS(true, EPI_NONE);
+        else if (epi == EPI_NORM) SMG_DS(true, EPI_NORM);
+        else SMG_DS(true, EPI_MR);
+    } else {
+        if (epi == EPI_NONE) SMG_DS(false, EPI_NONE);
+        else if (epi == EPI_NORM) SMG_DS(false, EPI_NORM);
+        else SMG_DS(false, EPI_MR);
+    }
+#undef SMG_DS
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+smg_status dslash_dispatch(smg_dirac* d, bool dag, int epi, const smg_field* src, smg_field* dst, const smg_field* w,
+                           double* out_dev) {
+    if (src->prec == SMG_F64) return launch_dslash<double>(d, dag, epi, src, dst, w, out_dev);
+    if (src->prec == SMG_F32) return launch_dslash<float>(d, dag, epi, src, dst, w, out_dev);
+    return smg_fail(src->ctx, SMG_UNSUPPORTED, "dslash on F16 field");
+}
+
+smg_status gamma5_inplace(smg_field* f) {
+    smg_context* ctx = f->ctx;
+    SiteLaunch sl = site_launch(f->g.V, f->nrhs);
+    if (f->prec == SMG_F64)
+        k_gamma5<double><<<sl.grid, sl.block, 0, ctx->stream>>>((cx<double>*)f->data, f->g.V, f->nrhs);
+    else if (f->prec == SMG_F32)
+        k_gamma5<float><<<sl.grid, sl.block, 0, ctx->stream>>>((cx<float>*)f->data, f->g.V, f->nrhs);
+    else
+        return smg_fail(ctx, SMG_UNSUPPORTED, "gamma5 on F16 field");
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+smg_status check_op_fields(smg_dirac* d, const smg_field* src, const smg_field* dst) {
+    if (!d || !src || !dst) return SMG_BAD_ARG;
+    smg_context* ctx = d->gauge->ctx;
+    if (src == dst) return smg_fail(ctx, SMG_BAD_ARG, "src and dst must be distinct fields");
+    SMG_TRY(smg_field_check_pair(src, dst));
+    if (src->ctx != ctx) return smg_fail(ctx, SMG_BAD_ARG, "field and operator belong to different contexts");
+    if (src->g.L != d->gauge->g.L) return smg_fail(ctx, SMG_BAD_ARG, "field L differs from gauge L");
+    return SMG_OK;
+}
+
+}  // namespace
+
+// ---- internal entry points used by solvers, MG and forces
+smg_status smg_dslash(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, double* norm2_dev) {
+    return dslash_dispatch(d, dag, norm2_dev ? EPI_NORM : EPI_NONE, src, dst, nullptr, norm2_dev);
+}
+smg_status smg_dslash_mr(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, const smg_field* w,
+                         double* out3_dev) {
+    return dslash_dispatch(d, dag, EPI_MR, src, dst, w, out3_dev);
+}
+
+smg_status smg_dirac_apply_internal(smg_dirac* d, smg_operator op, const smg_field* src, smg_field* dst,
+                                    double* norm2_out_dev) {
+    smg_context* ctx = src->ctx;
+    switch (op) {
+        case SMG_OP_D: return smg_dslash(d, false, src, dst, norm2_out_dev);
+        case SMG_OP_DDAG: return smg_dslash(d, true, src, dst, norm2_out_dev);
+        case SMG_OP_G5D:
+            SMG_TRY(smg_dslash(d, false, src, dst, nullptr));
+            return gamma5_inplace(dst);
+        case SMG_OP_DDAGD: {
+            smg_field* tmp = nullptr;
+            SMG_TRY(smg_field_alloc_like(src, src->prec, &tmp));
+            smg_status s = smg_dslash(d, false, src, tmp, nullptr);
+            if (s == SMG_OK) s = smg_dslash(d, true, tmp, dst, norm2_out_dev);
+            smg_field_destroy(tmp);
+            return s;
+        }
+    }
+    return smg_fail(ctx, SMG_BAD_ARG, "unknown operator");
+}
+
+extern "C" {
+
+SMG_API smg_status smg_dirac_create(smg_gauge* gf, double mass, double r, double c_sw, double mu_t, smg_dirac** out) {
+    if (!gf || !out) return SMG_BAD_ARG;
+    *out = nullptr;
+    smg_context* ctx = gf->ctx;
+    smg_dirac* d = new smg_dirac();
+    d->gauge = gf;
+    d->mass = mass;
+    d->r = r;
+    d->c_sw = c_sw;
+    d->mu_t = mu_t;
+    size_t V = gf->g.V;
+    if (cudaMalloc(&d->F01, V * sizeof(double)) != cudaSuccess) {
+        delete d;
+        return smg_fail(ctx, SMG_NO_MEMORY, "clover allocation");
+    }
+    if (c_sw != 0.0) {
+        if (cudaMalloc(&d->C64, V * sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&d->C32, V * sizeof(float)) != cudaSuccess) {
+            smg_dirac_destroy(d);
+            return smg_fail(ctx, SMG_NO_MEMORY, "clover allocation");
+        }
+    }
+    smg_status s = smg_dirac_refresh(d);
+    if (s != SMG_OK) {
+        smg_dirac_destroy(d);
+        return s;
+    }
+    *out = d;
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_dirac_destroy(smg_dirac* d) {
+    if (!d) return SMG_OK;
+    cudaStreamSynchronize(d->gauge->ctx->stream);
+    if (d->F01) cudaFree(d->F01);
+    if (d->C64) cudaFree(d->C64);
+    if (d->C32) cudaFree(d->C32);
+    delete d;
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_dirac_refresh(smg_dirac* d) {
+    if (!d) return SMG_BAD_ARG;
+    smg_context* ctx = d->gauge->ctx;
+    const Geom g = d->gauge->g;
+    if (d->c_sw != 0.0) {
+        k_clover<<<(g.V + 255) / 256, 256, 0, ctx->stream>>>(d->gauge->U64, g, d->c_sw, d->F01, d->C64, d->C32);
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+    } else {
+        SMG_CUDA(ctx, cudaMemsetAsync(d->F01, 0, (size_t)g.V * sizeof(double), ctx->stream));
+    }
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_dirac_get_clover(smg_dirac* d, double* F01) {
+    if (!d || !F01) return SMG_BAD_ARG;
+    smg_context* ctx = d->gauge->ctx;
+    const Geom g = d->gauge->g;
+    double* tmp = nullptr;
+    SMG_CUDA(ctx, cudaMallocAsync(&tmp, (size_t)g.V * sizeof(double), ctx->stream));
+    k_f01_out<<<(g.V + 255) / 256, 256, 0, ctx->stream>>>(d->F01, g, tmp);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    SMG_CUDA(ctx, cudaMemcpyAsync(F01, tmp, (size_t)g.V * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SMG_CUDA(ctx, cudaFreeAsync(tmp, ctx->stream));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_dirac_apply(smg_dirac* d, smg_operator op, const smg_field* src, smg_field* dst) {
+    SMG_TRY(check_op_fields(d, src, dst));
+    return smg_dirac_apply_internal(d, op, src, dst, nullptr);
+}
+
+}  // extern "C"

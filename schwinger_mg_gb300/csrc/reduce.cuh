@@ -1,0 +1,111 @@
+// Two-stage block reductions with a "last block finalises" epilogue.
+//
+// Kernels that reduce run with blockDim = (lanes, rows), lanes a power of two
+// <= 32 indexing right-hand sides, at most 256 threads per block.  Every
+// thread contributes K doubles; the block sums them per lane (warp shuffles,
+// then across warps), writes one partial per (rhs, k), and the block that
+// finishes last sums the partials in a fixed order (deterministic run to run)
+// and hands the totals to a finaliser functor `fin(rhs, const double* sums)`.
+// Partials live in the context's scratch buffer:
+//   partials[(rhs * K + k) * gridDim.x + blockIdx.x]
+// and ticket[blockIdx.y] counts finished blocks; the last block puts it back
+// to zero, so the scratch is ready for the next launch on the same stream.
+#pragma once
+#include "smg_internal.h"
+
+constexpr int kReduceMaxThreads = 256;
+
+struct FinStore {
+    double* out;  // out[rhs * K + k] = total
+    int K;
+    __device__ void operator()(int rhs, const double* s) const {
+        for (int k = 0; k < K; ++k) out[rhs * K + k] = s[k];
+    }
+};
+
+template <int K, typename Fin>
+__device__ __forceinline__ void block_reduce_finalise(double (&v)[K], double* __restrict__ partials,
+                                                      unsigned int* __restrict__ ticket, int nrhs,
+                                                      const Fin& fin) {
+    __shared__ double s_rows[K][kReduceMaxThreads / 32][32];
+    __shared__ double s_fin[K][32];
+    __shared__ int s_last;
+
+    const int lanes = blockDim.x;
+    const int t = threadIdx.y * lanes + threadIdx.x;
+    const int lane_id = t & 31;
+    const int warp = t >> 5;
+    const int nwarps = (blockDim.x * blockDim.y + 31) >> 5;
+    const int rhs0 = blockIdx.y * lanes;
+
+    // within a warp, lanes sharing threadIdx.x differ by multiples of `lanes`
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double a = v[k];
+        for (int off = 16; off >= lanes; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+        v[k] = a;
+    }
+    if (lane_id < lanes) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) s_rows[k][warp][lane_id] = v[k];
+    }
+    __syncthreads();
+    if (t < lanes && rhs0 + t < nrhs) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double a = 0.0;
+            for (int w = 0; w < nwarps; ++w) a += s_rows[k][w][t];
+            partials[((size_t)(rhs0 + t) * K + k) * gridDim.x + blockIdx.x] = a;
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (t == 0) {
+        unsigned int prev = atomicAdd(ticket + blockIdx.y, 1u);
+        s_last = (prev == gridDim.x - 1) ? 1 : 0;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    // last block: one warp per (lane, k) pair, strided sums in a fixed order
+    const int npairs = lanes * K;
+    for (int p = warp; p < npairs; p += nwarps) {
+        const int l = p / K, k = p - l * K;
+        const int r = rhs0 + l;
+        double a = 0.0;
+        if (r < nrhs) {
+            const double* src = partials + ((size_t)r * K + k) * gridDim.x;
+            for (int b = lane_id; b < (int)gridDim.x; b += 32) a += __ldcg(src + b);
+        }
+        for (int off = 16; off >= 1; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+        if (lane_id == 0) s_fin[k][l] = a;
+    }
+    __syncthreads();
+    if (t < lanes && rhs0 + t < nrhs) {
+        double sums[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) sums[k] = s_fin[k][t];
+        fin(rhs0 + t, sums);
+    }
+    if (t == 0) ticket[blockIdx.y] = 0u;
+}
+
+// Launch shape for reducing kernels: lanes is a power of two <= 32, at most
+// kMaxReduceBlocks blocks along x (kernels stride over the remaining sites).
+struct ReduceLaunch {
+    dim3 grid, block;
+    int lanes, rows;
+};
+inline ReduceLaunch reduce_launch(int nsites, int nrhs) {
+    ReduceLaunch s;
+    int lanes = 1;
+    while (lanes * 2 <= nrhs && lanes < 32) lanes *= 2;
+    s.lanes = lanes;
+    s.rows = kReduceMaxThreads / lanes;
+    int bx = (nsites + s.rows - 1) / s.rows;
+    if (bx > kMaxReduceBlocks) bx = kMaxReduceBlocks;
+    if (bx < 1) bx = 1;
+    s.block = dim3(lanes, s.rows, 1);
+    s.grid = dim3(bx, (nrhs + lanes - 1) / lanes, 1);
+    return s;
+}

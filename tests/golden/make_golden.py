@@ -1,0 +1,95 @@
+"""Generates the golden fixtures in tests/golden/ from the reference's own code.
+
+Runs the reference C++ sources (compiled by oracle/Makefile into
+oracle/_ref/libsmg_ref.so through oracle/ref_shim.cpp) on seeded inputs and
+stores inputs and outputs as compressed .npz files.  The GPU machine has no copy of
+the reference, so the GPU parity tests read these fixtures there.
+
+    python tests/golden/make_golden.py
+
+Inputs: gauge links from smg_host_gauge_normal (theta ~ N(0, 1/beta),
+std::mt19937) and sources from the reference's random_vec with a stated seed.
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle import oracle as O  # noqa: E402
+from schwinger_mg_gb300.api import gauge_normal  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def dirac_case(ref, name, L, beta, m, r, csw, mu, gseed, vseed):
+    U = gauge_normal(L, beta, gseed).reshape(-1)
+    n = 2 * L * L
+    src = ref.random_vecs(1, n, vseed)
+    d = dict(L=L, beta=beta, m=m, r=r, csw=csw, mu=mu, gseed=gseed, vseed=vseed, U=U, src=src,
+             clover=ref.clover(U), avg_plaq=ref.avg_plaq(U))
+    for op, key in enumerate(["D", "Ddag", "DdagD", "g5D"]):
+        d[key] = ref.dirac(U, m, r, csw, mu, op, src)
+    np.savez_compressed(OUT / f"{name}.npz", **d)
+    print("wrote", name)
+
+
+def cg_force_case(ref, name, L, beta, m, r, csw, mu, gseed, vseed, tol=1e-10):
+    U = gauge_normal(L, beta, gseed).reshape(-1)
+    n = 2 * L * L
+    eta = ref.random_vecs(1, n, vseed)
+    phi = ref.dirac(U, m, r, csw, mu, 1, eta)  # phi = D^dag eta (hmc_trajectory.cpp:32-36)
+    X, it, res = ref.cg(U, m, r, csw, mu, phi, 10000, tol)
+    F = ref.fermion_force(U, m, r, csw, mu, X)
+    G = ref.gauge_force(U, beta)
+    np.savez_compressed(OUT / f"{name}.npz", L=L, beta=beta, m=m, r=r, csw=csw, mu=mu, gseed=gseed, vseed=vseed,
+                        U=U, eta=eta, phi=phi, X=X, cg_iters=it, cg_res=res, tol=tol, fermion_force=F,
+                        gauge_force=G, gauge_action=ref.gauge_action(U, beta))
+    print("wrote", name, "cg iters", it)
+
+
+def mg_case(ref, name, L, beta, m, r, csw, mu, gseed, bs, k, null_iters, seed):
+    U = gauge_normal(L, beta, gseed).reshape(-1)
+    n = 2 * L * L
+    params = O.RefMGParams(2, bs, k, 0, null_iters, 1, 3, 3, 0)
+    init = ref.random_vecs(k, n, seed)                       # the vectors compute_near_null_space draws
+    nv = ref.near_null_space(U, m, r, csw, mu, k, null_iters, seed)
+    bv = ref.prolongator_build(L, bs, k, nv)
+    links = ref.sparse_coarse_build(U, m, r, csw, mu, bs, k, bv)
+    nbx = L // bs
+    csrc = ref.random_vecs(1, nbx * nbx * k, seed + 1)
+    capply = ref.sparse_coarse_apply(nbx, nbx, k, links, csrc)
+    fsrc = ref.random_vecs(1, n, seed + 2)
+    restr = ref.restrict(L, bs, k, bv, fsrc)
+    prol = ref.prolong(L, bs, k, bv, csrc)
+    mr = ref.mr_smooth(U, m, r, csw, mu, fsrc, np.zeros(n, complex), 4)
+    # 2-level hierarchy on exactly these null vectors: dense coarse LU solve
+    pre = ref.mg_precondition(U, m, r, csw, mu, O.RefMGParams(2, bs, k, 0, 0, 1, 3, 3, 0), seed, fsrc, warm=nv)
+    x, it, res = ref.mg_gcr(U, m, r, csw, mu, O.RefMGParams(2, bs, k, 0, 0, 1, 3, 3, 0), seed, fsrc, 200, 1e-10, 20,
+                            warm=nv)
+    np.savez_compressed(OUT / f"{name}.npz", L=L, beta=beta, m=m, r=r, csw=csw, mu=mu, gseed=gseed, bs=bs, k=k,
+                        null_iters=null_iters, seed=seed, U=U, init=init, null_vecs=nv, block_vecs=bv, links=links,
+                        coarse_src=csrc, coarse_apply=capply, fine_src=fsrc, restrict=restr, prolong=prol,
+                        mr4=mr, mg_precondition=pre, gcr_x=x, gcr_iters=it, gcr_res=res)
+    print("wrote", name, "gcr iters", it, "res", res)
+
+
+def main():
+    O.build(ref=True)
+    ref = O.ref()
+    if ref is None:
+        raise SystemExit("the reference shim is needed to generate fixtures")
+    dirac_case(ref, "dirac_L8_wilson", 8, 2.0, 0.3, 1.0, 0.0, 0.0, 11, 12)
+    dirac_case(ref, "dirac_L16_clover_twist", 16, 2.0, -0.05, 1.0, 1.0, 0.2, 21, 22)
+    dirac_case(ref, "dirac_L32_config1", 32, 2.0, 0.1, 1.0, 1.0, 0.0, 31, 32)
+    cg_force_case(ref, "cg_force_L32_config1", 32, 2.0, 0.1, 1.0, 1.0, 0.0, 31, 33)
+    cg_force_case(ref, "cg_force_L16_wilson", 16, 4.0, 0.2, 1.0, 0.0, 0.0, 41, 42)
+    mg_case(ref, "mg_L16_bs4_k4", 16, 2.0, 0.1, 1.0, 1.0, 0.0, 51, 4, 4, 5, 52)
+
+
+if __name__ == "__main__":
+    main()
