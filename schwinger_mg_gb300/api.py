@@ -12,6 +12,7 @@ reference's asserts and warnings.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -30,6 +31,35 @@ def _as_c128(a) -> np.ndarray:
 
 
 PRECISIONS = {"f64": _L.F64, "f32": _L.F32, "f16": _L.F16}
+
+
+class _Handle:
+    """Owns one C handle.  A dependent (e.g. a DiracOp on a GaugeField) is
+    registered with its owner and is always released before it, also when the
+    garbage collector finalises both in arbitrary order."""
+
+    h = None
+
+    def _adopt(self, h, owner: "_Handle | None", destroy) -> None:
+        self.h = h
+        self._destroy = destroy
+        self._dependents = weakref.WeakSet()
+        self._owner = owner
+        if owner is not None:
+            owner._dependents.add(self)
+
+    def release(self) -> None:
+        h = self.h
+        if not h:
+            return
+        for dep in list(getattr(self, "_dependents", ())):
+            dep.release()
+        self.h = None
+        if _L._lib is not None:
+            self._destroy(h)
+
+    def __del__(self):
+        self.release()
 
 
 class Context:
@@ -112,7 +142,7 @@ class Lattice:
         return ((s % self.L) + (s // self.L)) % 2
 
 
-class GaugeField:
+class GaugeField(_Handle):
     """U(1) links U[mu][s] resident on the device (reference src/gauge.h:10-36)."""
 
     def __init__(self, lat: Lattice, U=None, ctx: Context | None = None):
@@ -126,7 +156,7 @@ class GaugeField:
         h = C.c_void_p()
         _L.check(_L.lib().smg_gauge_create(self.ctx.h, lat.L, _ptr(U.view(np.float64)), C.byref(h)),
                  "smg_gauge_create", self.ctx.h)
-        self.h = h
+        self._adopt(h, None, _L.lib().smg_gauge_destroy)
 
     @property
     def U(self) -> np.ndarray:
@@ -143,13 +173,8 @@ class GaugeField:
         _L.check(_L.lib().smg_gauge_avg_plaq(self.h, C.byref(v)), "smg_gauge_avg_plaq", self.ctx.h)
         return v.value
 
-    def __del__(self):
-        if getattr(self, "h", None) and _L._lib is not None:
-            _L.lib().smg_gauge_destroy(self.h)
-            self.h = None
 
-
-class Field:
+class Field(_Handle):
     """nrhs spinors of an L x L lattice resident on the device."""
 
     def __init__(self, lat: Lattice, nrhs: int = 1, precision: str = "f64", ctx: Context | None = None, data=None):
@@ -160,7 +185,7 @@ class Field:
         h = C.c_void_p()
         _L.check(_L.lib().smg_field_create(self.ctx.h, lat.L, nrhs, PRECISIONS[precision], C.byref(h)),
                  "smg_field_create", self.ctx.h)
-        self.h = h
+        self._adopt(h, None, _L.lib().smg_field_destroy)
         if data is not None:
             self.upload(data)
 
@@ -181,11 +206,6 @@ class Field:
 
     def copy_from(self, other: "Field") -> None:
         _L.check(_L.lib().smg_field_copy(other.h, self.h), "smg_field_copy", self.ctx.h)
-
-    def __del__(self):
-        if getattr(self, "h", None) and _L._lib is not None:
-            _L.lib().smg_field_destroy(self.h)
-            self.h = None
 
 
 def dot(a: Field, b: Field) -> np.ndarray:
@@ -211,7 +231,7 @@ def scale(v: Field, alpha) -> None:
     _L.check(_L.lib().smg_blas_scale(_ptr(al.view(np.float64)), v.h), "smg_blas_scale", v.ctx.h)
 
 
-class DiracOp:
+class DiracOp(_Handle):
     """Wilson-clover Dirac operator (reference src/dirac.h:8-183) on the device."""
 
     def __init__(self, lat: Lattice, gauge: GaugeField, mass: float, r: float = 1.0, c_sw: float = 0.0,
@@ -223,7 +243,7 @@ class DiracOp:
         h = C.c_void_p()
         _L.check(_L.lib().smg_dirac_create(gauge.h, mass, r, c_sw, mu_t, C.byref(h)), "smg_dirac_create",
                  self.ctx.h)
-        self.h = h
+        self._adopt(h, gauge, _L.lib().smg_dirac_destroy)
 
     def refresh(self) -> None:
         """Recomputes the clover term after the gauge links changed."""
@@ -264,11 +284,6 @@ class DiracOp:
 
     def apply_g5D(self, src, dst=None):
         return self.apply_op(_L.OP_G5D, src, dst)
-
-    def __del__(self):
-        if getattr(self, "h", None) and _L._lib is not None:
-            _L.lib().smg_dirac_destroy(self.h)
-            self.h = None
 
 
 @dataclass

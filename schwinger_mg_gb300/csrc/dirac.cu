@@ -214,7 +214,7 @@ smg_status gamma5_inplace(smg_field* f) {
 
 smg_status check_op_fields(smg_dirac* d, const smg_field* src, const smg_field* dst) {
     if (!d || !src || !dst) return SMG_BAD_ARG;
-    smg_context* ctx = d->gauge->ctx;
+    smg_context* ctx = d->ctx;
     if (src == dst) return smg_fail(ctx, SMG_BAD_ARG, "src and dst must be distinct fields");
     SMG_TRY(smg_field_check_pair(src, dst));
     if (src->ctx != ctx) return smg_fail(ctx, SMG_BAD_ARG, "field and operator belong to different contexts");
@@ -261,6 +261,7 @@ SMG_API smg_status smg_dirac_create(smg_gauge* gf, double mass, double r, double
     *out = nullptr;
     smg_context* ctx = gf->ctx;
     smg_dirac* d = new smg_dirac();
+    d->ctx = ctx;
     d->gauge = gf;
     d->mass = mass;
     d->r = r;
@@ -289,7 +290,7 @@ SMG_API smg_status smg_dirac_create(smg_gauge* gf, double mass, double r, double
 
 SMG_API smg_status smg_dirac_destroy(smg_dirac* d) {
     if (!d) return SMG_OK;
-    cudaStreamSynchronize(d->gauge->ctx->stream);
+    cudaStreamSynchronize(d->ctx->stream);
     if (d->F01) cudaFree(d->F01);
     if (d->C64) cudaFree(d->C64);
     if (d->C32) cudaFree(d->C32);
@@ -299,7 +300,7 @@ SMG_API smg_status smg_dirac_destroy(smg_dirac* d) {
 
 SMG_API smg_status smg_dirac_refresh(smg_dirac* d) {
     if (!d) return SMG_BAD_ARG;
-    smg_context* ctx = d->gauge->ctx;
+    smg_context* ctx = d->ctx;
     const Geom g = d->gauge->g;
     if (d->c_sw != 0.0) {
         k_clover<<<(g.V + 255) / 256, 256, 0, ctx->stream>>>(d->gauge->U64, g, d->c_sw, d->F01, d->C64, d->C32);
@@ -313,7 +314,7 @@ SMG_API smg_status smg_dirac_refresh(smg_dirac* d) {
 
 SMG_API smg_status smg_dirac_get_clover(smg_dirac* d, double* F01) {
     if (!d || !F01) return SMG_BAD_ARG;
-    smg_context* ctx = d->gauge->ctx;
+    smg_context* ctx = d->ctx;
     const Geom g = d->gauge->g;
     double* tmp = nullptr;
     SMG_CUDA(ctx, cudaMallocAsync(&tmp, (size_t)g.V * sizeof(double), ctx->stream));

@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(TX* TY) k_fermion_force(ForceArgs a) {
 
 // Device-side force into a device array F[mu][s] (lexicographic).
 smg_status smg_fermion_force_dev(smg_dirac* d, const smg_field* X, double* F_dev) {
-    smg_context* ctx = d->gauge->ctx;
+    smg_context* ctx = d->ctx;
     ForceArgs a;
     a.X = (const cx<double>*)X->data;
     a.U = d->gauge->U64;
@@ -157,7 +157,7 @@ extern "C" {
 
 SMG_API smg_status smg_fermion_force(smg_dirac* d, const smg_field* X, double* force) {
     if (!d || !X || !force) return SMG_BAD_ARG;
-    smg_context* ctx = d->gauge->ctx;
+    smg_context* ctx = d->ctx;
     if (X->prec != SMG_F64 || X->nrhs != 1)
         return smg_fail(ctx, SMG_BAD_ARG, "fermion_force needs a single-RHS F64 field");
     if (X->g.L != d->gauge->g.L) return smg_fail(ctx, SMG_BAD_ARG, "field L differs from gauge L");

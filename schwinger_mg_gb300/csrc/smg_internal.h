@@ -141,7 +141,11 @@ struct smg_gauge {
     cx<float>* U32 = nullptr;
 };
 
+// A Dirac handle reads its gauge handle's links at every apply, so the gauge
+// must outlive it; destroying the Dirac handle touches only its own memory
+// and context.
 struct smg_dirac {
+    smg_context* ctx = nullptr;
     smg_gauge* gauge = nullptr;
     double mass = 0, r = 1, c_sw = 0, mu_t = 0;
     double* C64 = nullptr;  // 0.5 * c_sw * F01 per device site (nullptr when c_sw == 0)

@@ -272,7 +272,7 @@ extern "C" {
 SMG_API smg_status smg_cg_solve(smg_dirac* d, const smg_field* rhs, smg_field* x, int max_iter, double tol,
                                 smg_solve_result* res) {
     if (!d || !rhs || !x) return SMG_BAD_ARG;
-    smg_context* ctx = d->gauge->ctx;
+    smg_context* ctx = d->ctx;
     if (rhs == x) return smg_fail(ctx, SMG_BAD_ARG, "rhs and x must be distinct");
     SMG_TRY(smg_field_check_pair(rhs, x));
     if (rhs->g.L != d->gauge->g.L) return smg_fail(ctx, SMG_BAD_ARG, "field L differs from gauge L");
