@@ -188,6 +188,85 @@ SMG_API smg_status smg_blas_scale(const double* alpha, smg_field* v);
 SMG_API smg_status smg_cg_solve(smg_dirac* d, const smg_field* rhs, smg_field* x,
                                 int max_iter, double tol, smg_solve_result* res);
 
+/* -------------------------------------------------------------- multigrid */
+
+#define SMG_MAX_LEVELS 6
+
+/* Parameters of an MG hierarchy for A = D^dag D (reference src/config.h:19-30,
+ * src/multigrid.cpp:595-687).  Level 0 aggregates block[0][0] x block[0][1]
+ * fine sites; level l >= 1 aggregates block[l][0] x block[l][1] sites of the
+ * level-l coarse lattice.  The reference's linear blocking of 4k consecutive
+ * coarse dofs (src/prolongator.h:149-228) is the aggregate 4 x 1 when the
+ * coarse lattice width is a multiple of 4.  With chiral_split, each null
+ * vector v gives the two block vectors of (1 +- sigma3) v / 2, so a level has
+ * 2 * n_vec coarse dofs per site; without it, n_vec (the reference). */
+typedef struct {
+    int n_levels;                      /* 2 .. SMG_MAX_LEVELS              */
+    int block[SMG_MAX_LEVELS - 1][2];  /* aggregate per level transition   */
+    int n_vec[SMG_MAX_LEVELS - 1];     /* null vectors per transition      */
+    int chiral_split;                  /* 0: reference; 1: split by sigma3 */
+    int null_iters;                    /* inverse iterations (build_full_mg: 20) */
+    int null_mr_steps;                 /* MR steps per inverse iteration (5)    */
+    int pre_smooth, post_smooth;       /* MR steps per level (reference 3, 3)   */
+    int w_cycle;                       /* second coarse visit at levels < last-1 */
+    int coarse_max_iter;               /* coarsest CG (reference 200)           */
+    double coarse_tol;                 /* coarsest CG (reference 1e-12)         */
+    smg_precision precision;           /* F64, or F32 smoother and coarse levels */
+    uint32_t seed;                     /* std::mt19937 seed of the start vectors */
+} smg_mg_params;
+
+/* Fills p with the reference's defaults: 2 levels, 4 x 4 blocks, 4 null
+ * vectors, no chirality split, 20 inverse iterations of 5 MR steps, 3 + 3 MR
+ * smoothing, W-cycle, coarsest CG 200 iterations to 1e-12, FP64
+ * (reference src/config.h:19-30, src/mg_builder.cpp:18). */
+SMG_API smg_status smg_mg_params_default(smg_mg_params* p);
+
+/* build_mg_hierarchy / build_full_mg (reference src/multigrid.cpp:595-687,
+ * src/mg_builder.cpp:3-31): near-null vectors by inverse iteration
+ * (src/multigrid.cpp:435-484, 545-587), block-orthonormalised prolongators
+ * (src/prolongator.h:111-141) and 9-point Galerkin coarse operators, built
+ * directly from D P rather than by probing (src/coarse_op.h:241-279).
+ * warm_start: NULL, or n_vec[0] level-0 start vectors (each 2V complex in the
+ * reference layout) used instead of random draws, as build_mg_hierarchy's
+ * warm_start argument.  Every coarse lattice must be at least 3 x 3. */
+SMG_API smg_status smg_mg_create(smg_dirac* d, const smg_mg_params* p, const double* warm_start,
+                                 smg_mg** out);
+SMG_API smg_status smg_mg_destroy(smg_mg* mg);
+/* Sizes of level `level` (0 = fine): lattice width/height in sites and dofs
+ * per site. */
+SMG_API smg_status smg_mg_level_dims(smg_mg* mg, int level, int* nx, int* ny, int* ndof);
+/* MGHierarchy::null_vecs_l0: n_vec[0] vectors of 2V complex. */
+SMG_API smg_status smg_mg_null_vectors(smg_mg* mg, double* out);
+/* Block vectors of the prolongator from level `level` to level+1 in the
+ * reference layout [block][k][local dof] (src/prolongator.h:23) where a local
+ * dof of level 0 is 2*(lx + bx*ly) + spin and of level l >= 1 is
+ * (lx + ax*ly) * ndof_l + j. */
+SMG_API smg_status smg_mg_get_prolongator(smg_mg* mg, int level, double* block_vecs);
+/* Coarse operator of level `level` >= 1 as SparseCoarseOp::link
+ * (src/coarse_op.h:159-166): [site][dir][ki * k + kj] complex. */
+SMG_API smg_status smg_mg_get_coarse_op(smg_mg* mg, int level, double* links);
+/* x = M^-1 b, one MG cycle (MGHierarchy::precondition, src/multigrid.cpp:155;
+ * mg_cycle, :43-102).  b and x are fine fields of the hierarchy's L. */
+SMG_API smg_status smg_mg_precondition(smg_mg* mg, const smg_field* b, smg_field* x);
+/* Host-array versions of the transfer operators and the coarse operator at
+ * level `level` (Prolongator::prolong / restrict_vec, src/prolongator.h:77-108;
+ * SparseCoarseOp::apply_to, src/coarse_op.h:282-297).  Vectors use the
+ * reference's dof order: fine 2*s + spin, coarse site * ndof + j. */
+SMG_API smg_status smg_mg_prolong_host(smg_mg* mg, int level, const double* coarse, double* fine);
+SMG_API smg_status smg_mg_restrict_host(smg_mg* mg, int level, const double* fine, double* coarse);
+SMG_API smg_status smg_mg_coarse_apply_host(smg_mg* mg, int level, const double* in, double* out);
+
+/* fcg_solve / fcg_solve_mg: truncated GCR on A = D^dag D from x = 0
+ * (reference src/solvers.cpp:223-300, 803-811), preconditioned by one MG
+ * cycle per iteration (mg != NULL) or unpreconditioned (mg == NULL).  The
+ * orthogonalisation coefficient is <A p_i, A z> / <A p_i, A p_i>; the
+ * reference's conjugate of it (solvers.cpp:261) is used when
+ * reference_coefficient != 0.  Runs in the precision of the fields; with an
+ * F32 hierarchy and F64 fields the preconditioner runs in FP32 on the
+ * normalised residual. */
+SMG_API smg_status smg_gcr_solve(smg_dirac* d, smg_mg* mg, const smg_field* rhs, smg_field* x, int max_iter,
+                                 double tol, int trunc, int reference_coefficient, smg_solve_result* res);
+
 /* ------------------------------------------------------------------ forces */
 
 /* fermion_force (reference src/hmc_forces.cpp:134-194 and 198-495): with

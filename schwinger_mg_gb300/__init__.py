@@ -8,6 +8,13 @@ include/smg_gpu.h); this package is the Python mirror of that API.
 from ._lib import SmgError, SmgLibraryError, lib  # noqa: F401
 from .api import (  # noqa: F401
     CGResult,
+    FCGResult,
+    MGHierarchy,
+    build_full_mg,
+    build_mg_hierarchy,
+    fcg_solve,
+    fcg_solve_mg,
+    mg_params,
     Context,
     DiracOp,
     Field,

@@ -32,6 +32,18 @@ class SolveResult(C.Structure):
                 ("operator_applications", C.c_int)]
 
 
+MAX_LEVELS = 6
+
+
+class MGParams(C.Structure):
+    """smg_mg_params (include/smg_gpu.h)."""
+    _fields_ = [("n_levels", C.c_int), ("block", (C.c_int * 2) * (MAX_LEVELS - 1)),
+                ("n_vec", C.c_int * (MAX_LEVELS - 1)), ("chiral_split", C.c_int), ("null_iters", C.c_int),
+                ("null_mr_steps", C.c_int), ("pre_smooth", C.c_int), ("post_smooth", C.c_int), ("w_cycle", C.c_int),
+                ("coarse_max_iter", C.c_int), ("coarse_tol", C.c_double), ("precision", C.c_int),
+                ("seed", C.c_uint32)]
+
+
 _vp = C.c_void_p
 _dp = C.POINTER(C.c_double)
 _st = C.c_int
@@ -80,6 +92,18 @@ _SIGS = {
     "smg_blas_scale": (_st, [_dp, _vp]),
     "smg_cg_solve": (_st, [_vp, _vp, _vp, C.c_int, C.c_double, C.POINTER(SolveResult)]),
     "smg_fermion_force": (_st, [_vp, _vp, _dp]),
+    "smg_mg_params_default": (_st, [C.POINTER(MGParams)]),
+    "smg_mg_create": (_st, [_vp, C.POINTER(MGParams), _dp, C.POINTER(_vp)]),
+    "smg_mg_destroy": (_st, [_vp]),
+    "smg_mg_level_dims": (_st, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "smg_mg_null_vectors": (_st, [_vp, _dp]),
+    "smg_mg_get_prolongator": (_st, [_vp, C.c_int, _dp]),
+    "smg_mg_get_coarse_op": (_st, [_vp, C.c_int, _dp]),
+    "smg_mg_precondition": (_st, [_vp, _vp, _vp]),
+    "smg_mg_prolong_host": (_st, [_vp, C.c_int, _dp, _dp]),
+    "smg_mg_restrict_host": (_st, [_vp, C.c_int, _dp, _dp]),
+    "smg_mg_coarse_apply_host": (_st, [_vp, C.c_int, _dp, _dp]),
+    "smg_gcr_solve": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(SolveResult)]),
     "smg_host_gauge_normal": (_st, [C.c_int, C.c_double, C.c_uint32, _dp]),
     "smg_host_random_vec": (_st, [C.c_int64, C.c_uint32, _dp]),
 }

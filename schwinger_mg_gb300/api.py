@@ -345,3 +345,172 @@ def random_vec(n: int, seed: int) -> np.ndarray:
     out = np.empty(n, dtype=np.complex128)
     _L.check(_L.lib().smg_host_random_vec(n, seed, _ptr(out.view(np.float64))), "smg_host_random_vec")
     return out
+
+
+# ---------------------------------------------------------------- multigrid
+def mg_params(n_levels: int = 2, block_size: int = 4, k_null: int = 4, coarse_block=(4, 1), null_iters: int = 20,
+              w_cycle: bool = True, pre_smooth: int = 3, post_smooth: int = 3, chiral_split: bool = False,
+              blocks=None, n_vecs=None, null_mr_steps: int = 5, coarse_max_iter: int = 200,
+              coarse_tol: float = 1e-12, precision: str = "f64", seed: int = 42) -> _L.MGParams:
+    """smg_mg_params from the reference's build_mg_hierarchy arguments
+    (src/multigrid.cpp:595-602).  `blocks` / `n_vecs` override the per-level
+    aggregate shapes and null-vector counts."""
+    p = _L.MGParams()
+    _L.check(_L.lib().smg_mg_params_default(C.byref(p)), "smg_mg_params_default")
+    p.n_levels = n_levels
+    for l in range(_L.MAX_LEVELS - 1):
+        b = (blocks[l] if blocks is not None and l < len(blocks) else
+             ((block_size, block_size) if l == 0 else tuple(coarse_block)))
+        p.block[l][0], p.block[l][1] = int(b[0]), int(b[1])
+        p.n_vec[l] = int(n_vecs[l] if n_vecs is not None and l < len(n_vecs) else k_null)
+    p.chiral_split = int(chiral_split)
+    p.null_iters = null_iters
+    p.null_mr_steps = null_mr_steps
+    p.pre_smooth, p.post_smooth = pre_smooth, post_smooth
+    p.w_cycle = int(w_cycle)
+    p.coarse_max_iter, p.coarse_tol = coarse_max_iter, coarse_tol
+    p.precision = PRECISIONS[precision]
+    p.seed = seed
+    return p
+
+
+class MGHierarchy(_Handle):
+    """MG preconditioner for D^dag D (MGHierarchy, reference src/multigrid.h:41-107)."""
+
+    def __init__(self, D: DiracOp, params: _L.MGParams | None = None, warm_start=None):
+        self.D = D
+        self.ctx = D.ctx
+        self.params = params if params is not None else mg_params()
+        h = C.c_void_p()
+        warm = None
+        if warm_start is not None:
+            warm = _as_c128(warm_start).reshape(-1)
+            if warm.size != self.params.n_vec[0] * D.lat.ndof:
+                raise ValueError("warm_start must hold n_vec[0] fine vectors")
+        wp = _ptr(warm.view(np.float64)) if warm is not None else None
+        _L.check(_L.lib().smg_mg_create(D.h, C.byref(self.params), wp, C.byref(h)), "smg_mg_create", self.ctx.h)
+        self._adopt(h, D, _L.lib().smg_mg_destroy)
+
+    @property
+    def n_levels(self) -> int:
+        return self.params.n_levels
+
+    def level_dims(self, level: int):
+        nx, ny, nd = C.c_int(), C.c_int(), C.c_int()
+        _L.check(_L.lib().smg_mg_level_dims(self.h, level, C.byref(nx), C.byref(ny), C.byref(nd)),
+                 "smg_mg_level_dims", self.ctx.h)
+        return nx.value, ny.value, nd.value
+
+    def level_dim(self, level: int) -> int:
+        nx, ny, nd = self.level_dims(level)
+        return nx * ny * nd
+
+    @property
+    def null_vecs_l0(self) -> np.ndarray:
+        k = self.params.n_vec[0]
+        out = np.empty(k * self.D.lat.ndof, dtype=np.complex128)
+        _L.check(_L.lib().smg_mg_null_vectors(self.h, _ptr(out.view(np.float64))), "smg_mg_null_vectors", self.ctx.h)
+        return out.reshape(k, -1)
+
+    def prolongator(self, level: int = 0) -> np.ndarray:
+        """block_vecs in the reference layout [block][k][local dof]."""
+        n = self.level_dim(level) * self.level_dims(level + 1)[2]
+        out = np.empty(n, dtype=np.complex128)
+        _L.check(_L.lib().smg_mg_get_prolongator(self.h, level, _ptr(out.view(np.float64))),
+                 "smg_mg_get_prolongator", self.ctx.h)
+        return out
+
+    def coarse_op(self, level: int = 1) -> np.ndarray:
+        """SparseCoarseOp::link layout [site][dir][ki*k + kj]."""
+        nx, ny, nd = self.level_dims(level)
+        out = np.empty(nx * ny * 9 * nd * nd, dtype=np.complex128)
+        _L.check(_L.lib().smg_mg_get_coarse_op(self.h, level, _ptr(out.view(np.float64))), "smg_mg_get_coarse_op",
+                 self.ctx.h)
+        return out
+
+    def _host_op(self, fn, level, v, out_dim):
+        v = _as_c128(v).reshape(-1)
+        out = np.empty(out_dim, dtype=np.complex128)
+        _L.check(getattr(_L.lib(), fn)(self.h, level, _ptr(v.view(np.float64)), _ptr(out.view(np.float64))), fn,
+                 self.ctx.h)
+        return out
+
+    def prolong(self, level: int, coarse):
+        return self._host_op("smg_mg_prolong_host", level, coarse, self.level_dim(level))
+
+    def restrict_vec(self, level: int, fine):
+        return self._host_op("smg_mg_restrict_host", level, fine, self.level_dim(level + 1))
+
+    def coarse_apply(self, level: int, v):
+        return self._host_op("smg_mg_coarse_apply_host", level, v, self.level_dim(level))
+
+    def precondition(self, b):
+        """One MG cycle x = M^-1 b (MGHierarchy::precondition, src/multigrid.cpp:155)."""
+        if isinstance(b, Field):
+            x = Field(self.D.lat, b.nrhs, b.precision, self.ctx)
+            _L.check(_L.lib().smg_mg_precondition(self.h, b.h, x.h), "smg_mg_precondition", self.ctx.h)
+            return x
+        a = _as_c128(b)
+        nrhs = a.size // self.D.lat.ndof
+        prec = "f64" if self.params.precision == _L.F64 else "f32"
+        fb = Field(self.D.lat, nrhs, prec, self.ctx, data=a)
+        fx = Field(self.D.lat, nrhs, prec, self.ctx)
+        _L.check(_L.lib().smg_mg_precondition(self.h, fb.h, fx.h), "smg_mg_precondition", self.ctx.h)
+        return fx.download().reshape(a.shape)
+
+
+def build_mg_hierarchy(D: DiracOp, n_levels: int, block_size: int, k_null: int, coarse_block_agg: int,
+                       null_iters: int, seed: int, w_cycle: bool = True, pre_smooth: int = 3, post_smooth: int = 3,
+                       warm_start=None, **kw) -> MGHierarchy:
+    """build_mg_hierarchy (reference src/multigrid.cpp:595-687).  The
+    reference's rng argument is `seed` (std::mt19937(seed)); its deeper-level
+    linear blocking of coarse_block_agg = 4*k_null dofs is the 4 x 1 aggregate."""
+    agg = max(1, coarse_block_agg // max(1, k_null))
+    p = mg_params(n_levels, block_size, k_null, (agg, 1), null_iters, w_cycle, pre_smooth, post_smooth, seed=seed,
+                  **kw)
+    return MGHierarchy(D, p, warm_start)
+
+
+def build_full_mg(D: DiracOp, mg_levels: int = 1, block_size: int = 4, k_null: int = 4, coarse_block: int = 0,
+                  w_cycle: bool = True, pre_smooth: int = 3, post_smooth: int = 3, seed: int = 42, warm_start=None,
+                  **kw) -> MGHierarchy:
+    """build_full_mg (reference src/mg_builder.cpp:3-31) with the trlm null-space
+    path: 20 inverse iterations, or 5 when warm-started."""
+    cb = coarse_block if coarse_block > 0 else 4 * k_null
+    iters = 5 if warm_start is not None else 20
+    return build_mg_hierarchy(D, max(2, mg_levels), block_size, k_null, cb, iters, seed, w_cycle, pre_smooth,
+                              post_smooth, warm_start, **kw)
+
+
+@dataclass
+class FCGResult:
+    """FCGResult (reference src/solvers.h:31-35) plus the FP64 true residual."""
+    solution: np.ndarray
+    iterations: int
+    final_residual: float
+    true_residual: float = float("nan")
+    status: int = 0
+
+
+def fcg_solve(A: DiracOp, n: int, rhs, precond: "MGHierarchy | None", max_iter: int, tol: float, trunc: int = 30,
+              precision: str = "f64", reference_coefficient: bool = False) -> FCGResult:
+    """Truncated GCR on D^dag D (reference fcg_solve, src/solvers.cpp:223-300);
+    `precond` is an MGHierarchy (one cycle per iteration) or None."""
+    b = _as_c128(rhs)
+    if n != A.lat.ndof:
+        raise ValueError("n must equal 2*V")
+    nrhs = b.size // A.lat.ndof
+    fb = Field(A.lat, nrhs, precision, A.ctx, data=b)
+    fx = Field(A.lat, nrhs, precision, A.ctx)
+    res = _L.SolveResult()
+    st = _L.lib().smg_gcr_solve(A.h, precond.h if precond is not None else None, fb.h, fx.h, max_iter, tol, trunc,
+                                int(reference_coefficient), C.byref(res))
+    if st not in (_L.OK, _L.NOT_CONVERGED):
+        _L.check(st, "smg_gcr_solve", A.ctx.h)
+    return FCGResult(fx.download().reshape(b.shape), res.iterations, res.final_residual, res.true_residual, st)
+
+
+def fcg_solve_mg(A: DiracOp, n: int, rhs, mg: MGHierarchy, max_iter: int, tol: float, truncation: int = 20,
+                 **kw) -> FCGResult:
+    """fcg_solve_mg (reference src/solvers.cpp:803-811)."""
+    return fcg_solve(A, n, rhs, mg, max_iter, tol, truncation, **kw)

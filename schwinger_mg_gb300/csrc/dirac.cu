@@ -44,9 +44,18 @@ __global__ void __launch_bounds__(256) k_dslash(DslashArgs<T> a) {
     for (int k = 0; k < K; ++k) v[k] = 0.0;
 
     if (rhs < nrhs) {
-        for (int q = blockIdx.x * blockDim.y + threadIdx.y; q < g.V; q += gridDim.x * blockDim.y) {
-            int x, y, p;
-            site_coords(g, q, x, y, p);
+        // Work items walk rows with both parities interleaved (row y even
+        // sites, row y odd sites, row y+1, ...), so the neighbour rows a
+        // block reads were read moments ago by its predecessors and are still
+        // in L2; walking all even sites before all odd ones streams every
+        // spinor from DRAM twice once the field outgrows L2.
+        for (int w = blockIdx.x * blockDim.y + threadIdx.y; w < g.V; w += gridDim.x * blockDim.y) {
+            const int y = w / g.L;
+            const int rem = w - y * g.L;
+            const int p = rem >= g.Lh ? 1 : 0;
+            const int xh = rem - p * g.Lh;
+            const int x = 2 * xh + ((y + p) & 1);
+            const int q = p * g.Vh + y * g.Lh + xh;
             const int op = (1 - p) * g.Vh;
             const int xp = x + 1 == g.L ? 0 : x + 1;
             const int xm = x == 0 ? g.L - 1 : x - 1;
@@ -62,12 +71,16 @@ __global__ void __launch_bounds__(256) k_dslash(DslashArgs<T> a) {
             const cx<T> u1f = a.U[g.V + q];
             const cx<T> u1b = a.U[g.V + q_ym];
 
-            auto ld = [&](int qq, int sp) { return a.src[((int64_t)qq * 2 + sp) * nrhs + rhs]; };
-            const cx<T> s0 = ld(q, 0), s1 = ld(q, 1);
-            const cx<T> a0x = u0f * ld(q_xp, 0), a1x = u0f * ld(q_xp, 1);
-            const cx<T> b0x = cmulc(u0b, ld(q_xm, 0)), b1x = cmulc(u0b, ld(q_xm, 1));
-            const cx<T> a0y = u1f * ld(q_yp, 0), a1y = u1f * ld(q_yp, 1);
-            const cx<T> b0y = cmulc(u1b, ld(q_ym, 0)), b1y = cmulc(u1b, ld(q_ym, 1));
+            const Spinor<T> ps = ld_spinor(a.src, q, rhs, nrhs);
+            const Spinor<T> pxp = ld_spinor(a.src, q_xp, rhs, nrhs);
+            const Spinor<T> pxm = ld_spinor(a.src, q_xm, rhs, nrhs);
+            const Spinor<T> pyp = ld_spinor(a.src, q_yp, rhs, nrhs);
+            const Spinor<T> pym = ld_spinor(a.src, q_ym, rhs, nrhs);
+            const cx<T> s0 = ps.s0, s1 = ps.s1;
+            const cx<T> a0x = u0f * pxp.s0, a1x = u0f * pxp.s1;
+            const cx<T> b0x = cmulc(u0b, pxm.s0), b1x = cmulc(u0b, pxm.s1);
+            const cx<T> a0y = u1f * pyp.s0, a1y = u1f * pyp.s1;
+            const cx<T> b0y = cmulc(u1b, pym.s0), b1y = cmulc(u1b, pym.s1);
 
             const T Cq = a.C ? a.C[q] : T(0);
             const cx<T> dg0 = mk<T>(a.diag + Cq, a.mu_eff);
@@ -80,15 +93,16 @@ __global__ void __launch_bounds__(256) k_dslash(DslashArgs<T> a) {
 
             const cx<T> d0 = dg0 * s0 - half * (a.r * sr0 + sgn * off0);
             const cx<T> d1 = dg1 * s1 - half * (a.r * sr1 + sgn * off1);
-            a.dst[((int64_t)q * 2 + 0) * nrhs + rhs] = d0;
-            a.dst[((int64_t)q * 2 + 1) * nrhs + rhs] = d1;
+            Spinor<T> out;
+            out.s0 = d0;
+            out.s1 = d1;
+            st_spinor(a.dst, q, rhs, nrhs, out);
 
             if (EPI == EPI_NORM) {
                 v[0] += (double)(norm2(d0) + norm2(d1));
             } else if (EPI == EPI_MR) {
-                const cx<T> w0 = a.w[((int64_t)q * 2 + 0) * nrhs + rhs];
-                const cx<T> w1 = a.w[((int64_t)q * 2 + 1) * nrhs + rhs];
-                const cx<T> c = cmulc(d0, w0) + cmulc(d1, w1);
+                const Spinor<T> wv = ld_spinor(a.w, q, rhs, nrhs);
+                const cx<T> c = cmulc(d0, wv.s0) + cmulc(d1, wv.s1);
                 v[0] += (double)c.re;
                 v[1] += (double)c.im;
                 v[2] += (double)(norm2(d0) + norm2(d1));
@@ -135,7 +149,7 @@ __global__ void k_gamma5(cx<T>* __restrict__ v, int nsites, int nrhs) {
     int rhs = blockIdx.y * blockDim.x + threadIdx.x;
     int q = blockIdx.x * blockDim.y + threadIdx.y;
     if (rhs >= nrhs || q >= nsites) return;
-    int64_t i = ((int64_t)q * 2 + 1) * nrhs + rhs;
+    int64_t i = sidx(q, rhs, 1, nrhs);
     v[i] = -v[i];
 }
 

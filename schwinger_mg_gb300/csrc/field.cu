@@ -18,8 +18,8 @@ __global__ void k_host_to_field(const cx<double>* __restrict__ host, cx<T>* __re
     int x = s % g.L, y = s / g.L;
     int q = site_q(g, x, y);
     const cx<double>* h = host + ((int64_t)rhs * g.V + s) * 2;
-    out[((int64_t)q * 2 + 0) * nrhs + rhs] = cvt<T>(h[0]);
-    out[((int64_t)q * 2 + 1) * nrhs + rhs] = cvt<T>(h[1]);
+    out[sidx(q, rhs, 0, nrhs)] = cvt<T>(h[0]);
+    out[sidx(q, rhs, 1, nrhs)] = cvt<T>(h[1]);
 }
 
 template <typename T>
@@ -33,8 +33,8 @@ __global__ void k_field_to_host(const cx<T>* __restrict__ in, cx<double>* __rest
     int x = s % g.L, y = s / g.L;
     int q = site_q(g, x, y);
     cx<double>* h = host + ((int64_t)rhs * g.V + s) * 2;
-    h[0] = cvt<double>(in[((int64_t)q * 2 + 0) * nrhs + rhs]);
-    h[1] = cvt<double>(in[((int64_t)q * 2 + 1) * nrhs + rhs]);
+    h[0] = cvt<double>(in[sidx(q, rhs, 0, nrhs)]);
+    h[1] = cvt<double>(in[sidx(q, rhs, 1, nrhs)]);
 }
 
 template <typename D, typename S>
@@ -53,7 +53,7 @@ __global__ void k_dot(const cx<T>* __restrict__ a, const cx<T>* __restrict__ b, 
         for (int q = blockIdx.x * blockDim.y + threadIdx.y; q < nsites; q += gridDim.x * blockDim.y) {
 #pragma unroll
             for (int sp = 0; sp < 2; ++sp) {
-                int64_t i = ((int64_t)q * 2 + sp) * nrhs + rhs;
+                int64_t i = sidx(q, rhs, sp, nrhs);
                 cx<T> p = cmulc(a[i], b[i]);
                 v[0] += (double)p.re;
                 v[1] += (double)p.im;
@@ -70,8 +70,8 @@ __global__ void k_norm2(const cx<T>* __restrict__ a, int nsites, int nrhs, doubl
     double v[1] = {0.0};
     if (rhs < nrhs) {
         for (int q = blockIdx.x * blockDim.y + threadIdx.y; q < nsites; q += gridDim.x * blockDim.y) {
-            int64_t i0 = ((int64_t)q * 2) * nrhs + rhs;
-            v[0] += (double)(norm2(a[i0]) + norm2(a[i0 + nrhs]));
+            int64_t i0 = sidx(q, rhs, 0, nrhs);
+            v[0] += (double)(norm2(a[i0]) + norm2(a[i0 + 1]));
         }
     }
     block_reduce_finalise<1>(v, partials, ticket, nrhs, FinStore{out, 1});
@@ -86,7 +86,7 @@ __global__ void k_axpy(const double* __restrict__ alpha, const cx<T>* __restrict
     cx<T> a = mk<T>((T)alpha[2 * rhs], (T)alpha[2 * rhs + 1]);
 #pragma unroll
     for (int sp = 0; sp < 2; ++sp) {
-        int64_t i = ((int64_t)q * 2 + sp) * nrhs + rhs;
+        int64_t i = sidx(q, rhs, sp, nrhs);
         y[i] = y[i] + a * x[i];
     }
 }
@@ -99,7 +99,7 @@ __global__ void k_scale(const double* __restrict__ alpha, cx<T>* __restrict__ v,
     cx<T> a = mk<T>((T)alpha[2 * rhs], (T)alpha[2 * rhs + 1]);
 #pragma unroll
     for (int sp = 0; sp < 2; ++sp) {
-        int64_t i = ((int64_t)q * 2 + sp) * nrhs + rhs;
+        int64_t i = sidx(q, rhs, sp, nrhs);
         v[i] = a * v[i];
     }
 }

@@ -1,0 +1,1376 @@
+// Aggregation multigrid for A = D^dag D on the device
+// (reference src/multigrid.cpp, src/prolongator.h, src/coarse_op.h).
+//
+// Level 0 is the fine lattice (dof = 2 spins, device fields).  Level l >= 1 is
+// a coarse lattice of nx_l x ny_l sites with Nc_l dofs per site whose operator
+// is a 9-point stencil of Nc_l x Nc_l blocks (SparseCoarseOp,
+// src/coarse_op.h:154-297).  The transfer from level l to l+1 aggregates
+// ax x ay sites; its block vectors are stored V[agg][loc][dof][i] with the
+// coarse dof i innermost, so prolongation reads one contiguous row per fine
+// dof and restriction reads coalesced across i.
+//
+// Setup follows build_mg_hierarchy (src/multigrid.cpp:595-687): inverse
+// iteration for the near-null vectors (:435-484, :545-587), block
+// Gram-Schmidt (src/prolongator.h:111-130), then the Galerkin operator.  The
+// level-0 Galerkin operator is formed directly: with W_{B,i} = D P_{B,i}
+// (supported on block B plus a one-site halo),
+//   A_c[B][d](i, j) = <P_{B,i}, D^dag D P_{B+d,j}> = sum_x conj(W_{B,i}(x)) W_{B+d,j}(x),
+// which replaces the reference's probing with one fine D^dag D application
+// per coarse dof (src/coarse_op.h:241-279).  Deeper Galerkin operators are
+// triple products of the stencil blocks with the block vectors.
+#include "smg_internal.h"
+#include "vec.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <random>
+#include <vector>
+
+smg_status smg_dslash(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, double* norm2_dev);
+smg_status smg_dslash_mr(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, const smg_field* w,
+                         double* out3_dev);
+
+namespace {
+
+__constant__ int c_dx[9] = {0, 1, -1, 0, 0, 1, 1, -1, -1};
+__constant__ int c_dy[9] = {0, 0, 0, 1, -1, 1, -1, 1, -1};
+
+__host__ __device__ __forceinline__ int dir_of(int dx, int dy) {
+    // inverse of (c_dx, c_dy): 0 self, 1 +x, 2 -x, 3 +y, 4 -y, 5 +x+y, 6 +x-y, 7 -x+y, 8 -x-y
+    if (dy == 0) return dx == 0 ? 0 : (dx > 0 ? 1 : 2);
+    if (dx == 0) return dy > 0 ? 3 : 4;
+    if (dx > 0) return dy > 0 ? 5 : 6;
+    return dy > 0 ? 7 : 8;
+}
+
+struct Level {
+    int nx = 0, ny = 0, nsites = 0, ndof = 2;
+    // transfer to level + 1
+    int ax = 0, ay = 0, nvec = 0, nc_next = 0, nagg_x = 0, nagg_y = 0;
+    cx<double>* V64 = nullptr;  // [agg][loc][dof][i]
+    cx<float>* V32 = nullptr;
+    // operator of this level (l >= 1): [site][dir][j][i] = block(i, j)
+    cx<double>* A64 = nullptr;
+    cx<float>* A32 = nullptr;
+    int64_t vsize() const { return (int64_t)nagg_x * nagg_y * ax * ay * ndof * nc_next; }
+    int64_t asize() const { return (int64_t)nsites * 9 * ndof * ndof; }
+};
+
+// ------------------------------------------------------------ level-0 kernels
+
+// V[B][loc][sp][i] from null vector k: i = c * nvec + k with chirality c = sp
+// (split) or i = k (no split)
+__global__ void k_extract0(const cx<double>* __restrict__ nv, int k, Geom g, int bx, int by, int nvec, int nc,
+                           int split, cx<double>* __restrict__ V) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;  // lexicographic fine site
+    if (s >= g.V) return;
+    int x = s % g.L, y = s / g.L;
+    int q = site_q(g, x, y);
+    int nbx = g.L / bx;
+    int B = (x / bx) + nbx * (y / by);
+    int loc = (x % bx) + bx * (y % by);
+    int m = bx * by;
+    for (int sp = 0; sp < 2; ++sp) {
+        cx<double> v = nv[sidx(q, 0, sp, 1)];
+        if (split) {
+            for (int c = 0; c < 2; ++c) {
+                int i = c * nvec + k;
+                V[(((int64_t)B * m + loc) * 2 + sp) * nc + i] = (c == sp) ? v : mk(0.0, 0.0);
+            }
+        } else {
+            V[(((int64_t)B * m + loc) * 2 + sp) * nc + k] = v;
+        }
+    }
+}
+
+// coarse level: V[B][loc][j][i] from a coarse null vector (dof = ndof, lexicographic sites)
+__global__ void k_extract_c(const cx<double>* __restrict__ nv, int k, int nx, int ny, int ndof, int ax, int ay,
+                            int nvec, int nc, int split, cx<double>* __restrict__ V) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nx * ny * ndof) return;
+    int s = (int)(t / ndof), j = (int)(t - (int64_t)s * ndof);
+    int x = s % nx, y = s / nx;
+    int B = (x / ax) + (nx / ax) * (y / ay);
+    int loc = (x % ax) + ax * (y % ay);
+    int m = ax * ay;
+    cx<double> v = nv[(int64_t)s * ndof + j];
+    if (split) {
+        int chi = j < ndof / 2 ? 0 : 1;  // coarse dofs are chirality-major
+        for (int c = 0; c < 2; ++c)
+            V[(((int64_t)B * m + loc) * ndof + j) * nc + c * nvec + k] = (c == chi) ? v : mk(0.0, 0.0);
+    } else {
+        V[(((int64_t)B * m + loc) * ndof + j) * nc + k] = v;
+    }
+}
+
+// Modified Gram-Schmidt of the nc block vectors of one aggregate
+// (orthonormalise_block, src/prolongator.h:111-130): vectors of length
+// len = (aggregate sites) * dof, element e at V[(B * len + e) * nc + i].
+__global__ void k_block_orth(cx<double>* __restrict__ V, int len, int nc) {
+    extern __shared__ cx<double> sv[];  // [len][nc]
+    __shared__ double red[2][32];
+    const int B = blockIdx.x;
+    cx<double>* Vb = V + (int64_t)B * len * nc;
+    for (int t = threadIdx.x; t < len * nc; t += blockDim.x) sv[t] = Vb[t];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = 0; i < nc; ++i) {
+        for (int j = 0; j < i; ++j) {
+            double pr = 0, pi = 0;
+            for (int e = threadIdx.x; e < len; e += blockDim.x) {
+                cx<double> c = cmulc(sv[e * nc + j], sv[e * nc + i]);
+                pr += c.re;
+                pi += c.im;
+            }
+            for (int o = 16; o; o >>= 1) {
+                pr += __shfl_xor_sync(0xffffffffu, pr, o);
+                pi += __shfl_xor_sync(0xffffffffu, pi, o);
+            }
+            if (lane == 0) {
+                red[0][warp] = pr;
+                red[1][warp] = pi;
+            }
+            __syncthreads();
+            double tr = 0, ti = 0;
+            for (int w = 0; w < nw; ++w) {
+                tr += red[0][w];
+                ti += red[1][w];
+            }
+            const cx<double> proj = mk(tr, ti);
+            for (int e = threadIdx.x; e < len; e += blockDim.x) sv[e * nc + i] = sv[e * nc + i] - proj * sv[e * nc + j];
+            __syncthreads();
+        }
+        double nn = 0;
+        for (int e = threadIdx.x; e < len; e += blockDim.x) nn += norm2(sv[e * nc + i]);
+        for (int o = 16; o; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
+        if (lane == 0) red[0][warp] = nn;
+        __syncthreads();
+        double tot = 0;
+        for (int w = 0; w < nw; ++w) tot += red[0][w];
+        tot = sqrt(tot);
+        if (tot > 1e-14)
+            for (int e = threadIdx.x; e < len; e += blockDim.x) sv[e * nc + i] = (1.0 / tot) * sv[e * nc + i];
+        __syncthreads();
+    }
+    for (int t = threadIdx.x; t < len * nc; t += blockDim.x) Vb[t] = sv[t];
+}
+
+// restriction, level 0: c[B][rhs][i] = sum_{loc,sp} conj(V[B][loc][sp][i]) f[q][rhs][sp]
+template <typename T>
+__global__ void k_restrict0(const cx<T>* __restrict__ V, const cx<T>* __restrict__ f, cx<T>* __restrict__ c, Geom g,
+                            int bx, int by, int nc, int nrhs) {
+    // one thread per (B, rhs, i); i fastest
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int nbx = g.L / bx, nby = g.L / by;
+    int64_t total = (int64_t)nbx * nby * nrhs * nc;
+    if (t >= total) return;
+    int i = (int)(t % nc);
+    int64_t br = t / nc;
+    int rhs = (int)(br % nrhs);
+    int B = (int)(br / nrhs);
+    int x0 = (B % nbx) * bx, y0 = (B / nbx) * by;
+    int m = bx * by;
+    cx<T> acc = mk<T>(0, 0);
+    for (int loc = 0; loc < m; ++loc) {
+        int x = x0 + loc % bx, y = y0 + loc / bx;
+        int q = site_q(g, x, y);
+        Spinor<T> fv = ld_spinor(f, q, rhs, nrhs);
+        const cx<T>* v = V + ((int64_t)B * m + loc) * 2 * nc;
+        acc = acc + cmulc(v[i], fv.s0) + cmulc(v[nc + i], fv.s1);
+    }
+    c[((int64_t)B * nrhs + rhs) * nc + i] = acc;
+}
+
+// prolongation, level 0: f[q][rhs][sp] (+)= sum_i V[B][loc][sp][i] c[B][rhs][i]
+template <typename T>
+__global__ void k_prolong0(const cx<T>* __restrict__ V, const cx<T>* __restrict__ c, cx<T>* __restrict__ f, Geom g,
+                           int bx, int by, int nc, int nrhs, int accumulate) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)g.V * nrhs) return;
+    int rhs = (int)(t % nrhs);
+    int q = (int)(t / nrhs);
+    int x, y, p;
+    site_coords(g, q, x, y, p);
+    int nbx = g.L / bx;
+    int B = (x / bx) + nbx * (y / by);
+    int loc = (x % bx) + bx * (y % by);
+    int m = bx * by;
+    const cx<T>* v = V + ((int64_t)B * m + loc) * 2 * nc;
+    const cx<T>* cc = c + ((int64_t)B * nrhs + rhs) * nc;
+    cx<T> f0 = mk<T>(0, 0), f1 = mk<T>(0, 0);
+    for (int i = 0; i < nc; ++i) {
+        cx<T> ci = cc[i];
+        f0 = f0 + ci * v[i];
+        f1 = f1 + ci * v[nc + i];
+    }
+    Spinor<T> out;
+    if (accumulate) {
+        out = ld_spinor(f, q, rhs, nrhs);
+        out.s0 = out.s0 + f0;
+        out.s1 = out.s1 + f1;
+    } else {
+        out.s0 = f0;
+        out.s1 = f1;
+    }
+    st_spinor(f, q, rhs, nrhs, out);
+}
+
+// coarse restriction: c'[B][rhs][i] = sum_{loc,j} conj(V[B][loc][j][i]) c[site][rhs][j]
+template <typename T>
+__global__ void k_restrict_c(const cx<T>* __restrict__ V, const cx<T>* __restrict__ c, cx<T>* __restrict__ cn, int nx,
+                             int ax, int ay, int ndof, int nc, int nagg, int nrhs) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nagg * nrhs * nc) return;
+    int i = (int)(t % nc);
+    int64_t br = t / nc;
+    int rhs = (int)(br % nrhs);
+    int B = (int)(br / nrhs);
+    int nax = nx / ax;
+    int x0 = (B % nax) * ax, y0 = (B / nax) * ay;
+    int m = ax * ay;
+    cx<T> acc = mk<T>(0, 0);
+    for (int loc = 0; loc < m; ++loc) {
+        int s = (x0 + loc % ax) + nx * (y0 + loc / ax);
+        const cx<T>* cv = c + ((int64_t)s * nrhs + rhs) * ndof;
+        const cx<T>* v = V + ((int64_t)B * m + loc) * ndof * nc;
+        for (int j = 0; j < ndof; ++j) acc = acc + cmulc(v[j * nc + i], cv[j]);
+    }
+    cn[((int64_t)B * nrhs + rhs) * nc + i] = acc;
+}
+
+// coarse prolongation: c[site][rhs][j] (+)= sum_i V[B][loc][j][i] c'[B][rhs][i]
+template <typename T>
+__global__ void k_prolong_c(const cx<T>* __restrict__ V, const cx<T>* __restrict__ cn, cx<T>* __restrict__ c, int nx,
+                            int ny, int ax, int ay, int ndof, int nc, int nrhs, int accumulate) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nx * ny * nrhs * ndof) return;
+    int j = (int)(t % ndof);
+    int64_t sr = t / ndof;
+    int rhs = (int)(sr % nrhs);
+    int s = (int)(sr / nrhs);
+    int x = s % nx, y = s / nx;
+    int B = (x / ax) + (nx / ax) * (y / ay);
+    int loc = (x % ax) + ax * (y % ay);
+    int m = ax * ay;
+    const cx<T>* v = V + (((int64_t)B * m + loc) * ndof + j) * nc;
+    const cx<T>* cc = cn + ((int64_t)B * nrhs + rhs) * nc;
+    cx<T> acc = mk<T>(0, 0);
+    for (int i = 0; i < nc; ++i) acc = acc + v[i] * cc[i];
+    int64_t o = ((int64_t)s * nrhs + rhs) * ndof + j;
+    c[o] = accumulate ? c[o] + acc : acc;
+}
+
+// W[B][i][h][sp] = (D P_{B,i})(h) on the (bx+2) x (by+2) halo frame of block B
+__global__ void k_W0(const cx<double>* __restrict__ V, const cx<double>* __restrict__ U, const double* __restrict__ C,
+                     Geom g, int bx, int by, int nc, double diag, double mu, double r, cx<double>* __restrict__ W) {
+    const int B = blockIdx.x;
+    const int hx_n = bx + 2, hy_n = by + 2, nh = hx_n * hy_n;
+    const int nbx = g.L / bx;
+    const int x0 = (B % nbx) * bx, y0 = (B / nbx) * by;
+    const int m = bx * by;
+    for (int t = threadIdx.x; t < nh * nc; t += blockDim.x) {
+        const int i = t % nc, h = t / nc;
+        const int hx = h % hx_n, hy = h / hx_n;
+        const int x = wrap(x0 - 1 + hx, g.L), y = wrap(y0 - 1 + hy, g.L);
+        // P_{B,i} at block-frame coordinates (lx, ly); zero outside the block
+        auto Pv = [&](int lx, int ly, int sp) -> cx<double> {
+            if (lx < 0 || lx >= bx || ly < 0 || ly >= by) return mk(0.0, 0.0);
+            return V[(((int64_t)B * m + lx + bx * ly) * 2 + sp) * nc + i];
+        };
+        const int lx = hx - 1, ly = hy - 1;
+        const int q = site_q(g, x, y);
+        const int q_xm = site_q(g, wrap(x - 1, g.L), y);
+        const int q_ym = site_q(g, x, wrap(y - 1, g.L));
+        const cx<double> u0f = U[q], u0b = U[q_xm], u1f = U[(int64_t)g.V + q], u1b = U[(int64_t)g.V + q_ym];
+        const cx<double> a0x = u0f * Pv(lx + 1, ly, 0), a1x = u0f * Pv(lx + 1, ly, 1);
+        const cx<double> b0x = cmulc(u0b, Pv(lx - 1, ly, 0)), b1x = cmulc(u0b, Pv(lx - 1, ly, 1));
+        const cx<double> a0y = u1f * Pv(lx, ly + 1, 0), a1y = u1f * Pv(lx, ly + 1, 1);
+        const cx<double> b0y = cmulc(u1b, Pv(lx, ly - 1, 0)), b1y = cmulc(u1b, Pv(lx, ly - 1, 1));
+        const double Cq = C ? C[q] : 0.0;
+        const cx<double> dg0 = mk(diag + Cq, mu), dg1 = mk(diag - Cq, -mu);
+        const cx<double> sr0 = (a0x + b0x) + (a0y + b0y);
+        const cx<double> sr1 = (a1x + b1x) + (a1y + b1y);
+        const cx<double> off0 = (b1x - a1x) + times_i(a1y - b1y);
+        const cx<double> off1 = (b0x - a0x) - times_i(a0y - b0y);
+        const cx<double> w0 = dg0 * Pv(lx, ly, 0) - 0.5 * (r * sr0 + off0);
+        const cx<double> w1 = dg1 * Pv(lx, ly, 1) - 0.5 * (r * sr1 + off1);
+        cx<double>* o = W + (((int64_t)B * nc + i) * nh + h) * 2;
+        o[0] = w0;
+        o[1] = w1;
+    }
+}
+
+// A[B][d][j][i] = sum_{x in halo(B) and halo(B+d)} conj(W_{B,i}(x)) W_{B+d,j}(x)
+__global__ void k_galerkin0(const cx<double>* __restrict__ W, int nbx, int nby, int bx, int by, int nc,
+                            cx<double>* __restrict__ A) {
+    const int B = blockIdx.x, d = blockIdx.y;
+    const int hx_n = bx + 2, hy_n = by + 2, nh = hx_n * hy_n;
+    const int dx = c_dx[d], dy = c_dy[d];
+    const int Bx = B % nbx, By = B / nbx;
+    const int B2 = ((Bx + dx + nbx) % nbx) + nbx * ((By + dy + nby) % nby);
+    const int hx_lo = dx > 0 ? bx : 0, hx_hi = dx < 0 ? 2 : hx_n;
+    const int hy_lo = dy > 0 ? by : 0, hy_hi = dy < 0 ? 2 : hy_n;
+    for (int t = threadIdx.x; t < nc * nc; t += blockDim.x) {
+        const int i = t % nc, j = t / nc;
+        const cx<double>* w1 = W + ((int64_t)B * nc + i) * nh * 2;
+        const cx<double>* w2 = W + ((int64_t)B2 * nc + j) * nh * 2;
+        cx<double> acc = mk(0.0, 0.0);
+        for (int hy = hy_lo; hy < hy_hi; ++hy)
+            for (int hx = hx_lo; hx < hx_hi; ++hx) {
+                const int h1 = hx + hx_n * hy;
+                const int h2 = (hx - dx * bx) + hx_n * (hy - dy * by);
+                acc = acc + cmulc(w1[2 * h1], w2[2 * h2]) + cmulc(w1[2 * h1 + 1], w2[2 * h2 + 1]);
+            }
+        A[(((int64_t)B * 9 + d) * nc + j) * nc + i] = acc;
+    }
+}
+
+// Galerkin of a coarse level: A'[B][d'](i', j') = sum_{loc, d} V_B(loc)^dag L[b][d] V_{B2}(loc2)
+__global__ void k_galerkin_c(const cx<double>* __restrict__ Lk, const cx<double>* __restrict__ V, int nx, int ny, int ax,
+                             int ay, int ndof, int nc, cx<double>* __restrict__ A) {
+    extern __shared__ cx<double> sT[];  // [ndof][nc]
+    const int B = blockIdx.x;
+    const int nax = nx / ax, nay = ny / ay;
+    const int Bx = B % nax, By = B / nax;
+    const int m = ax * ay;
+    // each thread owns (i', j') pairs; accumulators for 9 directions
+    const int npair = nc * nc;
+    constexpr int kMaxPairs = 4;  // pairs per thread (blockDim * 4 >= nc * nc)
+    cx<double> acc[kMaxPairs][9];
+    for (int a = 0; a < kMaxPairs; ++a)
+        for (int d = 0; d < 9; ++d) acc[a][d] = mk(0.0, 0.0);
+    for (int loc = 0; loc < m; ++loc) {
+        const int x = Bx * ax + loc % ax, y = By * ay + loc / ax;
+        const int s = x + nx * y;
+        for (int d = 0; d < 9; ++d) {
+            const int x2 = (x + c_dx[d] + nx) % nx, y2 = (y + c_dy[d] + ny) % ny;
+            const int B2x = x2 / ax, B2y = y2 / ay;
+            int ddx = B2x - Bx, ddy = B2y - By;
+            if (ddx > 1) ddx -= nax;
+            if (ddx < -1) ddx += nax;
+            if (ddy > 1) ddy -= nay;
+            if (ddy < -1) ddy += nay;
+            const int dp = dir_of(ddx, ddy);
+            const int B2 = B2x + nax * B2y;
+            const int loc2 = (x2 % ax) + ax * (y2 % ay);
+            // T(k, j') = sum_j L[s][d](k, j) V_{B2}[loc2][j][j']
+            const cx<double>* Lsd = Lk + ((int64_t)s * 9 + d) * ndof * ndof;  // [j][k]
+            const cx<double>* V2 = V + ((int64_t)B2 * m + loc2) * ndof * nc;  // [j][j']
+            __syncthreads();
+            for (int t = threadIdx.x; t < ndof * nc; t += blockDim.x) {
+                const int k = t / nc, jp = t % nc;
+                cx<double> sum = mk(0.0, 0.0);
+                for (int j = 0; j < ndof; ++j) sum = sum + Lsd[j * ndof + k] * V2[j * nc + jp];
+                sT[k * nc + jp] = sum;
+            }
+            __syncthreads();
+            const cx<double>* V1 = V + ((int64_t)B * m + loc) * ndof * nc;  // [k][i']
+            for (int a = 0; a < kMaxPairs; ++a) {
+                const int t = threadIdx.x + a * blockDim.x;
+                if (t >= npair) break;
+                const int ip = t % nc, jp = t / nc;
+                cx<double> sum = mk(0.0, 0.0);
+                for (int k = 0; k < ndof; ++k) sum = sum + cmulc(V1[k * nc + ip], sT[k * nc + jp]);
+                for (int dd = 0; dd < 9; ++dd)
+                    if (dd == dp) acc[a][dd] = acc[a][dd] + sum;
+            }
+        }
+    }
+    for (int a = 0; a < kMaxPairs; ++a) {
+        const int t = threadIdx.x + a * blockDim.x;
+        if (t >= npair) break;
+        const int ip = t % nc, jp = t / nc;
+        for (int d = 0; d < 9; ++d) A[(((int64_t)B * 9 + d) * nc + jp) * nc + ip] = acc[a][d];
+    }
+}
+
+// y[s][rhs][i] = sum_d sum_j A[s][d][j][i] x[nb(s,d)][rhs][j]; optional fused
+// reductions <y, w> and ||y||^2 per rhs.  Threads: x = rhs lane, y = (site, i).
+template <typename T, int EPI>
+__global__ void __launch_bounds__(256) k_coarse_apply(const cx<T>* __restrict__ A, VecView<T> xin, cx<T>* __restrict__ y,
+                                                      int nx, int ny, const cx<T>* __restrict__ w, double* partials,
+                                                      unsigned int* ticket, double* out) {
+    constexpr int K = EPI == 2 ? 3 : 1;
+    const int nc = xin.ndof, nrhs = xin.nrhs;
+    const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
+    double v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = 0.0;
+    const int64_t nrow = (int64_t)xin.nsites * nc;
+    if (rhs < nrhs) {
+        for (int64_t row = (int64_t)blockIdx.x * blockDim.y + threadIdx.y; row < nrow;
+             row += (int64_t)gridDim.x * blockDim.y) {
+            const int s = (int)(row / nc), i = (int)(row - (int64_t)s * nc);
+            const int x = s % nx, yy = s / nx;
+            cx<T> acc = mk<T>(0, 0);
+#pragma unroll 1
+            for (int d = 0; d < 9; ++d) {
+                const int xn = x + c_dx[d], yn = yy + c_dy[d];
+                const int sn = (xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn)) +
+                               nx * (yn < 0 ? yn + ny : (yn >= ny ? yn - ny : yn));
+                const cx<T>* Ad = A + ((int64_t)s * 9 + d) * nc * nc + i;
+                const cx<T>* xv = xin.p + ((int64_t)sn * nrhs + rhs) * nc;
+                for (int j = 0; j < nc; ++j) acc = acc + Ad[(int64_t)j * nc] * xv[j];
+            }
+            const int64_t o = ((int64_t)s * nrhs + rhs) * nc + i;
+            y[o] = acc;
+            if (EPI == 1) {
+                v[0] += (double)norm2(acc);
+            } else if (EPI == 2) {
+                const cx<T> c = cmulc(acc, w[o]);
+                v[0] += (double)c.re;
+                v[1] += (double)c.im;
+                v[2] += (double)norm2(acc);
+            }
+        }
+    }
+    if (EPI != 0) block_reduce_finalise<K>(v, partials, ticket, nrhs, FinStore{out, K});
+}
+
+template <typename D, typename S>
+__global__ void k_cvt_flat(const cx<S>* __restrict__ in, cx<D>* __restrict__ out, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = cvt<D>(in[i]);
+}
+
+// coarsest-level CG scalars per rhs: rr, pAp (re, im, norm from the fused
+// epilogue), bnorm2, active, and the update kernel's finaliser
+struct CcgState {
+    double* rr;
+    double* pap3;  // [rhs][3]: <Ap, p> re, im, ||Ap||^2
+    double* bnorm2;
+    double* beta;
+    int* active;
+    int* n_active;
+    double tol2;
+};
+
+__global__ void k_ccg_init(CcgState s, int nrhs) {
+    if (threadIdx.x == 0) *s.n_active = 0;
+    __syncthreads();
+    for (int j = threadIdx.x; j < nrhs; j += blockDim.x) {
+        s.bnorm2[j] = s.rr[j];
+        s.beta[j] = 0.0;
+        int act = (s.rr[j] >= 1e-60 && isfinite(s.rr[j])) ? 1 : 0;
+        s.active[j] = act;
+        if (act) atomicAdd(s.n_active, 1);
+    }
+}
+
+struct FinCcg {
+    CcgState s;
+    __device__ void operator()(int j, const double* sums) const {
+        double rr_new = sums[0];
+        if (!s.active[j]) {
+            s.beta[j] = 0.0;
+            return;
+        }
+        if (!isfinite(rr_new) || rr_new < s.tol2 * s.bnorm2[j]) {
+            s.active[j] = 0;
+            atomicSub(s.n_active, 1);
+            s.beta[j] = 0.0;
+            return;
+        }
+        s.beta[j] = rr_new / s.rr[j];
+        s.rr[j] = rr_new;
+    }
+};
+
+// x += alpha p, r -= alpha Ap with alpha = rr / <p, Ap>; ||r||^2 -> finaliser
+template <typename T>
+__global__ void __launch_bounds__(256) k_ccg_update(CcgState s, VecView<T> x, cx<T>* __restrict__ r,
+                                                    const cx<T>* __restrict__ p, const cx<T>* __restrict__ Ap,
+                                                    double* partials, unsigned int* ticket) {
+    __shared__ T s_al[32];
+    const int nrhs = x.nrhs;
+    const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
+    if (threadIdx.y == 0) {
+        T al = 0;
+        if (rhs < nrhs && s.active[rhs]) {
+            // <p, Ap> = conj(<Ap, p>) is real for Hermitian positive A
+            double pap = s.pap3[3 * rhs];
+            if (fabs(pap) >= 1e-30 && isfinite(pap)) al = (T)(s.rr[rhs] / pap);
+        }
+        s_al[threadIdx.x] = al;
+    }
+    __syncthreads();
+    const T al = s_al[threadIdx.x];
+    double v[1] = {0.0};
+    if (rhs < nrhs) {
+        for (int st = blockIdx.x * blockDim.y + threadIdx.y; st < x.nsites; st += gridDim.x * blockDim.y) {
+            const int64_t base = x.idx(st, rhs, 0);
+            for (int d = 0; d < x.ndof; ++d) {
+                const cx<T> ri = r[base + d] - al * Ap[base + d];
+                x.p[base + d] = x.p[base + d] + al * p[base + d];
+                r[base + d] = ri;
+                v[0] += (double)norm2(ri);
+            }
+        }
+    }
+    block_reduce_finalise<1>(v, partials, ticket, nrhs, FinCcg{s});
+}
+
+template <typename T>
+__global__ void k_ccg_p(CcgState s, VecView<T> p, const cx<T>* __restrict__ r) {
+    const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
+    const int st = blockIdx.x * blockDim.y + threadIdx.y;
+    if (rhs >= p.nrhs || st >= p.nsites) return;
+    const T be = (T)s.beta[rhs];
+    const int64_t base = p.idx(st, rhs, 0);
+    for (int d = 0; d < p.ndof; ++d) p.p[base + d] = r[base + d] + be * p.p[base + d];
+}
+
+}  // namespace
+
+// ====================================================================== host
+
+struct CoarseWork {  // per level l >= 1, per precision
+    void* b = nullptr;
+    void* x = nullptr;
+    void* r = nullptr;
+    void* Ar = nullptr;
+    void* e = nullptr;
+    void* p = nullptr;
+};
+
+struct smg_mg {
+    smg_context* ctx = nullptr;
+    smg_dirac* dirac = nullptr;
+    smg_mg_params p{};
+    std::vector<Level> lv;
+    std::vector<smg_field*> null0;  // level-0 null vectors, single-RHS F64 fields
+    // workspace, rebuilt when nrhs or precision changes
+    int work_nrhs = 0;
+    smg_precision work_prec = SMG_F64;
+    smg_field *f_r = nullptr, *f_Ar = nullptr, *f_t = nullptr;  // fine MR temps
+    std::vector<CoarseWork> cw;
+    double* scal = nullptr;  // per-level scalar area
+    size_t scal_doubles = 0;
+};
+
+namespace {
+
+template <typename T>
+const cx<T>* Vp(const Level& L);
+template <>
+const cx<double>* Vp<double>(const Level& L) { return L.V64; }
+template <>
+const cx<float>* Vp<float>(const Level& L) { return L.V32; }
+template <typename T>
+const cx<T>* Ap(const Level& L);
+template <>
+const cx<double>* Ap<double>(const Level& L) { return L.A64; }
+template <>
+const cx<float>* Ap<float>(const Level& L) { return L.A32; }
+
+int blocks_for(int64_t n, int t = 256) { return (int)((n + t - 1) / t); }
+
+// --- fine-level helpers on smg_field
+template <typename T>
+VecView<T> fview(const smg_field* f) {
+    VecView<T> v;
+    v.p = (cx<T>*)f->data;
+    v.nsites = f->g.V;
+    v.nrhs = f->nrhs;
+    v.ndof = 2;
+    return v;
+}
+
+template <typename T>
+VecView<T> cview(void* p, const Level& L, int nrhs) {
+    VecView<T> v;
+    v.p = (cx<T>*)p;
+    v.nsites = L.nsites;
+    v.nrhs = nrhs;
+    v.ndof = L.ndof;
+    return v;
+}
+
+template <typename T>
+smg_status vreduce(smg_context* ctx, VecView<T> a, const cx<T>* b, int mode, double* out) {
+    ReduceLaunch rl = reduce_launch(a.nsites, a.nrhs);
+    SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * a.nrhs * 3));
+    if (mode == VR_DOT)
+        k_vreduce<T, VR_DOT><<<rl.grid, rl.block, 0, ctx->stream>>>(a, b, ctx->red.partials, ctx->red.tickets, out);
+    else if (mode == VR_NORM)
+        k_vreduce<T, VR_NORM><<<rl.grid, rl.block, 0, ctx->stream>>>(a, b, ctx->red.partials, ctx->red.tickets, out);
+    else
+        k_vreduce<T, VR_DOTNORM><<<rl.grid, rl.block, 0, ctx->stream>>>(a, b, ctx->red.partials, ctx->red.tickets, out);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+template <typename T>
+smg_status vaxpy(smg_context* ctx, VecView<T> y, const cx<T>* x, const double* coef, double sgn) {
+    k_vaxpy<T><<<vec_grid(y.nsites, y.nrhs), vec_block(y.nrhs), 0, ctx->stream>>>(y, x, coef, sgn);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+template <typename T>
+smg_status coarse_apply(smg_mg* mg, int l, VecView<T> x, cx<T>* y, int epi, const cx<T>* w, double* out) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[l];
+    ReduceLaunch rl = reduce_launch((int)((int64_t)L.nsites * L.ndof), x.nrhs);
+    // cap rows so a block holds whole sites
+    SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * x.nrhs * 3));
+    if (epi == 0) {
+        k_coarse_apply<T, 0><<<rl.grid, rl.block, 0, ctx->stream>>>(Ap<T>(L), x, y, L.nx, L.ny, w, nullptr, nullptr,
+                                                                  nullptr);
+    } else if (epi == 1) {
+        k_coarse_apply<T, 1><<<rl.grid, rl.block, 0, ctx->stream>>>(Ap<T>(L), x, y, L.nx, L.ny, w, ctx->red.partials,
+                                                                  ctx->red.tickets, out);
+    } else {
+        k_coarse_apply<T, 2><<<rl.grid, rl.block, 0, ctx->stream>>>(Ap<T>(L), x, y, L.nx, L.ny, w, ctx->red.partials,
+                                                                  ctx->red.tickets, out);
+    }
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+// A_l x -> y for any level; level 0 is D^dag D via the fine temp field
+template <typename T>
+smg_status level_apply_fine(smg_mg* mg, smg_field* x, smg_field* y, const smg_field* w, double* out3) {
+    SMG_TRY(smg_dslash(mg->dirac, false, x, mg->f_t, nullptr));
+    if (w) return smg_dslash_mr(mg->dirac, true, mg->f_t, y, w, out3);
+    return smg_dslash(mg->dirac, true, mg->f_t, y, nullptr);
+}
+
+// scalar area layout: per level 16 * nrhs doubles (MR: 3, CG: rr, pap3, bnorm2, beta, ints)
+double* lvl_scal(smg_mg* mg, int l) { return mg->scal + (size_t)l * 16 * mg->work_nrhs + 64; }
+
+smg_status free_work(smg_mg* mg) {
+    smg_field_destroy(mg->f_r);
+    smg_field_destroy(mg->f_Ar);
+    smg_field_destroy(mg->f_t);
+    mg->f_r = mg->f_Ar = mg->f_t = nullptr;
+    for (auto& w : mg->cw) {
+        for (void* p : {w.b, w.x, w.r, w.Ar, w.e, w.p})
+            if (p) cudaFree(p);
+    }
+    mg->cw.clear();
+    if (mg->scal) cudaFree(mg->scal);
+    mg->scal = nullptr;
+    mg->work_nrhs = 0;
+    return SMG_OK;
+}
+
+smg_status ensure_work(smg_mg* mg, int nrhs, smg_precision prec) {
+    if (mg->work_nrhs == nrhs && mg->work_prec == prec && mg->f_t) return SMG_OK;
+    smg_context* ctx = mg->ctx;
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    free_work(mg);
+    const int L = mg->lv[0].nx;
+    SMG_TRY(smg_field_create(ctx, L, nrhs, prec, &mg->f_r));
+    SMG_TRY(smg_field_create(ctx, L, nrhs, prec, &mg->f_Ar));
+    SMG_TRY(smg_field_create(ctx, L, nrhs, prec, &mg->f_t));
+    size_t es = prec == SMG_F64 ? sizeof(cx<double>) : sizeof(cx<float>);
+    mg->cw.resize(mg->lv.size());
+    for (size_t l = 1; l < mg->lv.size(); ++l) {
+        size_t bytes = (size_t)mg->lv[l].nsites * nrhs * mg->lv[l].ndof * es;
+        CoarseWork& w = mg->cw[l];
+        for (void** p : {&w.b, &w.x, &w.r, &w.Ar, &w.e, &w.p}) {
+            SMG_CUDA(ctx, cudaMalloc(p, bytes));
+            SMG_CUDA(ctx, cudaMemsetAsync(*p, 0, bytes, ctx->stream));
+        }
+    }
+    mg->scal_doubles = (size_t)mg->lv.size() * 16 * nrhs + 128;
+    SMG_CUDA(ctx, cudaMalloc(&mg->scal, mg->scal_doubles * sizeof(double)));
+    SMG_CUDA(ctx, cudaMemsetAsync(mg->scal, 0, mg->scal_doubles * sizeof(double), ctx->stream));
+    mg->work_nrhs = nrhs;
+    mg->work_prec = prec;
+    return SMG_OK;
+}
+
+// ------------------------------------------------------------ MR smoothers
+
+// Fine MR on D^dag D (reference mr_smooth_op, src/smoother.cpp:26-40): on
+// entry x holds the initial guess; x_is_zero skips r = b - A x.  The residual
+// is updated recursively, r -= omega A r.
+template <typename T>
+smg_status mr_fine(smg_mg* mg, smg_field* x, const smg_field* b, int niter, bool x_is_zero) {
+    smg_context* ctx = mg->ctx;
+    smg_field *r = mg->f_r, *Ar = mg->f_Ar;
+    const int64_t n = b->n_complex();
+    if (x_is_zero) {
+        SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
+        SMG_CUDA(ctx, cudaMemcpyAsync(r->data, b->data, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    } else {
+        SMG_TRY(level_apply_fine<T>(mg, x, Ar, nullptr, nullptr));
+        k_vsub<T><<<blocks_for(n), 256, 0, ctx->stream>>>((cx<T>*)r->data, (const cx<T>*)b->data,
+                                                        (const cx<T>*)Ar->data, n);
+        count_launch(ctx);
+    }
+    double* sc = lvl_scal(mg, 0);
+    for (int it = 0; it < niter; ++it) {
+        SMG_TRY(level_apply_fine<T>(mg, r, Ar, r, sc));
+        VecView<T> xv = fview<T>(x);
+        k_mr_update<T><<<vec_grid(xv.nsites, xv.nrhs), vec_block(xv.nrhs), 0, ctx->stream>>>(
+            xv, (cx<T>*)r->data, (const cx<T>*)Ar->data, sc);
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+    }
+    return SMG_OK;
+}
+
+// Coarse MR on the level-l stencil operator; b, x, r, Ar from the level's work
+template <typename T>
+smg_status mr_coarse(smg_mg* mg, int l, void* x, const void* b, int niter, bool x_is_zero) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[l];
+    CoarseWork& w = mg->cw[l];
+    const int nrhs = mg->work_nrhs;
+    VecView<T> xv = cview<T>(x, L, nrhs), rv = cview<T>(w.r, L, nrhs);
+    const int64_t n = xv.n();
+    const size_t bytes = (size_t)n * sizeof(cx<T>);
+    if (x_is_zero) {
+        SMG_CUDA(ctx, cudaMemsetAsync(x, 0, bytes, ctx->stream));
+        SMG_CUDA(ctx, cudaMemcpyAsync(w.r, b, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    } else {
+        SMG_TRY(coarse_apply<T>(mg, l, xv, (cx<T>*)w.Ar, 0, nullptr, nullptr));
+        k_vsub<T><<<blocks_for(n), 256, 0, ctx->stream>>>((cx<T>*)w.r, (const cx<T>*)b, (const cx<T>*)w.Ar, n);
+        count_launch(ctx);
+    }
+    double* sc = lvl_scal(mg, l);
+    for (int it = 0; it < niter; ++it) {
+        SMG_TRY(coarse_apply<T>(mg, l, rv, (cx<T>*)w.Ar, 2, (const cx<T>*)w.r, sc));
+        k_mr_update<T><<<vec_grid(xv.nsites, xv.nrhs), vec_block(xv.nrhs), 0, ctx->stream>>>(
+            xv, (cx<T>*)w.r, (const cx<T>*)w.Ar, sc);
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+    }
+    return SMG_OK;
+}
+
+// Coarsest solve: CG from x = 0 to coarse_tol (SparseCoarseOp::solve without
+// deflation, src/coarse_op.h:492-547); the host checks progress every 8 steps
+template <typename T>
+smg_status coarse_cg(smg_mg* mg, int l, void* x, const void* b) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[l];
+    CoarseWork& w = mg->cw[l];
+    const int nrhs = mg->work_nrhs;
+    VecView<T> xv = cview<T>(x, L, nrhs), pv = cview<T>(w.p, L, nrhs), rv = cview<T>(w.r, L, nrhs);
+    const size_t bytes = (size_t)xv.n() * sizeof(cx<T>);
+    double* sc = lvl_scal(mg, l);
+    CcgState s;
+    s.rr = sc;
+    s.pap3 = sc + nrhs;
+    s.bnorm2 = sc + 4 * nrhs;
+    s.beta = sc + 5 * nrhs;
+    s.active = (int*)(sc + 6 * nrhs);
+    s.n_active = (int*)(sc + 7 * nrhs);
+    s.tol2 = mg->p.coarse_tol * mg->p.coarse_tol;
+    SMG_CUDA(ctx, cudaMemsetAsync(x, 0, bytes, ctx->stream));
+    SMG_CUDA(ctx, cudaMemcpyAsync(w.r, b, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    SMG_CUDA(ctx, cudaMemcpyAsync(w.p, b, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    SMG_TRY(vreduce<T>(ctx, rv, nullptr, VR_NORM, s.rr));
+    k_ccg_init<<<1, 256, 0, ctx->stream>>>(s, nrhs);
+    count_launch(ctx);
+    ReduceLaunch rl = reduce_launch(L.nsites, nrhs);
+    SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * nrhs * 3));
+    SMG_TRY(smg_host_stage_reserve(ctx, 64));
+    int* h_act = (int*)ctx->host_stage;
+    int it = 0;
+    while (it < mg->p.coarse_max_iter) {
+        int chunk = std::min(8, mg->p.coarse_max_iter - it);
+        for (int c = 0; c < chunk; ++c) {
+            SMG_TRY(coarse_apply<T>(mg, l, pv, (cx<T>*)w.Ar, 2, (const cx<T>*)w.p, s.pap3));
+            k_ccg_update<T><<<rl.grid, rl.block, 0, ctx->stream>>>(s, xv, (cx<T>*)w.r, (const cx<T>*)w.p,
+                                                                   (const cx<T>*)w.Ar, ctx->red.partials,
+                                                                   ctx->red.tickets);
+            k_ccg_p<T><<<vec_grid(L.nsites, nrhs), vec_block(nrhs), 0, ctx->stream>>>(s, pv, (const cx<T>*)w.r);
+            count_launch(ctx, 2);
+            SMG_CHECK_LAUNCH(ctx);
+        }
+        it += chunk;
+        SMG_CUDA(ctx, cudaMemcpyAsync(h_act, s.n_active, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (*h_act == 0) break;
+    }
+    return SMG_OK;
+}
+
+template <typename T>
+smg_status restrict_to(smg_mg* mg, int l, const void* fine_or_coarse, void* out) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[l];
+    const Level& N = mg->lv[l + 1];
+    const int nrhs = mg->work_nrhs;
+    int64_t total = (int64_t)N.nsites * nrhs * L.nc_next;
+    if (l == 0) {
+        k_restrict0<T><<<blocks_for(total), 256, 0, ctx->stream>>>(Vp<T>(L), (const cx<T>*)fine_or_coarse, (cx<T>*)out,
+                                                                  mg->null0.empty() ? Geom{} : mg->null0[0]->g, L.ax,
+                                                                  L.ay, L.nc_next, nrhs);
+    } else {
+        k_restrict_c<T><<<blocks_for(total), 256, 0, ctx->stream>>>(Vp<T>(L), (const cx<T>*)fine_or_coarse,
+                                                                   (cx<T>*)out, L.nx, L.ax, L.ay, L.ndof, L.nc_next,
+                                                                   N.nsites, nrhs);
+    }
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+template <typename T>
+smg_status prolong_to(smg_mg* mg, int l, const void* coarse, void* out, int accumulate) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[l];
+    const int nrhs = mg->work_nrhs;
+    if (l == 0) {
+        const Geom g = mg->null0[0]->g;
+        k_prolong0<T><<<blocks_for((int64_t)g.V * nrhs), 256, 0, ctx->stream>>>(
+            Vp<T>(L), (const cx<T>*)coarse, (cx<T>*)out, g, L.ax, L.ay, L.nc_next, nrhs, accumulate);
+    } else {
+        int64_t total = (int64_t)L.nsites * nrhs * L.ndof;
+        k_prolong_c<T><<<blocks_for(total), 256, 0, ctx->stream>>>(Vp<T>(L), (const cx<T>*)coarse, (cx<T>*)out, L.nx,
+                                                                  L.ny, L.ax, L.ay, L.ndof, L.nc_next, nrhs,
+                                                                  accumulate);
+    }
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+// mg_cycle (reference src/multigrid.cpp:43-102) at a coarse level l >= 1:
+// b = cw[l].b, result in x
+template <typename T>
+smg_status cycle_coarse(smg_mg* mg, int l, void* x, const void* b) {
+    const int last = (int)mg->lv.size() - 1;
+    if (l == last) return coarse_cg<T>(mg, l, x, b);
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[l];
+    const int nrhs = mg->work_nrhs;
+    SMG_TRY(mr_coarse<T>(mg, l, x, b, mg->p.pre_smooth, true));
+    // residual of the smoothed x is in cw[l].r
+    CoarseWork& nw = mg->cw[l + 1];
+    SMG_TRY(restrict_to<T>(mg, l, mg->cw[l].r, nw.b));
+    SMG_TRY(cycle_coarse<T>(mg, l + 1, nw.x, nw.b));
+    if (mg->p.w_cycle && l + 1 < last) {
+        const Level& N = mg->lv[l + 1];
+        const int64_t nn = (int64_t)N.nsites * nrhs * N.ndof;
+        const size_t nb = (size_t)nn * sizeof(cx<T>);
+        SMG_CUDA(ctx, cudaMemcpyAsync(nw.e, nw.x, nb, cudaMemcpyDeviceToDevice, ctx->stream));
+        SMG_TRY(coarse_apply<T>(mg, l + 1, cview<T>(nw.e, N, nrhs), (cx<T>*)nw.Ar, 0, nullptr, nullptr));
+        k_vsub<T><<<blocks_for(nn), 256, 0, ctx->stream>>>((cx<T>*)nw.b, (const cx<T>*)nw.b, (const cx<T>*)nw.Ar, nn);
+        count_launch(ctx);
+        SMG_TRY(cycle_coarse<T>(mg, l + 1, nw.x, nw.b));
+        k_vadd<T><<<blocks_for(nn), 256, 0, ctx->stream>>>((cx<T>*)nw.x, (const cx<T>*)nw.e, nn);
+        count_launch(ctx);
+    }
+    SMG_TRY(prolong_to<T>(mg, l, nw.x, x, 1));
+    (void)L;
+    return mr_coarse<T>(mg, l, x, b, mg->p.post_smooth, false);
+}
+
+// mg_cycle at the fine level: x = M^-1 b for fine fields of precision T
+template <typename T>
+smg_status cycle_fine(smg_mg* mg, smg_field* x, const smg_field* b) {
+    smg_context* ctx = mg->ctx;
+    const int last = (int)mg->lv.size() - 1;
+    SMG_TRY(mr_fine<T>(mg, x, b, mg->p.pre_smooth, true));
+    CoarseWork& nw = mg->cw[1];
+    SMG_TRY(restrict_to<T>(mg, 0, mg->f_r->data, nw.b));
+    SMG_TRY(cycle_coarse<T>(mg, 1, nw.x, nw.b));
+    if (mg->p.w_cycle && 1 < last) {
+        const Level& N = mg->lv[1];
+        const int nrhs = mg->work_nrhs;
+        const int64_t nn = (int64_t)N.nsites * nrhs * N.ndof;
+        SMG_CUDA(ctx, cudaMemcpyAsync(nw.e, nw.x, (size_t)nn * sizeof(cx<T>), cudaMemcpyDeviceToDevice, ctx->stream));
+        SMG_TRY(coarse_apply<T>(mg, 1, cview<T>(nw.e, N, nrhs), (cx<T>*)nw.Ar, 0, nullptr, nullptr));
+        k_vsub<T><<<blocks_for(nn), 256, 0, ctx->stream>>>((cx<T>*)nw.b, (const cx<T>*)nw.b, (const cx<T>*)nw.Ar, nn);
+        count_launch(ctx);
+        SMG_TRY(cycle_coarse<T>(mg, 1, nw.x, nw.b));
+        k_vadd<T><<<blocks_for(nn), 256, 0, ctx->stream>>>((cx<T>*)nw.x, (const cx<T>*)nw.e, nn);
+        count_launch(ctx);
+    }
+    SMG_TRY(prolong_to<T>(mg, 0, nw.x, x->data, 1));
+    return mr_fine<T>(mg, x, b, mg->p.post_smooth, false);
+}
+
+// ------------------------------------------------------------ setup
+
+// inverse iteration for one level's near-null vectors (multigrid.cpp:435-484
+// at level 0, :545-587 at coarse levels); vecs hold the start vectors on entry
+smg_status null_space_fine(smg_mg* mg, std::vector<smg_field*>& vecs) {
+    smg_context* ctx = mg->ctx;
+    const int k = (int)vecs.size();
+    SMG_TRY(ensure_work(mg, 1, SMG_F64));
+    smg_field* xn = nullptr;
+    SMG_TRY(smg_field_create(ctx, vecs[0]->g.L, 1, SMG_F64, &xn));
+    double* sc = mg->scal;  // [0..1] norm, [2..3] dot
+    SMG_TRY(smg_host_stage_reserve(ctx, 64));
+    auto norm_of = [&](smg_field* f, double* hv) -> smg_status {
+        SMG_TRY(vreduce<double>(ctx, fview<double>(f), nullptr, VR_NORM, sc));
+        SMG_CUDA(ctx, cudaMemcpyAsync(ctx->host_stage, sc, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        *hv = std::sqrt(ctx->host_stage[0]);
+        return SMG_OK;
+    };
+    auto scale_by = [&](smg_field* f, double s) -> smg_status {
+        double a[2] = {s, 0.0};
+        return smg_blas_scale(a, f);
+    };
+    auto ortho = [&](smg_field* v, int upto) -> smg_status {
+        for (int j = 0; j < upto; ++j) {
+            SMG_TRY(vreduce<double>(ctx, fview<double>(vecs[j]), (const cx<double>*)v->data, VR_DOT, sc + 2));
+            SMG_TRY(vaxpy<double>(ctx, fview<double>(v), (const cx<double>*)vecs[j]->data, sc + 2, -1.0));
+        }
+        return SMG_OK;
+    };
+    for (int i = 0; i < k; ++i) {
+        double nv;
+        SMG_TRY(norm_of(vecs[i], &nv));
+        SMG_TRY(scale_by(vecs[i], 1.0 / nv));
+        for (int it = 0; it < mg->p.null_iters; ++it) {
+            SMG_TRY(mr_fine<double>(mg, xn, vecs[i], mg->p.null_mr_steps, true));
+            SMG_TRY(ortho(xn, i));
+            SMG_TRY(norm_of(xn, &nv));
+            if (nv > 1e-14) {
+                SMG_TRY(scale_by(xn, 1.0 / nv));
+                SMG_CUDA(ctx, cudaMemcpyAsync(vecs[i]->data, xn->data, xn->bytes, cudaMemcpyDeviceToDevice,
+                                              ctx->stream));
+            } else {
+                break;
+            }
+        }
+    }
+    for (int i = 0; i < k; ++i) {
+        SMG_TRY(ortho(vecs[i], i));
+        double nv;
+        SMG_TRY(norm_of(vecs[i], &nv));
+        if (nv > 1e-14) SMG_TRY(scale_by(vecs[i], 1.0 / nv));
+    }
+    smg_field_destroy(xn);
+    return SMG_OK;
+}
+
+smg_status null_space_coarse(smg_mg* mg, int l, std::vector<cx<double>*>& vecs) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[l];
+    const int k = (int)vecs.size();
+    SMG_TRY(ensure_work(mg, 1, SMG_F64));
+    CoarseWork& w = mg->cw[l];
+    double* sc = mg->scal;
+    SMG_TRY(smg_host_stage_reserve(ctx, 64));
+    auto view = [&](void* p) { return cview<double>(p, L, 1); };
+    auto norm_of = [&](void* f, double* hv) -> smg_status {
+        SMG_TRY(vreduce<double>(ctx, view(f), nullptr, VR_NORM, sc));
+        SMG_CUDA(ctx, cudaMemcpyAsync(ctx->host_stage, sc, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        *hv = std::sqrt(ctx->host_stage[0]);
+        return SMG_OK;
+    };
+    auto scale_by = [&](void* f, double s) -> smg_status {
+        double a[2] = {s - 1.0, 0.0};  // y += (s - 1) y
+        SMG_CUDA(ctx, cudaMemcpyAsync(sc + 8, a, sizeof(a), cudaMemcpyHostToDevice, ctx->stream));
+        return vaxpy<double>(ctx, view(f), (const cx<double>*)f, sc + 8, 1.0);
+    };
+    auto ortho = [&](void* v, int upto) -> smg_status {
+        for (int j = 0; j < upto; ++j) {
+            SMG_TRY(vreduce<double>(ctx, view(vecs[j]), (const cx<double>*)v, VR_DOT, sc + 2));
+            SMG_TRY(vaxpy<double>(ctx, view(v), (const cx<double>*)vecs[j], sc + 2, -1.0));
+        }
+        return SMG_OK;
+    };
+    const size_t bytes = (size_t)L.nsites * L.ndof * sizeof(cx<double>);
+    for (int i = 0; i < k; ++i) {
+        double nv;
+        SMG_TRY(norm_of(vecs[i], &nv));
+        SMG_TRY(scale_by(vecs[i], 1.0 / nv));
+        for (int it = 0; it < mg->p.null_iters; ++it) {
+            SMG_TRY(mr_coarse<double>(mg, l, w.x, vecs[i], mg->p.null_mr_steps, true));
+            SMG_TRY(ortho(w.x, i));
+            SMG_TRY(norm_of(w.x, &nv));
+            if (nv > 1e-14) {
+                SMG_TRY(scale_by(w.x, 1.0 / nv));
+                SMG_CUDA(ctx, cudaMemcpyAsync(vecs[i], w.x, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+            } else {
+                break;
+            }
+        }
+    }
+    for (int i = 0; i < k; ++i) {
+        SMG_TRY(ortho(vecs[i], i));
+        double nv;
+        SMG_TRY(norm_of(vecs[i], &nv));
+        if (nv > 1e-14) SMG_TRY(scale_by(vecs[i], 1.0 / nv));
+    }
+    return SMG_OK;
+}
+
+smg_status make_f32_copies(smg_mg* mg) {
+    smg_context* ctx = mg->ctx;
+    for (size_t l = 0; l < mg->lv.size(); ++l) {
+        Level& L = mg->lv[l];
+        if (L.V64) {
+            int64_t n = L.vsize();
+            if (!L.V32) SMG_CUDA(ctx, cudaMalloc(&L.V32, n * sizeof(cx<float>)));
+            k_cvt_flat<float, double><<<blocks_for(n), 256, 0, ctx->stream>>>(L.V64, L.V32, n);
+            count_launch(ctx);
+        }
+        if (L.A64) {
+            int64_t n = L.asize();
+            if (!L.A32) SMG_CUDA(ctx, cudaMalloc(&L.A32, n * sizeof(cx<float>)));
+            k_cvt_flat<float, double><<<blocks_for(n), 256, 0, ctx->stream>>>(L.A64, L.A32, n);
+            count_launch(ctx);
+        }
+    }
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+smg_status validate(smg_context* ctx, int L, const smg_mg_params* p) {
+    if (p->n_levels < 2 || p->n_levels > SMG_MAX_LEVELS)
+        return smg_fail(ctx, SMG_BAD_ARG, "n_levels must be in [2, SMG_MAX_LEVELS]");
+    int nx = L, ny = L, ndof = 2;
+    for (int l = 0; l < p->n_levels - 1; ++l) {
+        int ax = p->block[l][0], ay = p->block[l][1];
+        if (ax < 1 || ay < 1 || nx % ax || ny % ay)
+            return smg_fail(ctx, SMG_BAD_ARG, "aggregate size must divide the level's lattice");
+        if (l == 0 && (ax < 2 || ay < 2)) return smg_fail(ctx, SMG_BAD_ARG, "level-0 aggregates must be >= 2 x 2");
+        nx /= ax;
+        ny /= ay;
+        if (nx < 3 || ny < 3) return smg_fail(ctx, SMG_BAD_ARG, "every coarse lattice must be at least 3 x 3");
+        int nvec = p->n_vec[l];
+        int nc = p->chiral_split ? 2 * nvec : nvec;
+        if (nvec < 1 || nc > 64) return smg_fail(ctx, SMG_BAD_ARG, "coarse dofs per site must be in [1, 64]");
+        if (nc > ax * ay * ndof) return smg_fail(ctx, SMG_BAD_ARG, "more block vectors than aggregate dofs");
+        if (p->chiral_split && l > 0 && (ndof % 2))
+            return smg_fail(ctx, SMG_BAD_ARG, "chirality split needs a chirality-split parent level");
+        ndof = nc;
+    }
+    if (p->precision != SMG_F64 && p->precision != SMG_F32)
+        return smg_fail(ctx, SMG_BAD_ARG, "MG precision must be F64 or F32");
+    if (p->pre_smooth < 0 || p->post_smooth < 0 || p->null_iters < 0 || p->null_mr_steps < 0 ||
+        p->coarse_max_iter < 0)
+        return smg_fail(ctx, SMG_BAD_ARG, "negative iteration count");
+    return SMG_OK;
+}
+
+smg_status build(smg_mg* mg, const double* warm) {
+    smg_context* ctx = mg->ctx;
+    const smg_mg_params& P = mg->p;
+    const Geom g = mg->dirac->gauge->g;
+    const int nlev = P.n_levels;
+    mg->lv.resize(nlev);
+    // geometry
+    mg->lv[0].nx = mg->lv[0].ny = g.L;
+    mg->lv[0].nsites = g.V;
+    mg->lv[0].ndof = 2;
+    for (int l = 0; l < nlev - 1; ++l) {
+        Level& L = mg->lv[l];
+        L.ax = P.block[l][0];
+        L.ay = P.block[l][1];
+        L.nvec = P.n_vec[l];
+        L.nc_next = P.chiral_split ? 2 * L.nvec : L.nvec;
+        L.nagg_x = L.nx / L.ax;
+        L.nagg_y = L.ny / L.ay;
+        Level& N = mg->lv[l + 1];
+        N.nx = L.nagg_x;
+        N.ny = L.nagg_y;
+        N.nsites = N.nx * N.ny;
+        N.ndof = L.nc_next;
+    }
+    std::mt19937 rng(P.seed);
+    std::normal_distribution<double> dist(0.0, 1.0);
+    auto draw = [&](int64_t n, std::vector<double>& h) {  // random_vec order (linalg.cpp:44-48, GCC x86-64)
+        h.resize(2 * n);
+        for (int64_t i = 0; i < n; ++i) {
+            double im = dist(rng);
+            double re = dist(rng);
+            h[2 * i] = re;
+            h[2 * i + 1] = im;
+        }
+    };
+    // ---- level 0 null vectors
+    const Level& L0 = mg->lv[0];
+    const int k0 = L0.nvec;
+    std::vector<double> h;
+    for (int i = 0; i < k0; ++i) {
+        smg_field* f = nullptr;
+        SMG_TRY(smg_field_create(ctx, g.L, 1, SMG_F64, &f));
+        mg->null0.push_back(f);
+        if (warm) {
+            SMG_TRY(smg_field_upload(f, warm + (size_t)4 * g.V * i));
+        } else {
+            draw((int64_t)2 * g.V, h);
+            SMG_TRY(smg_field_upload(f, h.data()));
+        }
+    }
+    SMG_TRY(null_space_fine(mg, mg->null0));
+    // ---- level 0 prolongator and Galerkin operator
+    {
+        Level& L = mg->lv[0];
+        SMG_CUDA(ctx, cudaMalloc(&L.V64, L.vsize() * sizeof(cx<double>)));
+        SMG_CUDA(ctx, cudaMemsetAsync(L.V64, 0, L.vsize() * sizeof(cx<double>), ctx->stream));
+        for (int k = 0; k < k0; ++k) {
+            k_extract0<<<blocks_for(g.V), 256, 0, ctx->stream>>>((const cx<double>*)mg->null0[k]->data, k, g, L.ax,
+                                                                L.ay, L.nvec, L.nc_next, P.chiral_split, L.V64);
+            count_launch(ctx);
+        }
+        const int len = L.ax * L.ay * 2, nc = L.nc_next;
+        const int nagg = L.nagg_x * L.nagg_y;
+        size_t smem = (size_t)len * nc * sizeof(cx<double>);
+        if (smem > 200 * 1024) return smg_fail(ctx, SMG_UNSUPPORTED, "aggregate too large for block Gram-Schmidt");
+        SMG_CUDA(ctx, cudaFuncSetAttribute(k_block_orth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_block_orth<<<nagg, 128, smem, ctx->stream>>>(L.V64, len, nc);
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+        // W = D P on block halos, then the 9 Galerkin blocks
+        const int nh = (L.ax + 2) * (L.ay + 2);
+        cx<double>* W = nullptr;
+        SMG_CUDA(ctx, cudaMallocAsync(&W, (size_t)nagg * nc * nh * 2 * sizeof(cx<double>), ctx->stream));
+        smg_dirac* d = mg->dirac;
+        k_W0<<<nagg, 256, 0, ctx->stream>>>(L.V64, d->gauge->U64, d->C64, g, L.ax, L.ay, nc, 2.0 * d->r + d->mass,
+                                           d->mu_t, d->r, W);
+        count_launch(ctx);
+        Level& N = mg->lv[1];
+        SMG_CUDA(ctx, cudaMalloc(&N.A64, N.asize() * sizeof(cx<double>)));
+        k_galerkin0<<<dim3(nagg, 9), 256, 0, ctx->stream>>>(W, L.nagg_x, L.nagg_y, L.ax, L.ay, nc, N.A64);
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+        SMG_CUDA(ctx, cudaFreeAsync(W, ctx->stream));
+    }
+    // ---- deeper levels
+    for (int l = 1; l < nlev - 1; ++l) {
+        Level& L = mg->lv[l];
+        const int dim = L.nsites * L.ndof;
+        std::vector<cx<double>*> vecs(L.nvec, nullptr);
+        for (int i = 0; i < L.nvec; ++i) {
+            SMG_CUDA(ctx, cudaMalloc(&vecs[i], (size_t)dim * sizeof(cx<double>)));
+            draw(dim, h);
+            SMG_CUDA(ctx, cudaMemcpy(vecs[i], h.data(), (size_t)dim * sizeof(cx<double>), cudaMemcpyHostToDevice));
+        }
+        smg_status st = null_space_coarse(mg, l, vecs);
+        if (st == SMG_OK) {
+            SMG_CUDA(ctx, cudaMalloc(&L.V64, L.vsize() * sizeof(cx<double>)));
+            SMG_CUDA(ctx, cudaMemsetAsync(L.V64, 0, L.vsize() * sizeof(cx<double>), ctx->stream));
+            for (int k = 0; k < L.nvec; ++k) {
+                k_extract_c<<<blocks_for(dim), 256, 0, ctx->stream>>>(vecs[k], k, L.nx, L.ny, L.ndof, L.ax, L.ay,
+                                                                     L.nvec, L.nc_next, P.chiral_split, L.V64);
+                count_launch(ctx);
+            }
+            const int len = L.ax * L.ay * L.ndof, nc = L.nc_next, nagg = L.nagg_x * L.nagg_y;
+            size_t smem = (size_t)len * nc * sizeof(cx<double>);
+            if (smem > 200 * 1024) st = smg_fail(ctx, SMG_UNSUPPORTED, "aggregate too large for block Gram-Schmidt");
+            if (st == SMG_OK) {
+                cudaFuncSetAttribute(k_block_orth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                k_block_orth<<<nagg, 128, smem, ctx->stream>>>(L.V64, len, nc);
+                count_launch(ctx);
+                Level& N = mg->lv[l + 1];
+                SMG_CUDA(ctx, cudaMalloc(&N.A64, N.asize() * sizeof(cx<double>)));
+                size_t sm2 = (size_t)L.ndof * nc * sizeof(cx<double>);
+                int threads = 256;
+                while (threads * 4 < nc * nc) threads *= 2;
+                cudaFuncSetAttribute(k_galerkin_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2);
+                k_galerkin_c<<<nagg, threads, sm2, ctx->stream>>>(L.A64, L.V64, L.nx, L.ny, L.ax, L.ay, L.ndof, nc,
+                                                                  N.A64);
+                count_launch(ctx);
+                SMG_CHECK_LAUNCH(ctx);
+            }
+        }
+        cudaStreamSynchronize(ctx->stream);
+        for (auto* p : vecs) cudaFree(p);
+        SMG_TRY(st);
+    }
+    SMG_TRY(make_f32_copies(mg));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SMG_OK;
+}
+
+void destroy_levels(smg_mg* mg) {
+    for (auto& L : mg->lv) {
+        for (void* p : {(void*)L.V64, (void*)L.V32, (void*)L.A64, (void*)L.A32})
+            if (p) cudaFree(p);
+    }
+    mg->lv.clear();
+    for (auto* f : mg->null0) smg_field_destroy(f);
+    mg->null0.clear();
+}
+
+}  // namespace
+
+// ---- internal entry used by the GCR solver
+smg_status smg_mg_apply_internal(smg_mg* mg, const smg_field* b, smg_field* x) {
+    SMG_TRY(ensure_work(mg, b->nrhs, b->prec));
+    if (b->prec == SMG_F64) return cycle_fine<double>(mg, x, b);
+    if (b->prec == SMG_F32) return cycle_fine<float>(mg, x, b);
+    return smg_fail(mg->ctx, SMG_UNSUPPORTED, "MG cycle on F16 fields");
+}
+
+smg_precision smg_mg_precision(const smg_mg* mg) { return mg->p.precision; }
+
+extern "C" {
+
+SMG_API smg_status smg_mg_params_default(smg_mg_params* p) {
+    if (!p) return SMG_BAD_ARG;
+    std::memset(p, 0, sizeof(*p));
+    p->n_levels = 2;
+    for (int l = 0; l < SMG_MAX_LEVELS - 1; ++l) {
+        p->block[l][0] = l == 0 ? 4 : 4;
+        p->block[l][1] = l == 0 ? 4 : 1;
+        p->n_vec[l] = 4;
+    }
+    p->chiral_split = 0;
+    p->null_iters = 20;
+    p->null_mr_steps = 5;
+    p->pre_smooth = 3;
+    p->post_smooth = 3;
+    p->w_cycle = 1;
+    p->coarse_max_iter = 200;
+    p->coarse_tol = 1e-12;
+    p->precision = SMG_F64;
+    p->seed = 42;
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_create(smg_dirac* d, const smg_mg_params* p, const double* warm_start, smg_mg** out) {
+    if (!d || !p || !out) return SMG_BAD_ARG;
+    *out = nullptr;
+    smg_context* ctx = d->ctx;
+    SMG_TRY(validate(ctx, d->gauge->g.L, p));
+    smg_mg* mg = new smg_mg();
+    mg->ctx = ctx;
+    mg->dirac = d;
+    mg->p = *p;
+    smg_status st = build(mg, warm_start);
+    if (st != SMG_OK) {
+        cudaStreamSynchronize(ctx->stream);
+        free_work(mg);
+        destroy_levels(mg);
+        delete mg;
+        return st;
+    }
+    *out = mg;
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_destroy(smg_mg* mg) {
+    if (!mg) return SMG_OK;
+    cudaStreamSynchronize(mg->ctx->stream);
+    free_work(mg);
+    destroy_levels(mg);
+    delete mg;
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_level_dims(smg_mg* mg, int level, int* nx, int* ny, int* ndof) {
+    if (!mg || level < 0 || level >= (int)mg->lv.size()) return SMG_BAD_ARG;
+    if (nx) *nx = mg->lv[level].nx;
+    if (ny) *ny = mg->lv[level].ny;
+    if (ndof) *ndof = mg->lv[level].ndof;
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_null_vectors(smg_mg* mg, double* out) {
+    if (!mg || !out) return SMG_BAD_ARG;
+    const size_t per = (size_t)4 * mg->lv[0].nsites;
+    for (size_t i = 0; i < mg->null0.size(); ++i) SMG_TRY(smg_field_download(mg->null0[i], out + per * i));
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_get_prolongator(smg_mg* mg, int level, double* block_vecs) {
+    if (!mg || !block_vecs || level < 0 || level >= (int)mg->lv.size() - 1) return SMG_BAD_ARG;
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[level];
+    const int64_t n = L.vsize();
+    std::vector<std::complex<double>> h(n);
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    SMG_CUDA(ctx, cudaMemcpy(h.data(), L.V64, n * sizeof(cx<double>), cudaMemcpyDeviceToHost));
+    // device [agg][loc][dof][i] -> reference [agg][i][loc * dof_per_site + dof]
+    const int m = L.ax * L.ay, nd = L.ndof, nc = L.nc_next, nagg = L.nagg_x * L.nagg_y;
+    auto* o = reinterpret_cast<std::complex<double>*>(block_vecs);
+    for (int B = 0; B < nagg; ++B)
+        for (int loc = 0; loc < m; ++loc)
+            for (int j = 0; j < nd; ++j)
+                for (int i = 0; i < nc; ++i)
+                    o[((int64_t)B * nc + i) * m * nd + loc * nd + j] = h[(((int64_t)B * m + loc) * nd + j) * nc + i];
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_get_coarse_op(smg_mg* mg, int level, double* links) {
+    if (!mg || !links || level < 1 || level >= (int)mg->lv.size()) return SMG_BAD_ARG;
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[level];
+    const int64_t n = L.asize();
+    std::vector<std::complex<double>> h(n);
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    SMG_CUDA(ctx, cudaMemcpy(h.data(), L.A64, n * sizeof(cx<double>), cudaMemcpyDeviceToHost));
+    const int nc = L.ndof;
+    auto* o = reinterpret_cast<std::complex<double>*>(links);
+    for (int64_t sd = 0; sd < (int64_t)L.nsites * 9; ++sd)
+        for (int i = 0; i < nc; ++i)
+            for (int j = 0; j < nc; ++j) o[sd * nc * nc + i * nc + j] = h[sd * nc * nc + j * nc + i];
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_precondition(smg_mg* mg, const smg_field* b, smg_field* x) {
+    if (!mg || !b || !x) return SMG_BAD_ARG;
+    SMG_TRY(smg_field_check_pair(b, x));
+    if (b == x) return smg_fail(mg->ctx, SMG_BAD_ARG, "b and x must be distinct");
+    if (b->g.L != mg->lv[0].nx) return smg_fail(mg->ctx, SMG_BAD_ARG, "field L differs from the hierarchy's");
+    return smg_mg_apply_internal(mg, b, x);
+}
+
+SMG_API smg_status smg_mg_prolong_host(smg_mg* mg, int level, const double* coarse, double* fine) {
+    if (!mg || !coarse || !fine || level < 0 || level >= (int)mg->lv.size() - 1) return SMG_BAD_ARG;
+    smg_context* ctx = mg->ctx;
+    SMG_TRY(ensure_work(mg, 1, SMG_F64));
+    const Level& L = mg->lv[level];
+    const Level& N = mg->lv[level + 1];
+    CoarseWork& nw = mg->cw[level + 1];
+    const size_t cb = (size_t)N.nsites * N.ndof * sizeof(cx<double>);
+    SMG_CUDA(ctx, cudaMemcpyAsync(nw.x, coarse, cb, cudaMemcpyHostToDevice, ctx->stream));
+    if (level == 0) {
+        SMG_TRY(prolong_to<double>(mg, 0, nw.x, mg->f_t->data, 0));
+        return smg_field_download(mg->f_t, fine);
+    }
+    SMG_TRY(prolong_to<double>(mg, level, nw.x, mg->cw[level].x, 0));
+    const size_t fb = (size_t)L.nsites * L.ndof * sizeof(cx<double>);
+    SMG_CUDA(ctx, cudaMemcpyAsync(fine, mg->cw[level].x, fb, cudaMemcpyDeviceToHost, ctx->stream));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_restrict_host(smg_mg* mg, int level, const double* fine, double* coarse) {
+    if (!mg || !coarse || !fine || level < 0 || level >= (int)mg->lv.size() - 1) return SMG_BAD_ARG;
+    smg_context* ctx = mg->ctx;
+    SMG_TRY(ensure_work(mg, 1, SMG_F64));
+    const Level& L = mg->lv[level];
+    const Level& N = mg->lv[level + 1];
+    CoarseWork& nw = mg->cw[level + 1];
+    if (level == 0) {
+        SMG_TRY(smg_field_upload(mg->f_t, fine));
+        SMG_TRY(restrict_to<double>(mg, 0, mg->f_t->data, nw.b));
+    } else {
+        const size_t fb = (size_t)L.nsites * L.ndof * sizeof(cx<double>);
+        SMG_CUDA(ctx, cudaMemcpyAsync(mg->cw[level].x, fine, fb, cudaMemcpyHostToDevice, ctx->stream));
+        SMG_TRY(restrict_to<double>(mg, level, mg->cw[level].x, nw.b));
+    }
+    const size_t cb = (size_t)N.nsites * N.ndof * sizeof(cx<double>);
+    SMG_CUDA(ctx, cudaMemcpyAsync(coarse, nw.b, cb, cudaMemcpyDeviceToHost, ctx->stream));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_coarse_apply_host(smg_mg* mg, int level, const double* in, double* out) {
+    if (!mg || !in || !out || level < 1 || level >= (int)mg->lv.size()) return SMG_BAD_ARG;
+    smg_context* ctx = mg->ctx;
+    SMG_TRY(ensure_work(mg, 1, SMG_F64));
+    const Level& L = mg->lv[level];
+    CoarseWork& w = mg->cw[level];
+    const size_t b = (size_t)L.nsites * L.ndof * sizeof(cx<double>);
+    SMG_CUDA(ctx, cudaMemcpyAsync(w.x, in, b, cudaMemcpyHostToDevice, ctx->stream));
+    SMG_TRY(coarse_apply<double>(mg, level, cview<double>(w.x, L, 1), (cx<double>*)w.Ar, 0, nullptr, nullptr));
+    SMG_CUDA(ctx, cudaMemcpyAsync(out, w.Ar, b, cudaMemcpyDeviceToHost, ctx->stream));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SMG_OK;
+}
+
+}  // extern "C"

@@ -3,8 +3,10 @@
 // Device data layout (all precisions):
 //   site index   q = parity * Vh + cb, with cb = (x + L*y) / 2 for even L;
 //                cb equals the reference's eo_index (src/lattice.h:28-41)
-//   spinor       ((q * 2 + spin) * nrhs + rhs)  complex     -> right-hand
-//                side innermost so one link load serves every RHS lane
+//   spinor       ((q * nrhs + rhs) * 2 + spin)  complex     -> both spin
+//                components of one (site, rhs) are one 16-byte (FP32) or
+//                32-byte (FP64) vector, and the RHS lanes of a warp read
+//                consecutive vectors while sharing one link load
 //   links        U[(mu * 2 + parity) * Vh + cb] complex
 //   clover       C[q] = 0.5 * c_sw * F01 real (the diagonal shift of
 //                src/dirac.h:102)
@@ -57,6 +59,25 @@ __host__ __device__ __forceinline__ T norm2(cx<T> a) { return a.re * a.re + a.im
 
 template <typename D, typename S>
 __host__ __device__ __forceinline__ cx<D> cvt(cx<S> a) { return mk<D>((D)a.re, (D)a.im); }
+
+// spinor element index: site q, right-hand side rhs, spin sp (spin innermost)
+__host__ __device__ __forceinline__ int64_t sidx(int64_t q, int rhs, int sp, int nrhs) {
+    return (q * nrhs + rhs) * 2 + sp;
+}
+
+// both spin components of one (site, rhs), loaded and stored as one vector
+template <typename T>
+struct alignas(4 * sizeof(T)) Spinor {
+    cx<T> s0, s1;
+};
+template <typename T>
+__device__ __forceinline__ Spinor<T> ld_spinor(const cx<T>* __restrict__ f, int64_t q, int rhs, int nrhs) {
+    return reinterpret_cast<const Spinor<T>*>(f)[q * nrhs + rhs];
+}
+template <typename T>
+__device__ __forceinline__ void st_spinor(cx<T>* __restrict__ f, int64_t q, int rhs, int nrhs, Spinor<T> v) {
+    reinterpret_cast<Spinor<T>*>(f)[q * nrhs + rhs] = v;
+}
 
 // ------------------------------------------------------------ lattice geometry
 struct Geom {
