@@ -18,17 +18,17 @@ enum { EPI_NONE = 0, EPI_NORM = 1, EPI_MR = 2 };
 
 template <typename T>
 struct DslashArgs {
-    const cx<T>* __restrict__ src;
-    cx<T>* __restrict__ dst;
-    const cx<T>* __restrict__ U;   // [mu][parity][cb]
-    const T* __restrict__ C;       // clover shift per site or nullptr
-    const cx<T>* __restrict__ w;   // EPI_MR second field
-    Geom g;
-    int nrhs;
-    T diag, mu_eff, r;
-    double* partials;
-    unsigned int* ticket;
-    double* out;
+    const cx<T>* __restrict__ src = nullptr;
+    cx<T>* __restrict__ dst = nullptr;
+    const cx<T>* __restrict__ U = nullptr;  // [mu][parity][cb]
+    const T* __restrict__ C = nullptr;      // clover shift per site or nullptr
+    const cx<T>* __restrict__ w = nullptr;  // EPI_MR second field
+    Geom g{};
+    int nrhs = 1;
+    T diag = 0, mu_eff = 0, r = 0;
+    double* partials = nullptr;
+    unsigned int* ticket = nullptr;
+    double* out = nullptr;
 };
 
 template <typename T, bool DAG, int EPI>

@@ -18,12 +18,12 @@ constexpr int RX = TX + 4, RY = TY + 4;  // X / link region, origin (-2, -2)
 constexpr int CX = TX + 2, CY = TY + 2;  // chi / w region, origin (-1, -1)
 
 struct ForceArgs {
-    const cx<double>* __restrict__ X;  // single-RHS F64 field, device layout
-    const cx<double>* __restrict__ U;
-    const double* __restrict__ C;      // clover shift or nullptr
-    double* __restrict__ F;            // [mu][s] lexicographic
-    Geom g;
-    double diag, mu, r, c_sw;
+    const cx<double>* __restrict__ X = nullptr;  // single-RHS F64 field, device layout
+    const cx<double>* __restrict__ U = nullptr;
+    const double* __restrict__ C = nullptr;      // clover shift or nullptr
+    double* __restrict__ F = nullptr;            // [mu][s] lexicographic
+    Geom g{};
+    double diag = 0, mu = 0, r = 0, c_sw = 0;
 };
 
 __device__ __forceinline__ int pmod(int a, int L) {

@@ -438,13 +438,13 @@ __global__ void k_cvt_flat(const cx<S>* __restrict__ in, cx<D>* __restrict__ out
 // coarsest-level CG scalars per rhs: rr, pAp (re, im, norm from the fused
 // epilogue), bnorm2, active, and the update kernel's finaliser
 struct CcgState {
-    double* rr;
-    double* pap3;  // [rhs][3]: <Ap, p> re, im, ||Ap||^2
-    double* bnorm2;
-    double* beta;
-    int* active;
-    int* n_active;
-    double tol2;
+    double* rr = nullptr;
+    double* pap3 = nullptr;  // [rhs][3]: <Ap, p> re, im, ||Ap||^2
+    double* bnorm2 = nullptr;
+    double* beta = nullptr;
+    int* active = nullptr;
+    int* n_active = nullptr;
+    double tol2 = 0;
 };
 
 __global__ void k_ccg_init(CcgState s, int nrhs) {

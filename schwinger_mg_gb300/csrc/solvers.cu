@@ -23,16 +23,16 @@ namespace {
 
 constexpr int kCheckEvery = 8;
 
-struct CgState {      // device arrays of length nrhs each
-    double* rr;
-    double* pAp;
-    double* bnorm2;
-    double* beta;
-    int* active;
-    int* iters;
-    int* flags;       // bit 0: breakdown, bit 1: non-finite
-    int* n_active;    // scalar
-    double tol2;
+struct CgState {  // device arrays of length nrhs each
+    double* rr = nullptr;
+    double* pAp = nullptr;
+    double* bnorm2 = nullptr;
+    double* beta = nullptr;
+    int* active = nullptr;
+    int* iters = nullptr;
+    int* flags = nullptr;     // bit 0: breakdown, bit 1: non-finite
+    int* n_active = nullptr;  // scalar
+    double tol2 = 0;
 };
 
 // single block; loops so any nrhs is covered
@@ -300,12 +300,12 @@ smg_precision smg_mg_precision(const smg_mg* mg);
 namespace {
 
 struct GcrScalars {
-    double* rr;       // [rhs]
-    double* bnorm2;   // [rhs]
-    double* apr3;     // [rhs][3]: <Ap, r> re, im, ||Ap||^2
-    int* active;      // [rhs]
-    int* flags;       // [rhs] bit 0: breakdown this iteration
-    double tol2;
+    double* rr = nullptr;      // [rhs]
+    double* bnorm2 = nullptr;  // [rhs]
+    double* apr3 = nullptr;    // [rhs][3] of the current direction: <Ap, r> re, im, ||Ap||^2
+    int* active = nullptr;     // [rhs]
+    int* flags = nullptr;      // [rhs]
+    double tol2 = 0;
 };
 
 // beta = (ref ? <Az, AP_i> : <AP_i, Az>) / ApAp_i;  p -= beta P_i, Ap -= beta AP_i
@@ -507,6 +507,7 @@ smg_status gcr_run(smg_dirac* d, smg_mg* mg, const smg_field* b, smg_field* x, i
         }
         // <Ap, r> and ||Ap||^2 into this buffer's scalar slot
         SMG_TRY(reduce_into<T>(ctx, fv<T>(Ap), (const cx<T>*)r->data, VR_DOTNORM, apr_of(work)));
+        sc.apr3 = apr_of(work);
         k_gcr_update<T><<<rl.grid, rl.block, 0, ctx->stream>>>(sc, fv<T>(x), (cx<T>*)r->data, (const cx<T>*)p->data,
                                                                (const cx<T>*)Ap->data, ctx->red.partials,
                                                                ctx->red.tickets);
