@@ -179,6 +179,7 @@ SMG_API smg_status smg_blas_axpy(const double* alpha, const smg_field* x, smg_fi
 /* v *= alpha, alpha = nrhs complex (reference src/linalg.cpp:35-39). */
 SMG_API smg_status smg_blas_scale(const double* alpha, smg_field* v);
 
+
 /* ---------------------------------------------------------------- solvers */
 
 /* cg_solve on A = D^dag D (reference src/solvers.cpp:16-78): unpreconditioned

@@ -1,0 +1,279 @@
+// smg_gpu.hpp — header-only C++ drop-in over the C ABI (smg_gpu.h) with the
+// reference's own types and call shapes (cpviolator/Schwinger_MG):
+//   cx, Vec, RVec, OpApply                  src/types.h:7-10
+//   Lattice                                 src/lattice.h:4-42
+//   GaugeField                              src/gauge.h:10-36
+//   DiracOp::apply/apply_dag/apply_DdagD    src/dirac.h:115-152
+//   CGResult, cg_solve                      src/solvers.h:25-39
+//   FCGResult, fcg_solve, fcg_solve_mg      src/solvers.h:31-35, 57-84
+//   MGConfig, build_full_mg                 src/config.h:19-30, src/mg_builder.h:6-11
+//   MGHierarchy::precondition               src/multigrid.h:63
+//   fermion_force, gauge_force, gauge_action  src/hmc.h:46-69
+// Host vectors keep the reference layout (Vec v[2*s + spin]); each call copies
+// them to the device, runs the sm_103a kernels and copies results back.
+// Failures throw smg::Error carrying the smg_status, where the reference
+// asserts or prints a warning.
+#pragma once
+
+#include <array>
+#include <complex>
+#include <functional>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "smg_gpu.h"
+
+namespace smg {
+
+using cx = std::complex<double>;
+using Vec = std::vector<cx>;
+using RVec = std::vector<double>;
+using OpApply = std::function<void(const Vec& src, Vec& dst)>;
+
+struct Error : std::runtime_error {
+    smg_status status;
+    Error(smg_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+inline void check(smg_status s, smg_context* ctx, const char* where) {
+    if (s == SMG_OK) return;
+    std::string msg = std::string(where) + ": " + smg_status_string(s);
+    if (ctx) msg += std::string(" (") + smg_last_error(ctx) + ")";
+    throw Error(s, msg);
+}
+
+// One device + stream per host thread; created on first use.
+inline smg_context* default_context() {
+    static thread_local std::unique_ptr<smg_context, smg_status (*)(smg_context*)> ctx(
+        [] {
+            smg_context* c = nullptr;
+            check(smg_context_create(0, nullptr, &c), nullptr, "smg_context_create");
+            return c;
+        }(),
+        &smg_context_destroy);
+    return ctx.get();
+}
+
+struct Lattice {
+    int L, V, ndof, V_half;
+    explicit Lattice(int L_) : L(L_), V(L_ * L_), ndof(2 * L_ * L_), V_half(L_ * L_ / 2) {}
+};
+
+class GaugeField {
+   public:
+    const Lattice& lat;
+    std::array<Vec, 2> U;  // host copy, reference layout U[mu][s]
+
+    explicit GaugeField(const Lattice& lat_) : lat(lat_) {
+        U[0].assign(lat.V, 1.0);
+        U[1].assign(lat.V, 1.0);
+    }
+    // Copies the host links to the device; call after changing U.
+    void sync() const {
+        std::vector<double> flat(4 * (size_t)lat.V);
+        for (int mu = 0; mu < 2; ++mu)
+            for (int s = 0; s < lat.V; ++s) {
+                flat[2 * ((size_t)mu * lat.V + s)] = U[mu][s].real();
+                flat[2 * ((size_t)mu * lat.V + s) + 1] = U[mu][s].imag();
+            }
+        smg_context* ctx = default_context();
+        if (!h_) {
+            smg_gauge* g = nullptr;
+            check(smg_gauge_create(ctx, lat.L, flat.data(), &g), ctx, "smg_gauge_create");
+            h_.reset(g);
+        } else {
+            check(smg_gauge_set(h_.get(), flat.data()), ctx, "smg_gauge_set");
+        }
+    }
+    smg_gauge* handle() const {
+        if (!h_) sync();
+        return h_.get();
+    }
+    double avg_plaq() const {
+        double v = 0;
+        check(smg_gauge_avg_plaq(handle(), &v), default_context(), "smg_gauge_avg_plaq");
+        return v;
+    }
+
+   private:
+    mutable std::unique_ptr<smg_gauge, smg_status (*)(smg_gauge*)> h_{nullptr, &smg_gauge_destroy};
+};
+
+// Device field of nrhs spinors with host-Vec transfers.
+class DeviceField {
+   public:
+    DeviceField(int L, int nrhs, smg_precision p = SMG_F64) {
+        smg_field* f = nullptr;
+        check(smg_field_create(default_context(), L, nrhs, p, &f), default_context(), "smg_field_create");
+        h_.reset(f);
+    }
+    void upload(const Vec& v) {
+        check(smg_field_upload(h_.get(), reinterpret_cast<const double*>(v.data())), default_context(), "upload");
+    }
+    void download(Vec& v) const {
+        check(smg_field_download(h_.get(), reinterpret_cast<double*>(v.data())), default_context(), "download");
+    }
+    smg_field* get() const { return h_.get(); }
+
+   private:
+    std::unique_ptr<smg_field, smg_status (*)(smg_field*)> h_{nullptr, &smg_field_destroy};
+};
+
+class DiracOp {
+   public:
+    const Lattice& lat;
+    const GaugeField& gauge;
+    double mass, r, c_sw, mu_t;
+
+    DiracOp(const Lattice& lat_, const GaugeField& g_, double m_, double r_ = 1.0, double csw_ = 0.0,
+            double mu_t_ = 0.0)
+        : lat(lat_), gauge(g_), mass(m_), r(r_), c_sw(csw_), mu_t(mu_t_) {
+        smg_dirac* d = nullptr;
+        check(smg_dirac_create(gauge.handle(), mass, r, c_sw, mu_t, &d), default_context(), "smg_dirac_create");
+        h_.reset(d);
+    }
+    // Recomputes the clover term after GaugeField::sync().
+    void refresh() { check(smg_dirac_refresh(h_.get()), default_context(), "smg_dirac_refresh"); }
+
+    void apply(const Vec& src, Vec& dst) const { run(SMG_OP_D, src, dst); }
+    void apply_dag(const Vec& src, Vec& dst) const { run(SMG_OP_DDAG, src, dst); }
+    void apply_DdagD(const Vec& src, Vec& dst) const { run(SMG_OP_DDAGD, src, dst); }
+    void apply_g5D(const Vec& src, Vec& dst) const { run(SMG_OP_G5D, src, dst); }
+    OpApply as_DdagD_op() const {
+        return [this](const Vec& s, Vec& d) { apply_DdagD(s, d); };
+    }
+    smg_dirac* handle() const { return h_.get(); }
+
+   private:
+    void run(smg_operator op, const Vec& src, Vec& dst) const {
+        DeviceField a(lat.L, 1), b(lat.L, 1);
+        a.upload(src);
+        check(smg_dirac_apply(h_.get(), op, a.get(), b.get()), default_context(), "smg_dirac_apply");
+        dst.resize(src.size());
+        b.download(dst);
+    }
+    std::unique_ptr<smg_dirac, smg_status (*)(smg_dirac*)> h_{nullptr, &smg_dirac_destroy};
+};
+
+struct CGResult {
+    Vec solution;
+    int iterations;
+    double final_residual;
+};
+struct FCGResult {
+    Vec solution;
+    int iterations;
+    double final_residual;
+};
+
+// cg_solve(A, n, rhs, max_iter, tol) with A = D^dag D of `D`
+inline CGResult cg_solve(const DiracOp& D, int n, const Vec& rhs, int max_iter, double tol) {
+    if (n != D.lat.ndof) throw Error(SMG_BAD_ARG, "cg_solve: n must be 2*V");
+    DeviceField b(D.lat.L, 1), x(D.lat.L, 1);
+    b.upload(rhs);
+    smg_solve_result r{};
+    smg_status s = smg_cg_solve(D.handle(), b.get(), x.get(), max_iter, tol, &r);
+    if (s != SMG_OK && s != SMG_NOT_CONVERGED) check(s, default_context(), "smg_cg_solve");
+    CGResult out{Vec(n), r.iterations, r.final_residual};
+    x.download(out.solution);
+    return out;
+}
+
+struct MGConfig {  // reference src/config.h:19-30
+    int mg_levels = 2;
+    int block_size = 4;
+    int k_null = 4;
+    int coarse_block = 0;  // 0 = 4 * k_null dofs, i.e. 4 coarse sites
+    bool w_cycle = true;
+    int pre_smooth = 3;
+    int post_smooth = 3;
+};
+
+class MGHierarchy {
+   public:
+    MGHierarchy(const DiracOp& D, const smg_mg_params& p, const std::vector<Vec>* warm = nullptr) : D_(D) {
+        std::vector<cx> flat;
+        if (warm) {
+            for (const Vec& v : *warm) flat.insert(flat.end(), v.begin(), v.end());
+        }
+        smg_mg* mg = nullptr;
+        check(smg_mg_create(D.handle(), &p, warm ? reinterpret_cast<const double*>(flat.data()) : nullptr, &mg),
+              default_context(), "smg_mg_create");
+        h_.reset(mg);
+    }
+    Vec precondition(const Vec& b) {
+        DeviceField fb(D_.lat.L, 1), fx(D_.lat.L, 1);
+        fb.upload(b);
+        check(smg_mg_precondition(h_.get(), fb.get(), fx.get()), default_context(), "smg_mg_precondition");
+        Vec x(b.size());
+        fx.download(x);
+        return x;
+    }
+    smg_mg* handle() const { return h_.get(); }
+
+   private:
+    const DiracOp& D_;
+    std::unique_ptr<smg_mg, smg_status (*)(smg_mg*)> h_{nullptr, &smg_mg_destroy};
+};
+
+// build_full_mg(D, mcfg, scfg, rng, ...) with the rng given as its seed
+inline std::unique_ptr<MGHierarchy> build_full_mg(const DiracOp& D, const MGConfig& mcfg, uint32_t seed,
+                                                  const std::vector<Vec>* warm_start = nullptr) {
+    smg_mg_params p;
+    smg_mg_params_default(&p);
+    p.n_levels = mcfg.mg_levels < 2 ? 2 : mcfg.mg_levels;
+    p.block[0][0] = p.block[0][1] = mcfg.block_size;
+    int cb = mcfg.coarse_block > 0 ? mcfg.coarse_block : 4 * mcfg.k_null;
+    for (int l = 0; l < SMG_MAX_LEVELS - 1; ++l) {
+        p.n_vec[l] = mcfg.k_null;
+        if (l > 0) {
+            p.block[l][0] = cb / mcfg.k_null;
+            p.block[l][1] = 1;
+        }
+    }
+    p.null_iters = warm_start ? 5 : 20;
+    p.w_cycle = mcfg.w_cycle;
+    p.pre_smooth = mcfg.pre_smooth;
+    p.post_smooth = mcfg.post_smooth;
+    p.seed = seed;
+    return std::make_unique<MGHierarchy>(D, p, warm_start);
+}
+
+inline FCGResult fcg_solve_mg(const DiracOp& D, int n, const Vec& rhs, MGHierarchy& mg, int max_iter, double tol,
+                              int truncation = 20) {
+    if (n != D.lat.ndof) throw Error(SMG_BAD_ARG, "fcg_solve_mg: n must be 2*V");
+    DeviceField b(D.lat.L, 1), x(D.lat.L, 1);
+    b.upload(rhs);
+    smg_solve_result r{};
+    smg_status s = smg_gcr_solve(D.handle(), mg.handle(), b.get(), x.get(), max_iter, tol, truncation, 0, &r);
+    if (s != SMG_OK && s != SMG_NOT_CONVERGED) check(s, default_context(), "smg_gcr_solve");
+    FCGResult out{Vec(n), r.iterations, r.final_residual};
+    x.download(out.solution);
+    return out;
+}
+
+inline void fermion_force(const DiracOp& D, const Vec& X, std::array<RVec, 2>& force) {
+    DeviceField fx(D.lat.L, 1);
+    fx.upload(X);
+    RVec flat(2 * (size_t)D.lat.V);
+    check(smg_fermion_force(D.handle(), fx.get(), flat.data()), default_context(), "smg_fermion_force");
+    force[0].assign(flat.begin(), flat.begin() + D.lat.V);
+    force[1].assign(flat.begin() + D.lat.V, flat.end());
+}
+
+inline void gauge_force(const GaugeField& g, double beta, std::array<RVec, 2>& force) {
+    RVec flat(2 * (size_t)g.lat.V);
+    check(smg_gauge_force(g.handle(), beta, flat.data()), default_context(), "smg_gauge_force");
+    force[0].assign(flat.begin(), flat.begin() + g.lat.V);
+    force[1].assign(flat.begin() + g.lat.V, flat.end());
+}
+
+inline double gauge_action(const GaugeField& g, double beta) {
+    double v = 0;
+    check(smg_gauge_action(g.handle(), beta, &v), default_context(), "smg_gauge_action");
+    return v;
+}
+
+}  // namespace smg
