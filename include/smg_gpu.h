@@ -179,6 +179,25 @@ SMG_API smg_status smg_blas_axpy(const double* alpha, const smg_field* x, smg_fi
 /* v *= alpha, alpha = nrhs complex (reference src/linalg.cpp:35-39). */
 SMG_API smg_status smg_blas_scale(const double* alpha, smg_field* v);
 
+/* Dot products that allocate nothing.  No counterpart in the reference: it
+ * exists for callers that cannot call cudaMalloc when they need the result,
+ * such as a framework that owns all device memory through its own pool, a
+ * latency-critical loop that cannot afford an allocation, or a process under
+ * a fixed device-memory budget.  a and b are device pointers to nrhs vectors
+ * of n complex128 values each, stored one after another; out is a device
+ * pointer that receives nrhs complex results sum_i conj(a_i) b_i as
+ * interleaved (re, im) doubles.  Work is enqueued on `stream` (a cudaStream_t,
+ * NULL = the legacy default stream) of the current device, and the call
+ * returns without waiting for it.  Limit: nrhs <= 16 (larger values return
+ * SMG_BAD_ARG); any n.  The scratch is a fixed 78,080-byte array that every
+ * GPU loading this library keeps until the process exits; it is shared by all
+ * calls and keeps the last call's contents, so calls whose kernels overlap on
+ * the GPU (different streams, or different host threads on one device) race
+ * and must be serialised by the caller.  The first call on each device looks
+ * the array's device address up; make that first call before any stream
+ * capture. */
+SMG_API smg_status smg_blas_dot_noalloc(const double* a, const double* b, int64_t n, int nrhs, double* out,
+                                        void* stream);
 
 /* ---------------------------------------------------------------- solvers */
 

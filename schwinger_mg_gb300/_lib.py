@@ -90,6 +90,7 @@ _SIGS = {
     "smg_blas_norm": (_st, [_vp, _dp]),
     "smg_blas_axpy": (_st, [_dp, _vp, _vp]),
     "smg_blas_scale": (_st, [_dp, _vp]),
+    "smg_blas_dot_noalloc": (_st, [_vp, _vp, C.c_int64, C.c_int, _vp, _vp]),
     "smg_cg_solve": (_st, [_vp, _vp, _vp, C.c_int, C.c_double, C.POINTER(SolveResult)]),
     "smg_fermion_force": (_st, [_vp, _vp, _dp]),
     "smg_mg_params_default": (_st, [C.POINTER(MGParams)]),
