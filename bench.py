@@ -1,26 +1,32 @@
-"""Benchmark of the Wilson-clover Dirac operator / MG solve path on GB300.
+"""Benchmark of the Wilson-clover Dirac operator and its MG solve path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload dslash|cg] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload mg|dslash|cg] [--impl ours|reference]
 
 Prints ONE JSON line (rank 0).  A step is one pass of the hot path over one
-batch of seeded synthetic input (theta ~ N(0, 1/beta) links, Gaussian
-sources), timed with CUDA events on the library's stream between a barrier and
-a device synchronize, max over ranks.  Workloads:
+batch of seeded synthetic input (links U = exp(i theta), theta ~ N(0, 1/beta);
+Gaussian complex sources), timed with CUDA events on the library's stream
+(smg_timer_begin/end) between a barrier and a synchronize; the max over ranks
+is reported.  Workloads:
 
-* dslash — FP32 D applied to 32 right-hand sides on the 512 x 512 lattice
-  (beta = 6, m = -0.05, c_sw = 1), the fine-operator configuration of the
-  multi-RHS MG benchmark.  Inputs (134 MB) and outputs exceed the 129 MB L2.
-  value = algorithmic HBM GB/s.
-* cg     — FP64 CG on D^dag D to ||r||/||b|| <= 1e-10 on the 32 x 32 lattice
-  (beta = 2, m = 0.1, c_sw = 1).  value = solves/s.
+* mg (default) — the multi-RHS MG-GCR solve of BASELINE config 3: 512 x 512
+  lattice, beta = 6, m = -0.05, c_sw = 1; three levels (4 x 4 then 2 x 2
+  aggregates, 8 null vectors split by chirality = 16 coarse dofs per level);
+  32 right-hand sides solved together to a true FP64 residual of 1e-10 by an
+  FP64 GCR preconditioned with the FP32 hierarchy.  The hierarchy is built
+  once before timing.  value = solves/s.  The plain FP64 single-RHS MG on the
+  same inputs is measured beside it (config.plain_fp64_mg_solves_per_s).
+* dslash — FP32 D on 32 right-hand sides at L = 512; value = algorithmic GB/s.
+* cg — BASELINE config 1 (L = 32, beta = 2, m = 0.1, c_sw = 1) FP64 CG;
+  value = solves/s.
 
 `--impl reference` times the reference's CPU implementation of the same
-workload on this machine's host cores (the C restatement, oracle/), and prints
-the same line with "impl": "reference".
+workload on this machine's host cores: the C restatement in oracle/ (the
+reference tree is not present where the benchmark runs), with every host core.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes as Cc
 import json
 import os
 import subprocess
@@ -34,6 +40,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Dslash HBM GB/s; MG-GCR solves/s to 1e-10, mixed+batched vs plain FP64"
+DP = Cc.POINTER(Cc.c_double)
 
 
 def peaks():
@@ -45,7 +52,7 @@ def peaks():
 
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
 
     def __init__(self, device: int):
         self.device = device
@@ -62,6 +69,7 @@ class Clocks:
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
                  "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.25)  # first sample before the timed work starts
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -84,7 +92,7 @@ class Clocks:
             if len(parts) < 9:
                 continue
             try:
-                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
             except ValueError:
                 continue
         try:
@@ -94,19 +102,30 @@ class Clocks:
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        reasons = sorted({names[i] for _, _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
         return {"sm_mhz": float(np.median([r[0] for r in rows])), "sm_max_mhz": max(r[1] for r in rows),
-                "reasons": reasons, "samples": len(rows)}
+                "power_w_max": max(r[2] for r in rows), "reasons": reasons, "samples": len(rows)}
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
-# --------------------------------------------------------------------- workloads
+def max_over_ranks(v: float, ws: int) -> float:
+    if ws == 1:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ workloads
+MG = dict(L=512, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20240, nrhs=32, levels=3, blocks=[(4, 4), (2, 2)],
+          n_vec=8, chiral=True, null_iters=6, pre=4, post=4, coarse_max_iter=40, coarse_tol=5e-2, tol=1e-10,
+          max_iter=500, trunc=20)
 DSLASH = dict(L=512, nrhs=32, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20240)
 CG = dict(L=32, beta=2.0, m=0.1, r=1.0, csw=1.0, mu=0.0, seed=31, tol=1e-10, max_iter=10000)
 
@@ -123,9 +142,14 @@ def dslash_bytes_f64_single(L):
     return L * L * 104
 
 
-def run_ours(args, ws, rank, local):
-    import ctypes as Cc
+def mg_params(smg, c, precision):
+    return smg.mg_params(c["levels"], c["blocks"][0][0], c["n_vec"], blocks=c["blocks"], chiral_split=c["chiral"],
+                         null_iters=c["null_iters"], pre_smooth=c["pre"], post_smooth=c["post"],
+                         coarse_max_iter=c["coarse_max_iter"], coarse_tol=c["coarse_tol"], precision=precision,
+                         seed=c["seed"])
 
+
+def run_ours(args, ws, rank, local):
     import torch
 
     import schwinger_mg_gb300 as smg
@@ -135,8 +159,7 @@ def run_ours(args, ws, rank, local):
     lib = smg.lib()
     peak, peak_kind = peaks()
     out = {"metric": METRIC, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "scaling": "weak",
-           "vs_baseline": None, "data": "synthetic (seeded theta ~ N(0,1/beta) links, Gaussian sources)"}
-    dp = Cc.POINTER(Cc.c_double)
+           "vs_baseline": None, "data": "synthetic (seeded theta ~ N(0,1/beta) links, Gaussian complex sources)"}
 
     def timed(step, n):
         """Device milliseconds per step on the library's stream, max over ranks."""
@@ -149,7 +172,89 @@ def run_ours(args, ws, rank, local):
         ms = ctx.timer_end() / n
         return max_over_ranks(ms, ws)
 
-    if args.workload == "dslash":
+    if args.workload == "mg":
+        c = MG
+        L, nrhs = c["L"], c["nrhs"]
+        U = smg.gauge_normal(L, c["beta"], c["seed"])
+        lat = smg.Lattice(L)
+        g = smg.GaugeField(lat, U, ctx)
+        D = smg.DiracOp(lat, g, c["m"], c["r"], c["csw"], c["mu"])
+        t0 = time.perf_counter()
+        mg32 = smg.MGHierarchy(D, mg_params(smg, c, "f32"))
+        ctx.synchronize()
+        setup_s = time.perf_counter() - t0
+        B = np.stack([smg.random_vec(lat.ndof, c["seed"] + 1 + j) for j in range(nrhs)])
+        fb = smg.Field(lat, nrhs, "f64", ctx, data=B)
+        fx = smg.Field(lat, nrhs, "f64", ctx)
+        res = smg._lib.SolveResult()
+
+        def solve(mg, b, x):
+            st = lib.smg_gcr_solve(D.h, mg.h, b.h, x.h, c["max_iter"], c["tol"], c["trunc"], 0, Cc.byref(res))
+            smg._lib.check(st, "smg_gcr_solve", ctx.h)
+
+        step = lambda: solve(mg32, fb, fx)  # noqa: E731
+        for _ in range(args.warmup):
+            step()
+        l0 = ctx.kernel_launches
+        with Clocks(local) as clk:
+            ms = timed(step, args.steps)
+        launches = ctx.kernel_launches - l0
+        iters, true_res = res.iterations, res.true_residual
+        value = ws * nrhs / (ms * 1e-3)
+
+        # end to end through the C ABI: pinned host rhs in, solve, solutions out
+        host_in = torch.empty(B.size * 2, dtype=torch.float64).pin_memory()
+        host_in.numpy()[:] = B.reshape(-1).view(np.float64)
+        host_out = torch.empty_like(host_in).pin_memory()
+        pin, pout = Cc.cast(host_in.data_ptr(), DP), Cc.cast(host_out.data_ptr(), DP)
+
+        def e2e_step():
+            smg._lib.check(lib.smg_field_upload_async(fb.h, pin), "upload", ctx.h)
+            step()
+            smg._lib.check(lib.smg_field_download_async(fx.h, pout), "download", ctx.h)
+
+        e2e_step()
+        e2e_ms = timed(e2e_step, max(1, min(args.steps, 3)))
+        sol = host_out.numpy().view(np.complex128).reshape(nrhs, -1)
+        hb = B.size * 16
+
+        # plain FP64 single-RHS MG (the denominator of the BASELINE target)
+        mg64 = smg.MGHierarchy(D, mg_params(smg, c, "f64"))
+        b1 = smg.Field(lat, 1, "f64", ctx, data=B[0])
+        x1 = smg.Field(lat, 1, "f64", ctx)
+        solve(mg64, b1, x1)
+        ms64 = timed(lambda: solve(mg64, b1, x1), 2)
+        it64 = res.iterations
+
+        # dominant kernel: the coarse-operator apply at level 1 on 32 RHS, timed alone
+        cms, cbytes = Cc.c_double(), Cc.c_double()
+        smg._lib.check(lib.smg_mg_time_coarse_apply(mg32.h, 1, nrhs, 20, Cc.byref(cms), Cc.byref(cbytes)),
+                       "smg_mg_time_coarse_apply", ctx.h)
+        achieved = cbytes.value / (cms.value * 1e-3) / 1e9
+        # fine operator: FP32 D on 32 RHS
+        f32s = smg.Field(lat, nrhs, "f32", ctx, data=B)
+        f32d = smg.Field(lat, nrhs, "f32", ctx)
+        dms = timed(lambda: smg._lib.check(lib.smg_dirac_apply(D.h, 0, f32s.h, f32d.h), "dirac", ctx.h), 20)
+        dgbs = dslash_bytes_f32(L, nrhs) / (dms * 1e-3) / 1e9
+        out.update({
+            "value": value, "unit": "solves/s", "ms_per_step": ms, "higher_is_better": True, "dtype": "f32+f64",
+            "config": {"workload": "MG-GCR, L=512 (beta=6, m=-0.05, c_sw=1), 32 RHS, 3 levels (4x4, 2x2; 16 dof), "
+                                   "FP64 GCR with FP32 hierarchy, true FP64 residual 1e-10",
+                       "L": L, "nrhs": nrhs, "levels": c["levels"], "gcr_iterations": iters,
+                       "true_residual": true_res, "setup_s": setup_s,
+                       "plain_fp64_mg_solves_per_s": 1e3 / ms64, "plain_fp64_mg_iterations": it64,
+                       "mixed_batched_over_plain_fp64": value / ws / (1e3 / ms64),
+                       "fine_dslash_f32_32rhs_gbs": dgbs, "fine_dslash_frac_of_hbm": dgbs / peak,
+                       "l2": "fine fields of 32 RHS (134 MB FP32, 268 MB FP64) exceed the 129 MB L2; no flush"},
+            "e2e": {"value": ws * nrhs / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": hb,
+                    "d2h_bytes_per_step": hb, "ms_per_step": e2e_ms, "finite": bool(np.isfinite(sol).all())},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "kernel": "k_coarse_apply_tiled<float,0,16> (level 1, 128x128x16, 32 RHS)",
+                         "bytes_per_launch": cbytes.value, "ms_per_launch": cms.value, "peak_source": peak_kind},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+        })
+    elif args.workload == "dslash":
         c = DSLASH
         L, nrhs = c["L"], c["nrhs"]
         U = smg.gauge_normal(L, c["beta"], c["seed"])
@@ -168,41 +273,36 @@ def run_ours(args, ws, rank, local):
             step()
         l0 = ctx.kernel_launches
         with Clocks(local) as clk:
-            ms = timed(step, args.steps)
-        launches = ctx.kernel_launches - l0
+            ms = timed(step, max(args.steps, 2000))
+        launches = (ctx.kernel_launches - l0) * args.steps // max(args.steps, 2000)
         value = ws * bytes_step / (ms * 1e-3) / 1e9
         achieved = bytes_step / (ms * 1e-3) / 1e9
-
-        # end to end through the C ABI with pinned host buffers, every step
         host_in = torch.empty(srcs.size * 2, dtype=torch.float64).pin_memory()
         host_in.numpy()[:] = srcs.reshape(-1).view(np.float64)
         host_out = torch.empty_like(host_in).pin_memory()
-        pin, pout = Cc.cast(host_in.data_ptr(), dp), Cc.cast(host_out.data_ptr(), dp)
+        pin, pout = Cc.cast(host_in.data_ptr(), DP), Cc.cast(host_out.data_ptr(), DP)
 
         def e2e_step():
             smg._lib.check(lib.smg_field_upload_async(fs.h, pin), "upload", ctx.h)
             step()
             smg._lib.check(lib.smg_field_download_async(fd.h, pout), "download", ctx.h)
 
-        for _ in range(2):
-            e2e_step()
+        e2e_step()
         e2e_ms = timed(e2e_step, args.steps)
-        got = host_out.numpy().view(np.complex128).reshape(nrhs, -1)
         hb = srcs.size * 16
         out.update({
             "value": value, "unit": "GB/s", "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
             "config": {"workload": "FP32 Wilson-clover D on 32 RHS, L=512 (beta=6, m=-0.05, c_sw=1)",
                        "L": L, "nrhs": nrhs, "bytes_per_step": bytes_step,
-                       "l2": "inputs and outputs (268 MB) exceed the 129 MB L2; no flush"},
+                       "l2": "inputs and outputs (268 MB) exceed the 129 MB L2; no flush",
+                       "timed_steps": max(args.steps, 2000)},
             "e2e": {"value": ws * bytes_step / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
-                    "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb, "ms_per_step": e2e_ms,
-                    "finite": bool(np.isfinite(got).all())},
+                    "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb, "ms_per_step": e2e_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "kernel": "k_dslash<float,false,0>", "peak_source": peak_kind},
-            "gpu_launches": int(launches),
-            "clocks": clk.summary(),
+            "gpu_launches": int(launches), "clocks": clk.summary(),
         })
-    elif args.workload == "cg":
+    else:
         c = CG
         L = c["L"]
         U = smg.gauge_normal(L, c["beta"], c["seed"])
@@ -215,8 +315,7 @@ def run_ours(args, ws, rank, local):
         res = smg._lib.SolveResult()
 
         def step():
-            st = lib.smg_cg_solve(D.h, fb.h, fx.h, c["max_iter"], c["tol"], Cc.byref(res))
-            smg._lib.check(st, "cg_solve", ctx.h)
+            smg._lib.check(lib.smg_cg_solve(D.h, fb.h, fx.h, c["max_iter"], c["tol"], Cc.byref(res)), "cg", ctx.h)
 
         for _ in range(args.warmup):
             step()
@@ -226,18 +325,14 @@ def run_ours(args, ws, rank, local):
         launches = ctx.kernel_launches - l0
         bh = b.copy()
         xh = np.empty_like(bh)
-        pb, px = bh.view(np.float64).ctypes.data_as(dp), xh.view(np.float64).ctypes.data_as(dp)
+        pb, px = bh.view(np.float64).ctypes.data_as(DP), xh.view(np.float64).ctypes.data_as(DP)
 
         def e2e_step():
             smg._lib.check(lib.smg_field_upload(fb.h, pb), "upload", ctx.h)
             step()
             smg._lib.check(lib.smg_field_download(fx.h, px), "download", ctx.h)
 
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            e2e_step()
-        e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-        e2e_ms = max_over_ranks(e2e_ms, ws)
+        e2e_ms = timed(e2e_step, args.steps)
         out.update({"value": ws * 1e3 / ms, "unit": "solves/s", "ms_per_step": ms, "higher_is_better": True,
                     "dtype": "f64",
                     "config": {"workload": "FP64 CG on D^dag D, L=32 (beta=2, m=0.1, c_sw=1) to 1e-10",
@@ -247,21 +342,11 @@ def run_ours(args, ws, rank, local):
                             "d2h_bytes_per_step": xh.nbytes, "ms_per_step": e2e_ms},
                     "gpu_launches": int(launches), "clocks": clk.summary()})
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(args.workload)
+        out["cpu_baseline"] = cpu_baseline(args.workload, ctx_objects=locals())
     return out
 
 
-def max_over_ranks(v: float, ws: int) -> float:
-    if ws == 1:
-        return v
-    import torch
-
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    return float(t.item())
-
-
-def cpu_baseline(workload: str, threads: int | None = None):
+def cpu_baseline(workload: str, threads: int | None = None, ctx_objects=None):
     """The oracle (C restatement of the reference's CPU path) on this host's cores, bounded sample."""
     from oracle import oracle as O
 
@@ -270,12 +355,30 @@ def cpu_baseline(workload: str, threads: int | None = None):
     port = O.port()
     n_threads = threads or os.cpu_count() or 1
     port.set_threads(n_threads)
+    if workload == "mg":
+        c = MG
+        L = c["L"]
+        mg32 = ctx_objects["mg32"] if ctx_objects else None
+        U = smg.gauge_normal(L, c["beta"], c["seed"])
+        if mg32 is None:
+            raise RuntimeError("the MG CPU baseline needs the hierarchy")
+        ncs = [mg32.level_dims(l + 1)[2] for l in range(c["levels"] - 1)]
+        bvs = [mg32.prolongator(l) for l in range(c["levels"] - 1)]
+        links = [None] + [mg32.coarse_op(l) for l in range(1, c["levels"])]
+        p = port.mgN_params(L, c["m"], c["r"], c["csw"], c["mu"], c["blocks"], ncs, bvs, links, c["pre"], c["post"],
+                            True, c["coarse_max_iter"], c["coarse_tol"])
+        b = smg.random_vec(2 * L * L, c["seed"] + 1)
+        _, it, res, sec = port.mgN_gcr(p, U, b, c["max_iter"], c["tol"], c["trunc"])
+        return {"value": 1.0 / sec, "unit": "solves/s", "cores": n_threads, "kind": "port",
+                "sample": f"one full solve of 1 RHS with the same 3-level hierarchy (the reference solves one "
+                          f"right-hand side at a time): {it} GCR iterations to {res:.1e}, {sec:.1f} s",
+                "seconds": sec}
     if workload == "dslash":
         c = DSLASH
         L, nrhs = c["L"], 8
         U = smg.gauge_normal(L, c["beta"], c["seed"])
         srcs = np.stack([smg.random_vec(2 * L * L, c["seed"] + 1 + j) for j in range(nrhs)])
-        port.time_dirac(U, c["m"], c["r"], c["csw"], c["mu"], 0, srcs[:1], 1)  # warm
+        port.time_dirac(U, c["m"], c["r"], c["csw"], c["mu"], 0, srcs[:1], 1)
         t, _ = port.time_dirac(U, c["m"], c["r"], c["csw"], c["mu"], 0, srcs, 2)
         gbs = 2 * nrhs * dslash_bytes_f64_single(L) / t / 1e9
         return {"value": gbs, "unit": "GB/s", "cores": n_threads, "kind": "port",
@@ -284,7 +387,7 @@ def cpu_baseline(workload: str, threads: int | None = None):
     c = CG
     U = smg.gauge_normal(c["L"], c["beta"], c["seed"])
     b = smg.random_vec(2 * c["L"] ** 2, c["seed"] + 1)
-    reps, tot = 0, 0.0
+    reps, tot, it = 0, 0.0, 0
     while tot < 5.0 and reps < 200:
         t, _, it = port.time_cg(U, c["m"], c["r"], c["csw"], c["mu"], b, c["max_iter"], c["tol"])
         tot += t
@@ -294,30 +397,41 @@ def cpu_baseline(workload: str, threads: int | None = None):
 
 
 def run_reference(args, ws, rank):
+    """The reference's CPU path (C restatement) on every host core, same workload and metric."""
     if rank != 0:
         return None
-    base = cpu_baseline(args.workload)
+    if args.workload == "mg":
+        # the hierarchy is built on the GPU (the reference's own build cannot run at this size: its deeper
+        # levels are dense), then every timed step runs on the CPU
+        import schwinger_mg_gb300 as smg
+
+        c = MG
+        ctx = smg.Context(0)
+        U = smg.gauge_normal(c["L"], c["beta"], c["seed"])
+        lat = smg.Lattice(c["L"])
+        D = smg.DiracOp(lat, smg.GaugeField(lat, U, ctx), c["m"], c["r"], c["csw"], c["mu"])
+        mg32 = smg.MGHierarchy(D, mg_params(smg, c, "f64"))
+        base = cpu_baseline("mg", ctx_objects={"mg32": mg32})
+    else:
+        base = cpu_baseline(args.workload)
     val = base["value"]
-    line = {"metric": METRIC, "impl": "reference", "value": val, "unit": base["unit"], "n_gpus": ws,
+    return {"metric": METRIC, "impl": "reference", "value": val, "unit": base["unit"], "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": args.workload},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": {"workload": args.workload},
             "cpu_baseline": {"kind": base["kind"], "cores": base["cores"], "sample": base["sample"], "value": val},
             "e2e": {"value": val, "unit": base["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    return line
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="dslash", choices=["dslash", "cg"])
+    ap.add_argument("--workload", default="mg", choices=["mg", "dslash", "cg"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
+    args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()
     if args.impl == "reference":
         line = run_reference(args, ws, rank)

@@ -275,6 +275,13 @@ SMG_API smg_status smg_mg_precondition(smg_mg* mg, const smg_field* b, smg_field
 SMG_API smg_status smg_mg_prolong_host(smg_mg* mg, int level, const double* coarse, double* fine);
 SMG_API smg_status smg_mg_restrict_host(smg_mg* mg, int level, const double* fine, double* coarse);
 SMG_API smg_status smg_mg_coarse_apply_host(smg_mg* mg, int level, const double* in, double* out);
+/* Benchmark support, no reference counterpart: device milliseconds of one
+ * application of the level-`level` coarse operator to nrhs right-hand sides
+ * in the hierarchy's precision, averaged over `reps` back-to-back
+ * applications timed with CUDA events on the context's stream, and the
+ * algorithmic HBM bytes of one application (links once, input and output
+ * vectors once). */
+SMG_API smg_status smg_mg_time_coarse_apply(smg_mg* mg, int level, int nrhs, int reps, double* ms, double* bytes);
 
 /* fcg_solve / fcg_solve_mg: truncated GCR on A = D^dag D from x = 0
  * (reference src/solvers.cpp:223-300, 803-811), preconditioned by one MG

@@ -60,6 +60,17 @@ class OrcMG2Params(C.Structure):
                 ("coarse_max_iter", C.c_int), ("coarse_tol", C.c_double)]
 
 
+MAXL = 6
+
+
+class OrcMGNParams(C.Structure):
+    _fields_ = [("n_levels", C.c_int), ("L", C.c_int), ("m", C.c_double), ("r", C.c_double), ("csw", C.c_double),
+                ("mu", C.c_double), ("block", (C.c_int * 2) * (MAXL - 1)), ("nc", C.c_int * (MAXL - 1)),
+                ("block_vecs", C.POINTER(C.c_double) * (MAXL - 1)), ("links", C.POINTER(C.c_double) * MAXL),
+                ("pre_smooth", C.c_int), ("post_smooth", C.c_int), ("w_cycle", C.c_int),
+                ("coarse_max_iter", C.c_int), ("coarse_tol", C.c_double)]
+
+
 class _Lib:
     """Common numpy-facing wrappers; `prefix` is 'orc_' (port) or 'ref_' (reference)."""
 
@@ -213,6 +224,45 @@ class Port(_Lib):
         t = self.lib.orc_time_cg(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
                                  C.c_double(mu), _p(b), _p(x), C.c_int(max_iter), C.c_double(tol), C.byref(it))
         return t, x, it.value
+
+    def mgN_params(self, L, m, r, csw, mu, blocks, ncs, block_vecs, links, pre, post, w_cycle, coarse_max_iter,
+                   coarse_tol):
+        """Builds orc_mgN_params; the returned object keeps the arrays alive."""
+        p = OrcMGNParams()
+        p.n_levels = len(blocks) + 1
+        p.L, p.m, p.r, p.csw, p.mu = L, m, r, csw, mu
+        keep = []
+        for l, (b, nc, bv) in enumerate(zip(blocks, ncs, block_vecs)):
+            p.block[l][0], p.block[l][1] = b
+            p.nc[l] = nc
+            a = _c(bv)
+            keep.append(a)
+            p.block_vecs[l] = _p(a)
+        for l, lk in enumerate(links):
+            if lk is None:
+                continue
+            a = _c(lk)
+            keep.append(a)
+            p.links[l] = _p(a)
+        p.pre_smooth, p.post_smooth, p.w_cycle = pre, post, int(w_cycle)
+        p.coarse_max_iter, p.coarse_tol = coarse_max_iter, coarse_tol
+        p._keep = keep
+        return p
+
+    def mgN_precondition(self, p, U, b):
+        U, b = _c(U), _c(b)
+        out = np.empty_like(b)
+        self.lib.orc_mgN_precondition(C.byref(p), _p(U), _p(b), _p(out))
+        return out
+
+    def mgN_gcr(self, p, U, b, max_iter, tol, trunc):
+        U, b = _c(U), _c(b)
+        x = np.empty_like(b)
+        res, sec = C.c_double(0), C.c_double(0)
+        self.lib.orc_mgN_gcr.restype = C.c_int
+        it = self.lib.orc_mgN_gcr(C.byref(p), _p(U), _p(b), _p(x), C.c_int(max_iter), C.c_double(tol),
+                                  C.c_int(trunc), C.byref(res), C.byref(sec))
+        return x, it, res.value, sec.value
 
     def set_threads(self, n: int) -> None:
         self.lib.orc_set_threads(C.c_int(n))

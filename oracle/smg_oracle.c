@@ -984,3 +984,263 @@ double orc_time_cg(int L, const double* U, double m, double r, double csw, doubl
     d_free(&D);
     return t1 - t0;
 }
+
+/* ------------------------------------------------------------ N-level MG */
+/* mg_cycle over a hierarchy of sparse stencil levels (reference
+ * src/multigrid.cpp:43-102): MR pre-smoothing (mr_smooth_op,
+ * src/smoother.cpp:26-40), residual, restriction, coarse cycle (twice with the
+ * W-cycle when the next level is not the coarsest), prolongation, MR
+ * post-smoothing; coarsest level by CG (src/coarse_op.h:492-547).  Level 0 is
+ * D^dag D; level l >= 1 a 9-point stencil (SparseCoarseOp::apply_to).
+ * Transfers l -> l+1 aggregate ax x ay sites with block vectors in the layout
+ * [aggregate][i][loc * ndof_l + j] (Prolongator::block_vecs,
+ * src/prolongator.h:23; CoarseProlongator for deeper levels). */
+
+typedef struct {
+    int nx, ny, ndof;     /* lattice and dofs of this level */
+    int ax, ay, nc;       /* transfer to the next level */
+    cxd* bv;              /* block vectors of the transfer, [agg][i][loc*ndof + j] */
+    Coarse A;             /* operator of this level (l >= 1) */
+    cxd* lk;
+} NLevel;
+
+typedef struct {
+    const orc_mgN_params* p;
+    Dirac D;
+    int nl;
+    NLevel lv[ORC_MAX_LEVELS];
+} MGN;
+
+static void n_restrict(const NLevel* L, const cxd* f, cxd* c) {
+    const int nax = L->nx / L->ax, nay = L->ny / L->ay, m = L->ax * L->ay, nd = L->ndof;
+#pragma omp parallel for schedule(static) if (nax * nay > 64)
+    for (int B = 0; B < nax * nay; ++B) {
+        const int x0 = (B % nax) * L->ax, y0 = (B / nax) * L->ay;
+        for (int i = 0; i < L->nc; ++i) {
+            const cxd* v = L->bv + ((long)B * L->nc + i) * m * nd;
+            cxd acc = 0;
+            for (int loc = 0; loc < m; ++loc) {
+                int s = (x0 + loc % L->ax) + L->nx * (y0 + loc / L->ax);
+                for (int j = 0; j < nd; ++j) acc += conj(v[loc * nd + j]) * f[(long)s * nd + j];
+            }
+            c[(long)B * L->nc + i] = acc;
+        }
+    }
+}
+
+static void n_prolong_add(const NLevel* L, const cxd* c, cxd* f) {
+    const int nax = L->nx / L->ax, m = L->ax * L->ay, nd = L->ndof;
+    const int ns = L->nx * L->ny;
+#pragma omp parallel for schedule(static) if (ns > 256)
+    for (int s = 0; s < ns; ++s) {
+        const int x = s % L->nx, y = s / L->nx;
+        const int B = x / L->ax + nax * (y / L->ay), loc = (x % L->ax) + L->ax * (y % L->ay);
+        for (int j = 0; j < nd; ++j) {
+            cxd acc = 0;
+            for (int i = 0; i < L->nc; ++i) acc += c[(long)B * L->nc + i] * L->bv[((long)B * L->nc + i) * m * nd + loc * nd + j];
+            f[(long)s * nd + j] += acc;
+        }
+    }
+}
+
+/* level-0 vectors are lexicographic v[2*s + spin], the same layout */
+static void n_apply(const MGN* g, int l, const cxd* x, cxd* y) {
+    if (l == 0)
+        d_apply_DdagD(&g->D, x, y);
+    else
+        c_apply(&g->lv[l].A, x, y);
+}
+
+static long n_dim(const MGN* g, int l) { return (long)g->lv[l].nx * g->lv[l].ny * g->lv[l].ndof; }
+
+/* mr_smooth_op with the residual recomputed every step, as the reference */
+static void n_mr(const MGN* g, int l, cxd* x, const cxd* b, int niter) {
+    long n = n_dim(g, l);
+    cxd* r = (cxd*)malloc(sizeof(cxd) * (size_t)n);
+    cxd* Ar = (cxd*)malloc(sizeof(cxd) * (size_t)n);
+    for (int it = 0; it < niter; ++it) {
+        n_apply(g, l, x, r);
+        for (long i = 0; i < n; ++i) r[i] = b[i] - r[i];
+        n_apply(g, l, r, Ar);
+        cxd rAr = v_dot(Ar, r, n), ArAr = v_dot(Ar, Ar, n);
+        if (cabs(ArAr) < 1e-30) break;
+        v_axpy(rAr / ArAr, r, x, n);
+    }
+    free(r);
+    free(Ar);
+}
+
+static void n_cycle(const MGN* g, int l, const cxd* b, cxd* x) {
+    const int last = g->nl - 1;
+    long n = n_dim(g, l);
+    if (l == last) {
+        c_cg(&g->lv[l].A, b, x, g->p->coarse_max_iter, g->p->coarse_tol);
+        return;
+    }
+    memset(x, 0, sizeof(cxd) * (size_t)n);
+    n_mr(g, l, x, b, g->p->pre_smooth);
+    cxd* r = (cxd*)malloc(sizeof(cxd) * (size_t)n);
+    n_apply(g, l, x, r);
+    for (long i = 0; i < n; ++i) r[i] = b[i] - r[i];
+    long nc = n_dim(g, l + 1);
+    cxd* rc = (cxd*)malloc(sizeof(cxd) * (size_t)nc);
+    cxd* ec = (cxd*)malloc(sizeof(cxd) * (size_t)nc);
+    n_restrict(&g->lv[l], r, rc);
+    n_cycle(g, l + 1, rc, ec);
+    if (g->p->w_cycle && l + 1 < last) {
+        cxd* Ae = (cxd*)malloc(sizeof(cxd) * (size_t)nc);
+        cxd* e2 = (cxd*)malloc(sizeof(cxd) * (size_t)nc);
+        n_apply(g, l + 1, ec, Ae);
+        for (long i = 0; i < nc; ++i) Ae[i] = rc[i] - Ae[i];
+        n_cycle(g, l + 1, Ae, e2);
+        for (long i = 0; i < nc; ++i) ec[i] += e2[i];
+        free(Ae);
+        free(e2);
+    }
+    n_prolong_add(&g->lv[l], ec, x);
+    n_mr(g, l, x, b, g->p->post_smooth);
+    free(r);
+    free(rc);
+    free(ec);
+}
+
+static MGN n_make(const orc_mgN_params* p, const double* U) {
+    MGN g;
+    memset(&g, 0, sizeof(g));
+    g.p = p;
+    g.D = d_make(p->L, U, p->m, p->r, p->csw, p->mu);
+    g.nl = p->n_levels;
+    int nx = p->L, ny = p->L, nd = 2;
+    for (int l = 0; l < g.nl; ++l) {
+        NLevel* L = &g.lv[l];
+        L->nx = nx;
+        L->ny = ny;
+        L->ndof = nd;
+        if (l >= 1) {
+            L->lk = to_cx(p->links[l], (long)nx * ny * 9 * nd * nd);
+            L->A.nbx = nx;
+            L->A.nby = ny;
+            L->A.k = nd;
+            L->A.dim = nx * ny * nd;
+            L->A.lk = L->lk;
+        }
+        if (l < g.nl - 1) {
+            L->ax = p->block[l][0];
+            L->ay = p->block[l][1];
+            L->nc = p->nc[l];
+            L->bv = to_cx(p->block_vecs[l], (long)nx * ny * nd * L->nc);
+            nx /= L->ax;
+            ny /= L->ay;
+            nd = L->nc;
+        }
+    }
+    return g;
+}
+
+static void n_free(MGN* g) {
+    d_free(&g->D);
+    for (int l = 0; l < g->nl; ++l) {
+        free(g->lv[l].bv);
+        free(g->lv[l].lk);
+    }
+}
+
+void orc_mgN_precondition(const orc_mgN_params* p, const double* U, const double* b, double* out) {
+    MGN g = n_make(p, U);
+    long n = n_dim(&g, 0);
+    cxd* bb = to_cx(b, n);
+    cxd* xx = (cxd*)malloc(sizeof(cxd) * (size_t)n);
+    n_cycle(&g, 0, bb, xx);
+    from_cx(xx, n, out);
+    free(bb);
+    free(xx);
+    n_free(&g);
+}
+
+/* fcg_solve with the N-level preconditioner, projection coefficient; stops
+ * after max_iter iterations or at tol; *seconds = wall time of the iterations */
+int orc_mgN_gcr(const orc_mgN_params* p, const double* U, const double* bh, double* xh, int max_iter, double tol,
+                int trunc, double* final_res, double* seconds) {
+    MGN g = n_make(p, U);
+    long n = n_dim(&g, 0);
+    cxd* rhs = to_cx(bh, n);
+    double rhs_norm = v_norm(rhs, n);
+    cxd* x = (cxd*)calloc((size_t)n, sizeof(cxd));
+    cxd* r = (cxd*)malloc(sizeof(cxd) * (size_t)n);
+    memcpy(r, rhs, sizeof(cxd) * (size_t)n);
+    cxd** Pd = (cxd**)calloc((size_t)trunc + 1, sizeof(cxd*));
+    cxd** APd = (cxd**)calloc((size_t)trunc + 1, sizeof(cxd*));
+    double* ApAp = (double*)calloc((size_t)trunc + 1, sizeof(double));
+    cxd* z = (cxd*)malloc(sizeof(cxd) * (size_t)n);
+    cxd* Az = (cxd*)malloc(sizeof(cxd) * (size_t)n);
+    int nd = 0, iter = 0;
+#ifdef _OPENMP
+    double t0 = omp_get_wtime();
+#endif
+    while (rhs_norm >= 1e-30 && iter < max_iter) {
+        if (v_norm(r, n) / rhs_norm < tol) break;
+        n_cycle(&g, 0, r, z);
+        d_apply_DdagD(&g.D, z, Az);
+        cxd* pp = (cxd*)malloc(sizeof(cxd) * (size_t)n);
+        cxd* Ap = (cxd*)malloc(sizeof(cxd) * (size_t)n);
+        memcpy(pp, z, sizeof(cxd) * (size_t)n);
+        memcpy(Ap, Az, sizeof(cxd) * (size_t)n);
+        for (int i = 0; i < nd; ++i) {
+            cxd beta = v_dot(APd[i], Az, n) / ApAp[i];
+            for (long j = 0; j < n; ++j) {
+                pp[j] -= beta * Pd[i][j];
+                Ap[j] -= beta * APd[i][j];
+            }
+        }
+        double ApAp_val = creal(v_dot(Ap, Ap, n));
+        if (ApAp_val < 1e-30) {
+            for (int i = 0; i < nd; ++i) {
+                free(Pd[i]);
+                free(APd[i]);
+            }
+            nd = 0;
+            free(pp);
+            free(Ap);
+            continue;
+        }
+        cxd alpha = v_dot(Ap, r, n) / ApAp_val;
+        for (long j = 0; j < n; ++j) {
+            x[j] += alpha * pp[j];
+            r[j] -= alpha * Ap[j];
+        }
+        iter++;
+        if (nd >= trunc) {
+            free(Pd[0]);
+            free(APd[0]);
+            memmove(Pd, Pd + 1, sizeof(cxd*) * (size_t)(nd - 1));
+            memmove(APd, APd + 1, sizeof(cxd*) * (size_t)(nd - 1));
+            memmove(ApAp, ApAp + 1, sizeof(double) * (size_t)(nd - 1));
+            nd--;
+        }
+        Pd[nd] = pp;
+        APd[nd] = Ap;
+        ApAp[nd] = ApAp_val;
+        nd++;
+    }
+#ifdef _OPENMP
+    if (seconds) *seconds = omp_get_wtime() - t0;
+#else
+    if (seconds) *seconds = 0;
+#endif
+    if (final_res) *final_res = rhs_norm >= 1e-30 ? v_norm(r, n) / rhs_norm : 0.0;
+    from_cx(x, n, xh);
+    for (int i = 0; i < nd; ++i) {
+        free(Pd[i]);
+        free(APd[i]);
+    }
+    free(Pd);
+    free(APd);
+    free(ApAp);
+    free(z);
+    free(Az);
+    free(x);
+    free(r);
+    free(rhs);
+    n_free(&g);
+    return iter;
+}

@@ -70,6 +70,25 @@ int orc_mg2_gcr(const orc_mg2_params* p, const double* U, const double* block_ve
                 const double* b, double* x, int max_iter, double tol, int trunc, int ref_coeff,
                 double* final_res);
 
+/* N-level MG on a given hierarchy (block vectors and coarse operators as
+ * returned by smg_mg_get_prolongator / smg_mg_get_coarse_op).  links[0] is
+ * unused (level 0 is D^dag D). */
+#define ORC_MAX_LEVELS 6
+typedef struct {
+    int n_levels, L;
+    double m, r, csw, mu;
+    int block[ORC_MAX_LEVELS - 1][2];
+    int nc[ORC_MAX_LEVELS - 1];
+    const double* block_vecs[ORC_MAX_LEVELS - 1];
+    const double* links[ORC_MAX_LEVELS];
+    int pre_smooth, post_smooth, w_cycle, coarse_max_iter;
+    double coarse_tol;
+} orc_mgN_params;
+
+void orc_mgN_precondition(const orc_mgN_params* p, const double* U, const double* b, double* out);
+int orc_mgN_gcr(const orc_mgN_params* p, const double* U, const double* b, double* x, int max_iter, double tol,
+                int trunc, double* final_res, double* seconds);
+
 /* CPU timing of the restatement (bench.py's CPU baseline): seconds for `reps`
  * applications of D (op 0) or D^dag D (op 2) to nrhs spinors, and for one CG
  * solve; the operator is set up outside the timed region. */

@@ -104,6 +104,7 @@ _SIGS = {
     "smg_mg_prolong_host": (_st, [_vp, C.c_int, _dp, _dp]),
     "smg_mg_restrict_host": (_st, [_vp, C.c_int, _dp, _dp]),
     "smg_mg_coarse_apply_host": (_st, [_vp, C.c_int, _dp, _dp]),
+    "smg_mg_time_coarse_apply": (_st, [_vp, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     "smg_gcr_solve": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(SolveResult)]),
     "smg_host_gauge_normal": (_st, [C.c_int, C.c_double, C.c_uint32, _dp]),
     "smg_host_random_vec": (_st, [C.c_int64, C.c_uint32, _dp]),

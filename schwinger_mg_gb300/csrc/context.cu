@@ -10,9 +10,9 @@ smg_status smg_fail(smg_context* ctx, smg_status s, const std::string& msg) {
 
 smg_status smg_reduce_reserve(smg_context* ctx, size_t doubles) {
     if (ctx->red.capacity >= doubles) return SMG_OK;
-    // the scratch may be in use by kernels already queued on the stream
-    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (ctx->red.partials) cudaFree(ctx->red.partials);
+    // kernels already queued (or captured in a graph) may still use the old
+    // buffer, so it is retired rather than freed
+    if (ctx->red.partials) ctx->retired.push_back(ctx->red.partials);
     ctx->red.partials = nullptr;
     ctx->red.capacity = 0;
     size_t cap = doubles < (1u << 16) ? (1u << 16) : doubles;
@@ -93,6 +93,7 @@ SMG_API smg_status smg_context_destroy(smg_context* ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     if (ctx->red.partials) cudaFree(ctx->red.partials);
+    for (double* p : ctx->retired) cudaFree(p);
     if (ctx->red.tickets) cudaFree(ctx->red.tickets);
     if (ctx->host_stage) cudaFreeHost(ctx->host_stage);
     if (ctx->ev_begin) cudaEventDestroy(ctx->ev_begin);

@@ -391,7 +391,8 @@ __global__ void k_galerkin_c(const cx<double>* __restrict__ Lk, const cx<double>
 template <typename T, int EPI>
 __global__ void __launch_bounds__(256) k_coarse_apply(const cx<T>* __restrict__ A, VecView<T> xin, cx<T>* __restrict__ y,
                                                       int nx, int ny, const cx<T>* __restrict__ w, double* partials,
-                                                      unsigned int* ticket, double* out) {
+                                                      unsigned int* ticket, double* out, const int* __restrict__ gate) {
+    if (gate && *gate == 0) return;  // every right-hand side of the solve has converged
     constexpr int K = EPI == 2 ? 3 : 1;
     const int nc = xin.ndof, nrhs = xin.nrhs;
     const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
@@ -427,6 +428,297 @@ __global__ void __launch_bounds__(256) k_coarse_apply(const cx<T>* __restrict__ 
         }
     }
     if (EPI != 0) block_reduce_finalise<K>(v, partials, ticket, nrhs, FinStore{out, K});
+}
+
+// Single-RHS coarse apply: one thread per (site, i) row with the j loop
+// unrolled, so each thread has all Nc link and vector loads of a direction in
+// flight (the generic kernel's dependent j loop is latency-bound).
+template <typename T, int EPI, int NC>
+__global__ void __launch_bounds__(256) k_coarse_apply1(const cx<T>* __restrict__ A, VecView<T> xin,
+                                                       cx<T>* __restrict__ y, int nx, int ny,
+                                                       const cx<T>* __restrict__ w, double* partials,
+                                                       unsigned int* ticket, double* out, const int* __restrict__ gate) {
+    if (gate && *gate == 0) return;
+    constexpr int K = EPI == 2 ? 3 : 1;
+    double v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = 0.0;
+    const int64_t nrow = (int64_t)xin.nsites * NC;
+    for (int64_t row = (int64_t)blockIdx.x * blockDim.y + threadIdx.y; row < nrow;
+         row += (int64_t)gridDim.x * blockDim.y) {
+        const int s = (int)(row / NC), i = (int)(row % NC);
+        const int x = s % nx, yy = s / nx;
+        cx<T> acc = mk<T>(0, 0);
+#pragma unroll 3
+        for (int d = 0; d < 9; ++d) {
+            const int xn = x + c_dx[d], yn = yy + c_dy[d];
+            const int sn = (xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn)) +
+                           nx * (yn < 0 ? yn + ny : (yn >= ny ? yn - ny : yn));
+            const cx<T>* Ad = A + ((int64_t)s * 9 + d) * NC * NC + i;
+            const cx<T>* xv = xin.p + (int64_t)sn * NC;
+#pragma unroll
+            for (int j = 0; j < NC; ++j) acc = acc + Ad[j * NC] * xv[j];
+        }
+        y[row] = acc;
+        if (EPI == 1) {
+            v[0] += (double)norm2(acc);
+        } else if (EPI == 2) {
+            const cx<T> c = cmulc(acc, w[row]);
+            v[0] += (double)c.re;
+            v[1] += (double)c.im;
+            v[2] += (double)norm2(acc);
+        }
+    }
+    if (EPI != 0) block_reduce_finalise<K>(v, partials, ticket, 1, FinStore{out, K});
+}
+
+// Multi-RHS coarse apply, one coarse site per block iteration: for each of
+// the 9 directions the Nc x Nc link block and the neighbour's Nc x R vector
+// block (R right-hand sides of one lane chunk) are staged in shared memory,
+// then thread (r, row) accumulates y(i, r) for i = row, row + rows, ...
+// Rows of the staged vector block are padded by one complex so the RHS lanes
+// of a warp hit distinct banks.  Epilogue reductions as k_coarse_apply.
+template <typename T, int EPI, int NC>
+__global__ void __launch_bounds__(256) k_coarse_apply_tiled(const cx<T>* __restrict__ A, VecView<T> xin,
+                                                            cx<T>* __restrict__ y, int nx, int ny,
+                                                            const cx<T>* __restrict__ w, double* partials,
+                                                            unsigned int* ticket, double* out,
+                                                            const int* __restrict__ gate) {
+    if (gate && *gate == 0) return;  // every right-hand side of the solve has converged
+    constexpr int K = EPI == 2 ? 3 : 1;
+    constexpr int kPer = (NC + 7) / 8;  // outputs per thread; blockDim.y >= 8
+    __shared__ cx<T> sA[NC * NC];       // [j][i]
+    __shared__ cx<T> sX[32][NC + 1];    // [r][j]
+    const int lanes = blockDim.x, rows = blockDim.y;
+    const int nrhs = xin.nrhs;
+    const int r0 = blockIdx.y * lanes;
+    const int rhs = r0 + threadIdx.x;
+    const int tid = threadIdx.y * lanes + threadIdx.x, nthr = lanes * rows;
+    double v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = 0.0;
+    for (int s = blockIdx.x; s < xin.nsites; s += gridDim.x) {
+        const int x = s % nx, yy = s / nx;
+        cx<T> acc[kPer];
+#pragma unroll
+        for (int a = 0; a < kPer; ++a) acc[a] = mk<T>(0, 0);
+        for (int d = 0; d < 9; ++d) {
+            const int xn = x + c_dx[d], yn = yy + c_dy[d];
+            const int sn = (xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn)) +
+                           nx * (yn < 0 ? yn + ny : (yn >= ny ? yn - ny : yn));
+            __syncthreads();
+            const cx<T>* Ad = A + ((int64_t)s * 9 + d) * NC * NC;
+            for (int t = tid; t < NC * NC; t += nthr) sA[t] = Ad[t];
+            const cx<T>* Xn = xin.p + ((int64_t)sn * nrhs + r0) * NC;
+            for (int t = tid; t < lanes * NC; t += nthr) {
+                const int r = t / NC, j = t - r * NC;
+                sX[r][j] = (r0 + r < nrhs) ? Xn[t] : mk<T>(0, 0);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int a = 0; a < kPer; ++a) {
+                const int i = threadIdx.y + a * rows;
+                if (i < NC) {
+                    cx<T> sum = acc[a];
+#pragma unroll
+                    for (int j = 0; j < NC; ++j) sum = sum + sA[j * NC + i] * sX[threadIdx.x][j];
+                    acc[a] = sum;
+                }
+            }
+        }
+        if (rhs < nrhs) {
+#pragma unroll
+            for (int a = 0; a < kPer; ++a) {
+                const int i = threadIdx.y + a * rows;
+                if (i < NC) {
+                    const int64_t o = ((int64_t)s * nrhs + rhs) * NC + i;
+                    y[o] = acc[a];
+                    if (EPI == 1) {
+                        v[0] += (double)norm2(acc[a]);
+                    } else if (EPI == 2) {
+                        const cx<T> c = cmulc(acc[a], w[o]);
+                        v[0] += (double)c.re;
+                        v[1] += (double)c.im;
+                        v[2] += (double)norm2(acc[a]);
+                    }
+                }
+            }
+        }
+    }
+    if (EPI != 0) block_reduce_finalise<K>(v, partials, ticket, nrhs, FinStore{out, K});
+}
+
+// ------------------------------------------------------------ persistent coarsest CG
+// The whole coarsest-level CG of one right-hand side in one cooperative
+// launch (SparseCoarseOp::solve without deflation, src/coarse_op.h:492-547).
+// Per iteration: Ap = A p with the partial <p, Ap> of each block, barrier;
+// x += alpha p, r -= alpha Ap with the partial ||r||^2, barrier; p = r + beta p,
+// barrier.  Every block sums the per-block partials itself in block order, so
+// all blocks take identical (deterministic) scalar decisions without a further
+// barrier.  Every barrier wait is bounded; on timeout the kernel raises
+// *err and returns.
+struct CoarseCgArgs {
+    const void* A = nullptr;
+    const void* b = nullptr;
+    void* x = nullptr;
+    void* r = nullptr;
+    void* p = nullptr;
+    void* Ap = nullptr;
+    int nx = 0, ny = 0, nsites = 0, max_iter = 0;
+    double tol2 = 0;
+    double* part = nullptr;        // [2][gridDim.x]
+    unsigned int* bar = nullptr;   // [0] arrivals, [1] generation
+    int* err = nullptr;            // 0 ok, 1 barrier timeout
+    int* iters = nullptr;          // iterations done (written by block 0)
+};
+
+constexpr long long kBarrierSpinLimit = 1ll << 22;  // x 256 ns sleep ~ 1 s
+
+__device__ __forceinline__ bool grid_barrier(unsigned int* bar, int* err) {
+    __syncthreads();
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        volatile unsigned int* vgen = bar + 1;
+        volatile int* verr = err;
+        if (*verr) {
+            ok = 0;
+        } else {
+            const unsigned int gen = *vgen;
+            __threadfence();
+            const unsigned int arrived = atomicAdd(bar, 1u);
+            if (arrived == gridDim.x - 1) {
+                bar[0] = 0u;
+                __threadfence();
+                atomicAdd(bar + 1, 1u);
+            } else {
+                long long k = 0;
+                while (*vgen == gen) {
+                    if (*verr || ++k > kBarrierSpinLimit) {
+                        atomicExch(err, 1);
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(256);
+                }
+            }
+            __threadfence();
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// block sum of v (256 threads), result valid in every thread
+__device__ __forceinline__ double block_sum256(double v) {
+    __shared__ double s_w[8];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0;
+    for (int w = 0; w < 8; ++w) t += s_w[w];
+    return t;
+}
+
+// every block sums part[0 .. gridDim.x) in order (identical result everywhere)
+__device__ __forceinline__ double sum_partials(const double* part) {
+    __shared__ double s_tot;
+    if (threadIdx.x < 32) {
+        double t = 0;
+        for (int i = threadIdx.x; i < (int)gridDim.x; i += 32) t += __ldcg(part + i);
+        for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) s_tot = t;
+    }
+    __syncthreads();
+    return s_tot;
+}
+
+// L2-coherent load of a complex written by another block during this kernel
+__device__ __forceinline__ cx<float> ldcg_cx(const cx<float>* q) {
+    float2 v = __ldcg(reinterpret_cast<const float2*>(q));
+    return mk(v.x, v.y);
+}
+__device__ __forceinline__ cx<double> ldcg_cx(const cx<double>* q) {
+    double2 v = __ldcg(reinterpret_cast<const double2*>(q));
+    return mk(v.x, v.y);
+}
+
+template <typename T, int NC>
+__global__ void __launch_bounds__(256) k_coarse_cg1(CoarseCgArgs a) {
+    const cx<T>* A = (const cx<T>*)a.A;
+    const cx<T>* b = (const cx<T>*)a.b;
+    cx<T>* x = (cx<T>*)a.x;
+    cx<T>* r = (cx<T>*)a.r;
+    cx<T>* p = (cx<T>*)a.p;
+    cx<T>* Ap = (cx<T>*)a.Ap;
+    const int n = a.nsites * NC;
+    const int stride = gridDim.x * blockDim.x;
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+    double* part0 = a.part;              // <p, Ap> partials
+    double* part1 = a.part + gridDim.x;  // ||r||^2 partials
+    // x = 0, r = p = b (each element is owned by one thread for the whole solve)
+    double loc = 0;
+    for (int e = t0; e < n; e += stride) {
+        const cx<T> v = b[e];
+        x[e] = mk<T>(0, 0);
+        r[e] = v;
+        p[e] = v;
+        loc += (double)norm2(v);
+    }
+    loc = block_sum256(loc);
+    if (threadIdx.x == 0) part1[blockIdx.x] = loc;
+    if (!grid_barrier(a.bar, a.err)) return;
+    double rr = sum_partials(part1);
+    const double bnorm2 = rr;
+    int it = 0;
+    const bool solve = bnorm2 >= 1e-60 && isfinite(bnorm2);  // ||b|| < 1e-30 returns x = 0
+    while (solve && it < a.max_iter) {
+        // Ap = A p, partial <Ap, p>
+        double pap = 0;
+        for (int e = t0; e < n; e += stride) {
+            const int s = e / NC, i = e - s * NC;
+            const int xs = s % a.nx, ys = s / a.nx;
+            cx<T> acc = mk<T>(0, 0);
+#pragma unroll 3
+            for (int d = 0; d < 9; ++d) {
+                const int xn = xs + c_dx[d], yn = ys + c_dy[d];
+                const int sn = (xn < 0 ? xn + a.nx : (xn >= a.nx ? xn - a.nx : xn)) +
+                               a.nx * (yn < 0 ? yn + a.ny : (yn >= a.ny ? yn - a.ny : yn));
+                const cx<T>* Ad = A + ((int64_t)s * 9 + d) * NC * NC + i;
+                const cx<T>* pv = p + (int64_t)sn * NC;
+#pragma unroll
+                for (int j = 0; j < NC; ++j) acc = acc + Ad[j * NC] * ldcg_cx(pv + j);
+            }
+            Ap[e] = acc;
+            pap += (double)cmulc(acc, p[e]).re;
+        }
+        pap = block_sum256(pap);
+        if (threadIdx.x == 0) part0[blockIdx.x] = pap;
+        if (!grid_barrier(a.bar, a.err)) return;
+        pap = sum_partials(part0);
+        if (!(fabs(pap) >= 1e-30) || !isfinite(pap)) break;  // coarse_op.h:522
+        const T al = (T)(rr / pap);
+        double rloc = 0;
+        for (int e = t0; e < n; e += stride) {
+            const cx<T> ri = r[e] - al * Ap[e];
+            x[e] = x[e] + al * p[e];
+            r[e] = ri;
+            rloc += (double)norm2(ri);
+        }
+        rloc = block_sum256(rloc);
+        if (threadIdx.x == 0) part1[blockIdx.x] = rloc;
+        if (!grid_barrier(a.bar, a.err)) return;
+        const double rr_new = sum_partials(part1);
+        ++it;
+        if (!isfinite(rr_new) || rr_new < a.tol2 * bnorm2) break;  // coarse_op.h:531-536
+        const T be = (T)(rr_new / rr);
+        rr = rr_new;
+        for (int e = t0; e < n; e += stride) p[e] = r[e] + be * p[e];
+        if (!grid_barrier(a.bar, a.err)) return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters = it;
 }
 
 template <typename D, typename S>
@@ -483,6 +775,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_ccg_update(CcgState s, VecView<T> x, cx<T>* __restrict__ r,
                                                     const cx<T>* __restrict__ p, const cx<T>* __restrict__ Ap,
                                                     double* partials, unsigned int* ticket) {
+    if (*s.n_active == 0) return;  // read by every block before the finaliser can change it
     __shared__ T s_al[32];
     const int nrhs = x.nrhs;
     const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
@@ -514,6 +807,7 @@ __global__ void __launch_bounds__(256) k_ccg_update(CcgState s, VecView<T> x, cx
 
 template <typename T>
 __global__ void k_ccg_p(CcgState s, VecView<T> p, const cx<T>* __restrict__ r) {
+    if (*s.n_active == 0) return;
     const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
     const int st = blockIdx.x * blockDim.y + threadIdx.y;
     if (rhs >= p.nrhs || st >= p.nsites) return;
@@ -548,6 +842,18 @@ struct smg_mg {
     std::vector<CoarseWork> cw;
     double* scal = nullptr;  // per-level scalar area
     size_t scal_doubles = 0;
+    // CUDA graph of one cycle on internal input/output fields, per (nrhs, precision)
+    bool capturing = false;
+    bool use_graph = true;
+    smg_field* g_in = nullptr;
+    smg_field* g_out = nullptr;
+    cudaGraphExec_t g_exec = nullptr;
+    uint64_t g_launches = 0;
+    uint64_t work_gen = 0;   // bumped whenever the workspace is reallocated
+    uint64_t g_work_gen = 0; // workspace generation the graph was captured with
+    // persistent coarsest CG: barrier words, error flag, iteration count, partials
+    bool persistent = true;
+    void* cg_state = nullptr;  // [0..1] barrier, [2] err, [3] iters (ints), doubles from byte 256
 };
 
 namespace {
@@ -575,6 +881,17 @@ VecView<T> fview(const smg_field* f) {
     v.nsites = f->g.V;
     v.nrhs = f->nrhs;
     v.ndof = 2;
+    return v;
+}
+
+// a single-RHS vector viewed as a flat array of single-dof sites, so the
+// elementwise and reduction kernels get one thread per complex entry
+template <typename T>
+VecView<T> flat(VecView<T> v) {
+    if (v.nrhs == 1) {
+        v.nsites *= v.ndof;
+        v.ndof = 1;
+    }
     return v;
 }
 
@@ -611,22 +928,74 @@ smg_status vaxpy(smg_context* ctx, VecView<T> y, const cx<T>* x, const double* c
     return SMG_OK;
 }
 
+template <typename T, int NC>
+smg_status coarse_apply_tiled(smg_context* ctx, const Level& L, const cx<T>* A, VecView<T> x, cx<T>* y, int epi,
+                              const cx<T>* w, double* out, const int* gate) {
+    ReduceLaunch rl = reduce_launch(L.nsites, x.nrhs);  // lanes = rhs lanes, rows = 256 / lanes >= 8
+    SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * x.nrhs * 3));
+    if (epi == 0)
+        k_coarse_apply_tiled<T, 0, NC><<<rl.grid, rl.block, 0, ctx->stream>>>(A, x, y, L.nx, L.ny, w, nullptr,
+                                                                             nullptr, nullptr, gate);
+    else if (epi == 1)
+        k_coarse_apply_tiled<T, 1, NC><<<rl.grid, rl.block, 0, ctx->stream>>>(A, x, y, L.nx, L.ny, w,
+                                                                             ctx->red.partials, ctx->red.tickets, out,
+                                                                             gate);
+    else
+        k_coarse_apply_tiled<T, 2, NC><<<rl.grid, rl.block, 0, ctx->stream>>>(A, x, y, L.nx, L.ny, w,
+                                                                             ctx->red.partials, ctx->red.tickets, out,
+                                                                             gate);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
 template <typename T>
-smg_status coarse_apply(smg_mg* mg, int l, VecView<T> x, cx<T>* y, int epi, const cx<T>* w, double* out) {
+smg_status coarse_apply(smg_mg* mg, int l, VecView<T> x, cx<T>* y, int epi, const cx<T>* w, double* out,
+                        const int* gate = nullptr) {
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[l];
+    if (x.nrhs == 1 && (L.ndof == 8 || L.ndof == 16 || L.ndof == 32)) {
+        ReduceLaunch rl = reduce_launch((int)((int64_t)L.nsites * L.ndof), 1);
+        SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * 3));
+        double* pp = epi ? ctx->red.partials : nullptr;
+        unsigned int* tk = epi ? ctx->red.tickets : nullptr;
+#define SMG_CA1(NC)                                                                                                  \
+    do {                                                                                                             \
+        if (epi == 0)                                                                                                \
+            k_coarse_apply1<T, 0, NC><<<rl.grid, rl.block, 0, ctx->stream>>>(Ap<T>(L), x, y, L.nx, L.ny, w, pp, tk,  \
+                                                                            out, gate);                              \
+        else if (epi == 1)                                                                                           \
+            k_coarse_apply1<T, 1, NC><<<rl.grid, rl.block, 0, ctx->stream>>>(Ap<T>(L), x, y, L.nx, L.ny, w, pp, tk,  \
+                                                                            out, gate);                              \
+        else                                                                                                         \
+            k_coarse_apply1<T, 2, NC><<<rl.grid, rl.block, 0, ctx->stream>>>(Ap<T>(L), x, y, L.nx, L.ny, w, pp, tk,  \
+                                                                            out, gate);                              \
+    } while (0)
+        if (L.ndof == 8) SMG_CA1(8);
+        else if (L.ndof == 16) SMG_CA1(16);
+        else SMG_CA1(32);
+#undef SMG_CA1
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+        return SMG_OK;
+    }
+    // several right-hand sides: stage link and vector blocks in shared memory
+    if (x.nrhs >= 8) {
+        if (L.ndof == 8) return coarse_apply_tiled<T, 8>(ctx, L, Ap<T>(L), x, y, epi, w, out, gate);
+        if (L.ndof == 16) return coarse_apply_tiled<T, 16>(ctx, L, Ap<T>(L), x, y, epi, w, out, gate);
+        if (L.ndof == 32) return coarse_apply_tiled<T, 32>(ctx, L, Ap<T>(L), x, y, epi, w, out, gate);
+    }
     ReduceLaunch rl = reduce_launch((int)((int64_t)L.nsites * L.ndof), x.nrhs);
-    // cap rows so a block holds whole sites
     SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * x.nrhs * 3));
     if (epi == 0) {
         k_coarse_apply<T, 0><<<rl.grid, rl.block, 0, ctx->stream>>>(Ap<T>(L), x, y, L.nx, L.ny, w, nullptr, nullptr,
-                                                                  nullptr);
+                                                                  nullptr, gate);
     } else if (epi == 1) {
         k_coarse_apply<T, 1><<<rl.grid, rl.block, 0, ctx->stream>>>(Ap<T>(L), x, y, L.nx, L.ny, w, ctx->red.partials,
-                                                                  ctx->red.tickets, out);
+                                                                  ctx->red.tickets, out, gate);
     } else {
         k_coarse_apply<T, 2><<<rl.grid, rl.block, 0, ctx->stream>>>(Ap<T>(L), x, y, L.nx, L.ny, w, ctx->red.partials,
-                                                                  ctx->red.tickets, out);
+                                                                  ctx->red.tickets, out, gate);
     }
     count_launch(ctx);
     SMG_CHECK_LAUNCH(ctx);
@@ -656,7 +1025,52 @@ smg_status free_work(smg_mg* mg) {
     mg->cw.clear();
     if (mg->scal) cudaFree(mg->scal);
     mg->scal = nullptr;
+    if (mg->cg_state) cudaFree(mg->cg_state);
+    mg->cg_state = nullptr;
     mg->work_nrhs = 0;
+    return SMG_OK;
+}
+
+template <typename T, int NC>
+smg_status coarse_cg_persistent(smg_mg* mg, int l, void* x, const void* b) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[l];
+    CoarseWork& w = mg->cw[l];
+    static int blocks_per_sm = -1;  // per template instance
+    if (blocks_per_sm < 0) {
+        int nb = 0;
+        SMG_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_coarse_cg1<T, NC>, 256, 0));
+        blocks_per_sm = nb;
+    }
+    const int n = L.nsites * NC;
+    int grid = blocks_per_sm * ctx->num_sms;
+    const int need = (n + 255) / 256;
+    if (grid > need) grid = need;
+    if (grid > kMaxReduceBlocks) grid = kMaxReduceBlocks;
+    if (grid < 1) return smg_fail(ctx, SMG_UNSUPPORTED, "coarsest CG kernel cannot be resident");
+    CoarseCgArgs a;
+    a.A = Ap<T>(L);
+    a.b = b;
+    a.x = x;
+    a.r = w.r;
+    a.p = w.p;
+    a.Ap = w.Ar;
+    a.nx = L.nx;
+    a.ny = L.ny;
+    a.nsites = L.nsites;
+    a.max_iter = mg->p.coarse_max_iter;
+    a.tol2 = mg->p.coarse_tol * mg->p.coarse_tol;
+    char* st = static_cast<char*>(mg->cg_state);
+    a.bar = reinterpret_cast<unsigned int*>(st);
+    a.err = reinterpret_cast<int*>(st) + 2;
+    a.iters = reinterpret_cast<int*>(st) + 3;
+    a.part = reinterpret_cast<double*>(st + 256);
+    // barrier words back to zero; a raised error flag stays raised until read
+    SMG_CUDA(ctx, cudaMemsetAsync(st, 0, 2 * sizeof(unsigned int), ctx->stream));
+    void* args[] = {&a};
+    SMG_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_coarse_cg1<T, NC>, dim3(grid), dim3(256), args, 0,
+                                              ctx->stream));
+    count_launch(ctx);
     return SMG_OK;
 }
 
@@ -679,11 +1093,16 @@ smg_status ensure_work(smg_mg* mg, int nrhs, smg_precision prec) {
             SMG_CUDA(ctx, cudaMemsetAsync(*p, 0, bytes, ctx->stream));
         }
     }
+    if (!mg->cg_state) {
+        SMG_CUDA(ctx, cudaMalloc(&mg->cg_state, 256 + 2 * kMaxReduceBlocks * sizeof(double)));
+        SMG_CUDA(ctx, cudaMemsetAsync(mg->cg_state, 0, 256, ctx->stream));
+    }
     mg->scal_doubles = (size_t)mg->lv.size() * 16 * nrhs + 128;
     SMG_CUDA(ctx, cudaMalloc(&mg->scal, mg->scal_doubles * sizeof(double)));
     SMG_CUDA(ctx, cudaMemsetAsync(mg->scal, 0, mg->scal_doubles * sizeof(double), ctx->stream));
     mg->work_nrhs = nrhs;
     mg->work_prec = prec;
+    mg->work_gen++;
     return SMG_OK;
 }
 
@@ -709,7 +1128,7 @@ smg_status mr_fine(smg_mg* mg, smg_field* x, const smg_field* b, int niter, bool
     double* sc = lvl_scal(mg, 0);
     for (int it = 0; it < niter; ++it) {
         SMG_TRY(level_apply_fine<T>(mg, r, Ar, r, sc));
-        VecView<T> xv = fview<T>(x);
+        const VecView<T> xv = flat(fview<T>(x));
         k_mr_update<T><<<vec_grid(xv.nsites, xv.nrhs), vec_block(xv.nrhs), 0, ctx->stream>>>(
             xv, (cx<T>*)r->data, (const cx<T>*)Ar->data, sc);
         count_launch(ctx);
@@ -739,8 +1158,9 @@ smg_status mr_coarse(smg_mg* mg, int l, void* x, const void* b, int niter, bool 
     double* sc = lvl_scal(mg, l);
     for (int it = 0; it < niter; ++it) {
         SMG_TRY(coarse_apply<T>(mg, l, rv, (cx<T>*)w.Ar, 2, (const cx<T>*)w.r, sc));
-        k_mr_update<T><<<vec_grid(xv.nsites, xv.nrhs), vec_block(xv.nrhs), 0, ctx->stream>>>(
-            xv, (cx<T>*)w.r, (const cx<T>*)w.Ar, sc);
+        const VecView<T> xf = flat(xv);
+        k_mr_update<T><<<vec_grid(xf.nsites, xf.nrhs), vec_block(xf.nrhs), 0, ctx->stream>>>(
+            xf, (cx<T>*)w.r, (const cx<T>*)w.Ar, sc);
         count_launch(ctx);
         SMG_CHECK_LAUNCH(ctx);
     }
@@ -753,6 +1173,11 @@ template <typename T>
 smg_status coarse_cg(smg_mg* mg, int l, void* x, const void* b) {
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[l];
+    if (mg->persistent && mg->work_nrhs == 1) {
+        if (L.ndof == 8) return coarse_cg_persistent<T, 8>(mg, l, x, b);
+        if (L.ndof == 16) return coarse_cg_persistent<T, 16>(mg, l, x, b);
+        if (L.ndof == 32) return coarse_cg_persistent<T, 32>(mg, l, x, b);
+    }
     CoarseWork& w = mg->cw[l];
     const int nrhs = mg->work_nrhs;
     VecView<T> xv = cview<T>(x, L, nrhs), pv = cview<T>(w.p, L, nrhs), rv = cview<T>(w.r, L, nrhs);
@@ -769,10 +1194,11 @@ smg_status coarse_cg(smg_mg* mg, int l, void* x, const void* b) {
     SMG_CUDA(ctx, cudaMemsetAsync(x, 0, bytes, ctx->stream));
     SMG_CUDA(ctx, cudaMemcpyAsync(w.r, b, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     SMG_CUDA(ctx, cudaMemcpyAsync(w.p, b, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-    SMG_TRY(vreduce<T>(ctx, rv, nullptr, VR_NORM, s.rr));
+    SMG_TRY(vreduce<T>(ctx, flat(rv), nullptr, VR_NORM, s.rr));
     k_ccg_init<<<1, 256, 0, ctx->stream>>>(s, nrhs);
     count_launch(ctx);
-    ReduceLaunch rl = reduce_launch(L.nsites, nrhs);
+    const VecView<T> xf = flat(xv), pf = flat(pv);
+    ReduceLaunch rl = reduce_launch(xf.nsites, nrhs);
     SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * nrhs * 3));
     SMG_TRY(smg_host_stage_reserve(ctx, 64));
     int* h_act = (int*)ctx->host_stage;
@@ -780,15 +1206,16 @@ smg_status coarse_cg(smg_mg* mg, int l, void* x, const void* b) {
     while (it < mg->p.coarse_max_iter) {
         int chunk = std::min(8, mg->p.coarse_max_iter - it);
         for (int c = 0; c < chunk; ++c) {
-            SMG_TRY(coarse_apply<T>(mg, l, pv, (cx<T>*)w.Ar, 2, (const cx<T>*)w.p, s.pap3));
-            k_ccg_update<T><<<rl.grid, rl.block, 0, ctx->stream>>>(s, xv, (cx<T>*)w.r, (const cx<T>*)w.p,
+            SMG_TRY(coarse_apply<T>(mg, l, pv, (cx<T>*)w.Ar, 2, (const cx<T>*)w.p, s.pap3, s.n_active));
+            k_ccg_update<T><<<rl.grid, rl.block, 0, ctx->stream>>>(s, xf, (cx<T>*)w.r, (const cx<T>*)w.p,
                                                                    (const cx<T>*)w.Ar, ctx->red.partials,
                                                                    ctx->red.tickets);
-            k_ccg_p<T><<<vec_grid(L.nsites, nrhs), vec_block(nrhs), 0, ctx->stream>>>(s, pv, (const cx<T>*)w.r);
+            k_ccg_p<T><<<vec_grid(pf.nsites, nrhs), vec_block(nrhs), 0, ctx->stream>>>(s, pf, (const cx<T>*)w.r);
             count_launch(ctx, 2);
             SMG_CHECK_LAUNCH(ctx);
         }
         it += chunk;
+        if (mg->capturing) continue;  // inside a graph: the gated kernels finish the budget as no-ops
         SMG_CUDA(ctx, cudaMemcpyAsync(h_act, s.n_active, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         if (*h_act == 0) break;
@@ -906,7 +1333,7 @@ smg_status null_space_fine(smg_mg* mg, std::vector<smg_field*>& vecs) {
     double* sc = mg->scal;  // [0..1] norm, [2..3] dot
     SMG_TRY(smg_host_stage_reserve(ctx, 64));
     auto norm_of = [&](smg_field* f, double* hv) -> smg_status {
-        SMG_TRY(vreduce<double>(ctx, fview<double>(f), nullptr, VR_NORM, sc));
+        SMG_TRY(vreduce<double>(ctx, flat(fview<double>(f)), nullptr, VR_NORM, sc));
         SMG_CUDA(ctx, cudaMemcpyAsync(ctx->host_stage, sc, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         *hv = std::sqrt(ctx->host_stage[0]);
@@ -918,8 +1345,8 @@ smg_status null_space_fine(smg_mg* mg, std::vector<smg_field*>& vecs) {
     };
     auto ortho = [&](smg_field* v, int upto) -> smg_status {
         for (int j = 0; j < upto; ++j) {
-            SMG_TRY(vreduce<double>(ctx, fview<double>(vecs[j]), (const cx<double>*)v->data, VR_DOT, sc + 2));
-            SMG_TRY(vaxpy<double>(ctx, fview<double>(v), (const cx<double>*)vecs[j]->data, sc + 2, -1.0));
+            SMG_TRY(vreduce<double>(ctx, flat(fview<double>(vecs[j])), (const cx<double>*)v->data, VR_DOT, sc + 2));
+            SMG_TRY(vaxpy<double>(ctx, flat(fview<double>(v)), (const cx<double>*)vecs[j]->data, sc + 2, -1.0));
         }
         return SMG_OK;
     };
@@ -958,7 +1385,7 @@ smg_status null_space_coarse(smg_mg* mg, int l, std::vector<cx<double>*>& vecs) 
     CoarseWork& w = mg->cw[l];
     double* sc = mg->scal;
     SMG_TRY(smg_host_stage_reserve(ctx, 64));
-    auto view = [&](void* p) { return cview<double>(p, L, 1); };
+    auto view = [&](void* p) { return flat(cview<double>(p, L, 1)); };
     auto norm_of = [&](void* f, double* hv) -> smg_status {
         SMG_TRY(vreduce<double>(ctx, view(f), nullptr, VR_NORM, sc));
         SMG_CUDA(ctx, cudaMemcpyAsync(ctx->host_stage, sc, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1196,15 +1623,103 @@ void destroy_levels(smg_mg* mg) {
 
 }  // namespace
 
+namespace {
+
+void drop_graph(smg_mg* mg) {
+    if (mg->g_exec) cudaGraphExecDestroy(mg->g_exec);
+    mg->g_exec = nullptr;
+    smg_field_destroy(mg->g_in);
+    smg_field_destroy(mg->g_out);
+    mg->g_in = mg->g_out = nullptr;
+}
+
+// One cycle from mg->g_in to mg->g_out captured as a CUDA graph.  The
+// coarsest CG runs its full iteration budget inside the graph; its kernels
+// return at once after every right-hand side has converged.
+template <typename T>
+smg_status capture_cycle(smg_mg* mg, const smg_field* proto) {
+    smg_context* ctx = mg->ctx;
+    drop_graph(mg);
+    SMG_TRY(ensure_work(mg, proto->nrhs, proto->prec));
+    SMG_TRY(smg_field_alloc_like(proto, proto->prec, &mg->g_in));
+    SMG_TRY(smg_field_alloc_like(proto, proto->prec, &mg->g_out));
+    SMG_TRY(smg_reduce_reserve(ctx, (size_t)kMaxReduceBlocks * proto->nrhs * 3 + 1024));
+    SMG_TRY(smg_host_stage_reserve(ctx, 64));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const uint64_t l0 = ctx->launches;
+    cudaGraph_t graph = nullptr;
+    mg->capturing = true;
+    SMG_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    smg_status st = cycle_fine<T>(mg, mg->g_out, mg->g_in);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    mg->capturing = false;
+    mg->g_launches = ctx->launches - l0;
+    ctx->launches = l0;
+    if (st != SMG_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return st;
+    }
+    if (e != cudaSuccess || !graph)
+        return smg_fail(ctx, SMG_DEVICE_ERROR, std::string("cycle capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&mg->g_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        mg->g_exec = nullptr;
+        return smg_fail(ctx, SMG_DEVICE_ERROR, std::string("cycle graph: ") + cudaGetErrorString(e));
+    }
+    mg->g_work_gen = mg->work_gen;
+    return SMG_OK;
+}
+
+template <typename T>
+smg_status cycle_graph(smg_mg* mg, const smg_field* b, smg_field* x) {
+    smg_context* ctx = mg->ctx;
+    const bool stale = !mg->g_exec || !mg->g_in || mg->g_in->nrhs != b->nrhs || mg->g_in->prec != b->prec ||
+                       mg->work_nrhs != b->nrhs || mg->work_prec != b->prec || mg->g_work_gen != mg->work_gen;
+    if (stale) SMG_TRY(capture_cycle<T>(mg, b));
+    SMG_CUDA(ctx, cudaMemcpyAsync(mg->g_in->data, b->data, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    SMG_CUDA(ctx, cudaGraphLaunch(mg->g_exec, ctx->stream));
+    ctx->launches += mg->g_launches;
+    SMG_CUDA(ctx, cudaMemcpyAsync(x->data, mg->g_out->data, x->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    return SMG_OK;
+}
+
+}  // namespace
+
 // ---- internal entry used by the GCR solver
 smg_status smg_mg_apply_internal(smg_mg* mg, const smg_field* b, smg_field* x) {
+    if (b->prec != SMG_F64 && b->prec != SMG_F32)
+        return smg_fail(mg->ctx, SMG_UNSUPPORTED, "MG cycle on F16 fields");
+    if (mg->use_graph) {
+        smg_status st = b->prec == SMG_F64 ? cycle_graph<double>(mg, b, x) : cycle_graph<float>(mg, b, x);
+        if (st != SMG_DEVICE_ERROR || mg->g_exec) return st;
+        // capture or instantiation failed: run the cycle with direct launches from now on
+        cudaGetLastError();
+        drop_graph(mg);
+        mg->use_graph = false;
+    }
     SMG_TRY(ensure_work(mg, b->nrhs, b->prec));
     if (b->prec == SMG_F64) return cycle_fine<double>(mg, x, b);
-    if (b->prec == SMG_F32) return cycle_fine<float>(mg, x, b);
-    return smg_fail(mg->ctx, SMG_UNSUPPORTED, "MG cycle on F16 fields");
+    return cycle_fine<float>(mg, x, b);
 }
 
 smg_precision smg_mg_precision(const smg_mg* mg) { return mg->p.precision; }
+
+// Reads (and clears) the persistent coarsest CG's error flag: SMG_TIMEOUT if a
+// bounded grid-barrier wait ran out since the last check.  Synchronises.
+smg_status smg_mg_check_device_error(smg_mg* mg) {
+    if (!mg->cg_state) return SMG_OK;
+    smg_context* ctx = mg->ctx;
+    int err = 0;
+    SMG_CUDA(ctx, cudaMemcpyAsync(&err, static_cast<char*>(mg->cg_state) + 8, sizeof(int), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (err) {
+        SMG_CUDA(ctx, cudaMemsetAsync(static_cast<char*>(mg->cg_state) + 8, 0, sizeof(int), ctx->stream));
+        return smg_fail(ctx, SMG_TIMEOUT, "coarsest CG: a grid-barrier wait ran out");
+    }
+    return SMG_OK;
+}
 
 extern "C" {
 
@@ -1254,6 +1769,7 @@ SMG_API smg_status smg_mg_create(smg_dirac* d, const smg_mg_params* p, const dou
 SMG_API smg_status smg_mg_destroy(smg_mg* mg) {
     if (!mg) return SMG_OK;
     cudaStreamSynchronize(mg->ctx->stream);
+    drop_graph(mg);
     free_work(mg);
     destroy_levels(mg);
     delete mg;
@@ -1315,7 +1831,8 @@ SMG_API smg_status smg_mg_precondition(smg_mg* mg, const smg_field* b, smg_field
     SMG_TRY(smg_field_check_pair(b, x));
     if (b == x) return smg_fail(mg->ctx, SMG_BAD_ARG, "b and x must be distinct");
     if (b->g.L != mg->lv[0].nx) return smg_fail(mg->ctx, SMG_BAD_ARG, "field L differs from the hierarchy's");
-    return smg_mg_apply_internal(mg, b, x);
+    SMG_TRY(smg_mg_apply_internal(mg, b, x));
+    return smg_mg_check_device_error(mg);
 }
 
 SMG_API smg_status smg_mg_prolong_host(smg_mg* mg, int level, const double* coarse, double* fine) {
@@ -1356,6 +1873,41 @@ SMG_API smg_status smg_mg_restrict_host(smg_mg* mg, int level, const double* fin
     const size_t cb = (size_t)N.nsites * N.ndof * sizeof(cx<double>);
     SMG_CUDA(ctx, cudaMemcpyAsync(coarse, nw.b, cb, cudaMemcpyDeviceToHost, ctx->stream));
     SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_time_coarse_apply(smg_mg* mg, int level, int nrhs, int reps, double* ms, double* bytes) {
+    if (!mg || !ms || level < 1 || level >= (int)mg->lv.size() || nrhs < 1 || reps < 1) return SMG_BAD_ARG;
+    smg_context* ctx = mg->ctx;
+    const smg_precision prec = mg->p.precision;
+    SMG_TRY(ensure_work(mg, nrhs, prec));
+    const Level& L = mg->lv[level];
+    CoarseWork& w = mg->cw[level];
+    cudaEvent_t e0, e1;
+    SMG_CUDA(ctx, cudaEventCreate(&e0));
+    SMG_CUDA(ctx, cudaEventCreate(&e1));
+    smg_status st = SMG_OK;
+    for (int pass = 0; pass < 2 && st == SMG_OK; ++pass) {  // pass 0 warms up
+        SMG_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+        for (int i = 0; i < reps && st == SMG_OK; ++i) {
+            if (prec == SMG_F64)
+                st = coarse_apply<double>(mg, level, cview<double>(w.x, L, nrhs), (cx<double>*)w.Ar, 0, nullptr,
+                                          nullptr);
+            else
+                st = coarse_apply<float>(mg, level, cview<float>(w.x, L, nrhs), (cx<float>*)w.Ar, 0, nullptr,
+                                         nullptr);
+        }
+        SMG_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+    }
+    SMG_CUDA(ctx, cudaEventSynchronize(e1));
+    float f = 0;
+    SMG_CUDA(ctx, cudaEventElapsedTime(&f, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    SMG_TRY(st);
+    *ms = (double)f / reps;
+    const double es = prec == SMG_F64 ? 16.0 : 8.0;
+    if (bytes) *bytes = es * ((double)L.nsites * 9 * L.ndof * L.ndof + 2.0 * L.nsites * L.ndof * nrhs);
     return SMG_OK;
 }
 

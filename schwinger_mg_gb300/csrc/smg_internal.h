@@ -153,6 +153,9 @@ struct smg_context {
     size_t host_stage_bytes = 0;
     int num_sms = 0;
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+    // reduction buffers replaced by a larger one stay allocated until the
+    // context is destroyed: a captured CUDA graph may still reference them
+    std::vector<double*> retired;
 };
 
 struct smg_gauge {

@@ -296,6 +296,7 @@ SMG_API smg_status smg_cg_solve(smg_dirac* d, const smg_field* rhs, smg_field* x
 
 smg_status smg_mg_apply_internal(smg_mg* mg, const smg_field* b, smg_field* x);
 smg_precision smg_mg_precision(const smg_mg* mg);
+smg_status smg_mg_check_device_error(smg_mg* mg);
 
 namespace {
 
@@ -583,6 +584,7 @@ smg_status gcr_run(smg_dirac* d, smg_mg* mg, const smg_field* b, smg_field* x, i
         res->true_residual = worst_true;
         res->operator_applications = iter + 1;
     }
+    if (mg) SMG_TRY(smg_mg_check_device_error(mg));
     if (nonfinite) return smg_fail(ctx, SMG_NONFINITE, "gcr_solve: non-finite residual");
     if (notconv) return smg_fail(ctx, SMG_NOT_CONVERGED, "gcr_solve: iteration limit reached");
     return SMG_OK;

@@ -125,3 +125,23 @@ def test_mg_bad_parameters(smg_gpu):
         smg_gpu.MGHierarchy(D, smg_gpu.mg_params(2, 8, 4))  # 2 x 2 coarse lattice
     with pytest.raises(smg_gpu.SmgError):
         smg_gpu.MGHierarchy(D, smg_gpu.mg_params(2, 3, 4))  # 3 does not divide 16
+
+
+@pytest.mark.parametrize("chiral,k", [(False, 4), (True, 4)])
+def test_three_level_cycle_matches_oracle(smg_gpu, port, chiral, k):
+    """The GPU's 3-level W-cycle against the oracle's restatement of mg_cycle on the same hierarchy."""
+    L = 32
+    U = smg_gpu.gauge_normal(L, 3.0, 555)
+    lat = smg_gpu.Lattice(L)
+    D = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, U), 0.05, 1.0, 1.0, 0.0)
+    blocks = [(4, 4), (2, 2)]
+    p = smg_gpu.mg_params(3, 4, k, blocks=blocks, chiral_split=chiral, null_iters=3, coarse_tol=1e-13,
+                          coarse_max_iter=3000, seed=11)
+    mg = smg_gpu.MGHierarchy(D, p)
+    ncs = [mg.level_dims(1)[2], mg.level_dims(2)[2]]
+    po = port.mgN_params(L, 0.05, 1.0, 1.0, 0.0, blocks, ncs, [mg.prolongator(0), mg.prolongator(1)],
+                         [None, mg.coarse_op(1), mg.coarse_op(2)], 3, 3, True, 3000, 1e-13)
+    b = smg_gpu.random_vec(lat.ndof, 5)
+    got = mg.precondition(b)
+    want = port.mgN_precondition(po, U, b)
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-9

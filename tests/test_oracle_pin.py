@@ -126,3 +126,15 @@ def test_port_null_space_matches_reference(port, ref):
     want = ref.near_null_space(U, 0.1, 1.0, 1.0, 0.0, k, iters, seed)
     got = port.near_null_space(U, 0.1, 1.0, 1.0, 0.0, k, iters, init)
     assert np.max(np.abs(got - want)) < 1e-11
+
+
+def test_port_nlevel_cycle_matches_two_level_and_reference(port):
+    d = golden("mg_L16_bs4_k4")
+    L, bs, k = int(d["L"]), int(d["bs"]), int(d["k"])
+    args = (float(d["m"]), float(d["r"]), float(d["csw"]), float(d["mu"]))
+    p2 = port.mg2_params(L, bs, k, *args, 3, 3, 1000, 1e-13)
+    two = port.mg2_precondition(p2, d["U"], d["block_vecs"], d["links"], d["fine_src"])
+    pN = port.mgN_params(L, *args, [(bs, bs)], [k], [d["block_vecs"]], [None, d["links"]], 3, 3, True, 1000, 1e-13)
+    nl = port.mgN_precondition(pN, d["U"], d["fine_src"])
+    assert np.max(np.abs(nl - two)) / np.max(np.abs(two)) < 1e-13
+    assert np.linalg.norm(nl - d["mg_precondition"]) / np.linalg.norm(d["mg_precondition"]) < 1e-10
