@@ -157,19 +157,23 @@ __global__ void k_block_orth(cx<double>* __restrict__ V, int len, int nc) {
     for (int t = threadIdx.x; t < len * nc; t += blockDim.x) Vb[t] = sv[t];
 }
 
-// restriction, level 0: c[B][rhs][i] = sum_{loc,sp} conj(V[B][loc][sp][i]) f[q][rhs][sp]
+// Coarse vectors are [site][dof][rhs] (right-hand side innermost); the
+// transfer kernels run one thread per output element with the rhs fastest, so
+// coarse reads and writes are coalesced and block-vector reads are shared by
+// the rhs lanes of a warp.
+
+// restriction, level 0: c[B][i][rhs] = sum_{loc,sp} conj(V[B][loc][sp][i]) f[q][rhs][sp]
 template <typename T>
 __global__ void k_restrict0(const cx<T>* __restrict__ V, const cx<T>* __restrict__ f, cx<T>* __restrict__ c, Geom g,
                             int bx, int by, int nc, int nrhs) {
-    // one thread per (B, rhs, i); i fastest
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int nbx = g.L / bx, nby = g.L / by;
     int64_t total = (int64_t)nbx * nby * nrhs * nc;
     if (t >= total) return;
-    int i = (int)(t % nc);
-    int64_t br = t / nc;
-    int rhs = (int)(br % nrhs);
-    int B = (int)(br / nrhs);
+    int rhs = (int)(t % nrhs);
+    int64_t bi = t / nrhs;
+    int i = (int)(bi % nc);
+    int B = (int)(bi / nc);
     int x0 = (B % nbx) * bx, y0 = (B / nbx) * by;
     int m = bx * by;
     cx<T> acc = mk<T>(0, 0);
@@ -180,10 +184,10 @@ __global__ void k_restrict0(const cx<T>* __restrict__ V, const cx<T>* __restrict
         const cx<T>* v = V + ((int64_t)B * m + loc) * 2 * nc;
         acc = acc + cmulc(v[i], fv.s0) + cmulc(v[nc + i], fv.s1);
     }
-    c[((int64_t)B * nrhs + rhs) * nc + i] = acc;
+    c[t] = acc;  // t = (B * nc + i) * nrhs + rhs
 }
 
-// prolongation, level 0: f[q][rhs][sp] (+)= sum_i V[B][loc][sp][i] c[B][rhs][i]
+// prolongation, level 0: f[q][rhs][sp] (+)= sum_i V[B][loc][sp][i] c[B][i][rhs]
 template <typename T>
 __global__ void k_prolong0(const cx<T>* __restrict__ V, const cx<T>* __restrict__ c, cx<T>* __restrict__ f, Geom g,
                            int bx, int by, int nc, int nrhs, int accumulate) {
@@ -198,10 +202,10 @@ __global__ void k_prolong0(const cx<T>* __restrict__ V, const cx<T>* __restrict_
     int loc = (x % bx) + bx * (y % by);
     int m = bx * by;
     const cx<T>* v = V + ((int64_t)B * m + loc) * 2 * nc;
-    const cx<T>* cc = c + ((int64_t)B * nrhs + rhs) * nc;
+    const cx<T>* cc = c + (int64_t)B * nc * nrhs + rhs;
     cx<T> f0 = mk<T>(0, 0), f1 = mk<T>(0, 0);
     for (int i = 0; i < nc; ++i) {
-        cx<T> ci = cc[i];
+        cx<T> ci = cc[(int64_t)i * nrhs];
         f0 = f0 + ci * v[i];
         f1 = f1 + ci * v[nc + i];
     }
@@ -217,49 +221,48 @@ __global__ void k_prolong0(const cx<T>* __restrict__ V, const cx<T>* __restrict_
     st_spinor(f, q, rhs, nrhs, out);
 }
 
-// coarse restriction: c'[B][rhs][i] = sum_{loc,j} conj(V[B][loc][j][i]) c[site][rhs][j]
+// coarse restriction: c'[B][i][rhs] = sum_{loc,j} conj(V[B][loc][j][i]) c[site][j][rhs]
 template <typename T>
 __global__ void k_restrict_c(const cx<T>* __restrict__ V, const cx<T>* __restrict__ c, cx<T>* __restrict__ cn, int nx,
                              int ax, int ay, int ndof, int nc, int nagg, int nrhs) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)nagg * nrhs * nc) return;
-    int i = (int)(t % nc);
-    int64_t br = t / nc;
-    int rhs = (int)(br % nrhs);
-    int B = (int)(br / nrhs);
+    int rhs = (int)(t % nrhs);
+    int64_t bi = t / nrhs;
+    int i = (int)(bi % nc);
+    int B = (int)(bi / nc);
     int nax = nx / ax;
     int x0 = (B % nax) * ax, y0 = (B / nax) * ay;
     int m = ax * ay;
     cx<T> acc = mk<T>(0, 0);
     for (int loc = 0; loc < m; ++loc) {
         int s = (x0 + loc % ax) + nx * (y0 + loc / ax);
-        const cx<T>* cv = c + ((int64_t)s * nrhs + rhs) * ndof;
+        const cx<T>* cv = c + (int64_t)s * ndof * nrhs + rhs;
         const cx<T>* v = V + ((int64_t)B * m + loc) * ndof * nc;
-        for (int j = 0; j < ndof; ++j) acc = acc + cmulc(v[j * nc + i], cv[j]);
+        for (int j = 0; j < ndof; ++j) acc = acc + cmulc(v[j * nc + i], cv[(int64_t)j * nrhs]);
     }
-    cn[((int64_t)B * nrhs + rhs) * nc + i] = acc;
+    cn[t] = acc;  // t = (B * nc + i) * nrhs + rhs
 }
 
-// coarse prolongation: c[site][rhs][j] (+)= sum_i V[B][loc][j][i] c'[B][rhs][i]
+// coarse prolongation: c[site][j][rhs] (+)= sum_i V[B][loc][j][i] c'[B][i][rhs]
 template <typename T>
 __global__ void k_prolong_c(const cx<T>* __restrict__ V, const cx<T>* __restrict__ cn, cx<T>* __restrict__ c, int nx,
                             int ny, int ax, int ay, int ndof, int nc, int nrhs, int accumulate) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)nx * ny * nrhs * ndof) return;
-    int j = (int)(t % ndof);
-    int64_t sr = t / ndof;
-    int rhs = (int)(sr % nrhs);
-    int s = (int)(sr / nrhs);
+    int rhs = (int)(t % nrhs);
+    int64_t sj = t / nrhs;
+    int j = (int)(sj % ndof);
+    int s = (int)(sj / ndof);
     int x = s % nx, y = s / nx;
     int B = (x / ax) + (nx / ax) * (y / ay);
     int loc = (x % ax) + ax * (y % ay);
     int m = ax * ay;
     const cx<T>* v = V + (((int64_t)B * m + loc) * ndof + j) * nc;
-    const cx<T>* cc = cn + ((int64_t)B * nrhs + rhs) * nc;
+    const cx<T>* cc = cn + (int64_t)B * nc * nrhs + rhs;
     cx<T> acc = mk<T>(0, 0);
-    for (int i = 0; i < nc; ++i) acc = acc + v[i] * cc[i];
-    int64_t o = ((int64_t)s * nrhs + rhs) * ndof + j;
-    c[o] = accumulate ? c[o] + acc : acc;
+    for (int i = 0; i < nc; ++i) acc = acc + v[i] * cc[(int64_t)i * nrhs];
+    c[t] = accumulate ? c[t] + acc : acc;  // t = (s * ndof + j) * nrhs + rhs
 }
 
 // W[B][i][h][sp] = (D P_{B,i})(h) on the (bx+2) x (by+2) halo frame of block B
@@ -412,10 +415,10 @@ __global__ void __launch_bounds__(256) k_coarse_apply(const cx<T>* __restrict__ 
                 const int sn = (xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn)) +
                                nx * (yn < 0 ? yn + ny : (yn >= ny ? yn - ny : yn));
                 const cx<T>* Ad = A + ((int64_t)s * 9 + d) * nc * nc + i;
-                const cx<T>* xv = xin.p + ((int64_t)sn * nrhs + rhs) * nc;
-                for (int j = 0; j < nc; ++j) acc = acc + Ad[(int64_t)j * nc] * xv[j];
+                const cx<T>* xv = xin.p + (int64_t)sn * nc * nrhs + rhs;  // [site][dof][rhs]
+                for (int j = 0; j < nc; ++j) acc = acc + Ad[(int64_t)j * nc] * xv[(int64_t)j * nrhs];
             }
-            const int64_t o = ((int64_t)s * nrhs + rhs) * nc + i;
+            const int64_t o = ((int64_t)s * nc + i) * nrhs + rhs;
             y[o] = acc;
             if (EPI == 1) {
                 v[0] += (double)norm2(acc);
@@ -509,10 +512,10 @@ __global__ void __launch_bounds__(256) k_coarse_apply_tiled(const cx<T>* __restr
             __syncthreads();
             const cx<T>* Ad = A + ((int64_t)s * 9 + d) * NC * NC;
             for (int t = tid; t < NC * NC; t += nthr) sA[t] = Ad[t];
-            const cx<T>* Xn = xin.p + ((int64_t)sn * nrhs + r0) * NC;
+            const cx<T>* Xn = xin.p + (int64_t)sn * NC * nrhs + r0;  // [site][dof][rhs]
             for (int t = tid; t < lanes * NC; t += nthr) {
-                const int r = t / NC, j = t - r * NC;
-                sX[r][j] = (r0 + r < nrhs) ? Xn[t] : mk<T>(0, 0);
+                const int j = t / lanes, r = t - j * lanes;
+                sX[r][j] = (r0 + r < nrhs) ? Xn[(int64_t)j * nrhs + r] : mk<T>(0, 0);
             }
             __syncthreads();
 #pragma unroll
@@ -531,7 +534,7 @@ __global__ void __launch_bounds__(256) k_coarse_apply_tiled(const cx<T>* __restr
             for (int a = 0; a < kPer; ++a) {
                 const int i = threadIdx.y + a * rows;
                 if (i < NC) {
-                    const int64_t o = ((int64_t)s * nrhs + rhs) * NC + i;
+                    const int64_t o = ((int64_t)s * NC + i) * nrhs + rhs;
                     y[o] = acc[a];
                     if (EPI == 1) {
                         v[0] += (double)norm2(acc[a]);
@@ -794,10 +797,11 @@ __global__ void __launch_bounds__(256) k_ccg_update(CcgState s, VecView<T> x, cx
     if (rhs < nrhs) {
         for (int st = blockIdx.x * blockDim.y + threadIdx.y; st < x.nsites; st += gridDim.x * blockDim.y) {
             const int64_t base = x.idx(st, rhs, 0);
+            const int ds = x.dstride();
             for (int d = 0; d < x.ndof; ++d) {
-                const cx<T> ri = r[base + d] - al * Ap[base + d];
-                x.p[base + d] = x.p[base + d] + al * p[base + d];
-                r[base + d] = ri;
+                const cx<T> ri = r[base + (int64_t)d * ds] - al * Ap[base + (int64_t)d * ds];
+                x.p[base + (int64_t)d * ds] = x.p[base + (int64_t)d * ds] + al * p[base + (int64_t)d * ds];
+                r[base + (int64_t)d * ds] = ri;
                 v[0] += (double)norm2(ri);
             }
         }
@@ -813,7 +817,8 @@ __global__ void k_ccg_p(CcgState s, VecView<T> p, const cx<T>* __restrict__ r) {
     if (rhs >= p.nrhs || st >= p.nsites) return;
     const T be = (T)s.beta[rhs];
     const int64_t base = p.idx(st, rhs, 0);
-    for (int d = 0; d < p.ndof; ++d) p.p[base + d] = r[base + d] + be * p.p[base + d];
+    const int ds = p.dstride();
+    for (int d = 0; d < p.ndof; ++d) p.p[base + (int64_t)d * ds] = r[base + (int64_t)d * ds] + be * p.p[base + (int64_t)d * ds];
 }
 
 }  // namespace
@@ -902,6 +907,7 @@ VecView<T> cview(void* p, const Level& L, int nrhs) {
     v.nsites = L.nsites;
     v.nrhs = nrhs;
     v.ndof = L.ndof;
+    v.rhs_inner = 1;  // coarse vectors: [site][dof][rhs]
     return v;
 }
 

@@ -331,9 +331,10 @@ __global__ void __launch_bounds__(256) k_gcr_orth(VecView<T> p, cx<T>* __restric
     if (rhs >= p.nrhs || s >= p.nsites) return;
     const cx<T> be = s_b[threadIdx.x];
     const int64_t base = p.idx(s, rhs, 0);
+    const int ds = p.dstride();
     for (int d = 0; d < p.ndof; ++d) {
-        p.p[base + d] = p.p[base + d] - be * Pi[base + d];
-        Ap[base + d] = Ap[base + d] - be * APi[base + d];
+        p.p[base + (int64_t)d * ds] = p.p[base + (int64_t)d * ds] - be * Pi[base + (int64_t)d * ds];
+        Ap[base + (int64_t)d * ds] = Ap[base + (int64_t)d * ds] - be * APi[base + (int64_t)d * ds];
     }
 }
 
@@ -367,10 +368,11 @@ __global__ void __launch_bounds__(256) k_gcr_update(GcrScalars sc, VecView<T> x,
     if (rhs < nrhs) {
         for (int st = blockIdx.x * blockDim.y + threadIdx.y; st < x.nsites; st += gridDim.x * blockDim.y) {
             const int64_t base = x.idx(st, rhs, 0);
+            const int ds = x.dstride();
             for (int d = 0; d < x.ndof; ++d) {
-                const cx<T> ri = r[base + d] - al * Ap[base + d];
-                x.p[base + d] = x.p[base + d] + al * p[base + d];
-                r[base + d] = ri;
+                const cx<T> ri = r[base + (int64_t)d * ds] - al * Ap[base + (int64_t)d * ds];
+                x.p[base + (int64_t)d * ds] = x.p[base + (int64_t)d * ds] + al * p[base + (int64_t)d * ds];
+                r[base + (int64_t)d * ds] = ri;
                 v[0] += (double)norm2(ri);
             }
         }
@@ -409,128 +411,143 @@ smg_status reduce_into(smg_context* ctx, VecView<T> a, const cx<T>* b, int mode,
     return SMG_OK;
 }
 
+// Workspace of one GCR solve: residual, preconditioned residual, A z, the
+// D^dag D temporary, the ring of (p, A p) pairs and the device scalars.
 template <typename T>
-smg_status gcr_run(smg_dirac* d, smg_mg* mg, const smg_field* b, smg_field* x, int max_iter, double tol, int trunc,
-                   int ref_coeff, smg_solve_result* res) {
+struct GcrWs {
+    FieldSet fs;
+    smg_field *r = nullptr, *z = nullptr, *Az = nullptr, *tmp = nullptr;
+    std::vector<smg_field*> P, AP;
+    double* blk = nullptr;
+    smg_context* ctx = nullptr;
+    GcrScalars sc;
+    double* truev = nullptr;
+    double* dots = nullptr;
+    double* apr = nullptr;
+    int nrhs = 0, nbuf = 0;
+    double* apr_of(int buf) const { return apr + (size_t)buf * 3 * nrhs; }
+    ~GcrWs() {
+        if (blk) cudaFreeAsync(blk, ctx->stream);
+    }
+    smg_status init(smg_context* c, const smg_field* proto, int trunc) {
+        ctx = c;
+        nrhs = proto->nrhs;
+        nbuf = trunc + 1;
+        SMG_TRY(fs.add(proto, &r));
+        SMG_TRY(fs.add(proto, &z));
+        SMG_TRY(fs.add(proto, &Az));
+        SMG_TRY(fs.add(proto, &tmp));
+        P.resize(nbuf);
+        AP.resize(nbuf);
+        for (int i = 0; i < nbuf; ++i) {
+            SMG_TRY(fs.add(proto, &P[i]));
+            SMG_TRY(fs.add(proto, &AP[i]));
+        }
+        const size_t nd_ = (size_t)nrhs * (5 + 3 * nbuf) + 64;
+        const size_t bytes = nd_ * sizeof(double) + (size_t)nrhs * 2 * sizeof(int) + 64;
+        SMG_CUDA(ctx, cudaMallocAsync(&blk, bytes, ctx->stream));
+        SMG_CUDA(ctx, cudaMemsetAsync(blk, 0, bytes, ctx->stream));
+        sc.rr = blk;
+        sc.bnorm2 = blk + nrhs;
+        truev = blk + 2 * nrhs;
+        dots = blk + 3 * nrhs;  // 2 * nrhs
+        apr = blk + 5 * nrhs;   // nbuf * 3 * nrhs
+        sc.active = (int*)(blk + nd_);
+        sc.flags = sc.active + nrhs;
+        return SMG_OK;
+    }
+};
+
+struct GcrOut {
+    int iterations = 0;
+    bool nonfinite = false;
+    std::vector<int> active;     // per rhs: still above tolerance
+    std::vector<double> rr, b2;  // per rhs recursive ||r||^2 and ||b||^2
+};
+
+// The GCR iteration (fcg_solve, src/solvers.cpp:223-300) on fields of
+// precision T from x = 0; the preconditioner is one MG cycle in the field
+// precision (mg != nullptr) or the identity.
+template <typename T>
+smg_status gcr_core(smg_dirac* d, smg_mg* mg, GcrWs<T>& ws, const smg_field* b, smg_field* x, int max_iter, double tol,
+                    int trunc, int ref_coeff, GcrOut& out) {
     smg_context* ctx = d->ctx;
     const int nrhs = b->nrhs, V = b->g.V;
-    const int nbuf = trunc + 1;
-    FieldSet fs;
-    smg_field *r, *z, *Az, *tmp;
-    SMG_TRY(fs.add(b, &r));
-    SMG_TRY(fs.add(b, &z));
-    SMG_TRY(fs.add(b, &Az));
-    SMG_TRY(fs.add(b, &tmp));
-    std::vector<smg_field*> P(nbuf), AP(nbuf);
-    for (int i = 0; i < nbuf; ++i) {
-        SMG_TRY(fs.add(b, &P[i]));
-        SMG_TRY(fs.add(b, &AP[i]));
-    }
-    const bool mixed = mg && smg_mg_precision(mg) != b->prec;
-    smg_field *rlo = nullptr, *zlo = nullptr;
-    if (mixed) {
-        SMG_TRY(smg_field_alloc_like(b, smg_mg_precision(mg), &rlo));
-        fs.f.push_back(rlo);
-        SMG_TRY(smg_field_alloc_like(b, smg_mg_precision(mg), &zlo));
-        fs.f.push_back(zlo);
-    }
-    // scalar block: rr, bnorm2, true, dots (2), per buffer apr3 (3 each), ints
-    const size_t nd_ = (size_t)nrhs * (5 + 3 * nbuf) + 64;
-    double* blk = nullptr;
-    SMG_CUDA(ctx, cudaMallocAsync(&blk, nd_ * sizeof(double) + (size_t)nrhs * 2 * sizeof(int) + 64, ctx->stream));
-    SMG_CUDA(ctx, cudaMemsetAsync(blk, 0, nd_ * sizeof(double) + (size_t)nrhs * 2 * sizeof(int) + 64, ctx->stream));
-    GcrScalars sc;
-    sc.rr = blk;
-    sc.bnorm2 = blk + nrhs;
-    double* truev = blk + 2 * nrhs;
-    double* dots = blk + 3 * nrhs;  // 2 * nrhs
-    double* apr = blk + 5 * nrhs;   // nbuf * 3 * nrhs
-    sc.active = (int*)(blk + nd_);
-    sc.flags = sc.active + nrhs;
+    GcrScalars& sc = ws.sc;
     sc.tol2 = tol * tol;
-    auto apr_of = [&](int buf) { return apr + (size_t)buf * 3 * nrhs; };
-
     SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
-    SMG_CUDA(ctx, cudaMemcpyAsync(r->data, b->data, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-    SMG_TRY(reduce_into<T>(ctx, fv<T>(r), nullptr, VR_NORM, sc.rr));
+    SMG_CUDA(ctx, cudaMemcpyAsync(ws.r->data, b->data, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    SMG_TRY(reduce_into<T>(ctx, fv<T>(ws.r), nullptr, VR_NORM, sc.rr));
     SMG_CUDA(ctx, cudaMemcpyAsync(sc.bnorm2, sc.rr, nrhs * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-
-    std::vector<double> h_rr(nrhs), h_b2(nrhs);
-    std::vector<int> h_act(nrhs, 1);
-    SMG_CUDA(ctx, cudaMemcpyAsync(h_b2.data(), sc.bnorm2, nrhs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    out.rr.assign(nrhs, 0.0);
+    out.b2.assign(nrhs, 0.0);
+    out.active.assign(nrhs, 1);
+    SMG_CUDA(ctx, cudaMemcpyAsync(out.b2.data(), sc.bnorm2, nrhs * sizeof(double), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
     SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    for (int j = 0; j < nrhs; ++j) h_act[j] = (h_b2[j] >= 1e-60 && std::isfinite(h_b2[j])) ? 1 : 0;
-    bool nonfinite = false;
-    for (int j = 0; j < nrhs; ++j)
-        if (!std::isfinite(h_b2[j])) nonfinite = true;
-
+    out.rr = out.b2;
+    for (int j = 0; j < nrhs; ++j) {
+        out.active[j] = (out.b2[j] >= 1e-60 && std::isfinite(out.b2[j])) ? 1 : 0;
+        if (!std::isfinite(out.b2[j])) out.nonfinite = true;
+    }
     std::vector<int> ring;  // buffer indices of stored directions, oldest first
     int work = 0;           // buffer index of the current (p, Ap) pair
     std::vector<int> freeb;
-    for (int i = 1; i < nbuf; ++i) freeb.push_back(i);
+    for (int i = 1; i < ws.nbuf; ++i) freeb.push_back(i);
     int iter = 0;
     const ReduceLaunch rl = reduce_launch(V, nrhs);
     SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * nrhs * 3));
     bool any_active = false;
-    for (int j = 0; j < nrhs; ++j) any_active |= h_act[j] != 0;
+    for (int j = 0; j < nrhs; ++j) any_active |= out.active[j] != 0;
+    std::vector<double> h_apr(3 * nrhs);
     while (any_active && iter < max_iter) {
-        SMG_CUDA(ctx, cudaMemcpyAsync(sc.active, h_act.data(), nrhs * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+        SMG_CUDA(ctx, cudaMemcpyAsync(sc.active, out.active.data(), nrhs * sizeof(int), cudaMemcpyHostToDevice,
+                                      ctx->stream));
         // z = M^-1 r
-        if (!mg) {
-            SMG_CUDA(ctx, cudaMemcpyAsync(z->data, r->data, r->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-        } else if (!mixed) {
-            SMG_TRY(smg_mg_apply_internal(mg, r, z));
-        } else {
-            // FP32 cycle on r / ||r||, then z = ||r|| * M^-1 (r / ||r||) in FP64
-            VecView<float> rl32 = fv<float>(rlo);
-            k_vconvert_scaled<float, T><<<vec_grid(V, nrhs), vec_block(nrhs), 0, ctx->stream>>>(
-                rl32, (const cx<T>*)r->data, sc.rr, 1);
-            SMG_TRY(smg_mg_apply_internal(mg, rlo, zlo));
-            k_vconvert_scaled<T, float><<<vec_grid(V, nrhs), vec_block(nrhs), 0, ctx->stream>>>(
-                fv<T>(z), (const cx<float>*)zlo->data, sc.rr, 0);
-            count_launch(ctx, 2);
-            SMG_CHECK_LAUNCH(ctx);
-        }
+        if (!mg)
+            SMG_CUDA(ctx, cudaMemcpyAsync(ws.z->data, ws.r->data, ws.r->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+        else
+            SMG_TRY(smg_mg_apply_internal(mg, ws.r, ws.z));
         // p = z, Ap = A z, orthogonalised against the stored directions
-        smg_field* p = P[work];
-        smg_field* Ap = AP[work];
-        SMG_TRY(apply_A<T>(d, z, tmp, Az));
-        SMG_CUDA(ctx, cudaMemcpyAsync(p->data, z->data, z->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-        SMG_CUDA(ctx, cudaMemcpyAsync(Ap->data, Az->data, Az->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+        smg_field* p = ws.P[work];
+        smg_field* Ap = ws.AP[work];
+        SMG_TRY(apply_A<T>(d, ws.z, ws.tmp, ws.Az));
+        SMG_CUDA(ctx, cudaMemcpyAsync(p->data, ws.z->data, ws.z->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+        SMG_CUDA(ctx, cudaMemcpyAsync(Ap->data, ws.Az->data, ws.Az->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
         for (int slot : ring) {
             // <AP_i, Az> (classical Gram-Schmidt on Az, as solvers.cpp:260-267)
-            SMG_TRY(reduce_into<T>(ctx, fv<T>(AP[slot]), (const cx<T>*)Az->data, VR_DOT, dots));
+            SMG_TRY(reduce_into<T>(ctx, fv<T>(ws.AP[slot]), (const cx<T>*)ws.Az->data, VR_DOT, ws.dots));
             k_gcr_orth<T><<<vec_grid(V, nrhs), vec_block(nrhs), 0, ctx->stream>>>(
-                fv<T>(p), (cx<T>*)Ap->data, (const cx<T>*)P[slot]->data, (const cx<T>*)AP[slot]->data, dots,
-                apr_of(slot), ref_coeff);
+                fv<T>(p), (cx<T>*)Ap->data, (const cx<T>*)ws.P[slot]->data, (const cx<T>*)ws.AP[slot]->data, ws.dots,
+                ws.apr_of(slot), ref_coeff);
             count_launch(ctx);
             SMG_CHECK_LAUNCH(ctx);
         }
         // <Ap, r> and ||Ap||^2 into this buffer's scalar slot
-        SMG_TRY(reduce_into<T>(ctx, fv<T>(Ap), (const cx<T>*)r->data, VR_DOTNORM, apr_of(work)));
-        sc.apr3 = apr_of(work);
-        k_gcr_update<T><<<rl.grid, rl.block, 0, ctx->stream>>>(sc, fv<T>(x), (cx<T>*)r->data, (const cx<T>*)p->data,
-                                                               (const cx<T>*)Ap->data, ctx->red.partials,
-                                                               ctx->red.tickets);
+        SMG_TRY(reduce_into<T>(ctx, fv<T>(Ap), (const cx<T>*)ws.r->data, VR_DOTNORM, ws.apr_of(work)));
+        sc.apr3 = ws.apr_of(work);
+        k_gcr_update<T><<<rl.grid, rl.block, 0, ctx->stream>>>(sc, fv<T>(x), (cx<T>*)ws.r->data,
+                                                               (const cx<T>*)p->data, (const cx<T>*)Ap->data,
+                                                               ctx->red.partials, ctx->red.tickets);
         count_launch(ctx);
         SMG_CHECK_LAUNCH(ctx);
         // host: stop rule and breakdown (||Ap||^2 < 1e-30 clears the history, solvers.cpp:272-276)
-        std::vector<double> h_apr(3 * nrhs);
-        SMG_CUDA(ctx, cudaMemcpyAsync(h_rr.data(), sc.rr, nrhs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-        SMG_CUDA(ctx, cudaMemcpyAsync(h_apr.data(), apr_of(work), 3 * nrhs * sizeof(double), cudaMemcpyDeviceToHost,
+        SMG_CUDA(ctx, cudaMemcpyAsync(out.rr.data(), sc.rr, nrhs * sizeof(double), cudaMemcpyDeviceToHost,
                                       ctx->stream));
+        SMG_CUDA(ctx, cudaMemcpyAsync(h_apr.data(), ws.apr_of(work), 3 * nrhs * sizeof(double),
+                                      cudaMemcpyDeviceToHost, ctx->stream));
         SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         bool breakdown = false;
         for (int j = 0; j < nrhs; ++j)
-            if (h_act[j] && !(h_apr[3 * j + 2] >= 1e-30)) breakdown = true;
+            if (out.active[j] && !(h_apr[3 * j + 2] >= 1e-30)) breakdown = true;
         if (breakdown) {
             for (int slot : ring) freeb.push_back(slot);
             ring.clear();
             bool any_nan = false;
             for (int j = 0; j < nrhs; ++j)
-                if (h_act[j] && !std::isfinite(h_apr[3 * j + 2])) any_nan = true;
+                if (out.active[j] && !std::isfinite(h_apr[3 * j + 2])) any_nan = true;
             if (any_nan) {
-                nonfinite = true;
+                out.nonfinite = true;
                 break;
             }
             continue;  // the reference retries without counting an iteration
@@ -546,48 +563,195 @@ smg_status gcr_run(smg_dirac* d, smg_mg* mg, const smg_field* b, smg_field* x, i
         freeb.pop_back();
         any_active = false;
         for (int j = 0; j < nrhs; ++j) {
-            if (h_act[j]) {
-                if (!std::isfinite(h_rr[j])) {
-                    nonfinite = true;
-                    h_act[j] = 0;
-                } else if (h_rr[j] < tol * tol * h_b2[j]) {
-                    h_act[j] = 0;
+            if (out.active[j]) {
+                if (!std::isfinite(out.rr[j])) {
+                    out.nonfinite = true;
+                    out.active[j] = 0;
+                } else if (out.rr[j] < tol * tol * out.b2[j]) {
+                    out.active[j] = 0;
                 }
             }
-            any_active |= h_act[j] != 0;
+            any_active |= out.active[j] != 0;
         }
     }
+    out.iterations = iter;
+    return SMG_OK;
+}
+
+template <typename T>
+smg_status gcr_run(smg_dirac* d, smg_mg* mg, const smg_field* b, smg_field* x, int max_iter, double tol, int trunc,
+                   int ref_coeff, smg_solve_result* res) {
+    smg_context* ctx = d->ctx;
+    const int nrhs = b->nrhs;
+    GcrWs<T> ws;
+    SMG_TRY(ws.init(ctx, b, trunc));
+    GcrOut out;
+    SMG_TRY(gcr_core<T>(d, mg, ws, b, x, max_iter, tol, trunc, ref_coeff, out));
     // true residual in the field precision
-    SMG_TRY(apply_A<T>(d, x, tmp, Az));
+    SMG_TRY(apply_A<T>(d, x, ws.tmp, ws.Az));
     int64_t n = b->n_complex();
-    k_residual<T><<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>((const cx<T>*)b->data, (const cx<T>*)Az->data,
-                                                                      (cx<T>*)r->data, n);
+    k_residual<T><<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>((const cx<T>*)b->data,
+                                                                      (const cx<T>*)ws.Az->data,
+                                                                      (cx<T>*)ws.r->data, n);
     count_launch(ctx);
-    SMG_TRY(reduce_into<T>(ctx, fv<T>(r), nullptr, VR_NORM, truev));
+    SMG_TRY(reduce_into<T>(ctx, fv<T>(ws.r), nullptr, VR_NORM, ws.truev));
     std::vector<double> h_true(nrhs);
-    SMG_CUDA(ctx, cudaMemcpyAsync(h_true.data(), truev, nrhs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    SMG_CUDA(ctx, cudaMemcpyAsync(h_rr.data(), sc.rr, nrhs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    SMG_CUDA(ctx, cudaFreeAsync(blk, ctx->stream));
+    SMG_CUDA(ctx, cudaMemcpyAsync(h_true.data(), ws.truev, nrhs * sizeof(double), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
     SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     double worst_rec = 0, worst_true = 0;
     bool notconv = false;
     for (int j = 0; j < nrhs; ++j) {
-        if (h_b2[j] > 0 && std::isfinite(h_b2[j])) {
-            worst_rec = std::max(worst_rec, std::sqrt(h_rr[j] / h_b2[j]));
-            worst_true = std::max(worst_true, std::sqrt(h_true[j] / h_b2[j]));
+        if (out.b2[j] > 0 && std::isfinite(out.b2[j])) {
+            worst_rec = std::max(worst_rec, std::sqrt(out.rr[j] / out.b2[j]));
+            worst_true = std::max(worst_true, std::sqrt(h_true[j] / out.b2[j]));
         }
-        if (h_act[j]) notconv = true;
+        if (out.active[j]) notconv = true;
     }
     if (res) {
-        res->iterations = iter;
+        res->iterations = out.iterations;
         res->final_residual = worst_rec;
         res->true_residual = worst_true;
-        res->operator_applications = iter + 1;
+        res->operator_applications = out.iterations + 1;
     }
     if (mg) SMG_TRY(smg_mg_check_device_error(mg));
-    if (nonfinite) return smg_fail(ctx, SMG_NONFINITE, "gcr_solve: non-finite residual");
+    if (out.nonfinite) return smg_fail(ctx, SMG_NONFINITE, "gcr_solve: non-finite residual");
     if (notconv) return smg_fail(ctx, SMG_NOT_CONVERGED, "gcr_solve: iteration limit reached");
     return SMG_OK;
+}
+
+// out(D) = mult[rhs] * in(S) per right-hand side (fine fields)
+template <typename D, typename S>
+__global__ void k_convert_mul(VecView<D> out, const cx<S>* __restrict__ in, const double* __restrict__ mult) {
+    const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
+    const int s = blockIdx.x * blockDim.y + threadIdx.y;
+    if (rhs >= out.nrhs || s >= out.nsites) return;
+    const double f = mult[rhs];
+    const int64_t base = out.idx(s, rhs, 0);
+    for (int d = 0; d < out.ndof; ++d) {
+        const cx<S> v = in[base + d];
+        out.p[base + d] = mk<D>((D)((double)v.re * f), (D)((double)v.im * f));
+    }
+}
+
+// y(D) += mult[rhs] * x(S) per right-hand side (fine fields)
+template <typename D, typename S>
+__global__ void k_axpy_mul(VecView<D> y, const cx<S>* __restrict__ x, const double* __restrict__ mult) {
+    const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
+    const int s = blockIdx.x * blockDim.y + threadIdx.y;
+    if (rhs >= y.nrhs || s >= y.nsites) return;
+    const double f = mult[rhs];
+    const int64_t base = y.idx(s, rhs, 0);
+    for (int d = 0; d < y.ndof; ++d) {
+        const cx<S> v = x[base + d];
+        const cx<D> o = y.p[base + d];
+        y.p[base + d] = mk<D>((D)((double)o.re + (double)v.re * f), (D)((double)o.im + (double)v.im * f));
+    }
+}
+
+// Mixed precision: FP64 defect correction around an FP32 GCR preconditioned
+// by the FP32 hierarchy.  Each outer step forms the true FP64 residual
+// r = b - A x, solves A e = r / ||r|| in FP32 to kInnerTol (or further when
+// that suffices for tol), and adds x += ||r|| e in FP64.  FP64 work is one
+// D^dag D per outer step and the residual reductions.
+constexpr double kInnerTol = 1e-5;
+
+smg_status gcr_mixed(smg_dirac* d, smg_mg* mg, const smg_field* b, smg_field* x, int max_iter, double tol, int trunc,
+                     int ref_coeff, smg_solve_result* res) {
+    smg_context* ctx = d->ctx;
+    const int nrhs = b->nrhs, V = b->g.V;
+    FieldSet fs;
+    smg_field *r64, *t64, *Ax64;
+    SMG_TRY(fs.add(b, &r64));
+    SMG_TRY(fs.add(b, &t64));
+    SMG_TRY(fs.add(b, &Ax64));
+    smg_field *r32 = nullptr, *e32 = nullptr;
+    SMG_TRY(smg_field_alloc_like(b, SMG_F32, &r32));
+    fs.f.push_back(r32);
+    SMG_TRY(smg_field_alloc_like(b, SMG_F32, &e32));
+    fs.f.push_back(e32);
+    GcrWs<float> ws;
+    SMG_TRY(ws.init(ctx, r32, trunc));
+    double* sc = nullptr;  // [0, nrhs) ||r||^2, [nrhs, 2 nrhs) multipliers
+    SMG_CUDA(ctx, cudaMallocAsync((void**)&sc, (size_t)2 * nrhs * sizeof(double), ctx->stream));
+    std::vector<double> b2(nrhs), rr(nrhs), mult(nrhs);
+    // x = 0, r = b
+    SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
+    SMG_CUDA(ctx, cudaMemcpyAsync(r64->data, b->data, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    SMG_TRY(reduce_into<double>(ctx, fv<double>(r64), nullptr, VR_NORM, sc));
+    SMG_CUDA(ctx, cudaMemcpyAsync(b2.data(), sc, nrhs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    rr = b2;
+    bool nonfinite = false;
+    for (int j = 0; j < nrhs; ++j)
+        if (!std::isfinite(b2[j])) nonfinite = true;
+    int total = 0;
+    smg_status st = SMG_OK;
+    while (!nonfinite && total < max_iter) {
+        bool any = false;
+        double worst_ratio = 0;
+        for (int j = 0; j < nrhs; ++j) {
+            const bool act = b2[j] >= 1e-60 && rr[j] >= tol * tol * b2[j];
+            mult[j] = act ? 1.0 / std::sqrt(rr[j]) : 0.0;  // a finished rhs gets a zero inner rhs
+            if (act) {
+                any = true;
+                worst_ratio = std::max(worst_ratio, std::sqrt(rr[j] / b2[j]));
+            }
+        }
+        if (!any) break;
+        // inner tolerance: kInnerTol, or the reduction that reaches tol
+        const double inner_tol = std::max(kInnerTol, 0.5 * tol / worst_ratio);
+        SMG_CUDA(ctx, cudaMemcpyAsync(sc + nrhs, mult.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice,
+                                      ctx->stream));
+        k_convert_mul<float, double><<<vec_grid(V, nrhs), vec_block(nrhs), 0, ctx->stream>>>(
+            fv<float>(r32), (const cx<double>*)r64->data, sc + nrhs);
+        count_launch(ctx);
+        GcrOut out;
+        SMG_TRY(gcr_core<float>(d, mg, ws, r32, e32, max_iter - total, inner_tol, trunc, ref_coeff, out));
+        total += out.iterations;
+        if (out.nonfinite) {
+            nonfinite = true;
+            break;
+        }
+        for (int j = 0; j < nrhs; ++j) mult[j] = mult[j] > 0 ? std::sqrt(rr[j]) : 0.0;
+        SMG_CUDA(ctx, cudaMemcpyAsync(sc + nrhs, mult.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice,
+                                      ctx->stream));
+        k_axpy_mul<double, float><<<vec_grid(V, nrhs), vec_block(nrhs), 0, ctx->stream>>>(
+            fv<double>(x), (const cx<float>*)e32->data, sc + nrhs);
+        count_launch(ctx);
+        // true FP64 residual
+        SMG_TRY(apply_A<double>(d, x, t64, Ax64));
+        const int64_t n = b->n_complex();
+        k_residual<double><<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
+            (const cx<double>*)b->data, (const cx<double>*)Ax64->data, (cx<double>*)r64->data, n);
+        count_launch(ctx);
+        SMG_TRY(reduce_into<double>(ctx, fv<double>(r64), nullptr, VR_NORM, sc));
+        SMG_CUDA(ctx, cudaMemcpyAsync(rr.data(), sc, nrhs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int j = 0; j < nrhs; ++j)
+            if (!std::isfinite(rr[j])) nonfinite = true;
+        if (out.iterations == 0) break;  // no progress possible
+    }
+    SMG_CUDA(ctx, cudaFreeAsync(sc, ctx->stream));
+    double worst = 0;
+    bool notconv = false;
+    for (int j = 0; j < nrhs; ++j) {
+        if (b2[j] > 0 && std::isfinite(b2[j])) {
+            const double rel = std::sqrt(rr[j] / b2[j]);
+            worst = std::max(worst, rel);
+            if (!(rel < tol)) notconv = true;
+        }
+    }
+    if (res) {
+        res->iterations = total;
+        res->final_residual = worst;
+        res->true_residual = worst;
+        res->operator_applications = total + 1;
+    }
+    SMG_TRY(smg_mg_check_device_error(mg));
+    if (nonfinite) st = smg_fail(ctx, SMG_NONFINITE, "gcr_solve: non-finite residual");
+    else if (notconv) st = smg_fail(ctx, SMG_NOT_CONVERGED, "gcr_solve: iteration limit reached");
+    return st;
 }
 
 }  // namespace
@@ -603,7 +767,11 @@ SMG_API smg_status smg_gcr_solve(smg_dirac* d, smg_mg* mg, const smg_field* rhs,
     if (rhs->g.L != d->gauge->g.L) return smg_fail(ctx, SMG_BAD_ARG, "field L differs from gauge L");
     if (max_iter < 0 || !(tol > 0) || trunc < 1 || trunc > 256)
         return smg_fail(ctx, SMG_BAD_ARG, "max_iter >= 0, tol > 0 and trunc in [1, 256] required");
-    if (rhs->prec == SMG_F64) return gcr_run<double>(d, mg, rhs, x, max_iter, tol, trunc, reference_coefficient, res);
+    if (rhs->prec == SMG_F64) {
+        if (mg && smg_mg_precision(mg) == SMG_F32)
+            return gcr_mixed(d, mg, rhs, x, max_iter, tol, trunc, reference_coefficient, res);
+        return gcr_run<double>(d, mg, rhs, x, max_iter, tol, trunc, reference_coefficient, res);
+    }
     if (rhs->prec == SMG_F32) {
         if (mg && smg_mg_precision(mg) == SMG_F64)
             return smg_fail(ctx, SMG_UNSUPPORTED, "an F64 hierarchy needs F64 fields");

@@ -1,11 +1,14 @@
 // Generic vector kernels for fine and coarse MG vectors.
 //
-// Every MG vector has the layout [site][rhs][dof] with the dof index
-// innermost: dof = 2 spin components on the fine lattice (the smg_field
-// layout) and dof = Nc coarse degrees of freedom on a coarse lattice.  All
-// per-right-hand-side scalars live in device memory; kernels that need a
-// derived coefficient (alpha, omega, beta) compute it once per block from
-// those scalars, so no host round trip sits between solver steps.
+// Fine MG vectors (smg_field) have the layout [site][rhs][dof] with the two
+// spin components innermost.  Coarse MG vectors have the layout
+// [site][dof][rhs] with the right-hand side innermost, so a warp of RHS lanes
+// reads consecutive addresses for every dof and a dof row of all RHS is one
+// contiguous tile (the B operand of the coarse-operator contraction).  For one
+// right-hand side both layouts are the same array.  All per-right-hand-side
+// scalars live in device memory; kernels that need a derived coefficient
+// (alpha, omega, beta) compute it once per block from those scalars, so no
+// host round trip sits between solver steps.
 #pragma once
 #include "reduce.cuh"
 #include "smg_internal.h"
@@ -14,10 +17,13 @@ template <typename T>
 struct VecView {
     cx<T>* p = nullptr;
     int nsites = 0, nrhs = 1, ndof = 2;
+    int rhs_inner = 0;  // 0: [site][rhs][dof] (fine), 1: [site][dof][rhs] (coarse)
     __host__ __device__ int64_t n() const { return (int64_t)nsites * nrhs * ndof; }
     __host__ __device__ int64_t idx(int64_t site, int rhs, int dof) const {
-        return (site * nrhs + rhs) * ndof + dof;
+        return rhs_inner ? (site * ndof + dof) * nrhs + rhs : (site * nrhs + rhs) * ndof + dof;
     }
+    // distance between consecutive dofs of one (site, rhs)
+    __host__ __device__ int dstride() const { return rhs_inner ? nrhs : 1; }
 };
 
 // per-rhs scalar slots used by the MG kernels (device memory)
@@ -39,11 +45,12 @@ __global__ void __launch_bounds__(256) k_vreduce(VecView<T> a, const cx<T>* __re
     if (rhs < a.nrhs) {
         for (int s = blockIdx.x * blockDim.y + threadIdx.y; s < a.nsites; s += gridDim.x * blockDim.y) {
             const int64_t base = a.idx(s, rhs, 0);
+            const int ds = a.dstride();
             T r0 = 0, r1 = 0, r2 = 0;
             for (int d = 0; d < a.ndof; ++d) {
-                cx<T> x = a.p[base + d];
+                cx<T> x = a.p[base + (int64_t)d * ds];
                 if (MODE != VR_NORM) {
-                    cx<T> c = cmulc(x, b[base + d]);
+                    cx<T> c = cmulc(x, b[base + (int64_t)d * ds]);
                     r0 += c.re;
                     r1 += c.im;
                 }
@@ -72,7 +79,8 @@ __global__ void k_vaxpy(VecView<T> y, const cx<T>* __restrict__ x, const double*
     if (rhs >= y.nrhs || s >= y.nsites) return;
     const cx<T> a = mk<T>((T)(sgn * coef[2 * rhs]), (T)(sgn * coef[2 * rhs + 1]));
     const int64_t base = y.idx(s, rhs, 0);
-    for (int d = 0; d < y.ndof; ++d) y.p[base + d] = y.p[base + d] + a * x[base + d];
+    const int ds = y.dstride();
+    for (int d = 0; d < y.ndof; ++d) y.p[base + (int64_t)d * ds] = y.p[base + (int64_t)d * ds] + a * x[base + (int64_t)d * ds];
 }
 
 // MR step (reference src/smoother.cpp:26-40):  omega = <Ar, r> / <Ar, Ar>,
@@ -96,10 +104,11 @@ __global__ void __launch_bounds__(256) k_mr_update(VecView<T> x, cx<T>* __restri
     if (rhs >= x.nrhs || s >= x.nsites) return;
     const cx<T> om = s_om[threadIdx.x];
     const int64_t base = x.idx(s, rhs, 0);
+    const int ds = x.dstride();
     for (int d = 0; d < x.ndof; ++d) {
-        const cx<T> ri = r[base + d];
-        x.p[base + d] = x.p[base + d] + om * ri;
-        r[base + d] = ri - om * Ar[base + d];
+        const cx<T> ri = r[base + (int64_t)d * ds];
+        x.p[base + (int64_t)d * ds] = x.p[base + (int64_t)d * ds] + om * ri;
+        r[base + (int64_t)d * ds] = ri - om * Ar[base + (int64_t)d * ds];
     }
 }
 
@@ -131,9 +140,10 @@ __global__ void k_vconvert_scaled(VecView<D> out, const cx<S>* __restrict__ in, 
         f = invert ? (sv > 0 ? 1.0 / sqrt(sv) : 0.0) : sqrt(sv);
     }
     const int64_t base = out.idx(s, rhs, 0);
+    const int ds = out.dstride();
     for (int d = 0; d < out.ndof; ++d) {
-        cx<S> v = in[base + d];
-        out.p[base + d] = mk<D>((D)((double)v.re * f), (D)((double)v.im * f));
+        cx<S> v = in[base + (int64_t)d * ds];
+        out.p[base + (int64_t)d * ds] = mk<D>((D)((double)v.re * f), (D)((double)v.im * f));
     }
 }
 
