@@ -1,6 +1,6 @@
 """Benchmark of the Wilson-clover Dirac operator and its MG solve path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload mg|dslash|cg] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload mg|dslash|cg|coarse] [--impl ours|reference]
 
 Prints ONE JSON line (rank 0).  A step is one pass of the hot path over one
 batch of seeded synthetic input (links U = exp(i theta), theta ~ N(0, 1/beta);
@@ -8,15 +8,17 @@ Gaussian complex sources), timed with CUDA events on the library's stream
 (smg_timer_begin/end) between a barrier and a synchronize; the max over ranks
 is reported.  Workloads:
 
-* mg (default) — the multi-RHS MG-GCR solve of BASELINE config 3: 512 x 512
-  lattice, beta = 6, m = -0.05, c_sw = 1; three levels (4 x 4 then 2 x 2
+* mg (default) — the multi-RHS MG-GCR solve on a 512 x 512 lattice, beta = 6, m = -0.05, c_sw = 1; three levels (4 x 4 then 2 x 2
   aggregates, 8 null vectors split by chirality = 16 coarse dofs per level);
   32 right-hand sides solved together to a true FP64 residual of 1e-10 by an
-  FP64 GCR preconditioned with the FP32 hierarchy.  The hierarchy is built
+  FP32 GCR preconditioned with the FP32 hierarchy inside FP64 defect correction.  The hierarchy is built
   once before timing.  value = solves/s.  The plain FP64 single-RHS MG on the
   same inputs is measured beside it (config.plain_fp64_mg_solves_per_s).
 * dslash — FP32 D on 32 right-hand sides at L = 512; value = algorithmic GB/s.
-* cg — BASELINE config 1 (L = 32, beta = 2, m = 0.1, c_sw = 1) FP64 CG;
+* coarse — the level-1 coarse operator of the mg workload alone (128 x 128
+  sites, 16 dofs, 32 RHS); value = algorithmic GB/s.  A small case for
+  kernel profiles.
+* cg — the small single-RHS case (L = 32, beta = 2, m = 0.1, c_sw = 1) FP64 CG;
   value = solves/s.
 
 `--impl reference` times the reference's CPU implementation of the same
@@ -31,6 +33,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -57,11 +60,10 @@ class Clocks:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        self.path = Path(tempfile.gettempdir()) / f"smg_clocks_{os.getpid()}.csv"
 
     def __enter__(self):
         try:
-            self.path.parent.mkdir(exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device),
@@ -142,6 +144,23 @@ def dslash_bytes_f64_single(L):
     return L * L * 104
 
 
+def sized(base: dict, args) -> dict:
+    """A workload's configuration with the --L / --nrhs overrides (smaller cases for profiles)."""
+    c = dict(base)
+    if args.L:
+        c["L"] = args.L
+    if args.nrhs:
+        c["nrhs"] = args.nrhs
+    return c
+
+
+def coarse_kernel_name(c, L, nrhs):
+    lc = L // c["blocks"][0][0]
+    if nrhs % 32 == 0 and lc % 8 == 0:
+        return f"k_coarse_apply_tc<0> (tcgen05 BF16, level 1, {lc}x{lc}x16, {nrhs} RHS)"
+    return f"k_coarse_apply_tiled<float,0,16> (level 1, {lc}x{lc}x16, {nrhs} RHS)"
+
+
 def mg_params(smg, c, precision):
     return smg.mg_params(c["levels"], c["blocks"][0][0], c["n_vec"], blocks=c["blocks"], chiral_split=c["chiral"],
                          null_iters=c["null_iters"], pre_smooth=c["pre"], post_smooth=c["post"],
@@ -173,7 +192,7 @@ def run_ours(args, ws, rank, local):
         return max_over_ranks(ms, ws)
 
     if args.workload == "mg":
-        c = MG
+        c = sized(MG, args)
         L, nrhs = c["L"], c["nrhs"]
         U = smg.gauge_normal(L, c["beta"], c["seed"])
         lat = smg.Lattice(L)
@@ -218,7 +237,7 @@ def run_ours(args, ws, rank, local):
         sol = host_out.numpy().view(np.complex128).reshape(nrhs, -1)
         hb = B.size * 16
 
-        # plain FP64 single-RHS MG (the denominator of the BASELINE target)
+        # plain FP64 single-RHS MG on the same inputs (the comparison point of the mixed batched solve)
         mg64 = smg.MGHierarchy(D, mg_params(smg, c, "f64"))
         b1 = smg.Field(lat, 1, "f64", ctx, data=B[0])
         x1 = smg.Field(lat, 1, "f64", ctx)
@@ -238,24 +257,26 @@ def run_ours(args, ws, rank, local):
         dgbs = dslash_bytes_f32(L, nrhs) / (dms * 1e-3) / 1e9
         out.update({
             "value": value, "unit": "solves/s", "ms_per_step": ms, "higher_is_better": True, "dtype": "f32+f64",
-            "config": {"workload": "MG-GCR, L=512 (beta=6, m=-0.05, c_sw=1), 32 RHS, 3 levels (4x4, 2x2; 16 dof), "
-                                   "FP64 GCR with FP32 hierarchy, true FP64 residual 1e-10",
+            "config": {"workload": f"MG-GCR, L={L} (beta=6, m=-0.05, c_sw=1), {nrhs} RHS, 3 levels (4x4, 2x2; 16 dof), "
+                                   "FP32 GCR + FP32 hierarchy inside FP64 defect correction, true FP64 residual 1e-10",
                        "L": L, "nrhs": nrhs, "levels": c["levels"], "gcr_iterations": iters,
+                       "launches_before_timed": int(l0),
                        "true_residual": true_res, "setup_s": setup_s,
                        "plain_fp64_mg_solves_per_s": 1e3 / ms64, "plain_fp64_mg_iterations": it64,
                        "mixed_batched_over_plain_fp64": value / ws / (1e3 / ms64),
                        "fine_dslash_f32_32rhs_gbs": dgbs, "fine_dslash_frac_of_hbm": dgbs / peak,
-                       "l2": "fine fields of 32 RHS (134 MB FP32, 268 MB FP64) exceed the 129 MB L2; no flush"},
+                       "l2": f"fine fields of {nrhs} RHS ({16 * L * L * nrhs / 1e6:.0f} MB FP32) "
+                                 f"{'exceed' if 16 * L * L * nrhs > 129e6 else 'fit in'} the 129 MB L2; no flush"},
             "e2e": {"value": ws * nrhs / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": hb,
                     "d2h_bytes_per_step": hb, "ms_per_step": e2e_ms, "finite": bool(np.isfinite(sol).all())},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "kernel": "k_coarse_apply_tiled<float,0,16> (level 1, 128x128x16, 32 RHS)",
+                         "traffic": None, "kernel": coarse_kernel_name(c, L, nrhs),
                          "bytes_per_launch": cbytes.value, "ms_per_launch": cms.value, "peak_source": peak_kind},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
         })
     elif args.workload == "dslash":
-        c = DSLASH
+        c = sized(DSLASH, args)
         L, nrhs = c["L"], c["nrhs"]
         U = smg.gauge_normal(L, c["beta"], c["seed"])
         lat = smg.Lattice(L)
@@ -292,7 +313,7 @@ def run_ours(args, ws, rank, local):
         hb = srcs.size * 16
         out.update({
             "value": value, "unit": "GB/s", "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
-            "config": {"workload": "FP32 Wilson-clover D on 32 RHS, L=512 (beta=6, m=-0.05, c_sw=1)",
+            "config": {"workload": f"FP32 Wilson-clover D on {nrhs} RHS, L={L} (beta=6, m=-0.05, c_sw=1)",
                        "L": L, "nrhs": nrhs, "bytes_per_step": bytes_step,
                        "l2": "inputs and outputs (268 MB) exceed the 129 MB L2; no flush",
                        "timed_steps": max(args.steps, 2000)},
@@ -300,6 +321,34 @@ def run_ours(args, ws, rank, local):
                     "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb, "ms_per_step": e2e_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "kernel": "k_dslash<float,false,0>", "peak_source": peak_kind},
+            "gpu_launches": int(launches), "clocks": clk.summary(),
+        })
+    elif args.workload == "coarse":
+        # the level-1 coarse operator alone: (L/4)^2 sites, 16 dofs, 32 RHS, 9-point stencil
+        c = sized(MG, args)
+        L, nrhs = c["L"], c["nrhs"]
+        U = smg.gauge_normal(L, c["beta"], c["seed"])
+        lat = smg.Lattice(L)
+        g = smg.GaugeField(lat, U, ctx)
+        D = smg.DiracOp(lat, g, c["m"], c["r"], c["csw"], c["mu"])
+        mg32 = smg.MGHierarchy(D, mg_params(smg, c, "f32"))
+        cms, cbytes = Cc.c_double(), Cc.c_double()
+        reps = max(args.steps, 200)
+        l0 = ctx.kernel_launches
+        with Clocks(local) as clk:
+            smg._lib.check(lib.smg_mg_time_coarse_apply(mg32.h, 1, nrhs, reps, Cc.byref(cms), Cc.byref(cbytes)),
+                           "smg_mg_time_coarse_apply", ctx.h)
+        launches = (ctx.kernel_launches - l0) // 2  # warm-up pass + timed pass
+        gbs = cbytes.value / (cms.value * 1e-3) / 1e9
+        out.update({
+            "value": gbs * ws, "unit": "GB/s", "ms_per_step": cms.value, "higher_is_better": True, "dtype": "f32",
+            "config": {"workload": f"level-1 coarse operator apply, {L // 4}x{L // 4} sites x 16 dof, {nrhs} RHS "
+                                   f"(L={L} fine, 4x4 aggregates, 8 chiral null vectors)",
+                       "bytes_per_launch": cbytes.value, "timed_launches": reps,
+                       "l2": "links and vectors exceed the 129 MB L2 at L=512; no flush"},
+            "e2e": None,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "traffic": None, "kernel": coarse_kernel_name(c, L, nrhs), "peak_source": peak_kind},
             "gpu_launches": int(launches), "clocks": clk.summary(),
         })
     else:
@@ -341,7 +390,7 @@ def run_ours(args, ws, rank, local):
                     "e2e": {"value": ws * 1e3 / e2e_ms, "unit": "solves/s", "h2d_bytes_per_step": bh.nbytes,
                             "d2h_bytes_per_step": xh.nbytes, "ms_per_step": e2e_ms},
                     "gpu_launches": int(launches), "clocks": clk.summary()})
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and args.workload != "coarse":
         out["cpu_baseline"] = cpu_baseline(args.workload, ctx_objects=locals())
     return out
 
@@ -356,7 +405,7 @@ def cpu_baseline(workload: str, threads: int | None = None, ctx_objects=None):
     n_threads = threads or os.cpu_count() or 1
     port.set_threads(n_threads)
     if workload == "mg":
-        c = MG
+        c = ctx_objects.get("c", MG) if ctx_objects else MG
         L = c["L"]
         mg32 = ctx_objects["mg32"] if ctx_objects else None
         U = smg.gauge_normal(L, c["beta"], c["seed"])
@@ -427,9 +476,11 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="mg", choices=["mg", "dslash", "cg"])
+    ap.add_argument("--workload", default="mg", choices=["mg", "dslash", "cg", "coarse"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--L", type=int, default=0, help="lattice size override (smaller cases for profiles)")
+    ap.add_argument("--nrhs", type=int, default=0, help="right-hand-side count override")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()

@@ -233,6 +233,10 @@ typedef struct {
     double coarse_tol;                 /* coarsest CG (reference 1e-12)         */
     smg_precision precision;           /* F64, or F32 smoother and coarse levels */
     uint32_t seed;                     /* std::mt19937 seed of the start vectors */
+    int tensor_cores;                  /* 1 (default): an F32 hierarchy applies its coarse operators
+                                          with 16 dofs per site to multiples of 32 right-hand sides
+                                          on the tensor cores (BF16 operands, FP32 accumulation);
+                                          0: FP32 on the CUDA cores */
 } smg_mg_params;
 
 /* Fills p with the reference's defaults: 2 levels, 4 x 4 blocks, 4 null
@@ -266,7 +270,10 @@ SMG_API smg_status smg_mg_get_prolongator(smg_mg* mg, int level, double* block_v
  * (src/coarse_op.h:159-166): [site][dir][ki * k + kj] complex. */
 SMG_API smg_status smg_mg_get_coarse_op(smg_mg* mg, int level, double* links);
 /* x = M^-1 b, one MG cycle (MGHierarchy::precondition, src/multigrid.cpp:155;
- * mg_cycle, :43-102).  b and x are fine fields of the hierarchy's L. */
+ * mg_cycle, :43-102).  b and x are fine fields of the hierarchy's L.  The
+ * cycle is replayed as a CUDA graph per (nrhs, precision); with the
+ * environment variable SMG_CUDA_GRAPHS=0 at smg_mg_create it is launched
+ * kernel by kernel instead. */
 SMG_API smg_status smg_mg_precondition(smg_mg* mg, const smg_field* b, smg_field* x);
 /* Host-array versions of the transfer operators and the coarse operator at
  * level `level` (Prolongator::prolong / restrict_vec, src/prolongator.h:77-108;
@@ -281,6 +288,15 @@ SMG_API smg_status smg_mg_coarse_apply_host(smg_mg* mg, int level, const double*
  * applications timed with CUDA events on the context's stream, and the
  * algorithmic HBM bytes of one application (links once, input and output
  * vectors once). */
+/* The batched coarse operator of level `level` >= 1 of an F32 hierarchy on
+ * host arrays in the device layout, [site][dof][rhs] complex64 with sites
+ * lexicographic on the coarse lattice (SparseCoarseOp::apply on nrhs vectors,
+ * src/coarse_op.h:282-297).  engine 0: FP32 on the CUDA cores; engine 1: the
+ * tensor-core kernel (SMG_UNSUPPORTED unless the level has 16 dofs, a width
+ * divisible by 8 and nrhs is a multiple of 32).  dots (optional, per rhs):
+ * with w, <out, w> (re, im) and ||out||^2; without w, ||out||^2. */
+SMG_API smg_status smg_mg_coarse_apply_batch(smg_mg* mg, int level, int nrhs, int engine, const float* in,
+                                             const float* w, float* out, double* dots);
 SMG_API smg_status smg_mg_time_coarse_apply(smg_mg* mg, int level, int nrhs, int reps, double* ms, double* bytes);
 
 /* fcg_solve / fcg_solve_mg: truncated GCR on A = D^dag D from x = 0

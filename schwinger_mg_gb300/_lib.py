@@ -41,11 +41,12 @@ class MGParams(C.Structure):
                 ("n_vec", C.c_int * (MAX_LEVELS - 1)), ("chiral_split", C.c_int), ("null_iters", C.c_int),
                 ("null_mr_steps", C.c_int), ("pre_smooth", C.c_int), ("post_smooth", C.c_int), ("w_cycle", C.c_int),
                 ("coarse_max_iter", C.c_int), ("coarse_tol", C.c_double), ("precision", C.c_int),
-                ("seed", C.c_uint32)]
+                ("seed", C.c_uint32), ("tensor_cores", C.c_int)]
 
 
 _vp = C.c_void_p
 _dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
 _st = C.c_int
 
 _SIGS = {
@@ -105,6 +106,7 @@ _SIGS = {
     "smg_mg_restrict_host": (_st, [_vp, C.c_int, _dp, _dp]),
     "smg_mg_coarse_apply_host": (_st, [_vp, C.c_int, _dp, _dp]),
     "smg_mg_time_coarse_apply": (_st, [_vp, C.c_int, C.c_int, C.c_int, _dp, _dp]),
+    "smg_mg_coarse_apply_batch": (_st, [_vp, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _dp]),
     "smg_gcr_solve": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(SolveResult)]),
     "smg_host_gauge_normal": (_st, [C.c_int, C.c_double, C.c_uint32, _dp]),
     "smg_host_random_vec": (_st, [C.c_int64, C.c_uint32, _dp]),

@@ -351,10 +351,12 @@ def random_vec(n: int, seed: int) -> np.ndarray:
 def mg_params(n_levels: int = 2, block_size: int = 4, k_null: int = 4, coarse_block=(4, 1), null_iters: int = 20,
               w_cycle: bool = True, pre_smooth: int = 3, post_smooth: int = 3, chiral_split: bool = False,
               blocks=None, n_vecs=None, null_mr_steps: int = 5, coarse_max_iter: int = 200,
-              coarse_tol: float = 1e-12, precision: str = "f64", seed: int = 42) -> _L.MGParams:
+              coarse_tol: float = 1e-12, precision: str = "f64", seed: int = 42,
+              tensor_cores: bool = True) -> _L.MGParams:
     """smg_mg_params from the reference's build_mg_hierarchy arguments
     (src/multigrid.cpp:595-602).  `blocks` / `n_vecs` override the per-level
-    aggregate shapes and null-vector counts."""
+    aggregate shapes and null-vector counts.  `tensor_cores` lets an F32
+    hierarchy apply its batched coarse operators on the tensor cores."""
     p = _L.MGParams()
     _L.check(_L.lib().smg_mg_params_default(C.byref(p)), "smg_mg_params_default")
     p.n_levels = n_levels
@@ -371,6 +373,7 @@ def mg_params(n_levels: int = 2, block_size: int = 4, k_null: int = 4, coarse_bl
     p.coarse_max_iter, p.coarse_tol = coarse_max_iter, coarse_tol
     p.precision = PRECISIONS[precision]
     p.seed = seed
+    p.tensor_cores = int(tensor_cores)
     return p
 
 
@@ -443,6 +446,33 @@ class MGHierarchy(_Handle):
 
     def coarse_apply(self, level: int, v):
         return self._host_op("smg_mg_coarse_apply_host", level, v, self.level_dim(level))
+
+    def coarse_apply_batch(self, level: int, v, engine: str = "cuda", w=None, dots: bool = False):
+        """Batched coarse operator of an F32 hierarchy on a complex64 array
+        [site][dof][rhs] (sites lexicographic on the coarse lattice).  engine
+        "cuda" (FP32 CUDA cores) or "tensor" (BF16 tensor cores, FP32
+        accumulation).  With dots, also returns per rhs ||Av||^2, or
+        (<Av, w>, ||Av||^2) when w is given."""
+        nx, ny, nd = self.level_dims(level)
+        a = np.ascontiguousarray(v, dtype=np.complex64)
+        nrhs = a.size // (nx * ny * nd)
+        if a.size != nx * ny * nd * nrhs:
+            raise ValueError("input size is not a multiple of the coarse vector size")
+        out = np.empty_like(a)
+        fp = C.POINTER(C.c_float)
+        wa = None if w is None else np.ascontiguousarray(w, dtype=np.complex64)
+        k = 3 if wa is not None else 1
+        d = np.zeros(nrhs * k) if dots else None
+        _L.check(_L.lib().smg_mg_coarse_apply_batch(
+            self.h, level, nrhs, {"cuda": 0, "tensor": 1}[engine], a.ctypes.data_as(fp),
+            None if wa is None else wa.ctypes.data_as(fp), out.ctypes.data_as(fp),
+            None if d is None else d.ctypes.data_as(C.POINTER(C.c_double))), "smg_mg_coarse_apply_batch", self.ctx.h)
+        if not dots:
+            return out
+        d = d.reshape(nrhs, k)
+        if wa is None:
+            return out, d[:, 0]
+        return out, d[:, 0] + 1j * d[:, 1], d[:, 2]
 
     def precondition(self, b):
         """One MG cycle x = M^-1 b (MGHierarchy::precondition, src/multigrid.cpp:155)."""

@@ -1,0 +1,519 @@
+// Batched coarse-operator apply on the 5th-generation tensor cores (tcgen05).
+//
+// The coarse operator is a 9-point stencil of Nc x Nc complex blocks
+// (SparseCoarseOp::apply, src/coarse_op.h:154-297):
+//     y[s](i, r) = sum_d sum_j L[s][d](i, j) x[nb(s, d)](j, r)
+// for right-hand sides r.  With Nc = 16 and 32 right-hand sides each site is
+// nine small complex GEMMs.  This kernel computes the transposed product
+// y^T = sum_d x_nb^T L_d^T as real MMAs with BF16 operands and FP32
+// accumulation:
+//
+//   A operand (M x K = 64 x 16, vectors):  row m = 2 r + c holds the real
+//       (c = 0) or imaginary (c = 1) part of x(j, r) for K index j
+//   B operand (N x K = 32 x 16, links):    row n = c' * 16 + i holds
+//       Re L(i, j) (c' = 0) or Im L(i, j) (c' = 1) for K index j
+//   D (M x N, FP32 in tensor memory):      D[2r + c][c' * 16 + i]
+//
+// and the epilogue forms Re y(i, r) = D[2r][i] - D[2r+1][16+i] and
+// Im y(i, r) = D[2r][16+i] + D[2r+1][i] (the two rows sit in adjacent lanes
+// of one warp).  One MMA per direction (K = 16 is one kind::f16 step), nine
+// per site, accumulated in 32 tensor-memory columns.  The MMA is issued with
+// M = 128: rows 64..127 read the next 2 KB of shared memory and are never
+// read back, which keeps the accumulator in the plain one-lane-per-row layout.
+//
+// Data movement (one CTA = a strip of kW = 8 sites along x, H rows):
+//   * links are pre-tiled once per hierarchy into the exact shared-memory
+//     image of the B operand (K-major, no swizzle; 1 KB per site and
+//     direction), so each site's 9 KB arrive with one cp.async.bulk into a
+//     ring of kLinkSlots site slots;
+//   * each source row (kW + 2 sites with the x halo) is converted from the
+//     FP32 vector [site][dof][rhs] layout into BF16 A tiles by four stager
+//     warps and kept in a ring of four rows: the MMAs of output row y read
+//     source rows y-1, y, y+1 and every source tile serves the nine output
+//     sites around it through its shared-memory descriptor;
+//   * warp 0 issues the link copies, warp 1 the MMAs, warps 4 and 5 read the
+//     accumulators (TMEM lanes 0..63) and write y, with the fused per-rhs
+//     reductions ||y||^2 and <y, w> of the FP32 kernels.
+// Every mbarrier wait is bounded (about one second of SM clock); on timeout
+// the CTA raises *err = 2, waits (bounded) for its own bulk copies and MMAs,
+// frees its tensor memory and returns.
+#include <cuda_bf16.h>
+
+#include "smg_internal.h"
+
+namespace {
+
+constexpr int kNc = 16;                       // coarse dofs per site (the supported shape)
+constexpr int kRhsTile = 32;                  // right-hand sides per CTA
+constexpr int kW = 8;                         // output sites per row of a CTA strip
+constexpr int kSrcSites = kW + 2;             // source sites per row (x halo)
+constexpr int kRing = 4;                      // source rows resident
+constexpr int kSboA = 272;                    // A tile: byte stride of 8-row groups (256 + 16 spreads banks)
+constexpr int kTileA = 8 * kSboA;             // 64 rows x 16 K (BF16) = 2176 bytes
+constexpr int kRowBytes = kSrcSites * kTileA;  // one source row
+constexpr int kRingBytes = kRing * kRowBytes;
+constexpr int kLinkDir = 1024;                // 32 x 16 BF16, K-major, no swizzle
+constexpr int kLinkSite = 9 * kLinkDir;       // one site's nine blocks
+constexpr int kLinkSlots = 12;
+constexpr int kLinkBytes = kLinkSlots * kLinkSite;
+constexpr int kAccSlots = 16;                 // 32 TMEM columns each
+constexpr int kTmemCols = 512;
+// barriers: src_full[4], src_empty[4], link_full[LS], link_empty[LS], acc_full[AS], acc_empty[AS], final
+constexpr int kBarSrcFull = 0;
+constexpr int kBarSrcEmpty = kBarSrcFull + kRing;
+constexpr int kBarLinkFull = kBarSrcEmpty + kRing;
+constexpr int kBarLinkEmpty = kBarLinkFull + kLinkSlots;
+constexpr int kBarAccFull = kBarLinkEmpty + kLinkSlots;
+constexpr int kBarAccEmpty = kBarAccFull + kAccSlots;
+constexpr int kBarFinal = kBarAccEmpty + kAccSlots;
+constexpr int kNumBars = kBarFinal + 1;
+constexpr int kBarOffset = kRingBytes + kLinkBytes;           // A-tile over-read (M = 128) lands in the link ring
+constexpr int kMiscOffset = kBarOffset + kNumBars * 8;
+constexpr int kRedOffset = (kMiscOffset + 16 + 15) / 16 * 16;  // 32 rhs x 3 doubles
+constexpr int kSmemBytes = kRedOffset + kRhsTile * 3 * 8;
+static_assert(kSmemBytes <= 227 * 1024, "shared memory budget");
+static_assert(kTileA % 16 == 0 && kRowBytes % 16 == 0 && kLinkSite % 16 == 0, "16-byte alignment");
+
+constexpr long long kWaitCycles = 2000000000ll;  // ~1 s at 2 GHz
+constexpr long long kDrainCycles = 200000000ll;  // ~0.1 s
+
+__device__ __forceinline__ int dir_dx(int d) { return d == 0 || d == 3 || d == 4 ? 0 : (d == 1 || d == 5 || d == 6 ? 1 : -1); }
+__device__ __forceinline__ int dir_dy(int d) { return d <= 2 ? 0 : (d == 3 || d == 5 || d == 7 ? 1 : -1); }
+__device__ __forceinline__ int wrapi(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// ------------------------------------------------------------ mbarrier / bulk copy
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Wait for phase `parity` of a barrier.  Gives up when another thread of the
+// CTA has raised the abort flag, or after kWaitCycles (then raises it).
+__device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+    if (mbar_try(bar, parity)) return true;
+    const long long t0 = clock64();
+    for (int k = 1;; ++k) {
+        if (mbar_try(bar, parity)) return true;
+        if ((k & 31) == 0) {
+            if (*abort_flag) return false;
+            if (clock64() - t0 > kWaitCycles) {
+                *abort_flag = 1;
+                return false;
+            }
+        }
+    }
+}
+// Bounded wait used while shutting down: ignores the abort flag.
+__device__ __forceinline__ void drain_bar(uint32_t bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try(bar, parity))
+        if (clock64() - t0 > kDrainCycles) return;
+}
+
+// ------------------------------------------------------------ tcgen05
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor, no swizzle, K-major canonical layout:
+// core matrices of 8 rows x 16 bytes; lbo = byte stride between the two core
+// matrices along K, sbo = byte stride between 8-row groups.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major, N = 32, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// 32 consecutive FP32 columns of this thread's TMEM lane, waited for in the same asm block
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+
+struct TcArgs {
+    const uint8_t* links = nullptr;  // pre-tiled BF16 B operands, kLinkSite bytes per site
+    const float2* x = nullptr;       // [site][dof][nrhs]
+    float2* y = nullptr;
+    const float2* w = nullptr;       // EPI 2
+    double* partials = nullptr;
+    unsigned int* tickets = nullptr;
+    double* out = nullptr;
+    const int* gate = nullptr;
+    int* err = nullptr;
+    int nx = 0, ny = 0, nrhs = 0, H = 0;
+};
+
+template <int EPI>
+__global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
+    if (a.gate && *a.gate == 0) return;  // every right-hand side of the solve has converged
+    constexpr int K = EPI == 2 ? 3 : 1;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int H = a.H, nx = a.nx, ny = a.ny, nrhs = a.nrhs;
+    const int x0 = blockIdx.x * kW, y0 = blockIdx.y * H, rhs0 = blockIdx.z * kRhsTile;
+    const int nseq = H * kW;
+    const uint32_t ring_a = smem_u32(smem);
+    const uint32_t link_a = ring_a + kRingBytes;
+    const uint32_t bar_a = ring_a + kBarOffset;
+    int* misc = reinterpret_cast<int*>(smem + kMiscOffset);  // [0] TMEM base, [1] abort flag
+    double* red = reinterpret_cast<double*>(smem + kRedOffset);
+    volatile int* abort_flag = misc + 1;
+    auto bar = [&](int i) { return bar_a + 8u * (uint32_t)i; };
+
+    if (tid == 0) {
+        for (int i = 0; i < kRing; ++i) {
+            mbar_init(bar(kBarSrcFull + i), 128);
+            mbar_init(bar(kBarSrcEmpty + i), 1);
+        }
+        for (int i = 0; i < kLinkSlots; ++i) {
+            mbar_init(bar(kBarLinkFull + i), 1);
+            mbar_init(bar(kBarLinkEmpty + i), 1);
+        }
+        for (int i = 0; i < kAccSlots; ++i) {
+            mbar_init(bar(kBarAccFull + i), 1);
+            mbar_init(bar(kBarAccEmpty + i), 64);
+        }
+        mbar_init(bar(kBarFinal), 1);
+        misc[1] = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        fence_proxy_async();
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(misc)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(misc);
+
+    if (warp == 0) {
+        // ---------------- link producer: one bulk copy of 9 KB per output site
+        if (lane == 0) {
+            int issued = 0;
+            for (int seq = 0; seq < nseq; ++seq) {
+                const int slot = seq % kLinkSlots, use = seq / kLinkSlots;
+                if (use > 0 && !wait_bar(bar(kBarLinkEmpty + slot), (use - 1) & 1, abort_flag)) break;
+                const int r = seq / kW, i = seq - r * kW;
+                const int64_t site = (int64_t)(x0 + i) + (int64_t)nx * (y0 + r);
+                mbar_expect_tx(bar(kBarLinkFull + slot), kLinkSite);
+                bulk_g2s(link_a + slot * kLinkSite, a.links + site * kLinkSite, kLinkSite, bar(kBarLinkFull + slot));
+                issued = seq + 1;
+            }
+            // every issued copy has landed before the CTA can leave
+            for (int seq = issued > kLinkSlots ? issued - kLinkSlots : 0; seq < issued; ++seq)
+                drain_bar(bar(kBarLinkFull + seq % kLinkSlots), (seq / kLinkSlots) & 1);
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---------------- MMA issuer
+        if (lane == 0) {
+            bool ok = true;
+            int seq = 0;
+            for (int r = 0; r < H && ok; ++r) {
+                for (int lr = (r == 0 ? 0 : r + 2); lr <= r + 2 && ok; ++lr)
+                    ok = wait_bar(bar(kBarSrcFull + lr % kRing), (lr / kRing) & 1, abort_flag);
+                if (!ok) break;
+                tc_fence_after();
+                for (int i = 0; i < kW; ++i, ++seq) {
+                    const int ls = seq % kLinkSlots, as = seq % kAccSlots;
+                    if (!wait_bar(bar(kBarLinkFull + ls), (seq / kLinkSlots) & 1, abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    if (seq >= kAccSlots &&
+                        !wait_bar(bar(kBarAccEmpty + as), ((seq / kAccSlots) - 1) & 1, abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t d_tmem = tmem + (uint32_t)(as * 32);
+#pragma unroll
+                    for (int d = 0; d < 9; ++d) {
+                        const int lr = r + 1 + dir_dy(d), t = i + 1 + dir_dx(d);
+                        const uint32_t aa = ring_a + (uint32_t)((lr % kRing) * kRowBytes + t * kTileA);
+                        const uint32_t ba = link_a + (uint32_t)(ls * kLinkSite + d * kLinkDir);
+                        mma_bf16(d_tmem, smem_desc(aa, 128, kSboA), smem_desc(ba, 128, 256), d > 0 ? 1u : 0u);
+                    }
+                    mma_commit(bar(kBarLinkEmpty + ls));
+                    mma_commit(bar(kBarAccFull + as));
+                }
+                if (!ok) break;
+                mma_commit(bar(kBarSrcEmpty + r % kRing));  // source row r is not read again
+            }
+            // all MMAs of this CTA have completed before tensor memory is freed
+            mma_commit(bar(kBarFinal));
+            drain_bar(bar(kBarFinal), 0);
+        }
+        __syncwarp();
+    } else if (warp == 4 || warp == 5) {
+        // ---------------- epilogue: TMEM lanes 0..63 hold the 64 useful rows
+        const int sub = warp - 4;
+        const int m = 32 * sub + lane;
+        const int rhs = m >> 1, c = m & 1;
+        double v[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[k] = 0.0;
+        const int64_t rstride = 2ll * nrhs;  // floats between consecutive dofs
+        for (int seq = 0; seq < nseq; ++seq) {
+            const int as = seq % kAccSlots;
+            bool ok = wait_bar(bar(kBarAccFull + as), (seq / kAccSlots) & 1, abort_flag);
+            if (!__all_sync(0xffffffffu, ok)) break;
+            tc_fence_after();
+            float d[32];
+            tmem_ld32(tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)(as * 32), d);
+            tc_fence_before();
+            mbar_arrive(bar(kBarAccEmpty + as));
+            const int r = seq / kW, i = seq - r * kW;
+            const int64_t site = (int64_t)(x0 + i) + (int64_t)nx * (y0 + r);
+            const int64_t base = (site * kNc * nrhs + rhs0 + rhs) * 2 + c;
+            float* yp = reinterpret_cast<float*>(a.y) + base;
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll
+            for (int k = 0; k < kNc; ++k) {
+                const float other = __shfl_xor_sync(0xffffffffu, d[16 + k], 1);
+                const float o = c == 0 ? d[k] - other : d[k] + other;
+                yp[k * rstride] = o;
+                if (EPI == 1) {
+                    s0 += o * o;
+                } else if (EPI == 2) {
+                    const float wc = reinterpret_cast<const float*>(a.w)[base + k * rstride];
+                    const float wo = __shfl_xor_sync(0xffffffffu, wc, 1);
+                    s0 += o * wc;                     // Re <y, w>: yr wr + yi wi
+                    s1 += c == 0 ? o * wo : -o * wo;  // Im <y, w>: yr wi - yi wr
+                    s2 += o * o;
+                }
+            }
+            if (EPI == 1) {
+                v[0] += (double)s0;
+            } else if (EPI == 2) {
+                v[0] += (double)s0;
+                v[1] += (double)s1;
+                v[K - 1] += (double)s2;
+            }
+        }
+        if (EPI != 0) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], 1);
+            if (c == 0)
+#pragma unroll
+                for (int k = 0; k < K; ++k) red[rhs * K + k] = v[k];
+        }
+    } else {
+        // ---------------- stagers (warps 2, 3, 6, 7): FP32 source rows -> BF16 A tiles
+        const int st = (warp < 4 ? warp - 2 : warp - 4) * 32 + lane;  // 0..127
+        for (int lr = 0; lr < H + 2; ++lr) {
+            const int slot = lr % kRing, use = lr / kRing;
+            if (use > 0 && !wait_bar(bar(kBarSrcEmpty + slot), (use - 1) & 1, abort_flag)) break;
+            const int gy = wrapi(y0 - 1 + lr, ny);
+            uint8_t* row = smem + slot * kRowBytes;
+            constexpr int kItems = kSrcSites * 2 * 32;  // (site, 8-dof group, rhs)
+            static_assert(kItems % 128 == 0, "stager items");
+#pragma unroll
+            for (int it = 0; it < kItems / 128; ++it) {
+                const int item = st + it * 128;
+                const int r = item & 31, g = (item >> 5) & 1, t = item >> 6;
+                const int gx = wrapi(x0 - 1 + t, nx);
+                const float2* src = a.x + ((int64_t)(gx + (int64_t)nx * gy) * kNc + g * 8) * nrhs + rhs0 + r;
+                float2 e[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) e[j] = src[(int64_t)j * nrhs];
+                uint4 re, im;
+                re.x = pack_bf16(e[0].x, e[1].x);
+                re.y = pack_bf16(e[2].x, e[3].x);
+                re.z = pack_bf16(e[4].x, e[5].x);
+                re.w = pack_bf16(e[6].x, e[7].x);
+                im.x = pack_bf16(e[0].y, e[1].y);
+                im.y = pack_bf16(e[2].y, e[3].y);
+                im.z = pack_bf16(e[4].y, e[5].y);
+                im.w = pack_bf16(e[6].y, e[7].y);
+                uint8_t* tile = row + t * kTileA;
+                const int mr = 2 * r, mi = 2 * r + 1;
+                *reinterpret_cast<uint4*>(tile + (mr >> 3) * kSboA + g * 128 + (mr & 7) * 16) = re;
+                *reinterpret_cast<uint4*>(tile + (mi >> 3) * kSboA + g * 128 + (mi & 7) * 16) = im;
+            }
+            fence_proxy_async();
+            mbar_arrive(bar(kBarSrcFull + slot));
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    const bool aborted = *abort_flag != 0;
+    if (aborted && tid == 0 && a.err) atomicExch(a.err, 2);
+
+    if (EPI != 0) {
+        // per-rhs partials of this CTA, then the last CTA of this rhs tile sums them in block order
+        const int nblk = gridDim.x * gridDim.y;
+        const int blin = blockIdx.x + gridDim.x * blockIdx.y;
+        __shared__ int s_last;
+        if (tid < kRhsTile) {
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                a.partials[((int64_t)(rhs0 + tid) * K + k) * nblk + blin] = aborted ? 0.0 : red[tid * K + k];
+        }
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) s_last = atomicAdd(a.tickets + blockIdx.z, 1u) == (unsigned)(nblk - 1) ? 1 : 0;
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            if (tid < kRhsTile) {
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    const double* src = a.partials + ((int64_t)(rhs0 + tid) * K + k) * nblk;
+                    double sum = 0.0;
+                    for (int b = 0; b < nblk; ++b) sum += __ldcg(src + b);
+                    a.out[(rhs0 + tid) * K + k] = sum;
+                }
+            }
+            if (tid == 0) a.tickets[blockIdx.z] = 0u;
+        }
+    }
+}
+
+// B operands of every (site, direction): row n = c * 16 + i, K index j,
+// value Re / Im of L[s][d](i, j) (stored [s][d][j][i]), rounded to BF16.
+// One thread writes one 16-byte core-matrix row (8 consecutive j).
+__global__ void k_tile_links(const cx<double>* __restrict__ A, int64_t nsites, uint8_t* __restrict__ out) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nsites * 9 * 32 * 2) return;
+    const int g = (int)(t & 1);
+    const int n = (int)((t >> 1) & 31);
+    const int64_t sd = t >> 6;  // site * 9 + d
+    const int cpart = n >> 4, i = n & 15;
+    const cx<double>* blk = A + sd * kNc * kNc;
+    float f[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const cx<double> z = blk[(g * 8 + k) * kNc + i];
+        f[k] = (float)(cpart == 0 ? z.re : z.im);
+    }
+    uint4 v;
+    v.x = pack_bf16(f[0], f[1]);
+    v.y = pack_bf16(f[2], f[3]);
+    v.z = pack_bf16(f[4], f[5]);
+    v.w = pack_bf16(f[6], f[7]);
+    *reinterpret_cast<uint4*>(out + sd * kLinkDir + (n >> 3) * 256 + g * 128 + (n & 7) * 16) = v;
+}
+
+int rows_per_cta(int nx, int ny, int nz) {
+    int H = ny;
+    while (H % 2 == 0 && H > 4 && (nx / kW) * (ny / H) * nz < 120) H /= 2;
+    return H;
+}
+
+}  // namespace
+
+bool smg_coarse_tc_shape_ok(int nx, int ny, int ndof) { return ndof == kNc && nx % kW == 0 && nx > 0 && ny > 0; }
+
+size_t smg_coarse_tc_link_bytes(int64_t nsites) { return (size_t)nsites * kLinkSite; }
+
+smg_status smg_coarse_tc_tile_links(smg_context* ctx, const cx<double>* A64, int64_t nsites, void* out) {
+    const int64_t n = nsites * 9 * 32 * 2;
+    k_tile_links<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(A64, nsites, static_cast<uint8_t*>(out));
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    // the apply kernels need more than the default 48 KB of dynamic shared memory
+    SMG_CUDA(ctx, cudaFuncSetAttribute(k_coarse_apply_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    SMG_CUDA(ctx, cudaFuncSetAttribute(k_coarse_apply_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    SMG_CUDA(ctx, cudaFuncSetAttribute(k_coarse_apply_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    return SMG_OK;
+}
+
+// y = A x on nrhs (a multiple of 32) right-hand sides; epi 1 adds ||y||^2 and
+// epi 2 <y, w> and ||y||^2 per rhs into out[rhs * K + k] (K = 1 or 3).
+smg_status smg_coarse_tc_apply(smg_context* ctx, const void* links, int nx, int ny, int nrhs, const cx<float>* x,
+                               cx<float>* y, int epi, const cx<float>* w, double* out, const int* gate, int* err) {
+    if (!smg_coarse_tc_shape_ok(nx, ny, kNc) || nrhs % kRhsTile != 0 || nrhs / kRhsTile > kMaxTickets)
+        return smg_fail(ctx, SMG_UNSUPPORTED, "tensor-core coarse apply: shape not supported");
+    const int nz = nrhs / kRhsTile;
+    const int H = rows_per_cta(nx, ny, nz);
+    const dim3 grid(nx / kW, ny / H, nz);
+    TcArgs a;
+    a.links = static_cast<const uint8_t*>(links);
+    a.x = reinterpret_cast<const float2*>(x);
+    a.y = reinterpret_cast<float2*>(y);
+    a.w = reinterpret_cast<const float2*>(w);
+    a.gate = gate;
+    a.err = err;
+    a.nx = nx;
+    a.ny = ny;
+    a.nrhs = nrhs;
+    a.H = H;
+    if (epi != 0) {
+        SMG_TRY(smg_reduce_reserve(ctx, (size_t)grid.x * grid.y * nrhs * 3));
+        a.partials = ctx->red.partials;
+        a.tickets = ctx->red.tickets;
+        a.out = out;
+    }
+    if (epi == 0)
+        k_coarse_apply_tc<0><<<grid, 256, kSmemBytes, ctx->stream>>>(a);
+    else if (epi == 1)
+        k_coarse_apply_tc<1><<<grid, 256, kSmemBytes, ctx->stream>>>(a);
+    else
+        k_coarse_apply_tc<2><<<grid, 256, kSmemBytes, ctx->stream>>>(a);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}

@@ -24,13 +24,21 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <cstdlib>
 #include <cstring>
 #include <random>
+#include <type_traits>
 #include <vector>
 
 smg_status smg_dslash(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, double* norm2_dev);
 smg_status smg_dslash_mr(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, const smg_field* w,
                          double* out3_dev);
+// tensor-core coarse apply (coarse_tc.cu)
+bool smg_coarse_tc_shape_ok(int nx, int ny, int ndof);
+size_t smg_coarse_tc_link_bytes(int64_t nsites);
+smg_status smg_coarse_tc_tile_links(smg_context* ctx, const cx<double>* A64, int64_t nsites, void* out);
+smg_status smg_coarse_tc_apply(smg_context* ctx, const void* links, int nx, int ny, int nrhs, const cx<float>* x,
+                               cx<float>* y, int epi, const cx<float>* w, double* out, const int* gate, int* err);
 
 namespace {
 
@@ -54,6 +62,7 @@ struct Level {
     // operator of this level (l >= 1): [site][dir][j][i] = block(i, j)
     cx<double>* A64 = nullptr;
     cx<float>* A32 = nullptr;
+    void* Atc = nullptr;  // BF16 links pre-tiled for the tensor-core apply (F32 hierarchies)
     int64_t vsize() const { return (int64_t)nagg_x * nagg_y * ax * ay * ndof * nc_next; }
     int64_t asize() const { return (int64_t)nsites * 9 * ndof * ndof; }
 };
@@ -955,11 +964,25 @@ smg_status coarse_apply_tiled(smg_context* ctx, const Level& L, const cx<T>* A, 
     return SMG_OK;
 }
 
+// the tensor-core kernel takes FP32 coarse vectors of 16 dofs, rhs innermost, in multiples of 32
+bool tc_path(const smg_mg* mg, int l, int nrhs) {
+    const Level& L = mg->lv[l];
+    return L.Atc != nullptr && nrhs % 32 == 0 && nrhs / 32 <= kMaxTickets;
+}
+
+int* device_err(smg_mg* mg) { return mg->cg_state ? reinterpret_cast<int*>(static_cast<char*>(mg->cg_state) + 8) : nullptr; }
+
 template <typename T>
 smg_status coarse_apply(smg_mg* mg, int l, VecView<T> x, cx<T>* y, int epi, const cx<T>* w, double* out,
-                        const int* gate = nullptr) {
+                        const int* gate = nullptr, int engine = -1) {
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[l];
+    if constexpr (std::is_same<T, float>::value) {
+        // engine -1: tensor cores where the shape allows; 0: CUDA cores; 1: tensor cores
+        if (engine != 0 && x.rhs_inner && tc_path(mg, l, x.nrhs))
+            return smg_coarse_tc_apply(ctx, L.Atc, L.nx, L.ny, x.nrhs, x.p, y, epi, w, out, gate, device_err(mg));
+        if (engine == 1) return smg_fail(ctx, SMG_UNSUPPORTED, "tensor-core coarse apply: shape not supported");
+    }
     if (x.nrhs == 1 && (L.ndof == 8 || L.ndof == 16 || L.ndof == 32)) {
         ReduceLaunch rl = reduce_launch((int)((int64_t)L.nsites * L.ndof), 1);
         SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * 3));
@@ -1452,6 +1475,10 @@ smg_status make_f32_copies(smg_mg* mg) {
             if (!L.A32) SMG_CUDA(ctx, cudaMalloc(&L.A32, n * sizeof(cx<float>)));
             k_cvt_flat<float, double><<<blocks_for(n), 256, 0, ctx->stream>>>(L.A64, L.A32, n);
             count_launch(ctx);
+            if (mg->p.precision == SMG_F32 && mg->p.tensor_cores && smg_coarse_tc_shape_ok(L.nx, L.ny, L.ndof)) {
+                if (!L.Atc) SMG_CUDA(ctx, cudaMalloc(&L.Atc, smg_coarse_tc_link_bytes(L.nsites)));
+                SMG_TRY(smg_coarse_tc_tile_links(ctx, L.A64, L.nsites, L.Atc));
+            }
         }
     }
     SMG_CHECK_LAUNCH(ctx);
@@ -1619,7 +1646,7 @@ smg_status build(smg_mg* mg, const double* warm) {
 
 void destroy_levels(smg_mg* mg) {
     for (auto& L : mg->lv) {
-        for (void* p : {(void*)L.V64, (void*)L.V32, (void*)L.A64, (void*)L.A32})
+        for (void* p : {(void*)L.V64, (void*)L.V32, (void*)L.A64, (void*)L.A32, L.Atc})
             if (p) cudaFree(p);
     }
     mg->lv.clear();
@@ -1722,7 +1749,9 @@ smg_status smg_mg_check_device_error(smg_mg* mg) {
     SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (err) {
         SMG_CUDA(ctx, cudaMemsetAsync(static_cast<char*>(mg->cg_state) + 8, 0, sizeof(int), ctx->stream));
-        return smg_fail(ctx, SMG_TIMEOUT, "coarsest CG: a grid-barrier wait ran out");
+        return smg_fail(ctx, SMG_TIMEOUT,
+                        err == 2 ? "tensor-core coarse apply: a pipeline wait ran out"
+                                 : "coarsest CG: a grid-barrier wait ran out");
     }
     return SMG_OK;
 }
@@ -1748,6 +1777,7 @@ SMG_API smg_status smg_mg_params_default(smg_mg_params* p) {
     p->coarse_tol = 1e-12;
     p->precision = SMG_F64;
     p->seed = 42;
+    p->tensor_cores = 1;
     return SMG_OK;
 }
 
@@ -1760,6 +1790,8 @@ SMG_API smg_status smg_mg_create(smg_dirac* d, const smg_mg_params* p, const dou
     mg->ctx = ctx;
     mg->dirac = d;
     mg->p = *p;
+    // SMG_CUDA_GRAPHS=0 launches the cycle kernel by kernel (for tools that cannot follow graph replays)
+    if (const char* e = std::getenv("SMG_CUDA_GRAPHS")) mg->use_graph = std::atoi(e) != 0;
     smg_status st = build(mg, warm_start);
     if (st != SMG_OK) {
         cudaStreamSynchronize(ctx->stream);
@@ -1911,10 +1943,54 @@ SMG_API smg_status smg_mg_time_coarse_apply(smg_mg* mg, int level, int nrhs, int
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     SMG_TRY(st);
+    SMG_TRY(smg_mg_check_device_error(mg));
     *ms = (double)f / reps;
+    // compulsory bytes: the links once, the input and output vectors once
     const double es = prec == SMG_F64 ? 16.0 : 8.0;
-    if (bytes) *bytes = es * ((double)L.nsites * 9 * L.ndof * L.ndof + 2.0 * L.nsites * L.ndof * nrhs);
+    const double link_bytes = (prec == SMG_F32 && tc_path(mg, level, nrhs))
+                                  ? (double)smg_coarse_tc_link_bytes(L.nsites)
+                                  : es * (double)L.nsites * 9 * L.ndof * L.ndof;
+    if (bytes) *bytes = link_bytes + es * 2.0 * L.nsites * L.ndof * nrhs;
     return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_coarse_apply_batch(smg_mg* mg, int level, int nrhs, int engine, const float* in,
+                                             const float* w, float* out, double* dots) {
+    if (!mg || !in || !out || level < 1 || level >= (int)mg->lv.size() || nrhs < 1 || engine < 0 || engine > 1)
+        return SMG_BAD_ARG;
+    smg_context* ctx = mg->ctx;
+    if (mg->p.precision != SMG_F32) return smg_fail(ctx, SMG_UNSUPPORTED, "coarse_apply_batch needs an F32 hierarchy");
+    if (engine == 1 && !tc_path(mg, level, nrhs))
+        return smg_fail(ctx, SMG_UNSUPPORTED, "tensor-core coarse apply: shape not supported");
+    SMG_TRY(ensure_work(mg, nrhs, SMG_F32));
+    const Level& L = mg->lv[level];
+    CoarseWork& cw = mg->cw[level];
+    const size_t b = (size_t)L.nsites * L.ndof * nrhs * sizeof(cx<float>);
+    const int K = w ? 3 : 1;
+    cx<float>* wdev = nullptr;
+    double* ddev = nullptr;
+    SMG_CUDA(ctx, cudaMemcpyAsync(cw.x, in, b, cudaMemcpyHostToDevice, ctx->stream));
+    if (w) {
+        SMG_CUDA(ctx, cudaMemcpyAsync(cw.r, w, b, cudaMemcpyHostToDevice, ctx->stream));
+        wdev = (cx<float>*)cw.r;
+    }
+    if (dots) {
+        SMG_CUDA(ctx, cudaMallocAsync((void**)&ddev, (size_t)nrhs * K * sizeof(double), ctx->stream));
+        SMG_CUDA(ctx, cudaMemsetAsync(ddev, 0, (size_t)nrhs * K * sizeof(double), ctx->stream));
+    }
+    const int epi = dots ? (w ? 2 : 1) : 0;
+    smg_status st = coarse_apply<float>(mg, level, cview<float>(cw.x, L, nrhs), (cx<float>*)cw.Ar, epi, wdev, ddev,
+                                        nullptr, engine);
+    if (st == SMG_OK) {
+        SMG_CUDA(ctx, cudaMemcpyAsync(out, cw.Ar, b, cudaMemcpyDeviceToHost, ctx->stream));
+        if (dots)
+            SMG_CUDA(ctx, cudaMemcpyAsync(dots, ddev, (size_t)nrhs * K * sizeof(double), cudaMemcpyDeviceToHost,
+                                          ctx->stream));
+    }
+    if (ddev) cudaFreeAsync(ddev, ctx->stream);
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    SMG_TRY(st);
+    return smg_mg_check_device_error(mg);
 }
 
 SMG_API smg_status smg_mg_coarse_apply_host(smg_mg* mg, int level, const double* in, double* out) {

@@ -309,33 +309,108 @@ struct GcrScalars {
     double tol2 = 0;
 };
 
-// beta = (ref ? <Az, AP_i> : <AP_i, Az>) / ApAp_i;  p -= beta P_i, Ap -= beta AP_i
+// Classical Gram-Schmidt of the new direction against the stored window
+// (solvers.cpp:260-267) in two passes over the fine fields:
+//   k_gcr_multidot   <AP_i, Az> for up to kDotChunk stored directions at once
+//   k_gcr_orth_all   p = z - sum_i beta_i P_i, Ap = Az - sum_i beta_i AP_i for
+//                    up to kOrthChunk directions, fused with <Ap, r>, ||Ap||^2
+constexpr int kDotChunk = 8;
+constexpr int kOrthChunk = 32;
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_gcr_orth(VecView<T> p, cx<T>* __restrict__ Ap, const cx<T>* __restrict__ Pi,
-                                                  const cx<T>* __restrict__ APi, const double* __restrict__ dot,
-                                                  const double* __restrict__ apap_i, int ref_coeff) {
-    __shared__ cx<T> s_b[32];
+struct DotPtrs {
+    const cx<T>* ap[kDotChunk];
+};
+
+struct FinDots {  // out[rhs * stride + k] = sums[k], k < nk
+    double* out;
+    int stride, nk;
+    __device__ void operator()(int rhs, const double* s) const {
+        for (int k = 0; k < nk; ++k) out[rhs * stride + k] = s[k];
+    }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_gcr_multidot(VecView<T> az, DotPtrs<T> ptr, int ns, double* partials,
+                                                      unsigned int* ticket, double* out, int stride) {
+    constexpr int K = 2 * kDotChunk;
     const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
-    if (threadIdx.y == 0) {
-        cx<T> be = mk<T>(0, 0);
-        if (rhs < p.nrhs) {
-            double den = apap_i[3 * rhs + 2];
-            // dot holds <AP_i, Az>; the reference's coefficient is its conjugate
-            double re = dot[2 * rhs], im = ref_coeff ? -dot[2 * rhs + 1] : dot[2 * rhs + 1];
-            if (den > 0) be = mk<T>((T)(re / den), (T)(im / den));
+    double v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = 0.0;
+    if (rhs < az.nrhs) {
+        for (int s = blockIdx.x * blockDim.y + threadIdx.y; s < az.nsites; s += gridDim.x * blockDim.y) {
+            const Spinor<T> z = ld_spinor(az.p, s, rhs, az.nrhs);
+#pragma unroll
+            for (int i = 0; i < kDotChunk; ++i) {
+                if (i < ns) {
+                    const Spinor<T> a = ld_spinor(ptr.ap[i], s, rhs, az.nrhs);
+                    const cx<T> c = cmulc(a.s0, z.s0) + cmulc(a.s1, z.s1);
+                    v[2 * i] += (double)c.re;
+                    v[2 * i + 1] += (double)c.im;
+                }
+            }
         }
-        s_b[threadIdx.x] = be;
+    }
+    block_reduce_finalise<K>(v, partials, ticket, az.nrhs, FinDots{out, stride, 2 * ns});
+}
+
+template <typename T>
+struct OrthPtrs {
+    const cx<T>* P[kOrthChunk];
+    const cx<T>* AP[kOrthChunk];
+    const double* apap[kOrthChunk];  // [rhs][3] scalar slot of each stored direction (||AP_i||^2 at 2)
+};
+
+// beta_i = (ref ? conj : id)(<AP_i, Az>) / ||AP_i||^2, dots[rhs * stride + 2 (i0 + i)] = <AP_i, Az>
+template <typename T>
+__global__ void __launch_bounds__(256) k_gcr_orth_all(VecView<T> p, cx<T>* Ap,
+                                                      const cx<T>* z, const cx<T>* Az,
+                                                      const cx<T>* __restrict__ r, OrthPtrs<T> ptr, int ns, int i0,
+                                                      const double* __restrict__ dots, int stride, int ref_coeff,
+                                                      int last, double* partials, unsigned int* ticket,
+                                                      double* apr3) {
+    __shared__ cx<T> s_b[kOrthChunk][32];
+    const int nrhs = p.nrhs;
+    const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
+    for (int i = threadIdx.y; i < ns; i += blockDim.y) {
+        cx<T> be = mk<T>(0, 0);
+        if (rhs < nrhs) {
+            const double den = ptr.apap[i][3 * rhs + 2];
+            const double re = dots[rhs * stride + 2 * (i0 + i)];
+            const double im = dots[rhs * stride + 2 * (i0 + i) + 1];
+            if (den > 0) be = mk<T>((T)(re / den), (T)((ref_coeff ? -im : im) / den));
+        }
+        s_b[i][threadIdx.x] = be;
     }
     __syncthreads();
-    const int s = blockIdx.x * blockDim.y + threadIdx.y;
-    if (rhs >= p.nrhs || s >= p.nsites) return;
-    const cx<T> be = s_b[threadIdx.x];
-    const int64_t base = p.idx(s, rhs, 0);
-    const int ds = p.dstride();
-    for (int d = 0; d < p.ndof; ++d) {
-        p.p[base + (int64_t)d * ds] = p.p[base + (int64_t)d * ds] - be * Pi[base + (int64_t)d * ds];
-        Ap[base + (int64_t)d * ds] = Ap[base + (int64_t)d * ds] - be * APi[base + (int64_t)d * ds];
+    double v[3] = {0.0, 0.0, 0.0};
+    if (rhs < nrhs) {
+        for (int s = blockIdx.x * blockDim.y + threadIdx.y; s < p.nsites; s += gridDim.x * blockDim.y) {
+            Spinor<T> q = ld_spinor(z, s, rhs, nrhs);
+            Spinor<T> aq = ld_spinor(Az, s, rhs, nrhs);
+#pragma unroll 4
+            for (int i = 0; i < ns; ++i) {
+                const cx<T> be = s_b[i][threadIdx.x];
+                const Spinor<T> pi = ld_spinor(ptr.P[i], s, rhs, nrhs);
+                const Spinor<T> ai = ld_spinor(ptr.AP[i], s, rhs, nrhs);
+                q.s0 = q.s0 - be * pi.s0;
+                q.s1 = q.s1 - be * pi.s1;
+                aq.s0 = aq.s0 - be * ai.s0;
+                aq.s1 = aq.s1 - be * ai.s1;
+            }
+            st_spinor(p.p, s, rhs, nrhs, q);
+            st_spinor(Ap, s, rhs, nrhs, aq);
+            if (last) {
+                const Spinor<T> rr = ld_spinor(r, s, rhs, nrhs);
+                const cx<T> c = cmulc(aq.s0, rr.s0) + cmulc(aq.s1, rr.s1);
+                v[0] += (double)c.re;
+                v[1] += (double)c.im;
+                v[2] += (double)(norm2(aq.s0) + norm2(aq.s1));
+            }
+        }
     }
+    if (last) block_reduce_finalise<3>(v, partials, ticket, nrhs, FinStore{apr3, 3});
 }
 
 struct FinGcr {
@@ -443,15 +518,15 @@ struct GcrWs {
             SMG_TRY(fs.add(proto, &P[i]));
             SMG_TRY(fs.add(proto, &AP[i]));
         }
-        const size_t nd_ = (size_t)nrhs * (5 + 3 * nbuf) + 64;
+        const size_t nd_ = (size_t)nrhs * (3 + 5 * nbuf) + 64;
         const size_t bytes = nd_ * sizeof(double) + (size_t)nrhs * 2 * sizeof(int) + 64;
         SMG_CUDA(ctx, cudaMallocAsync(&blk, bytes, ctx->stream));
         SMG_CUDA(ctx, cudaMemsetAsync(blk, 0, bytes, ctx->stream));
         sc.rr = blk;
         sc.bnorm2 = blk + nrhs;
         truev = blk + 2 * nrhs;
-        dots = blk + 3 * nrhs;  // 2 * nrhs
-        apr = blk + 5 * nrhs;   // nbuf * 3 * nrhs
+        dots = blk + 3 * nrhs;                    // [rhs][nbuf][2]
+        apr = blk + 3 * nrhs + 2 * nrhs * nbuf;  // nbuf * 3 * nrhs
         sc.active = (int*)(blk + nd_);
         sc.flags = sc.active + nrhs;
         return SMG_OK;
@@ -496,7 +571,7 @@ smg_status gcr_core(smg_dirac* d, smg_mg* mg, GcrWs<T>& ws, const smg_field* b, 
     for (int i = 1; i < ws.nbuf; ++i) freeb.push_back(i);
     int iter = 0;
     const ReduceLaunch rl = reduce_launch(V, nrhs);
-    SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * nrhs * 3));
+    SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * nrhs * 2 * kDotChunk));
     bool any_active = false;
     for (int j = 0; j < nrhs; ++j) any_active |= out.active[j] != 0;
     std::vector<double> h_apr(3 * nrhs);
@@ -512,19 +587,36 @@ smg_status gcr_core(smg_dirac* d, smg_mg* mg, GcrWs<T>& ws, const smg_field* b, 
         smg_field* p = ws.P[work];
         smg_field* Ap = ws.AP[work];
         SMG_TRY(apply_A<T>(d, ws.z, ws.tmp, ws.Az));
-        SMG_CUDA(ctx, cudaMemcpyAsync(p->data, ws.z->data, ws.z->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-        SMG_CUDA(ctx, cudaMemcpyAsync(Ap->data, ws.Az->data, ws.Az->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-        for (int slot : ring) {
-            // <AP_i, Az> (classical Gram-Schmidt on Az, as solvers.cpp:260-267)
-            SMG_TRY(reduce_into<T>(ctx, fv<T>(ws.AP[slot]), (const cx<T>*)ws.Az->data, VR_DOT, ws.dots));
-            k_gcr_orth<T><<<vec_grid(V, nrhs), vec_block(nrhs), 0, ctx->stream>>>(
-                fv<T>(p), (cx<T>*)Ap->data, (const cx<T>*)ws.P[slot]->data, (const cx<T>*)ws.AP[slot]->data, ws.dots,
-                ws.apr_of(slot), ref_coeff);
+        const int nring = (int)ring.size();
+        // <AP_i, Az> for every stored direction, kDotChunk per pass over Az
+        for (int c0 = 0; c0 < nring; c0 += kDotChunk) {
+            DotPtrs<T> dp{};
+            const int ns = std::min(kDotChunk, nring - c0);
+            for (int i = 0; i < ns; ++i) dp.ap[i] = (const cx<T>*)ws.AP[ring[c0 + i]]->data;
+            k_gcr_multidot<T><<<rl.grid, rl.block, 0, ctx->stream>>>(fv<T>(ws.Az), dp, ns, ctx->red.partials,
+                                                                    ctx->red.tickets, ws.dots + 2 * c0,
+                                                                    2 * ws.nbuf);
             count_launch(ctx);
             SMG_CHECK_LAUNCH(ctx);
         }
-        // <Ap, r> and ||Ap||^2 into this buffer's scalar slot
-        SMG_TRY(reduce_into<T>(ctx, fv<T>(Ap), (const cx<T>*)ws.r->data, VR_DOTNORM, ws.apr_of(work)));
+        // p and Ap in kOrthChunk passes; the last one also forms <Ap, r> and ||Ap||^2
+        for (int c0 = 0; c0 == 0 || c0 < nring; c0 += kOrthChunk) {
+            OrthPtrs<T> op{};
+            const int ns = std::min(kOrthChunk, nring - c0);
+            for (int i = 0; i < ns; ++i) {
+                op.P[i] = (const cx<T>*)ws.P[ring[c0 + i]]->data;
+                op.AP[i] = (const cx<T>*)ws.AP[ring[c0 + i]]->data;
+                op.apap[i] = ws.apr_of(ring[c0 + i]);
+            }
+            const bool first = c0 == 0, last = c0 + kOrthChunk >= nring;
+            k_gcr_orth_all<T><<<rl.grid, rl.block, 0, ctx->stream>>>(
+                fv<T>(p), (cx<T>*)Ap->data, first ? (const cx<T>*)ws.z->data : (const cx<T>*)p->data,
+                first ? (const cx<T>*)ws.Az->data : (const cx<T>*)Ap->data, (const cx<T>*)ws.r->data, op, ns, c0,
+                ws.dots, 2 * ws.nbuf, ref_coeff, last ? 1 : 0, ctx->red.partials, ctx->red.tickets,
+                ws.apr_of(work));
+            count_launch(ctx);
+            SMG_CHECK_LAUNCH(ctx);
+        }
         sc.apr3 = ws.apr_of(work);
         k_gcr_update<T><<<rl.grid, rl.block, 0, ctx->stream>>>(sc, fv<T>(x), (cx<T>*)ws.r->data,
                                                                (const cx<T>*)p->data, (const cx<T>*)Ap->data,
