@@ -8,10 +8,11 @@ Gaussian complex sources), timed with CUDA events on the library's stream
 (smg_timer_begin/end) between a barrier and a synchronize; the max over ranks
 is reported.  Workloads:
 
-* mg (default) — the multi-RHS MG-GCR solve on a 512 x 512 lattice, beta = 6, m = -0.05, c_sw = 1; three levels (4 x 4 then 2 x 2
-  aggregates, 8 null vectors split by chirality = 16 coarse dofs per level);
-  32 right-hand sides solved together to a true FP64 residual of 1e-10 by an
-  FP32 GCR preconditioned with the FP32 hierarchy inside FP64 defect correction.  The hierarchy is built
+* mg (default) — the multi-RHS MG-GCR solve on a 512 x 512 lattice, beta = 6,
+  m = -0.05, c_sw = 1; three levels (4 x 4 then 2 x 2 aggregates, 16 null
+  vectors per level = 16 coarse dofs, V-cycle); 32 right-hand sides solved
+  together to a true FP64 residual of 1e-10 by an FP32 GCR preconditioned with
+  the FP32 hierarchy inside FP64 defect correction.  The hierarchy is built
   once before timing.  value = solves/s.  The plain FP64 single-RHS MG on the
   same inputs is measured beside it (config.plain_fp64_mg_solves_per_s).
 * dslash — FP32 D on 32 right-hand sides at L = 512; value = algorithmic GB/s.
@@ -126,7 +127,8 @@ def max_over_ranks(v: float, ws: int) -> float:
 
 # ------------------------------------------------------------------ workloads
 MG = dict(L=512, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20240, nrhs=32, levels=3, blocks=[(4, 4), (2, 2)],
-          n_vec=8, chiral=True, null_iters=6, pre=4, post=4, coarse_max_iter=40, coarse_tol=5e-2, tol=1e-10,
+          n_vec=16, chiral=False, w_cycle=False, null_iters=6, pre=4, post=4, coarse_max_iter=40, coarse_tol=5e-2,
+          tol=1e-10,
           max_iter=500, trunc=20)
 DSLASH = dict(L=512, nrhs=32, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20240)
 CG = dict(L=32, beta=2.0, m=0.1, r=1.0, csw=1.0, mu=0.0, seed=31, tol=1e-10, max_iter=10000)
@@ -163,7 +165,7 @@ def coarse_kernel_name(c, L, nrhs):
 
 def mg_params(smg, c, precision):
     return smg.mg_params(c["levels"], c["blocks"][0][0], c["n_vec"], blocks=c["blocks"], chiral_split=c["chiral"],
-                         null_iters=c["null_iters"], pre_smooth=c["pre"], post_smooth=c["post"],
+                         null_iters=c["null_iters"], pre_smooth=c["pre"], post_smooth=c["post"], w_cycle=c["w_cycle"],
                          coarse_max_iter=c["coarse_max_iter"], coarse_tol=c["coarse_tol"], precision=precision,
                          seed=c["seed"])
 
@@ -257,7 +259,7 @@ def run_ours(args, ws, rank, local):
         dgbs = dslash_bytes_f32(L, nrhs) / (dms * 1e-3) / 1e9
         out.update({
             "value": value, "unit": "solves/s", "ms_per_step": ms, "higher_is_better": True, "dtype": "f32+f64",
-            "config": {"workload": f"MG-GCR, L={L} (beta=6, m=-0.05, c_sw=1), {nrhs} RHS, 3 levels (4x4, 2x2; 16 dof), "
+            "config": {"workload": f"MG-GCR, L={L} (beta=6, m=-0.05, c_sw=1), {nrhs} RHS, 3 levels (4x4, 2x2; 16 null vectors), V-cycle, "
                                    "FP32 GCR + FP32 hierarchy inside FP64 defect correction, true FP64 residual 1e-10",
                        "L": L, "nrhs": nrhs, "levels": c["levels"], "gcr_iterations": iters,
                        "launches_before_timed": int(l0),
@@ -343,7 +345,7 @@ def run_ours(args, ws, rank, local):
         out.update({
             "value": gbs * ws, "unit": "GB/s", "ms_per_step": cms.value, "higher_is_better": True, "dtype": "f32",
             "config": {"workload": f"level-1 coarse operator apply, {L // 4}x{L // 4} sites x 16 dof, {nrhs} RHS "
-                                   f"(L={L} fine, 4x4 aggregates, 8 chiral null vectors)",
+                                   f"(L={L} fine, 4x4 aggregates, 16 null vectors)",
                        "bytes_per_launch": cbytes.value, "timed_launches": reps,
                        "l2": "links and vectors exceed the 129 MB L2 at L=512; no flush"},
             "e2e": None,
@@ -415,7 +417,7 @@ def cpu_baseline(workload: str, threads: int | None = None, ctx_objects=None):
         bvs = [mg32.prolongator(l) for l in range(c["levels"] - 1)]
         links = [None] + [mg32.coarse_op(l) for l in range(1, c["levels"])]
         p = port.mgN_params(L, c["m"], c["r"], c["csw"], c["mu"], c["blocks"], ncs, bvs, links, c["pre"], c["post"],
-                            True, c["coarse_max_iter"], c["coarse_tol"])
+                            c["w_cycle"], c["coarse_max_iter"], c["coarse_tol"])
         b = smg.random_vec(2 * L * L, c["seed"] + 1)
         _, it, res, sec = port.mgN_gcr(p, U, b, c["max_iter"], c["tol"], c["trunc"])
         return {"value": 1.0 / sec, "unit": "solves/s", "cores": n_threads, "kind": "port",

@@ -39,9 +39,9 @@ __global__ void __launch_bounds__(256) k_dslash(DslashArgs<T> a) {
     const int nrhs = a.nrhs;
     const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
     const Geom g = a.g;
-    double v[K];
+    T v[K];  // per-thread partials in the field precision (FP64 is scarce on this part)
 #pragma unroll
-    for (int k = 0; k < K; ++k) v[k] = 0.0;
+    for (int k = 0; k < K; ++k) v[k] = T(0);
 
     if (rhs < nrhs) {
         // Work items walk rows with both parities interleaved (row y even
@@ -99,13 +99,13 @@ __global__ void __launch_bounds__(256) k_dslash(DslashArgs<T> a) {
             st_spinor(a.dst, q, rhs, nrhs, out);
 
             if (EPI == EPI_NORM) {
-                v[0] += (double)(norm2(d0) + norm2(d1));
+                v[0] += norm2(d0) + norm2(d1);
             } else if (EPI == EPI_MR) {
                 const Spinor<T> wv = ld_spinor(a.w, q, rhs, nrhs);
                 const cx<T> c = cmulc(d0, wv.s0) + cmulc(d1, wv.s1);
-                v[0] += (double)c.re;
-                v[1] += (double)c.im;
-                v[2] += (double)(norm2(d0) + norm2(d1));
+                v[0] += c.re;
+                v[1] += c.im;
+                v[2] += norm2(d0) + norm2(d1);
             }
         }
     }

@@ -48,15 +48,15 @@ template <typename T>
 __global__ void k_dot(const cx<T>* __restrict__ a, const cx<T>* __restrict__ b, int nsites, int nrhs,
                       double* partials, unsigned int* ticket, double* out) {
     const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
-    double v[2] = {0.0, 0.0};
+    T v[2] = {T(0), T(0)};
     if (rhs < nrhs) {
         for (int q = blockIdx.x * blockDim.y + threadIdx.y; q < nsites; q += gridDim.x * blockDim.y) {
 #pragma unroll
             for (int sp = 0; sp < 2; ++sp) {
                 int64_t i = sidx(q, rhs, sp, nrhs);
                 cx<T> p = cmulc(a[i], b[i]);
-                v[0] += (double)p.re;
-                v[1] += (double)p.im;
+                v[0] += p.re;
+                v[1] += p.im;
             }
         }
     }
@@ -67,11 +67,11 @@ template <typename T>
 __global__ void k_norm2(const cx<T>* __restrict__ a, int nsites, int nrhs, double* partials,
                         unsigned int* ticket, double* out) {
     const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
-    double v[1] = {0.0};
+    T v[1] = {T(0)};
     if (rhs < nrhs) {
         for (int q = blockIdx.x * blockDim.y + threadIdx.y; q < nsites; q += gridDim.x * blockDim.y) {
             int64_t i0 = sidx(q, rhs, 0, nrhs);
-            v[0] += (double)(norm2(a[i0]) + norm2(a[i0 + 1]));
+            v[0] += norm2(a[i0]) + norm2(a[i0 + 1]);
         }
     }
     block_reduce_finalise<1>(v, partials, ticket, nrhs, FinStore{out, 1});

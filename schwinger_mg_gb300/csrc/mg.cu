@@ -274,6 +274,88 @@ __global__ void k_prolong_c(const cx<T>* __restrict__ V, const cx<T>* __restrict
     c[t] = accumulate ? c[t] + acc : acc;  // t = (s * ndof + j) * nrhs + rhs
 }
 
+// Aggregate-blocked transfers: one block per (aggregate, chunk of up to 32
+// right-hand sides), threads (rhs lane, row).  Restriction reads every input
+// value of the aggregate once and keeps the NC outputs of its rhs in
+// registers (rows reduced through shared memory); prolongation keeps the NC
+// coarse values of its rhs in registers and writes each output once.  Level 0
+// inputs/outputs are fine spinors (dof = spin), coarse levels [site][dof][rhs].
+struct TransferGeom {
+    Geom g;            // level 0 only
+    int nx = 0;        // coarse input/output lattice width (level >= 1)
+    int ax = 0, ay = 0, nax = 0;
+    int ndof = 2, nrhs = 1;
+    int level0 = 0;
+};
+
+__device__ __forceinline__ int64_t transfer_site(const TransferGeom& t, int B, int loc) {
+    const int x = (B % t.nax) * t.ax + loc % t.ax, y = (B / t.nax) * t.ay + loc / t.ax;
+    return t.level0 ? (int64_t)site_q(t.g, x, y) : (int64_t)x + (int64_t)t.nx * y;
+}
+// element (site s, dof j, rhs) of a level-0 spinor field [q][rhs][spin] or a coarse vector [site][dof][rhs]
+__device__ __forceinline__ int64_t transfer_idx(const TransferGeom& t, int64_t s, int j, int rhs) {
+    return t.level0 ? (s * t.nrhs + rhs) * 2 + j : (s * t.ndof + j) * t.nrhs + rhs;
+}
+constexpr int kTransferChunk = 4;  // outputs reduced across rows per shared-memory pass
+
+template <typename T, int NC>
+__global__ void __launch_bounds__(256) k_restrict_agg(const cx<T>* __restrict__ V, const cx<T>* __restrict__ in,
+                                                      cx<T>* __restrict__ out, TransferGeom t) {
+    extern __shared__ unsigned char s_raw[];
+    cx<T>* s_acc = reinterpret_cast<cx<T>*>(s_raw);  // [rows][kTransferChunk][lanes]
+    const int lanes = blockDim.x, rows = blockDim.y;
+    const int B = blockIdx.x, m = t.ax * t.ay, nd = t.ndof, nrhs = t.nrhs;
+    const int rhs = blockIdx.y * lanes + threadIdx.x;
+    const bool live = rhs < nrhs;
+    cx<T> acc[NC];
+#pragma unroll
+    for (int i = 0; i < NC; ++i) acc[i] = mk<T>(0, 0);
+    for (int e = threadIdx.y; e < m * nd; e += rows) {
+        const int loc = e / nd, j = e - loc * nd;
+        const int64_t s = transfer_site(t, B, loc);
+        const cx<T> f = live ? in[transfer_idx(t, s, j, rhs)] : mk<T>(0, 0);
+        const cx<T>* v = V + (((int64_t)B * m + loc) * nd + j) * NC;
+#pragma unroll
+        for (int i = 0; i < NC; ++i) acc[i] = acc[i] + cmulc(v[i], f);
+    }
+    // rows summed in a fixed order, kTransferChunk outputs per pass
+#pragma unroll
+    for (int i0 = 0; i0 < NC; i0 += kTransferChunk) {
+#pragma unroll
+        for (int ii = 0; ii < kTransferChunk; ++ii)
+            s_acc[(threadIdx.y * kTransferChunk + ii) * lanes + threadIdx.x] = acc[i0 + ii];
+        __syncthreads();
+        if (live && threadIdx.y < kTransferChunk) {
+            cx<T> sum = mk<T>(0, 0);
+            for (int r = 0; r < rows; ++r) sum = sum + s_acc[(r * kTransferChunk + threadIdx.y) * lanes + threadIdx.x];
+            out[((int64_t)B * NC + i0 + threadIdx.y) * nrhs + rhs] = sum;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T, int NC>
+__global__ void __launch_bounds__(256) k_prolong_agg(const cx<T>* __restrict__ V, const cx<T>* __restrict__ cin,
+                                                     cx<T>* __restrict__ out, TransferGeom t, int accumulate) {
+    const int lanes = blockDim.x, rows = blockDim.y;
+    const int B = blockIdx.x, m = t.ax * t.ay, nd = t.ndof, nrhs = t.nrhs;
+    const int rhs = blockIdx.y * lanes + threadIdx.x;
+    if (rhs >= nrhs) return;
+    cx<T> c[NC];
+#pragma unroll
+    for (int i = 0; i < NC; ++i) c[i] = cin[((int64_t)B * NC + i) * nrhs + rhs];
+    for (int e = threadIdx.y; e < m * nd; e += rows) {
+        const int loc = e / nd, j = e - loc * nd;
+        const int64_t s = transfer_site(t, B, loc);
+        const cx<T>* v = V + (((int64_t)B * m + loc) * nd + j) * NC;
+        cx<T> acc = mk<T>(0, 0);
+#pragma unroll
+        for (int i = 0; i < NC; ++i) acc = acc + v[i] * c[i];
+        const int64_t o = transfer_idx(t, s, j, rhs);
+        out[o] = accumulate ? out[o] + acc : acc;
+    }
+}
+
 // W[B][i][h][sp] = (D P_{B,i})(h) on the (bx+2) x (by+2) halo frame of block B
 __global__ void k_W0(const cx<double>* __restrict__ V, const cx<double>* __restrict__ U, const double* __restrict__ C,
                      Geom g, int bx, int by, int nc, double diag, double mu, double r, cx<double>* __restrict__ W) {
@@ -408,9 +490,9 @@ __global__ void __launch_bounds__(256) k_coarse_apply(const cx<T>* __restrict__ 
     constexpr int K = EPI == 2 ? 3 : 1;
     const int nc = xin.ndof, nrhs = xin.nrhs;
     const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
-    double v[K];
+    T v[K];  // per-thread partials in the field precision (FP64 is scarce on this part)
 #pragma unroll
-    for (int k = 0; k < K; ++k) v[k] = 0.0;
+    for (int k = 0; k < K; ++k) v[k] = T(0);
     const int64_t nrow = (int64_t)xin.nsites * nc;
     if (rhs < nrhs) {
         for (int64_t row = (int64_t)blockIdx.x * blockDim.y + threadIdx.y; row < nrow;
@@ -430,12 +512,12 @@ __global__ void __launch_bounds__(256) k_coarse_apply(const cx<T>* __restrict__ 
             const int64_t o = ((int64_t)s * nc + i) * nrhs + rhs;
             y[o] = acc;
             if (EPI == 1) {
-                v[0] += (double)norm2(acc);
+                v[0] += norm2(acc);
             } else if (EPI == 2) {
                 const cx<T> c = cmulc(acc, w[o]);
-                v[0] += (double)c.re;
-                v[1] += (double)c.im;
-                v[2] += (double)norm2(acc);
+                v[0] += c.re;
+                v[1] += c.im;
+                v[2] += norm2(acc);
             }
         }
     }
@@ -452,9 +534,9 @@ __global__ void __launch_bounds__(256) k_coarse_apply1(const cx<T>* __restrict__
                                                        unsigned int* ticket, double* out, const int* __restrict__ gate) {
     if (gate && *gate == 0) return;
     constexpr int K = EPI == 2 ? 3 : 1;
-    double v[K];
+    T v[K];  // per-thread partials in the field precision (FP64 is scarce on this part)
 #pragma unroll
-    for (int k = 0; k < K; ++k) v[k] = 0.0;
+    for (int k = 0; k < K; ++k) v[k] = T(0);
     const int64_t nrow = (int64_t)xin.nsites * NC;
     for (int64_t row = (int64_t)blockIdx.x * blockDim.y + threadIdx.y; row < nrow;
          row += (int64_t)gridDim.x * blockDim.y) {
@@ -473,12 +555,12 @@ __global__ void __launch_bounds__(256) k_coarse_apply1(const cx<T>* __restrict__
         }
         y[row] = acc;
         if (EPI == 1) {
-            v[0] += (double)norm2(acc);
+            v[0] += norm2(acc);
         } else if (EPI == 2) {
             const cx<T> c = cmulc(acc, w[row]);
-            v[0] += (double)c.re;
-            v[1] += (double)c.im;
-            v[2] += (double)norm2(acc);
+            v[0] += c.re;
+            v[1] += c.im;
+            v[2] += norm2(acc);
         }
     }
     if (EPI != 0) block_reduce_finalise<K>(v, partials, ticket, 1, FinStore{out, K});
@@ -506,9 +588,9 @@ __global__ void __launch_bounds__(256) k_coarse_apply_tiled(const cx<T>* __restr
     const int r0 = blockIdx.y * lanes;
     const int rhs = r0 + threadIdx.x;
     const int tid = threadIdx.y * lanes + threadIdx.x, nthr = lanes * rows;
-    double v[K];
+    T v[K];  // per-thread partials in the field precision (FP64 is scarce on this part)
 #pragma unroll
-    for (int k = 0; k < K; ++k) v[k] = 0.0;
+    for (int k = 0; k < K; ++k) v[k] = T(0);
     for (int s = blockIdx.x; s < xin.nsites; s += gridDim.x) {
         const int x = s % nx, yy = s / nx;
         cx<T> acc[kPer];
@@ -546,12 +628,12 @@ __global__ void __launch_bounds__(256) k_coarse_apply_tiled(const cx<T>* __restr
                     const int64_t o = ((int64_t)s * NC + i) * nrhs + rhs;
                     y[o] = acc[a];
                     if (EPI == 1) {
-                        v[0] += (double)norm2(acc[a]);
+                        v[0] += norm2(acc[a]);
                     } else if (EPI == 2) {
                         const cx<T> c = cmulc(acc[a], w[o]);
-                        v[0] += (double)c.re;
-                        v[1] += (double)c.im;
-                        v[2] += (double)norm2(acc[a]);
+                        v[0] += c.re;
+                        v[1] += c.im;
+                        v[2] += norm2(acc[a]);
                     }
                 }
             }
@@ -671,15 +753,15 @@ __global__ void __launch_bounds__(256) k_coarse_cg1(CoarseCgArgs a) {
     double* part0 = a.part;              // <p, Ap> partials
     double* part1 = a.part + gridDim.x;  // ||r||^2 partials
     // x = 0, r = p = b (each element is owned by one thread for the whole solve)
-    double loc = 0;
+    T loc_t = 0;  // per-thread partials in the field precision
     for (int e = t0; e < n; e += stride) {
         const cx<T> v = b[e];
         x[e] = mk<T>(0, 0);
         r[e] = v;
         p[e] = v;
-        loc += (double)norm2(v);
+        loc_t += norm2(v);
     }
-    loc = block_sum256(loc);
+    double loc = block_sum256((double)loc_t);
     if (threadIdx.x == 0) part1[blockIdx.x] = loc;
     if (!grid_barrier(a.bar, a.err)) return;
     double rr = sum_partials(part1);
@@ -688,7 +770,7 @@ __global__ void __launch_bounds__(256) k_coarse_cg1(CoarseCgArgs a) {
     const bool solve = bnorm2 >= 1e-60 && isfinite(bnorm2);  // ||b|| < 1e-30 returns x = 0
     while (solve && it < a.max_iter) {
         // Ap = A p, partial <Ap, p>
-        double pap = 0;
+        T pap_t = 0;
         for (int e = t0; e < n; e += stride) {
             const int s = e / NC, i = e - s * NC;
             const int xs = s % a.nx, ys = s / a.nx;
@@ -704,22 +786,22 @@ __global__ void __launch_bounds__(256) k_coarse_cg1(CoarseCgArgs a) {
                 for (int j = 0; j < NC; ++j) acc = acc + Ad[j * NC] * ldcg_cx(pv + j);
             }
             Ap[e] = acc;
-            pap += (double)cmulc(acc, p[e]).re;
+            pap_t += cmulc(acc, p[e]).re;
         }
-        pap = block_sum256(pap);
+        double pap = block_sum256((double)pap_t);
         if (threadIdx.x == 0) part0[blockIdx.x] = pap;
         if (!grid_barrier(a.bar, a.err)) return;
         pap = sum_partials(part0);
         if (!(fabs(pap) >= 1e-30) || !isfinite(pap)) break;  // coarse_op.h:522
         const T al = (T)(rr / pap);
-        double rloc = 0;
+        T rloc_t = 0;
         for (int e = t0; e < n; e += stride) {
             const cx<T> ri = r[e] - al * Ap[e];
             x[e] = x[e] + al * p[e];
             r[e] = ri;
-            rloc += (double)norm2(ri);
+            rloc_t += norm2(ri);
         }
-        rloc = block_sum256(rloc);
+        double rloc = block_sum256((double)rloc_t);
         if (threadIdx.x == 0) part1[blockIdx.x] = rloc;
         if (!grid_barrier(a.bar, a.err)) return;
         const double rr_new = sum_partials(part1);
@@ -802,7 +884,7 @@ __global__ void __launch_bounds__(256) k_ccg_update(CcgState s, VecView<T> x, cx
     }
     __syncthreads();
     const T al = s_al[threadIdx.x];
-    double v[1] = {0.0};
+    T v[1] = {T(0)};
     if (rhs < nrhs) {
         for (int st = blockIdx.x * blockDim.y + threadIdx.y; st < x.nsites; st += gridDim.x * blockDim.y) {
             const int64_t base = x.idx(st, rhs, 0);
@@ -811,7 +893,7 @@ __global__ void __launch_bounds__(256) k_ccg_update(CcgState s, VecView<T> x, cx
                 const cx<T> ri = r[base + (int64_t)d * ds] - al * Ap[base + (int64_t)d * ds];
                 x.p[base + (int64_t)d * ds] = x.p[base + (int64_t)d * ds] + al * p[base + (int64_t)d * ds];
                 r[base + (int64_t)d * ds] = ri;
-                v[0] += (double)norm2(ri);
+                v[0] += norm2(ri);
             }
         }
     }
@@ -1252,21 +1334,53 @@ smg_status coarse_cg(smg_mg* mg, int l, void* x, const void* b) {
     return SMG_OK;
 }
 
+TransferGeom transfer_geom(const smg_mg* mg, int l, int nrhs) {
+    const Level& L = mg->lv[l];
+    TransferGeom t;
+    t.level0 = l == 0 ? 1 : 0;
+    if (l == 0) t.g = mg->null0[0]->g;
+    t.nx = L.nx;
+    t.ax = L.ax;
+    t.ay = L.ay;
+    t.nax = L.nx / L.ax;
+    t.ndof = L.ndof;
+    t.nrhs = nrhs;
+    return t;
+}
+
+dim3 transfer_block(int nrhs) {
+    int lanes = 1;
+    while (lanes * 2 <= nrhs && lanes < 32) lanes *= 2;
+    return dim3(lanes, 256 / lanes);
+}
+
 template <typename T>
 smg_status restrict_to(smg_mg* mg, int l, const void* fine_or_coarse, void* out) {
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[l];
     const Level& N = mg->lv[l + 1];
     const int nrhs = mg->work_nrhs;
-    int64_t total = (int64_t)N.nsites * nrhs * L.nc_next;
-    if (l == 0) {
-        k_restrict0<T><<<blocks_for(total), 256, 0, ctx->stream>>>(Vp<T>(L), (const cx<T>*)fine_or_coarse, (cx<T>*)out,
-                                                                  mg->null0.empty() ? Geom{} : mg->null0[0]->g, L.ax,
-                                                                  L.ay, L.nc_next, nrhs);
+    const int nc = L.nc_next;
+    if ((nc == 8 || nc == 16 || nc == 32) && nrhs >= 8) {  // few rhs: one thread per output below
+        TransferGeom t = transfer_geom(mg, l, nrhs);
+        const dim3 block = transfer_block(nrhs);
+        const dim3 grid(N.nsites, (nrhs + block.x - 1) / block.x);
+        const size_t sm = (size_t)block.x * block.y * kTransferChunk * sizeof(cx<T>);
+#define SMG_RA(NC) k_restrict_agg<T, NC><<<grid, block, sm, ctx->stream>>>(Vp<T>(L), (const cx<T>*)fine_or_coarse, (cx<T>*)out, t)
+        if (nc == 8) SMG_RA(8);
+        else if (nc == 16) SMG_RA(16);
+        else SMG_RA(32);
+#undef SMG_RA
     } else {
-        k_restrict_c<T><<<blocks_for(total), 256, 0, ctx->stream>>>(Vp<T>(L), (const cx<T>*)fine_or_coarse,
-                                                                   (cx<T>*)out, L.nx, L.ax, L.ay, L.ndof, L.nc_next,
-                                                                   N.nsites, nrhs);
+        int64_t total = (int64_t)N.nsites * nrhs * nc;
+        if (l == 0)
+            k_restrict0<T><<<blocks_for(total), 256, 0, ctx->stream>>>(Vp<T>(L), (const cx<T>*)fine_or_coarse,
+                                                                      (cx<T>*)out, mg->null0[0]->g, L.ax, L.ay, nc,
+                                                                      nrhs);
+        else
+            k_restrict_c<T><<<blocks_for(total), 256, 0, ctx->stream>>>(Vp<T>(L), (const cx<T>*)fine_or_coarse,
+                                                                       (cx<T>*)out, L.nx, L.ax, L.ay, L.ndof, nc,
+                                                                       N.nsites, nrhs);
     }
     count_launch(ctx);
     SMG_CHECK_LAUNCH(ctx);
@@ -1277,16 +1391,26 @@ template <typename T>
 smg_status prolong_to(smg_mg* mg, int l, const void* coarse, void* out, int accumulate) {
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[l];
+    const Level& N = mg->lv[l + 1];
     const int nrhs = mg->work_nrhs;
-    if (l == 0) {
+    const int nc = L.nc_next;
+    if ((nc == 8 || nc == 16 || nc == 32) && nrhs >= 8) {  // few rhs: one thread per output below
+        TransferGeom t = transfer_geom(mg, l, nrhs);
+        const dim3 block = transfer_block(nrhs);
+        const dim3 grid(N.nsites, (nrhs + block.x - 1) / block.x);
+#define SMG_PA(NC) k_prolong_agg<T, NC><<<grid, block, 0, ctx->stream>>>(Vp<T>(L), (const cx<T>*)coarse, (cx<T>*)out, t, accumulate)
+        if (nc == 8) SMG_PA(8);
+        else if (nc == 16) SMG_PA(16);
+        else SMG_PA(32);
+#undef SMG_PA
+    } else if (l == 0) {
         const Geom g = mg->null0[0]->g;
         k_prolong0<T><<<blocks_for((int64_t)g.V * nrhs), 256, 0, ctx->stream>>>(
-            Vp<T>(L), (const cx<T>*)coarse, (cx<T>*)out, g, L.ax, L.ay, L.nc_next, nrhs, accumulate);
+            Vp<T>(L), (const cx<T>*)coarse, (cx<T>*)out, g, L.ax, L.ay, nc, nrhs, accumulate);
     } else {
         int64_t total = (int64_t)L.nsites * nrhs * L.ndof;
         k_prolong_c<T><<<blocks_for(total), 256, 0, ctx->stream>>>(Vp<T>(L), (const cx<T>*)coarse, (cx<T>*)out, L.nx,
-                                                                  L.ny, L.ax, L.ay, L.ndof, L.nc_next, nrhs,
-                                                                  accumulate);
+                                                                  L.ny, L.ax, L.ay, L.ndof, nc, nrhs, accumulate);
     }
     count_launch(ctx);
     SMG_CHECK_LAUNCH(ctx);

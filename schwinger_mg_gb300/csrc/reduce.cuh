@@ -74,8 +74,19 @@ __device__ __forceinline__ void block_reduce_finalise(double (&v)[K], double* __
         const int r = rhs0 + l;
         double a = 0.0;
         if (r < nrhs) {
+            // eight independent accumulators keep eight loads in flight; fixed order, deterministic
             const double* src = partials + ((size_t)r * K + k) * gridDim.x;
-            for (int b = lane_id; b < (int)gridDim.x; b += 32) a += __ldcg(src + b);
+            const int nb = (int)gridDim.x;
+            double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            int b = lane_id;
+            for (; b + 7 * 32 < nb; b += 8 * 32) {
+#pragma unroll
+                for (int u = 0; u < 8; ++u) acc[u] += __ldcg(src + b + u * 32);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (b + u * 32 < nb) acc[u] += __ldcg(src + b + u * 32);
+            a = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
         }
         for (int off = 16; off >= 1; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
         if (lane_id == 0) s_fin[k][l] = a;
@@ -88,6 +99,16 @@ __device__ __forceinline__ void block_reduce_finalise(double (&v)[K], double* __
         fin(rhs0 + t, sums);
     }
     if (t == 0) ticket[blockIdx.y] = 0u;
+}
+
+// FP32 per-thread partials: widened to FP64 once per thread, then reduced as above.
+template <int K, typename Fin>
+__device__ __forceinline__ void block_reduce_finalise(float (&v)[K], double* __restrict__ partials,
+                                                      unsigned int* __restrict__ ticket, int nrhs, const Fin& fin) {
+    double d[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) d[k] = (double)v[k];
+    block_reduce_finalise<K>(d, partials, ticket, nrhs, fin);
 }
 
 // Launch shape for reducing kernels: lanes is a power of two <= 32, at most

@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) k_cg_update(CgState s, cx<T>* __restrict_
     }
     __syncthreads();
     const T al = s_alpha[threadIdx.x];
-    double v[1] = {0.0};
+    T v[1] = {T(0)};
     if (rhs < nrhs) {
         for (int q = blockIdx.x * blockDim.y + threadIdx.y; q < nsites; q += gridDim.x * blockDim.y) {
 #pragma unroll
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(256) k_cg_update(CgState s, cx<T>* __restrict_
                 cx<T> ri = r[i] - al * Ap[i];
                 x[i] = x[i] + al * pi;
                 r[i] = ri;
-                v[0] += (double)norm2(ri);
+                v[0] += norm2(ri);
             }
         }
     }
@@ -335,9 +335,9 @@ __global__ void __launch_bounds__(256) k_gcr_multidot(VecView<T> az, DotPtrs<T> 
                                                       unsigned int* ticket, double* out, int stride) {
     constexpr int K = 2 * kDotChunk;
     const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
-    double v[K];
+    T v[K];  // per-thread partials in the field precision (FP64 is scarce on this part)
 #pragma unroll
-    for (int k = 0; k < K; ++k) v[k] = 0.0;
+    for (int k = 0; k < K; ++k) v[k] = T(0);
     if (rhs < az.nrhs) {
         for (int s = blockIdx.x * blockDim.y + threadIdx.y; s < az.nsites; s += gridDim.x * blockDim.y) {
             const Spinor<T> z = ld_spinor(az.p, s, rhs, az.nrhs);
@@ -346,8 +346,8 @@ __global__ void __launch_bounds__(256) k_gcr_multidot(VecView<T> az, DotPtrs<T> 
                 if (i < ns) {
                     const Spinor<T> a = ld_spinor(ptr.ap[i], s, rhs, az.nrhs);
                     const cx<T> c = cmulc(a.s0, z.s0) + cmulc(a.s1, z.s1);
-                    v[2 * i] += (double)c.re;
-                    v[2 * i + 1] += (double)c.im;
+                    v[2 * i] += c.re;
+                    v[2 * i + 1] += c.im;
                 }
             }
         }
@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(256) k_gcr_orth_all(VecView<T> p, cx<T>* Ap,
         s_b[i][threadIdx.x] = be;
     }
     __syncthreads();
-    double v[3] = {0.0, 0.0, 0.0};
+    T v[3] = {T(0), T(0), T(0)};
     if (rhs < nrhs) {
         for (int s = blockIdx.x * blockDim.y + threadIdx.y; s < p.nsites; s += gridDim.x * blockDim.y) {
             Spinor<T> q = ld_spinor(z, s, rhs, nrhs);
@@ -404,9 +404,9 @@ __global__ void __launch_bounds__(256) k_gcr_orth_all(VecView<T> p, cx<T>* Ap,
             if (last) {
                 const Spinor<T> rr = ld_spinor(r, s, rhs, nrhs);
                 const cx<T> c = cmulc(aq.s0, rr.s0) + cmulc(aq.s1, rr.s1);
-                v[0] += (double)c.re;
-                v[1] += (double)c.im;
-                v[2] += (double)(norm2(aq.s0) + norm2(aq.s1));
+                v[0] += c.re;
+                v[1] += c.im;
+                v[2] += norm2(aq.s0) + norm2(aq.s1);
             }
         }
     }
@@ -439,7 +439,7 @@ __global__ void __launch_bounds__(256) k_gcr_update(GcrScalars sc, VecView<T> x,
     }
     __syncthreads();
     const cx<T> al = s_al[threadIdx.x];
-    double v[1] = {0.0};
+    T v[1] = {T(0)};
     if (rhs < nrhs) {
         for (int st = blockIdx.x * blockDim.y + threadIdx.y; st < x.nsites; st += gridDim.x * blockDim.y) {
             const int64_t base = x.idx(st, rhs, 0);
@@ -448,7 +448,7 @@ __global__ void __launch_bounds__(256) k_gcr_update(GcrScalars sc, VecView<T> x,
                 const cx<T> ri = r[base + (int64_t)d * ds] - al * Ap[base + (int64_t)d * ds];
                 x.p[base + (int64_t)d * ds] = x.p[base + (int64_t)d * ds] + al * p[base + (int64_t)d * ds];
                 r[base + (int64_t)d * ds] = ri;
-                v[0] += (double)norm2(ri);
+                v[0] += norm2(ri);
             }
         }
     }
@@ -593,7 +593,9 @@ smg_status gcr_core(smg_dirac* d, smg_mg* mg, GcrWs<T>& ws, const smg_field* b, 
             DotPtrs<T> dp{};
             const int ns = std::min(kDotChunk, nring - c0);
             for (int i = 0; i < ns; ++i) dp.ap[i] = (const cx<T>*)ws.AP[ring[c0 + i]]->data;
-            k_gcr_multidot<T><<<rl.grid, rl.block, 0, ctx->stream>>>(fv<T>(ws.Az), dp, ns, ctx->red.partials,
+            // 2 blocks per SM: the 2 ns partials per rhs and block stay few for the final sum
+            const dim3 mgrid(std::min(rl.grid.x, 304u), rl.grid.y);
+            k_gcr_multidot<T><<<mgrid, rl.block, 0, ctx->stream>>>(fv<T>(ws.Az), dp, ns, ctx->red.partials,
                                                                     ctx->red.tickets, ws.dots + 2 * c0,
                                                                     2 * ws.nbuf);
             count_launch(ctx);

@@ -39,9 +39,9 @@ __global__ void __launch_bounds__(256) k_vreduce(VecView<T> a, const cx<T>* __re
                                                  unsigned int* ticket, double* out) {
     constexpr int K = MODE == VR_DOT ? 2 : (MODE == VR_NORM ? 1 : 3);
     const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
-    double v[K];
+    T v[K];  // per-thread partials in the field precision (FP64 is scarce on this part)
 #pragma unroll
-    for (int k = 0; k < K; ++k) v[k] = 0.0;
+    for (int k = 0; k < K; ++k) v[k] = T(0);
     if (rhs < a.nrhs) {
         for (int s = blockIdx.x * blockDim.y + threadIdx.y; s < a.nsites; s += gridDim.x * blockDim.y) {
             const int64_t base = a.idx(s, rhs, 0);
@@ -57,14 +57,14 @@ __global__ void __launch_bounds__(256) k_vreduce(VecView<T> a, const cx<T>* __re
                 if (MODE != VR_DOT) r2 += norm2(x);
             }
             if (MODE == VR_DOT) {
-                v[0] += (double)r0;
-                v[1] += (double)r1;
+                v[0] += r0;
+                v[1] += r1;
             } else if (MODE == VR_NORM) {
-                v[0] += (double)r2;
+                v[0] += r2;
             } else {
-                v[0] += (double)r0;
-                v[1] += (double)r1;
-                v[2] += (double)r2;
+                v[0] += r0;
+                v[1] += r1;
+                v[2] += r2;
             }
         }
     }

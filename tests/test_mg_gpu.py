@@ -104,16 +104,19 @@ def test_chiral_mg_gcr_true_residual(smg_gpu, levels, prec):
     assert np.linalg.norm(b - Ax) / np.linalg.norm(b) < 1e-10
 
 
-def test_multi_rhs_cycle_equals_single(smg_gpu):
+@pytest.mark.parametrize("nrhs,levels", [(4, 2), (16, 3)])
+def test_multi_rhs_cycle_equals_single(smg_gpu, nrhs, levels):
+    """The batched cycle (aggregate-blocked transfers from 8 RHS up) equals one cycle per RHS."""
     L = 32
     U = smg_gpu.gauge_normal(L, 4.0, 17)
     lat = smg_gpu.Lattice(L)
     D = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, U), 0.05, 1.0, 1.0, 0.0)
-    p = smg_gpu.mg_params(2, 4, 4, chiral_split=True, null_iters=3, coarse_tol=1e-6, coarse_max_iter=500)
+    p = smg_gpu.mg_params(levels, 4, 4, blocks=[(4, 4), (2, 2)], chiral_split=True, null_iters=3, coarse_tol=1e-6,
+                          coarse_max_iter=500)
     mg = smg_gpu.MGHierarchy(D, p)
-    B = np.stack([smg_gpu.random_vec(lat.ndof, 300 + j) for j in range(4)])
+    B = np.stack([smg_gpu.random_vec(lat.ndof, 300 + j) for j in range(nrhs)])
     multi = mg.precondition(B)
-    for j in (0, 3):
+    for j in (0, nrhs - 1):
         single = mg.precondition(B[j])
         assert np.linalg.norm(multi[j] - single) / np.linalg.norm(single) < 1e-10
 
