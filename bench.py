@@ -127,7 +127,7 @@ def max_over_ranks(v: float, ws: int) -> float:
 
 # ------------------------------------------------------------------ workloads
 MG = dict(L=512, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20240, nrhs=32, levels=3, blocks=[(4, 4), (2, 2)],
-          n_vec=16, chiral=False, w_cycle=False, null_iters=6, pre=4, post=4, coarse_max_iter=40, coarse_tol=5e-2,
+          n_vec=16, chiral=False, w_cycle=False, null_iters=6, pre=4, post=4, coarse_max_iter=20, coarse_tol=5e-2,
           tol=1e-10,
           max_iter=500, trunc=20)
 DSLASH = dict(L=512, nrhs=32, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20240)

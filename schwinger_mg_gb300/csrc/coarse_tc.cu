@@ -16,24 +16,33 @@
 //
 // and the epilogue forms Re y(i, r) = D[2r][i] - D[2r+1][16+i] and
 // Im y(i, r) = D[2r][16+i] + D[2r+1][i] (the two rows sit in adjacent lanes
-// of one warp).  One MMA per direction (K = 16 is one kind::f16 step), nine
-// per site, accumulated in 32 tensor-memory columns.  The MMA is issued with
-// M = 128: rows 64..127 read the next 2 KB of shared memory and are never
-// read back, which keeps the accumulator in the plain one-lane-per-row layout.
+// of one warp).  The MMA is issued with M = 128: rows 64..127 read the next
+// 2 KB of shared memory and are never read back, which keeps the accumulator
+// in the plain one-lane-per-row layout.
 //
-// Data movement (one CTA = a strip of kW = 8 sites along x, H rows):
-//   * links are pre-tiled once per hierarchy into the exact shared-memory
-//     image of the B operand (K-major, no swizzle; 1 KB per site and
-//     direction), so each site's 9 KB arrive with one cp.async.bulk into a
-//     ring of kLinkSlots site slots;
+// Source grouping.  A source tile x_t serves the three output sites of its
+// row that reach it along x (dx = +1, 0, -1): one MMA with the three link
+// blocks stacked along N (N = 96) accumulates into the three sites' adjacent
+// 32-column accumulators.  A small MMA costs the same issue time for N up to
+// 128, so a row of kW = 8 sites takes 3 x 10 MMAs instead of 72.  The links
+// are pre-tiled once per hierarchy so that, for an output row y and a source
+// row offset dy, block L[x][(dx, dy)] sits at position P = 3x + 4 + 2dx
+// (mod 3 nx): the nine sites' blocks of a CTA strip for one dy form one
+// contiguous run of 3 kW + 2 blocks and the stacked operand of source t is
+// three consecutive blocks.
+//
+// Data movement (one CTA = a strip of kW sites along x, H rows):
+//   * per output row and dy one 26 KB run of BF16 link blocks arrives by
+//     cp.async.bulk (two when the run wraps around the lattice) into a ring
+//     of kUnits units;
 //   * each source row (kW + 2 sites with the x halo) is converted from the
 //     FP32 vector [site][dof][rhs] layout into BF16 A tiles by four stager
-//     warps and kept in a ring of four rows: the MMAs of output row y read
-//     source rows y-1, y, y+1 and every source tile serves the nine output
-//     sites around it through its shared-memory descriptor;
+//     warps and kept in a ring of four rows (output row y reads source rows
+//     y-1, y, y+1);
 //   * warp 0 issues the link copies, warp 1 the MMAs, warps 4 and 5 read the
-//     accumulators (TMEM lanes 0..63) and write y, with the fused per-rhs
-//     reductions ||y||^2 and <y, w> of the FP32 kernels.
+//     accumulators (TMEM lanes 0..63, one 256-column slot per output row, two
+//     slots) and write y, with the fused per-rhs reductions ||y||^2 and
+//     <y, w> of the FP32 kernels.
 // Every mbarrier wait is bounded (about one second of SM clock); on timeout
 // the CTA raises *err = 2, waits (bounded) for its own bulk copies and MMAs,
 // frees its tensor memory and returns.
@@ -53,26 +62,29 @@ constexpr int kTileA = 8 * kSboA;             // 64 rows x 16 K (BF16) = 2176 by
 constexpr int kRowBytes = kSrcSites * kTileA;  // one source row
 constexpr int kRingBytes = kRing * kRowBytes;
 constexpr int kLinkDir = 1024;                // 32 x 16 BF16, K-major, no swizzle
-constexpr int kLinkSite = 9 * kLinkDir;       // one site's nine blocks
-constexpr int kLinkSlots = 12;
-constexpr int kLinkBytes = kLinkSlots * kLinkSite;
-constexpr int kAccSlots = 16;                 // 32 TMEM columns each
-constexpr int kTmemCols = 512;
-// barriers: src_full[4], src_empty[4], link_full[LS], link_empty[LS], acc_full[AS], acc_empty[AS], final
+constexpr int kLinkSite = 9 * kLinkDir;       // one site's nine blocks (HBM bytes per site)
+constexpr int kRunBlocks = 3 * kW + 2;        // link blocks of one (output row, dy) run of a strip
+constexpr int kUnitBytes = kRunBlocks * kLinkDir;
+constexpr int kUnits = 5;                     // link runs resident
+constexpr int kLinkBytes = kUnits * kUnitBytes;
+constexpr int kAccCols = kW * 32;             // one output row of accumulators
+constexpr int kTmemCols = 512;                // two row slots
+// barriers: src_full[4], src_empty[4], unit_full[U], unit_empty[U], acc_full[2], acc_empty[2], final
 constexpr int kBarSrcFull = 0;
 constexpr int kBarSrcEmpty = kBarSrcFull + kRing;
-constexpr int kBarLinkFull = kBarSrcEmpty + kRing;
-constexpr int kBarLinkEmpty = kBarLinkFull + kLinkSlots;
-constexpr int kBarAccFull = kBarLinkEmpty + kLinkSlots;
-constexpr int kBarAccEmpty = kBarAccFull + kAccSlots;
-constexpr int kBarFinal = kBarAccEmpty + kAccSlots;
+constexpr int kBarUnitFull = kBarSrcEmpty + kRing;
+constexpr int kBarUnitEmpty = kBarUnitFull + kUnits;
+constexpr int kBarAccFull = kBarUnitEmpty + kUnits;
+constexpr int kBarAccEmpty = kBarAccFull + 2;
+constexpr int kBarFinal = kBarAccEmpty + 2;
 constexpr int kNumBars = kBarFinal + 1;
 constexpr int kBarOffset = kRingBytes + kLinkBytes;           // A-tile over-read (M = 128) lands in the link ring
 constexpr int kMiscOffset = kBarOffset + kNumBars * 8;
 constexpr int kRedOffset = (kMiscOffset + 16 + 15) / 16 * 16;  // 32 rhs x 3 doubles
 constexpr int kSmemBytes = kRedOffset + kRhsTile * 3 * 8;
-static_assert(kSmemBytes <= 227 * 1024, "shared memory budget");
-static_assert(kTileA % 16 == 0 && kRowBytes % 16 == 0 && kLinkSite % 16 == 0, "16-byte alignment");
+static_assert(kSmemBytes + 1024 <= 227 * 1024, "shared memory budget");
+static_assert(kTileA % 16 == 0 && kRowBytes % 16 == 0 && kUnitBytes % 16 == 0, "16-byte alignment");
+static_assert(2 * kAccCols <= kTmemCols, "tensor memory budget");
 
 constexpr long long kWaitCycles = 2000000000ll;  // ~1 s at 2 GHz
 constexpr long long kDrainCycles = 200000000ll;  // ~0.1 s
@@ -148,16 +160,36 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
-// Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major, N = 32, M = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+// Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+}
 
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "setp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
         : "memory");
+}
+
+// Source t (x = x0 - 1 + t) of a strip row feeds output sites t-2 (dx = +1),
+// t-1 (dx = 0) and t (dx = -1) that lie in [0, kW): the first of them, their
+// count, and the offset of their stacked link blocks inside a run.
+struct SrcGroup {
+    int first, count, run_off;
+};
+__device__ __forceinline__ SrcGroup src_group(int t) {
+    const int lo = t - 2 < 0 ? 0 : t - 2, hi = t > kW - 1 ? kW - 1 : t;
+    // block of (site i, dx) sits at run position 3 i + 4 + 2 dx - 2; the group's first block is
+    // (lo, dx = t - 1 - lo)
+    SrcGroup g;
+    g.first = lo;
+    g.count = hi - lo + 1;
+    g.run_off = (3 * lo + 2 + 2 * (t - 1 - lo)) * kLinkDir;
+    return g;
 }
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
@@ -206,7 +238,6 @@ __global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int H = a.H, nx = a.nx, ny = a.ny, nrhs = a.nrhs;
     const int x0 = blockIdx.x * kW, y0 = blockIdx.y * H, rhs0 = blockIdx.z * kRhsTile;
-    const int nseq = H * kW;
     const uint32_t ring_a = smem_u32(smem);
     const uint32_t link_a = ring_a + kRingBytes;
     const uint32_t bar_a = ring_a + kBarOffset;
@@ -220,11 +251,11 @@ __global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
             mbar_init(bar(kBarSrcFull + i), 128);
             mbar_init(bar(kBarSrcEmpty + i), 1);
         }
-        for (int i = 0; i < kLinkSlots; ++i) {
-            mbar_init(bar(kBarLinkFull + i), 1);
-            mbar_init(bar(kBarLinkEmpty + i), 1);
+        for (int i = 0; i < kUnits; ++i) {
+            mbar_init(bar(kBarUnitFull + i), 1);
+            mbar_init(bar(kBarUnitEmpty + i), 1);
         }
-        for (int i = 0; i < kAccSlots; ++i) {
+        for (int i = 0; i < 2; ++i) {
             mbar_init(bar(kBarAccFull + i), 1);
             mbar_init(bar(kBarAccEmpty + i), 64);
         }
@@ -245,57 +276,64 @@ __global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
     const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(misc);
 
     if (warp == 0) {
-        // ---------------- link producer: one bulk copy of 9 KB per output site
+        // ---------------- link producer: per output row and dy one run of kRunBlocks blocks
         if (lane == 0) {
+            const int ring3 = 3 * nx;  // blocks per (output row, dy) on the lattice
             int issued = 0;
-            for (int seq = 0; seq < nseq; ++seq) {
-                const int slot = seq % kLinkSlots, use = seq / kLinkSlots;
-                if (use > 0 && !wait_bar(bar(kBarLinkEmpty + slot), (use - 1) & 1, abort_flag)) break;
-                const int r = seq / kW, i = seq - r * kW;
-                const int64_t site = (int64_t)(x0 + i) + (int64_t)nx * (y0 + r);
-                mbar_expect_tx(bar(kBarLinkFull + slot), kLinkSite);
-                bulk_g2s(link_a + slot * kLinkSite, a.links + site * kLinkSite, kLinkSite, bar(kBarLinkFull + slot));
-                issued = seq + 1;
+            const int nunits = 3 * H;
+            for (int u = 0; u < nunits; ++u) {
+                const int slot = u % kUnits, use = u / kUnits;
+                if (use > 0 && !wait_bar(bar(kBarUnitEmpty + slot), (use - 1) & 1, abort_flag)) break;
+                const int r = u / 3, dyi = u - 3 * r;  // dy = dyi - 1
+                const uint8_t* row = a.links + ((int64_t)(y0 + r) * 3 + dyi) * ring3 * kLinkDir;
+                const int p0 = (3 * x0 + 2) % ring3;
+                const int n1 = ring3 - p0 < kRunBlocks ? ring3 - p0 : kRunBlocks;
+                const uint32_t dst = link_a + (uint32_t)(slot * kUnitBytes);
+                mbar_expect_tx(bar(kBarUnitFull + slot), kUnitBytes);
+                bulk_g2s(dst, row + (int64_t)p0 * kLinkDir, (uint32_t)(n1 * kLinkDir), bar(kBarUnitFull + slot));
+                if (n1 < kRunBlocks)  // the run wraps around the lattice
+                    bulk_g2s(dst + (uint32_t)(n1 * kLinkDir), row, (uint32_t)((kRunBlocks - n1) * kLinkDir),
+                             bar(kBarUnitFull + slot));
+                issued = u + 1;
             }
             // every issued copy has landed before the CTA can leave
-            for (int seq = issued > kLinkSlots ? issued - kLinkSlots : 0; seq < issued; ++seq)
-                drain_bar(bar(kBarLinkFull + seq % kLinkSlots), (seq / kLinkSlots) & 1);
+            for (int u = issued > kUnits ? issued - kUnits : 0; u < issued; ++u)
+                drain_bar(bar(kBarUnitFull + u % kUnits), (u / kUnits) & 1);
         }
         __syncwarp();
     } else if (warp == 1) {
-        // ---------------- MMA issuer
+        // ---------------- MMA issuer: per output row, 3 dy x 10 source groups
         if (lane == 0) {
             bool ok = true;
-            int seq = 0;
             for (int r = 0; r < H && ok; ++r) {
                 for (int lr = (r == 0 ? 0 : r + 2); lr <= r + 2 && ok; ++lr)
                     ok = wait_bar(bar(kBarSrcFull + lr % kRing), (lr / kRing) & 1, abort_flag);
+                if (ok && r >= 2) ok = wait_bar(bar(kBarAccEmpty + (r & 1)), ((r >> 1) - 1) & 1, abort_flag);
                 if (!ok) break;
-                tc_fence_after();
-                for (int i = 0; i < kW; ++i, ++seq) {
-                    const int ls = seq % kLinkSlots, as = seq % kAccSlots;
-                    if (!wait_bar(bar(kBarLinkFull + ls), (seq / kLinkSlots) & 1, abort_flag)) {
-                        ok = false;
-                        break;
-                    }
-                    if (seq >= kAccSlots &&
-                        !wait_bar(bar(kBarAccEmpty + as), ((seq / kAccSlots) - 1) & 1, abort_flag)) {
-                        ok = false;
-                        break;
-                    }
+                const uint32_t acc = tmem + (uint32_t)((r & 1) * kAccCols);
+                for (int dyi = 0; dyi < 3 && ok; ++dyi) {
+                    const int u = 3 * r + dyi, slot = u % kUnits;
+                    ok = wait_bar(bar(kBarUnitFull + slot), (u / kUnits) & 1, abort_flag);
+                    if (!ok) break;
                     tc_fence_after();
-                    const uint32_t d_tmem = tmem + (uint32_t)(as * 32);
+                    const int lr = r + dyi;  // source row y + dy, dy = dyi - 1
+                    const uint32_t arow = ring_a + (uint32_t)((lr % kRing) * kRowBytes);
+                    const uint32_t unit = link_a + (uint32_t)(slot * kUnitBytes);
 #pragma unroll
-                    for (int d = 0; d < 9; ++d) {
-                        const int lr = r + 1 + dir_dy(d), t = i + 1 + dir_dx(d);
-                        const uint32_t aa = ring_a + (uint32_t)((lr % kRing) * kRowBytes + t * kTileA);
-                        const uint32_t ba = link_a + (uint32_t)(ls * kLinkSite + d * kLinkDir);
-                        mma_bf16(d_tmem, smem_desc(aa, 128, kSboA), smem_desc(ba, 128, 256), d > 0 ? 1u : 0u);
+                    for (int k = 0; k < kSrcSites; ++k) {
+                        // the first run of a row starts every site with sources 2, 5, 8 (disjoint
+                        // groups covering the row), then accumulates; later runs accumulate
+                        const int t = dyi == 0 ? (k < 3 ? 2 + 3 * k : (k < 5 ? k - 3 : (k < 7 ? k - 2 : (k < 9 ? k - 1 : 9)))) : k;
+                        const SrcGroup g = src_group(t);
+                        const uint32_t accumulate = (dyi == 0 && k < 3) ? 0u : 1u;
+                        mma_bf16(acc + (uint32_t)(32 * g.first), smem_desc(arow + (uint32_t)(t * kTileA), 128, kSboA),
+                                 smem_desc(unit + (uint32_t)g.run_off, 128, 256), idesc_bf16(32u * (uint32_t)g.count),
+                                 accumulate);
                     }
-                    mma_commit(bar(kBarLinkEmpty + ls));
-                    mma_commit(bar(kBarAccFull + as));
+                    mma_commit(bar(kBarUnitEmpty + slot));  // this run of links is not read again
                 }
                 if (!ok) break;
+                mma_commit(bar(kBarAccFull + (r & 1)));
                 mma_commit(bar(kBarSrcEmpty + r % kRing));  // source row r is not read again
             }
             // all MMAs of this CTA have completed before tensor memory is freed
@@ -312,42 +350,65 @@ __global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
 #pragma unroll
         for (int k = 0; k < K; ++k) v[k] = 0.0;
         const int64_t rstride = 2ll * nrhs;  // floats between consecutive dofs
-        for (int seq = 0; seq < nseq; ++seq) {
-            const int as = seq % kAccSlots;
-            bool ok = wait_bar(bar(kBarAccFull + as), (seq / kAccSlots) & 1, abort_flag);
+        const float* __restrict__ wbase = reinterpret_cast<const float*>(a.w);
+        float* __restrict__ ybase = reinterpret_cast<float*>(a.y);
+        for (int r = 0; r < H; ++r) {
+            const int64_t row0 = ((int64_t)x0 + (int64_t)nx * (y0 + r)) * kNc * nrhs + rhs0 + rhs;  // site x0
+            // EPI 2: w of the first kPre sites is requested before the accumulators are ready and
+            // each later site's w kPre sites ahead, so the L2 latency overlaps the epilogue work
+            constexpr int kPre = 4;
+            float wb[kPre][kNc];
+            if (EPI == 2) {
+#pragma unroll
+                for (int q = 0; q < kPre; ++q)
+#pragma unroll
+                    for (int k = 0; k < kNc; ++k)
+                        wb[q][k] = __ldcg(wbase + (row0 + (int64_t)q * kNc * nrhs) * 2 + c + k * rstride);
+            }
+            bool ok = wait_bar(bar(kBarAccFull + (r & 1)), (r >> 1) & 1, abort_flag);
             if (!__all_sync(0xffffffffu, ok)) break;
             tc_fence_after();
-            float d[32];
-            tmem_ld32(tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)(as * 32), d);
-            tc_fence_before();
-            mbar_arrive(bar(kBarAccEmpty + as));
-            const int r = seq / kW, i = seq - r * kW;
-            const int64_t site = (int64_t)(x0 + i) + (int64_t)nx * (y0 + r);
-            const int64_t base = (site * kNc * nrhs + rhs0 + rhs) * 2 + c;
-            float* yp = reinterpret_cast<float*>(a.y) + base;
-            float s0 = 0.f, s1 = 0.f, s2 = 0.f;
 #pragma unroll
-            for (int k = 0; k < kNc; ++k) {
-                const float other = __shfl_xor_sync(0xffffffffu, d[16 + k], 1);
-                const float o = c == 0 ? d[k] - other : d[k] + other;
-                yp[k * rstride] = o;
+            for (int i = 0; i < kW; ++i) {
+                float d[32];
+                tmem_ld32(tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)((r & 1) * kAccCols + 32 * i), d);
+                const int64_t base = (row0 + (int64_t)i * kNc * nrhs) * 2 + c;
+                float o[kNc];
+#pragma unroll
+                for (int k = 0; k < kNc; ++k) {
+                    const float other = __shfl_xor_sync(0xffffffffu, d[16 + k], 1);
+                    o[k] = c == 0 ? d[k] - other : d[k] + other;
+                }
+                float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+#pragma unroll
+                for (int k = 0; k < kNc; ++k) {
+                    if (EPI == 1) {
+                        s0 += o[k] * o[k];
+                    } else if (EPI == 2) {
+                        const float wc = wb[i % kPre][k];
+                        const float wo = __shfl_xor_sync(0xffffffffu, wc, 1);
+                        s0 += o[k] * wc;                     // Re <y, w>: yr wr + yi wi
+                        s1 += c == 0 ? o[k] * wo : -o[k] * wo;  // Im <y, w>: yr wi - yi wr
+                        s2 += o[k] * o[k];
+                    }
+                }
+                if (EPI == 2 && i + kPre < kW) {
+#pragma unroll
+                    for (int k = 0; k < kNc; ++k)
+                        wb[i % kPre][k] = __ldcg(wbase + base + (int64_t)kPre * kNc * nrhs * 2 + k * rstride);
+                }
+#pragma unroll
+                for (int k = 0; k < kNc; ++k) ybase[base + k * rstride] = o[k];
                 if (EPI == 1) {
-                    s0 += o * o;
+                    v[0] += (double)s0;
                 } else if (EPI == 2) {
-                    const float wc = reinterpret_cast<const float*>(a.w)[base + k * rstride];
-                    const float wo = __shfl_xor_sync(0xffffffffu, wc, 1);
-                    s0 += o * wc;                     // Re <y, w>: yr wr + yi wi
-                    s1 += c == 0 ? o * wo : -o * wo;  // Im <y, w>: yr wi - yi wr
-                    s2 += o * o;
+                    v[0] += (double)s0;
+                    v[1] += (double)s1;
+                    v[K - 1] += (double)s2;
                 }
             }
-            if (EPI == 1) {
-                v[0] += (double)s0;
-            } else if (EPI == 2) {
-                v[0] += (double)s0;
-                v[1] += (double)s1;
-                v[K - 1] += (double)s2;
-            }
+            tc_fence_before();
+            mbar_arrive(bar(kBarAccEmpty + (r & 1)));
         }
         if (EPI != 0) {
 #pragma unroll
@@ -417,14 +478,29 @@ __global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
         if (tid == 0) s_last = atomicAdd(a.tickets + blockIdx.z, 1u) == (unsigned)(nblk - 1) ? 1 : 0;
         __syncthreads();
         if (s_last) {
+            // each warp sums four (rhs, k) pairs at a time, lanes striding over the CTAs, so many
+            // independent loads are in flight; the order is fixed (deterministic)
             __threadfence();
-            if (tid < kRhsTile) {
+            constexpr int kPairs = kRhsTile * K;
+            for (int p0 = warp * 4; p0 < kPairs; p0 += 4 * 8) {
+                double acc[4] = {0.0, 0.0, 0.0, 0.0};
+                const double* src[4];
 #pragma unroll
-                for (int k = 0; k < K; ++k) {
-                    const double* src = a.partials + ((int64_t)(rhs0 + tid) * K + k) * nblk;
-                    double sum = 0.0;
-                    for (int b = 0; b < nblk; ++b) sum += __ldcg(src + b);
-                    a.out[(rhs0 + tid) * K + k] = sum;
+                for (int q = 0; q < 4; ++q) {
+                    const int pq = p0 + q < kPairs ? p0 + q : kPairs - 1;
+                    src[q] = a.partials + ((int64_t)(rhs0 + pq / K) * K + pq % K) * nblk;
+                }
+#pragma unroll 4
+                for (int b = lane; b < nblk; b += 32) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) acc[q] += __ldcg(src[q] + b);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    double v = acc[q];
+                    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    if (lane == 0 && p0 + q < kPairs)
+                        a.out[(rhs0 + (p0 + q) / K) * K + (p0 + q) % K] = v;
                 }
             }
             if (tid == 0) a.tickets[blockIdx.z] = 0u;
@@ -433,14 +509,19 @@ __global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
 }
 
 // B operands of every (site, direction): row n = c * 16 + i, K index j,
-// value Re / Im of L[s][d](i, j) (stored [s][d][j][i]), rounded to BF16.
-// One thread writes one 16-byte core-matrix row (8 consecutive j).
-__global__ void k_tile_links(const cx<double>* __restrict__ A, int64_t nsites, uint8_t* __restrict__ out) {
+// value Re / Im of L[s][d](i, j) (stored [s][d][j][i]), rounded to BF16, in
+// the run order of the source grouping: output row y, source row offset dy,
+// position P = 3x + 4 + 2dx (mod 3 nx).  One thread writes one 16-byte
+// core-matrix row (8 consecutive j).
+__global__ void k_tile_links(const cx<double>* __restrict__ A, int nx, int64_t nsites, uint8_t* __restrict__ out) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nsites * 9 * 32 * 2) return;
     const int g = (int)(t & 1);
     const int n = (int)((t >> 1) & 31);
     const int64_t sd = t >> 6;  // site * 9 + d
+    const int64_t site = sd / 9;
+    const int d = (int)(sd - site * 9);
+    const int x = (int)(site % nx), y = (int)(site / nx);
     const int cpart = n >> 4, i = n & 15;
     const cx<double>* blk = A + sd * kNc * kNc;
     float f[8];
@@ -454,7 +535,10 @@ __global__ void k_tile_links(const cx<double>* __restrict__ A, int64_t nsites, u
     v.y = pack_bf16(f[2], f[3]);
     v.z = pack_bf16(f[4], f[5]);
     v.w = pack_bf16(f[6], f[7]);
-    *reinterpret_cast<uint4*>(out + sd * kLinkDir + (n >> 3) * 256 + g * 128 + (n & 7) * 16) = v;
+    const int ring3 = 3 * nx;
+    const int P = (3 * x + 4 + 2 * dir_dx(d)) % ring3;
+    const int64_t block = ((int64_t)y * 3 + dir_dy(d) + 1) * ring3 + P;
+    *reinterpret_cast<uint4*>(out + block * kLinkDir + (n >> 3) * 256 + g * 128 + (n & 7) * 16) = v;
 }
 
 int rows_per_cta(int nx, int ny, int nz) {
@@ -469,9 +553,9 @@ bool smg_coarse_tc_shape_ok(int nx, int ny, int ndof) { return ndof == kNc && nx
 
 size_t smg_coarse_tc_link_bytes(int64_t nsites) { return (size_t)nsites * kLinkSite; }
 
-smg_status smg_coarse_tc_tile_links(smg_context* ctx, const cx<double>* A64, int64_t nsites, void* out) {
+smg_status smg_coarse_tc_tile_links(smg_context* ctx, const cx<double>* A64, int nx, int64_t nsites, void* out) {
     const int64_t n = nsites * 9 * 32 * 2;
-    k_tile_links<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(A64, nsites, static_cast<uint8_t*>(out));
+    k_tile_links<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(A64, nx, nsites, static_cast<uint8_t*>(out));
     count_launch(ctx);
     SMG_CHECK_LAUNCH(ctx);
     // the apply kernels need more than the default 48 KB of dynamic shared memory

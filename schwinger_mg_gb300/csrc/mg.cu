@@ -36,7 +36,7 @@ smg_status smg_dslash_mr(smg_dirac* d, bool dag, const smg_field* src, smg_field
 // tensor-core coarse apply (coarse_tc.cu)
 bool smg_coarse_tc_shape_ok(int nx, int ny, int ndof);
 size_t smg_coarse_tc_link_bytes(int64_t nsites);
-smg_status smg_coarse_tc_tile_links(smg_context* ctx, const cx<double>* A64, int64_t nsites, void* out);
+smg_status smg_coarse_tc_tile_links(smg_context* ctx, const cx<double>* A64, int nx, int64_t nsites, void* out);
 smg_status smg_coarse_tc_apply(smg_context* ctx, const void* links, int nx, int ny, int nrhs, const cx<float>* x,
                                cx<float>* y, int epi, const cx<float>* w, double* out, const int* gate, int* err);
 
@@ -885,14 +885,17 @@ __global__ void __launch_bounds__(256) k_ccg_update(CcgState s, VecView<T> x, cx
     __syncthreads();
     const T al = s_al[threadIdx.x];
     T v[1] = {T(0)};
+    cx<T>* __restrict__ xp = x.p;
     if (rhs < nrhs) {
+        const int ds = x.dstride();
+#pragma unroll 2
         for (int st = blockIdx.x * blockDim.y + threadIdx.y; st < x.nsites; st += gridDim.x * blockDim.y) {
             const int64_t base = x.idx(st, rhs, 0);
-            const int ds = x.dstride();
             for (int d = 0; d < x.ndof; ++d) {
-                const cx<T> ri = r[base + (int64_t)d * ds] - al * Ap[base + (int64_t)d * ds];
-                x.p[base + (int64_t)d * ds] = x.p[base + (int64_t)d * ds] + al * p[base + (int64_t)d * ds];
-                r[base + (int64_t)d * ds] = ri;
+                const int64_t e = base + (int64_t)d * ds;
+                const cx<T> ri = r[e] - al * Ap[e];
+                xp[e] = xp[e] + al * p[e];
+                r[e] = ri;
                 v[0] += norm2(ri);
             }
         }
@@ -1601,7 +1604,7 @@ smg_status make_f32_copies(smg_mg* mg) {
             count_launch(ctx);
             if (mg->p.precision == SMG_F32 && mg->p.tensor_cores && smg_coarse_tc_shape_ok(L.nx, L.ny, L.ndof)) {
                 if (!L.Atc) SMG_CUDA(ctx, cudaMalloc(&L.Atc, smg_coarse_tc_link_bytes(L.nsites)));
-                SMG_TRY(smg_coarse_tc_tile_links(ctx, L.A64, L.nsites, L.Atc));
+                SMG_TRY(smg_coarse_tc_tile_links(ctx, L.A64, L.nx, L.nsites, L.Atc));
             }
         }
     }

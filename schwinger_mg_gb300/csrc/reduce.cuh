@@ -112,7 +112,8 @@ __device__ __forceinline__ void block_reduce_finalise(float (&v)[K], double* __r
 }
 
 // Launch shape for reducing kernels: lanes is a power of two <= 32, at most
-// kMaxReduceBlocks blocks along x (kernels stride over the remaining sites).
+// kReduceResidentBlocks blocks in all (kernels stride over the remaining sites).
+constexpr int kReduceResidentBlocks = 152 * 4;
 struct ReduceLaunch {
     dim3 grid, block;
     int lanes, rows;
@@ -123,10 +124,14 @@ inline ReduceLaunch reduce_launch(int nsites, int nrhs) {
     while (lanes * 2 <= nrhs && lanes < 32) lanes *= 2;
     s.lanes = lanes;
     s.rows = kReduceMaxThreads / lanes;
+    const int by = (nrhs + lanes - 1) / lanes;
+    // every block resident at once: the reducing kernels use 40-64 registers, so 4 blocks of
+    // 256 threads per SM; more blocks would run as a second, partial wave
+    const int cap = kReduceResidentBlocks / by > 0 ? kReduceResidentBlocks / by : 1;
     int bx = (nsites + s.rows - 1) / s.rows;
-    if (bx > kMaxReduceBlocks) bx = kMaxReduceBlocks;
+    if (bx > cap) bx = cap;
     if (bx < 1) bx = 1;
     s.block = dim3(lanes, s.rows, 1);
-    s.grid = dim3(bx, (nrhs + lanes - 1) / lanes, 1);
+    s.grid = dim3(bx, by, 1);
     return s;
 }
