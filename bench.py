@@ -146,6 +146,50 @@ def dslash_bytes_f64_single(L):
     return L * L * 104
 
 
+def kernel_trace(step, ctx, path: str, what: str) -> None:
+    """One extra step under the CUPTI kernel tracer (schwinger_mg_gb300/profiling/kernel_trace.cpp):
+    launches, device time and share per kernel, written as a table to `path`."""
+    import shutil
+
+    so = ROOT / "schwinger_mg_gb300" / "libsmg_ktrace.so"
+    if not so.exists():
+        from schwinger_mg_gb300.build import build_kernel_trace
+
+        if build_kernel_trace() is None:
+            raise RuntimeError("--kernel-trace needs CUPTI")
+    kt = Cc.CDLL(str(so))
+    ctx.synchronize()
+    if kt.smg_ktrace_start() != 0:
+        raise RuntimeError("CUPTI activity tracing could not start")
+    step()
+    ctx.synchronize()
+    raw = path + ".raw"
+    kt.smg_ktrace_stop(raw.encode())
+    lines = Path(raw).read_text().splitlines()
+    span = float(lines[0].split()[2])
+    rows = [l.split(" ", 2) for l in lines[1:]]
+    names = [r[2] for r in rows]
+    if shutil.which("c++filt"):
+        names = subprocess.run(["c++filt"], input="\n".join(names), capture_output=True, text=True).stdout.splitlines()
+    agg = {}
+    for r, nm in zip(rows, names):
+        nm = nm.replace("(anonymous namespace)::", "")
+        key = nm.split("(")[0] if "<" not in nm.split("(")[0] else nm[: nm.find(">(") + 1] if ">(" in nm else nm
+        n, t = agg.get(key, (0, 0.0))
+        agg[key] = (n + int(r[0]), t + float(r[1]))
+    tot = sum(t for _, t in agg.values())
+    out = [f"# CUPTI kernel trace: {what}", f"# kernel time {tot / 1e6:.2f} ms, span {span / 1e6:.2f} ms", "",
+           "| launches | total ms | avg us | share | kernel |", "|---:|---:|---:|---:|---|"]
+    for k, (n, t) in sorted(agg.items(), key=lambda kv: -kv[1][1]):
+        out.append(f"| {n} | {t / 1e6:.2f} | {t / n / 1e3:.1f} | {100 * t / tot:.1f}% | `{k}` |")
+    Path(path).write_text("\n".join(out) + "\n")
+
+
+# DRAM read + write bytes of one level-1 tensor-core coarse apply at L = 512, 32 RHS, from one ncu capture
+# (profiles/coarse_apply_tc_L512_level1_32rhs.md)
+TC_LEVEL1_L512_DRAM_BYTES = 226.540288e6 + 42.035968e6
+
+
 def sized(base: dict, args) -> dict:
     """A workload's configuration with the --L / --nrhs overrides (smaller cases for profiles)."""
     c = dict(base)
@@ -221,6 +265,9 @@ def run_ours(args, ws, rank, local):
             ms = timed(step, args.steps)
         launches = ctx.kernel_launches - l0
         iters, true_res = res.iterations, res.true_residual
+        if args.kernel_trace and rank == 0:
+            kernel_trace(step, ctx, args.kernel_trace, f"one step of the mg workload (L={L}, {nrhs} RHS, "
+                                                       f"{iters} GCR iterations)")
         value = ws * nrhs / (ms * 1e-3)
 
         # end to end through the C ABI: pinned host rhs in, solve, solutions out
@@ -272,7 +319,8 @@ def run_ours(args, ws, rank, local):
             "e2e": {"value": ws * nrhs / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": hb,
                     "d2h_bytes_per_step": hb, "ms_per_step": e2e_ms, "finite": bool(np.isfinite(sol).all())},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "kernel": coarse_kernel_name(c, L, nrhs),
+                         "traffic": TC_LEVEL1_L512_DRAM_BYTES if (L, nrhs) == (512, 32) else None,
+                         "traffic_unit": "bytes per launch (ncu)", "kernel": coarse_kernel_name(c, L, nrhs),
                          "bytes_per_launch": cbytes.value, "ms_per_launch": cms.value, "peak_source": peak_kind},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
@@ -296,8 +344,8 @@ def run_ours(args, ws, rank, local):
             step()
         l0 = ctx.kernel_launches
         with Clocks(local) as clk:
-            ms = timed(step, max(args.steps, 2000))
-        launches = (ctx.kernel_launches - l0) * args.steps // max(args.steps, 2000)
+            ms = timed(step, max(args.steps, 500))
+        launches = (ctx.kernel_launches - l0) * args.steps // max(args.steps, 500)
         value = ws * bytes_step / (ms * 1e-3) / 1e9
         achieved = bytes_step / (ms * 1e-3) / 1e9
         host_in = torch.empty(srcs.size * 2, dtype=torch.float64).pin_memory()
@@ -318,11 +366,13 @@ def run_ours(args, ws, rank, local):
             "config": {"workload": f"FP32 Wilson-clover D on {nrhs} RHS, L={L} (beta=6, m=-0.05, c_sw=1)",
                        "L": L, "nrhs": nrhs, "bytes_per_step": bytes_step,
                        "l2": "inputs and outputs (268 MB) exceed the 129 MB L2; no flush",
-                       "timed_steps": max(args.steps, 2000)},
+                       "timed_steps": max(args.steps, 500)},
             "e2e": {"value": ws * bytes_step / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
                     "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb, "ms_per_step": e2e_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "kernel": "k_dslash<float,false,0>", "peak_source": peak_kind},
+                         "traffic": (140.034304e6 + 99.262464e6) if (L, nrhs) == (512, 32) else None,
+                         "traffic_unit": "bytes per launch (ncu, profiles/dslash_f32_L512_32rhs.md)",
+                         "kernel": "k_dslash<float,false,0>", "peak_source": peak_kind},
             "gpu_launches": int(launches), "clocks": clk.summary(),
         })
     elif args.workload == "coarse":
@@ -350,7 +400,9 @@ def run_ours(args, ws, rank, local):
                        "l2": "links and vectors exceed the 129 MB L2 at L=512; no flush"},
             "e2e": None,
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
-                         "traffic": None, "kernel": coarse_kernel_name(c, L, nrhs), "peak_source": peak_kind},
+                         "traffic": TC_LEVEL1_L512_DRAM_BYTES if (L, nrhs) == (512, 32) else None,
+                         "traffic_unit": "bytes per launch (ncu)", "kernel": coarse_kernel_name(c, L, nrhs),
+                         "bytes_per_launch": cbytes.value, "peak_source": peak_kind},
             "gpu_launches": int(launches), "clocks": clk.summary(),
         })
     else:
@@ -429,11 +481,12 @@ def cpu_baseline(workload: str, threads: int | None = None, ctx_objects=None):
         L, nrhs = c["L"], 8
         U = smg.gauge_normal(L, c["beta"], c["seed"])
         srcs = np.stack([smg.random_vec(2 * L * L, c["seed"] + 1 + j) for j in range(nrhs)])
-        port.time_dirac(U, c["m"], c["r"], c["csw"], c["mu"], 0, srcs[:1], 1)
-        t, _ = port.time_dirac(U, c["m"], c["r"], c["csw"], c["mu"], 0, srcs, 2)
-        gbs = 2 * nrhs * dslash_bytes_f64_single(L) / t / 1e9
+        t1, _ = port.time_dirac(U, c["m"], c["r"], c["csw"], c["mu"], 0, srcs[:1], 1)
+        reps = max(2, int(10.0 / max(t1 * nrhs, 1e-6)))  # about 10 s of CPU work
+        t, _ = port.time_dirac(U, c["m"], c["r"], c["csw"], c["mu"], 0, srcs, reps)
+        gbs = reps * nrhs * dslash_bytes_f64_single(L) / t / 1e9
         return {"value": gbs, "unit": "GB/s", "cores": n_threads, "kind": "port",
-                "sample": f"FP64 D on {nrhs} RHS x 2 reps at L={L} (the reference computes one RHS at a time "
+                "sample": f"FP64 D on {nrhs} RHS x {reps} reps at L={L} (the reference computes one RHS at a time "
                           "in FP64; 104 B/site per application)", "seconds": t}
     c = CG
     U = smg.gauge_normal(c["L"], c["beta"], c["seed"])
@@ -483,6 +536,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--L", type=int, default=0, help="lattice size override (smaller cases for profiles)")
     ap.add_argument("--nrhs", type=int, default=0, help="right-hand-side count override")
+    ap.add_argument("--kernel-trace", default="", help="mg workload: write a CUPTI per-kernel summary of one extra "
+                                                         "(untimed) step to this path")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_env()

@@ -18,6 +18,8 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libsmg_gpu.so"
+KTRACE_SRC = PKG / "profiling" / "kernel_trace.cpp"
+KTRACE_LIB = PKG / "libsmg_ktrace.so"
 INCLUDE = PKG.parent / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -80,6 +82,32 @@ def build_library(verbose: bool = False, ptxas_verbose: bool = False) -> Path:
     return LIB
 
 
+def _cuda_root() -> Path:
+    return Path(_nvcc()).resolve().parent.parent
+
+
+def build_kernel_trace(verbose: bool = False) -> Path | None:
+    """The optional CUPTI kernel tracer (libsmg_ktrace.so) used by the benchmark's
+    --kernel-trace; returns None when CUPTI is not available."""
+    if KTRACE_LIB.exists() and KTRACE_LIB.stat().st_mtime >= KTRACE_SRC.stat().st_mtime:
+        return KTRACE_LIB
+    root = _cuda_root()
+    incs = [root / "include", *root.glob("targets/*/include"), root / "extras" / "CUPTI" / "include"]
+    libs = [root / "lib64", *root.glob("targets/*/lib"), root / "extras" / "CUPTI" / "lib64"]
+    if not any((i / "cupti.h").exists() for i in incs):
+        return None
+    cmd = ["g++", "-O2", "-std=c++17", "-shared", "-fPIC", *[f"-I{i}" for i in incs if i.exists()], str(KTRACE_SRC),
+           *[f"-L{d}" for d in libs if d.exists()], "-lcupti", "-o", str(KTRACE_LIB)]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        print(f"kernel tracer not built (CUPTI): {r.stderr.strip()[:200]}", file=sys.stderr)
+        return None
+    return KTRACE_LIB
+
+
 if __name__ == "__main__":
     p = build_library(verbose=True, ptxas_verbose="-v" in sys.argv)
     print(p)
+    print(build_kernel_trace(verbose=True))
