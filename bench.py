@@ -1,6 +1,6 @@
 """Benchmark of the Wilson-clover Dirac operator and its MG solve path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload mg|dslash|cg|coarse] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload mg|dslash|cg|coarse|hmc] [--impl ours|reference]
 
 Prints ONE JSON line (rank 0).  A step is one pass of the hot path over one
 batch of seeded synthetic input (links U = exp(i theta), theta ~ N(0, 1/beta);
@@ -19,6 +19,10 @@ is reported.  Workloads:
 * coarse — the level-1 coarse operator of the mg workload alone (128 x 128
   sites, 16 dofs, 32 RHS); value = algorithmic GB/s.  A small case for
   kernel profiles.
+* hmc — differentiated HMC at L = 128 (beta = 4, m = 0.1, c_sw = 1): nested
+  Omelyan with 10 fermion-force steps and 4 gauge-force substeps per inner
+  integration, mixed-precision solves to 1e-10, 20 trajectories;
+  value = trajectories/s, with dH, acceptance and plaquette in config.
 * cg — the small single-RHS case (L = 32, beta = 2, m = 0.1, c_sw = 1) FP64 CG;
   value = solves/s.
 
@@ -132,6 +136,8 @@ MG = dict(L=512, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20240, nrhs=32,
           max_iter=500, trunc=20)
 DSLASH = dict(L=512, nrhs=32, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20240)
 CG = dict(L=32, beta=2.0, m=0.1, r=1.0, csw=1.0, mu=0.0, seed=31, tol=1e-10, max_iter=10000)
+HMC = dict(L=128, beta=4.0, m=0.1, r=1.0, csw=1.0, seed=2024, rng_seed=4048, tau=1.0, n_outer=10, n_inner=4,
+           tol=1e-10, n_traj=20)
 
 
 def dslash_bytes_f32(L, nrhs):
@@ -375,6 +381,49 @@ def run_ours(args, ws, rank, local):
                          "kernel": "k_dslash<float,false,0>", "peak_source": peak_kind},
             "gpu_launches": int(launches), "clocks": clk.summary(),
         })
+    elif args.workload == "hmc":
+        # differentiated HMC: nested Omelyan (fermion force outside, gauge force inside), mixed solves
+        c = sized(HMC, args)
+        L = c["L"]
+        U = smg.gauge_normal(L, c["beta"], c["seed"])
+        lat = smg.Lattice(L)
+        g = smg.GaugeField(lat, U, ctx)
+        p = smg.hmc_params(c["beta"], tau=c["tau"], n_steps=c["n_outer"], omelyan=True, n_inner=c["n_inner"],
+                           cg_tol=c["tol"], c_sw=c["csw"], mixed_precision=True)
+        rng = smg.Rng(c["rng_seed"])
+        results = []
+
+        def step():
+            results.append(smg.hmc_trajectory(g, c["m"], c["r"], p, rng))
+
+        for _ in range(args.warmup):
+            step()
+        n_timed = max(args.steps, c["n_traj"] - args.warmup)
+        l0 = ctx.kernel_launches
+        with Clocks(local) as clk:
+            ms = timed(step, n_timed)
+        launches = (ctx.kernel_launches - l0) * args.steps // n_timed
+        acc = [r.accepted for r in results]
+        out.update({
+            "value": ws * 1e3 / ms, "unit": "trajectories/s", "ms_per_step": ms, "higher_is_better": True,
+            "dtype": "f64+f32",
+            "config": {"workload": f"HMC, L={L} (beta={c['beta']}, m={c['m']}, c_sw={c['csw']}), two flavours, "
+                                   f"tau={c['tau']}, nested Omelyan: {c['n_outer']} fermion-force steps, "
+                                   f"{c['n_inner']} gauge-force substeps per inner integration, "
+                                   "mixed-precision CG to a true FP64 residual of 1e-10",
+                       "trajectories": len(results), "timed_trajectories": n_timed,
+                       "acceptance": float(np.mean(acc)),
+                       "dH": [round(r.dH, 6) for r in results],
+                       "mean_exp_minus_dH": float(np.mean([np.exp(-r.dH) for r in results])),
+                       "plaquette": [round(r.plaquette, 6) for r in results],
+                       "solves_per_trajectory": results[-1].solves,
+                       "cg_iterations_per_trajectory": float(np.mean([r.total_cg_iters for r in results])),
+                       "l2": "gauge, momenta and fields (a few MB) are L2-resident; no flush"},
+            "e2e": {"value": ws * 1e3 / ms, "unit": "trajectories/s", "h2d_bytes_per_step": 12 * lat.V * 8,
+                    "d2h_bytes_per_step": 0, "ms_per_step": ms,
+                    "note": "the trajectory runs through the C ABI; its host inputs (momenta, eta) are copied in"},
+            "gpu_launches": int(launches), "clocks": clk.summary(),
+        })
     elif args.workload == "coarse":
         # the level-1 coarse operator alone: (L/4)^2 sites, 16 dofs, 32 RHS, 9-point stencil
         c = sized(MG, args)
@@ -488,6 +537,23 @@ def cpu_baseline(workload: str, threads: int | None = None, ctx_objects=None):
         return {"value": gbs, "unit": "GB/s", "cores": n_threads, "kind": "port",
                 "sample": f"FP64 D on {nrhs} RHS x {reps} reps at L={L} (the reference computes one RHS at a time "
                           "in FP64; 104 B/site per application)", "seconds": t}
+    if workload == "hmc":
+        # one fermion-force evaluation (CG to 1e-10 + force) and one gauge force on the CPU; a nested
+        # Omelyan trajectory makes 2 n_outer + 1 of them plus the two Hamiltonian solves
+        c = HMC
+        L = c["L"]
+        U = smg.gauge_normal(L, c["beta"], c["seed"]).reshape(-1)
+        phi = smg.random_vec(2 * L * L, c["seed"] + 7)
+        t0 = time.perf_counter()
+        X, it, _ = port.cg(U, c["m"], c["r"], c["csw"], 0.0, phi, 100000, c["tol"])
+        port.fermion_force(U, c["m"], c["r"], c["csw"], 0.0, X)
+        port.gauge_force(U, c["beta"])
+        t_force = time.perf_counter() - t0
+        n_solves = 2 * c["n_outer"] + 3
+        return {"value": 1.0 / (n_solves * t_force), "unit": "trajectories/s", "cores": n_threads, "kind": "port",
+                "sample": f"one force evaluation at L={L} (FP64 CG, {it} iterations, to 1e-10, fermion + gauge "
+                          f"force) in {t_force:.2f} s, times the {n_solves} solves of one trajectory",
+                "seconds": t_force}
     c = CG
     U = smg.gauge_normal(c["L"], c["beta"], c["seed"])
     b = smg.random_vec(2 * c["L"] ** 2, c["seed"] + 1)
@@ -531,7 +597,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="mg", choices=["mg", "dslash", "cg", "coarse"])
+    ap.add_argument("--workload", default="mg", choices=["mg", "dslash", "cg", "coarse", "hmc"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--L", type=int, default=0, help="lattice size override (smaller cases for profiles)")

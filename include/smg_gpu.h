@@ -207,6 +207,12 @@ SMG_API smg_status smg_blas_dot_noalloc(const double* a, const double* b, int64_
  * independently and stops on its own. */
 SMG_API smg_status smg_cg_solve(smg_dirac* d, const smg_field* rhs, smg_field* x,
                                 int max_iter, double tol, smg_solve_result* res);
+/* The same solve to a true FP64 residual below tol with FP32 CG inside FP64
+ * defect correction: each outer step solves A e = r/||r|| with the FP32
+ * operator and adds x += ||r|| e.  F64 fields only; iterations count the
+ * FP32 CG iterations. */
+SMG_API smg_status smg_cg_solve_mixed(smg_dirac* d, const smg_field* rhs, smg_field* x,
+                                      int max_iter, double tol, smg_solve_result* res);
 
 /* -------------------------------------------------------------- multigrid */
 
@@ -317,6 +323,66 @@ SMG_API smg_status smg_gcr_solve(smg_dirac* d, smg_mg* mg, const smg_field* rhs,
  * -dS/dtheta_mu(s) for S = phi^dag (D^dag D)^-1 phi, X = (D^dag D)^-1 phi.
  * X is a single-RHS F64 field; force is 2*V doubles on the host. */
 SMG_API smg_status smg_fermion_force(smg_dirac* d, const smg_field* X, double* force);
+
+/* --------------------------------------------------------------------- HMC */
+
+/* The reference's std::mt19937 passed through an HMC run (momenta, the
+ * pseudofermion's eta and the Metropolis draw come from it in the reference's
+ * order). */
+typedef struct smg_rng smg_rng;
+SMG_API smg_status smg_rng_create(uint32_t seed, smg_rng** out);
+SMG_API smg_status smg_rng_destroy(smg_rng* rng);
+/* std::uniform_real_distribution<double>(0, 1) draw, as the accept step. */
+SMG_API smg_status smg_rng_uniform(smg_rng* rng, double* out);
+/* n draws of one std::normal_distribution<double>(0, 1) object, as
+ * MomentumField::randomise and random_vec make them. */
+SMG_API smg_status smg_rng_normal(smg_rng* rng, int64_t n, double* out);
+
+/* HMCParams (reference src/hmc.h:107-119) plus the nested multi-timescale
+ * integrator of hmc_trajectory_mg_multiscale (src/hmc_multiscale.cpp:660-710)
+ * with the gauge force as its cheap inner force:
+ *   n_inner = 0: hmc_trajectory's integrator (src/hmc_trajectory.cpp:243-409),
+ *                leapfrog or Omelyan (lambda = 0.1932) over gauge + fermion
+ *                forces with n_steps steps of tau / n_steps;
+ *   n_inner > 0: the fermion force drives the outer integrator (n_steps
+ *                steps, leapfrog or Omelyan) and every outer momentum kick is
+ *                separated by an inner leapfrog of n_inner steps on the gauge
+ *                force alone.
+ * mixed_precision selects smg_cg_solve_mixed for every solve (otherwise FP64
+ * CG). */
+typedef struct {
+    double beta;
+    double tau;
+    int n_steps;
+    int omelyan;
+    int n_inner;
+    int cg_maxiter;
+    double cg_tol;
+    double c_sw;
+    double mu_t;
+    int force_accept;
+    int mixed_precision;
+} smg_hmc_params;
+
+/* HMCResult (reference src/hmc.h:121-129) plus the plaquette after the
+ * trajectory (accepted or restored) and the number of solves. */
+typedef struct {
+    int accepted;
+    double dH, dKE, dSG, dSF;
+    int total_cg_iters;
+    int solves;
+    double plaquette;
+} smg_hmc_result;
+
+SMG_API smg_status smg_hmc_params_default(smg_hmc_params* p);
+/* hmc_trajectory (reference src/hmc_trajectory.cpp:38-235, full-lattice
+ * path): momenta pi ~ N(0,1) from rng, phi = D^dag eta with eta = random_vec,
+ * H = KE + S_G + S_F with S_F = Re <phi, (D^dag D)^-1 phi>, molecular
+ * dynamics with the device forces, Metropolis with rng; a rejected
+ * trajectory restores the links.  The gauge handle is updated in place;
+ * gauge, momenta, forces and fields stay on the device. */
+SMG_API smg_status smg_hmc_trajectory(smg_gauge* g, double mass, double wilson_r, const smg_hmc_params* p,
+                                      smg_rng* rng, smg_hmc_result* res);
 
 /* -------------------------------------------------------- host utilities */
 

@@ -362,6 +362,18 @@ class Ref(_Lib):
                                  C.c_int(max_iter), C.c_double(tol), C.c_int(trunc), C.byref(res))
         return x, it, res.value
 
+    def hmc_trajectories(self, U, m, r, beta, tau, n_steps, omelyan, cg_maxiter, cg_tol, csw, mu, force_accept,
+                         seed, n_traj):
+        """The reference's hmc_trajectory n_traj times with one std::mt19937(seed); returns the
+        final links and per trajectory (accepted, dH, dKE, dSG, dSF, cg iterations, plaquette)."""
+        U = _c(U).copy()
+        out = np.zeros(8 * n_traj)
+        self.lib.ref_hmc_trajectories(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(beta),
+                                      C.c_double(tau), C.c_int(n_steps), C.c_int(omelyan), C.c_int(cg_maxiter),
+                                      C.c_double(cg_tol), C.c_double(csw), C.c_double(mu), C.c_int(force_accept),
+                                      C.c_uint(seed), C.c_int(n_traj), _p(out))
+        return U, out.reshape(n_traj, 8)[:, :7]
+
     def pseudofermion(self, U, m, r, csw, mu, seed):
         U = _c(U)
         L = self._L(U)

@@ -310,4 +310,45 @@ void ref_pseudofermion(int L, const double* U, double m, double r, double csw, d
     from_vec(p, phi);
 }
 
+
+// hmc_trajectory (src/hmc_trajectory.cpp:38-235, full-lattice path, no
+// preconditioner, no tracking) for n_traj trajectories threading one
+// std::mt19937(seed).  U (2V complex) is updated in place; per trajectory
+// out[8 t + {0..6}] = accepted, dH, dKE, dSG, dSF, total CG iterations,
+// average plaquette after the trajectory.
+void ref_hmc_trajectories(int L, double* U, double mass, double r, double beta, double tau, int n_steps,
+                          int omelyan, int cg_maxiter, double cg_tol, double c_sw, double mu_t, int force_accept,
+                          unsigned seed, int n_traj, double* out) {
+    World w(L, U);
+    HMCParams hp{};
+    hp.beta = beta;
+    hp.tau = tau;
+    hp.n_steps = n_steps;
+    hp.cg_maxiter = cg_maxiter;
+    hp.cg_tol = cg_tol;
+    hp.use_mg = false;
+    hp.c_sw = c_sw;
+    hp.mu_t = mu_t;
+    hp.use_eo = false;
+    hp.omelyan = omelyan != 0;
+    hp.force_accept = force_accept != 0;
+    std::mt19937 rng(seed);
+    for (int t = 0; t < n_traj; ++t) {
+        HMCResult res = hmc_trajectory(w.g, w.lat, mass, r, hp, rng);
+        out[8 * t + 0] = res.accepted ? 1.0 : 0.0;
+        out[8 * t + 1] = res.dH;
+        out[8 * t + 2] = res.dKE;
+        out[8 * t + 3] = res.dSG;
+        out[8 * t + 4] = res.dSF;
+        out[8 * t + 5] = res.total_cg_iters;
+        out[8 * t + 6] = w.g.avg_plaq();
+        out[8 * t + 7] = 0.0;
+    }
+    for (int mu = 0; mu < 2; ++mu)
+        for (int s = 0; s < w.lat.V; ++s) {
+            U[2 * (mu * w.lat.V + s)] = w.g.U[mu][s].real();
+            U[2 * (mu * w.lat.V + s) + 1] = w.g.U[mu][s].imag();
+        }
+}
+
 }  // extern "C"

@@ -9,6 +9,11 @@ from ._lib import SmgError, SmgLibraryError, lib  # noqa: F401
 from .api import (  # noqa: F401
     CGResult,
     FCGResult,
+    HMCResult,
+    Rng,
+    cg_solve_mixed,
+    hmc_params,
+    hmc_trajectory,
     MGHierarchy,
     build_full_mg,
     build_mg_hierarchy,

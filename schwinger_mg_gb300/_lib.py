@@ -35,6 +35,19 @@ class SolveResult(C.Structure):
 MAX_LEVELS = 6
 
 
+class HMCParams(C.Structure):
+    """smg_hmc_params (include/smg_gpu.h)."""
+    _fields_ = [("beta", C.c_double), ("tau", C.c_double), ("n_steps", C.c_int), ("omelyan", C.c_int),
+                ("n_inner", C.c_int), ("cg_maxiter", C.c_int), ("cg_tol", C.c_double), ("c_sw", C.c_double),
+                ("mu_t", C.c_double), ("force_accept", C.c_int), ("mixed_precision", C.c_int)]
+
+
+class HMCResult(C.Structure):
+    """smg_hmc_result (include/smg_gpu.h)."""
+    _fields_ = [("accepted", C.c_int), ("dH", C.c_double), ("dKE", C.c_double), ("dSG", C.c_double),
+                ("dSF", C.c_double), ("total_cg_iters", C.c_int), ("solves", C.c_int), ("plaquette", C.c_double)]
+
+
 class MGParams(C.Structure):
     """smg_mg_params (include/smg_gpu.h)."""
     _fields_ = [("n_levels", C.c_int), ("block", (C.c_int * 2) * (MAX_LEVELS - 1)),
@@ -93,6 +106,13 @@ _SIGS = {
     "smg_blas_scale": (_st, [_dp, _vp]),
     "smg_blas_dot_noalloc": (_st, [_vp, _vp, C.c_int64, C.c_int, _vp, _vp]),
     "smg_cg_solve": (_st, [_vp, _vp, _vp, C.c_int, C.c_double, C.POINTER(SolveResult)]),
+    "smg_cg_solve_mixed": (_st, [_vp, _vp, _vp, C.c_int, C.c_double, C.POINTER(SolveResult)]),
+    "smg_rng_create": (_st, [C.c_uint32, C.POINTER(_vp)]),
+    "smg_rng_destroy": (_st, [_vp]),
+    "smg_rng_uniform": (_st, [_vp, _dp]),
+    "smg_rng_normal": (_st, [_vp, C.c_int64, _dp]),
+    "smg_hmc_params_default": (_st, [C.POINTER(HMCParams)]),
+    "smg_hmc_trajectory": (_st, [_vp, C.c_double, C.c_double, C.POINTER(HMCParams), _vp, C.POINTER(HMCResult)]),
     "smg_fermion_force": (_st, [_vp, _vp, _dp]),
     "smg_mg_params_default": (_st, [C.POINTER(MGParams)]),
     "smg_mg_create": (_st, [_vp, C.POINTER(MGParams), _dp, C.POINTER(_vp)]),

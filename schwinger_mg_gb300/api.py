@@ -311,6 +311,22 @@ def cg_solve(A: DiracOp, n: int, rhs, max_iter: int, tol: float, precision: str 
     return CGResult(fx.download().reshape(b.shape), res.iterations, res.final_residual, res.true_residual)
 
 
+def cg_solve_mixed(A: DiracOp, n: int, rhs, max_iter: int, tol: float) -> CGResult:
+    """CG on D^dag D to a true FP64 residual below tol with FP32 CG inside FP64
+    defect correction (same result contract as cg_solve in FP64)."""
+    b = _as_c128(rhs)
+    nrhs = b.size // A.lat.ndof
+    if n != A.lat.ndof:
+        raise ValueError("n must equal 2*V")
+    fb = Field(A.lat, nrhs, "f64", A.ctx, data=b)
+    fx = Field(A.lat, nrhs, "f64", A.ctx)
+    res = _L.SolveResult()
+    st = _L.lib().smg_cg_solve_mixed(A.h, fb.h, fx.h, max_iter, tol, C.byref(res))
+    if st not in (_L.OK, _L.NOT_CONVERGED):
+        _L.check(st, "smg_cg_solve_mixed", A.ctx.h)
+    return CGResult(fx.download().reshape(b.shape), res.iterations, res.final_residual, res.true_residual)
+
+
 def fermion_force(D: DiracOp, X) -> np.ndarray:
     """F[mu][s] = -dS/dtheta for S = phi^dag (D^dag D)^-1 phi at X = (D^dag D)^-1 phi
     (reference src/hmc_forces.cpp:134-495)."""
@@ -330,6 +346,63 @@ def gauge_action(g: GaugeField, beta: float) -> float:
     v = C.c_double()
     _L.check(_L.lib().smg_gauge_action(g.h, beta, C.byref(v)), "smg_gauge_action", g.ctx.h)
     return v.value
+
+
+# ---------------------------------------------------------------- HMC
+class Rng(_Handle):
+    """The reference's std::mt19937 threaded through HMC trajectories."""
+
+    def __init__(self, seed: int):
+        h = C.c_void_p()
+        _L.check(_L.lib().smg_rng_create(seed, C.byref(h)), "smg_rng_create")
+        self.ctx = None
+        self._adopt(h, None, _L.lib().smg_rng_destroy)
+
+    def uniform(self) -> float:
+        v = C.c_double()
+        _L.check(_L.lib().smg_rng_uniform(self.h, C.byref(v)), "smg_rng_uniform")
+        return v.value
+
+    def normal(self, n: int) -> np.ndarray:
+        """n draws of one fresh std::normal_distribution (as MomentumField::randomise)."""
+        out = np.empty(n)
+        _L.check(_L.lib().smg_rng_normal(self.h, n, _ptr(out)), "smg_rng_normal")
+        return out
+
+
+def hmc_params(beta: float, tau: float = 1.0, n_steps: int = 10, omelyan: bool = True, n_inner: int = 0,
+               cg_maxiter: int = 10000, cg_tol: float = 1e-10, c_sw: float = 0.0, mu_t: float = 0.0,
+               force_accept: bool = False, mixed_precision: bool = False) -> _L.HMCParams:
+    """smg_hmc_params from the reference's HMCParams fields (src/hmc.h:107-119); n_inner > 0
+    selects the nested integrator with n_inner gauge-force steps between fermion-force kicks."""
+    p = _L.HMCParams()
+    _L.check(_L.lib().smg_hmc_params_default(C.byref(p)), "smg_hmc_params_default")
+    p.beta, p.tau, p.n_steps, p.omelyan, p.n_inner = beta, tau, n_steps, int(omelyan), n_inner
+    p.cg_maxiter, p.cg_tol, p.c_sw, p.mu_t = cg_maxiter, cg_tol, c_sw, mu_t
+    p.force_accept, p.mixed_precision = int(force_accept), int(mixed_precision)
+    return p
+
+
+@dataclass
+class HMCResult:
+    """HMCResult (reference src/hmc.h:121-129) plus the plaquette and the number of solves."""
+    accepted: bool
+    dH: float
+    dKE: float
+    dSG: float
+    dSF: float
+    total_cg_iters: int
+    solves: int
+    plaquette: float
+
+
+def hmc_trajectory(g: GaugeField, mass: float, wilson_r: float, params: _L.HMCParams, rng: Rng) -> HMCResult:
+    """One HMC trajectory on the device (reference hmc_trajectory, src/hmc_trajectory.cpp:38-235);
+    the links of `g` are updated in place (restored on rejection)."""
+    r = _L.HMCResult()
+    _L.check(_L.lib().smg_hmc_trajectory(g.h, mass, wilson_r, C.byref(params), rng.h, C.byref(r)),
+             "smg_hmc_trajectory", g.ctx.h)
+    return HMCResult(bool(r.accepted), r.dH, r.dKE, r.dSG, r.dSF, r.total_cg_iters, r.solves, r.plaquette)
 
 
 # ---------------------------------------------------------------- host inputs

@@ -37,75 +37,86 @@ __global__ void __launch_bounds__(256) k_dslash(DslashArgs<T> a) {
     const T half = T(0.5);
     const T sgn = DAG ? T(-1) : T(1);
     const int nrhs = a.nrhs;
-    const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
     const Geom g = a.g;
     T v[K];  // per-thread partials in the field precision (FP64 is scarce on this part)
 #pragma unroll
     for (int k = 0; k < K; ++k) v[k] = T(0);
 
-    if (rhs < nrhs) {
-        // Work items walk rows with both parities interleaved (row y even
-        // sites, row y odd sites, row y+1, ...), so the neighbour rows a
-        // block reads were read moments ago by its predecessors and are still
-        // in L2; walking all even sites before all odd ones streams every
-        // spinor from DRAM twice once the field outgrows L2.
-        for (int w = blockIdx.x * blockDim.y + threadIdx.y; w < g.V; w += gridDim.x * blockDim.y) {
-            const int y = w / g.L;
-            const int rem = w - y * g.L;
-            const int p = rem >= g.Lh ? 1 : 0;
-            const int xh = rem - p * g.Lh;
-            const int x = 2 * xh + ((y + p) & 1);
-            const int q = p * g.Vh + y * g.Lh + xh;
-            const int op = (1 - p) * g.Vh;
-            const int xp = x + 1 == g.L ? 0 : x + 1;
-            const int xm = x == 0 ? g.L - 1 : x - 1;
-            const int yp = y + 1 == g.L ? 0 : y + 1;
-            const int ym = y == 0 ? g.L - 1 : y - 1;
-            const int q_xp = op + ((xp + g.L * y) >> 1);
-            const int q_xm = op + ((xm + g.L * y) >> 1);
-            const int q_yp = op + ((x + g.L * yp) >> 1);
-            const int q_ym = op + ((x + g.L * ym) >> 1);
+    // one (row y, position rem) work item: rem < L/2 even sites of the row, the rest odd sites
+    auto site = [&](int y, int rem, int rhs) {
+        const int p = rem >= g.Lh ? 1 : 0;
+        const int xh = rem - p * g.Lh;
+        const int x = 2 * xh + ((y + p) & 1);
+        const int q = p * g.Vh + y * g.Lh + xh;
+        const int op = (1 - p) * g.Vh;
+        const int xp = x + 1 == g.L ? 0 : x + 1;
+        const int xm = x == 0 ? g.L - 1 : x - 1;
+        const int yp = y + 1 == g.L ? 0 : y + 1;
+        const int ym = y == 0 ? g.L - 1 : y - 1;
+        const int q_xp = op + ((xp + g.L * y) >> 1);
+        const int q_xm = op + ((xm + g.L * y) >> 1);
+        const int q_yp = op + ((x + g.L * yp) >> 1);
+        const int q_ym = op + ((x + g.L * ym) >> 1);
 
-            const cx<T> u0f = a.U[q];
-            const cx<T> u0b = a.U[q_xm];
-            const cx<T> u1f = a.U[g.V + q];
-            const cx<T> u1b = a.U[g.V + q_ym];
+        const cx<T> u0f = a.U[q];
+        const cx<T> u0b = a.U[q_xm];
+        const cx<T> u1f = a.U[g.V + q];
+        const cx<T> u1b = a.U[g.V + q_ym];
 
-            const Spinor<T> ps = ld_spinor(a.src, q, rhs, nrhs);
-            const Spinor<T> pxp = ld_spinor(a.src, q_xp, rhs, nrhs);
-            const Spinor<T> pxm = ld_spinor(a.src, q_xm, rhs, nrhs);
-            const Spinor<T> pyp = ld_spinor(a.src, q_yp, rhs, nrhs);
-            const Spinor<T> pym = ld_spinor(a.src, q_ym, rhs, nrhs);
-            const cx<T> s0 = ps.s0, s1 = ps.s1;
-            const cx<T> a0x = u0f * pxp.s0, a1x = u0f * pxp.s1;
-            const cx<T> b0x = cmulc(u0b, pxm.s0), b1x = cmulc(u0b, pxm.s1);
-            const cx<T> a0y = u1f * pyp.s0, a1y = u1f * pyp.s1;
-            const cx<T> b0y = cmulc(u1b, pym.s0), b1y = cmulc(u1b, pym.s1);
+        const Spinor<T> ps = ld_spinor(a.src, q, rhs, nrhs);
+        const Spinor<T> pxp = ld_spinor(a.src, q_xp, rhs, nrhs);
+        const Spinor<T> pxm = ld_spinor(a.src, q_xm, rhs, nrhs);
+        const Spinor<T> pyp = ld_spinor(a.src, q_yp, rhs, nrhs);
+        const Spinor<T> pym = ld_spinor(a.src, q_ym, rhs, nrhs);
+        const cx<T> s0 = ps.s0, s1 = ps.s1;
+        const cx<T> a0x = u0f * pxp.s0, a1x = u0f * pxp.s1;
+        const cx<T> b0x = cmulc(u0b, pxm.s0), b1x = cmulc(u0b, pxm.s1);
+        const cx<T> a0y = u1f * pyp.s0, a1y = u1f * pyp.s1;
+        const cx<T> b0y = cmulc(u1b, pym.s0), b1y = cmulc(u1b, pym.s1);
 
-            const T Cq = a.C ? a.C[q] : T(0);
-            const cx<T> dg0 = mk<T>(a.diag + Cq, a.mu_eff);
-            const cx<T> dg1 = mk<T>(a.diag - Cq, -a.mu_eff);
+        const T Cq = a.C ? a.C[q] : T(0);
+        const cx<T> dg0 = mk<T>(a.diag + Cq, a.mu_eff);
+        const cx<T> dg1 = mk<T>(a.diag - Cq, -a.mu_eff);
 
-            const cx<T> sr0 = (a0x + b0x) + (a0y + b0y);
-            const cx<T> sr1 = (a1x + b1x) + (a1y + b1y);
-            const cx<T> off0 = (b1x - a1x) + times_i(a1y - b1y);
-            const cx<T> off1 = (b0x - a0x) - times_i(a0y - b0y);
+        const cx<T> sr0 = (a0x + b0x) + (a0y + b0y);
+        const cx<T> sr1 = (a1x + b1x) + (a1y + b1y);
+        const cx<T> off0 = (b1x - a1x) + times_i(a1y - b1y);
+        const cx<T> off1 = (b0x - a0x) - times_i(a0y - b0y);
 
-            const cx<T> d0 = dg0 * s0 - half * (a.r * sr0 + sgn * off0);
-            const cx<T> d1 = dg1 * s1 - half * (a.r * sr1 + sgn * off1);
-            Spinor<T> out;
-            out.s0 = d0;
-            out.s1 = d1;
-            st_spinor(a.dst, q, rhs, nrhs, out);
+        const cx<T> d0 = dg0 * s0 - half * (a.r * sr0 + sgn * off0);
+        const cx<T> d1 = dg1 * s1 - half * (a.r * sr1 + sgn * off1);
+        Spinor<T> out;
+        out.s0 = d0;
+        out.s1 = d1;
+        st_spinor(a.dst, q, rhs, nrhs, out);
 
-            if (EPI == EPI_NORM) {
-                v[0] += norm2(d0) + norm2(d1);
-            } else if (EPI == EPI_MR) {
-                const Spinor<T> wv = ld_spinor(a.w, q, rhs, nrhs);
-                const cx<T> c = cmulc(d0, wv.s0) + cmulc(d1, wv.s1);
-                v[0] += c.re;
-                v[1] += c.im;
-                v[2] += norm2(d0) + norm2(d1);
+        if (EPI == EPI_NORM) {
+            v[0] += norm2(d0) + norm2(d1);
+        } else if (EPI == EPI_MR) {
+            const Spinor<T> wv = ld_spinor(a.w, q, rhs, nrhs);
+            const cx<T> c = cmulc(d0, wv.s0) + cmulc(d1, wv.s1);
+            v[0] += c.re;
+            v[1] += c.im;
+            v[2] += norm2(d0) + norm2(d1);
+        }
+    };
+
+    if (EPI == EPI_NONE) {
+        // one item per thread: row = blockIdx.y, no index division
+        const int rhs = blockIdx.z * blockDim.x + threadIdx.x;
+        const int rem = blockIdx.x * blockDim.y + threadIdx.y;
+        if (rhs < nrhs && rem < g.L) site(blockIdx.y, rem, rhs);
+    } else {
+        const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
+        if (rhs < nrhs) {
+            // Work items walk rows with both parities interleaved (row y even
+            // sites, row y odd sites, row y+1, ...), so the neighbour rows a
+            // block reads were read moments ago by its predecessors and are still
+            // in L2; walking all even sites before all odd ones streams every
+            // spinor from DRAM twice once the field outgrows L2.
+            for (int w = blockIdx.x * blockDim.y + threadIdx.y; w < g.V; w += gridDim.x * blockDim.y) {
+                const int y = w / g.L;
+                site(y, w - y * g.L, rhs);
             }
         }
     }
@@ -178,10 +189,11 @@ smg_status launch_dslash(smg_dirac* d, bool dag, int epi, const smg_field* src, 
     a.out = out_dev;
     dim3 grid, block;
     if (epi == EPI_NONE) {
-        SiteLaunch sl = site_launch(src->g.V, src->nrhs);
-        // the kernel needs power-of-two lanes only for reductions
-        grid = sl.grid;
-        block = sl.block;
+        // (row segment, row, rhs chunk) grid, one site and rhs per thread
+        const int lanes = src->nrhs < 32 ? src->nrhs : 32;
+        const int rows = 256 / lanes;
+        block = dim3(lanes, rows, 1);
+        grid = dim3((src->g.L + rows - 1) / rows, src->g.L, (src->nrhs + lanes - 1) / lanes);
     } else {
         ReduceLaunch rl = reduce_launch(src->g.V, src->nrhs);
         SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * src->nrhs * 3));

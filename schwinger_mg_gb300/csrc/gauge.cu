@@ -80,6 +80,15 @@ smg_status plaq_sum(smg_gauge* gf, double* out_host) {
 
 }  // namespace
 
+// gauge_force into a device array F[mu][s] (lexicographic)
+smg_status smg_gauge_force_dev(smg_gauge* gf, double beta, double* F_dev) {
+    smg_context* ctx = gf->ctx;
+    k_gauge_force<<<(gf->g.V + 255) / 256, 256, 0, ctx->stream>>>(gf->U64, gf->g, beta, F_dev);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
 smg_status smg_gauge_ensure_f32(smg_gauge* gf) {
     smg_context* ctx = gf->ctx;
     if (!gf->U32) SMG_CUDA(ctx, cudaMalloc(&gf->U32, (size_t)2 * gf->g.V * sizeof(cx<float>)));

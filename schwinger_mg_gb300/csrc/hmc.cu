@@ -1,0 +1,368 @@
+// Hybrid Monte Carlo on the device (reference src/hmc_trajectory.cpp:32-409,
+// src/hmc_multiscale.cpp:660-710, src/hmc_forces.cpp:64-111).
+//
+// The links, momenta, forces, pseudofermion and solutions stay in device
+// memory for the whole trajectory; the host draws the random numbers with the
+// reference's generator and distributions (momenta, eta, Metropolis) and runs
+// the integrator schedule.  Momenta and forces are lexicographic [mu][s]
+// doubles, as the reference's MomentumField and force arrays.
+#include <cmath>
+#include <random>
+#include <vector>
+
+#include "reduce.cuh"
+#include "smg_internal.h"
+
+struct smg_rng {
+    std::mt19937 gen;
+};
+
+smg_status smg_fermion_force_dev(smg_dirac* d, const smg_field* X, double* F_dev);
+smg_status smg_gauge_force_dev(smg_gauge* gf, double beta, double* F_dev);
+
+namespace {
+
+constexpr double kOmelyanLambda = 0.1932;  // hmc_trajectory.cpp:355
+
+// pi += scale * (f1 + f2)  (update_mom, hmc_trajectory.cpp:330-335); f2 may be null
+__global__ void k_kick(double* __restrict__ pi, const double* __restrict__ f1, const double* __restrict__ f2,
+                       double scale, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double f = f1 ? f1[i] : 0.0;
+    if (f2) f += f2[i];
+    pi[i] += scale * f;
+}
+
+// U_mu(s) *= exp(i * scale * pi_mu(s))  (update_gauge, hmc_trajectory.cpp:337-342)
+__global__ void k_links_exp(cx<double>* __restrict__ U, const double* __restrict__ pi, double scale, Geom g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2 * g.V) return;
+    const int mu = i / g.V, s = i - mu * g.V;
+    double sn, cs;
+    sincos(scale * pi[i], &sn, &cs);
+    cx<double>& u = U[(int64_t)mu * g.V + site_q(g, s % g.L, s / g.L)];
+    u = u * mk(cs, sn);
+}
+
+// sum of squares of n doubles (MomentumField::kinetic_energy without the 1/2)
+__global__ void __launch_bounds__(256) k_sumsq(const double* __restrict__ a, int n, double* partials,
+                                               unsigned int* ticket, double* out) {
+    double v[1] = {0.0};
+    for (int i = blockIdx.x * blockDim.y + threadIdx.y; i < n; i += gridDim.x * blockDim.y) v[0] += a[i] * a[i];
+    block_reduce_finalise<1>(v, partials, ticket, 1, FinStore{out, 1});
+}
+
+struct Hmc {
+    smg_context* ctx = nullptr;
+    smg_gauge* g = nullptr;
+    smg_dirac* d = nullptr;
+    smg_hmc_params p{};
+    double mass = 0, r = 1;
+    double* pi = nullptr;  // device [mu][s]
+    double* gf = nullptr;
+    double* ff = nullptr;
+    double* scal = nullptr;  // device scalars
+    cx<double>* U_old = nullptr;
+    smg_field* phi = nullptr;
+    smg_field* X = nullptr;
+    smg_field* eta = nullptr;
+    bool stale = false;  // links changed since the clover field and the FP32 links were formed
+    int cg_iters = 0, solves = 0;
+    smg_status warn = SMG_OK;
+
+    ~Hmc() {
+        if (ctx) cudaStreamSynchronize(ctx->stream);
+        for (void* q : {(void*)pi, (void*)gf, (void*)ff, (void*)scal, (void*)U_old})
+            if (q) cudaFree(q);
+        smg_field_destroy(phi);
+        smg_field_destroy(X);
+        smg_field_destroy(eta);
+        smg_dirac_destroy(d);
+    }
+
+    int n2() const { return 2 * g->g.V; }
+
+    smg_status refresh() {
+        if (!stale) return SMG_OK;
+        SMG_TRY(smg_gauge_ensure_f32(g));
+        SMG_TRY(smg_dirac_refresh(d));
+        stale = false;
+        return SMG_OK;
+    }
+
+    // X = (D^dag D)^-1 phi with the current links
+    smg_status solve() {
+        SMG_TRY(refresh());
+        smg_solve_result res{};
+        const smg_status st = p.mixed_precision ? smg_cg_solve_mixed(d, phi, X, p.cg_maxiter, p.cg_tol, &res)
+                                                : smg_cg_solve(d, phi, X, p.cg_maxiter, p.cg_tol, &res);
+        cg_iters += res.iterations;
+        ++solves;
+        // the reference warns and carries on when CG stops early (solvers.cpp:55-62)
+        if (st == SMG_NOT_CONVERGED || st == SMG_BREAKDOWN) {
+            warn = st;
+            return SMG_OK;
+        }
+        return st;
+    }
+
+    smg_status fermion_force() {
+        SMG_TRY(solve());
+        return smg_fermion_force_dev(d, X, ff);
+    }
+
+    smg_status gauge_force() {
+        SMG_TRY(refresh());
+        return smg_gauge_force_dev(g, p.beta, gf);
+    }
+
+    smg_status kick(const double* f1, const double* f2, double scale) {
+        k_kick<<<(n2() + 255) / 256, 256, 0, ctx->stream>>>(pi, f1, f2, scale, n2());
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+        return SMG_OK;
+    }
+
+    smg_status update_gauge(double scale) {
+        k_links_exp<<<(n2() + 255) / 256, 256, 0, ctx->stream>>>(g->U64, pi, scale, g->g);
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+        stale = true;
+        return SMG_OK;
+    }
+
+    smg_status kinetic(double* ke) {
+        ReduceLaunch rl = reduce_launch(n2(), 1);
+        SMG_TRY(smg_reduce_reserve(ctx, rl.grid.x));
+        k_sumsq<<<rl.grid, rl.block, 0, ctx->stream>>>(pi, n2(), ctx->red.partials, ctx->red.tickets, scal);
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+        double h = 0;
+        SMG_CUDA(ctx, cudaMemcpyAsync(&h, scal, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        *ke = 0.5 * h;
+        return SMG_OK;
+    }
+
+    // S_F = Re <phi, (D^dag D)^-1 phi> with a fresh solve (hmc_trajectory.cpp:170-182)
+    smg_status fermion_action(double* sf) {
+        SMG_TRY(solve());
+        double dot[2] = {0, 0};
+        SMG_TRY(smg_blas_dot(phi, X, dot));
+        *sf = dot[0];
+        return SMG_OK;
+    }
+
+    // plain_leapfrog_evolve (hmc_trajectory.cpp:243-409): gauge + fermion force at every kick
+    smg_status evolve_plain() {
+        const double dt = p.tau / p.n_steps;
+        auto solve_force = [&]() -> smg_status {
+            SMG_TRY(gauge_force());
+            return fermion_force();
+        };
+        if (p.omelyan) {
+            const double lam = kOmelyanLambda;
+            SMG_TRY(solve_force());
+            SMG_TRY(kick(gf, ff, lam * dt));
+            for (int step = 0; step < p.n_steps; ++step) {
+                SMG_TRY(update_gauge(0.5 * dt));
+                SMG_TRY(solve_force());
+                SMG_TRY(kick(gf, ff, (1.0 - 2.0 * lam) * dt));
+                SMG_TRY(update_gauge(0.5 * dt));
+                SMG_TRY(solve_force());
+                SMG_TRY(kick(gf, ff, step < p.n_steps - 1 ? 2.0 * lam * dt : lam * dt));
+            }
+        } else {
+            SMG_TRY(solve_force());
+            SMG_TRY(kick(gf, ff, 0.5 * dt));
+            for (int step = 0; step < p.n_steps - 1; ++step) {
+                SMG_TRY(update_gauge(dt));
+                SMG_TRY(solve_force());
+                SMG_TRY(kick(gf, ff, dt));
+            }
+            SMG_TRY(update_gauge(dt));
+            SMG_TRY(solve_force());
+            SMG_TRY(kick(gf, ff, 0.5 * dt));
+        }
+        return SMG_OK;
+    }
+
+    // nested integrator (hmc_multiscale.cpp:660-710): the fermion force on the outer
+    // steps, an inner leapfrog of n_inner steps on the gauge force between them
+    smg_status evolve_nested() {
+        const double h = p.tau / p.n_steps;
+        auto inner = [&](double dt_total) -> smg_status {
+            const int ni = p.n_inner;
+            const double dti = dt_total / ni;
+            SMG_TRY(gauge_force());
+            SMG_TRY(kick(gf, nullptr, 0.5 * dti));
+            for (int i = 0; i < ni; ++i) {
+                SMG_TRY(update_gauge(dti));
+                SMG_TRY(gauge_force());
+                SMG_TRY(kick(gf, nullptr, i < ni - 1 ? dti : 0.5 * dti));
+            }
+            return SMG_OK;
+        };
+        if (p.omelyan) {
+            const double lam = kOmelyanLambda;
+            SMG_TRY(fermion_force());
+            SMG_TRY(kick(ff, nullptr, lam * h));
+            for (int o = 0; o < p.n_steps; ++o) {
+                SMG_TRY(inner(0.5 * h));
+                SMG_TRY(fermion_force());
+                SMG_TRY(kick(ff, nullptr, (1.0 - 2.0 * lam) * h));
+                SMG_TRY(inner(0.5 * h));
+                SMG_TRY(fermion_force());
+                SMG_TRY(kick(ff, nullptr, o < p.n_steps - 1 ? 2.0 * lam * h : lam * h));
+            }
+        } else {
+            SMG_TRY(fermion_force());
+            SMG_TRY(kick(ff, nullptr, 0.5 * h));
+            for (int o = 0; o < p.n_steps; ++o) {
+                SMG_TRY(inner(h));
+                SMG_TRY(fermion_force());
+                SMG_TRY(kick(ff, nullptr, o < p.n_steps - 1 ? h : 0.5 * h));
+            }
+        }
+        return SMG_OK;
+    }
+};
+
+}  // namespace
+
+// gauge_force into a device array (defined next to the kernel in gauge.cu)
+
+extern "C" {
+
+SMG_API smg_status smg_rng_create(uint32_t seed, smg_rng** out) {
+    if (!out) return SMG_BAD_ARG;
+    *out = new smg_rng{std::mt19937(seed)};
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_rng_destroy(smg_rng* rng) {
+    delete rng;
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_rng_uniform(smg_rng* rng, double* out) {
+    if (!rng || !out) return SMG_BAD_ARG;
+    std::uniform_real_distribution<double> uniform(0.0, 1.0);
+    *out = uniform(rng->gen);
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_rng_normal(smg_rng* rng, int64_t n, double* out) {
+    if (!rng || n < 0 || (!out && n > 0)) return SMG_BAD_ARG;
+    std::normal_distribution<double> dist(0.0, 1.0);
+    for (int64_t i = 0; i < n; ++i) out[i] = dist(rng->gen);
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_hmc_params_default(smg_hmc_params* p) {
+    if (!p) return SMG_BAD_ARG;
+    *p = smg_hmc_params{};
+    p->beta = 4.0;
+    p->tau = 1.0;
+    p->n_steps = 10;
+    p->omelyan = 1;
+    p->n_inner = 0;
+    p->cg_maxiter = 10000;
+    p->cg_tol = 1e-10;
+    p->c_sw = 0.0;
+    p->mu_t = 0.0;
+    p->force_accept = 0;
+    p->mixed_precision = 0;
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_hmc_trajectory(smg_gauge* g, double mass, double wilson_r, const smg_hmc_params* p,
+                                      smg_rng* rng, smg_hmc_result* res) {
+    if (!g || !p || !rng) return SMG_BAD_ARG;
+    smg_context* ctx = g->ctx;
+    if (p->n_steps < 1 || p->n_inner < 0 || !(p->tau > 0) || p->cg_maxiter < 1 || !(p->cg_tol > 0))
+        return smg_fail(ctx, SMG_BAD_ARG, "hmc: n_steps >= 1, n_inner >= 0, tau > 0, cg_maxiter >= 1, cg_tol > 0");
+    Hmc h;
+    h.ctx = ctx;
+    h.g = g;
+    h.p = *p;
+    h.mass = mass;
+    h.r = wilson_r;
+    const int V = g->g.V, L = g->g.L;
+    const size_t fb = (size_t)2 * V * sizeof(double);
+    SMG_CUDA(ctx, cudaMalloc(&h.pi, fb));
+    SMG_CUDA(ctx, cudaMalloc(&h.gf, fb));
+    SMG_CUDA(ctx, cudaMalloc(&h.ff, fb));
+    SMG_CUDA(ctx, cudaMalloc(&h.scal, 64));
+    SMG_CUDA(ctx, cudaMalloc(&h.U_old, (size_t)2 * V * sizeof(cx<double>)));
+    SMG_CUDA(ctx, cudaMemcpyAsync(h.U_old, g->U64, (size_t)2 * V * sizeof(cx<double>), cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+    SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.phi));
+    SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.X));
+    SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.eta));
+    SMG_TRY(smg_dirac_create(g, mass, wilson_r, p->c_sw, p->mu_t, &h.d));
+
+    // momenta: MomentumField::randomise (hmc_forces.cpp:64-69), mu-major then site order
+    {
+        std::vector<double> pi_h((size_t)2 * V);
+        std::normal_distribution<double> dist(0.0, 1.0);
+        for (auto& v : pi_h) v = dist(rng->gen);
+        SMG_CUDA(ctx, cudaMemcpyAsync(h.pi, pi_h.data(), fb, cudaMemcpyHostToDevice, ctx->stream));
+        SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    // pseudofermion phi = D^dag eta, eta = random_vec(n, rng) (hmc_trajectory.cpp:32-36); the
+    // reference's random_vec draws each entry's imaginary part first (GCC argument order)
+    {
+        std::vector<double> eta_h((size_t)4 * V);
+        std::normal_distribution<double> dist(0.0, 1.0);
+        for (size_t i = 0; i < (size_t)2 * V; ++i) {
+            const double im = dist(rng->gen);
+            const double re = dist(rng->gen);
+            eta_h[2 * i] = re;
+            eta_h[2 * i + 1] = im;
+        }
+        SMG_TRY(smg_field_upload(h.eta, eta_h.data()));
+        SMG_TRY(smg_dirac_apply(h.d, SMG_OP_DDAG, h.eta, h.phi));
+    }
+
+    double KE0 = 0, SG0 = 0, SF0 = 0;
+    SMG_TRY(h.kinetic(&KE0));
+    SMG_TRY(smg_gauge_action(g, p->beta, &SG0));
+    SMG_TRY(h.fermion_action(&SF0));
+
+    SMG_TRY(p->n_inner > 0 ? h.evolve_nested() : h.evolve_plain());
+
+    double KE1 = 0, SG1 = 0, SF1 = 0;
+    SMG_TRY(h.refresh());
+    SMG_TRY(h.kinetic(&KE1));
+    SMG_TRY(smg_gauge_action(g, p->beta, &SG1));
+    SMG_TRY(h.fermion_action(&SF1));
+    const double dH = (KE1 + SG1 + SF1) - (KE0 + SG0 + SF0);
+    // Metropolis (hmc_trajectory.cpp:226-228): the uniform draw happens only when needed
+    bool accept = p->force_accept != 0 || dH < 0;
+    if (!accept) {
+        std::uniform_real_distribution<double> uniform(0.0, 1.0);
+        accept = uniform(rng->gen) < std::exp(-dH);
+    }
+    if (!accept) {
+        SMG_CUDA(ctx, cudaMemcpyAsync(g->U64, h.U_old, (size_t)2 * V * sizeof(cx<double>), cudaMemcpyDeviceToDevice,
+                                      ctx->stream));
+        SMG_TRY(smg_gauge_ensure_f32(g));
+    }
+    double plaq = 0;
+    SMG_TRY(smg_gauge_avg_plaq(g, &plaq));
+    if (res) {
+        res->accepted = accept ? 1 : 0;
+        res->dH = dH;
+        res->dKE = KE1 - KE0;
+        res->dSG = SG1 - SG0;
+        res->dSF = SF1 - SF0;
+        res->total_cg_iters = h.cg_iters;
+        res->solves = h.solves;
+        res->plaquette = plaq;
+    }
+    return SMG_OK;
+}
+
+}  // extern "C"

@@ -1120,8 +1120,12 @@ smg_status coarse_apply(smg_mg* mg, int l, VecView<T> x, cx<T>* y, int epi, cons
 template <typename T>
 smg_status level_apply_fine(smg_mg* mg, smg_field* x, smg_field* y, const smg_field* w, double* out3) {
     SMG_TRY(smg_dslash(mg->dirac, false, x, mg->f_t, nullptr));
-    if (w) return smg_dslash_mr(mg->dirac, true, mg->f_t, y, w, out3);
-    return smg_dslash(mg->dirac, true, mg->f_t, y, nullptr);
+    if (w && x->nrhs < 4) return smg_dslash_mr(mg->dirac, true, mg->f_t, y, w, out3);
+    SMG_TRY(smg_dslash(mg->dirac, true, mg->f_t, y, nullptr));
+    // several RHS: the one-item-per-thread stencil plus a streaming <y, w>, ||y||^2 pass beats the
+    // stencil with the reduction fused into its grid-stride loop
+    if (w) return vreduce<T>(mg->ctx, fview<T>(y), (const cx<T>*)w->data, VR_DOTNORM, out3);
+    return SMG_OK;
 }
 
 // scalar area layout: per level 16 * nrhs doubles (MR: 3, CG: rr, pap3, bnorm2, beta, ints)

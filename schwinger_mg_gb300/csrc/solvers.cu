@@ -848,9 +848,116 @@ smg_status gcr_mixed(smg_dirac* d, smg_mg* mg, const smg_field* b, smg_field* x,
     return st;
 }
 
+// Mixed-precision CG: FP64 defect correction around the FP32 CG.  Each outer
+// step forms the true FP64 residual r = b - A x, solves A e = r / ||r|| with
+// the FP32 operator to kInnerTol (or further when that suffices for tol), and
+// adds x += ||r|| e in FP64 (same scheme as the mixed GCR above).
+smg_status cg_mixed(smg_dirac* d, const smg_field* b, smg_field* x, int max_iter, double tol, smg_solve_result* res) {
+    smg_context* ctx = d->ctx;
+    const int nrhs = b->nrhs, V = b->g.V;
+    FieldSet fs;
+    smg_field *r64, *t64, *Ax64;
+    SMG_TRY(fs.add(b, &r64));
+    SMG_TRY(fs.add(b, &t64));
+    SMG_TRY(fs.add(b, &Ax64));
+    smg_field *r32 = nullptr, *e32 = nullptr;
+    SMG_TRY(smg_field_alloc_like(b, SMG_F32, &r32));
+    fs.f.push_back(r32);
+    SMG_TRY(smg_field_alloc_like(b, SMG_F32, &e32));
+    fs.f.push_back(e32);
+    SMG_TRY(smg_gauge_ensure_f32(d->gauge));
+    double* sc = nullptr;  // [0, nrhs) ||r||^2, [nrhs, 2 nrhs) multipliers
+    SMG_CUDA(ctx, cudaMallocAsync((void**)&sc, (size_t)2 * nrhs * sizeof(double), ctx->stream));
+    std::vector<double> b2(nrhs), rr(nrhs), mult(nrhs);
+    SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
+    SMG_CUDA(ctx, cudaMemcpyAsync(r64->data, b->data, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    SMG_TRY(reduce_into<double>(ctx, fv<double>(r64), nullptr, VR_NORM, sc));
+    SMG_CUDA(ctx, cudaMemcpyAsync(b2.data(), sc, nrhs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    rr = b2;
+    bool nonfinite = false;
+    for (int j = 0; j < nrhs; ++j)
+        if (!std::isfinite(b2[j])) nonfinite = true;
+    int total = 0;
+    while (!nonfinite && total < max_iter) {
+        bool any = false;
+        double worst_ratio = 0;
+        for (int j = 0; j < nrhs; ++j) {
+            const bool act = b2[j] >= 1e-60 && rr[j] >= tol * tol * b2[j];
+            mult[j] = act ? 1.0 / std::sqrt(rr[j]) : 0.0;
+            if (act) {
+                any = true;
+                worst_ratio = std::max(worst_ratio, std::sqrt(rr[j] / b2[j]));
+            }
+        }
+        if (!any) break;
+        const double inner_tol = std::max(kInnerTol, 0.5 * tol / worst_ratio);
+        SMG_CUDA(ctx, cudaMemcpyAsync(sc + nrhs, mult.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice,
+                                      ctx->stream));
+        k_convert_mul<float, double><<<vec_grid(V, nrhs), vec_block(nrhs), 0, ctx->stream>>>(
+            fv<float>(r32), (const cx<double>*)r64->data, sc + nrhs);
+        count_launch(ctx);
+        smg_solve_result ir{};
+        const smg_status ist = cg_run<float>(d, r32, e32, max_iter - total, inner_tol, &ir);
+        if (ist == SMG_NONFINITE) {
+            nonfinite = true;
+            break;
+        }
+        total += ir.iterations;
+        for (int j = 0; j < nrhs; ++j) mult[j] = mult[j] > 0 ? std::sqrt(rr[j]) : 0.0;
+        SMG_CUDA(ctx, cudaMemcpyAsync(sc + nrhs, mult.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice,
+                                      ctx->stream));
+        k_axpy_mul<double, float><<<vec_grid(V, nrhs), vec_block(nrhs), 0, ctx->stream>>>(
+            fv<double>(x), (const cx<float>*)e32->data, sc + nrhs);
+        count_launch(ctx);
+        SMG_TRY(apply_A<double>(d, x, t64, Ax64));
+        const int64_t n = b->n_complex();
+        k_residual<double><<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(
+            (const cx<double>*)b->data, (const cx<double>*)Ax64->data, (cx<double>*)r64->data, n);
+        count_launch(ctx);
+        SMG_TRY(reduce_into<double>(ctx, fv<double>(r64), nullptr, VR_NORM, sc));
+        SMG_CUDA(ctx, cudaMemcpyAsync(rr.data(), sc, nrhs * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int j = 0; j < nrhs; ++j)
+            if (!std::isfinite(rr[j])) nonfinite = true;
+        if (ir.iterations == 0) break;  // no progress possible
+    }
+    SMG_CUDA(ctx, cudaFreeAsync(sc, ctx->stream));
+    double worst = 0;
+    bool notconv = false;
+    for (int j = 0; j < nrhs; ++j) {
+        if (b2[j] > 0 && std::isfinite(b2[j])) {
+            const double rel = std::sqrt(rr[j] / b2[j]);
+            worst = std::max(worst, rel);
+            if (!(rel < tol)) notconv = true;
+        }
+    }
+    if (res) {
+        res->iterations = total;
+        res->final_residual = worst;
+        res->true_residual = worst;
+        res->operator_applications = total + 1;
+    }
+    if (nonfinite) return smg_fail(ctx, SMG_NONFINITE, "cg_solve_mixed: non-finite residual");
+    if (notconv) return smg_fail(ctx, SMG_NOT_CONVERGED, "cg_solve_mixed: iteration limit reached");
+    return SMG_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+SMG_API smg_status smg_cg_solve_mixed(smg_dirac* d, const smg_field* rhs, smg_field* x, int max_iter, double tol,
+                                      smg_solve_result* res) {
+    if (!d || !rhs || !x) return SMG_BAD_ARG;
+    smg_context* ctx = d->ctx;
+    if (rhs == x) return smg_fail(ctx, SMG_BAD_ARG, "rhs and x must be distinct");
+    SMG_TRY(smg_field_check_pair(rhs, x));
+    if (rhs->prec != SMG_F64) return smg_fail(ctx, SMG_BAD_ARG, "cg_solve_mixed needs F64 fields");
+    if (rhs->g.L != d->gauge->g.L) return smg_fail(ctx, SMG_BAD_ARG, "field L differs from gauge L");
+    if (max_iter < 0 || !(tol > 0)) return smg_fail(ctx, SMG_BAD_ARG, "max_iter >= 0 and tol > 0 required");
+    return cg_mixed(d, rhs, x, max_iter, tol, res);
+}
 
 SMG_API smg_status smg_gcr_solve(smg_dirac* d, smg_mg* mg, const smg_field* rhs, smg_field* x, int max_iter, double tol,
                                  int trunc, int reference_coefficient, smg_solve_result* res) {

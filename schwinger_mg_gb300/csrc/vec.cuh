@@ -42,7 +42,44 @@ __global__ void __launch_bounds__(256) k_vreduce(VecView<T> a, const cx<T>* __re
     T v[K];  // per-thread partials in the field precision (FP64 is scarce on this part)
 #pragma unroll
     for (int k = 0; k < K; ++k) v[k] = T(0);
-    if (rhs < a.nrhs) {
+    if (rhs < a.nrhs && a.ndof == 2 && !a.rhs_inner) {
+        // fine fields: one 2-spinor vector per (site, rhs), four sites per pass with every load issued first
+        const Spinor<T>* __restrict__ ap = reinterpret_cast<const Spinor<T>*>(a.p);
+        const Spinor<T>* __restrict__ bp = reinterpret_cast<const Spinor<T>*>(b);
+        const int stride = gridDim.x * blockDim.y;
+        T r0 = 0, r1 = 0, r2 = 0;
+        for (int s0 = blockIdx.x * blockDim.y + threadIdx.y; s0 < a.nsites; s0 += 4 * stride) {
+            Spinor<T> xa[4], xb[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int s = s0 + u * stride;
+                if (s < a.nsites) {
+                    xa[u] = ap[(int64_t)s * a.nrhs + rhs];
+                    if (MODE != VR_NORM) xb[u] = bp[(int64_t)s * a.nrhs + rhs];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (s0 + u * stride >= a.nsites) continue;
+                if (MODE != VR_NORM) {
+                    const cx<T> c = cmulc(xa[u].s0, xb[u].s0) + cmulc(xa[u].s1, xb[u].s1);
+                    r0 += c.re;
+                    r1 += c.im;
+                }
+                if (MODE != VR_DOT) r2 += norm2(xa[u].s0) + norm2(xa[u].s1);
+            }
+        }
+        if (MODE == VR_DOT) {
+            v[0] = r0;
+            v[1] = r1;
+        } else if (MODE == VR_NORM) {
+            v[0] = r2;
+        } else {
+            v[0] = r0;
+            v[1] = r1;
+            v[2] = r2;
+        }
+    } else if (rhs < a.nrhs) {
         for (int s = blockIdx.x * blockDim.y + threadIdx.y; s < a.nsites; s += gridDim.x * blockDim.y) {
             const int64_t base = a.idx(s, rhs, 0);
             const int ds = a.dstride();

@@ -78,6 +78,16 @@ def mg_case(ref, name, L, beta, m, r, csw, mu, gseed, bs, k, null_iters, seed):
     print("wrote", name, "gcr iters", it, "res", res)
 
 
+def hmc_case(ref, name, L, beta, m, r, csw, gseed, seed, n_steps, omelyan, n_traj, tau=1.0):
+    """Trajectories of the reference's hmc_trajectory (full lattice, clover) from one rng."""
+    U = gauge_normal(L, beta, gseed).reshape(-1)
+    U_out, out = ref.hmc_trajectories(U, m, r, beta, tau, n_steps, omelyan, 10000, 1e-12, csw, 0.0, 0, seed, n_traj)
+    np.savez_compressed(OUT / f"{name}.npz", L=L, beta=beta, m=m, r=r, csw=csw, gseed=gseed, seed=seed,
+                        n_steps=n_steps, omelyan=omelyan, tau=tau, n_traj=n_traj, cg_tol=1e-12, U=U, U_out=U_out,
+                        traj=out)
+    print("wrote", name, out[:, :2].tolist())
+
+
 def main():
     O.build(ref=True)
     ref = O.ref()
@@ -89,6 +99,8 @@ def main():
     cg_force_case(ref, "cg_force_L32_config1", 32, 2.0, 0.1, 1.0, 1.0, 0.0, 31, 33)
     cg_force_case(ref, "cg_force_L16_wilson", 16, 4.0, 0.2, 1.0, 0.0, 0.0, 41, 42)
     mg_case(ref, "mg_L16_bs4_k4", 16, 2.0, 0.1, 1.0, 1.0, 0.0, 51, 4, 4, 5, 52)
+    hmc_case(ref, "hmc_L8_omelyan", 8, 4.0, 0.1, 1.0, 1.0, 61, 62, 5, 1, 3)
+    hmc_case(ref, "hmc_L8_leapfrog", 8, 4.0, 0.1, 1.0, 1.0, 63, 64, 8, 0, 2)
 
 
 if __name__ == "__main__":
