@@ -49,7 +49,8 @@ typedef enum {
     SMG_DEVICE_ERROR = 5,   /* a CUDA call failed                            */
     SMG_TIMEOUT = 6,        /* a bounded device-side wait ran out            */
     SMG_NO_MEMORY = 7,      /* device allocation failed                      */
-    SMG_UNSUPPORTED = 8     /* configuration not built in this library       */
+    SMG_UNSUPPORTED = 8,    /* configuration not built in this library       */
+    SMG_IO_ERROR = 9        /* a file could not be opened, read or written   */
 } smg_status;
 
 typedef enum {
@@ -214,6 +215,26 @@ SMG_API smg_status smg_cg_solve(smg_dirac* d, const smg_field* rhs, smg_field* x
 SMG_API smg_status smg_cg_solve_mixed(smg_dirac* d, const smg_field* rhs, smg_field* x,
                                       int max_iter, double tol, smg_solve_result* res);
 
+/* Preconditioned CG (the reference's cg_solve_core, src/solvers.cpp:16-72,
+ * as cg_solve_precond / cg_solve_x0 / cg_solve_x0_precond, :80-96).  mg: one
+ * MG cycle per iteration as the preconditioner (NULL: none); use_x0 != 0:
+ * x holds the start vector on entry (else x = 0).  Complex alpha = <r,z>/<p,Ap>
+ * and beta = <r',z'>/<r,z> per right-hand side; each stops on its own when
+ * the recursive ||r||/||b|| < tol.  F64 or F32 fields. */
+SMG_API smg_status smg_cg_solve_precond(smg_dirac* d, smg_mg* mg, const smg_field* rhs, smg_field* x,
+                                        int use_x0, int max_iter, double tol, smg_solve_result* res);
+
+/* mr_smooth (reference src/smoother.cpp:9-23): niter MR steps on A = D^dag D
+ * from the x given on entry, omega = <Ar, r> / <Ar, Ar> per right-hand side. */
+SMG_API smg_status smg_mr_smooth(smg_dirac* d, const smg_field* b, smg_field* x, int niter);
+/* richardson_smooth_op on A = D^dag D (src/smoother.cpp:64-73): x += omega (b - A x),
+ * niter steps from the x given on entry, omega > 0 fixed. */
+SMG_API smg_status smg_richardson_smooth(smg_dirac* d, const smg_field* b, smg_field* x, int niter,
+                                         double omega);
+/* estimate_lambda_max of A = D^dag D (src/smoother.cpp:43-60): niter power
+ * steps from random_vec(2V, std::mt19937(12345)); lambda = ||A v|| of the last. */
+SMG_API smg_status smg_estimate_lambda_max(smg_dirac* d, int niter, double* lambda);
+
 /* -------------------------------------------------------------- multigrid */
 
 #define SMG_MAX_LEVELS 6
@@ -281,6 +302,14 @@ SMG_API smg_status smg_mg_get_coarse_op(smg_mg* mg, int level, double* links);
  * environment variable SMG_CUDA_GRAPHS=0 at smg_mg_create it is launched
  * kernel by kernel instead. */
 SMG_API smg_status smg_mg_precondition(smg_mg* mg, const smg_field* b, smg_field* x);
+/* estimate_lambda_max (src/smoother.cpp:43-60) of the level-`level` operator
+ * (0: D^dag D) in FP64 from random_vec(dim, std::mt19937(12345)). */
+SMG_API smg_status smg_mg_estimate_lambda_max(smg_mg* mg, int level, int niter, double* lambda);
+/* MGHierarchy::set_symmetric (src/multigrid.cpp:144-152): every level but the
+ * coarsest smooths with Richardson at omega = damping / lambda_max (30 power
+ * steps), which makes the cycle linear and Hermitian for CG; damping <= 0
+ * returns to MR.  omega (optional) receives n_levels - 1 values. */
+SMG_API smg_status smg_mg_set_symmetric(smg_mg* mg, double damping, double* omega);
 /* Host-array versions of the transfer operators and the coarse operator at
  * level `level` (Prolongator::prolong / restrict_vec, src/prolongator.h:77-108;
  * SparseCoarseOp::apply_to, src/coarse_op.h:282-297).  Vectors use the
@@ -316,6 +345,20 @@ SMG_API smg_status smg_mg_time_coarse_apply(smg_mg* mg, int level, int nrhs, int
 SMG_API smg_status smg_gcr_solve(smg_dirac* d, smg_mg* mg, const smg_field* rhs, smg_field* x, int max_iter,
                                  double tol, int trunc, int reference_coefficient, smg_solve_result* res);
 
+/* fgmres_solve_generic / fgmres_solve_mg (src/solvers.cpp:555-800): restarted
+ * flexible GMRES(restart) on D^dag D with one MG cycle per step (mg != NULL)
+ * or none, Ritz harvesting of n_ritz_harvest pairs per cycle (reference
+ * default 4) and deflation of later preconditioned vectors with them.
+ * Every right-hand side runs its own Arnoldi process; each stops on
+ * |g_k+1| / ||b|| < tol inside a cycle or on the true residual at a restart.
+ * res->final_residual and res->true_residual are the true ||b - A x|| / ||b||
+ * (worst over right-hand sides).  Optional outputs: ritz_values
+ * [rhs][3 * n_ritz_harvest] (the Ritz values kept at the end, in list order)
+ * and n_ritz[rhs] (how many).  1 <= restart <= 32, n_ritz_harvest <= 8. */
+SMG_API smg_status smg_fgmres_solve(smg_dirac* d, smg_mg* mg, const smg_field* rhs, smg_field* x, int restart,
+                                    int max_iter, double tol, int n_ritz_harvest, smg_solve_result* res,
+                                    double* ritz_values, int* n_ritz);
+
 /* ------------------------------------------------------------------ forces */
 
 /* fermion_force (reference src/hmc_forces.cpp:134-194 and 198-495): with
@@ -323,6 +366,12 @@ SMG_API smg_status smg_gcr_solve(smg_dirac* d, smg_mg* mg, const smg_field* rhs,
  * -dS/dtheta_mu(s) for S = phi^dag (D^dag D)^-1 phi, X = (D^dag D)^-1 phi.
  * X is a single-RHS F64 field; force is 2*V doubles on the host. */
 SMG_API smg_status smg_fermion_force(smg_dirac* d, const smg_field* X, double* force);
+/* Forward pass of the pseudofermion action (fermion_action /
+ * fermion_action_precond, src/hmc_forces.cpp:113-131): X = (D^dag D)^-1 phi
+ * by PCG (mg: preconditioner or NULL) and action[rhs] = Re <phi, X>.  X is
+ * what smg_fermion_force (the backward pass) takes. */
+SMG_API smg_status smg_fermion_action(smg_dirac* d, smg_mg* mg, const smg_field* phi, smg_field* X, int max_iter,
+                                      double tol, double* action, smg_solve_result* res);
 
 /* --------------------------------------------------------------------- HMC */
 
@@ -383,6 +432,34 @@ SMG_API smg_status smg_hmc_params_default(smg_hmc_params* p);
  * gauge, momenta, forces and fields stay on the device. */
 SMG_API smg_status smg_hmc_trajectory(smg_gauge* g, double mass, double wilson_r, const smg_hmc_params* p,
                                       smg_rng* rng, smg_hmc_result* res);
+
+/* ------------------------------------------------------------ gauge files */
+
+/* GaugeHeader (reference src/hmc.h:19-25): the 32-byte header of the "SWNG"
+ * gauge file, little-endian, followed by U[0][0..V) and U[1][0..V) as
+ * complex128 (save_gauge / load_gauge, src/hmc_forces.cpp:18-62). */
+typedef struct {
+    uint32_t magic; /* 0x53574E47 */
+    uint32_t L;
+    double beta;
+    double mass;
+    double avg_plaq;
+} smg_gauge_header;
+
+/* save_gauge: writes hdr {magic, L, beta, mass, avg_plaq} and the links. */
+SMG_API smg_status smg_host_gauge_write_swng(const char* path, int L, const double* U, double beta, double mass,
+                                             double avg_plaq);
+/* load_gauge: reads the header (SMG_BAD_ARG on a wrong magic, or on an L other
+ * than L_expected when L_expected > 0) and, when U != NULL, the links divided
+ * by their modulus as the reference does after reading. */
+SMG_API smg_status smg_host_gauge_read_swng(const char* path, int L_expected, smg_gauge_header* hdr, double* U);
+/* GaugeField::save / load (src/gauge.h:38-57): int32 V, then the links. */
+SMG_API smg_status smg_host_gauge_write_raw(const char* path, int L, const double* U);
+SMG_API smg_status smg_host_gauge_read_raw(const char* path, int L, double* U);
+/* The same formats from and into a device gauge handle; smg_gauge_save writes
+ * the handle's plaquette into the header. */
+SMG_API smg_status smg_gauge_save(smg_gauge* g, double beta, double mass, const char* path);
+SMG_API smg_status smg_gauge_load(smg_gauge* g, const char* path, smg_gauge_header* hdr);
 
 /* -------------------------------------------------------- host utilities */
 

@@ -9,6 +9,13 @@
 //   MGConfig, build_full_mg                 src/config.h:19-30, src/mg_builder.h:6-11
 //   MGHierarchy::precondition               src/multigrid.h:63
 //   fermion_force, gauge_force, gauge_action  src/hmc.h:46-69
+//   cg_solve_precond, cg_solve_x0(_precond)   src/solvers.h:41-53, 99-104
+//   FGMRESResult, RitzPair, fgmres_solve_mg   src/solvers.h:13-23, 62-79
+//   mr_smooth, richardson_smooth_op,
+//   estimate_lambda_max                     src/smoother.h
+//   MGHierarchy::set_symmetric              src/multigrid.h:62
+//   fermion_action(_precond) + fermion_force as a forward/backward pair
+//                                           src/hmc.h (FermionActionResult)
 // Host vectors keep the reference layout (Vec v[2*s + spin]); each call copies
 // them to the device, runs the sm_103a kernels and copies results back.
 // Failures throw smg::Error carrying the smg_status, where the reference
@@ -181,6 +188,32 @@ inline CGResult cg_solve(const DiracOp& D, int n, const Vec& rhs, int max_iter, 
     return out;
 }
 
+// mr_smooth(D, x, b, niter): x is the start vector and the result
+inline void mr_smooth(const DiracOp& D, Vec& x, const Vec& b, int niter) {
+    DeviceField fb(D.lat.L, 1), fx(D.lat.L, 1);
+    fb.upload(b);
+    fx.upload(x);
+    check(smg_mr_smooth(D.handle(), fb.get(), fx.get(), niter), default_context(), "smg_mr_smooth");
+    fx.download(x);
+}
+
+// richardson_smooth_op with A = D^dag D of `D`
+inline void richardson_smooth(const DiracOp& D, Vec& x, const Vec& b, int niter, double omega) {
+    DeviceField fb(D.lat.L, 1), fx(D.lat.L, 1);
+    fb.upload(b);
+    fx.upload(x);
+    check(smg_richardson_smooth(D.handle(), fb.get(), fx.get(), niter, omega), default_context(),
+          "smg_richardson_smooth");
+    fx.download(x);
+}
+
+// estimate_lambda_max(A, n, niter) with A = D^dag D of `D`
+inline double estimate_lambda_max(const DiracOp& D, int niter) {
+    double l = 0;
+    check(smg_estimate_lambda_max(D.handle(), niter, &l), default_context(), "smg_estimate_lambda_max");
+    return l;
+}
+
 struct MGConfig {  // reference src/config.h:19-30
     int mg_levels = 2;
     int block_size = 4;
@@ -210,6 +243,10 @@ class MGHierarchy {
         Vec x(b.size());
         fx.download(x);
         return x;
+    }
+    // Richardson smoothing at omega = damping / lambda_max on every level but the coarsest
+    void set_symmetric(double damping = 0.8) {
+        check(smg_mg_set_symmetric(h_.get(), damping, nullptr), default_context(), "smg_mg_set_symmetric");
     }
     smg_mg* handle() const { return h_.get(); }
 
@@ -253,6 +290,90 @@ inline FCGResult fcg_solve_mg(const DiracOp& D, int n, const Vec& rhs, MGHierarc
     x.download(out.solution);
     return out;
 }
+
+// cg_solve_precond / cg_solve_x0 / cg_solve_x0_precond (mg == nullptr: no
+// preconditioner; x0 == nullptr or empty: start from zero)
+inline CGResult cg_solve_x0_precond(const DiracOp& D, int n, const Vec& rhs, const Vec* x0, MGHierarchy* mg,
+                                    int max_iter, double tol) {
+    if (n != D.lat.ndof) throw Error(SMG_BAD_ARG, "cg_solve_precond: n must be 2*V");
+    DeviceField b(D.lat.L, 1), x(D.lat.L, 1);
+    b.upload(rhs);
+    const bool use_x0 = x0 && !x0->empty();
+    if (use_x0) x.upload(*x0);
+    smg_solve_result r{};
+    smg_status s = smg_cg_solve_precond(D.handle(), mg ? mg->handle() : nullptr, b.get(), x.get(), use_x0 ? 1 : 0,
+                                        max_iter, tol, &r);
+    if (s != SMG_OK && s != SMG_NOT_CONVERGED) check(s, default_context(), "smg_cg_solve_precond");
+    CGResult out{Vec(n), r.iterations, r.final_residual};
+    x.download(out.solution);
+    return out;
+}
+inline CGResult cg_solve_precond(const DiracOp& D, int n, const Vec& rhs, MGHierarchy& mg, int max_iter,
+                                 double tol) {
+    return cg_solve_x0_precond(D, n, rhs, nullptr, &mg, max_iter, tol);
+}
+inline CGResult cg_solve_x0(const DiracOp& D, int n, const Vec& rhs, const Vec& x0, int max_iter, double tol) {
+    return cg_solve_x0_precond(D, n, rhs, &x0, nullptr, max_iter, tol);
+}
+
+struct RitzPair {
+    double value;
+    Vec vector;  // not returned by the device solver: left empty
+};
+struct FGMRESResult {
+    Vec solution;
+    int iterations;
+    double final_residual;
+    std::vector<RitzPair> ritz_pairs;
+};
+
+inline FGMRESResult fgmres_solve_mg(const DiracOp& D, int n, const Vec& rhs, MGHierarchy* mg, int restart,
+                                    int max_iter, double tol, int n_ritz_harvest = 4) {
+    if (n != D.lat.ndof) throw Error(SMG_BAD_ARG, "fgmres_solve_mg: n must be 2*V");
+    DeviceField b(D.lat.L, 1), x(D.lat.L, 1);
+    b.upload(rhs);
+    smg_solve_result r{};
+    std::vector<double> vals(3 * (size_t)(n_ritz_harvest > 0 ? n_ritz_harvest : 1));
+    int nr = 0;
+    smg_status s = smg_fgmres_solve(D.handle(), mg ? mg->handle() : nullptr, b.get(), x.get(), restart, max_iter,
+                                    tol, n_ritz_harvest, &r, vals.data(), &nr);
+    if (s != SMG_OK && s != SMG_NOT_CONVERGED) check(s, default_context(), "smg_fgmres_solve");
+    FGMRESResult out{Vec(n), r.iterations, r.true_residual, {}};
+    x.download(out.solution);
+    for (int i = 0; i < nr; ++i) out.ritz_pairs.push_back({vals[i], {}});
+    return out;
+}
+
+// The pseudofermion action as a differentiable pair: forward solves
+// X = (D^dag D)^-1 phi and returns S = Re <phi, X>; backward returns
+// F = -dS/dtheta from the X kept by forward (chi = D X is recomputed).
+class PseudofermionAction {
+   public:
+    PseudofermionAction(const DiracOp& D, MGHierarchy* mg = nullptr) : D_(D), mg_(mg), X_(D.lat.L, 1) {}
+    double forward(const Vec& phi, int max_iter, double tol) {
+        DeviceField fp(D_.lat.L, 1);
+        fp.upload(phi);
+        double S = 0;
+        smg_solve_result r{};
+        check(smg_fermion_action(D_.handle(), mg_ ? mg_->handle() : nullptr, fp.get(), X_.get(), max_iter, tol, &S,
+                                 &r),
+              default_context(), "smg_fermion_action");
+        iterations = r.iterations;
+        return S;
+    }
+    void backward(std::array<RVec, 2>& force) const {
+        RVec flat(2 * (size_t)D_.lat.V);
+        check(smg_fermion_force(D_.handle(), X_.get(), flat.data()), default_context(), "smg_fermion_force");
+        force[0].assign(flat.begin(), flat.begin() + D_.lat.V);
+        force[1].assign(flat.begin() + D_.lat.V, flat.end());
+    }
+    int iterations = 0;
+
+   private:
+    const DiracOp& D_;
+    MGHierarchy* mg_;
+    DeviceField X_;
+};
 
 inline void fermion_force(const DiracOp& D, const Vec& X, std::array<RVec, 2>& force) {
     DeviceField fx(D.lat.L, 1);

@@ -374,6 +374,85 @@ class Ref(_Lib):
                                       C.c_uint(seed), C.c_int(n_traj), _p(out))
         return U, out.reshape(n_traj, 8)[:, :7]
 
+    def richardson_smooth(self, U, m, r, csw, mu, b, x0, niter, omega):
+        U, b = _c(U), _c(b)
+        x = _c(x0).copy()
+        self.lib.ref_richardson_smooth(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                                       C.c_double(mu), _p(b), _p(x), C.c_int(niter), C.c_double(omega))
+        return x
+
+    def estimate_lambda_max(self, U, m, r, csw, mu, niter):
+        U = _c(U)
+        f = self.lib.ref_estimate_lambda_max
+        f.restype = C.c_double
+        return f(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw), C.c_double(mu),
+                 C.c_int(niter))
+
+    def mg_precondition_sym(self, U, m, r, csw, mu, params: RefMGParams, seed, damping, b):
+        """set_symmetric(damping) then precondition(b); returns (M b, omegas)."""
+        U, b = _c(U), _c(b)
+        out = np.empty_like(b)
+        om = np.zeros(max(1, params.levels - 1))
+        self.lib.ref_mg_precondition_sym(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r),
+                                         C.c_double(csw), C.c_double(mu), C.byref(params), C.c_uint(seed),
+                                         C.c_double(damping), _p(b), _p(out), _p(om))
+        return out, om
+
+    def cg_precond(self, U, m, r, csw, mu, params, seed, damping, b, x0, max_iter, tol):
+        """cg_solve / cg_solve_x0 / cg_solve_precond / cg_solve_x0_precond; params None: no MG."""
+        U, b = _c(U), _c(b)
+        x = np.empty_like(b)
+        keep = _c(x0) if x0 is not None else None
+        res = C.c_double(0)
+        f = self.lib.ref_cg_precond
+        f.restype = C.c_int
+        it = f(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw), C.c_double(mu),
+               C.c_int(int(params is not None)), C.byref(params) if params is not None else None, C.c_uint(seed),
+               C.c_double(damping), _p(b), _p(keep) if keep is not None else None, _p(x), C.c_int(max_iter),
+               C.c_double(tol), C.byref(res))
+        return x, it, res.value
+
+    def fgmres(self, U, m, r, csw, mu, params, seed, b, restart, max_iter, tol, n_ritz):
+        """fgmres_solve_mg (params given) or fgmres_solve_generic with the identity; returns
+        (x, iterations, final residual, ritz values)."""
+        U, b = _c(U), _c(b)
+        x = np.empty_like(b)
+        res = C.c_double(0)
+        ritz = np.zeros(3 * max(1, n_ritz))
+        nr = C.c_int(0)
+        f = self.lib.ref_fgmres
+        f.restype = C.c_int
+        it = f(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw), C.c_double(mu),
+               C.c_int(int(params is not None)), C.byref(params) if params is not None else None, C.c_uint(seed),
+               _p(b), _p(x), C.c_int(restart), C.c_int(max_iter), C.c_double(tol), C.c_int(n_ritz), C.byref(res),
+               _p(ritz), C.byref(nr))
+        return x, it, res.value, ritz[:nr.value].copy()
+
+    def fermion_action(self, U, m, r, csw, mu, phi, max_iter, tol):
+        U, phi = _c(U), _c(phi)
+        X = np.empty_like(phi)
+        f = self.lib.ref_fermion_action
+        f.restype = C.c_double
+        S = f(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw), C.c_double(mu), _p(phi),
+              C.c_int(max_iter), C.c_double(tol), _p(X))
+        return S, X
+
+    def save_gauge(self, U, beta, mass, swng_path, raw_path):
+        """save_gauge and GaugeField::save of the links U into the two files."""
+        U = _c(U)
+        f = self.lib.ref_save_gauge
+        f.restype = C.c_int
+        return f(C.c_int(self._L(U)), _p(U), C.c_double(beta), C.c_double(mass), str(swng_path).encode(),
+                 str(raw_path).encode()) == 1
+
+    def load_gauge(self, L, path):
+        U = np.empty(2 * L * L, dtype=np.complex128)
+        hdr = np.zeros(3)
+        f = self.lib.ref_load_gauge
+        f.restype = C.c_int
+        ok = f(C.c_int(L), str(path).encode(), _p(U), _p(hdr)) == 1
+        return (U, hdr) if ok else (None, None)
+
     def pseudofermion(self, U, m, r, csw, mu, seed):
         U = _c(U)
         L = self._L(U)

@@ -351,4 +351,126 @@ void ref_hmc_trajectories(int L, double* U, double mass, double r, double beta, 
         }
 }
 
+
+// richardson_smooth_op (src/smoother.cpp:64-73) with A = D^dag D; x updated in place
+void ref_richardson_smooth(int L, const double* U, double m, double r, double csw, double mu, const double* b,
+                           double* x, int niter, double omega) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    OpApply A = [&D](const Vec& s, Vec& d) { D.apply_DdagD(s, d); };
+    Vec xv = to_vec(x, w.lat.ndof);
+    richardson_smooth_op(A, xv, to_vec(b, w.lat.ndof), niter, omega);
+    from_vec(xv, x);
+}
+
+// estimate_lambda_max (src/smoother.cpp:43-60) of D^dag D
+double ref_estimate_lambda_max(int L, const double* U, double m, double r, double csw, double mu, int niter) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    OpApply A = [&D](const Vec& s, Vec& d) { D.apply_DdagD(s, d); };
+    return estimate_lambda_max(A, w.lat.ndof, niter);
+}
+
+// MGHierarchy::set_symmetric(damping) (src/multigrid.cpp:144-152) followed by
+// precondition (:155-157); omega receives levels - 1 values
+void ref_mg_precondition_sym(int L, const double* U, double m, double r, double csw, double mu,
+                             const RefMGParams* p, unsigned seed, double damping, const double* b, double* out,
+                             double* omega) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    MGHierarchy mg = ref_build(D, *p, seed, nullptr);
+    mg.set_symmetric(damping);
+    for (size_t l = 0; l + 1 < mg.levels.size(); ++l) omega[l] = mg.levels[l].richardson_omega;
+    from_vec(mg.precondition(to_vec(b, w.lat.ndof)), out);
+}
+
+// cg_solve_core (src/solvers.cpp:16-72) through cg_solve / cg_solve_x0 /
+// cg_solve_precond / cg_solve_x0_precond: with_mg != 0 builds the hierarchy
+// (set_symmetric(damping) when damping > 0) as the preconditioner; x0 may be
+// NULL.  Returns the iteration count.
+int ref_cg_precond(int L, const double* U, double m, double r, double csw, double mu, int with_mg,
+                   const RefMGParams* p, unsigned seed, double damping, const double* b, const double* x0,
+                   double* x, int max_iter, double tol, double* final_res) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    OpApply A = [&D](const Vec& s, Vec& d) { D.apply_DdagD(s, d); };
+    const int n = w.lat.ndof;
+    Vec bv = to_vec(b, n);
+    CGResult res;
+    if (with_mg) {
+        MGHierarchy mg = ref_build(D, *p, seed, nullptr);
+        if (damping > 0) mg.set_symmetric(damping);
+        auto precond = [&mg](const Vec& v) { return mg.precondition(v); };
+        res = x0 ? cg_solve_x0_precond(A, n, bv, to_vec(x0, n), precond, max_iter, tol)
+                 : cg_solve_precond(A, n, bv, precond, max_iter, tol);
+    } else {
+        res = x0 ? cg_solve_x0(A, n, bv, to_vec(x0, n), max_iter, tol) : cg_solve(A, n, bv, max_iter, tol);
+    }
+    from_vec(res.solution, x);
+    if (final_res) *final_res = res.final_residual;
+    return res.iterations;
+}
+
+// fgmres_solve_mg (src/solvers.cpp:776-787), or fgmres_solve_generic with the
+// identity preconditioner when with_mg == 0.  ritz receives up to 3 *
+// n_ritz_harvest values (RitzPair::value, list order), n_ritz their count.
+int ref_fgmres(int L, const double* U, double m, double r, double csw, double mu, int with_mg,
+               const RefMGParams* p, unsigned seed, const double* b, double* x, int restart, int max_iter,
+               double tol, int n_ritz_harvest, double* final_res, double* ritz, int* n_ritz) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    OpApply A = [&D](const Vec& s, Vec& d) { D.apply_DdagD(s, d); };
+    const int n = w.lat.ndof;
+    FGMRESResult res;
+    if (with_mg) {
+        MGHierarchy mg = ref_build(D, *p, seed, nullptr);
+        res = fgmres_solve_mg(A, n, to_vec(b, n), mg, restart, max_iter, tol, n_ritz_harvest);
+    } else {
+        auto identity = [](const Vec& v) { return v; };
+        res = fgmres_solve_generic(A, n, to_vec(b, n), identity, restart, max_iter, tol, n_ritz_harvest);
+    }
+    from_vec(res.solution, x);
+    if (final_res) *final_res = res.final_residual;
+    *n_ritz = (int)res.ritz_pairs.size();
+    for (size_t i = 0; i < res.ritz_pairs.size(); ++i) ritz[i] = res.ritz_pairs[i].value;
+    return res.iterations;
+}
+
+// fermion_action (src/hmc_forces.cpp:113-119): S = Re <phi, X>, X = (D^dag D)^-1 phi by cg_solve
+double ref_fermion_action(int L, const double* U, double m, double r, double csw, double mu, const double* phi,
+                          int max_iter, double tol, double* X) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    FermionActionResult fa = fermion_action(D, to_vec(phi, w.lat.ndof), max_iter, tol);
+    from_vec(fa.X, X);
+    return fa.action;
+}
+
+
+// save_gauge (src/hmc_forces.cpp:18-35) and GaugeField::save (src/gauge.h:38-46)
+int ref_save_gauge(int L, const double* U, double beta, double mass, const char* swng_path, const char* raw_path) {
+    World w(L, U);
+    bool ok = save_gauge(w.g, beta, mass, swng_path);
+    ok = w.g.save(raw_path) && ok;
+    return ok ? 1 : 0;
+}
+
+// load_gauge (src/hmc_forces.cpp:37-62): links into U, header fields into hdr[0..2]
+// (beta, mass, avg_plaq); returns 1 on success
+int ref_load_gauge(int L, const char* path, double* U, double* hdr) {
+    Lattice lat(L);
+    GaugeField g(lat);
+    GaugeHeader h{};
+    if (!load_gauge(g, h, path)) return 0;
+    for (int mu = 0; mu < 2; ++mu)
+        for (int s = 0; s < lat.V; ++s) {
+            U[2 * (mu * lat.V + s)] = g.U[mu][s].real();
+            U[2 * (mu * lat.V + s) + 1] = g.U[mu][s].imag();
+        }
+    hdr[0] = h.beta;
+    hdr[1] = h.mass;
+    hdr[2] = h.avg_plaq;
+    return 1;
+}
+
 }  // extern "C"

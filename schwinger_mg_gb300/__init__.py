@@ -9,6 +9,14 @@ from ._lib import SmgError, SmgLibraryError, lib  # noqa: F401
 from .api import (  # noqa: F401
     CGResult,
     FCGResult,
+    FGMRESResult,
+    cg_solve_precond,
+    estimate_lambda_max,
+    fermion_action,
+    fgmres_solve,
+    fgmres_solve_mg,
+    mr_smooth,
+    richardson_smooth,
     HMCResult,
     Rng,
     cg_solve_mixed,
@@ -32,6 +40,10 @@ from .api import (  # noqa: F401
     gauge_action,
     gauge_force,
     gauge_normal,
+    load_gauge,
+    load_gauge_raw,
+    save_gauge,
+    save_gauge_raw,
     norm,
     random_vec,
     scale,

@@ -12,7 +12,7 @@ from pathlib import Path
 LIB_PATH = Path(__file__).resolve().parent / "libsmg_gpu.so"
 
 # smg_status codes (include/smg_gpu.h)
-OK, NOT_CONVERGED, BREAKDOWN, NONFINITE, BAD_ARG, DEVICE_ERROR, TIMEOUT, NO_MEMORY, UNSUPPORTED = range(9)
+OK, NOT_CONVERGED, BREAKDOWN, NONFINITE, BAD_ARG, DEVICE_ERROR, TIMEOUT, NO_MEMORY, UNSUPPORTED, IO_ERROR = range(10)
 F64, F32, F16 = 0, 1, 2
 OP_D, OP_DDAG, OP_DDAGD, OP_G5D = 0, 1, 2, 3
 
@@ -33,6 +33,12 @@ class SolveResult(C.Structure):
 
 
 MAX_LEVELS = 6
+
+
+class GaugeHeader(C.Structure):
+    """smg_gauge_header = the reference's GaugeHeader (src/hmc.h:19-25)."""
+    _fields_ = [("magic", C.c_uint32), ("L", C.c_uint32), ("beta", C.c_double), ("mass", C.c_double),
+                ("avg_plaq", C.c_double)]
 
 
 class HMCParams(C.Structure):
@@ -128,6 +134,21 @@ _SIGS = {
     "smg_mg_time_coarse_apply": (_st, [_vp, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     "smg_mg_coarse_apply_batch": (_st, [_vp, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _dp]),
     "smg_gcr_solve": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(SolveResult)]),
+    "smg_cg_solve_precond": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_double, C.POINTER(SolveResult)]),
+    "smg_mr_smooth": (_st, [_vp, _vp, _vp, C.c_int]),
+    "smg_richardson_smooth": (_st, [_vp, _vp, _vp, C.c_int, C.c_double]),
+    "smg_estimate_lambda_max": (_st, [_vp, C.c_int, _dp]),
+    "smg_mg_estimate_lambda_max": (_st, [_vp, C.c_int, C.c_int, _dp]),
+    "smg_mg_set_symmetric": (_st, [_vp, C.c_double, _dp]),
+    "smg_fgmres_solve": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(SolveResult),
+                               _dp, C.POINTER(C.c_int)]),
+    "smg_fermion_action": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_double, _dp, C.POINTER(SolveResult)]),
+    "smg_host_gauge_write_swng": (_st, [C.c_char_p, C.c_int, _dp, C.c_double, C.c_double, C.c_double]),
+    "smg_host_gauge_read_swng": (_st, [C.c_char_p, C.c_int, C.POINTER(GaugeHeader), _dp]),
+    "smg_host_gauge_write_raw": (_st, [C.c_char_p, C.c_int, _dp]),
+    "smg_host_gauge_read_raw": (_st, [C.c_char_p, C.c_int, _dp]),
+    "smg_gauge_save": (_st, [_vp, C.c_double, C.c_double, C.c_char_p]),
+    "smg_gauge_load": (_st, [_vp, C.c_char_p, C.POINTER(GaugeHeader)]),
     "smg_host_gauge_normal": (_st, [C.c_int, C.c_double, C.c_uint32, _dp]),
     "smg_host_random_vec": (_st, [C.c_int64, C.c_uint32, _dp]),
 }

@@ -327,6 +327,67 @@ def cg_solve_mixed(A: DiracOp, n: int, rhs, max_iter: int, tol: float) -> CGResu
     return CGResult(fx.download().reshape(b.shape), res.iterations, res.final_residual, res.true_residual)
 
 
+def cg_solve_precond(A: DiracOp, n: int, rhs, precond: "MGHierarchy | None", max_iter: int, tol: float,
+                     x0=None, precision: str = "f64") -> CGResult:
+    """Preconditioned CG on D^dag D (reference cg_solve_precond / cg_solve_x0 /
+    cg_solve_x0_precond, src/solvers.cpp:16-96): `precond` is an MGHierarchy
+    (one cycle per iteration) or None; `x0` an optional start vector."""
+    b = _as_c128(rhs)
+    if n != A.lat.ndof:
+        raise ValueError("n must equal 2*V")
+    nrhs = b.size // A.lat.ndof
+    fb = Field(A.lat, nrhs, precision, A.ctx, data=b)
+    fx = Field(A.lat, nrhs, precision, A.ctx, data=_as_c128(x0) if x0 is not None else None)
+    res = _L.SolveResult()
+    st = _L.lib().smg_cg_solve_precond(A.h, precond.h if precond is not None else None, fb.h, fx.h,
+                                       int(x0 is not None), max_iter, tol, C.byref(res))
+    if st not in (_L.OK, _L.NOT_CONVERGED):
+        _L.check(st, "smg_cg_solve_precond", A.ctx.h)
+    return CGResult(fx.download().reshape(b.shape), res.iterations, res.final_residual, res.true_residual)
+
+
+def mr_smooth(D: DiracOp, x, b, niter: int) -> np.ndarray:
+    """mr_smooth (reference src/smoother.cpp:9-23) on D^dag D from the start vector x."""
+    bb = _as_c128(b)
+    nrhs = bb.size // D.lat.ndof
+    fb = Field(D.lat, nrhs, "f64", D.ctx, data=bb)
+    fx = Field(D.lat, nrhs, "f64", D.ctx, data=_as_c128(x))
+    _L.check(_L.lib().smg_mr_smooth(D.h, fb.h, fx.h, niter), "smg_mr_smooth", D.ctx.h)
+    return fx.download().reshape(bb.shape)
+
+
+def richardson_smooth(D: DiracOp, x, b, niter: int, omega: float) -> np.ndarray:
+    """richardson_smooth_op (reference src/smoother.cpp:64-73) on D^dag D from the start vector x."""
+    bb = _as_c128(b)
+    nrhs = bb.size // D.lat.ndof
+    fb = Field(D.lat, nrhs, "f64", D.ctx, data=bb)
+    fx = Field(D.lat, nrhs, "f64", D.ctx, data=_as_c128(x))
+    _L.check(_L.lib().smg_richardson_smooth(D.h, fb.h, fx.h, niter, omega), "smg_richardson_smooth", D.ctx.h)
+    return fx.download().reshape(bb.shape)
+
+
+def estimate_lambda_max(D: DiracOp, niter: int = 30) -> float:
+    """estimate_lambda_max of D^dag D (reference src/smoother.cpp:43-60)."""
+    v = C.c_double(0)
+    _L.check(_L.lib().smg_estimate_lambda_max(D.h, niter, C.byref(v)), "smg_estimate_lambda_max", D.ctx.h)
+    return v.value
+
+
+def fermion_action(D: DiracOp, phi, max_iter: int, tol: float, precond: "MGHierarchy | None" = None):
+    """Forward pass (fermion_action / fermion_action_precond, src/hmc_forces.cpp:113-131):
+    returns (S = Re <phi, X>, X = (D^dag D)^-1 phi as a device Field, iterations).
+    fermion_force(D, X) is the backward pass."""
+    p = _as_c128(phi)
+    nrhs = p.size // D.lat.ndof
+    fp = Field(D.lat, nrhs, "f64", D.ctx, data=p)
+    fx = Field(D.lat, nrhs, "f64", D.ctx)
+    S = np.zeros(nrhs)
+    res = _L.SolveResult()
+    _L.check(_L.lib().smg_fermion_action(D.h, precond.h if precond is not None else None, fp.h, fx.h, max_iter, tol,
+                                         _ptr(S), C.byref(res)), "smg_fermion_action", D.ctx.h)
+    return (S[0] if nrhs == 1 else S), fx, res.iterations
+
+
 def fermion_force(D: DiracOp, X) -> np.ndarray:
     """F[mu][s] = -dS/dtheta for S = phi^dag (D^dag D)^-1 phi at X = (D^dag D)^-1 phi
     (reference src/hmc_forces.cpp:134-495)."""
@@ -406,6 +467,49 @@ def hmc_trajectory(g: GaugeField, mass: float, wilson_r: float, params: _L.HMCPa
 
 
 # ---------------------------------------------------------------- host inputs
+def save_gauge(g: "GaugeField | np.ndarray", beta: float, mass: float, path, avg_plaq: float | None = None) -> None:
+    """save_gauge (reference src/hmc_forces.cpp:18-35): the "SWNG" file.  `g` is a
+    device GaugeField (its plaquette goes into the header) or host links [2][V]."""
+    p = str(path).encode()
+    if isinstance(g, GaugeField):
+        _L.check(_L.lib().smg_gauge_save(g.h, beta, mass, p), "smg_gauge_save", g.ctx.h)
+        return
+    U = _as_c128(g).reshape(-1)
+    L = int(round((U.size // 2) ** 0.5))
+    _L.check(_L.lib().smg_host_gauge_write_swng(p, L, _ptr(U.view(np.float64)), beta, mass,
+                                                float(avg_plaq if avg_plaq is not None else 0.0)),
+             "smg_host_gauge_write_swng")
+
+
+def load_gauge(path, L: int = 0):
+    """load_gauge (reference src/hmc_forces.cpp:37-62): returns (links [2][V] divided by their
+    modulus, header dict).  L > 0 checks the lattice size like the reference."""
+    p = str(path).encode()
+    hdr = _L.GaugeHeader()
+    _L.check(_L.lib().smg_host_gauge_read_swng(p, L, C.byref(hdr), None), "smg_host_gauge_read_swng")
+    n = int(hdr.L)
+    U = np.empty(2 * n * n, dtype=np.complex128)
+    _L.check(_L.lib().smg_host_gauge_read_swng(p, L, C.byref(hdr), _ptr(U.view(np.float64))),
+             "smg_host_gauge_read_swng")
+    return U.reshape(2, n * n), dict(L=n, beta=hdr.beta, mass=hdr.mass, avg_plaq=hdr.avg_plaq)
+
+
+def save_gauge_raw(U, path) -> None:
+    """GaugeField::save (reference src/gauge.h:38-46): int32 V, then the links."""
+    U = _as_c128(U).reshape(-1)
+    L = int(round((U.size // 2) ** 0.5))
+    _L.check(_L.lib().smg_host_gauge_write_raw(str(path).encode(), L, _ptr(U.view(np.float64))),
+             "smg_host_gauge_write_raw")
+
+
+def load_gauge_raw(path, L: int) -> np.ndarray:
+    """GaugeField::load (reference src/gauge.h:48-57)."""
+    U = np.empty(2 * L * L, dtype=np.complex128)
+    _L.check(_L.lib().smg_host_gauge_read_raw(str(path).encode(), L, _ptr(U.view(np.float64))),
+             "smg_host_gauge_read_raw")
+    return U.reshape(2, L * L)
+
+
 def gauge_normal(L: int, beta: float, seed: int) -> np.ndarray:
     """U = exp(i theta), theta ~ N(0, 1/beta) from std::mt19937(seed); shape (2, V)."""
     out = np.empty(2 * L * L, dtype=np.complex128)
@@ -562,6 +666,21 @@ class MGHierarchy(_Handle):
         return fx.download().reshape(a.shape)
 
 
+    def estimate_lambda_max(self, level: int = 0, niter: int = 30) -> float:
+        """estimate_lambda_max (src/smoother.cpp:43-60) of the level operator."""
+        v = C.c_double(0)
+        _L.check(_L.lib().smg_mg_estimate_lambda_max(self.h, level, niter, C.byref(v)),
+                 "smg_mg_estimate_lambda_max", self.ctx.h)
+        return v.value
+
+    def set_symmetric(self, damping: float = 0.8) -> np.ndarray:
+        """MGHierarchy::set_symmetric (src/multigrid.cpp:144-152): Richardson
+        smoothing with omega = damping / lambda_max per level; returns the omegas."""
+        om = np.zeros(max(1, self.n_levels - 1))
+        _L.check(_L.lib().smg_mg_set_symmetric(self.h, damping, _ptr(om)), "smg_mg_set_symmetric", self.ctx.h)
+        return om
+
+
 def build_mg_hierarchy(D: DiracOp, n_levels: int, block_size: int, k_null: int, coarse_block_agg: int,
                        null_iters: int, seed: int, w_cycle: bool = True, pre_smooth: int = 3, post_smooth: int = 3,
                        warm_start=None, **kw) -> MGHierarchy:
@@ -617,3 +736,43 @@ def fcg_solve_mg(A: DiracOp, n: int, rhs, mg: MGHierarchy, max_iter: int, tol: f
                  **kw) -> FCGResult:
     """fcg_solve_mg (reference src/solvers.cpp:803-811)."""
     return fcg_solve(A, n, rhs, mg, max_iter, tol, truncation, **kw)
+
+
+@dataclass
+class FGMRESResult:
+    """FGMRESResult (reference src/solvers.h:18-23): Ritz values per right-hand
+    side stand in for ritz_pairs (the vectors stay on the device)."""
+    solution: np.ndarray
+    iterations: int
+    final_residual: float
+    ritz_values: list
+    status: int = 0
+
+
+def fgmres_solve(A: DiracOp, n: int, rhs, precond: "MGHierarchy | None", restart: int, max_iter: int, tol: float,
+                 n_ritz_harvest: int = 4, precision: str = "f64") -> FGMRESResult:
+    """Restarted flexible GMRES on D^dag D (reference fgmres_solve_generic,
+    src/solvers.cpp:555-773) with one MG cycle per step (`precond`) or none."""
+    b = _as_c128(rhs)
+    if n != A.lat.ndof:
+        raise ValueError("n must equal 2*V")
+    nrhs = b.size // A.lat.ndof
+    fb = Field(A.lat, nrhs, precision, A.ctx, data=b)
+    fx = Field(A.lat, nrhs, precision, A.ctx)
+    res = _L.SolveResult()
+    vals = np.zeros(nrhs * 3 * max(1, n_ritz_harvest))
+    cnt = (C.c_int * nrhs)()
+    st = _L.lib().smg_fgmres_solve(A.h, precond.h if precond is not None else None, fb.h, fx.h, restart, max_iter,
+                                   tol, n_ritz_harvest, C.byref(res), _ptr(vals), cnt)
+    if st not in (_L.OK, _L.NOT_CONVERGED):
+        _L.check(st, "smg_fgmres_solve", A.ctx.h)
+    vals = vals.reshape(nrhs, -1)
+    ritz = [list(vals[j, :cnt[j]]) for j in range(nrhs)]
+    return FGMRESResult(fx.download().reshape(b.shape), res.iterations, res.true_residual,
+                        ritz[0] if nrhs == 1 else ritz, st)
+
+
+def fgmres_solve_mg(A: DiracOp, n: int, rhs, mg: MGHierarchy, restart: int, max_iter: int, tol: float,
+                    n_ritz_harvest: int = 4, **kw) -> FGMRESResult:
+    """fgmres_solve_mg (reference src/solvers.cpp:776-787)."""
+    return fgmres_solve(A, n, rhs, mg, restart, max_iter, tol, n_ritz_harvest, **kw)

@@ -48,6 +48,7 @@ SMG_API const char* smg_status_string(smg_status s) {
         case SMG_TIMEOUT: return "device wait timed out";
         case SMG_NO_MEMORY: return "out of device memory";
         case SMG_UNSUPPORTED: return "unsupported";
+        case SMG_IO_ERROR: return "file input/output error";
     }
     return "unknown status";
 }

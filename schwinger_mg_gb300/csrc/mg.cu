@@ -63,6 +63,7 @@ struct Level {
     cx<double>* A64 = nullptr;
     cx<float>* A32 = nullptr;
     void* Atc = nullptr;  // BF16 links pre-tiled for the tensor-core apply (F32 hierarchies)
+    double rich_omega = 0;  // > 0: Richardson smoothing with this omega (MGLevel::richardson_omega)
     int64_t vsize() const { return (int64_t)nagg_x * nagg_y * ax * ay * ndof * nc_next; }
     int64_t asize() const { return (int64_t)nsites * 9 * ndof * ndof; }
 };
@@ -1285,6 +1286,67 @@ smg_status mr_coarse(smg_mg* mg, int l, void* x, const void* b, int niter, bool 
     return SMG_OK;
 }
 
+// Richardson smoothing (richardson_smooth_op, src/smoother.cpp:64-73) with the
+// level's fixed omega; same entry state and residual contract as the MR
+// smoothers above, so the cycle picks either per level (mg_cycle,
+// src/multigrid.cpp:57-61, 95-98).
+template <typename T>
+smg_status smooth_fine(smg_mg* mg, smg_field* x, const smg_field* b, int niter, bool x_is_zero) {
+    const double om = mg->lv[0].rich_omega;
+    if (!(om > 0)) return mr_fine<T>(mg, x, b, niter, x_is_zero);
+    smg_context* ctx = mg->ctx;
+    smg_field *r = mg->f_r, *Ar = mg->f_Ar;
+    const int64_t n = b->n_complex();
+    if (x_is_zero) {
+        SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
+        SMG_CUDA(ctx, cudaMemcpyAsync(r->data, b->data, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    } else {
+        SMG_TRY(level_apply_fine<T>(mg, x, Ar, nullptr, nullptr));
+        k_vsub<T><<<blocks_for(n), 256, 0, ctx->stream>>>((cx<T>*)r->data, (const cx<T>*)b->data,
+                                                        (const cx<T>*)Ar->data, n);
+        count_launch(ctx);
+    }
+    for (int it = 0; it < niter; ++it) {
+        SMG_TRY(level_apply_fine<T>(mg, r, Ar, nullptr, nullptr));
+        const VecView<T> xv = flat(fview<T>(x));
+        k_rich_update<T><<<vec_grid(xv.nsites, xv.nrhs), vec_block(xv.nrhs), 0, ctx->stream>>>(
+            xv, (cx<T>*)r->data, (const cx<T>*)Ar->data, (T)om);
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+    }
+    return SMG_OK;
+}
+
+template <typename T>
+smg_status smooth_coarse(smg_mg* mg, int l, void* x, const void* b, int niter, bool x_is_zero) {
+    const double om = mg->lv[l].rich_omega;
+    if (!(om > 0)) return mr_coarse<T>(mg, l, x, b, niter, x_is_zero);
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[l];
+    CoarseWork& w = mg->cw[l];
+    const int nrhs = mg->work_nrhs;
+    VecView<T> xv = cview<T>(x, L, nrhs), rv = cview<T>(w.r, L, nrhs);
+    const int64_t n = xv.n();
+    const size_t bytes = (size_t)n * sizeof(cx<T>);
+    if (x_is_zero) {
+        SMG_CUDA(ctx, cudaMemsetAsync(x, 0, bytes, ctx->stream));
+        SMG_CUDA(ctx, cudaMemcpyAsync(w.r, b, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    } else {
+        SMG_TRY(coarse_apply<T>(mg, l, xv, (cx<T>*)w.Ar, 0, nullptr, nullptr));
+        k_vsub<T><<<blocks_for(n), 256, 0, ctx->stream>>>((cx<T>*)w.r, (const cx<T>*)b, (const cx<T>*)w.Ar, n);
+        count_launch(ctx);
+    }
+    for (int it = 0; it < niter; ++it) {
+        SMG_TRY(coarse_apply<T>(mg, l, rv, (cx<T>*)w.Ar, 0, nullptr, nullptr));
+        const VecView<T> xf = flat(xv);
+        k_rich_update<T><<<vec_grid(xf.nsites, xf.nrhs), vec_block(xf.nrhs), 0, ctx->stream>>>(
+            xf, (cx<T>*)w.r, (const cx<T>*)w.Ar, (T)om);
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+    }
+    return SMG_OK;
+}
+
 // Coarsest solve: CG from x = 0 to coarse_tol (SparseCoarseOp::solve without
 // deflation, src/coarse_op.h:492-547); the host checks progress every 8 steps
 template <typename T>
@@ -1433,7 +1495,7 @@ smg_status cycle_coarse(smg_mg* mg, int l, void* x, const void* b) {
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[l];
     const int nrhs = mg->work_nrhs;
-    SMG_TRY(mr_coarse<T>(mg, l, x, b, mg->p.pre_smooth, true));
+    SMG_TRY(smooth_coarse<T>(mg, l, x, b, mg->p.pre_smooth, true));
     // residual of the smoothed x is in cw[l].r
     CoarseWork& nw = mg->cw[l + 1];
     SMG_TRY(restrict_to<T>(mg, l, mg->cw[l].r, nw.b));
@@ -1452,7 +1514,7 @@ smg_status cycle_coarse(smg_mg* mg, int l, void* x, const void* b) {
     }
     SMG_TRY(prolong_to<T>(mg, l, nw.x, x, 1));
     (void)L;
-    return mr_coarse<T>(mg, l, x, b, mg->p.post_smooth, false);
+    return smooth_coarse<T>(mg, l, x, b, mg->p.post_smooth, false);
 }
 
 // mg_cycle at the fine level: x = M^-1 b for fine fields of precision T
@@ -1460,7 +1522,7 @@ template <typename T>
 smg_status cycle_fine(smg_mg* mg, smg_field* x, const smg_field* b) {
     smg_context* ctx = mg->ctx;
     const int last = (int)mg->lv.size() - 1;
-    SMG_TRY(mr_fine<T>(mg, x, b, mg->p.pre_smooth, true));
+    SMG_TRY(smooth_fine<T>(mg, x, b, mg->p.pre_smooth, true));
     CoarseWork& nw = mg->cw[1];
     SMG_TRY(restrict_to<T>(mg, 0, mg->f_r->data, nw.b));
     SMG_TRY(cycle_coarse<T>(mg, 1, nw.x, nw.b));
@@ -1477,7 +1539,7 @@ smg_status cycle_fine(smg_mg* mg, smg_field* x, const smg_field* b) {
         count_launch(ctx);
     }
     SMG_TRY(prolong_to<T>(mg, 0, nw.x, x->data, 1));
-    return mr_fine<T>(mg, x, b, mg->p.post_smooth, false);
+    return smooth_fine<T>(mg, x, b, mg->p.post_smooth, false);
 }
 
 // ------------------------------------------------------------ setup
@@ -1869,6 +1931,67 @@ smg_status smg_mg_apply_internal(smg_mg* mg, const smg_field* b, smg_field* x) {
 
 smg_precision smg_mg_precision(const smg_mg* mg) { return mg->p.precision; }
 
+smg_status smg_mg_level0_L(const smg_mg* mg, int* L) {
+    *L = mg->lv[0].nx;
+    return SMG_OK;
+}
+
+namespace {
+
+// estimate_lambda_max (src/smoother.cpp:43-60) of the level-l operator in
+// FP64: niter power steps from random_vec(dim, std::mt19937(12345)), with
+// lambda = ||A v|| of the last step.  Level-l vectors use the reference's
+// dof order (fine: 2 * site + spin, coarse: site * ndof + j).
+smg_status lambda_max_level(smg_mg* mg, int l, int niter, double* out) {
+    smg_context* ctx = mg->ctx;
+    SMG_TRY(ensure_work(mg, 1, SMG_F64));
+    const Level& L = mg->lv[l];
+    const int64_t dim = (int64_t)L.nsites * L.ndof;
+    std::vector<double> h(2 * dim);
+    SMG_TRY(smg_host_random_vec(dim, 12345u, h.data()));
+    double* sc = lvl_scal(mg, l);
+    SMG_TRY(smg_host_stage_reserve(ctx, 64));
+    VecView<double> v, Av;
+    smg_field* fv0 = mg->f_r;
+    smg_field* fAv = mg->f_Ar;
+    if (l == 0) {
+        SMG_TRY(smg_field_upload(fv0, h.data()));
+        v = flat(fview<double>(fv0));
+        Av = flat(fview<double>(fAv));
+    } else {
+        CoarseWork& w = mg->cw[l];
+        SMG_CUDA(ctx, cudaMemcpyAsync(w.x, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                      ctx->stream));
+        v = flat(cview<double>(w.x, L, 1));
+        Av = flat(cview<double>(w.Ar, L, 1));
+    }
+    auto scale_into = [&](VecView<double> dst, const cx<double>* src) {
+        k_vconvert_scaled<double, double><<<vec_grid(dst.nsites, 1), vec_block(1), 0, ctx->stream>>>(dst, src, sc,
+                                                                                                    1);
+        count_launch(ctx);
+    };
+    SMG_TRY(vreduce<double>(ctx, v, nullptr, VR_NORM, sc));
+    scale_into(v, v.p);
+    double lam = 0;
+    for (int i = 0; i < niter; ++i) {
+        if (l == 0)
+            SMG_TRY(level_apply_fine<double>(mg, fv0, fAv, nullptr, nullptr));
+        else
+            SMG_TRY(coarse_apply<double>(mg, l, cview<double>(v.p, L, 1), Av.p, 0, nullptr, nullptr));
+        SMG_TRY(vreduce<double>(ctx, Av, nullptr, VR_NORM, sc));
+        SMG_CUDA(ctx, cudaMemcpyAsync(ctx->host_stage, sc, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        lam = std::sqrt(ctx->host_stage[0]);
+        if (lam < 1e-30) break;
+        scale_into(v, Av.p);
+    }
+    SMG_CHECK_LAUNCH(ctx);
+    *out = lam;
+    return SMG_OK;
+}
+
+}  // namespace
+
 // Reads (and clears) the persistent coarsest CG's error flag: SMG_TIMEOUT if a
 // bounded grid-barrier wait ran out since the last check.  Synchronises.
 smg_status smg_mg_check_device_error(smg_mg* mg) {
@@ -2135,6 +2258,31 @@ SMG_API smg_status smg_mg_coarse_apply_host(smg_mg* mg, int level, const double*
     SMG_TRY(coarse_apply<double>(mg, level, cview<double>(w.x, L, 1), (cx<double>*)w.Ar, 0, nullptr, nullptr));
     SMG_CUDA(ctx, cudaMemcpyAsync(out, w.Ar, b, cudaMemcpyDeviceToHost, ctx->stream));
     SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_estimate_lambda_max(smg_mg* mg, int level, int niter, double* lambda) {
+    if (!mg || !lambda || niter < 0 || level < 0 || level >= (int)mg->lv.size()) return SMG_BAD_ARG;
+    return lambda_max_level(mg, level, niter, lambda);
+}
+
+SMG_API smg_status smg_mg_set_symmetric(smg_mg* mg, double damping, double* omega) {
+    if (!mg || !std::isfinite(damping)) return SMG_BAD_ARG;
+    const int nl = (int)mg->lv.size();
+    std::vector<double> om(nl - 1, 0.0);
+    if (damping > 0) {
+        for (int l = 0; l + 1 < nl; ++l) {
+            double lmax = 0;
+            SMG_TRY(lambda_max_level(mg, l, 30, &lmax));
+            if (!(lmax > 0) || !std::isfinite(lmax))
+                return smg_fail(mg->ctx, SMG_BREAKDOWN, "set_symmetric: lambda_max estimate is not positive");
+            om[l] = damping / lmax;
+        }
+    }
+    for (int l = 0; l + 1 < nl; ++l) mg->lv[l].rich_omega = om[l];
+    drop_graph(mg);  // a captured cycle holds the old smoother
+    if (omega)
+        for (int l = 0; l + 1 < nl; ++l) omega[l] = om[l];
     return SMG_OK;
 }
 

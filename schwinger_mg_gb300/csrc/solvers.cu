@@ -10,14 +10,11 @@
 // right-hand side; a stopped rhs gets alpha = beta = 0 from then on, so the
 // remaining ones keep iterating in the same launches.  The host reads the
 // number of active right-hand sides every `kCheckEvery` iterations only.
-#include "smg_internal.h"
-#include "reduce.cuh"
+#include "krylov.cuh"
 
 #include <algorithm>
 #include <cmath>
 
-smg_status smg_dslash(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, double* norm2_dev);
-smg_status smg_norm2_dev(const smg_field* a, double* out_dev);
 
 namespace {
 
@@ -136,25 +133,6 @@ __global__ void k_cg_p(const CgState s, const cx<T>* __restrict__ r, cx<T>* __re
         p[i] = r[i] + be * p[i];
     }
 }
-
-template <typename T>
-__global__ void k_residual(const cx<T>* __restrict__ b, const cx<T>* __restrict__ Ax, cx<T>* __restrict__ r,
-                           int64_t n) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) r[i] = b[i] - Ax[i];
-}
-
-struct FieldSet {
-    std::vector<smg_field*> f;
-    ~FieldSet() {
-        for (auto* p : f) smg_field_destroy(p);
-    }
-    smg_status add(const smg_field* proto, smg_field** out) {
-        SMG_TRY(smg_field_alloc_like(proto, proto->prec, out));
-        f.push_back(*out);
-        return SMG_OK;
-    }
-};
 
 template <typename T>
 smg_status cg_run(smg_dirac* d, const smg_field* b, smg_field* x, int max_iter, double tol, smg_solve_result* res) {
@@ -292,8 +270,6 @@ SMG_API smg_status smg_cg_solve(smg_dirac* d, const smg_field* rhs, smg_field* x
 // All scalars stay on the device; the host reads the per-rhs residuals once
 // per iteration to apply the stop rule.
 // =====================================================================
-#include "vec.cuh"
-
 smg_status smg_mg_apply_internal(smg_mg* mg, const smg_field* b, smg_field* x);
 smg_precision smg_mg_precision(const smg_mg* mg);
 smg_status smg_mg_check_device_error(smg_mg* mg);
@@ -453,37 +429,6 @@ __global__ void __launch_bounds__(256) k_gcr_update(GcrScalars sc, VecView<T> x,
         }
     }
     block_reduce_finalise<1>(v, partials, ticket, nrhs, FinGcr{sc});
-}
-
-template <typename T>
-VecView<T> fv(const smg_field* f) {
-    VecView<T> v;
-    v.p = (cx<T>*)f->data;
-    v.nsites = f->g.V;
-    v.nrhs = f->nrhs;
-    v.ndof = 2;
-    return v;
-}
-
-template <typename T>
-smg_status apply_A(smg_dirac* d, const smg_field* in, smg_field* tmp, smg_field* out) {
-    SMG_TRY(smg_dslash(d, false, in, tmp, nullptr));
-    return smg_dslash(d, true, tmp, out, nullptr);
-}
-
-template <typename T>
-smg_status reduce_into(smg_context* ctx, VecView<T> a, const cx<T>* b, int mode, double* out) {
-    ReduceLaunch rl = reduce_launch(a.nsites, a.nrhs);
-    SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * a.nrhs * 3));
-    if (mode == VR_DOT)
-        k_vreduce<T, VR_DOT><<<rl.grid, rl.block, 0, ctx->stream>>>(a, b, ctx->red.partials, ctx->red.tickets, out);
-    else if (mode == VR_NORM)
-        k_vreduce<T, VR_NORM><<<rl.grid, rl.block, 0, ctx->stream>>>(a, b, ctx->red.partials, ctx->red.tickets, out);
-    else
-        k_vreduce<T, VR_DOTNORM><<<rl.grid, rl.block, 0, ctx->stream>>>(a, b, ctx->red.partials, ctx->red.tickets, out);
-    count_launch(ctx);
-    SMG_CHECK_LAUNCH(ctx);
-    return SMG_OK;
 }
 
 // Workspace of one GCR solve: residual, preconditioned residual, A z, the

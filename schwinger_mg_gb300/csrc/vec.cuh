@@ -149,6 +149,24 @@ __global__ void __launch_bounds__(256) k_mr_update(VecView<T> x, cx<T>* __restri
     }
 }
 
+// Richardson step with a fixed real omega (reference src/smoother.cpp:64-73):
+// x += omega r, r -= omega Ar.  The residual is carried recursively, so a step
+// costs one operator application as in the reference, which recomputes
+// r = b - A x instead.
+template <typename T>
+__global__ void k_rich_update(VecView<T> x, cx<T>* __restrict__ r, const cx<T>* __restrict__ Ar, T omega) {
+    const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
+    const int s = blockIdx.x * blockDim.y + threadIdx.y;
+    if (rhs >= x.nrhs || s >= x.nsites) return;
+    const int64_t base = x.idx(s, rhs, 0);
+    const int ds = x.dstride();
+    for (int d = 0; d < x.ndof; ++d) {
+        const cx<T> ri = r[base + (int64_t)d * ds];
+        x.p[base + (int64_t)d * ds] = x.p[base + (int64_t)d * ds] + omega * ri;
+        r[base + (int64_t)d * ds] = ri - omega * Ar[base + (int64_t)d * ds];
+    }
+}
+
 // r = b - Ax
 template <typename T>
 __global__ void k_vsub(cx<T>* __restrict__ r, const cx<T>* __restrict__ b, const cx<T>* __restrict__ Ax, int64_t n) {

@@ -88,19 +88,68 @@ def hmc_case(ref, name, L, beta, m, r, csw, gseed, seed, n_steps, omelyan, n_tra
     print("wrote", name, out[:, :2].tolist())
 
 
+def solvers_case(ref, name, L, beta, m, r, csw, gseed, seed, null_iters=5):
+    """PCG (plain with a start vector, and with the symmetric MG), FGMRES (with MG and
+    unpreconditioned, Ritz harvesting on), the Richardson/MR smoothers, lambda_max,
+    set_symmetric and the pseudofermion action, all from the reference."""
+    U = gauge_normal(L, beta, gseed).reshape(-1)
+    n = 2 * L * L
+    b = ref.random_vecs(1, n, seed + 1)
+    x0 = ref.random_vecs(1, n, seed + 2)
+    lam = ref.estimate_lambda_max(U, m, r, csw, 0.0, 30)
+    omega = 0.8 / lam
+    rich = ref.richardson_smooth(U, m, r, csw, 0.0, b, np.zeros(n, complex), 4, omega)
+    rich_x0 = ref.richardson_smooth(U, m, r, csw, 0.0, b, x0, 3, omega)
+    mr_x0 = ref.mr_smooth(U, m, r, csw, 0.0, b, x0, 4)
+    params = O.RefMGParams(2, 4, 4, 0, null_iters, 1, 3, 3, 0)
+    pre_sym, om = ref.mg_precondition_sym(U, m, r, csw, 0.0, params, seed, 0.8, b)
+    pcg_x, pcg_it, pcg_res = ref.cg_precond(U, m, r, csw, 0.0, params, seed, 0.8, b, None, 500, 1e-10)
+    cgx0_x, cgx0_it, cgx0_res = ref.cg_precond(U, m, r, csw, 0.0, None, 0, 0.0, b, x0, 2000, 1e-10)
+    fm_x, fm_it, fm_res, fm_ritz = ref.fgmres(U, m, r, csw, 0.0, params, seed, b, 4, 200, 1e-10, 2)
+    fp_x, fp_it, fp_res, fp_ritz = ref.fgmres(U, m, r, csw, 0.0, None, 0, b, 12, 2000, 1e-10, 4)
+    S, X = ref.fermion_action(U, m, r, csw, 0.0, b, 2000, 1e-10)
+    np.savez_compressed(OUT / f"{name}.npz", L=L, beta=beta, m=m, r=r, csw=csw, gseed=gseed, seed=seed,
+                        null_iters=null_iters, U=U, b=b, x0=x0, lam=lam, omega=omega, rich4=rich, rich3_x0=rich_x0,
+                        mr4_x0=mr_x0, sym_omega=om, sym_precondition=pre_sym, pcg_x=pcg_x, pcg_iters=pcg_it,
+                        pcg_res=pcg_res, cgx0_x=cgx0_x, cgx0_iters=cgx0_it, cgx0_res=cgx0_res, fgm_mg_x=fm_x,
+                        fgm_mg_iters=fm_it, fgm_mg_res=fm_res, fgm_mg_ritz=fm_ritz, fgm_x=fp_x, fgm_iters=fp_it,
+                        fgm_res=fp_res, fgm_ritz=fp_ritz, action=S, action_X=X)
+    print("wrote", name, "lambda", lam, "pcg", pcg_it, "cg x0", cgx0_it, "fgmres mg", fm_it, fm_ritz, "fgmres",
+          fp_it, fp_ritz)
+
+
+def gauge_files_case(ref, name, L, beta, mass, gseed):
+    """A configuration written by the reference's save_gauge ("SWNG") and GaugeField::save (raw)."""
+    U = gauge_normal(L, beta, gseed).reshape(-1)
+    assert ref.save_gauge(U, beta, mass, OUT / f"{name}.swng", OUT / f"{name}.raw")
+    print("wrote", name)
+
+
+CASES = {
+    "dirac_L8_wilson": lambda ref: dirac_case(ref, "dirac_L8_wilson", 8, 2.0, 0.3, 1.0, 0.0, 0.0, 11, 12),
+    "dirac_L16_clover_twist": lambda ref: dirac_case(ref, "dirac_L16_clover_twist", 16, 2.0, -0.05, 1.0, 1.0, 0.2,
+                                                     21, 22),
+    "dirac_L32_config1": lambda ref: dirac_case(ref, "dirac_L32_config1", 32, 2.0, 0.1, 1.0, 1.0, 0.0, 31, 32),
+    "cg_force_L32_config1": lambda ref: cg_force_case(ref, "cg_force_L32_config1", 32, 2.0, 0.1, 1.0, 1.0, 0.0, 31,
+                                                      33),
+    "cg_force_L16_wilson": lambda ref: cg_force_case(ref, "cg_force_L16_wilson", 16, 4.0, 0.2, 1.0, 0.0, 0.0, 41, 42),
+    "mg_L16_bs4_k4": lambda ref: mg_case(ref, "mg_L16_bs4_k4", 16, 2.0, 0.1, 1.0, 1.0, 0.0, 51, 4, 4, 5, 52),
+    "hmc_L8_omelyan": lambda ref: hmc_case(ref, "hmc_L8_omelyan", 8, 4.0, 0.1, 1.0, 1.0, 61, 62, 5, 1, 3),
+    "hmc_L8_leapfrog": lambda ref: hmc_case(ref, "hmc_L8_leapfrog", 8, 4.0, 0.1, 1.0, 1.0, 63, 64, 8, 0, 2),
+    "solvers_L16": lambda ref: solvers_case(ref, "solvers_L16", 16, 2.0, 0.1, 1.0, 1.0, 71, 72),
+    "gauge_L8": lambda ref: gauge_files_case(ref, "gauge_L8", 8, 3.0, 0.05, 81),
+}
+
+
 def main():
+    """python make_golden.py [case ...]: regenerates the named fixtures (all without arguments)."""
     O.build(ref=True)
     ref = O.ref()
     if ref is None:
         raise SystemExit("the reference shim is needed to generate fixtures")
-    dirac_case(ref, "dirac_L8_wilson", 8, 2.0, 0.3, 1.0, 0.0, 0.0, 11, 12)
-    dirac_case(ref, "dirac_L16_clover_twist", 16, 2.0, -0.05, 1.0, 1.0, 0.2, 21, 22)
-    dirac_case(ref, "dirac_L32_config1", 32, 2.0, 0.1, 1.0, 1.0, 0.0, 31, 32)
-    cg_force_case(ref, "cg_force_L32_config1", 32, 2.0, 0.1, 1.0, 1.0, 0.0, 31, 33)
-    cg_force_case(ref, "cg_force_L16_wilson", 16, 4.0, 0.2, 1.0, 0.0, 0.0, 41, 42)
-    mg_case(ref, "mg_L16_bs4_k4", 16, 2.0, 0.1, 1.0, 1.0, 0.0, 51, 4, 4, 5, 52)
-    hmc_case(ref, "hmc_L8_omelyan", 8, 4.0, 0.1, 1.0, 1.0, 61, 62, 5, 1, 3)
-    hmc_case(ref, "hmc_L8_leapfrog", 8, 4.0, 0.1, 1.0, 1.0, 63, 64, 8, 0, 2)
+    names = sys.argv[1:] or list(CASES)
+    for nm in names:
+        CASES[nm](ref)
 
 
 if __name__ == "__main__":

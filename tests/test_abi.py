@@ -80,3 +80,32 @@ def test_context_without_gpu_reports_device_error():
     h = C.c_void_p()
     st = _lib.lib().smg_context_create(0, None, C.byref(h))
     assert st == _lib.DEVICE_ERROR
+
+
+def test_cpp_dropin_header_compiles(tmp_path):
+    """include/smg_gpu.hpp (the reference's C++ call shapes over the C ABI) compiles as C++17."""
+    import shutil
+    import subprocess
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    src = tmp_path / "use.cpp"
+    src.write_text(
+        '#include "smg_gpu.hpp"\n'
+        "double use(const smg::DiracOp& D, smg::MGHierarchy& mg, const smg::Vec& b) {\n"
+        "    smg::Vec x(b.size());\n"
+        "    smg::mr_smooth(D, x, b, 4);\n"
+        "    smg::richardson_smooth(D, x, b, 4, 0.8 / smg::estimate_lambda_max(D, 30));\n"
+        "    mg.set_symmetric(0.8);\n"
+        "    auto c = smg::cg_solve_precond(D, D.lat.ndof, b, mg, 100, 1e-10);\n"
+        "    auto f = smg::fgmres_solve_mg(D, D.lat.ndof, b, &mg, 30, 300, 1e-10);\n"
+        "    smg::PseudofermionAction act(D, &mg);\n"
+        "    double S = act.forward(b, 1000, 1e-10);\n"
+        "    std::array<smg::RVec, 2> F;\n"
+        "    act.backward(F);\n"
+        "    return S + c.final_residual + f.final_residual + F[0][0];\n"
+        "}\n")
+    r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-I", str(ROOT / "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

@@ -71,3 +71,43 @@ def test_force_finite_differences(smg_gpu):
     D.refresh()
     rel = max(errs) / max(vals)
     assert rel < 1e-7, f"force vs finite differences: rel {rel:.3e}"
+
+
+def test_force_finite_differences_L128_64_links(smg_gpu):
+    """Differentiated-HMC check at L = 128, beta = 4, m = 0.1, c_sw = 1: eps = 1e-5 on 64
+    seeded links, relative error per link below 1e-7.  S(theta') - S(theta) is formed as
+    -X'^dag (A' - A) X = -[(D X')^dag dX + dX'^dag (D X) + dX'^dag dX] with dv = (D' - D) v:
+    the two operators do identical arithmetic away from the perturbed link, so dv is exactly
+    zero there and the difference keeps the precision of the few sites it lives on."""
+    L, beta, m, csw, eps = 128, 4.0, 0.1, 1.0, 1e-5
+    U = smg_gpu.gauge_normal(L, beta, 4001)
+    lat = smg_gpu.Lattice(L)
+    D = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, U), m, 1.0, csw, 0.0)
+    eta = smg_gpu.random_vec(lat.ndof, 4002)
+    phi = D.apply_dag(eta)
+    X = smg_gpu.cg_solve(D, lat.ndof, phi, 50000, 1e-13).solution
+    F = smg_gpu.fermion_force(D, X)
+    DX = D.apply(X)
+    g2 = smg_gpu.GaugeField(lat, U)
+    D2 = smg_gpu.DiracOp(lat, g2, m, 1.0, csw, 0.0)
+    rng = np.random.default_rng(4003)
+    links = [(int(rng.integers(2)), int(rng.integers(lat.V))) for _ in range(64)]
+
+    def delta_S(Uv):
+        g2.set_links(Uv)
+        D2.refresh()
+        Xp = smg_gpu.cg_solve(D2, lat.ndof, phi, 50000, 1e-13).solution
+        dX = D2.apply(X) - DX
+        DXp = D.apply(Xp)
+        dXp = D2.apply(Xp) - DXp
+        return -float(np.real(np.vdot(DXp, dX) + np.vdot(dXp, DX) + np.vdot(dXp, dX)))
+
+    rel = []
+    for mu, s in links:
+        Up = U.copy()
+        Up[mu, s] *= np.exp(1j * eps)
+        Um = U.copy()
+        Um[mu, s] *= np.exp(-1j * eps)
+        fd = -(delta_S(Up) - delta_S(Um)) / (2 * eps)
+        rel.append(abs(F[mu, s] - fd) / abs(F[mu, s]))
+    assert max(rel) < 1e-7, f"force vs finite differences at L=128: max rel {max(rel):.3e}"

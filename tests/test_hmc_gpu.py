@@ -144,3 +144,24 @@ def test_hmc_bad_parameters(smg_gpu):
     g = smg_gpu.GaugeField(lat)
     with pytest.raises(smg_gpu.SmgError):
         smg_gpu.hmc_trajectory(g, 0.1, 1.0, smg_gpu.hmc_params(4.0, n_steps=0), smg_gpu.Rng(1))
+
+
+def test_gauge_file_round_trip_through_device(smg_gpu, tmp_path):
+    """smg_gauge_save writes the device links and their plaquette; smg_gauge_load reads them back."""
+    from conftest import GOLDEN
+
+    lat = smg_gpu.Lattice(8)
+    g = smg_gpu.GaugeField(lat)
+    _, hdr = smg_gpu.load_gauge(GOLDEN / "gauge_L8.swng")
+    lib = smg_gpu.lib()
+    from schwinger_mg_gb300 import _lib as _L
+    import ctypes as C
+
+    h = _L.GaugeHeader()
+    _L.check(lib.smg_gauge_load(g.h, str(GOLDEN / "gauge_L8.swng").encode(), C.byref(h)), "smg_gauge_load")
+    assert abs(g.avg_plaq() - hdr["avg_plaq"]) < 1e-14
+    smg_gpu.save_gauge(g, h.beta, h.mass, tmp_path / "dev.swng")
+    V, h2 = smg_gpu.load_gauge(tmp_path / "dev.swng", 8)
+    U, _ = smg_gpu.load_gauge(GOLDEN / "gauge_L8.swng", 8)
+    np.testing.assert_allclose(V, U, rtol=0, atol=1e-15)
+    assert h2["beta"] == h.beta and abs(h2["avg_plaq"] - hdr["avg_plaq"]) < 1e-14
