@@ -67,6 +67,19 @@ typedef enum {
     SMG_OP_G5D = 3      /* DiracOp::apply_g5D    dirac.h:145 */
 } smg_operator;
 
+/* Even-odd (Schur complement) operators (reference EvenOddDiracOp,
+ * src/dirac.h:190-553).  They act on full fields whose odd half holds the
+ * reference's odd-site half vector (and even half its even-site vector):
+ * half-vector index i = eo_index[s] = (x + L y) / 2 is the site order within
+ * a parity half of a field. */
+typedef enum {
+    SMG_EO_SCHUR = 0,           /* M = D_oo - D_oe D_ee^-1 D_eo   apply_schur          dirac.h:425 */
+    SMG_EO_SCHUR_DAG = 1,       /* M^dag = g5 M(-mu) g5           apply_schur_dag      dirac.h:430 */
+    SMG_EO_SCHUR_DAG_SCHUR = 2, /* M^dag M                        apply_schur_dag_schur dirac.h:441 */
+    SMG_EO_HOP_EO = 3,          /* even half -> odd half hopping  apply_eo             dirac.h:252 */
+    SMG_EO_HOP_OE = 4           /* odd half -> even half hopping  apply_oe             dirac.h:257 */
+} smg_eo_operator;
+
 typedef struct smg_context smg_context;
 typedef struct smg_gauge smg_gauge;
 typedef struct smg_dirac smg_dirac;
@@ -234,6 +247,28 @@ SMG_API smg_status smg_richardson_smooth(smg_dirac* d, const smg_field* b, smg_f
 /* estimate_lambda_max of A = D^dag D (src/smoother.cpp:43-60): niter power
  * steps from random_vec(2V, std::mt19937(12345)); lambda = ||A v|| of the last. */
 SMG_API smg_status smg_estimate_lambda_max(smg_dirac* d, int niter, double* lambda);
+
+/* --------------------------------------------------------------- even-odd */
+
+/* Applies an even-odd operator: Schur operators read the odd half of src and
+ * write the odd half of dst; the hops read one half and write the other. */
+SMG_API smg_status smg_eo_apply(smg_dirac* d, smg_eo_operator op, const smg_field* src, smg_field* dst);
+/* EvenOddDiracOp::reconstruct (src/dirac.h:527-540): with x_o in the odd half
+ * of x, writes x_e = D_ee^-1 (phi_e - D_oe x_o) into its even half; phi ==
+ * NULL gives reconstruct_full (x_e = -D_ee^-1 D_oe x_o, :499-508). */
+SMG_API smg_status smg_eo_reconstruct(smg_dirac* d, const smg_field* phi, smg_field* x);
+/* EvenOddDiracOp::log_det_ee (src/dirac.h:511-521): Re log det D_ee. */
+SMG_API smg_status smg_eo_logdet_ee(smg_dirac* d, double* logdet);
+/* cg_solve on M^dag M over the odd halves (the e/o HMC solve,
+ * src/hmc_trajectory.cpp:70-104): rhs and x are full fields of which the odd
+ * halves are used; the even half of x is set to zero. */
+SMG_API smg_status smg_eo_cg_solve(smg_dirac* d, const smg_field* rhs, smg_field* x, int max_iter, double tol,
+                                   smg_solve_result* res);
+/* eo_fermion_force (src/hmc_forces.cpp:812-867): F = -dS/dtheta for
+ * S = phi_o^dag (M^dag M)^-1 phi_o - 2 log det D_ee at x_o = the odd half of
+ * X (single-RHS F64); y_o = M x_o and the even-site reconstructions are
+ * recomputed on the device.  force is 2*V doubles [mu][s]. */
+SMG_API smg_status smg_eo_fermion_force(smg_dirac* d, const smg_field* X, double* force);
 
 /* -------------------------------------------------------------- multigrid */
 
@@ -411,6 +446,10 @@ typedef struct {
     double mu_t;
     int force_accept;
     int mixed_precision;
+    int use_eo;  /* the reference's even-odd path: Schur-complement pseudofermion
+                    phi_o = M^dag eta_o, CG on M^dag M, eo_fermion_force and
+                    H += -2 log det D_ee (src/hmc_trajectory.cpp:59-165); with
+                    n_inner == 0 it integrates with leapfrog as the reference does */
 } smg_hmc_params;
 
 /* HMCResult (reference src/hmc.h:121-129) plus the plaquette after the
@@ -421,6 +460,7 @@ typedef struct {
     int total_cg_iters;
     int solves;
     double plaquette;
+    double dLD;  /* change of -2 log det D_ee (even-odd path; 0 otherwise) */
 } smg_hmc_result;
 
 SMG_API smg_status smg_hmc_params_default(smg_hmc_params* p);

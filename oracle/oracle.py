@@ -363,16 +363,58 @@ class Ref(_Lib):
         return x, it, res.value
 
     def hmc_trajectories(self, U, m, r, beta, tau, n_steps, omelyan, cg_maxiter, cg_tol, csw, mu, force_accept,
-                         seed, n_traj):
+                         seed, n_traj, use_eo=False):
         """The reference's hmc_trajectory n_traj times with one std::mt19937(seed); returns the
-        final links and per trajectory (accepted, dH, dKE, dSG, dSF, cg iterations, plaquette)."""
+        final links and per trajectory (accepted, dH, dKE, dSG, dSF, cg iterations, plaquette)
+        and, with use_eo, dLD as an eighth column."""
         U = _c(U).copy()
         out = np.zeros(8 * n_traj)
         self.lib.ref_hmc_trajectories(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(beta),
                                       C.c_double(tau), C.c_int(n_steps), C.c_int(omelyan), C.c_int(cg_maxiter),
                                       C.c_double(cg_tol), C.c_double(csw), C.c_double(mu), C.c_int(force_accept),
-                                      C.c_uint(seed), C.c_int(n_traj), _p(out))
-        return U, out.reshape(n_traj, 8)[:, :7]
+                                      C.c_uint(seed), C.c_int(n_traj), _p(out), C.c_int(int(use_eo)))
+        return U, out.reshape(n_traj, 8)[:, :8 if use_eo else 7]
+
+    def eo_apply(self, U, m, r, csw, mu, op, src):
+        U, src = _c(U), _c(src)
+        L = self._L(U)
+        out = np.empty(L * L, dtype=np.complex128)
+        self.lib.ref_eo_apply(C.c_int(L), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw), C.c_double(mu),
+                              C.c_int(op), _p(src), _p(out))
+        return out
+
+    def eo_reconstruct(self, U, m, r, csw, mu, x_o, phi=None):
+        U, x_o = _c(U), _c(x_o)
+        L = self._L(U)
+        out = np.empty(2 * L * L, dtype=np.complex128)
+        keep = _c(phi) if phi is not None else None
+        self.lib.ref_eo_reconstruct(C.c_int(L), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                                    C.c_double(mu), _p(x_o), _p(keep) if keep is not None else None, _p(out))
+        return out
+
+    def eo_logdet(self, U, m, r, csw, mu):
+        U = _c(U)
+        f = self.lib.ref_eo_logdet
+        f.restype = C.c_double
+        return f(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw), C.c_double(mu))
+
+    def eo_cg(self, U, m, r, csw, mu, phi_o, max_iter, tol):
+        U, phi_o = _c(U), _c(phi_o)
+        x = np.empty_like(phi_o)
+        res = C.c_double(0)
+        f = self.lib.ref_eo_cg
+        f.restype = C.c_int
+        it = f(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw), C.c_double(mu),
+               _p(phi_o), _p(x), C.c_int(max_iter), C.c_double(tol), C.byref(res))
+        return x, it, res.value
+
+    def eo_force(self, U, m, r, csw, mu, x_o):
+        U, x_o = _c(U), _c(x_o)
+        L = self._L(U)
+        F = np.empty(2 * L * L)
+        self.lib.ref_eo_force(C.c_int(L), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw), C.c_double(mu),
+                              _p(x_o), _p(F))
+        return F
 
     def richardson_smooth(self, U, m, r, csw, mu, b, x0, niter, omega):
         U, b = _c(U), _c(b)

@@ -318,7 +318,7 @@ void ref_pseudofermion(int L, const double* U, double m, double r, double csw, d
 // average plaquette after the trajectory.
 void ref_hmc_trajectories(int L, double* U, double mass, double r, double beta, double tau, int n_steps,
                           int omelyan, int cg_maxiter, double cg_tol, double c_sw, double mu_t, int force_accept,
-                          unsigned seed, int n_traj, double* out) {
+                          unsigned seed, int n_traj, double* out, int use_eo) {
     World w(L, U);
     HMCParams hp{};
     hp.beta = beta;
@@ -329,7 +329,7 @@ void ref_hmc_trajectories(int L, double* U, double mass, double r, double beta, 
     hp.use_mg = false;
     hp.c_sw = c_sw;
     hp.mu_t = mu_t;
-    hp.use_eo = false;
+    hp.use_eo = use_eo != 0;
     hp.omelyan = omelyan != 0;
     hp.force_accept = force_accept != 0;
     std::mt19937 rng(seed);
@@ -342,7 +342,7 @@ void ref_hmc_trajectories(int L, double* U, double mass, double r, double beta, 
         out[8 * t + 4] = res.dSF;
         out[8 * t + 5] = res.total_cg_iters;
         out[8 * t + 6] = w.g.avg_plaq();
-        out[8 * t + 7] = 0.0;
+        out[8 * t + 7] = res.dLD;
     }
     for (int mu = 0; mu < 2; ++mu)
         for (int s = 0; s < w.lat.V; ++s) {
@@ -471,6 +471,69 @@ int ref_load_gauge(int L, const char* path, double* U, double* hdr) {
     hdr[1] = h.mass;
     hdr[2] = h.avg_plaq;
     return 1;
+}
+
+
+// EvenOddDiracOp (src/dirac.h:190-553) on half vectors of 2 * V/2 complex:
+// op 0 apply_schur, 1 apply_schur_dag, 2 apply_schur_dag_schur, 3 apply_eo, 4 apply_oe
+void ref_eo_apply(int L, const double* U, double m, double r, double csw, double mu, int op, const double* src,
+                  double* dst) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    EvenOddDiracOp eo(D);
+    const int nh = 2 * w.lat.V_half;
+    Vec in = to_vec(src, nh), out(nh);
+    if (op == 0) eo.apply_schur(in, out);
+    else if (op == 1) eo.apply_schur_dag(in, out);
+    else if (op == 2) eo.apply_schur_dag_schur(in, out);
+    else if (op == 3) eo.apply_eo(in, out);
+    else eo.apply_oe(in, out);
+    from_vec(out, dst);
+}
+
+// reconstruct(x_o, phi) (src/dirac.h:527-540), or reconstruct_full(x_o) when phi is NULL
+void ref_eo_reconstruct(int L, const double* U, double m, double r, double csw, double mu, const double* x_o,
+                        const double* phi, double* full) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    EvenOddDiracOp eo(D);
+    const int nh = 2 * w.lat.V_half;
+    Vec x = phi ? eo.reconstruct(to_vec(x_o, nh), to_vec(phi, w.lat.ndof)) : eo.reconstruct_full(to_vec(x_o, nh));
+    from_vec(x, full);
+}
+
+double ref_eo_logdet(int L, const double* U, double m, double r, double csw, double mu) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    return EvenOddDiracOp(D).log_det_ee();
+}
+
+// cg_solve on apply_schur_dag_schur (src/hmc_trajectory.cpp:70-104); returns iterations
+int ref_eo_cg(int L, const double* U, double m, double r, double csw, double mu, const double* phi_o, double* x_o,
+              int max_iter, double tol, double* final_res) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    EvenOddDiracOp eo(D);
+    const int nh = 2 * w.lat.V_half;
+    OpApply A = [&eo](const Vec& s, Vec& d) { eo.apply_schur_dag_schur(s, d); };
+    CGResult res = cg_solve(A, nh, to_vec(phi_o, nh), max_iter, tol);
+    from_vec(res.solution, x_o);
+    if (final_res) *final_res = res.final_residual;
+    return res.iterations;
+}
+
+// eo_fermion_force (src/hmc_forces.cpp:812-867) at x_o with y_o = M x_o
+void ref_eo_force(int L, const double* U, double m, double r, double csw, double mu, const double* x_o,
+                  double* F) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    EvenOddDiracOp eo(D);
+    const int nh = 2 * w.lat.V_half;
+    Vec x = to_vec(x_o, nh), y(nh);
+    eo.apply_schur(x, y);
+    std::array<RVec, 2> f;
+    eo_fermion_force(D, eo, x, y, f);
+    for (int mu_ = 0; mu_ < 2; ++mu_) std::memcpy(F + (size_t)mu_ * w.lat.V, f[mu_].data(), sizeof(double) * w.lat.V);
 }
 
 }  // extern "C"

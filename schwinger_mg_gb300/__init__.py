@@ -30,6 +30,7 @@ from .api import (  # noqa: F401
     mg_params,
     Context,
     DiracOp,
+    EvenOddDiracOp,
     Field,
     GaugeField,
     Lattice,

@@ -15,6 +15,7 @@ LIB_PATH = Path(__file__).resolve().parent / "libsmg_gpu.so"
 OK, NOT_CONVERGED, BREAKDOWN, NONFINITE, BAD_ARG, DEVICE_ERROR, TIMEOUT, NO_MEMORY, UNSUPPORTED, IO_ERROR = range(10)
 F64, F32, F16 = 0, 1, 2
 OP_D, OP_DDAG, OP_DDAGD, OP_G5D = 0, 1, 2, 3
+EO_SCHUR, EO_SCHUR_DAG, EO_SCHUR_DAG_SCHUR, EO_HOP_EO, EO_HOP_OE = 0, 1, 2, 3, 4
 
 
 class SmgLibraryError(RuntimeError):
@@ -45,13 +46,15 @@ class HMCParams(C.Structure):
     """smg_hmc_params (include/smg_gpu.h)."""
     _fields_ = [("beta", C.c_double), ("tau", C.c_double), ("n_steps", C.c_int), ("omelyan", C.c_int),
                 ("n_inner", C.c_int), ("cg_maxiter", C.c_int), ("cg_tol", C.c_double), ("c_sw", C.c_double),
-                ("mu_t", C.c_double), ("force_accept", C.c_int), ("mixed_precision", C.c_int)]
+                ("mu_t", C.c_double), ("force_accept", C.c_int), ("mixed_precision", C.c_int),
+                ("use_eo", C.c_int)]
 
 
 class HMCResult(C.Structure):
     """smg_hmc_result (include/smg_gpu.h)."""
     _fields_ = [("accepted", C.c_int), ("dH", C.c_double), ("dKE", C.c_double), ("dSG", C.c_double),
-                ("dSF", C.c_double), ("total_cg_iters", C.c_int), ("solves", C.c_int), ("plaquette", C.c_double)]
+                ("dSF", C.c_double), ("total_cg_iters", C.c_int), ("solves", C.c_int), ("plaquette", C.c_double),
+                ("dLD", C.c_double)]
 
 
 class MGParams(C.Structure):
@@ -143,6 +146,11 @@ _SIGS = {
     "smg_fgmres_solve": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(SolveResult),
                                _dp, C.POINTER(C.c_int)]),
     "smg_fermion_action": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_double, _dp, C.POINTER(SolveResult)]),
+    "smg_eo_apply": (_st, [_vp, C.c_int, _vp, _vp]),
+    "smg_eo_reconstruct": (_st, [_vp, _vp, _vp]),
+    "smg_eo_logdet_ee": (_st, [_vp, _dp]),
+    "smg_eo_cg_solve": (_st, [_vp, _vp, _vp, C.c_int, C.c_double, C.POINTER(SolveResult)]),
+    "smg_eo_fermion_force": (_st, [_vp, _vp, _dp]),
     "smg_host_gauge_write_swng": (_st, [C.c_char_p, C.c_int, _dp, C.c_double, C.c_double, C.c_double]),
     "smg_host_gauge_read_swng": (_st, [C.c_char_p, C.c_int, C.POINTER(GaugeHeader), _dp]),
     "smg_host_gauge_write_raw": (_st, [C.c_char_p, C.c_int, _dp]),

@@ -286,6 +286,93 @@ class DiracOp(_Handle):
         return self.apply_op(_L.OP_G5D, src, dst)
 
 
+class EvenOddDiracOp:
+    """EvenOddDiracOp (reference src/dirac.h:190-553) on host half-lattice vectors:
+    a half vector holds 2 * V/2 complex values in the reference's even_sites /
+    odd_sites order.  Each call moves the halves into device fields, runs the
+    sm_103a kernels and copies the result back."""
+
+    def __init__(self, D: DiracOp):
+        self.D = D
+        self.lat = D.lat
+        self.ctx = D.ctx
+
+    # host-side layout helpers (scatter / gather_even / gather_odd, dirac.h:449-485)
+    def scatter(self, half_e, half_o) -> np.ndarray:
+        full = np.zeros((self.lat.V, 2), dtype=np.complex128)
+        if half_e is not None:
+            full[self.lat.even_sites] = _as_c128(half_e).reshape(-1, 2)
+        if half_o is not None:
+            full[self.lat.odd_sites] = _as_c128(half_o).reshape(-1, 2)
+        return full.reshape(-1)
+
+    def gather_even(self, full) -> np.ndarray:
+        return _as_c128(full).reshape(-1, 2)[self.lat.even_sites].reshape(-1)
+
+    def gather_odd(self, full) -> np.ndarray:
+        return _as_c128(full).reshape(-1, 2)[self.lat.odd_sites].reshape(-1)
+
+    def _run(self, op, half_e, half_o, out_parity):
+        fs = Field(self.lat, 1, "f64", self.ctx, data=self.scatter(half_e, half_o))
+        fd = Field(self.lat, 1, "f64", self.ctx)
+        _L.check(_L.lib().smg_eo_apply(self.D.h, op, fs.h, fd.h), "smg_eo_apply", self.ctx.h)
+        full = fd.download()
+        return self.gather_odd(full) if out_parity else self.gather_even(full)
+
+    def apply_schur(self, src_o):
+        return self._run(_L.EO_SCHUR, None, src_o, 1)
+
+    def apply_schur_dag(self, src_o):
+        return self._run(_L.EO_SCHUR_DAG, None, src_o, 1)
+
+    def apply_schur_dag_schur(self, src_o):
+        return self._run(_L.EO_SCHUR_DAG_SCHUR, None, src_o, 1)
+
+    def apply_eo(self, src_e):
+        return self._run(_L.EO_HOP_EO, src_e, None, 1)
+
+    def apply_oe(self, src_o):
+        return self._run(_L.EO_HOP_OE, None, src_o, 0)
+
+    def reconstruct(self, x_o, phi=None) -> np.ndarray:
+        """Full solution from x_o: x_e = D_ee^-1 (phi_e - D_oe x_o) (reconstruct /
+        reconstruct_full, dirac.h:499-540); returns the full vector."""
+        fx = Field(self.lat, 1, "f64", self.ctx, data=self.scatter(None, x_o))
+        fp = Field(self.lat, 1, "f64", self.ctx, data=_as_c128(phi)) if phi is not None else None
+        _L.check(_L.lib().smg_eo_reconstruct(self.D.h, fp.h if fp is not None else None, fx.h),
+                 "smg_eo_reconstruct", self.ctx.h)
+        return fx.download()
+
+    def log_det_ee(self) -> float:
+        v = C.c_double(0)
+        _L.check(_L.lib().smg_eo_logdet_ee(self.D.h, C.byref(v)), "smg_eo_logdet_ee", self.ctx.h)
+        return v.value
+
+    def generate_pseudofermion_eo(self, rng: "Rng") -> np.ndarray:
+        """phi_o = M^dag eta_o with eta_o = random_vec(V, rng) (dirac.h:491-497)."""
+        d = rng.normal(2 * self.lat.V)
+        eta = d[1::2] + 1j * d[0::2]  # random_vec draws each entry's imaginary part first
+        return self.apply_schur_dag(eta)
+
+    def cg_solve(self, phi_o, max_iter: int, tol: float) -> "CGResult":
+        """cg_solve on M^dag M over odd-site half vectors."""
+        b = _as_c128(phi_o).reshape(-1)
+        fb = Field(self.lat, 1, "f64", self.ctx, data=self.scatter(None, b))
+        fx = Field(self.lat, 1, "f64", self.ctx)
+        res = _L.SolveResult()
+        st = _L.lib().smg_eo_cg_solve(self.D.h, fb.h, fx.h, max_iter, tol, C.byref(res))
+        if st not in (_L.OK, _L.NOT_CONVERGED):
+            _L.check(st, "smg_eo_cg_solve", self.ctx.h)
+        return CGResult(self.gather_odd(fx.download()), res.iterations, res.final_residual, res.true_residual)
+
+    def fermion_force(self, x_o) -> np.ndarray:
+        """eo_fermion_force (src/hmc_forces.cpp:812-867) at x_o; returns F[mu][s]."""
+        fx = Field(self.lat, 1, "f64", self.ctx, data=self.scatter(None, x_o))
+        out = np.empty(2 * self.lat.V)
+        _L.check(_L.lib().smg_eo_fermion_force(self.D.h, fx.h, _ptr(out)), "smg_eo_fermion_force", self.ctx.h)
+        return out.reshape(2, self.lat.V)
+
+
 @dataclass
 class CGResult:
     """Mirrors CGResult / FCGResult (reference src/solvers.h:25-35) plus the FP64 true residual."""
@@ -433,14 +520,15 @@ class Rng(_Handle):
 
 def hmc_params(beta: float, tau: float = 1.0, n_steps: int = 10, omelyan: bool = True, n_inner: int = 0,
                cg_maxiter: int = 10000, cg_tol: float = 1e-10, c_sw: float = 0.0, mu_t: float = 0.0,
-               force_accept: bool = False, mixed_precision: bool = False) -> _L.HMCParams:
+               force_accept: bool = False, mixed_precision: bool = False, use_eo: bool = False) -> _L.HMCParams:
     """smg_hmc_params from the reference's HMCParams fields (src/hmc.h:107-119); n_inner > 0
-    selects the nested integrator with n_inner gauge-force steps between fermion-force kicks."""
+    selects the nested integrator with n_inner gauge-force steps between fermion-force kicks;
+    use_eo the reference's even-odd (Schur complement) trajectory."""
     p = _L.HMCParams()
     _L.check(_L.lib().smg_hmc_params_default(C.byref(p)), "smg_hmc_params_default")
     p.beta, p.tau, p.n_steps, p.omelyan, p.n_inner = beta, tau, n_steps, int(omelyan), n_inner
     p.cg_maxiter, p.cg_tol, p.c_sw, p.mu_t = cg_maxiter, cg_tol, c_sw, mu_t
-    p.force_accept, p.mixed_precision = int(force_accept), int(mixed_precision)
+    p.force_accept, p.mixed_precision, p.use_eo = int(force_accept), int(mixed_precision), int(use_eo)
     return p
 
 
@@ -455,6 +543,7 @@ class HMCResult:
     total_cg_iters: int
     solves: int
     plaquette: float
+    dLD: float = 0.0
 
 
 def hmc_trajectory(g: GaugeField, mass: float, wilson_r: float, params: _L.HMCParams, rng: Rng) -> HMCResult:
@@ -463,7 +552,7 @@ def hmc_trajectory(g: GaugeField, mass: float, wilson_r: float, params: _L.HMCPa
     r = _L.HMCResult()
     _L.check(_L.lib().smg_hmc_trajectory(g.h, mass, wilson_r, C.byref(params), rng.h, C.byref(r)),
              "smg_hmc_trajectory", g.ctx.h)
-    return HMCResult(bool(r.accepted), r.dH, r.dKE, r.dSG, r.dSF, r.total_cg_iters, r.solves, r.plaquette)
+    return HMCResult(bool(r.accepted), r.dH, r.dKE, r.dSG, r.dSF, r.total_cg_iters, r.solves, r.plaquette, r.dLD)
 
 
 # ---------------------------------------------------------------- host inputs

@@ -19,6 +19,11 @@ struct smg_rng {
 
 smg_status smg_fermion_force_dev(smg_dirac* d, const smg_field* X, double* F_dev);
 smg_status smg_gauge_force_dev(smg_gauge* gf, double beta, double* F_dev);
+smg_status smg_eo_schur_internal(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, smg_field* tmp,
+                                 double* norm2_dev);
+smg_status smg_eo_force_dev(smg_dirac* d, const smg_field* X, smg_field* chi, smg_field* psi, double* W,
+                            double* F_dev);
+smg_status smg_eo_logdet_dev(smg_dirac* d, double* out_dev);
 
 namespace {
 
@@ -67,17 +72,23 @@ struct Hmc {
     smg_field* phi = nullptr;
     smg_field* X = nullptr;
     smg_field* eta = nullptr;
+    smg_field* chi = nullptr;  // even-odd force scratch
+    smg_field* psi = nullptr;
+    double* W = nullptr;
+    bool eo = false;
     bool stale = false;  // links changed since the clover field and the FP32 links were formed
     int cg_iters = 0, solves = 0;
     smg_status warn = SMG_OK;
 
     ~Hmc() {
         if (ctx) cudaStreamSynchronize(ctx->stream);
-        for (void* q : {(void*)pi, (void*)gf, (void*)ff, (void*)scal, (void*)U_old})
+        for (void* q : {(void*)pi, (void*)gf, (void*)ff, (void*)scal, (void*)U_old, (void*)W})
             if (q) cudaFree(q);
         smg_field_destroy(phi);
         smg_field_destroy(X);
         smg_field_destroy(eta);
+        smg_field_destroy(chi);
+        smg_field_destroy(psi);
         smg_dirac_destroy(d);
     }
 
@@ -95,8 +106,9 @@ struct Hmc {
     smg_status solve() {
         SMG_TRY(refresh());
         smg_solve_result res{};
-        const smg_status st = p.mixed_precision ? smg_cg_solve_mixed(d, phi, X, p.cg_maxiter, p.cg_tol, &res)
-                                                : smg_cg_solve(d, phi, X, p.cg_maxiter, p.cg_tol, &res);
+        const smg_status st = eo                  ? smg_eo_cg_solve(d, phi, X, p.cg_maxiter, p.cg_tol, &res)
+                              : p.mixed_precision ? smg_cg_solve_mixed(d, phi, X, p.cg_maxiter, p.cg_tol, &res)
+                                                  : smg_cg_solve(d, phi, X, p.cg_maxiter, p.cg_tol, &res);
         cg_iters += res.iterations;
         ++solves;
         // the reference warns and carries on when CG stops early (solvers.cpp:55-62)
@@ -109,7 +121,21 @@ struct Hmc {
 
     smg_status fermion_force() {
         SMG_TRY(solve());
+        if (eo) return smg_eo_force_dev(d, X, chi, psi, W, ff);
         return smg_fermion_force_dev(d, X, ff);
+    }
+
+    // -2 log det D_ee (even-odd path with clover; 0 otherwise)
+    smg_status log_det_term(double* ld) {
+        *ld = 0;
+        if (!eo || p.c_sw == 0.0) return SMG_OK;
+        SMG_TRY(refresh());
+        SMG_TRY(smg_eo_logdet_dev(d, scal + 1));
+        double h = 0;
+        SMG_CUDA(ctx, cudaMemcpyAsync(&h, scal + 1, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        *ld = -2.0 * h;
+        return SMG_OK;
     }
 
     smg_status gauge_force() {
@@ -161,7 +187,7 @@ struct Hmc {
             SMG_TRY(gauge_force());
             return fermion_force();
         };
-        if (p.omelyan) {
+        if (p.omelyan && !eo) {  // the reference's even-odd trajectory always uses leapfrog
             const double lam = kOmelyanLambda;
             SMG_TRY(solve_force());
             SMG_TRY(kick(gf, ff, lam * dt));
@@ -283,6 +309,8 @@ SMG_API smg_status smg_hmc_trajectory(smg_gauge* g, double mass, double wilson_r
     smg_context* ctx = g->ctx;
     if (p->n_steps < 1 || p->n_inner < 0 || !(p->tau > 0) || p->cg_maxiter < 1 || !(p->cg_tol > 0))
         return smg_fail(ctx, SMG_BAD_ARG, "hmc: n_steps >= 1, n_inner >= 0, tau > 0, cg_maxiter >= 1, cg_tol > 0");
+    if (p->use_eo && (p->mixed_precision || g->g.L % 2))
+        return smg_fail(ctx, SMG_UNSUPPORTED, "hmc: the even-odd path runs FP64 solves on an even L");
     Hmc h;
     h.ctx = ctx;
     h.g = g;
@@ -302,6 +330,14 @@ SMG_API smg_status smg_hmc_trajectory(smg_gauge* g, double mass, double wilson_r
     SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.X));
     SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.eta));
     SMG_TRY(smg_dirac_create(g, mass, wilson_r, p->c_sw, p->mu_t, &h.d));
+    h.eo = p->use_eo != 0;
+    if (h.eo) {
+        SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.chi));
+        SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.psi));
+        SMG_CUDA(ctx, cudaMalloc(&h.W, (size_t)V * sizeof(double)));
+        SMG_CUDA(ctx, cudaMemsetAsync(h.phi->data, 0, h.phi->bytes, ctx->stream));
+        SMG_CUDA(ctx, cudaMemsetAsync(h.eta->data, 0, h.eta->bytes, ctx->stream));
+    }
 
     // momenta: MomentumField::randomise (hmc_forces.cpp:64-69), mu-major then site order
     {
@@ -311,9 +347,25 @@ SMG_API smg_status smg_hmc_trajectory(smg_gauge* g, double mass, double wilson_r
         SMG_CUDA(ctx, cudaMemcpyAsync(h.pi, pi_h.data(), fb, cudaMemcpyHostToDevice, ctx->stream));
         SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
-    // pseudofermion phi = D^dag eta, eta = random_vec(n, rng) (hmc_trajectory.cpp:32-36); the
-    // reference's random_vec draws each entry's imaginary part first (GCC argument order)
-    {
+    if (h.eo) {
+        // phi_o = M^dag eta_o, eta_o = random_vec(V, rng) on the odd sites
+        // (generate_pseudofermion_eo, src/dirac.h:491-497); the odd half of a field is the
+        // reference's half vector in order
+        std::vector<double> eta_h((size_t)2 * V);
+        std::normal_distribution<double> dist(0.0, 1.0);
+        for (size_t i = 0; i < (size_t)V; ++i) {
+            const double im = dist(rng->gen);
+            const double re = dist(rng->gen);
+            eta_h[2 * i] = re;
+            eta_h[2 * i + 1] = im;
+        }
+        SMG_CUDA(ctx, cudaMemcpyAsync((char*)h.eta->data + h.eta->bytes / 2, eta_h.data(), h.eta->bytes / 2,
+                                      cudaMemcpyHostToDevice, ctx->stream));
+        SMG_TRY(smg_eo_schur_internal(h.d, true, h.eta, h.phi, h.chi, nullptr));
+        SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    } else {
+        // pseudofermion phi = D^dag eta, eta = random_vec(n, rng) (hmc_trajectory.cpp:32-36); the
+        // reference's random_vec draws each entry's imaginary part first (GCC argument order)
         std::vector<double> eta_h((size_t)4 * V);
         std::normal_distribution<double> dist(0.0, 1.0);
         for (size_t i = 0; i < (size_t)2 * V; ++i) {
@@ -326,19 +378,21 @@ SMG_API smg_status smg_hmc_trajectory(smg_gauge* g, double mass, double wilson_r
         SMG_TRY(smg_dirac_apply(h.d, SMG_OP_DDAG, h.eta, h.phi));
     }
 
-    double KE0 = 0, SG0 = 0, SF0 = 0;
+    double KE0 = 0, SG0 = 0, SF0 = 0, LD0 = 0;
     SMG_TRY(h.kinetic(&KE0));
     SMG_TRY(smg_gauge_action(g, p->beta, &SG0));
     SMG_TRY(h.fermion_action(&SF0));
+    SMG_TRY(h.log_det_term(&LD0));
 
     SMG_TRY(p->n_inner > 0 ? h.evolve_nested() : h.evolve_plain());
 
-    double KE1 = 0, SG1 = 0, SF1 = 0;
+    double KE1 = 0, SG1 = 0, SF1 = 0, LD1 = 0;
     SMG_TRY(h.refresh());
     SMG_TRY(h.kinetic(&KE1));
     SMG_TRY(smg_gauge_action(g, p->beta, &SG1));
     SMG_TRY(h.fermion_action(&SF1));
-    const double dH = (KE1 + SG1 + SF1) - (KE0 + SG0 + SF0);
+    SMG_TRY(h.log_det_term(&LD1));
+    const double dH = (KE1 + SG1 + SF1 + LD1) - (KE0 + SG0 + SF0 + LD0);
     // Metropolis (hmc_trajectory.cpp:226-228): the uniform draw happens only when needed
     bool accept = p->force_accept != 0 || dH < 0;
     if (!accept) {
@@ -361,6 +415,7 @@ SMG_API smg_status smg_hmc_trajectory(smg_gauge* g, double mass, double wilson_r
         res->total_cg_iters = h.cg_iters;
         res->solves = h.solves;
         res->plaquette = plaq;
+        res->dLD = LD1 - LD0;
     }
     return SMG_OK;
 }

@@ -16,6 +16,9 @@
 #include <cmath>
 
 
+smg_status smg_eo_schur_internal(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, smg_field* tmp,
+                                 double* norm2_dev);
+
 namespace {
 
 constexpr int kCheckEvery = 8;
@@ -134,17 +137,36 @@ __global__ void k_cg_p(const CgState s, const cx<T>* __restrict__ r, cx<T>* __re
     }
 }
 
+// eo: CG on the Schur complement M^dag M (EvenOddDiracOp::apply_schur_dag_schur,
+// src/dirac.h:441-447) over the odd halves of the fields, as the reference's
+// e/o HMC runs cg_solve on half-lattice vectors (src/hmc_trajectory.cpp:70-104)
 template <typename T>
-smg_status cg_run(smg_dirac* d, const smg_field* b, smg_field* x, int max_iter, double tol, smg_solve_result* res) {
+smg_status cg_run(smg_dirac* d, const smg_field* b, smg_field* x, int max_iter, double tol, smg_solve_result* res,
+                  bool eo = false) {
     smg_context* ctx = b->ctx;
     const int nrhs = b->nrhs;
-    const int V = b->g.V;
+    const int V = eo ? b->g.Vh : b->g.V;                   // sites the solver runs over
+    const int64_t off = eo ? (int64_t)b->g.Vh * nrhs * 2 : 0;  // complex offset of the odd half
     FieldSet fs;
-    smg_field *r, *p, *t, *Ap;
+    smg_field *r, *p, *t, *Ap, *te = nullptr;
     SMG_TRY(fs.add(b, &r));
     SMG_TRY(fs.add(b, &p));
     SMG_TRY(fs.add(b, &t));
     SMG_TRY(fs.add(b, &Ap));
+    if (eo) SMG_TRY(fs.add(b, &te));
+    auto vp = [&](const smg_field* f) { return (cx<T>*)f->data + off; };
+    auto half_view = [&](const smg_field* f) {
+        VecView<T> v = fv<T>(f);
+        v.p += off;
+        v.nsites = V;
+        return v;
+    };
+    auto apply_normal = [&](const smg_field* in, smg_field* out, double* n2) {
+        return eo ? smg_eo_schur_internal(d, false, in, out, te, n2) : smg_dslash(d, false, in, out, n2);
+    };
+    auto apply_dag = [&](const smg_field* in, smg_field* out) {
+        return eo ? smg_eo_schur_internal(d, true, in, out, te, nullptr) : smg_dslash(d, true, in, out, nullptr);
+    };
 
     // device scalar block
     size_t nbytes = (size_t)nrhs * (5 * sizeof(double) + 3 * sizeof(int)) + 64;
@@ -165,7 +187,7 @@ smg_status cg_run(smg_dirac* d, const smg_field* b, smg_field* x, int max_iter, 
     SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
     SMG_CUDA(ctx, cudaMemcpyAsync(r->data, b->data, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     SMG_CUDA(ctx, cudaMemcpyAsync(p->data, b->data, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-    SMG_TRY(smg_norm2_dev(r, s.rr));
+    SMG_TRY(reduce_into<T>(ctx, half_view(r), nullptr, VR_NORM, s.rr));
     k_cg_init<<<1, 256, 0, ctx->stream>>>(s, nrhs);
     count_launch(ctx);
     SMG_CHECK_LAUNCH(ctx);
@@ -185,13 +207,12 @@ smg_status cg_run(smg_dirac* d, const smg_field* b, smg_field* x, int max_iter, 
     while (!done && it < max_iter) {
         int chunk = std::min(kCheckEvery, max_iter - it);
         for (int c = 0; c < chunk; ++c) {
-            SMG_TRY(smg_dslash(d, false, p, t, s.pAp));
-            SMG_TRY(smg_dslash(d, true, t, Ap, nullptr));
+            SMG_TRY(apply_normal(p, t, s.pAp));
+            SMG_TRY(apply_dag(t, Ap));
             k_cg_check_pap<<<(nrhs + 127) / 128, 128, 0, ctx->stream>>>(s, nrhs);
-            k_cg_update<T><<<rl.grid, rl.block, 0, ctx->stream>>>(s, (cx<T>*)x->data, (cx<T>*)r->data,
-                                                                 (const cx<T>*)p->data, (const cx<T>*)Ap->data, V,
-                                                                 nrhs, ctx->red.partials, ctx->red.tickets);
-            k_cg_p<T><<<sl.grid, sl.block, 0, ctx->stream>>>(s, (const cx<T>*)r->data, (cx<T>*)p->data, V, nrhs);
+            k_cg_update<T><<<rl.grid, rl.block, 0, ctx->stream>>>(s, vp(x), vp(r), vp(p), vp(Ap), V, nrhs,
+                                                                 ctx->red.partials, ctx->red.tickets);
+            k_cg_p<T><<<sl.grid, sl.block, 0, ctx->stream>>>(s, vp(r), vp(p), V, nrhs);
             count_launch(ctx, 3);
             SMG_CHECK_LAUNCH(ctx);
         }
@@ -202,13 +223,12 @@ smg_status cg_run(smg_dirac* d, const smg_field* b, smg_field* x, int max_iter, 
     }
 
     // true residual ||b - A x|| / ||b|| with the operator of the field precision
-    SMG_TRY(smg_dslash(d, false, x, t, nullptr));
-    SMG_TRY(smg_dslash(d, true, t, Ap, nullptr));
-    int64_t n = b->n_complex();
-    k_residual<T><<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>((const cx<T>*)b->data,
-                                                                      (const cx<T>*)Ap->data, (cx<T>*)r->data, n);
+    SMG_TRY(apply_normal(x, t, nullptr));
+    SMG_TRY(apply_dag(t, Ap));
+    const int64_t n = (int64_t)V * nrhs * 2;
+    k_residual<T><<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(vp(b), vp(Ap), vp(r), n);
     count_launch(ctx);
-    SMG_TRY(smg_norm2_dev(r, scratch_true));
+    SMG_TRY(reduce_into<T>(ctx, half_view(r), nullptr, VR_NORM, scratch_true));
 
     std::vector<double> h((size_t)nrhs * 5);
     std::vector<int> hi((size_t)nrhs * 3);
@@ -246,6 +266,19 @@ smg_status cg_run(smg_dirac* d, const smg_field* b, smg_field* x, int max_iter, 
 }  // namespace
 
 extern "C" {
+
+SMG_API smg_status smg_eo_cg_solve(smg_dirac* d, const smg_field* rhs, smg_field* x, int max_iter, double tol,
+                                   smg_solve_result* res) {
+    if (!d || !rhs || !x) return SMG_BAD_ARG;
+    smg_context* ctx = d->ctx;
+    if (rhs == x) return smg_fail(ctx, SMG_BAD_ARG, "rhs and x must be distinct");
+    SMG_TRY(smg_field_check_pair(rhs, x));
+    if (rhs->g.L != d->gauge->g.L || rhs->g.L % 2) return smg_fail(ctx, SMG_BAD_ARG, "field L differs from gauge L");
+    if (max_iter < 0 || !(tol > 0)) return smg_fail(ctx, SMG_BAD_ARG, "max_iter >= 0 and tol > 0 required");
+    if (rhs->prec == SMG_F64) return cg_run<double>(d, rhs, x, max_iter, tol, res, true);
+    if (rhs->prec == SMG_F32) return cg_run<float>(d, rhs, x, max_iter, tol, res, true);
+    return smg_fail(ctx, SMG_UNSUPPORTED, "eo_cg_solve on F16 fields");
+}
 
 SMG_API smg_status smg_cg_solve(smg_dirac* d, const smg_field* rhs, smg_field* x, int max_iter, double tol,
                                 smg_solve_result* res) {

@@ -118,6 +118,37 @@ def solvers_case(ref, name, L, beta, m, r, csw, gseed, seed, null_iters=5):
           fp_it, fp_ritz)
 
 
+def eo_case(ref, name, L, beta, m, r, csw, mu, gseed, seed):
+    """EvenOddDiracOp operators, reconstruction, log det D_ee, the Schur CG and the e/o force."""
+    U = gauge_normal(L, beta, gseed).reshape(-1)
+    V = L * L
+    src_o = ref.random_vecs(1, V, seed)        # half vectors: V/2 sites x 2 spins
+    src_e = ref.random_vecs(1, V, seed + 1)
+    phi = ref.random_vecs(1, 2 * V, seed + 2)
+    d = dict(L=L, beta=beta, m=m, r=r, csw=csw, mu=mu, gseed=gseed, seed=seed, U=U, src_o=src_o, src_e=src_e,
+             phi=phi)
+    for op, key in enumerate(["schur", "schur_dag", "mdagm", "hop_eo", "hop_oe"]):
+        d[key] = ref.eo_apply(U, m, r, csw, mu, op, src_e if op == 3 else src_o)
+    d["recon"] = ref.eo_reconstruct(U, m, r, csw, mu, src_o, phi)
+    d["recon_full"] = ref.eo_reconstruct(U, m, r, csw, mu, src_o, None)
+    d["logdet"] = ref.eo_logdet(U, m, r, csw, mu)
+    phi_o = ref.eo_apply(U, m, r, csw, mu, 1, src_o)  # phi_o = M^dag eta_o
+    x_o, it, res = ref.eo_cg(U, m, r, csw, mu, phi_o, 5000, 1e-12)
+    d.update(phi_o=phi_o, cg_x=x_o, cg_iters=it, cg_res=res, force=ref.eo_force(U, m, r, csw, mu, x_o))
+    np.savez_compressed(OUT / f"{name}.npz", **d)
+    print("wrote", name, "eo cg iters", it)
+
+
+def hmc_eo_case(ref, name, L, beta, m, r, csw, gseed, seed, n_steps, n_traj, tau=1.0):
+    """Trajectories of the reference's even-odd hmc_trajectory (leapfrog, Schur CG, log det D_ee)."""
+    U = gauge_normal(L, beta, gseed).reshape(-1)
+    U_out, out = ref.hmc_trajectories(U, m, r, beta, tau, n_steps, 0, 10000, 1e-12, csw, 0.0, 0, seed, n_traj,
+                                      use_eo=True)
+    np.savez_compressed(OUT / f"{name}.npz", L=L, beta=beta, m=m, r=r, csw=csw, gseed=gseed, seed=seed,
+                        n_steps=n_steps, tau=tau, n_traj=n_traj, cg_tol=1e-12, U=U, U_out=U_out, traj=out)
+    print("wrote", name, out[:, :2].tolist())
+
+
 def gauge_files_case(ref, name, L, beta, mass, gseed):
     """A configuration written by the reference's save_gauge ("SWNG") and GaugeField::save (raw)."""
     U = gauge_normal(L, beta, gseed).reshape(-1)
@@ -138,6 +169,9 @@ CASES = {
     "hmc_L8_leapfrog": lambda ref: hmc_case(ref, "hmc_L8_leapfrog", 8, 4.0, 0.1, 1.0, 1.0, 63, 64, 8, 0, 2),
     "solvers_L16": lambda ref: solvers_case(ref, "solvers_L16", 16, 2.0, 0.1, 1.0, 1.0, 71, 72),
     "gauge_L8": lambda ref: gauge_files_case(ref, "gauge_L8", 8, 3.0, 0.05, 81),
+    "eo_L16_clover_twist": lambda ref: eo_case(ref, "eo_L16_clover_twist", 16, 2.0, 0.1, 1.0, 1.0, 0.2, 91, 92),
+    "eo_L16_wilson": lambda ref: eo_case(ref, "eo_L16_wilson", 16, 4.0, 0.2, 1.0, 0.0, 0.0, 93, 94),
+    "hmc_eo_L8": lambda ref: hmc_eo_case(ref, "hmc_eo_L8", 8, 4.0, 0.1, 1.0, 1.0, 95, 96, 6, 3),
 }
 
 

@@ -33,3 +33,24 @@ def test_richardson_fixture_against_oracle_operator(port):
         x = x + float(d["omega"]) * (d["b"] - port.dirac(*args, 2, x))
     assert np.linalg.norm(x - d["rich4"]) / np.linalg.norm(d["rich4"]) < 1e-13
     assert float(d["omega"]) == 0.8 / float(d["lam"])
+
+
+def test_eo_fixture_is_the_schur_complement_of_the_oracle_operator(port):
+    """D applied to (x_e, x_o) with x_e = -D_ee^-1 D_oe x_o (the fixture's reconstruct_full)
+    is zero on even sites and M x_o (the fixture's apply_schur) on odd sites."""
+    from conftest import golden as _g
+
+    for name in ("eo_L16_clover_twist", "eo_L16_wilson"):
+        d = _g(name)
+        L = int(d["L"])
+        s = np.arange(L * L)
+        odd = ((s % L) + (s // L)) % 2 == 1
+        Dx = port.dirac(d["U"], float(d["m"]), float(d["r"]), float(d["csw"]), float(d["mu"]), 0,
+                        d["recon_full"]).reshape(-1, 2)
+        scale = np.max(np.abs(d["schur"]))
+        assert np.max(np.abs(Dx[~odd])) < 1e-13 * scale
+        np.testing.assert_allclose(Dx[odd].reshape(-1), d["schur"], rtol=0, atol=1e-13 * scale)
+        # the even half of the twisted D_ee^-1 D_oe on top of phi (reconstruct with phi)
+        Dr = port.dirac(d["U"], float(d["m"]), float(d["r"]), float(d["csw"]), float(d["mu"]), 0,
+                        d["recon"]).reshape(-1, 2)
+        np.testing.assert_allclose(Dr[~odd], d["phi"].reshape(-1, 2)[~odd], rtol=0, atol=1e-12)
