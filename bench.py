@@ -1,6 +1,7 @@
 """Benchmark of the Wilson-clover Dirac operator and its MG solve path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload mg|dslash|cg|coarse|hmc] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload mg|dslash|cg|coarse|hmc|batch]
+                    [--impl ours|reference]
 
 Prints ONE JSON line (rank 0).  A step is one pass of the hot path over one
 batch of seeded synthetic input (links U = exp(i theta), theta ~ N(0, 1/beta);
@@ -23,6 +24,11 @@ is reported.  Workloads:
   Omelyan with 10 fermion-force steps and 4 gauge-force substeps per inner
   integration, mixed-precision solves to 1e-10, 20 trajectories;
   value = trajectories/s, with dH, acceptance and plaquette in config.
+* batch — 64 independent lattices, L drawn from {64, 96, 128, 192, 256, 384},
+  beta ~ U[2, 8], m ~ U[-0.05, 0.2], c_sw = 1, 8 Gaussian RHS each; every
+  lattice runs a 2-level MG (4 x 4, 8 null vectors) mixed GCR to a true FP64
+  residual of 1e-10 plus its pseudofermion force; one stream per lattice, a
+  pool of host workers over one largest-first queue; value = solves/s.
 * cg — the small single-RHS case (L = 32, beta = 2, m = 0.1, c_sw = 1) FP64 CG;
   value = solves/s.
 
@@ -138,6 +144,21 @@ DSLASH = dict(L=512, nrhs=32, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20
 CG = dict(L=32, beta=2.0, m=0.1, r=1.0, csw=1.0, mu=0.0, seed=31, tol=1e-10, max_iter=10000)
 HMC = dict(L=128, beta=4.0, m=0.1, r=1.0, csw=1.0, seed=2024, rng_seed=4048, tau=1.0, n_outer=10, n_inner=4,
            tol=1e-10, n_traj=20)
+BATCH = dict(n_lat=64, sizes=[64, 96, 128, 192, 256, 384], seed=5005, nrhs=8, r=1.0, csw=1.0, levels=2,
+             blocks=[(4, 4)], n_vec=8, chiral=False, w_cycle=False, null_iters=4, pre=4, post=4, coarse_max_iter=20,
+             coarse_tol=5e-2, tol=1e-10, max_iter=500, trunc=20, workers=8)
+
+
+def batch_lattices(c):
+    """The uneven batch: L from the size list, beta ~ U[2, 8], m ~ U[-0.05, 0.2], drawn from one seed."""
+    rng = np.random.default_rng(c["seed"])
+    out = []
+    for i in range(c["n_lat"]):
+        L = int(rng.choice(c["sizes"]))
+        beta = float(rng.uniform(2.0, 8.0))
+        m = float(rng.uniform(-0.05, 0.2))
+        out.append((L, beta, m, c["seed"] + 1 + i))
+    return out
 
 
 def dslash_bytes_f32(L, nrhs):
@@ -424,6 +445,104 @@ def run_ours(args, ws, rank, local):
                     "note": "the trajectory runs through the C ABI; its host inputs (momenta, eta) are copied in"},
             "gpu_launches": int(launches), "clocks": clk.summary(),
         })
+    elif args.workload == "batch":
+        # uneven multi-lattice batch: every lattice's 8 RHS by mixed MG-GCR to 1e-10 plus its pseudofermion force
+        c = dict(BATCH)
+        if args.nrhs:
+            c["nrhs"] = args.nrhs
+        if args.L:
+            c["n_lat"] = args.L  # --L N: the first N lattices of the batch (a small case)
+        lats = batch_lattices(c)
+        nrhs = c["nrhs"]
+        batch = smg.LatticeBatch(n_workers=c["workers"], device=local)
+        sources = []
+        for i, (L, beta, m, gseed) in enumerate(lats):
+            batch.add(L, smg.gauge_normal(L, beta, gseed), m, c_sw=c["csw"], wilson_r=c["r"], nrhs=nrhs)
+            B = np.stack([smg.random_vec(2 * L * L, gseed * 100 + j) for j in range(nrhs)])
+            sources.append(B)
+        t0 = time.perf_counter()
+        batch.setup(mg_params(smg, c, "f32"))
+        setup_s = time.perf_counter() - t0
+        for i, B in enumerate(sources):
+            batch.bind(i, B)
+
+        def step():
+            st, sec = batch.solve(c["max_iter"], c["tol"], c["trunc"], with_force=True)
+            smg._lib.check(st, "smg_batch_solve")
+            return sec
+
+        for _ in range(args.warmup):
+            step()
+        l0 = batch.kernel_launches
+        if ws > 1:
+            torch.distributed.barrier()
+        with Clocks(local) as clk:
+            torch.cuda.synchronize()
+            secs = [step() for _ in range(args.steps)]
+            torch.cuda.synchronize()
+        launches = (batch.kernel_launches - l0) // args.steps
+        ms = max_over_ranks(1e3 * float(np.mean(secs)), ws)
+        n_solves = len(lats) * nrhs
+        worst_res, iters = 0.0, []
+        for i in range(len(lats)):
+            st, r, _ = batch.result(i)
+            smg._lib.check(st, "batch lattice")
+            worst_res = max(worst_res, r.true_residual)
+            iters.append(r.iterations)
+        # end to end: host right-hand sides in, solutions and forces out, inside the timed call
+        host = []
+        for i, (L, beta, m, gseed) in enumerate(lats):
+            xin = torch.from_numpy(sources[i].reshape(-1).view(np.float64)).pin_memory()
+            xo = torch.empty(nrhs * 4 * L * L, dtype=torch.float64).pin_memory()
+            fo = torch.empty(2 * L * L, dtype=torch.float64).pin_memory()
+            host.append((xin, xo, fo))
+            smg._lib.check(lib.smg_batch_bind_host(batch.h, i, Cc.cast(xin.data_ptr(), DP), Cc.cast(xo.data_ptr(), DP),
+                                                   Cc.cast(fo.data_ptr(), DP)), "bind")
+        st, _ = batch.solve(c["max_iter"], c["tol"], c["trunc"], with_force=True, host_io=True)
+        smg._lib.check(st, "batch e2e")
+        e2e_secs = []
+        for _ in range(max(1, min(args.steps, 3))):
+            torch.cuda.synchronize()
+            st, sec = batch.solve(c["max_iter"], c["tol"], c["trunc"], with_force=True, host_io=True)
+            smg._lib.check(st, "batch e2e")
+            e2e_secs.append(sec)
+        e2e_ms = max_over_ranks(1e3 * float(np.mean(e2e_secs)), ws)
+        hb = sum(B.size * 16 for B in sources)
+        db = hb + sum(2 * L * L * 8 for (L, _, _, _) in lats)
+        # dominant kernel: FP32 D of the largest lattice on its 8 RHS, timed alone
+        Lmax = max(L for (L, _, _, _) in lats)
+        jmax = [L for (L, _, _, _) in lats].index(Lmax)
+        latm = smg.Lattice(Lmax)
+        Dm = smg.DiracOp(latm, smg.GaugeField(latm, smg.gauge_normal(Lmax, lats[jmax][1], lats[jmax][3]), ctx),
+                         lats[jmax][2], c["r"], c["csw"], 0.0)
+        f32s = smg.Field(latm, nrhs, "f32", ctx, data=sources[jmax])
+        f32d = smg.Field(latm, nrhs, "f32", ctx)
+        dms = timed(lambda: smg._lib.check(lib.smg_dirac_apply(Dm.h, 0, f32s.h, f32d.h), "dirac", ctx.h), 50)
+        dgbs = dslash_bytes_f32(Lmax, nrhs) / (dms * 1e-3) / 1e9
+        sizes = {}
+        for (L, _, _, _) in lats:
+            sizes[L] = sizes.get(L, 0) + 1
+        out.update({
+            "value": ws * n_solves / (ms * 1e-3), "unit": "solves/s", "ms_per_step": ms, "higher_is_better": True,
+            "dtype": "f32+f64",
+            "config": {"workload": f"uneven batch of {len(lats)} lattices (L in {c['sizes']}, beta~U[2,8], "
+                                   f"m~U[-0.05,0.2], c_sw=1), {nrhs} RHS each, 2-level MG (4x4, 8 null vectors), "
+                                   "mixed FP32/FP64 GCR to a true FP64 residual of 1e-10, plus each lattice's "
+                                   "pseudofermion force", "lattices": len(lats), "sizes": sizes,
+                       "sites_total": int(sum(L * L for (L, _, _, _) in lats)), "rhs_per_lattice": nrhs,
+                       "worst_true_residual": worst_res, "gcr_iterations_min_max": [min(iters), max(iters)],
+                       "host_workers": c["workers"], "setup_s": setup_s,
+                       "timing": "wall time of smg_batch_solve between device synchronisations (one stream per "
+                                 "lattice, so no single stream brackets the work)",
+                       "l2": "the batch's fields (several GB) exceed the 129 MB L2; no flush"},
+            "e2e": {"value": ws * n_solves / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": hb,
+                    "d2h_bytes_per_step": db, "ms_per_step": e2e_ms},
+            "roofline": {"bound": "hbm", "achieved": dgbs, "peak": peak, "unit": "GB/s", "frac": dgbs / peak,
+                         "traffic": None, "kernel": f"k_dslash<float,false,0> (L={Lmax}, {nrhs} RHS)",
+                         "ms_per_launch": dms, "peak_source": peak_kind},
+            "gpu_launches": int(launches), "clocks": clk.summary(),
+        })
+        batch.close()
     elif args.workload == "coarse":
         # the level-1 coarse operator alone: (L/4)^2 sites, 16 dofs, 32 RHS, 9-point stencil
         c = sized(MG, args)
@@ -537,6 +656,30 @@ def cpu_baseline(workload: str, threads: int | None = None, ctx_objects=None):
         return {"value": gbs, "unit": "GB/s", "cores": n_threads, "kind": "port",
                 "sample": f"FP64 D on {nrhs} RHS x {reps} reps at L={L} (the reference computes one RHS at a time "
                           "in FP64; 104 B/site per application)", "seconds": t}
+    if workload == "batch":
+        # one right-hand side of one sampled lattice (L = 128) through the port's MG-GCR with a hierarchy of
+        # the batch's parameters, scaled to the whole batch by site count
+        import schwinger_mg_gb300 as smg2
+
+        c = BATCH
+        lats = batch_lattices(c)
+        L, beta, m, gseed = next(t for t in lats if t[0] == 128)
+        U = smg2.gauge_normal(L, beta, gseed)
+        lat = smg2.Lattice(L)
+        D = smg2.DiracOp(lat, smg2.GaugeField(lat, U), m, c["r"], c["csw"], 0.0)
+        mgh = smg2.MGHierarchy(D, mg_params(smg2, c, "f64"))
+        ncs = [mgh.level_dims(1)[2]]
+        p = port.mgN_params(L, m, c["r"], c["csw"], 0.0, c["blocks"], ncs, [mgh.prolongator(0)],
+                            [None, mgh.coarse_op(1)], c["pre"], c["post"], c["w_cycle"], c["coarse_max_iter"],
+                            c["coarse_tol"])
+        b = smg2.random_vec(2 * L * L, gseed * 100)
+        _, it, res, sec = port.mgN_gcr(p, U, b, c["max_iter"], c["tol"], c["trunc"])
+        total_sites = sum(t[0] ** 2 for t in lats)
+        est = sec * c["nrhs"] * total_sites / (L * L)
+        return {"value": c["n_lat"] * c["nrhs"] / est, "unit": "solves/s", "cores": n_threads, "kind": "port",
+                "sample": f"one 1-RHS solve of an L={L} lattice of the batch ({it} GCR iterations to {res:.1e}, "
+                          f"{sec:.2f} s), scaled by site count to the {c['n_lat']} x {c['nrhs']} solves "
+                          "(forces excluded)", "seconds": sec}
     if workload == "hmc":
         # one fermion-force evaluation (CG to 1e-10 + force) and one gauge force on the CPU; a nested
         # Omelyan trajectory makes 2 n_outer + 1 of them plus the two Hamiltonian solves
@@ -597,7 +740,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="mg", choices=["mg", "dslash", "cg", "coarse", "hmc"])
+    ap.add_argument("--workload", default="mg", choices=["mg", "dslash", "cg", "coarse", "hmc", "batch"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--L", type=int, default=0, help="lattice size override (smaller cases for profiles)")

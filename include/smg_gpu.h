@@ -85,6 +85,7 @@ typedef struct smg_gauge smg_gauge;
 typedef struct smg_dirac smg_dirac;
 typedef struct smg_field smg_field;
 typedef struct smg_mg smg_mg;
+typedef struct smg_batch smg_batch;
 
 /* Result of a Krylov solve; mirrors CGResult / FCGResult
  * (reference src/solvers.h:25-35).  final_residual is the solver's own
@@ -393,6 +394,39 @@ SMG_API smg_status smg_gcr_solve(smg_dirac* d, smg_mg* mg, const smg_field* rhs,
 SMG_API smg_status smg_fgmres_solve(smg_dirac* d, smg_mg* mg, const smg_field* rhs, smg_field* x, int restart,
                                     int max_iter, double tol, int n_ritz_harvest, smg_solve_result* res,
                                     double* ritz_values, int* n_ritz);
+
+/* ------------------------------------------------------ multi-lattice batch */
+
+/* Many independent lattices of uneven size on one GPU (no reference
+ * counterpart: the reference runs one lattice per process).  Every lattice
+ * gets its own context and stream; n_workers host threads take lattices from
+ * one queue, largest first, so up to n_workers lattices run at once. */
+SMG_API smg_status smg_batch_create(int device, int n_workers, smg_batch** out);
+SMG_API smg_status smg_batch_destroy(smg_batch* b);
+/* Adds a lattice (links U in the reference layout, 2*L*L complex) with nrhs
+ * right-hand sides; id receives its index. */
+SMG_API smg_status smg_batch_add(smg_batch* b, int L, const double* U, double mass, double wilson_r, double c_sw,
+                                 double mu_t, int nrhs, int* id);
+/* Builds every lattice's MG hierarchy with the same parameters, concurrently. */
+SMG_API smg_status smg_batch_setup(smg_batch* b, const smg_mg_params* p);
+/* Host arrays of a lattice: rhs (nrhs * 2 L^2 complex, uploaded now), and the
+ * destinations of x and of the force (2 L^2 doubles) for host_io solves;
+ * any may be NULL. */
+SMG_API smg_status smg_batch_bind_host(smg_batch* b, int id, const double* rhs, double* x, double* force);
+/* Solves D^dag D x = b for every lattice with smg_gcr_solve and its hierarchy
+ * (FP32 hierarchy: FP32 GCR inside FP64 defect correction to a true FP64
+ * residual below tol) and, with with_force, accumulates F = sum_j F(X_j), the
+ * pseudofermion force of S = sum_j phi_j^dag (D^dag D)^-1 phi_j with phi = b.
+ * host_io != 0 copies the bound host right-hand sides in and x / force out
+ * inside the call.  seconds: wall time of the whole batch.  Returns the worst
+ * status over lattices (smg_batch_result gives each). */
+SMG_API smg_status smg_batch_solve(smg_batch* b, int max_iter, double tol, int trunc, int with_force, int host_io,
+                                   double* seconds);
+SMG_API smg_status smg_batch_result(smg_batch* b, int id, smg_solve_result* res, smg_status* status,
+                                    double* seconds);
+SMG_API smg_status smg_batch_download(smg_batch* b, int id, double* x, double* force);
+/* Kernels launched so far by all lattices of the batch. */
+SMG_API smg_status smg_batch_kernel_launches(smg_batch* b, uint64_t* n);
 
 /* ------------------------------------------------------------------ forces */
 

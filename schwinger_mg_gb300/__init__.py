@@ -34,6 +34,7 @@ from .api import (  # noqa: F401
     Field,
     GaugeField,
     Lattice,
+    LatticeBatch,
     axpy,
     cg_solve,
     dot,

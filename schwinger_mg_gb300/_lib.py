@@ -151,6 +151,16 @@ _SIGS = {
     "smg_eo_logdet_ee": (_st, [_vp, _dp]),
     "smg_eo_cg_solve": (_st, [_vp, _vp, _vp, C.c_int, C.c_double, C.POINTER(SolveResult)]),
     "smg_eo_fermion_force": (_st, [_vp, _vp, _dp]),
+    "smg_batch_create": (_st, [C.c_int, C.c_int, C.POINTER(_vp)]),
+    "smg_batch_destroy": (_st, [_vp]),
+    "smg_batch_add": (_st, [_vp, C.c_int, _dp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int,
+                            C.POINTER(C.c_int)]),
+    "smg_batch_setup": (_st, [_vp, C.POINTER(MGParams)]),
+    "smg_batch_bind_host": (_st, [_vp, C.c_int, _dp, _dp, _dp]),
+    "smg_batch_solve": (_st, [_vp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_int, _dp]),
+    "smg_batch_result": (_st, [_vp, C.c_int, C.POINTER(SolveResult), C.POINTER(C.c_int), _dp]),
+    "smg_batch_download": (_st, [_vp, C.c_int, _dp, _dp]),
+    "smg_batch_kernel_launches": (_st, [_vp, C.POINTER(C.c_uint64)]),
     "smg_host_gauge_write_swng": (_st, [C.c_char_p, C.c_int, _dp, C.c_double, C.c_double, C.c_double]),
     "smg_host_gauge_read_swng": (_st, [C.c_char_p, C.c_int, C.POINTER(GaugeHeader), _dp]),
     "smg_host_gauge_write_raw": (_st, [C.c_char_p, C.c_int, _dp]),

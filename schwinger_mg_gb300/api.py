@@ -865,3 +865,74 @@ def fgmres_solve_mg(A: DiracOp, n: int, rhs, mg: MGHierarchy, restart: int, max_
                     n_ritz_harvest: int = 4, **kw) -> FGMRESResult:
     """fgmres_solve_mg (reference src/solvers.cpp:776-787)."""
     return fgmres_solve(A, n, rhs, mg, restart, max_iter, tol, n_ritz_harvest, **kw)
+
+
+class LatticeBatch:
+    """Independent lattices of uneven size solved together on one GPU (smg_batch_*):
+    one stream per lattice, n_workers host threads over one largest-first queue."""
+
+    def __init__(self, n_workers: int = 8, device: int = 0):
+        h = C.c_void_p()
+        _L.check(_L.lib().smg_batch_create(device, n_workers, C.byref(h)), "smg_batch_create")
+        self.h = h
+        self.lattices = []  # (L, nrhs)
+        self._keep = []
+
+    def add(self, L: int, U, mass: float, c_sw: float = 0.0, wilson_r: float = 1.0, mu_t: float = 0.0,
+            nrhs: int = 1) -> int:
+        Ua = _as_c128(U).reshape(-1)
+        i = C.c_int(0)
+        _L.check(_L.lib().smg_batch_add(self.h, L, _ptr(Ua.view(np.float64)), mass, wilson_r, c_sw, mu_t, nrhs,
+                                        C.byref(i)), "smg_batch_add")
+        self.lattices.append((L, nrhs))
+        return i.value
+
+    def setup(self, params: _L.MGParams) -> None:
+        _L.check(_L.lib().smg_batch_setup(self.h, C.byref(params)), "smg_batch_setup")
+
+    def bind(self, i: int, rhs, x_out: np.ndarray | None = None, force_out: np.ndarray | None = None) -> None:
+        """rhs: host array (nrhs, 2V) complex, uploaded now; x_out / force_out: host arrays the
+        host_io solves write (kept referenced by the batch)."""
+        r = _as_c128(rhs).reshape(-1)
+        self._keep += [r, x_out, force_out]
+        _L.check(_L.lib().smg_batch_bind_host(self.h, i, _ptr(r.view(np.float64)),
+                                              _ptr(x_out.view(np.float64)) if x_out is not None else None,
+                                              _ptr(force_out) if force_out is not None else None),
+                 "smg_batch_bind_host")
+
+    def solve(self, max_iter: int, tol: float, trunc: int = 20, with_force: bool = True,
+              host_io: bool = False) -> tuple[int, float]:
+        sec = C.c_double(0)
+        st = _L.lib().smg_batch_solve(self.h, max_iter, tol, trunc, int(with_force), int(host_io), C.byref(sec))
+        return st, sec.value
+
+    def result(self, i: int):
+        r = _L.SolveResult()
+        st = C.c_int(0)
+        sec = C.c_double(0)
+        _L.check(_L.lib().smg_batch_result(self.h, i, C.byref(r), C.byref(st), C.byref(sec)), "smg_batch_result")
+        return st.value, r, sec.value
+
+    def download(self, i: int):
+        L, nrhs = self.lattices[i]
+        x = np.empty(nrhs * 2 * L * L, dtype=np.complex128)
+        F = np.empty(2 * L * L)
+        _L.check(_L.lib().smg_batch_download(self.h, i, _ptr(x.view(np.float64)), _ptr(F)), "smg_batch_download")
+        return x.reshape(nrhs, 2 * L * L), F.reshape(2, L * L)
+
+    @property
+    def kernel_launches(self) -> int:
+        n = C.c_uint64(0)
+        _L.check(_L.lib().smg_batch_kernel_launches(self.h, C.byref(n)), "smg_batch_kernel_launches")
+        return n.value
+
+    def close(self) -> None:
+        if self.h:
+            _L.lib().smg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -12,6 +12,8 @@
 #include "smg_internal.h"
 #include "reduce.cuh"
 
+#include <cstdlib>
+
 namespace {
 
 enum { EPI_NONE = 0, EPI_NORM = 1, EPI_MR = 2 };
@@ -123,6 +125,101 @@ __global__ void __launch_bounds__(256) k_dslash(DslashArgs<T> a) {
     if (EPI != EPI_NONE) block_reduce_finalise<K>(v, a.partials, a.ticket, nrhs, FinStore{a.out, K});
 }
 
+// ---------------------------------------------------------------- tiled stencil
+//
+// The same operator for a CTA tile of TY rows x 2*TXH columns (TXH sites of
+// each parity per row).  Both parity planes of the tile plus a one-site halo
+// are staged in shared memory with 16-byte cp.async copies (the halo wraps
+// periodically, which a TMA tile load cannot express), so every spinor is read
+// from L2 about (TY+2)(TXH+2)/(TY TXH) times instead of five times; links and
+// the clover term are read directly (one value per site shared by all RHS
+// lanes).  Shared memory holds [parity][TY+2][TXH+2][rhs] spinors.
+constexpr int kTileXH = 8;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+template <typename T, bool DAG>
+__global__ void __launch_bounds__(256) k_dslash_tile(DslashArgs<T> a, int TY) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Spinor<T>* sp = reinterpret_cast<Spinor<T>*>(smem_raw);
+    const Geom g = a.g;
+    const int nrhs = a.nrhs;
+    const int X0 = blockIdx.x * kTileXH, y0 = blockIdx.y * TY;
+    const int RW = kTileXH + 2, RH = TY + 2;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+    // stage: every 16-byte chunk of [parity][row][col] sites, each nrhs spinors
+    {
+        const int site_bytes = nrhs * (int)sizeof(Spinor<T>);
+        const int chunks_per_site = site_bytes / 16;
+        const int total = 2 * RH * RW * chunks_per_site;
+        for (int c = tid; c < total; c += nthr) {
+            const int k = c % chunks_per_site;
+            const int site = c / chunks_per_site;
+            const int col = site % RW, rest = site / RW;
+            const int row = rest % RH, par = rest / RH;
+            const int y = wrap(y0 - 1 + row, g.L);
+            const int xh = wrap(X0 - 1 + col, g.Lh);
+            const char* src = reinterpret_cast<const char*>(a.src) +
+                              ((int64_t)(par * g.Vh + y * g.Lh + xh) * site_bytes) + 16 * k;
+            cp_async16(smem_raw + (int64_t)site * site_bytes + 16 * k, src);
+        }
+        cp_async_wait_all();
+        __syncthreads();
+    }
+    const T half = T(0.5);
+    const T sgn = DAG ? T(-1) : T(1);
+    const int rhs = threadIdx.x;
+    if (rhs >= nrhs) return;
+    auto S = [&](int par, int row, int col) -> const Spinor<T>& {
+        return sp[((par * RH + row) * RW + col) * nrhs + rhs];
+    };
+    for (int it = threadIdx.y; it < 2 * TY * kTileXH; it += blockDim.y) {
+        const int c = it % kTileXH, rest = it / kTileXH;
+        const int r = rest % TY, p = rest / TY;
+        const int y = y0 + r, xh = X0 + c;
+        const int b = (y + p) & 1;
+        const int x = 2 * xh + b;
+        const int q = p * g.Vh + y * g.Lh + xh;
+        const int op = 1 - p;
+        const int xm = x == 0 ? g.L - 1 : x - 1;
+        const int ym = y == 0 ? g.L - 1 : y - 1;
+        const int q_xm = op * g.Vh + ((xm + g.L * y) >> 1);
+        const int q_ym = op * g.Vh + ((x + g.L * ym) >> 1);
+        const cx<T> u0f = a.U[q], u0b = a.U[q_xm];
+        const cx<T> u1f = a.U[g.V + q], u1b = a.U[g.V + q_ym];
+        const Spinor<T> ps = S(p, r + 1, c + 1);
+        const Spinor<T> pxp = S(op, r + 1, c + 1 + b);
+        const Spinor<T> pxm = S(op, r + 1, c + b);
+        const Spinor<T> pyp = S(op, r + 2, c + 1);
+        const Spinor<T> pym = S(op, r, c + 1);
+        const cx<T> a0x = u0f * pxp.s0, a1x = u0f * pxp.s1;
+        const cx<T> b0x = cmulc(u0b, pxm.s0), b1x = cmulc(u0b, pxm.s1);
+        const cx<T> a0y = u1f * pyp.s0, a1y = u1f * pyp.s1;
+        const cx<T> b0y = cmulc(u1b, pym.s0), b1y = cmulc(u1b, pym.s1);
+        const T Cq = a.C ? a.C[q] : T(0);
+        const cx<T> dg0 = mk<T>(a.diag + Cq, a.mu_eff);
+        const cx<T> dg1 = mk<T>(a.diag - Cq, -a.mu_eff);
+        const cx<T> sr0 = (a0x + b0x) + (a0y + b0y);
+        const cx<T> sr1 = (a1x + b1x) + (a1y + b1y);
+        const cx<T> off0 = (b1x - a1x) + times_i(a1y - b1y);
+        const cx<T> off1 = (b0x - a0x) - times_i(a0y - b0y);
+        Spinor<T> o;
+        o.s0 = dg0 * ps.s0 - half * (a.r * sr0 + sgn * off0);
+        o.s1 = dg1 * ps.s1 - half * (a.r * sr1 + sgn * off1);
+        st_spinor(a.dst, q, rhs, nrhs, o);
+    }
+}
+
+// shared-memory bytes of a tile with TY rows
+template <typename T>
+size_t tile_smem(int TY, int nrhs) {
+    return (size_t)2 * (TY + 2) * (kTileXH + 2) * nrhs * sizeof(Spinor<T>);
+}
+
 // F01(s) = Im(P_ur + P_ul + P_ll + P_lr) / 4   (dirac.h:26-52)
 __device__ __forceinline__ cx<double> lkd(const cx<double>* __restrict__ U, const Geom& g, int mu, int x, int y) {
     return U[(int64_t)mu * g.V + site_q(g, wrap(x, g.L), wrap(y, g.L))];
@@ -164,6 +261,102 @@ __global__ void k_gamma5(cx<T>* __restrict__ v, int nsites, int nrhs) {
     v[i] = -v[i];
 }
 
+constexpr int kTileSmemMax = 112 * 1024;
+
+// both instantiations may use up to kTileSmemMax of dynamic shared memory (process-wide, set once)
+template <typename T>
+void ensure_tile_attr() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaFuncSetAttribute((const void*)k_dslash_tile<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kTileSmemMax);
+        cudaFuncSetAttribute((const void*)k_dslash_tile<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kTileSmemMax);
+    });
+}
+
+// variant 0: one (site, rhs) per thread over rows; v >= 1: the tiled kernel with TY = 2^v rows
+template <typename T>
+smg_status launch_tile(smg_context* ctx, const DslashArgs<T>& a, bool dag, int v) {
+    const int TY = 1 << v;
+    const int nrhs = a.nrhs;
+    const size_t sm = tile_smem<T>(TY, nrhs);
+    const dim3 block(nrhs, 256 / nrhs), grid(a.g.Lh / kTileXH, a.g.L / TY);
+    if (dag)
+        k_dslash_tile<T, true><<<grid, block, sm, ctx->stream>>>(a, TY);
+    else
+        k_dslash_tile<T, false><<<grid, block, sm, ctx->stream>>>(a, TY);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+template <typename T>
+bool tile_ok(const Geom& g, int nrhs, int v) {
+    const int TY = 1 << v;
+    return nrhs >= 4 && nrhs <= 32 && 256 % nrhs == 0 && g.Lh % kTileXH == 0 && g.L % TY == 0 &&
+           (nrhs * sizeof(Spinor<T>)) % 16 == 0 && tile_smem<T>(TY, nrhs) <= (size_t)kTileSmemMax;
+}
+
+// The launch shape of the plain stencil is chosen once per (L, nrhs, precision)
+// and context by timing every variant on the caller's own operands (a few
+// launches each, CUDA events on the context's stream); the choice is cached.
+// During CUDA-graph capture, or when nothing is cached yet for a capture, the
+// row kernel runs.
+template <typename T>
+int dslash_variant(smg_context* ctx, const DslashArgs<T>& a, bool dag) {
+    const uint64_t key = ((uint64_t)a.g.L << 24) ^ ((uint64_t)a.nrhs << 8) ^ (uint64_t)sizeof(T);
+    for (const auto& kv : ctx->dslash_plans)
+        if (kv.first == key) return kv.second;
+    ensure_tile_attr<T>();
+    if (const char* e = std::getenv("SMG_DSLASH_VARIANT")) {  // fixed choice, for measurements
+        const int v = std::atoi(e);
+        if (v == 0 || tile_ok<T>(a.g, a.nrhs, v)) return v;
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return 0;
+    std::vector<int> cands{0};
+    for (int v = 1; v <= 3; ++v)
+        if (tile_ok<T>(a.g, a.nrhs, v)) cands.push_back(v);
+    int best = 0;
+    if (cands.size() > 1) {
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        float best_ms = 1e30f;
+        for (int v : cands) {
+            auto run = [&]() {
+                if (v == 0) {
+                    const int lanes = a.nrhs < 32 ? a.nrhs : 32, rows = 256 / lanes;
+                    const dim3 block(lanes, rows), grid((a.g.L + rows - 1) / rows, a.g.L, (a.nrhs + lanes - 1) / lanes);
+                    if (dag)
+                        k_dslash<T, true, EPI_NONE><<<grid, block, 0, ctx->stream>>>(a);
+                    else
+                        k_dslash<T, false, EPI_NONE><<<grid, block, 0, ctx->stream>>>(a);
+                    count_launch(ctx);
+                } else {
+                    launch_tile<T>(ctx, a, dag, v);
+                }
+            };
+            run();
+            cudaEventRecord(e0, ctx->stream);
+            for (int i = 0; i < 5; ++i) run();
+            cudaEventRecord(e1, ctx->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (cudaGetLastError() == cudaSuccess && ms < best_ms) {
+                best_ms = ms;
+                best = v;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    ctx->dslash_plans.push_back({key, best});
+    return best;
+}
+
 template <typename T>
 smg_status launch_dslash(smg_dirac* d, bool dag, int epi, const smg_field* src, smg_field* dst, const smg_field* w,
                          double* out_dev) {
@@ -189,6 +382,9 @@ smg_status launch_dslash(smg_dirac* d, bool dag, int epi, const smg_field* src, 
     a.out = out_dev;
     dim3 grid, block;
     if (epi == EPI_NONE) {
+        const int variant = dslash_variant<T>(ctx, a, dag);
+        if (variant > 0) return launch_tile<T>(ctx, a, dag, variant);
+
         // (row segment, row, rhs chunk) grid, one site and rhs per thread
         const int lanes = src->nrhs < 32 ? src->nrhs : 32;
         const int rows = 256 / lanes;

@@ -1931,6 +1931,11 @@ smg_status smg_mg_apply_internal(smg_mg* mg, const smg_field* b, smg_field* x) {
 
 smg_precision smg_mg_precision(const smg_mg* mg) { return mg->p.precision; }
 
+// The grid-barrier coarsest CG needs every block of its grid resident at once,
+// which kernels of other streams on the same GPU can prevent; a hierarchy
+// shared with concurrent streams uses the host-checked CG instead.
+void smg_mg_set_persistent_internal(smg_mg* mg, bool on) { mg->persistent = on; }
+
 smg_status smg_mg_level0_L(const smg_mg* mg, int* L) {
     *L = mg->lv[0].nx;
     return SMG_OK;

@@ -156,6 +156,8 @@ struct smg_context {
     // reduction buffers replaced by a larger one stay allocated until the
     // context is destroyed: a captured CUDA graph may still reference them
     std::vector<double*> retired;
+    // stencil launch shape chosen by timing per (L, nrhs, precision): key -> variant
+    std::vector<std::pair<uint64_t, int>> dslash_plans;
 };
 
 struct smg_gauge {
