@@ -157,6 +157,11 @@ SMG_API smg_status smg_dirac_get_clover(smg_dirac* d, double* F01);
  * src and dst must have the same L, nrhs and precision and be distinct. */
 SMG_API smg_status smg_dirac_apply(smg_dirac* d, smg_operator op, const smg_field* src,
                                    smg_field* dst);
+/* DiracOp::apply_delta_D (reference src/dirac.h:154-174): dst = (D(e^{i dt pi} U)
+ * - D(U)) src through the hopping terms (the reference leaves the clover term
+ * out); pi is 2*V doubles [mu][s] on the host.  F64 fields. */
+SMG_API smg_status smg_dirac_apply_delta(smg_dirac* d, const double* pi, double dt, const smg_field* src,
+                                         smg_field* dst);
 
 /* ---------------------------------------------------------- spinor fields */
 

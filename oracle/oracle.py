@@ -375,6 +375,15 @@ class Ref(_Lib):
                                       C.c_uint(seed), C.c_int(n_traj), _p(out), C.c_int(int(use_eo)))
         return U, out.reshape(n_traj, 8)[:, :8 if use_eo else 7]
 
+    def apply_delta_D(self, U, m, r, csw, mu, pi, dt, src):
+        U, src = _c(U), _c(src)
+        pi = np.ascontiguousarray(pi, dtype=np.float64).reshape(-1)
+        out = np.empty_like(src)
+        self.lib.ref_apply_delta_D(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
+                                   C.c_double(mu), pi.ctypes.data_as(C.POINTER(C.c_double)), C.c_double(dt), _p(src),
+                                   _p(out))
+        return out
+
     def eo_apply(self, U, m, r, csw, mu, op, src):
         U, src = _c(U), _c(src)
         L = self._L(U)

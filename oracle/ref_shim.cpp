@@ -536,4 +536,17 @@ void ref_eo_force(int L, const double* U, double m, double r, double csw, double
     for (int mu_ = 0; mu_ < 2; ++mu_) std::memcpy(F + (size_t)mu_ * w.lat.V, f[mu_].data(), sizeof(double) * w.lat.V);
 }
 
+
+// DiracOp::apply_delta_D (src/dirac.h:159-174): (D(e^{i dt pi} U) - D(U)) v through the hopping terms
+void ref_apply_delta_D(int L, const double* U, double m, double r, double csw, double mu, const double* pi,
+                       double dt, const double* src, double* dst) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    std::array<RVec, 2> p;
+    for (int mu_ = 0; mu_ < 2; ++mu_) p[mu_].assign(pi + (size_t)mu_ * w.lat.V, pi + (size_t)(mu_ + 1) * w.lat.V);
+    Vec out(w.lat.ndof);
+    D.apply_delta_D(to_vec(src, w.lat.ndof), out, p, dt);
+    from_vec(out, dst);
+}
+
 }  // extern "C"

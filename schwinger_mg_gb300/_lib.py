@@ -146,6 +146,7 @@ _SIGS = {
     "smg_fgmres_solve": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(SolveResult),
                                _dp, C.POINTER(C.c_int)]),
     "smg_fermion_action": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_double, _dp, C.POINTER(SolveResult)]),
+    "smg_dirac_apply_delta": (_st, [_vp, _dp, C.c_double, _vp, _vp]),
     "smg_eo_apply": (_st, [_vp, C.c_int, _vp, _vp]),
     "smg_eo_reconstruct": (_st, [_vp, _vp, _vp]),
     "smg_eo_logdet_ee": (_st, [_vp, _dp]),

@@ -276,6 +276,16 @@ class DiracOp(_Handle):
     def apply(self, src, dst=None):
         return self.apply_op(_L.OP_D, src, dst)
 
+    def apply_delta_D(self, src, pi, dt: float) -> np.ndarray:
+        """(D(e^{i dt pi} U) - D(U)) src through the hopping terms (reference src/dirac.h:154-174)."""
+        a = _as_c128(src)
+        nrhs = a.size // self.lat.ndof
+        p = np.ascontiguousarray(pi, dtype=np.float64).reshape(-1)
+        fs = Field(self.lat, nrhs, "f64", self.ctx, data=a)
+        fd = Field(self.lat, nrhs, "f64", self.ctx)
+        _L.check(_L.lib().smg_dirac_apply_delta(self.h, _ptr(p), dt, fs.h, fd.h), "smg_dirac_apply_delta", self.ctx.h)
+        return fd.download().reshape(a.shape)
+
     def apply_dag(self, src, dst=None):
         return self.apply_op(_L.OP_DDAG, src, dst)
 

@@ -27,6 +27,7 @@ struct DslashArgs {
     const cx<T>* __restrict__ w = nullptr;  // EPI_MR second field
     Geom g{};
     int nrhs = 1;
+    int px = 0;  // EPI_NONE: 0 = a block walks one row; > 0 = a block is a px-wide patch of rows
     T diag = 0, mu_eff = 0, r = 0;
     double* partials = nullptr;
     unsigned int* ticket = nullptr;
@@ -104,10 +105,19 @@ __global__ void __launch_bounds__(256) k_dslash(DslashArgs<T> a) {
     };
 
     if (EPI == EPI_NONE) {
-        // one item per thread: row = blockIdx.y, no index division
         const int rhs = blockIdx.z * blockDim.x + threadIdx.x;
-        const int rem = blockIdx.x * blockDim.y + threadIdx.y;
-        if (rhs < nrhs && rem < g.L) site(blockIdx.y, rem, rhs);
+        if (a.px == 0) {
+            // one item per thread: row = blockIdx.y, no index division
+            const int rem = blockIdx.x * blockDim.y + threadIdx.y;
+            if (rhs < nrhs && rem < g.L) site(blockIdx.y, rem, rhs);
+        } else {
+            // a block is a patch of px columns x (blockDim.y / px) rows holding both parities, so the
+            // x and y neighbours of most of its sites are sites of the same block (L1 hits)
+            const int x = blockIdx.x * a.px + (int)threadIdx.y % a.px;
+            const int y = blockIdx.y * ((int)blockDim.y / a.px) + (int)threadIdx.y / a.px;
+            const int p = (x + y) & 1;
+            if (rhs < nrhs) site(y, p * g.Lh + (x >> 1), rhs);
+        }
     } else {
         const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
         if (rhs < nrhs) {
@@ -220,6 +230,45 @@ size_t tile_smem(int TY, int nrhs) {
     return (size_t)2 * (TY + 2) * (kTileXH + 2) * nrhs * sizeof(Spinor<T>);
 }
 
+// (D(e^{i dt pi} U) - D(U)) v through the hopping terms only (apply_delta_D, dirac.h:154-174): the
+// forward hop's link is scaled by (e^{i dt pi_mu(x)} - 1), the backward hop's U^dag by
+// (e^{-i dt pi_mu(x - mu)} - 1); pi is lexicographic [mu][s]
+__global__ void k_delta_dslash(const cx<double>* __restrict__ src, cx<double>* __restrict__ dst,
+                               const cx<double>* __restrict__ U, const double* __restrict__ pi, double dt, double r,
+                               Geom g, int nrhs) {
+    const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
+    const int q = blockIdx.x * blockDim.y + threadIdx.y;
+    if (rhs >= nrhs || q >= g.V) return;
+    int x, y, p;
+    site_coords(g, q, x, y, p);
+    const int xp = x + 1 == g.L ? 0 : x + 1, xm = x == 0 ? g.L - 1 : x - 1;
+    const int yp = y + 1 == g.L ? 0 : y + 1, ym = y == 0 ? g.L - 1 : y - 1;
+    const int q_xp = site_q(g, xp, y), q_xm = site_q(g, xm, y), q_yp = site_q(g, x, yp), q_ym = site_q(g, x, ym);
+    auto phase_m1 = [&](double a) {  // e^{i a} - 1
+        double sn, cs;
+        sincos(a, &sn, &cs);
+        return mk(cs - 1.0, sn);
+    };
+    const cx<double> u0f = phase_m1(dt * pi[x + g.L * y]) * U[q];
+    const cx<double> u0b = phase_m1(-dt * pi[xm + g.L * y]) * conj(U[q_xm]);
+    const cx<double> u1f = phase_m1(dt * pi[g.V + x + g.L * y]) * U[g.V + q];
+    const cx<double> u1b = phase_m1(-dt * pi[g.V + x + g.L * ym]) * conj(U[g.V + q_ym]);
+    const Spinor<double> pxp = ld_spinor(src, q_xp, rhs, nrhs), pxm = ld_spinor(src, q_xm, rhs, nrhs);
+    const Spinor<double> pyp = ld_spinor(src, q_yp, rhs, nrhs), pym = ld_spinor(src, q_ym, rhs, nrhs);
+    const cx<double> a0x = u0f * pxp.s0, a1x = u0f * pxp.s1;
+    const cx<double> b0x = u0b * pxm.s0, b1x = u0b * pxm.s1;
+    const cx<double> a0y = u1f * pyp.s0, a1y = u1f * pyp.s1;
+    const cx<double> b0y = u1b * pym.s0, b1y = u1b * pym.s1;
+    const cx<double> sr0 = (a0x + b0x) + (a0y + b0y);
+    const cx<double> sr1 = (a1x + b1x) + (a1y + b1y);
+    const cx<double> off0 = (b1x - a1x) + times_i(a1y - b1y);
+    const cx<double> off1 = (b0x - a0x) - times_i(a0y - b0y);
+    Spinor<double> o;
+    o.s0 = -0.5 * (r * sr0 + off0);
+    o.s1 = -0.5 * (r * sr1 + off1);
+    st_spinor(dst, q, rhs, nrhs, o);
+}
+
 // F01(s) = Im(P_ur + P_ul + P_ll + P_lr) / 4   (dirac.h:26-52)
 __device__ __forceinline__ cx<double> lkd(const cx<double>* __restrict__ U, const Geom& g, int mu, int x, int y) {
     return U[(int64_t)mu * g.V + site_q(g, wrap(x, g.L), wrap(y, g.L))];
@@ -275,7 +324,40 @@ void ensure_tile_attr() {
     });
 }
 
-// variant 0: one (site, rhs) per thread over rows; v >= 1: the tiled kernel with TY = 2^v rows
+// patch mapping of the row kernel: variant 4, 5, 6 = patches px = 2, 4, 8 sites wide and
+// (256 / lanes) / px rows high, both parities
+inline void patch_shape(int nrhs, int v, int& px, int& py) {
+    const int lanes = nrhs < 32 ? nrhs : 32;
+    const int sites = 256 / lanes;
+    px = 1 << (v - 3);
+    py = sites / px;
+}
+
+bool patch_ok(const Geom& g, int nrhs, int v) {
+    const int lanes = nrhs < 32 ? nrhs : 32;
+    int px, py;
+    patch_shape(nrhs, v, px, py);
+    return 256 % lanes == 0 && py >= 1 && px * py * lanes == 256 && g.L % px == 0 && g.L % py == 0;
+}
+
+template <typename T>
+smg_status launch_patch(smg_context* ctx, DslashArgs<T> a, bool dag, int v) {
+    const int lanes = a.nrhs < 32 ? a.nrhs : 32;
+    int px, py;
+    patch_shape(a.nrhs, v, px, py);
+    a.px = px;
+    const dim3 block(lanes, py * px), grid(a.g.L / px, a.g.L / py, (a.nrhs + lanes - 1) / lanes);
+    if (dag)
+        k_dslash<T, true, EPI_NONE><<<grid, block, 0, ctx->stream>>>(a);
+    else
+        k_dslash<T, false, EPI_NONE><<<grid, block, 0, ctx->stream>>>(a);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+// variant 0: one (site, rhs) per thread over rows; v in 1..3: the tiled kernel with TY = 2^v rows;
+// v in 4..6: the row kernel on 2-D patches (patch_shape)
 template <typename T>
 smg_status launch_tile(smg_context* ctx, const DslashArgs<T>& a, bool dag, int v) {
     const int TY = 1 << v;
@@ -311,13 +393,16 @@ int dslash_variant(smg_context* ctx, const DslashArgs<T>& a, bool dag) {
     ensure_tile_attr<T>();
     if (const char* e = std::getenv("SMG_DSLASH_VARIANT")) {  // fixed choice, for measurements
         const int v = std::atoi(e);
-        if (v == 0 || tile_ok<T>(a.g, a.nrhs, v)) return v;
+        if (v == 0 || (v <= 3 && tile_ok<T>(a.g, a.nrhs, v)) || (v >= 4 && v <= 6 && patch_ok(a.g, a.nrhs, v)))
+            return v;
     }
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return 0;
     std::vector<int> cands{0};
     for (int v = 1; v <= 3; ++v)
         if (tile_ok<T>(a.g, a.nrhs, v)) cands.push_back(v);
+    for (int v = 4; v <= 6; ++v)
+        if (patch_ok(a.g, a.nrhs, v)) cands.push_back(v);
     int best = 0;
     if (cands.size() > 1) {
         cudaEvent_t e0, e1;
@@ -334,8 +419,10 @@ int dslash_variant(smg_context* ctx, const DslashArgs<T>& a, bool dag) {
                     else
                         k_dslash<T, false, EPI_NONE><<<grid, block, 0, ctx->stream>>>(a);
                     count_launch(ctx);
-                } else {
+                } else if (v <= 3) {
                     launch_tile<T>(ctx, a, dag, v);
+                } else {
+                    launch_patch<T>(ctx, a, dag, v);
                 }
             };
             run();
@@ -383,6 +470,7 @@ smg_status launch_dslash(smg_dirac* d, bool dag, int epi, const smg_field* src, 
     dim3 grid, block;
     if (epi == EPI_NONE) {
         const int variant = dslash_variant<T>(ctx, a, dag);
+        if (variant >= 4) return launch_patch<T>(ctx, a, dag, variant);
         if (variant > 0) return launch_tile<T>(ctx, a, dag, variant);
 
         // (row segment, row, rhs chunk) grid, one site and rhs per thread
@@ -545,6 +633,26 @@ SMG_API smg_status smg_dirac_get_clover(smg_dirac* d, double* F01) {
     SMG_CHECK_LAUNCH(ctx);
     SMG_CUDA(ctx, cudaMemcpyAsync(F01, tmp, (size_t)g.V * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     SMG_CUDA(ctx, cudaFreeAsync(tmp, ctx->stream));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_dirac_apply_delta(smg_dirac* d, const double* pi, double dt, const smg_field* src,
+                                         smg_field* dst) {
+    SMG_TRY(check_op_fields(d, src, dst));
+    smg_context* ctx = d->ctx;
+    if (!pi) return SMG_BAD_ARG;
+    if (src->prec != SMG_F64) return smg_fail(ctx, SMG_UNSUPPORTED, "apply_delta_D on non-F64 fields");
+    const Geom g = src->g;
+    double* pd = nullptr;
+    SMG_CUDA(ctx, cudaMallocAsync((void**)&pd, (size_t)2 * g.V * sizeof(double), ctx->stream));
+    SMG_CUDA(ctx, cudaMemcpyAsync(pd, pi, (size_t)2 * g.V * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    const SiteLaunch sl = site_launch(g.V, src->nrhs);
+    k_delta_dslash<<<sl.grid, sl.block, 0, ctx->stream>>>((const cx<double>*)src->data, (cx<double>*)dst->data,
+                                                          d->gauge->U64, pd, dt, d->r, g, src->nrhs);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    SMG_CUDA(ctx, cudaFreeAsync(pd, ctx->stream));
     SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return SMG_OK;
 }

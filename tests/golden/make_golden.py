@@ -149,6 +149,17 @@ def hmc_eo_case(ref, name, L, beta, m, r, csw, gseed, seed, n_steps, n_traj, tau
     print("wrote", name, out[:, :2].tolist())
 
 
+def delta_case(ref, name, L, beta, m, r, csw, mu, gseed, seed, dt):
+    """DiracOp::apply_delta_D with Gaussian momenta."""
+    U = gauge_normal(L, beta, gseed).reshape(-1)
+    pi = np.random.default_rng(seed).standard_normal(2 * L * L)
+    src = ref.random_vecs(1, 2 * L * L, seed + 1)
+    out = ref.apply_delta_D(U, m, r, csw, mu, pi, dt, src)
+    np.savez_compressed(OUT / f"{name}.npz", L=L, beta=beta, m=m, r=r, csw=csw, mu=mu, gseed=gseed, seed=seed, dt=dt,
+                        U=U, pi=pi, src=src, delta=out)
+    print("wrote", name)
+
+
 def gauge_files_case(ref, name, L, beta, mass, gseed):
     """A configuration written by the reference's save_gauge ("SWNG") and GaugeField::save (raw)."""
     U = gauge_normal(L, beta, gseed).reshape(-1)
@@ -172,6 +183,7 @@ CASES = {
     "eo_L16_clover_twist": lambda ref: eo_case(ref, "eo_L16_clover_twist", 16, 2.0, 0.1, 1.0, 1.0, 0.2, 91, 92),
     "eo_L16_wilson": lambda ref: eo_case(ref, "eo_L16_wilson", 16, 4.0, 0.2, 1.0, 0.0, 0.0, 93, 94),
     "hmc_eo_L8": lambda ref: hmc_eo_case(ref, "hmc_eo_L8", 8, 4.0, 0.1, 1.0, 1.0, 95, 96, 6, 3),
+    "delta_L16": lambda ref: delta_case(ref, "delta_L16", 16, 3.0, 0.1, 1.0, 1.0, 0.1, 97, 98, 0.05),
 }
 
 

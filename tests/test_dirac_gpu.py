@@ -112,7 +112,7 @@ def test_bad_arguments_raise(smg_gpu):
         smg_gpu.Field(smg_gpu.Lattice(7), 1, "f64")
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
 @pytest.mark.parametrize("nrhs,prec", [(8, "f32"), (32, "f32"), (4, "f64"), (16, "f64")])
 def test_stencil_launch_variants_agree(smg_gpu, port, monkeypatch, variant, nrhs, prec):
     """Every launch shape the stencil autotuner can pick (row kernel, shared-memory tiles of 2, 4, 8
@@ -131,3 +131,27 @@ def test_stencil_launch_variants_agree(smg_gpu, port, monkeypatch, variant, nrhs
         for j in (0, nrhs // 2, nrhs - 1):
             want = port.dirac(U, m, 1.0, csw, mu, op, B[j])
             assert rel_err_per_site(out[j], want) < tol, (variant, op, j)
+
+
+def test_apply_delta_D_matches_reference(smg_gpu):
+    d = golden("delta_L16")
+    L = int(d["L"])
+    lat = smg_gpu.Lattice(L)
+    D = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, d["U"]), float(d["m"]), float(d["r"]), float(d["csw"]),
+                        float(d["mu"]))
+    got = D.apply_delta_D(d["src"], d["pi"], float(d["dt"]))
+    assert rel_err_per_site(got, d["delta"]) < 1e-13
+
+
+def test_apply_delta_D_is_the_operator_difference_without_clover(smg_gpu):
+    """With c_sw = 0 only the hops depend on the links: D(U') v - D(U) v = apply_delta_D v."""
+    L, dt = 24, 0.1
+    U = smg_gpu.gauge_normal(L, 3.0, 71)
+    pi = np.random.default_rng(72).standard_normal((2, L * L))
+    lat = smg_gpu.Lattice(L)
+    D0 = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, U), 0.1, 1.0, 0.0, 0.2)
+    D1 = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, U * np.exp(1j * dt * pi)), 0.1, 1.0, 0.0, 0.2)
+    v = smg_gpu.random_vec(lat.ndof, 73)
+    want = D1.apply(v) - D0.apply(v)
+    got = D0.apply_delta_D(v, pi, dt)
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-13
