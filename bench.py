@@ -12,8 +12,9 @@ is reported.  Workloads:
 * mg (default) — the multi-RHS MG-GCR solve on a 512 x 512 lattice, beta = 6,
   m = -0.05, c_sw = 1; three levels (4 x 4 then 2 x 2 aggregates, 16 null
   vectors per level = 16 coarse dofs, V-cycle); 32 right-hand sides solved
-  together to a true FP64 residual of 1e-10 by an FP32 GCR preconditioned with
-  the FP32 hierarchy inside FP64 defect correction.  The hierarchy is built
+  together to a true FP64 residual of 1e-10 by an FP32 GCR (truncation 10)
+  preconditioned with the FP32 hierarchy, whose fine smoother keeps its work
+  vectors in FP16 with per-site scales, inside FP64 defect correction.  The hierarchy is built
   once before timing.  value = solves/s.  The plain FP64 single-RHS MG on the
   same inputs is measured beside it (config.plain_fp64_mg_solves_per_s).
 * dslash — FP32 D on 32 right-hand sides at L = 512; value = algorithmic GB/s.
@@ -138,8 +139,7 @@ def max_over_ranks(v: float, ws: int) -> float:
 # ------------------------------------------------------------------ workloads
 MG = dict(L=512, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20240, nrhs=32, levels=3, blocks=[(4, 4), (2, 2)],
           n_vec=16, chiral=False, w_cycle=False, null_iters=6, pre=4, post=4, coarse_max_iter=20, coarse_tol=5e-2,
-          tol=1e-10,
-          max_iter=500, trunc=20)
+          tol=1e-10, max_iter=500, trunc=10)
 DSLASH = dict(L=512, nrhs=32, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20240)
 CG = dict(L=32, beta=2.0, m=0.1, r=1.0, csw=1.0, mu=0.0, seed=31, tol=1e-10, max_iter=10000)
 HMC = dict(L=128, beta=4.0, m=0.1, r=1.0, csw=1.0, seed=2024, rng_seed=4048, tau=1.0, n_outer=10, n_inner=4,
@@ -238,7 +238,7 @@ def mg_params(smg, c, precision):
     return smg.mg_params(c["levels"], c["blocks"][0][0], c["n_vec"], blocks=c["blocks"], chiral_split=c["chiral"],
                          null_iters=c["null_iters"], pre_smooth=c["pre"], post_smooth=c["post"], w_cycle=c["w_cycle"],
                          coarse_max_iter=c["coarse_max_iter"], coarse_tol=c["coarse_tol"], precision=precision,
-                         seed=c["seed"])
+                         seed=c["seed"], smoother_half=c.get("smoother_half", False) and precision == "f32")
 
 
 def run_ours(args, ws, rank, local):
@@ -266,6 +266,9 @@ def run_ours(args, ws, rank, local):
 
     if args.workload == "mg":
         c = sized(MG, args)
+        c["smoother_half"] = args.smoother == "f16"
+        if args.trunc:
+            c["trunc"] = args.trunc
         L, nrhs = c["L"], c["nrhs"]
         U = smg.gauge_normal(L, c["beta"], c["seed"])
         lat = smg.Lattice(L)
@@ -336,6 +339,8 @@ def run_ours(args, ws, rank, local):
             "config": {"workload": f"MG-GCR, L={L} (beta=6, m=-0.05, c_sw=1), {nrhs} RHS, 3 levels (4x4, 2x2; 16 null vectors), V-cycle, "
                                    "FP32 GCR + FP32 hierarchy inside FP64 defect correction, true FP64 residual 1e-10",
                        "L": L, "nrhs": nrhs, "levels": c["levels"], "gcr_iterations": iters,
+                       "smoother_work_vectors": "FP16, per-site scales" if c["smoother_half"] else "FP32",
+                       "gcr_truncation": c["trunc"],
                        "launches_before_timed": int(l0),
                        "true_residual": true_res, "setup_s": setup_s,
                        "plain_fp64_mg_solves_per_s": 1e3 / ms64, "plain_fp64_mg_iterations": it64,
@@ -745,6 +750,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--L", type=int, default=0, help="lattice size override (smaller cases for profiles)")
     ap.add_argument("--nrhs", type=int, default=0, help="right-hand-side count override")
+    ap.add_argument("--smoother", default="f16", choices=["f32", "f16"],
+                    help="mg workload: precision of the fine smoother's work vectors (f16: per-site scaled FP16)")
+    ap.add_argument("--trunc", type=int, default=0, help="mg workload: GCR truncation override")
     ap.add_argument("--kernel-trace", default="", help="mg workload: write a CUPTI per-kernel summary of one extra "
                                                          "(untimed) step to this path")
     args = ap.parse_args()

@@ -305,6 +305,10 @@ typedef struct {
                                           with 16 dofs per site to multiples of 32 right-hand sides
                                           on the tensor cores (BF16 operands, FP32 accumulation);
                                           0: FP32 on the CUDA cores */
+    int smoother_half;                 /* 1: an F32 hierarchy keeps the fine-level smoother's work
+                                          vectors (residual, A r, D r) in FP16 with one FP32 scale
+                                          per site, arithmetic in FP32 (power-of-two nrhs from 8
+                                          to 32); 0 (default): FP32 */
 } smg_mg_params;
 
 /* Fills p with the reference's defaults: 2 levels, 4 x 4 blocks, 4 null

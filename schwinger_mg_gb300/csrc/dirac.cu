@@ -11,6 +11,7 @@
 // <p, D^dag D p> = ||D p||^2) and, for the MR smoother, <out, w> and ||out||^2.
 #include "smg_internal.h"
 #include "reduce.cuh"
+#include "half.cuh"
 
 #include <cstdlib>
 
@@ -135,6 +136,59 @@ __global__ void __launch_bounds__(256) k_dslash(DslashArgs<T> a) {
     if (EPI != EPI_NONE) block_reduce_finalise<K>(v, a.partials, a.ticket, nrhs, FinStore{a.out, K});
 }
 
+// ---------------------------------------------------------------- two RHS per thread
+//
+// The row kernel with every thread owning right-hand sides rhs and rhs + lanes (lanes = nrhs / 2):
+// the index arithmetic and the link and clover loads of a site are shared by two right-hand sides,
+// and each spinor load of a warp still covers 2 x lanes consecutive 16-byte vectors.
+template <typename T, bool DAG>
+__global__ void __launch_bounds__(256) k_dslash_r2(DslashArgs<T> a) {
+    const T half = T(0.5);
+    const T sgn = DAG ? T(-1) : T(1);
+    const Geom g = a.g;
+    const int nrhs = a.nrhs, lanes = blockDim.x;
+    const int rhs = threadIdx.x;
+    const int rem = blockIdx.x * blockDim.y + threadIdx.y;
+    const int y = blockIdx.y;
+    if (rem >= g.L) return;
+    const int p = rem >= g.Lh ? 1 : 0;
+    const int xh = rem - p * g.Lh;
+    const int x = 2 * xh + ((y + p) & 1);
+    const int q = p * g.Vh + y * g.Lh + xh;
+    const int op = (1 - p) * g.Vh;
+    const int xp = x + 1 == g.L ? 0 : x + 1, xm = x == 0 ? g.L - 1 : x - 1;
+    const int yp = y + 1 == g.L ? 0 : y + 1, ym = y == 0 ? g.L - 1 : y - 1;
+    const int q_xp = op + ((xp + g.L * y) >> 1), q_xm = op + ((xm + g.L * y) >> 1);
+    const int q_yp = op + ((x + g.L * yp) >> 1), q_ym = op + ((x + g.L * ym) >> 1);
+    const cx<T> u0f = a.U[q], u0b = a.U[q_xm], u1f = a.U[g.V + q], u1b = a.U[g.V + q_ym];
+    const T Cq = a.C ? a.C[q] : T(0);
+    const cx<T> dg0 = mk<T>(a.diag + Cq, a.mu_eff), dg1 = mk<T>(a.diag - Cq, -a.mu_eff);
+    Spinor<T> ps[2], pxp[2], pxm[2], pyp[2], pym[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {  // every load of both right-hand sides issued first
+        const int rr = rhs + k * lanes;
+        ps[k] = ld_spinor(a.src, q, rr, nrhs);
+        pxp[k] = ld_spinor(a.src, q_xp, rr, nrhs);
+        pxm[k] = ld_spinor(a.src, q_xm, rr, nrhs);
+        pyp[k] = ld_spinor(a.src, q_yp, rr, nrhs);
+        pym[k] = ld_spinor(a.src, q_ym, rr, nrhs);
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const cx<T> a0x = u0f * pxp[k].s0, a1x = u0f * pxp[k].s1;
+        const cx<T> b0x = cmulc(u0b, pxm[k].s0), b1x = cmulc(u0b, pxm[k].s1);
+        const cx<T> a0y = u1f * pyp[k].s0, a1y = u1f * pyp[k].s1;
+        const cx<T> b0y = cmulc(u1b, pym[k].s0), b1y = cmulc(u1b, pym[k].s1);
+        const cx<T> sr0 = (a0x + b0x) + (a0y + b0y), sr1 = (a1x + b1x) + (a1y + b1y);
+        const cx<T> off0 = (b1x - a1x) + times_i(a1y - b1y);
+        const cx<T> off1 = (b0x - a0x) - times_i(a0y - b0y);
+        Spinor<T> o;
+        o.s0 = dg0 * ps[k].s0 - half * (a.r * sr0 + sgn * off0);
+        o.s1 = dg1 * ps[k].s1 - half * (a.r * sr1 + sgn * off1);
+        st_spinor(a.dst, q, rhs + k * lanes, nrhs, o);
+    }
+}
+
 // ---------------------------------------------------------------- tiled stencil
 //
 // The same operator for a CTA tile of TY rows x 2*TXH columns (TXH sites of
@@ -228,6 +282,135 @@ __global__ void __launch_bounds__(256) k_dslash_tile(DslashArgs<T> a, int TY) {
 template <typename T>
 size_t tile_smem(int TY, int nrhs) {
     return (size_t)2 * (TY + 2) * (kTileXH + 2) * nrhs * sizeof(Spinor<T>);
+}
+
+// ---------------------------------------------------------------- FP16 storage
+//
+// The row kernel with FP16 (per-site scaled) input and/or output fields and FP32
+// arithmetic and links: the MG smoother's work vectors.  A warp holds 32/nrhs
+// sites of nrhs lanes each, so an output site's scale is a shuffle reduction.
+struct DslashH {
+    const cx<float>* __restrict__ src32 = nullptr;
+    const __half2* __restrict__ src16 = nullptr;
+    const float* __restrict__ src_scale = nullptr;
+    cx<float>* __restrict__ dst32 = nullptr;
+    __half2* __restrict__ dst16 = nullptr;
+    float* __restrict__ dst_scale = nullptr;
+    const cx<float>* __restrict__ U = nullptr;
+    const float* __restrict__ C = nullptr;
+    Geom g{};
+    int nrhs = 1;
+    float diag = 0, mu_eff = 0, r = 0;
+};
+
+// thread = right-hand sides rhs and rhs + lanes (lanes = nrhs / 2) of one site
+template <bool DAG, bool IN_H, bool OUT_H>
+__global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
+    const Geom g = a.g;
+    const int nrhs = a.nrhs, lanes = blockDim.x;
+    const int rhs = threadIdx.x;
+    const int rem = blockIdx.x * blockDim.y + threadIdx.y;
+    const int y = blockIdx.y;
+    const bool valid = rem < g.L;
+    const int p = rem >= g.Lh ? 1 : 0;
+    const int xh = rem - p * g.Lh;
+    const int q = p * g.Vh + y * g.Lh + xh;
+    Spinor<float> out[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        out[k].s0 = mk(0.f, 0.f);
+        out[k].s1 = mk(0.f, 0.f);
+    }
+    if (valid) {
+        const int x = 2 * xh + ((y + p) & 1);
+        const int op = (1 - p) * g.Vh;
+        const int xp = x + 1 == g.L ? 0 : x + 1, xm = x == 0 ? g.L - 1 : x - 1;
+        const int yp = y + 1 == g.L ? 0 : y + 1, ym = y == 0 ? g.L - 1 : y - 1;
+        const int q_xp = op + ((xp + g.L * y) >> 1), q_xm = op + ((xm + g.L * y) >> 1);
+        const int q_yp = op + ((x + g.L * yp) >> 1), q_ym = op + ((x + g.L * ym) >> 1);
+        auto ld = [&](int qq, int rr) {
+            return IN_H ? ld_spinor_h(a.src16, a.src_scale, qq, rr, nrhs) : ld_spinor(a.src32, qq, rr, nrhs);
+        };
+        const cx<float> u0f = a.U[q], u0b = a.U[q_xm], u1f = a.U[g.V + q], u1b = a.U[g.V + q_ym];
+        const float Cq = a.C ? a.C[q] : 0.f;
+        const cx<float> dg0 = mk(a.diag + Cq, a.mu_eff), dg1 = mk(a.diag - Cq, -a.mu_eff);
+        const float sgn = DAG ? -1.f : 1.f;
+        Spinor<float> ps[2], pxp[2], pxm[2], pyp[2], pym[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int rr = rhs + k * lanes;
+            ps[k] = ld(q, rr);
+            pxp[k] = ld(q_xp, rr);
+            pxm[k] = ld(q_xm, rr);
+            pyp[k] = ld(q_yp, rr);
+            pym[k] = ld(q_ym, rr);
+        }
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const cx<float> a0x = u0f * pxp[k].s0, a1x = u0f * pxp[k].s1;
+            const cx<float> b0x = cmulc(u0b, pxm[k].s0), b1x = cmulc(u0b, pxm[k].s1);
+            const cx<float> a0y = u1f * pyp[k].s0, a1y = u1f * pyp[k].s1;
+            const cx<float> b0y = cmulc(u1b, pym[k].s0), b1y = cmulc(u1b, pym[k].s1);
+            const cx<float> sr0 = (a0x + b0x) + (a0y + b0y), sr1 = (a1x + b1x) + (a1y + b1y);
+            const cx<float> off0 = (b1x - a1x) + times_i(a1y - b1y);
+            const cx<float> off1 = (b0x - a0x) - times_i(a0y - b0y);
+            out[k].s0 = dg0 * ps[k].s0 - 0.5f * (a.r * sr0 + sgn * off0);
+            out[k].s1 = dg1 * ps[k].s1 - 0.5f * (a.r * sr1 + sgn * off1);
+        }
+    }
+    if (OUT_H) {
+        st_spinor2_h(a.dst16, a.dst_scale, q, rhs, nrhs, lanes, out[0], out[1], valid);
+    } else if (valid) {
+        st_spinor(a.dst32, q, rhs, nrhs, out[0]);
+        st_spinor(a.dst32, q, rhs + lanes, nrhs, out[1]);
+    }
+}
+
+smg_status launch_dslash_h(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst) {
+    smg_context* ctx = src->ctx;
+    const int nrhs = src->nrhs;
+    if (!f16_nrhs_ok(nrhs) || nrhs < 2)
+        return smg_fail(ctx, SMG_UNSUPPORTED, "F16 stencil: nrhs a power of two from 2 to 32");
+    if (src->prec == SMG_F64 || dst->prec == SMG_F64)
+        return smg_fail(ctx, SMG_UNSUPPORTED, "dslash between F16 and F64 fields");
+    if (!d->gauge->U32) return smg_fail(ctx, SMG_DEVICE_ERROR, "FP32 links missing");
+    DslashH a;
+    const bool ih = src->prec == SMG_F16, oh = dst->prec == SMG_F16;
+    if (ih) {
+        a.src16 = (const __half2*)src->data;
+        a.src_scale = src->scale;
+    } else {
+        a.src32 = (const cx<float>*)src->data;
+    }
+    if (oh) {
+        a.dst16 = (__half2*)dst->data;
+        a.dst_scale = dst->scale;
+    } else {
+        a.dst32 = (cx<float>*)dst->data;
+    }
+    a.U = d->gauge->U32;
+    a.C = d->C32;
+    a.g = src->g;
+    a.nrhs = nrhs;
+    a.diag = (float)(2.0 * d->r + d->mass);
+    a.mu_eff = (float)(dag ? -d->mu_t : d->mu_t);
+    a.r = (float)d->r;
+    const int lanes = nrhs / 2, rows = 256 / lanes;
+    const dim3 block(lanes, rows), grid((a.g.L + rows - 1) / rows, a.g.L);
+#define SMG_DH(DG, I, O) k_dslash_h<DG, I, O><<<grid, block, 0, ctx->stream>>>(a)
+    if (dag) {
+        if (ih && oh) SMG_DH(true, true, true);
+        else if (ih) SMG_DH(true, true, false);
+        else SMG_DH(true, false, true);
+    } else {
+        if (ih && oh) SMG_DH(false, true, true);
+        else if (ih) SMG_DH(false, true, false);
+        else SMG_DH(false, false, true);
+    }
+#undef SMG_DH
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
 }
 
 // (D(e^{i dt pi} U) - D(U)) v through the hopping terms only (apply_delta_D, dirac.h:154-174): the
@@ -356,6 +539,22 @@ smg_status launch_patch(smg_context* ctx, DslashArgs<T> a, bool dag, int v) {
     return SMG_OK;
 }
 
+// variant 7: two right-hand sides per thread (nrhs even, nrhs / 2 <= 32 lanes)
+bool r2_ok(int nrhs) { return nrhs >= 2 && nrhs % 2 == 0 && nrhs / 2 <= 32 && 256 % (nrhs / 2) == 0; }
+
+template <typename T>
+smg_status launch_r2(smg_context* ctx, const DslashArgs<T>& a, bool dag) {
+    const int lanes = a.nrhs / 2, rows = 256 / lanes;
+    const dim3 block(lanes, rows), grid((a.g.L + rows - 1) / rows, a.g.L);
+    if (dag)
+        k_dslash_r2<T, true><<<grid, block, 0, ctx->stream>>>(a);
+    else
+        k_dslash_r2<T, false><<<grid, block, 0, ctx->stream>>>(a);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
 // variant 0: one (site, rhs) per thread over rows; v in 1..3: the tiled kernel with TY = 2^v rows;
 // v in 4..6: the row kernel on 2-D patches (patch_shape)
 template <typename T>
@@ -393,7 +592,8 @@ int dslash_variant(smg_context* ctx, const DslashArgs<T>& a, bool dag) {
     ensure_tile_attr<T>();
     if (const char* e = std::getenv("SMG_DSLASH_VARIANT")) {  // fixed choice, for measurements
         const int v = std::atoi(e);
-        if (v == 0 || (v <= 3 && tile_ok<T>(a.g, a.nrhs, v)) || (v >= 4 && v <= 6 && patch_ok(a.g, a.nrhs, v)))
+        if (v == 0 || (v <= 3 && tile_ok<T>(a.g, a.nrhs, v)) || (v >= 4 && v <= 6 && patch_ok(a.g, a.nrhs, v)) ||
+            (v == 7 && r2_ok(a.nrhs)))
             return v;
     }
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -403,6 +603,7 @@ int dslash_variant(smg_context* ctx, const DslashArgs<T>& a, bool dag) {
         if (tile_ok<T>(a.g, a.nrhs, v)) cands.push_back(v);
     for (int v = 4; v <= 6; ++v)
         if (patch_ok(a.g, a.nrhs, v)) cands.push_back(v);
+    if (r2_ok(a.nrhs)) cands.push_back(7);
     int best = 0;
     if (cands.size() > 1) {
         cudaEvent_t e0, e1;
@@ -421,8 +622,10 @@ int dslash_variant(smg_context* ctx, const DslashArgs<T>& a, bool dag) {
                     count_launch(ctx);
                 } else if (v <= 3) {
                     launch_tile<T>(ctx, a, dag, v);
-                } else {
+                } else if (v <= 6) {
                     launch_patch<T>(ctx, a, dag, v);
+                } else {
+                    launch_r2<T>(ctx, a, dag);
                 }
             };
             run();
@@ -470,6 +673,7 @@ smg_status launch_dslash(smg_dirac* d, bool dag, int epi, const smg_field* src, 
     dim3 grid, block;
     if (epi == EPI_NONE) {
         const int variant = dslash_variant<T>(ctx, a, dag);
+        if (variant == 7) return launch_r2<T>(ctx, a, dag);
         if (variant >= 4) return launch_patch<T>(ctx, a, dag, variant);
         if (variant > 0) return launch_tile<T>(ctx, a, dag, variant);
 
@@ -503,6 +707,11 @@ smg_status launch_dslash(smg_dirac* d, bool dag, int epi, const smg_field* src, 
 
 smg_status dslash_dispatch(smg_dirac* d, bool dag, int epi, const smg_field* src, smg_field* dst, const smg_field* w,
                            double* out_dev) {
+    if (src->prec == SMG_F16 || dst->prec == SMG_F16) {
+        if (epi != EPI_NONE) return smg_fail(src->ctx, SMG_UNSUPPORTED, "fused reductions on F16 fields");
+        return launch_dslash_h(d, dag, src, dst);
+    }
+    if (src->prec != dst->prec) return smg_fail(src->ctx, SMG_BAD_ARG, "dslash between F32 and F64 fields");
     if (src->prec == SMG_F64) return launch_dslash<double>(d, dag, epi, src, dst, w, out_dev);
     if (src->prec == SMG_F32) return launch_dslash<float>(d, dag, epi, src, dst, w, out_dev);
     return smg_fail(src->ctx, SMG_UNSUPPORTED, "dslash on F16 field");

@@ -143,7 +143,7 @@ smg_status launch_eo(smg_dirac* d, bool dag, int mode, int p, const smg_field* h
         a.U = (const cx<T>*)d->gauge->U64;
         a.C = (const T*)d->C64;
     } else {
-        SMG_TRY(smg_gauge_ensure_f32(d->gauge));
+        if (!d->gauge->U32) return smg_fail(ctx, SMG_DEVICE_ERROR, "FP32 links missing");
         a.U = (const cx<T>*)d->gauge->U32;
         a.C = (const T*)d->C32;
     }

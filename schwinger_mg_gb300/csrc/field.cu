@@ -2,6 +2,7 @@
 // permutation, precision conversion, and the BLAS-1 kernels
 // (reference src/linalg.cpp:8-48).
 #include "smg_internal.h"
+#include "half.cuh"
 #include "reduce.cuh"
 
 namespace {
@@ -104,6 +105,38 @@ __global__ void k_scale(const double* __restrict__ alpha, cx<T>* __restrict__ v,
     }
 }
 
+// F16 fields: one thread per (device site, rhs), a lane group of nrhs threads per site
+__global__ void k_host_to_field_h(const cx<double>* __restrict__ host, __half2* __restrict__ out,
+                                  float* __restrict__ scale, Geom g, int nrhs) {
+    const int rhs = threadIdx.x;
+    const int q = blockIdx.x * blockDim.y + threadIdx.y;
+    const bool valid = q < g.V;
+    Spinor<float> v;
+    v.s0 = mk(0.f, 0.f);
+    v.s1 = mk(0.f, 0.f);
+    if (valid) {
+        int x, y, p;
+        site_coords(g, q, x, y, p);
+        const cx<double>* h = host + ((int64_t)rhs * g.V + x + (int64_t)g.L * y) * 2;
+        v.s0 = cvt<float>(h[0]);
+        v.s1 = cvt<float>(h[1]);
+    }
+    st_spinor_h(out, scale, q, rhs, nrhs, blockDim.x, v, valid);
+}
+
+__global__ void k_field_h_to_host(const __half2* __restrict__ in, const float* __restrict__ scale,
+                                  cx<double>* __restrict__ host, Geom g, int nrhs) {
+    const int rhs = threadIdx.x;
+    const int q = blockIdx.x * blockDim.y + threadIdx.y;
+    if (q >= g.V) return;
+    int x, y, p;
+    site_coords(g, q, x, y, p);
+    const Spinor<float> v = ld_spinor_h(in, scale, q, rhs, nrhs);
+    cx<double>* h = host + ((int64_t)rhs * g.V + x + (int64_t)g.L * y) * 2;
+    h[0] = cvt<double>(v.s0);
+    h[1] = cvt<double>(v.s1);
+}
+
 size_t elem_bytes(smg_precision p) {
     switch (p) {
         case SMG_F64: return sizeof(cx<double>);
@@ -118,12 +151,15 @@ smg_status transfer_in(smg_field* f, const double* host) {
     SMG_CUDA(ctx, cudaSetDevice(ctx->device));
     const int64_t n = f->n_complex();
     cx<double>* tmp = nullptr;
-    if (f->prec == SMG_F16) return smg_fail(ctx, SMG_UNSUPPORTED, "F16 host transfer");
     SMG_CUDA(ctx, cudaMallocAsync(&tmp, n * sizeof(cx<double>), ctx->stream));
     SMG_CUDA(ctx, cudaMemcpyAsync(tmp, host, n * sizeof(cx<double>), cudaMemcpyHostToDevice, ctx->stream));
     int64_t total = (int64_t)f->g.V * f->nrhs;
     int blocks = (int)((total + 255) / 256);
-    if (f->prec == SMG_F64)
+    if (f->prec == SMG_F16) {
+        const dim3 block(f->nrhs, 256 / f->nrhs);
+        k_host_to_field_h<<<(f->g.V + block.y - 1) / block.y, block, 0, ctx->stream>>>(
+            tmp, (__half2*)f->data, f->scale, f->g, f->nrhs);
+    } else if (f->prec == SMG_F64)
         k_host_to_field<double><<<blocks, 256, 0, ctx->stream>>>(tmp, (cx<double>*)f->data, f->g, f->nrhs);
     else
         k_host_to_field<float><<<blocks, 256, 0, ctx->stream>>>(tmp, (cx<float>*)f->data, f->g, f->nrhs);
@@ -137,12 +173,15 @@ smg_status transfer_out(const smg_field* f, double* host, bool sync) {
     smg_context* ctx = f->ctx;
     SMG_CUDA(ctx, cudaSetDevice(ctx->device));
     const int64_t n = f->n_complex();
-    if (f->prec == SMG_F16) return smg_fail(ctx, SMG_UNSUPPORTED, "F16 host transfer");
     cx<double>* tmp = nullptr;
     SMG_CUDA(ctx, cudaMallocAsync(&tmp, n * sizeof(cx<double>), ctx->stream));
     int64_t total = (int64_t)f->g.V * f->nrhs;
     int blocks = (int)((total + 255) / 256);
-    if (f->prec == SMG_F64)
+    if (f->prec == SMG_F16) {
+        const dim3 block(f->nrhs, 256 / f->nrhs);
+        k_field_h_to_host<<<(f->g.V + block.y - 1) / block.y, block, 0, ctx->stream>>>(
+            (const __half2*)f->data, f->scale, tmp, f->g, f->nrhs);
+    } else if (f->prec == SMG_F64)
         k_field_to_host<double><<<blocks, 256, 0, ctx->stream>>>((const cx<double>*)f->data, tmp, f->g, f->nrhs);
     else
         k_field_to_host<float><<<blocks, 256, 0, ctx->stream>>>((const cx<float>*)f->data, tmp, f->g, f->nrhs);
@@ -230,6 +269,8 @@ SMG_API smg_status smg_field_create(smg_context* ctx, int L, int nrhs, smg_preci
     if (L < 4 || (L & 1)) return smg_fail(ctx, SMG_BAD_ARG, "L must be even and >= 4");
     if (nrhs < 1 || nrhs > 2048) return smg_fail(ctx, SMG_BAD_ARG, "nrhs must be in [1, 2048]");
     if (prec != SMG_F64 && prec != SMG_F32 && prec != SMG_F16) return smg_fail(ctx, SMG_BAD_ARG, "precision");
+    if (prec == SMG_F16 && !f16_nrhs_ok(nrhs))
+        return smg_fail(ctx, SMG_BAD_ARG, "F16 fields need nrhs a power of two <= 32");
     SMG_CUDA(ctx, cudaSetDevice(ctx->device));
     smg_field* f = new smg_field();
     f->ctx = ctx;
@@ -243,7 +284,7 @@ SMG_API smg_status smg_field_create(smg_context* ctx, int L, int nrhs, smg_preci
         return smg_fail(ctx, SMG_NO_MEMORY, std::string("field allocation: ") + cudaGetErrorString(e));
     }
     if (prec == SMG_F16) {
-        e = cudaMalloc(&f->scale, (size_t)f->g.V * nrhs * sizeof(float));
+        e = cudaMalloc(&f->scale, (size_t)f->g.V * sizeof(float));
         if (e != cudaSuccess) {
             cudaFree(f->data);
             delete f;
@@ -295,7 +336,7 @@ SMG_API smg_status smg_field_download_async(const smg_field* f, double* host) {
 SMG_API smg_status smg_field_zero(smg_field* f) {
     if (!f) return SMG_BAD_ARG;
     SMG_CUDA(f->ctx, cudaMemsetAsync(f->data, 0, f->bytes, f->ctx->stream));
-    if (f->scale) SMG_CUDA(f->ctx, cudaMemsetAsync(f->scale, 0, (size_t)f->g.V * f->nrhs * sizeof(float), f->ctx->stream));
+    if (f->scale) SMG_CUDA(f->ctx, cudaMemsetAsync(f->scale, 0, (size_t)f->g.V * sizeof(float), f->ctx->stream));
     return SMG_OK;
 }
 
@@ -308,7 +349,7 @@ SMG_API smg_status smg_field_copy(const smg_field* src, smg_field* dst) {
     if (src->prec == dst->prec) {
         SMG_CUDA(ctx, cudaMemcpyAsync(dst->data, src->data, src->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
         if (src->scale)
-            SMG_CUDA(ctx, cudaMemcpyAsync(dst->scale, src->scale, (size_t)src->g.V * src->nrhs * sizeof(float),
+            SMG_CUDA(ctx, cudaMemcpyAsync(dst->scale, src->scale, (size_t)src->g.V * sizeof(float),
                                           cudaMemcpyDeviceToDevice, ctx->stream));
         return SMG_OK;
     }

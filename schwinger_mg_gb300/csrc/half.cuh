@@ -1,0 +1,72 @@
+// FP16 fine-field storage with one FP32 scale per site.
+//
+// An F16 field stores, for every site q, the nrhs two-spinors of its
+// right-hand sides as __half2 pairs (re, im) in the layout of the FP32 field,
+// [q][rhs][spin], divided by the site's scale: the largest |re| or |im| over
+// all right-hand sides and spins of that site ("per-site block scaling").
+// Values are in [-1, 1], so FP16's 11-bit mantissa holds every component to
+// about 5e-4 of the site's largest one; all arithmetic is FP32.
+//
+// Writers need the site maximum over the right-hand sides before they can
+// store: the kernels that write F16 fields give each site one group of
+// `lanes` = nrhs threads of a warp (nrhs a power of two <= 32) and reduce the
+// maximum with shuffles inside the group.
+#pragma once
+#include <cuda_fp16.h>
+
+#include "smg_internal.h"
+
+struct alignas(8) Spinor16 {
+    __half2 s0, s1;
+};
+
+__device__ __forceinline__ Spinor<float> ld_spinor_h(const __half2* __restrict__ f, const float* __restrict__ scale,
+                                                      int64_t q, int rhs, int nrhs) {
+    const Spinor16 h = reinterpret_cast<const Spinor16*>(f)[q * nrhs + rhs];
+    const float s = scale[q];
+    const float2 a = __half22float2(h.s0), b = __half22float2(h.s1);
+    Spinor<float> o;
+    o.s0 = mk(a.x * s, a.y * s);
+    o.s1 = mk(b.x * s, b.y * s);
+    return o;
+}
+
+// Stores one two-spinor per thread.  The `lanes` threads of a site group (consecutive lanes of one
+// warp with blockDim.x == lanes) cooperate on the site's scale; every thread of the warp must call
+// this (the shuffles span the warp), and `valid` (uniform within a group) says whether to store.
+__device__ __forceinline__ void st_spinor_h(__half2* __restrict__ f, float* __restrict__ scale, int64_t q, int rhs,
+                                            int nrhs, int lanes, Spinor<float> v, bool valid) {
+    float m = valid ? fmaxf(fmaxf(fabsf(v.s0.re), fabsf(v.s0.im)), fmaxf(fabsf(v.s1.re), fabsf(v.s1.im))) : 0.f;
+    for (int o = lanes >> 1; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o, lanes));
+    if (!valid) return;
+    const float inv = m > 0.f ? 1.0f / m : 0.f;
+    Spinor16 h;
+    h.s0 = __floats2half2_rn(v.s0.re * inv, v.s0.im * inv);
+    h.s1 = __floats2half2_rn(v.s1.re * inv, v.s1.im * inv);
+    reinterpret_cast<Spinor16*>(f)[q * nrhs + rhs] = h;
+    if ((threadIdx.x & (lanes - 1)) == 0) scale[q] = m;
+}
+
+// Two spinors per thread (right-hand sides rhs and rhs + lanes of one site), same contract as above.
+__device__ __forceinline__ void st_spinor2_h(__half2* __restrict__ f, float* __restrict__ scale, int64_t q, int rhs,
+                                             int nrhs, int lanes, Spinor<float> v, Spinor<float> w, bool valid) {
+    float m = 0.f;
+    if (valid) {
+        m = fmaxf(fmaxf(fabsf(v.s0.re), fabsf(v.s0.im)), fmaxf(fabsf(v.s1.re), fabsf(v.s1.im)));
+        m = fmaxf(m, fmaxf(fmaxf(fabsf(w.s0.re), fabsf(w.s0.im)), fmaxf(fabsf(w.s1.re), fabsf(w.s1.im))));
+    }
+    for (int o = lanes >> 1; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o, lanes));
+    if (!valid) return;
+    const float inv = m > 0.f ? 1.0f / m : 0.f;
+    Spinor16 h;
+    h.s0 = __floats2half2_rn(v.s0.re * inv, v.s0.im * inv);
+    h.s1 = __floats2half2_rn(v.s1.re * inv, v.s1.im * inv);
+    reinterpret_cast<Spinor16*>(f)[q * nrhs + rhs] = h;
+    h.s0 = __floats2half2_rn(w.s0.re * inv, w.s0.im * inv);
+    h.s1 = __floats2half2_rn(w.s1.re * inv, w.s1.im * inv);
+    reinterpret_cast<Spinor16*>(f)[q * nrhs + rhs + lanes] = h;
+    if ((threadIdx.x & (lanes - 1)) == 0) scale[q] = m;
+}
+
+// nrhs values whose sites can be written as F16 (one site per power-of-two lane group)
+inline bool f16_nrhs_ok(int nrhs) { return nrhs >= 1 && nrhs <= 32 && (nrhs & (nrhs - 1)) == 0; }

@@ -20,6 +20,7 @@
 // triple products of the stencil blocks with the block vectors.
 #include "smg_internal.h"
 #include "vec.cuh"
+#include "half.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -299,8 +300,24 @@ __device__ __forceinline__ int64_t transfer_idx(const TransferGeom& t, int64_t s
 }
 constexpr int kTransferChunk = 4;  // outputs reduced across rows per shared-memory pass
 
-template <typename T, int NC>
-__global__ void __launch_bounds__(256) k_restrict_agg(const cx<T>* __restrict__ V, const cx<T>* __restrict__ in,
+// fine/coarse vector readers for the restriction: plain, or FP16 with per-site scales
+template <typename T>
+struct InPlain {
+    const cx<T>* __restrict__ p;
+    __device__ __forceinline__ cx<T> operator()(int64_t idx, int64_t) const { return p[idx]; }
+};
+struct InHalf {
+    const __half2* __restrict__ p;
+    const float* __restrict__ scale;
+    __device__ __forceinline__ cx<float> operator()(int64_t idx, int64_t site) const {
+        const float2 v = __half22float2(p[idx]);
+        const float s = scale[site];
+        return mk(v.x * s, v.y * s);
+    }
+};
+
+template <typename T, int NC, typename In = InPlain<T>>
+__global__ void __launch_bounds__(256) k_restrict_agg(const cx<T>* __restrict__ V, In in,
                                                       cx<T>* __restrict__ out, TransferGeom t) {
     extern __shared__ unsigned char s_raw[];
     cx<T>* s_acc = reinterpret_cast<cx<T>*>(s_raw);  // [rows][kTransferChunk][lanes]
@@ -314,7 +331,7 @@ __global__ void __launch_bounds__(256) k_restrict_agg(const cx<T>* __restrict__ 
     for (int e = threadIdx.y; e < m * nd; e += rows) {
         const int loc = e / nd, j = e - loc * nd;
         const int64_t s = transfer_site(t, B, loc);
-        const cx<T> f = live ? in[transfer_idx(t, s, j, rhs)] : mk<T>(0, 0);
+        const cx<T> f = live ? in(transfer_idx(t, s, j, rhs), s) : mk<T>(0, 0);
         const cx<T>* v = V + (((int64_t)B * m + loc) * nd + j) * NC;
 #pragma unroll
         for (int i = 0; i < NC; ++i) acc[i] = acc[i] + cmulc(v[i], f);
@@ -1193,15 +1210,24 @@ smg_status coarse_cg_persistent(smg_mg* mg, int l, void* x, const void* b) {
     return SMG_OK;
 }
 
+// the fine smoother's work vectors are FP16 for F32 cycles of hierarchies that ask for it, when the
+// right-hand sides fit the FP16 writers (power-of-two lane groups) and the aggregate restriction
+bool half_smoother(const smg_mg* mg, int nrhs, smg_precision prec) {
+    const int nc = mg->lv[0].nc_next;
+    return mg->p.smoother_half && prec == SMG_F32 && nrhs >= 8 && f16_nrhs_ok(nrhs) &&
+           (nc == 8 || nc == 16 || nc == 32);
+}
+
 smg_status ensure_work(smg_mg* mg, int nrhs, smg_precision prec) {
     if (mg->work_nrhs == nrhs && mg->work_prec == prec && mg->f_t) return SMG_OK;
     smg_context* ctx = mg->ctx;
     SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     free_work(mg);
     const int L = mg->lv[0].nx;
-    SMG_TRY(smg_field_create(ctx, L, nrhs, prec, &mg->f_r));
-    SMG_TRY(smg_field_create(ctx, L, nrhs, prec, &mg->f_Ar));
-    SMG_TRY(smg_field_create(ctx, L, nrhs, prec, &mg->f_t));
+    const smg_precision wp = half_smoother(mg, nrhs, prec) ? SMG_F16 : prec;
+    SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &mg->f_r));
+    SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &mg->f_Ar));
+    SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &mg->f_t));
     size_t es = prec == SMG_F64 ? sizeof(cx<double>) : sizeof(cx<float>);
     mg->cw.resize(mg->lv.size());
     for (size_t l = 1; l < mg->lv.size(); ++l) {
@@ -1226,6 +1252,185 @@ smg_status ensure_work(smg_mg* mg, int nrhs, smg_precision prec) {
 }
 
 // ------------------------------------------------------------ MR smoothers
+
+// ------------------------------------------------------------ FP16 smoother work vectors
+//
+// One thread per (fine site, pair of right-hand sides rhs and rhs + lanes); a block is
+// (lanes = nrhs / 2, 256 / lanes sites), so the threads of a site are one lane group of a warp
+// (FP16 writers reduce the site scale across it).
+
+// r16 = b - Ax (Ax16 optional: r16 = b)
+__global__ void __launch_bounds__(256) k_sub_h(const cx<float>* __restrict__ b, const __half2* __restrict__ ax,
+                                               const float* __restrict__ axs, __half2* __restrict__ r,
+                                               float* __restrict__ rs, int nsites, int nrhs) {
+    const int lanes = blockDim.x, rhs = threadIdx.x;
+    const int s = blockIdx.x * blockDim.y + threadIdx.y;
+    const bool valid = s < nsites;
+    Spinor<float> v[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        v[k].s0 = mk(0.f, 0.f);
+        v[k].s1 = mk(0.f, 0.f);
+        if (valid) {
+            v[k] = ld_spinor(b, s, rhs + k * lanes, nrhs);
+            if (ax) {
+                const Spinor<float> a = ld_spinor_h(ax, axs, s, rhs + k * lanes, nrhs);
+                v[k].s0 = v[k].s0 - a.s0;
+                v[k].s1 = v[k].s1 - a.s1;
+            }
+        }
+    }
+    st_spinor2_h(r, rs, s, rhs, nrhs, lanes, v[0], v[1], valid);
+}
+
+// MR (sc = [rhs][3] <Ar, r>, ||Ar||^2) or Richardson (fixed omega) step:
+// x += omega r (x FP32), r -= omega Ar (r, Ar FP16); omega formed once per block
+__global__ void __launch_bounds__(256) k_smooth_update_h(cx<float>* __restrict__ x, __half2* __restrict__ r,
+                                                         float* __restrict__ rs, const __half2* __restrict__ ar,
+                                                         const float* __restrict__ ars, const double* __restrict__ sc,
+                                                         float omega, int nsites, int nrhs) {
+    __shared__ cx<float> s_om[64];
+    const int lanes = blockDim.x, rhs = threadIdx.x;
+    if (threadIdx.y < 2) {
+        const int rr = rhs + threadIdx.y * lanes;
+        cx<float> om = mk(omega, 0.f);
+        if (sc) {
+            const double den = sc[3 * rr + 2];
+            om = (fabs(den) >= 1e-30 && isfinite(den)) ? mk((float)(sc[3 * rr] / den), (float)(sc[3 * rr + 1] / den))
+                                                       : mk(0.f, 0.f);
+        }
+        s_om[rr] = om;
+    }
+    __syncthreads();
+    const int s = blockIdx.x * blockDim.y + threadIdx.y;
+    const bool valid = s < nsites;
+    Spinor<float> rn[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        rn[k].s0 = mk(0.f, 0.f);
+        rn[k].s1 = mk(0.f, 0.f);
+    }
+    if (valid) {
+        Spinor<float> rv[2], av[2], xv[2];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int rr = rhs + k * lanes;
+            rv[k] = ld_spinor_h(r, rs, s, rr, nrhs);
+            av[k] = ld_spinor_h(ar, ars, s, rr, nrhs);
+            xv[k] = ld_spinor(x, s, rr, nrhs);
+        }
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int rr = rhs + k * lanes;
+            const cx<float> om = s_om[rr];
+            xv[k].s0 = xv[k].s0 + om * rv[k].s0;
+            xv[k].s1 = xv[k].s1 + om * rv[k].s1;
+            st_spinor(x, s, rr, nrhs, xv[k]);
+            rn[k].s0 = rv[k].s0 - om * av[k].s0;
+            rn[k].s1 = rv[k].s1 - om * av[k].s1;
+        }
+    }
+    st_spinor2_h(r, rs, s, rhs, nrhs, lanes, rn[0], rn[1], valid);
+}
+
+// <Ar, r> (re, im) and ||Ar||^2 per rhs from FP16 fields, FP32 partials; a reducing lane owns
+// right-hand sides lane and lane + nlanes (nlanes = nrhs / 2)
+struct FinPairs3 {
+    double* out;
+    int nlanes;
+    __device__ void operator()(int lane, const double* s) const {
+        for (int k = 0; k < 3; ++k) {
+            out[3 * lane + k] = s[k];
+            out[3 * (lane + nlanes) + k] = s[3 + k];
+        }
+    }
+};
+
+__global__ void __launch_bounds__(256) k_dotnorm_h(const __half2* __restrict__ ar, const float* __restrict__ ars,
+                                                   const __half2* __restrict__ r, const float* __restrict__ rs,
+                                                   int nsites, int nrhs, double* partials, unsigned int* ticket,
+                                                   double* out) {
+    const int nl = nrhs / 2;
+    const int lane = blockIdx.y * blockDim.x + threadIdx.x;
+    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (lane < nl)
+        for (int s = blockIdx.x * blockDim.y + threadIdx.y; s < nsites; s += gridDim.x * blockDim.y) {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const Spinor<float> a = ld_spinor_h(ar, ars, s, lane + k * nl, nrhs);
+                const Spinor<float> b = ld_spinor_h(r, rs, s, lane + k * nl, nrhs);
+                const cx<float> c = cmulc(a.s0, b.s0) + cmulc(a.s1, b.s1);
+                v[3 * k] += c.re;
+                v[3 * k + 1] += c.im;
+                v[3 * k + 2] += norm2(a.s0) + norm2(a.s1);
+            }
+        }
+    block_reduce_finalise<6>(v, partials, ticket, nl, FinPairs3{out, nl});
+}
+
+// mr_fine / smooth_fine with FP16 r, A r and D r (x and b FP32)
+smg_status smooth_fine_half(smg_mg* mg, smg_field* x, const smg_field* b, int niter, bool x_is_zero, double omega) {
+    smg_context* ctx = mg->ctx;
+    smg_field *r = mg->f_r, *Ar = mg->f_Ar, *t = mg->f_t;
+    const int V = b->g.V, nrhs = b->nrhs;
+    const dim3 blk(nrhs / 2, 512 / nrhs), grd((V + blk.y - 1) / blk.y);
+    if (x_is_zero) {
+        SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
+        k_sub_h<<<grd, blk, 0, ctx->stream>>>((const cx<float>*)b->data, nullptr, nullptr, (__half2*)r->data,
+                                              r->scale, V, nrhs);
+    } else {
+        SMG_TRY(smg_dslash(mg->dirac, false, x, t, nullptr));
+        SMG_TRY(smg_dslash(mg->dirac, true, t, Ar, nullptr));
+        k_sub_h<<<grd, blk, 0, ctx->stream>>>((const cx<float>*)b->data, (const __half2*)Ar->data, Ar->scale,
+                                              (__half2*)r->data, r->scale, V, nrhs);
+    }
+    count_launch(ctx);
+    double* sc = lvl_scal(mg, 0);
+    const ReduceLaunch rl = reduce_launch(V, nrhs / 2);
+    SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * nrhs * 3));
+    for (int it = 0; it < niter; ++it) {
+        SMG_TRY(smg_dslash(mg->dirac, false, r, t, nullptr));
+        SMG_TRY(smg_dslash(mg->dirac, true, t, Ar, nullptr));
+        if (!(omega > 0)) {
+            k_dotnorm_h<<<rl.grid, rl.block, 0, ctx->stream>>>((const __half2*)Ar->data, Ar->scale,
+                                                              (const __half2*)r->data, r->scale, V, nrhs,
+                                                              ctx->red.partials, ctx->red.tickets, sc);
+            count_launch(ctx);
+        }
+        k_smooth_update_h<<<grd, blk, 0, ctx->stream>>>((cx<float>*)x->data, (__half2*)r->data, r->scale,
+                                                        (const __half2*)Ar->data, Ar->scale,
+                                                        omega > 0 ? nullptr : sc, (float)omega, V, nrhs);
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+    }
+    return SMG_OK;
+}
+
+TransferGeom transfer_geom(const smg_mg* mg, int l, int nrhs);
+dim3 transfer_block(int nrhs);
+
+// restriction of the FP16 fine residual (k_restrict_agg with an FP16 reader)
+smg_status restrict_half(smg_mg* mg, const smg_field* r, void* out) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[0];
+    const Level& N = mg->lv[1];
+    const int nrhs = mg->work_nrhs;
+    const int nc = L.nc_next;
+    TransferGeom t = transfer_geom(mg, 0, nrhs);
+    const dim3 block = transfer_block(nrhs);
+    const dim3 grid(N.nsites, (nrhs + block.x - 1) / block.x);
+    const size_t sm = (size_t)block.x * block.y * kTransferChunk * sizeof(cx<float>);
+    const InHalf in{(const __half2*)r->data, r->scale};
+    if (nc == 8)
+        k_restrict_agg<float, 8, InHalf><<<grid, block, sm, ctx->stream>>>(L.V32, in, (cx<float>*)out, t);
+    else if (nc == 16)
+        k_restrict_agg<float, 16, InHalf><<<grid, block, sm, ctx->stream>>>(L.V32, in, (cx<float>*)out, t);
+    else
+        k_restrict_agg<float, 32, InHalf><<<grid, block, sm, ctx->stream>>>(L.V32, in, (cx<float>*)out, t);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
 
 // Fine MR on D^dag D (reference mr_smooth_op, src/smoother.cpp:26-40): on
 // entry x holds the initial guess; x_is_zero skips r = b - A x.  The residual
@@ -1293,6 +1498,7 @@ smg_status mr_coarse(smg_mg* mg, int l, void* x, const void* b, int niter, bool 
 template <typename T>
 smg_status smooth_fine(smg_mg* mg, smg_field* x, const smg_field* b, int niter, bool x_is_zero) {
     const double om = mg->lv[0].rich_omega;
+    if (mg->f_r->prec == SMG_F16) return smooth_fine_half(mg, x, b, niter, x_is_zero, om);
     if (!(om > 0)) return mr_fine<T>(mg, x, b, niter, x_is_zero);
     smg_context* ctx = mg->ctx;
     smg_field *r = mg->f_r, *Ar = mg->f_Ar;
@@ -1435,7 +1641,7 @@ smg_status restrict_to(smg_mg* mg, int l, const void* fine_or_coarse, void* out)
         const dim3 block = transfer_block(nrhs);
         const dim3 grid(N.nsites, (nrhs + block.x - 1) / block.x);
         const size_t sm = (size_t)block.x * block.y * kTransferChunk * sizeof(cx<T>);
-#define SMG_RA(NC) k_restrict_agg<T, NC><<<grid, block, sm, ctx->stream>>>(Vp<T>(L), (const cx<T>*)fine_or_coarse, (cx<T>*)out, t)
+#define SMG_RA(NC) k_restrict_agg<T, NC><<<grid, block, sm, ctx->stream>>>(Vp<T>(L), InPlain<T>{(const cx<T>*)fine_or_coarse}, (cx<T>*)out, t)
         if (nc == 8) SMG_RA(8);
         else if (nc == 16) SMG_RA(16);
         else SMG_RA(32);
@@ -1524,7 +1730,10 @@ smg_status cycle_fine(smg_mg* mg, smg_field* x, const smg_field* b) {
     const int last = (int)mg->lv.size() - 1;
     SMG_TRY(smooth_fine<T>(mg, x, b, mg->p.pre_smooth, true));
     CoarseWork& nw = mg->cw[1];
-    SMG_TRY(restrict_to<T>(mg, 0, mg->f_r->data, nw.b));
+    if (mg->f_r->prec == SMG_F16)
+        SMG_TRY(restrict_half(mg, mg->f_r, nw.b));
+    else
+        SMG_TRY(restrict_to<T>(mg, 0, mg->f_r->data, nw.b));
     SMG_TRY(cycle_coarse<T>(mg, 1, nw.x, nw.b));
     if (mg->p.w_cycle && 1 < last) {
         const Level& N = mg->lv[1];

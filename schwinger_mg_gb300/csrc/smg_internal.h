@@ -185,7 +185,7 @@ struct smg_field {
     int nrhs = 1;
     smg_precision prec = SMG_F64;
     void* data = nullptr;
-    float* scale = nullptr;  // F16 only: one per (site, rhs)
+    float* scale = nullptr;  // F16 only: one per site (largest component over its RHS)
     size_t bytes = 0;
     int64_t n_complex() const { return (int64_t)g.V * 2 * nrhs; }
 };

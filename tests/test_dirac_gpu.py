@@ -112,7 +112,7 @@ def test_bad_arguments_raise(smg_gpu):
         smg_gpu.Field(smg_gpu.Lattice(7), 1, "f64")
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7])
 @pytest.mark.parametrize("nrhs,prec", [(8, "f32"), (32, "f32"), (4, "f64"), (16, "f64")])
 def test_stencil_launch_variants_agree(smg_gpu, port, monkeypatch, variant, nrhs, prec):
     """Every launch shape the stencil autotuner can pick (row kernel, shared-memory tiles of 2, 4, 8

@@ -1,0 +1,66 @@
+"""FP16 fields with one FP32 scale per site (SMG_F16) and the MG cycle whose
+fine smoother keeps its work vectors in them: storage error bounded by the
+site scale, the operator on FP16 fields against FP64, and mixed MG-GCR
+solves that still reach a true FP64 residual of 1e-10."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_f16_round_trip_error_is_bounded_by_the_site_scale(smg_gpu):
+    L, nrhs = 32, 8
+    lat = smg_gpu.Lattice(L)
+    rng = np.random.default_rng(3)
+    # magnitudes spread over six decades across sites, equal within a site
+    mag = 10.0 ** rng.uniform(-3, 3, size=lat.V)
+    B = np.stack([smg_gpu.random_vec(lat.ndof, 10 + j) * np.repeat(mag, 2) for j in range(nrhs)])
+    f = smg_gpu.Field(lat, nrhs, "f16", data=B)
+    got = f.download().reshape(nrhs, lat.V, 2)
+    want = B.reshape(nrhs, lat.V, 2)
+    site_max = np.max(np.maximum(np.abs(want.real), np.abs(want.imag)), axis=(0, 2))
+    err = np.max(np.maximum(np.abs((got - want).real), np.abs((got - want).imag)), axis=(0, 2))
+    assert np.all(err <= 2.0 ** -11 * site_max * 1.001)
+
+
+def test_f16_nrhs_must_be_a_power_of_two(smg_gpu):
+    lat = smg_gpu.Lattice(16)
+    with pytest.raises(smg_gpu.SmgError):
+        smg_gpu.Field(lat, 12, "f16")
+
+
+@pytest.mark.parametrize("nrhs", [8, 32])
+def test_operator_on_f16_fields(smg_gpu, nrhs):
+    L = 64
+    U = smg_gpu.gauge_normal(L, 6.0, 21)
+    lat = smg_gpu.Lattice(L)
+    D = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, U), -0.05, 1.0, 1.0, 0.0)
+    B = np.stack([smg_gpu.random_vec(lat.ndof, 30 + j) for j in range(nrhs)])
+    for op in (0, 1):
+        want = D.apply_op(op, B)
+        f16 = smg_gpu.Field(lat, nrhs, "f16", data=B)
+        got = D.apply_op(op, f16).download().reshape(want.shape)
+        assert np.linalg.norm(got - want) / np.linalg.norm(want) < 2e-3
+
+
+@pytest.mark.parametrize("nrhs,levels", [(8, 2), (32, 3)])
+def test_half_smoother_cycle_and_solve(smg_gpu, nrhs, levels):
+    L = 64
+    U = smg_gpu.gauge_normal(L, 6.0, 41)
+    lat = smg_gpu.Lattice(L)
+    D = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, U), -0.05, 1.0, 1.0, 0.0)
+    kw = dict(blocks=[(4, 4), (2, 2)], chiral_split=False, null_iters=4, pre_smooth=4, post_smooth=4,
+              w_cycle=False, coarse_max_iter=20, coarse_tol=5e-2, precision="f32", seed=9)
+    mg32 = smg_gpu.MGHierarchy(D, smg_gpu.mg_params(levels, 4, 16, **kw))
+    mg16 = smg_gpu.MGHierarchy(D, smg_gpu.mg_params(levels, 4, 16, smoother_half=True, **kw))
+    B = np.stack([smg_gpu.random_vec(lat.ndof, 50 + j) for j in range(nrhs)])
+    b32 = smg_gpu.Field(lat, nrhs, "f32", data=B)
+    c32 = mg32.precondition(b32).download()
+    c16 = mg16.precondition(b32).download()
+    assert np.linalg.norm(c16 - c32) / np.linalg.norm(c32) < 2e-2
+    r = smg_gpu.fcg_solve_mg(D, lat.ndof, B, mg16, 300, 1e-10, 20)
+    assert r.status == 0 and r.true_residual < 1e-10
+    for j in (0, nrhs - 1):
+        assert np.linalg.norm(B[j] - D.apply_DdagD(r.solution[j])) / np.linalg.norm(B[j]) < 1e-10
