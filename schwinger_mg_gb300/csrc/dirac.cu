@@ -12,6 +12,7 @@
 #include "smg_internal.h"
 #include "reduce.cuh"
 #include "half.cuh"
+#include "stencil.cuh"
 
 #include <cstdlib>
 
@@ -35,11 +36,10 @@ struct DslashArgs {
     double* out = nullptr;
 };
 
-template <typename T, bool DAG, int EPI>
+template <typename T, bool DAG, int EPI, bool R1>
 __global__ void __launch_bounds__(256) k_dslash(DslashArgs<T> a) {
     constexpr int K = EPI == EPI_MR ? 3 : 1;
     const T half = T(0.5);
-    const T sgn = DAG ? T(-1) : T(1);
     const int nrhs = a.nrhs;
     const Geom g = a.g;
     T v[K];  // per-thread partials in the field precision (FP64 is scarce on this part)
@@ -73,22 +73,13 @@ __global__ void __launch_bounds__(256) k_dslash(DslashArgs<T> a) {
         const Spinor<T> pyp = ld_spinor(a.src, q_yp, rhs, nrhs);
         const Spinor<T> pym = ld_spinor(a.src, q_ym, rhs, nrhs);
         const cx<T> s0 = ps.s0, s1 = ps.s1;
-        const cx<T> a0x = u0f * pxp.s0, a1x = u0f * pxp.s1;
-        const cx<T> b0x = cmulc(u0b, pxm.s0), b1x = cmulc(u0b, pxm.s1);
-        const cx<T> a0y = u1f * pyp.s0, a1y = u1f * pyp.s1;
-        const cx<T> b0y = cmulc(u1b, pym.s0), b1y = cmulc(u1b, pym.s1);
-
         const T Cq = a.C ? a.C[q] : T(0);
         const cx<T> dg0 = mk<T>(a.diag + Cq, a.mu_eff);
         const cx<T> dg1 = mk<T>(a.diag - Cq, -a.mu_eff);
-
-        const cx<T> sr0 = (a0x + b0x) + (a0y + b0y);
-        const cx<T> sr1 = (a1x + b1x) + (a1y + b1y);
-        const cx<T> off0 = (b1x - a1x) + times_i(a1y - b1y);
-        const cx<T> off1 = (b0x - a0x) - times_i(a0y - b0y);
-
-        const cx<T> d0 = dg0 * s0 - half * (a.r * sr0 + sgn * off0);
-        const cx<T> d1 = dg1 * s1 - half * (a.r * sr1 + sgn * off1);
+        cx<T> S0, S1;
+        hop_sum<T, DAG, R1>(u0f, u0b, u1f, u1b, pxp, pxm, pyp, pym, a.r, S0, S1);
+        const cx<T> d0 = dg0 * s0 - half * S0;
+        const cx<T> d1 = dg1 * s1 - half * S1;
         Spinor<T> out;
         out.s0 = d0;
         out.s1 = d1;
@@ -144,7 +135,6 @@ __global__ void __launch_bounds__(256) k_dslash(DslashArgs<T> a) {
 template <typename T, bool DAG>
 __global__ void __launch_bounds__(256) k_dslash_r2(DslashArgs<T> a) {
     const T half = T(0.5);
-    const T sgn = DAG ? T(-1) : T(1);
     const Geom g = a.g;
     const int nrhs = a.nrhs, lanes = blockDim.x;
     const int rhs = threadIdx.x;
@@ -175,16 +165,11 @@ __global__ void __launch_bounds__(256) k_dslash_r2(DslashArgs<T> a) {
     }
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
-        const cx<T> a0x = u0f * pxp[k].s0, a1x = u0f * pxp[k].s1;
-        const cx<T> b0x = cmulc(u0b, pxm[k].s0), b1x = cmulc(u0b, pxm[k].s1);
-        const cx<T> a0y = u1f * pyp[k].s0, a1y = u1f * pyp[k].s1;
-        const cx<T> b0y = cmulc(u1b, pym[k].s0), b1y = cmulc(u1b, pym[k].s1);
-        const cx<T> sr0 = (a0x + b0x) + (a0y + b0y), sr1 = (a1x + b1x) + (a1y + b1y);
-        const cx<T> off0 = (b1x - a1x) + times_i(a1y - b1y);
-        const cx<T> off1 = (b0x - a0x) - times_i(a0y - b0y);
+        cx<T> S0, S1;
+        hop_sum<T, DAG, false>(u0f, u0b, u1f, u1b, pxp[k], pxm[k], pyp[k], pym[k], a.r, S0, S1);
         Spinor<T> o;
-        o.s0 = dg0 * ps[k].s0 - half * (a.r * sr0 + sgn * off0);
-        o.s1 = dg1 * ps[k].s1 - half * (a.r * sr1 + sgn * off1);
+        o.s0 = dg0 * ps[k].s0 - half * S0;
+        o.s1 = dg1 * ps[k].s1 - half * S1;
         st_spinor(a.dst, q, rhs + k * lanes, nrhs, o);
     }
 }
@@ -235,7 +220,6 @@ __global__ void __launch_bounds__(256) k_dslash_tile(DslashArgs<T> a, int TY) {
         __syncthreads();
     }
     const T half = T(0.5);
-    const T sgn = DAG ? T(-1) : T(1);
     const int rhs = threadIdx.x;
     if (rhs >= nrhs) return;
     auto S = [&](int par, int row, int col) -> const Spinor<T>& {
@@ -260,20 +244,14 @@ __global__ void __launch_bounds__(256) k_dslash_tile(DslashArgs<T> a, int TY) {
         const Spinor<T> pxm = S(op, r + 1, c + b);
         const Spinor<T> pyp = S(op, r + 2, c + 1);
         const Spinor<T> pym = S(op, r, c + 1);
-        const cx<T> a0x = u0f * pxp.s0, a1x = u0f * pxp.s1;
-        const cx<T> b0x = cmulc(u0b, pxm.s0), b1x = cmulc(u0b, pxm.s1);
-        const cx<T> a0y = u1f * pyp.s0, a1y = u1f * pyp.s1;
-        const cx<T> b0y = cmulc(u1b, pym.s0), b1y = cmulc(u1b, pym.s1);
         const T Cq = a.C ? a.C[q] : T(0);
         const cx<T> dg0 = mk<T>(a.diag + Cq, a.mu_eff);
         const cx<T> dg1 = mk<T>(a.diag - Cq, -a.mu_eff);
-        const cx<T> sr0 = (a0x + b0x) + (a0y + b0y);
-        const cx<T> sr1 = (a1x + b1x) + (a1y + b1y);
-        const cx<T> off0 = (b1x - a1x) + times_i(a1y - b1y);
-        const cx<T> off1 = (b0x - a0x) - times_i(a0y - b0y);
+        cx<T> S0, S1;
+        hop_sum<T, DAG, false>(u0f, u0b, u1f, u1b, pxp, pxm, pyp, pym, a.r, S0, S1);
         Spinor<T> o;
-        o.s0 = dg0 * ps.s0 - half * (a.r * sr0 + sgn * off0);
-        o.s1 = dg1 * ps.s1 - half * (a.r * sr1 + sgn * off1);
+        o.s0 = dg0 * ps.s0 - half * S0;
+        o.s1 = dg1 * ps.s1 - half * S1;
         st_spinor(a.dst, q, rhs, nrhs, o);
     }
 }
@@ -304,7 +282,7 @@ struct DslashH {
 };
 
 // thread = right-hand sides rhs and rhs + lanes (lanes = nrhs / 2) of one site
-template <bool DAG, bool IN_H, bool OUT_H>
+template <bool DAG, bool IN_H, bool OUT_H, bool R1>
 __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
     const Geom g = a.g;
     const int nrhs = a.nrhs, lanes = blockDim.x;
@@ -334,7 +312,6 @@ __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
         const cx<float> u0f = a.U[q], u0b = a.U[q_xm], u1f = a.U[g.V + q], u1b = a.U[g.V + q_ym];
         const float Cq = a.C ? a.C[q] : 0.f;
         const cx<float> dg0 = mk(a.diag + Cq, a.mu_eff), dg1 = mk(a.diag - Cq, -a.mu_eff);
-        const float sgn = DAG ? -1.f : 1.f;
         Spinor<float> ps[2], pxp[2], pxm[2], pyp[2], pym[2];
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
@@ -347,15 +324,10 @@ __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
         }
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
-            const cx<float> a0x = u0f * pxp[k].s0, a1x = u0f * pxp[k].s1;
-            const cx<float> b0x = cmulc(u0b, pxm[k].s0), b1x = cmulc(u0b, pxm[k].s1);
-            const cx<float> a0y = u1f * pyp[k].s0, a1y = u1f * pyp[k].s1;
-            const cx<float> b0y = cmulc(u1b, pym[k].s0), b1y = cmulc(u1b, pym[k].s1);
-            const cx<float> sr0 = (a0x + b0x) + (a0y + b0y), sr1 = (a1x + b1x) + (a1y + b1y);
-            const cx<float> off0 = (b1x - a1x) + times_i(a1y - b1y);
-            const cx<float> off1 = (b0x - a0x) - times_i(a0y - b0y);
-            out[k].s0 = dg0 * ps[k].s0 - 0.5f * (a.r * sr0 + sgn * off0);
-            out[k].s1 = dg1 * ps[k].s1 - 0.5f * (a.r * sr1 + sgn * off1);
+            cx<float> S0, S1;
+            hop_sum<float, DAG, R1>(u0f, u0b, u1f, u1b, pxp[k], pxm[k], pyp[k], pym[k], a.r, S0, S1);
+            out[k].s0 = dg0 * ps[k].s0 - 0.5f * S0;
+            out[k].s1 = dg1 * ps[k].s1 - 0.5f * S1;
         }
     }
     if (OUT_H) {
@@ -397,7 +369,11 @@ smg_status launch_dslash_h(smg_dirac* d, bool dag, const smg_field* src, smg_fie
     a.r = (float)d->r;
     const int lanes = nrhs / 2, rows = 256 / lanes;
     const dim3 block(lanes, rows), grid((a.g.L + rows - 1) / rows, a.g.L);
-#define SMG_DH(DG, I, O) k_dslash_h<DG, I, O><<<grid, block, 0, ctx->stream>>>(a)
+#define SMG_DH(DG, I, O)                                                          \
+    do {                                                                          \
+        if (d->r == 1.0) k_dslash_h<DG, I, O, true><<<grid, block, 0, ctx->stream>>>(a);  \
+        else k_dslash_h<DG, I, O, false><<<grid, block, 0, ctx->stream>>>(a);            \
+    } while (0)
     if (dag) {
         if (ih && oh) SMG_DH(true, true, true);
         else if (ih) SMG_DH(true, true, false);
@@ -507,6 +483,15 @@ void ensure_tile_attr() {
     });
 }
 
+// the row kernel with the spin-projected hops when r = 1
+template <typename T, bool DAG, int EPI>
+void launch_row(smg_context* ctx, const DslashArgs<T>& a, dim3 grid, dim3 block) {
+    if (a.r == T(1))
+        k_dslash<T, DAG, EPI, true><<<grid, block, 0, ctx->stream>>>(a);
+    else
+        k_dslash<T, DAG, EPI, false><<<grid, block, 0, ctx->stream>>>(a);
+}
+
 // patch mapping of the row kernel: variant 4, 5, 6 = patches px = 2, 4, 8 sites wide and
 // (256 / lanes) / px rows high, both parities
 inline void patch_shape(int nrhs, int v, int& px, int& py) {
@@ -531,9 +516,9 @@ smg_status launch_patch(smg_context* ctx, DslashArgs<T> a, bool dag, int v) {
     a.px = px;
     const dim3 block(lanes, py * px), grid(a.g.L / px, a.g.L / py, (a.nrhs + lanes - 1) / lanes);
     if (dag)
-        k_dslash<T, true, EPI_NONE><<<grid, block, 0, ctx->stream>>>(a);
+        launch_row<T, true, EPI_NONE>(ctx, a, grid, block);
     else
-        k_dslash<T, false, EPI_NONE><<<grid, block, 0, ctx->stream>>>(a);
+        launch_row<T, false, EPI_NONE>(ctx, a, grid, block);
     count_launch(ctx);
     SMG_CHECK_LAUNCH(ctx);
     return SMG_OK;
@@ -616,9 +601,9 @@ int dslash_variant(smg_context* ctx, const DslashArgs<T>& a, bool dag) {
                     const int lanes = a.nrhs < 32 ? a.nrhs : 32, rows = 256 / lanes;
                     const dim3 block(lanes, rows), grid((a.g.L + rows - 1) / rows, a.g.L, (a.nrhs + lanes - 1) / lanes);
                     if (dag)
-                        k_dslash<T, true, EPI_NONE><<<grid, block, 0, ctx->stream>>>(a);
+                        launch_row<T, true, EPI_NONE>(ctx, a, grid, block);
                     else
-                        k_dslash<T, false, EPI_NONE><<<grid, block, 0, ctx->stream>>>(a);
+                        launch_row<T, false, EPI_NONE>(ctx, a, grid, block);
                     count_launch(ctx);
                 } else if (v <= 3) {
                     launch_tile<T>(ctx, a, dag, v);
@@ -689,7 +674,7 @@ smg_status launch_dslash(smg_dirac* d, bool dag, int epi, const smg_field* src, 
         grid = rl.grid;
         block = rl.block;
     }
-#define SMG_DS(DAG, EPI) k_dslash<T, DAG, EPI><<<grid, block, 0, ctx->stream>>>(a)
+#define SMG_DS(DAG, EPI) launch_row<T, DAG, EPI>(ctx, a, grid, block)
     if (dag) {
         if (epi == EPI_NONE) SMG_DS(true, EPI_NONE);
         else if (epi == EPI_NORM) SMG_DS(true, EPI_NORM);

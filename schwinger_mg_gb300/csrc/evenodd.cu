@@ -25,6 +25,7 @@
 // plaquette insertion of a clover weight (clover_deriv_insert); the factors
 // are those of eo_fermion_force (2 x schur_deriv_plus + logdet_ee_force).
 #include "krylov.cuh"
+#include "stencil.cuh"
 
 #include <cmath>
 
@@ -52,7 +53,6 @@ struct EoArgs {
 template <typename T, bool DAG, int MODE, bool EPI>
 __global__ void __launch_bounds__(256) k_eo(EoArgs<T> a) {
     const T half = T(0.5);
-    const T sgn = DAG ? T(-1) : T(1);
     const Geom g = a.g;
     const int nrhs = a.nrhs;
     T v[1] = {T(0)};
@@ -75,17 +75,11 @@ __global__ void __launch_bounds__(256) k_eo(EoArgs<T> a) {
         const Spinor<T> pxm = ld_spinor(a.hop_src, q_xm, rhs, nrhs);
         const Spinor<T> pyp = ld_spinor(a.hop_src, q_yp, rhs, nrhs);
         const Spinor<T> pym = ld_spinor(a.hop_src, q_ym, rhs, nrhs);
-        const cx<T> a0x = u0f * pxp.s0, a1x = u0f * pxp.s1;
-        const cx<T> b0x = cmulc(u0b, pxm.s0), b1x = cmulc(u0b, pxm.s1);
-        const cx<T> a0y = u1f * pyp.s0, a1y = u1f * pyp.s1;
-        const cx<T> b0y = cmulc(u1b, pym.s0), b1y = cmulc(u1b, pym.s1);
-        const cx<T> sr0 = (a0x + b0x) + (a0y + b0y);
-        const cx<T> sr1 = (a1x + b1x) + (a1y + b1y);
-        const cx<T> off0 = (b1x - a1x) + times_i(a1y - b1y);
-        const cx<T> off1 = (b0x - a0x) - times_i(a0y - b0y);
-        // (H psi)(q) = -1/2 (r sr + sgn off), apply_hop (src/dirac.h:197-249)
-        const cx<T> h0 = -half * (a.r * sr0 + sgn * off0);
-        const cx<T> h1 = -half * (a.r * sr1 + sgn * off1);
+        // (H psi)(q) = -1/2 S, apply_hop (src/dirac.h:197-249)
+        cx<T> S0, S1;
+        hop_sum<T, DAG, false>(u0f, u0b, u1f, u1b, pxp, pxm, pyp, pym, a.r, S0, S1);
+        const cx<T> h0 = -half * S0;
+        const cx<T> h1 = -half * S1;
         const T Cq = a.C ? a.C[q] : T(0);
         const cx<T> dg0 = mk<T>(a.diag + Cq, a.mu_eff);
         const cx<T> dg1 = mk<T>(a.diag - Cq, -a.mu_eff);

@@ -660,6 +660,55 @@ __global__ void __launch_bounds__(256) k_coarse_apply_tiled(const cx<T>* __restr
     if (EPI != 0) block_reduce_finalise<K>(v, partials, ticket, nrhs, FinStore{out, K});
 }
 
+// One thread per output entry y[s][i][rhs] (rhs fastest, so a warp's stores are contiguous): the
+// 9 x NC link entries of column i are shared through L1 by the threads of the other right-hand
+// sides, the neighbour vectors by the threads of the other output dofs.  No shared memory or
+// barriers: every entry's 9 NC complex products run independently, which suits small NC and
+// few right-hand sides, where the tiled kernel above leaves most threads idle between barriers.
+template <typename T, int EPI, int NC>
+__global__ void __launch_bounds__(256) k_coarse_apply_flat(const cx<T>* __restrict__ A, VecView<T> xin,
+                                                           cx<T>* __restrict__ y, int nx, int ny,
+                                                           const cx<T>* __restrict__ w, double* partials,
+                                                           unsigned int* ticket, double* out,
+                                                           const int* __restrict__ gate) {
+    if (gate && *gate == 0) return;  // every right-hand side of the solve has converged
+    constexpr int K = EPI == 2 ? 3 : 1;
+    const int nrhs = xin.nrhs;
+    const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
+    T v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = T(0);
+    const int64_t items = (int64_t)xin.nsites * NC;
+    if (rhs < nrhs)
+        for (int64_t it = (int64_t)blockIdx.x * blockDim.y + threadIdx.y; it < items;
+             it += (int64_t)gridDim.x * blockDim.y) {
+            const int s = (int)(it / NC), i = (int)(it - (int64_t)s * NC);
+            const int x = s % nx, yy = s / nx;
+            cx<T> acc = mk<T>(0, 0);
+#pragma unroll
+            for (int d = 0; d < 9; ++d) {
+                const int xn = x + c_dx[d], yn = yy + c_dy[d];
+                const int sn = (xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn)) +
+                               nx * (yn < 0 ? yn + ny : (yn >= ny ? yn - ny : yn));
+                const cx<T>* Ad = A + ((int64_t)s * 9 + d) * NC * NC + i;      // [j][i]
+                const cx<T>* Xn = xin.p + (int64_t)sn * NC * nrhs + rhs;      // [dof][rhs]
+#pragma unroll
+                for (int j = 0; j < NC; ++j) acc = acc + Ad[j * NC] * Xn[(int64_t)j * nrhs];
+            }
+            const int64_t o = ((int64_t)s * NC + i) * nrhs + rhs;
+            y[o] = acc;
+            if (EPI == 1) {
+                v[0] += norm2(acc);
+            } else if (EPI == 2) {
+                const cx<T> c = cmulc(acc, w[o]);
+                v[0] += c.re;
+                v[1] += c.im;
+                v[2] += norm2(acc);
+            }
+        }
+    if (EPI != 0) block_reduce_finalise<K>(v, partials, ticket, nrhs, FinStore{out, K});
+}
+
 // ------------------------------------------------------------ persistent coarsest CG
 // The whole coarsest-level CG of one right-hand side in one cooperative
 // launch (SparseCoarseOp::solve without deflation, src/coarse_op.h:492-547).
@@ -1049,6 +1098,24 @@ smg_status vaxpy(smg_context* ctx, VecView<T> y, const cx<T>* x, const double* c
 template <typename T, int NC>
 smg_status coarse_apply_tiled(smg_context* ctx, const Level& L, const cx<T>* A, VecView<T> x, cx<T>* y, int epi,
                               const cx<T>* w, double* out, const int* gate) {
+    if (x.nrhs < 32) {  // few right-hand sides: one thread per output entry
+        ReduceLaunch rl = reduce_launch((int)((int64_t)L.nsites * NC), x.nrhs);
+        SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * x.nrhs * 3));
+        double* part = epi ? ctx->red.partials : nullptr;
+        unsigned int* tick = epi ? ctx->red.tickets : nullptr;
+        if (epi == 0)
+            k_coarse_apply_flat<T, 0, NC><<<rl.grid, rl.block, 0, ctx->stream>>>(A, x, y, L.nx, L.ny, w, part, tick,
+                                                                                out, gate);
+        else if (epi == 1)
+            k_coarse_apply_flat<T, 1, NC><<<rl.grid, rl.block, 0, ctx->stream>>>(A, x, y, L.nx, L.ny, w, part, tick,
+                                                                                out, gate);
+        else
+            k_coarse_apply_flat<T, 2, NC><<<rl.grid, rl.block, 0, ctx->stream>>>(A, x, y, L.nx, L.ny, w, part, tick,
+                                                                                out, gate);
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+        return SMG_OK;
+    }
     ReduceLaunch rl = reduce_launch(L.nsites, x.nrhs);  // lanes = rhs lanes, rows = 256 / lanes >= 8
     SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * x.nrhs * 3));
     if (epi == 0)
@@ -1353,18 +1420,35 @@ __global__ void __launch_bounds__(256) k_dotnorm_h(const __half2* __restrict__ a
     const int nl = nrhs / 2;
     const int lane = blockIdx.y * blockDim.x + threadIdx.x;
     float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (lane < nl)
-        for (int s = blockIdx.x * blockDim.y + threadIdx.y; s < nsites; s += gridDim.x * blockDim.y) {
+    if (lane < nl) {
+        // two sites per pass with every load of the pass issued first
+        const int stride = gridDim.x * blockDim.y;
+        for (int s0 = blockIdx.x * blockDim.y + threadIdx.y; s0 < nsites; s0 += 2 * stride) {
+            Spinor<float> A[2][2], Bv[2][2];
 #pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const Spinor<float> a = ld_spinor_h(ar, ars, s, lane + k * nl, nrhs);
-                const Spinor<float> b = ld_spinor_h(r, rs, s, lane + k * nl, nrhs);
-                const cx<float> c = cmulc(a.s0, b.s0) + cmulc(a.s1, b.s1);
-                v[3 * k] += c.re;
-                v[3 * k + 1] += c.im;
-                v[3 * k + 2] += norm2(a.s0) + norm2(a.s1);
+            for (int u = 0; u < 2; ++u) {
+                const int s = s0 + u * stride;
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    if (s < nsites) {
+                        A[u][k] = ld_spinor_h(ar, ars, s, lane + k * nl, nrhs);
+                        Bv[u][k] = ld_spinor_h(r, rs, s, lane + k * nl, nrhs);
+                    } else {
+                        A[u][k].s0 = A[u][k].s1 = Bv[u][k].s0 = Bv[u][k].s1 = mk(0.f, 0.f);
+                    }
+                }
             }
+#pragma unroll
+            for (int u = 0; u < 2; ++u)
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    const cx<float> c = cmulc(A[u][k].s0, Bv[u][k].s0) + cmulc(A[u][k].s1, Bv[u][k].s1);
+                    v[3 * k] += c.re;
+                    v[3 * k + 1] += c.im;
+                    v[3 * k + 2] += norm2(A[u][k].s0) + norm2(A[u][k].s1);
+                }
         }
+    }
     block_reduce_finalise<6>(v, partials, ticket, nl, FinPairs3{out, nl});
 }
 
