@@ -145,8 +145,8 @@ CG = dict(L=32, beta=2.0, m=0.1, r=1.0, csw=1.0, mu=0.0, seed=31, tol=1e-10, max
 HMC = dict(L=128, beta=4.0, m=0.1, r=1.0, csw=1.0, seed=2024, rng_seed=4048, tau=1.0, n_outer=10, n_inner=4,
            tol=1e-10, n_traj=20)
 BATCH = dict(n_lat=64, sizes=[64, 96, 128, 192, 256, 384], seed=5005, nrhs=8, r=1.0, csw=1.0, levels=2,
-             blocks=[(4, 4)], n_vec=8, chiral=False, w_cycle=False, null_iters=4, pre=4, post=4, coarse_max_iter=20,
-             coarse_tol=5e-2, tol=1e-10, max_iter=500, trunc=20, workers=8)
+             blocks=[(4, 4)], n_vec=8, chiral=False, w_cycle=False, null_iters=4, pre=4, post=4, coarse_max_iter=10,
+             coarse_tol=5e-2, tol=1e-10, max_iter=500, trunc=10, workers=8, smoother_half=True)
 
 
 def batch_lattices(c):
@@ -402,9 +402,9 @@ def run_ours(args, ws, rank, local):
             "e2e": {"value": ws * bytes_step / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
                     "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb, "ms_per_step": e2e_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": (140.034304e6 + 99.262464e6) if (L, nrhs) == (512, 32) else None,
+                         "traffic": (140.034048e6 + 98.370048e6) if (L, nrhs) == (512, 32) else None,
                          "traffic_unit": "bytes per launch (ncu, profiles/dslash_f32_L512_32rhs.md)",
-                         "kernel": "k_dslash<float,false,0>", "peak_source": peak_kind},
+                         "kernel": "k_dslash<float,false,0,r=1> (autotuned row kernel)", "peak_source": peak_kind},
             "gpu_launches": int(launches), "clocks": clk.summary(),
         })
     elif args.workload == "hmc":
@@ -453,6 +453,11 @@ def run_ours(args, ws, rank, local):
     elif args.workload == "batch":
         # uneven multi-lattice batch: every lattice's 8 RHS by mixed MG-GCR to 1e-10 plus its pseudofermion force
         c = dict(BATCH)
+        c["smoother_half"] = args.smoother == "f16"
+        if args.trunc:
+            c["trunc"] = args.trunc
+        if args.coarse_iters:
+            c["coarse_max_iter"] = args.coarse_iters
         if args.nrhs:
             c["nrhs"] = args.nrhs
         if args.L:
@@ -549,6 +554,8 @@ def run_ours(args, ws, rank, local):
                                    f"m~U[-0.05,0.2], c_sw=1), {nrhs} RHS each, 2-level MG (4x4, 8 null vectors), "
                                    "mixed FP32/FP64 GCR to a true FP64 residual of 1e-10, plus each lattice's "
                                    "pseudofermion force", "lattices": len(lats), "sizes": sizes,
+                       "smoother_work_vectors": "FP16, per-site scales" if c["smoother_half"] else "FP32",
+                       "gcr_truncation": c["trunc"], "coarsest_cg_iterations": c["coarse_max_iter"],
                        "sites_total": int(sum(L * L for (L, _, _, _) in lats)), "rhs_per_lattice": nrhs,
                        "worst_true_residual": worst_res, "gcr_iterations_min_max": [min(iters), max(iters)],
                        "host_workers": c["workers"], "setup_s": setup_s,
@@ -768,7 +775,8 @@ def main():
     ap.add_argument("--nrhs", type=int, default=0, help="right-hand-side count override")
     ap.add_argument("--smoother", default="f16", choices=["f32", "f16"],
                     help="mg workload: precision of the fine smoother's work vectors (f16: per-site scaled FP16)")
-    ap.add_argument("--trunc", type=int, default=0, help="mg workload: GCR truncation override")
+    ap.add_argument("--trunc", type=int, default=0, help="mg / batch workloads: GCR truncation override")
+    ap.add_argument("--coarse-iters", type=int, default=0, help="batch workload: coarsest-CG iteration cap override")
     ap.add_argument("--kernel-trace", default="", help="mg and batch workloads: write a CUPTI per-kernel summary of "
                                                          "one extra (untimed) step to this path")
     args = ap.parse_args()
