@@ -276,6 +276,8 @@ def run_ours(args, ws, rank, local):
         c["smoother_half"] = args.smoother == "f16"
         if args.trunc:
             c["trunc"] = args.trunc
+        if args.coarse_iters:
+            c["coarse_max_iter"] = args.coarse_iters
         L, nrhs = c["L"], c["nrhs"]
         U = smg.gauge_normal(L, c["beta"], c["seed"])
         lat = smg.Lattice(L)
@@ -786,7 +788,7 @@ def main():
     ap.add_argument("--smoother", default="f16", choices=["f32", "f16"],
                     help="mg workload: precision of the fine smoother's work vectors (f16: per-site scaled FP16)")
     ap.add_argument("--trunc", type=int, default=0, help="mg / batch workloads: GCR truncation override")
-    ap.add_argument("--coarse-iters", type=int, default=0, help="batch workload: coarsest-CG iteration cap override")
+    ap.add_argument("--coarse-iters", type=int, default=0, help="mg / batch workloads: coarsest-CG iteration cap override")
     ap.add_argument("--kernel-trace", default="", help="mg and batch workloads: write a CUPTI per-kernel summary of "
                                                          "one extra (untimed) step to this path")
     args = ap.parse_args()

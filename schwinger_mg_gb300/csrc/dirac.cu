@@ -279,10 +279,14 @@ struct DslashH {
     Geom g{};
     int nrhs = 1;
     float diag = 0, mu_eff = 0, r = 0;
+    // DOTS: <out, w> and ||out||^2 per block and rhs into part[block][rhs][3] (w FP16)
+    const __half2* __restrict__ w16 = nullptr;
+    const float* __restrict__ w_scale = nullptr;
+    float* __restrict__ part = nullptr;
 };
 
 // thread = right-hand sides rhs and rhs + lanes (lanes = nrhs / 2) of one site
-template <bool DAG, bool IN_H, bool OUT_H, bool R1>
+template <bool DAG, bool IN_H, bool OUT_H, bool R1, bool DOTS = false>
 __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
     const Geom g = a.g;
     const int nrhs = a.nrhs, lanes = blockDim.x;
@@ -330,12 +334,59 @@ __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
             out[k].s1 = dg1 * ps[k].s1 - 0.5f * S1;
         }
     }
+    if (DOTS) {
+        // <out, w> and ||out||^2 of this block's sites, per rhs, summed over the block's rows in a fixed order
+        __shared__ float s_d[256 * 6];
+        float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (valid) {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const Spinor<float> wv = ld_spinor_h(a.w16, a.w_scale, q, rhs + k * lanes, nrhs);
+                const cx<float> c = cmulc(out[k].s0, wv.s0) + cmulc(out[k].s1, wv.s1);
+                v[3 * k] = c.re;
+                v[3 * k + 1] = c.im;
+                v[3 * k + 2] = norm2(out[k].s0) + norm2(out[k].s1);
+            }
+        }
+        const int t = threadIdx.y * lanes + rhs;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s_d[k * 256 + t] = v[k];
+        __syncthreads();
+        if (threadIdx.y == 0) {
+            float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            for (int row = 0; row < (int)blockDim.y; ++row)
+#pragma unroll
+                for (int k = 0; k < 6; ++k) acc[k] += s_d[k * 256 + row * lanes + rhs];
+            float* p = a.part + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * nrhs * 3;
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                p[3 * (rhs + k * lanes)] = acc[3 * k];
+                p[3 * (rhs + k * lanes) + 1] = acc[3 * k + 1];
+                p[3 * (rhs + k * lanes) + 2] = acc[3 * k + 2];
+            }
+        }
+    }
     if (OUT_H) {
         st_spinor2_h(a.dst16, a.dst_scale, q, rhs, nrhs, lanes, out[0], out[1], valid);
     } else if (valid) {
         st_spinor(a.dst32, q, rhs, nrhs, out[0]);
         st_spinor(a.dst32, q, rhs + lanes, nrhs, out[1]);
     }
+}
+
+// out[j] = sum over blocks of part[block][j] (j = rhs * 3 + k), in FP64 and a fixed order
+__global__ void k_dots_finish(const float* __restrict__ part, int nblocks, int ncol, double* __restrict__ out) {
+    __shared__ double s[256];
+    const int j = blockIdx.x;
+    double acc = 0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc += (double)part[(int64_t)b * ncol + j];
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[j] = s[0];
 }
 
 smg_status launch_dslash_h(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst) {
@@ -385,6 +436,48 @@ smg_status launch_dslash_h(smg_dirac* d, bool dag, const smg_field* src, smg_fie
     }
 #undef SMG_DH
     count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+// blocks of the FP16 stencil's grid (the size of the partial-sum buffer of the fused dot/norm)
+int dslash_h_blocks(int L, int nrhs) {
+    const int rows = 256 / (nrhs / 2);
+    return ((L + rows - 1) / rows) * L;
+}
+
+// Ar = D^dag t on FP16 fields with <Ar, w>, ||Ar||^2 per rhs into out3 [rhs][3] (the MR step's
+// reductions fused into the stencil; part holds dslash_h_blocks * nrhs * 3 floats)
+smg_status launch_dslash_h_dots(smg_dirac* d, const smg_field* src, smg_field* dst, const smg_field* w, float* part,
+                                double* out3) {
+    smg_context* ctx = src->ctx;
+    const int nrhs = src->nrhs;
+    if (src->prec != SMG_F16 || dst->prec != SMG_F16 || w->prec != SMG_F16 || !f16_nrhs_ok(nrhs) || nrhs < 2)
+        return smg_fail(ctx, SMG_UNSUPPORTED, "fused FP16 stencil reductions: F16 fields, nrhs a power of two");
+    if (!d->gauge->U32) return smg_fail(ctx, SMG_DEVICE_ERROR, "FP32 links missing");
+    DslashH a;
+    a.src16 = (const __half2*)src->data;
+    a.src_scale = src->scale;
+    a.dst16 = (__half2*)dst->data;
+    a.dst_scale = dst->scale;
+    a.w16 = (const __half2*)w->data;
+    a.w_scale = w->scale;
+    a.part = part;
+    a.U = d->gauge->U32;
+    a.C = d->C32;
+    a.g = src->g;
+    a.nrhs = nrhs;
+    a.diag = (float)(2.0 * d->r + d->mass);
+    a.mu_eff = (float)(-d->mu_t);
+    a.r = (float)d->r;
+    const int lanes = nrhs / 2, rows = 256 / lanes;
+    const dim3 block(lanes, rows), grid((a.g.L + rows - 1) / rows, a.g.L);
+    if (d->r == 1.0)
+        k_dslash_h<true, true, true, true, true><<<grid, block, 0, ctx->stream>>>(a);
+    else
+        k_dslash_h<true, true, true, false, true><<<grid, block, 0, ctx->stream>>>(a);
+    k_dots_finish<<<nrhs * 3, 256, 0, ctx->stream>>>(part, (int)(grid.x * grid.y), nrhs * 3, out3);
+    count_launch(ctx, 2);
     SMG_CHECK_LAUNCH(ctx);
     return SMG_OK;
 }
@@ -736,6 +829,11 @@ smg_status smg_dslash_mr(smg_dirac* d, bool dag, const smg_field* src, smg_field
                          double* out3_dev) {
     return dslash_dispatch(d, dag, EPI_MR, src, dst, w, out3_dev);
 }
+smg_status smg_dslash_h_dots(smg_dirac* d, const smg_field* src, smg_field* dst, const smg_field* w, float* part,
+                             double* out3_dev) {
+    return launch_dslash_h_dots(d, src, dst, w, part, out3_dev);
+}
+int smg_dslash_h_blocks(int L, int nrhs) { return dslash_h_blocks(L, nrhs); }
 
 smg_status smg_dirac_apply_internal(smg_dirac* d, smg_operator op, const smg_field* src, smg_field* dst,
                                     double* norm2_out_dev) {

@@ -34,6 +34,9 @@
 smg_status smg_dslash(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, double* norm2_dev);
 smg_status smg_dslash_mr(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, const smg_field* w,
                          double* out3_dev);
+smg_status smg_dslash_h_dots(smg_dirac* d, const smg_field* src, smg_field* dst, const smg_field* w, float* part,
+                             double* out3_dev);
+int smg_dslash_h_blocks(int L, int nrhs);
 // tensor-core coarse apply (coarse_tc.cu)
 bool smg_coarse_tc_shape_ok(int nx, int ny, int ndof);
 size_t smg_coarse_tc_link_bytes(int64_t nsites);
@@ -1005,6 +1008,7 @@ struct smg_mg {
     int work_nrhs = 0;
     smg_precision work_prec = SMG_F64;
     smg_field *f_r = nullptr, *f_Ar = nullptr, *f_t = nullptr;  // fine MR temps
+    float* hdots = nullptr;  // per-block partial sums of the FP16 smoother's fused reductions
     std::vector<CoarseWork> cw;
     double* scal = nullptr;  // per-level scalar area
     size_t scal_doubles = 0;
@@ -1221,6 +1225,8 @@ smg_status free_work(smg_mg* mg) {
     smg_field_destroy(mg->f_Ar);
     smg_field_destroy(mg->f_t);
     mg->f_r = mg->f_Ar = mg->f_t = nullptr;
+    if (mg->hdots) cudaFree(mg->hdots);
+    mg->hdots = nullptr;
     for (auto& w : mg->cw) {
         for (void* p : {w.b, w.x, w.r, w.Ar, w.e, w.p})
             if (p) cudaFree(p);
@@ -1295,6 +1301,8 @@ smg_status ensure_work(smg_mg* mg, int nrhs, smg_precision prec) {
     SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &mg->f_r));
     SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &mg->f_Ar));
     SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &mg->f_t));
+    if (wp == SMG_F16)
+        SMG_CUDA(ctx, cudaMalloc(&mg->hdots, (size_t)smg_dslash_h_blocks(L, nrhs) * nrhs * 3 * sizeof(float)));
     size_t es = prec == SMG_F64 ? sizeof(cx<double>) : sizeof(cx<float>);
     mg->cw.resize(mg->lv.size());
     for (size_t l = 1; l < mg->lv.size(); ++l) {
@@ -1474,12 +1482,16 @@ smg_status smooth_fine_half(smg_mg* mg, smg_field* x, const smg_field* b, int ni
     SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * nrhs * 3));
     for (int it = 0; it < niter; ++it) {
         SMG_TRY(smg_dslash(mg->dirac, false, r, t, nullptr));
-        SMG_TRY(smg_dslash(mg->dirac, true, t, Ar, nullptr));
-        if (!(omega > 0)) {
-            k_dotnorm_h<<<rl.grid, rl.block, 0, ctx->stream>>>((const __half2*)Ar->data, Ar->scale,
-                                                              (const __half2*)r->data, r->scale, V, nrhs,
-                                                              ctx->red.partials, ctx->red.tickets, sc);
-            count_launch(ctx);
+        if (!(omega > 0) && mg->hdots) {
+            SMG_TRY(smg_dslash_h_dots(mg->dirac, t, Ar, r, mg->hdots, sc));  // MR: <Ar, r>, ||Ar||^2 fused
+        } else {
+            SMG_TRY(smg_dslash(mg->dirac, true, t, Ar, nullptr));
+            if (!(omega > 0)) {
+                k_dotnorm_h<<<rl.grid, rl.block, 0, ctx->stream>>>((const __half2*)Ar->data, Ar->scale,
+                                                                  (const __half2*)r->data, r->scale, V, nrhs,
+                                                                  ctx->red.partials, ctx->red.tickets, sc);
+                count_launch(ctx);
+            }
         }
         k_smooth_update_h<<<grd, blk, 0, ctx->stream>>>((cx<float>*)x->data, (__half2*)r->data, r->scale,
                                                         (const __half2*)Ar->data, Ar->scale,
