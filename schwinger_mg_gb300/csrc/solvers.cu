@@ -13,6 +13,7 @@
 #include "krylov.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 
 
@@ -22,6 +23,12 @@ smg_status smg_eo_schur_internal(smg_dirac* d, bool dag, const smg_field* src, s
 namespace {
 
 constexpr int kCheckEvery = 8;
+
+// SMG_CUDA_GRAPHS=0 in the environment launches the CG chunks kernel by kernel
+bool chunk_graphs_enabled() {
+    const char* e = std::getenv("SMG_CUDA_GRAPHS");
+    return !(e && std::atoi(e) == 0);
+}
 
 struct CgState {  // device arrays of length nrhs each
     double* rr = nullptr;
@@ -204,9 +211,8 @@ smg_status cg_run(smg_dirac* d, const smg_field* b, smg_field* x, int max_iter, 
     SMG_CUDA(ctx, cudaMemcpyAsync(h_active, s.n_active, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     done = (*h_active == 0);
-    while (!done && it < max_iter) {
-        int chunk = std::min(kCheckEvery, max_iter - it);
-        for (int c = 0; c < chunk; ++c) {
+    auto body = [&](int n) -> smg_status {
+        for (int c = 0; c < n; ++c) {
             SMG_TRY(apply_normal(p, t, s.pAp));
             SMG_TRY(apply_dag(t, Ap));
             k_cg_check_pap<<<(nrhs + 127) / 128, 128, 0, ctx->stream>>>(s, nrhs);
@@ -216,11 +222,50 @@ smg_status cg_run(smg_dirac* d, const smg_field* b, smg_field* x, int max_iter, 
             count_launch(ctx, 3);
             SMG_CHECK_LAUNCH(ctx);
         }
+        return SMG_OK;
+    };
+    // After the first chunk (which also settles the stencil's launch shape), a full chunk of
+    // kCheckEvery iterations is captured once as a CUDA graph and replayed: the kernels of a small
+    // lattice run a few microseconds each, so launch overhead would otherwise dominate.
+    cudaGraphExec_t gexec = nullptr;
+    uint64_t graph_launches = 0;
+    bool use_graph = chunk_graphs_enabled();
+    while (!done && it < max_iter) {
+        int chunk = std::min(kCheckEvery, max_iter - it);
+        if (use_graph && it > 0 && chunk == kCheckEvery) {
+            if (!gexec) {
+                const uint64_t l0 = ctx->launches;
+                cudaGraph_t graph = nullptr;
+                smg_status st = SMG_OK;
+                if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+                    st = body(kCheckEvery);
+                    const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+                    if (st == SMG_OK && e == cudaSuccess && graph &&
+                        cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess)
+                        gexec = nullptr;
+                    if (graph) cudaGraphDestroy(graph);
+                }
+                graph_launches = ctx->launches - l0;
+                ctx->launches = l0;
+                cudaGetLastError();
+                if (!gexec) use_graph = false;  // capture failed: launch kernel by kernel
+            }
+            if (gexec) {
+                SMG_CUDA(ctx, cudaGraphLaunch(gexec, ctx->stream));
+                count_launch(ctx, (int)graph_launches);
+            } else {
+                SMG_TRY(body(chunk));
+            }
+        } else {
+            SMG_TRY(body(chunk));
+        }
         it += chunk;
         SMG_CUDA(ctx, cudaMemcpyAsync(h_active, s.n_active, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         done = (*h_active == 0);
     }
+
+    if (gexec) cudaGraphExecDestroy(gexec);
 
     // true residual ||b - A x|| / ||b|| with the operator of the field precision
     SMG_TRY(apply_normal(x, t, nullptr));
