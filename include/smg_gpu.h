@@ -328,6 +328,12 @@ SMG_API smg_status smg_mg_params_default(smg_mg_params* p);
 SMG_API smg_status smg_mg_create(smg_dirac* d, const smg_mg_params* p, const double* warm_start,
                                  smg_mg** out);
 SMG_API smg_status smg_mg_destroy(smg_mg* mg);
+/* MGHierarchy::rebuild_deeper_levels with the level-0 Galerkin rebuild it
+ * assumes (reference src/multigrid.cpp:158-193): after the gauge field of the
+ * hierarchy's Dirac handle changed (smg_gauge_set + smg_dirac_refresh), every
+ * coarse operator is recomputed from the existing prolongators; no new
+ * near-null vectors are computed. */
+SMG_API smg_status smg_mg_rebuild(smg_mg* mg);
 /* Sizes of level `level` (0 = fine): lattice width/height in sites and dofs
  * per site. */
 SMG_API smg_status smg_mg_level_dims(smg_mg* mg, int level, int* nx, int* ny, int* ndof);
@@ -515,6 +521,26 @@ SMG_API smg_status smg_hmc_params_default(smg_hmc_params* p);
  * gauge, momenta, forces and fields stay on the device. */
 SMG_API smg_status smg_hmc_trajectory(smg_gauge* g, double mass, double wilson_r, const smg_hmc_params* p,
                                       smg_rng* rng, smg_hmc_result* res);
+
+/* ReversibilityResult (reference src/hmc.h:402-408) plus the number of solves. */
+typedef struct {
+    double gauge_delta;  /* ||U_end - U_start|| / ||U_start|| */
+    double mom_delta;    /* ||-pi_end - pi_start|| / ||pi_start|| */
+    double dH_forward;
+    double dH_backward;  /* -dH_forward for a reversible integrator */
+    int total_cg_iters;
+    int solves;
+} smg_reversibility_result;
+
+/* reversibility_test_plain (reference src/hmc_trajectory.cpp:416-509): the
+ * pseudofermion phi = D^dag eta and then the momenta are drawn from rng, the
+ * molecular dynamics of smg_hmc_trajectory runs forward, the momenta are
+ * negated, it runs again, and the links and momenta are compared with the
+ * start.  The links at entry are restored before return.  The integrator is
+ * the one smg_hmc_trajectory uses for *p (n_inner and use_eo included; the
+ * reference's test covers n_inner = 0, use_eo = 0). */
+SMG_API smg_status smg_hmc_reversibility(smg_gauge* g, double mass, double wilson_r, const smg_hmc_params* p,
+                                         smg_rng* rng, smg_reversibility_result* res);
 
 /* ------------------------------------------------------------ gauge files */
 

@@ -14,6 +14,7 @@
 //   mr_smooth, richardson_smooth_op,
 //   estimate_lambda_max                     src/smoother.h
 //   MGHierarchy::set_symmetric              src/multigrid.h:62
+//   MGHierarchy::rebuild                    src/multigrid.cpp:158-193 (rebuild_deeper_levels)
 //   fermion_action(_precond) + fermion_force as a forward/backward pair
 //                                           src/hmc.h (FermionActionResult)
 // Host vectors keep the reference layout (Vec v[2*s + spin]); each call copies
@@ -248,6 +249,8 @@ class MGHierarchy {
     void set_symmetric(double damping = 0.8) {
         check(smg_mg_set_symmetric(h_.get(), damping, nullptr), default_context(), "smg_mg_set_symmetric");
     }
+    // MGHierarchy::rebuild_deeper_levels (src/multigrid.cpp:158-193) after the links changed
+    void rebuild() { check(smg_mg_rebuild(h_.get()), default_context(), "smg_mg_rebuild"); }
     smg_mg* handle() const { return h_.get(); }
 
    private:

@@ -375,6 +375,16 @@ class Ref(_Lib):
                                       C.c_uint(seed), C.c_int(n_traj), _p(out), C.c_int(int(use_eo)))
         return U, out.reshape(n_traj, 8)[:, :8 if use_eo else 7]
 
+    def hmc_reversibility(self, U, m, r, beta, tau, n_steps, omelyan, cg_maxiter, cg_tol, csw, mu, seed):
+        """The reference's reversibility_test_plain with std::mt19937(seed): (gauge_delta,
+        mom_delta, dH_forward, dH_backward, total CG iterations)."""
+        U = _c(U)
+        out = np.zeros(5)
+        self.lib.ref_hmc_reversibility(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.c_double(beta),
+                                       C.c_double(tau), C.c_int(n_steps), C.c_int(omelyan), C.c_int(cg_maxiter),
+                                       C.c_double(cg_tol), C.c_double(csw), C.c_double(mu), C.c_uint(seed), _p(out))
+        return out
+
     def apply_delta_D(self, U, m, r, csw, mu, pi, dt, src):
         U, src = _c(U), _c(src)
         pi = np.ascontiguousarray(pi, dtype=np.float64).reshape(-1)

@@ -311,6 +311,32 @@ void ref_pseudofermion(int L, const double* U, double m, double r, double csw, d
 }
 
 
+// reversibility_test_plain (src/hmc_trajectory.cpp:416-509) with one std::mt19937(seed) and no
+// preconditioner; out = {gauge_delta, mom_delta, dH_forward, dH_backward, total_cg}.  The links
+// are restored by the reference itself.
+void ref_hmc_reversibility(int L, const double* U, double mass, double r, double beta, double tau, int n_steps,
+                           int omelyan, int cg_maxiter, double cg_tol, double c_sw, double mu_t, unsigned seed,
+                           double* out) {
+    World w(L, U);
+    HMCParams hp{};
+    hp.beta = beta;
+    hp.tau = tau;
+    hp.n_steps = n_steps;
+    hp.cg_maxiter = cg_maxiter;
+    hp.cg_tol = cg_tol;
+    hp.use_mg = false;
+    hp.c_sw = c_sw;
+    hp.mu_t = mu_t;
+    hp.omelyan = omelyan != 0;
+    std::mt19937 rng(seed);
+    ReversibilityResult res = reversibility_test_plain(w.g, w.lat, mass, r, hp, rng, nullptr);
+    out[0] = res.gauge_delta;
+    out[1] = res.mom_delta;
+    out[2] = res.dH_forward;
+    out[3] = res.dH_backward;
+    out[4] = res.total_cg;
+}
+
 // hmc_trajectory (src/hmc_trajectory.cpp:38-235, full-lattice path, no
 // preconditioner, no tracking) for n_traj trajectories threading one
 // std::mt19937(seed).  U (2V complex) is updated in place; per trajectory

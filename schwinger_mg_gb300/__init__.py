@@ -18,9 +18,11 @@ from .api import (  # noqa: F401
     mr_smooth,
     richardson_smooth,
     HMCResult,
+    ReversibilityResult,
     Rng,
     cg_solve_mixed,
     hmc_params,
+    hmc_reversibility,
     hmc_trajectory,
     MGHierarchy,
     build_full_mg,

@@ -57,6 +57,12 @@ class HMCResult(C.Structure):
                 ("dLD", C.c_double)]
 
 
+class ReversibilityResult(C.Structure):
+    """smg_reversibility_result (include/smg_gpu.h)."""
+    _fields_ = [("gauge_delta", C.c_double), ("mom_delta", C.c_double), ("dH_forward", C.c_double),
+                ("dH_backward", C.c_double), ("total_cg_iters", C.c_int), ("solves", C.c_int)]
+
+
 class MGParams(C.Structure):
     """smg_mg_params (include/smg_gpu.h)."""
     _fields_ = [("n_levels", C.c_int), ("block", (C.c_int * 2) * (MAX_LEVELS - 1)),
@@ -122,6 +128,8 @@ _SIGS = {
     "smg_rng_normal": (_st, [_vp, C.c_int64, _dp]),
     "smg_hmc_params_default": (_st, [C.POINTER(HMCParams)]),
     "smg_hmc_trajectory": (_st, [_vp, C.c_double, C.c_double, C.POINTER(HMCParams), _vp, C.POINTER(HMCResult)]),
+    "smg_hmc_reversibility": (_st, [_vp, C.c_double, C.c_double, C.POINTER(HMCParams), _vp,
+                                    C.POINTER(ReversibilityResult)]),
     "smg_fermion_force": (_st, [_vp, _vp, _dp]),
     "smg_mg_params_default": (_st, [C.POINTER(MGParams)]),
     "smg_mg_create": (_st, [_vp, C.POINTER(MGParams), _dp, C.POINTER(_vp)]),
@@ -141,6 +149,7 @@ _SIGS = {
     "smg_mr_smooth": (_st, [_vp, _vp, _vp, C.c_int]),
     "smg_richardson_smooth": (_st, [_vp, _vp, _vp, C.c_int, C.c_double]),
     "smg_estimate_lambda_max": (_st, [_vp, C.c_int, _dp]),
+    "smg_mg_rebuild": (_st, [_vp]),
     "smg_mg_estimate_lambda_max": (_st, [_vp, C.c_int, C.c_int, _dp]),
     "smg_mg_set_symmetric": (_st, [_vp, C.c_double, _dp]),
     "smg_fgmres_solve": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(SolveResult),

@@ -565,6 +565,27 @@ def hmc_trajectory(g: GaugeField, mass: float, wilson_r: float, params: _L.HMCPa
     return HMCResult(bool(r.accepted), r.dH, r.dKE, r.dSG, r.dSF, r.total_cg_iters, r.solves, r.plaquette, r.dLD)
 
 
+@dataclass
+class ReversibilityResult:
+    """ReversibilityResult (reference src/hmc.h:402-408) plus the number of solves."""
+    gauge_delta: float
+    mom_delta: float
+    dH_forward: float
+    dH_backward: float
+    total_cg_iters: int
+    solves: int
+
+
+def hmc_reversibility(g: GaugeField, mass: float, wilson_r: float, params: _L.HMCParams,
+                      rng: Rng) -> ReversibilityResult:
+    """reversibility_test_plain (reference src/hmc_trajectory.cpp:416-509): forward molecular
+    dynamics, momentum flip, backward; the links of `g` are restored afterwards."""
+    r = _L.ReversibilityResult()
+    _L.check(_L.lib().smg_hmc_reversibility(g.h, mass, wilson_r, C.byref(params), rng.h, C.byref(r)),
+             "smg_hmc_reversibility", g.ctx.h)
+    return ReversibilityResult(r.gauge_delta, r.mom_delta, r.dH_forward, r.dH_backward, r.total_cg_iters, r.solves)
+
+
 # ---------------------------------------------------------------- host inputs
 def save_gauge(g: "GaugeField | np.ndarray", beta: float, mass: float, path, avg_plaq: float | None = None) -> None:
     """save_gauge (reference src/hmc_forces.cpp:18-35): the "SWNG" file.  `g` is a
@@ -767,6 +788,12 @@ class MGHierarchy(_Handle):
         _L.check(_L.lib().smg_mg_precondition(self.h, fb.h, fx.h), "smg_mg_precondition", self.ctx.h)
         return fx.download().reshape(a.shape)
 
+
+    def rebuild(self) -> None:
+        """rebuild_deeper_levels (src/multigrid.cpp:158-193): the coarse operators from the current
+        links of the Dirac operator (refresh it after changing its gauge field) and the existing
+        prolongators."""
+        _L.check(_L.lib().smg_mg_rebuild(self.h), "smg_mg_rebuild", self.ctx.h)
 
     def estimate_lambda_max(self, level: int = 0, niter: int = 30) -> float:
         """estimate_lambda_max (src/smoother.cpp:43-60) of the level operator."""

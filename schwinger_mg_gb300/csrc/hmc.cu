@@ -6,6 +6,7 @@
 // reference's generator and distributions (momenta, eta, Metropolis) and runs
 // the integrator schedule.  Momenta and forces are lexicographic [mu][s]
 // doubles, as the reference's MomentumField and force arrays.
+#include <algorithm>
 #include <cmath>
 #include <random>
 #include <vector>
@@ -48,6 +49,12 @@ __global__ void k_links_exp(cx<double>* __restrict__ U, const double* __restrict
     sincos(scale * pi[i], &sn, &cs);
     cx<double>& u = U[(int64_t)mu * g.V + site_q(g, s % g.L, s / g.L)];
     u = u * mk(cs, sn);
+}
+
+// pi = -pi (the momentum flip between the two halves of reversibility_test_plain)
+__global__ void k_negate(double* __restrict__ pi, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) pi[i] = -pi[i];
 }
 
 // sum of squares of n doubles (MomentumField::kinetic_energy without the 1/2)
@@ -180,6 +187,17 @@ struct Hmc {
         return SMG_OK;
     }
 
+    // H = KE + S_G + S_F (+ -2 log det D_ee on the even-odd path) with the current links
+    smg_status hamiltonian(double* ke, double* sg, double* sf, double* ld) {
+        SMG_TRY(refresh());
+        SMG_TRY(kinetic(ke));
+        SMG_TRY(smg_gauge_action(g, p.beta, sg));
+        SMG_TRY(fermion_action(sf));
+        return log_det_term(ld);
+    }
+
+    smg_status evolve() { return p.n_inner > 0 ? evolve_nested() : evolve_plain(); }
+
     // plain_leapfrog_evolve (hmc_trajectory.cpp:243-409): gauge + fermion force at every kick
     smg_status evolve_plain() {
         const double dt = p.tau / p.n_steps;
@@ -255,6 +273,94 @@ struct Hmc {
     }
 };
 
+smg_status hmc_check(smg_gauge* g, const smg_hmc_params* p) {
+    smg_context* ctx = g->ctx;
+    if (p->n_steps < 1 || p->n_inner < 0 || !(p->tau > 0) || p->cg_maxiter < 1 || !(p->cg_tol > 0))
+        return smg_fail(ctx, SMG_BAD_ARG, "hmc: n_steps >= 1, n_inner >= 0, tau > 0, cg_maxiter >= 1, cg_tol > 0");
+    if (p->use_eo && (p->mixed_precision || g->g.L % 2))
+        return smg_fail(ctx, SMG_UNSUPPORTED, "hmc: the even-odd path runs FP64 solves on an even L");
+    return SMG_OK;
+}
+
+// device state of one trajectory; the links at entry are kept in U_old
+smg_status hmc_setup(Hmc& h, smg_gauge* g, double mass, double wilson_r, const smg_hmc_params* p) {
+    smg_context* ctx = g->ctx;
+    h.ctx = ctx;
+    h.g = g;
+    h.p = *p;
+    h.mass = mass;
+    h.r = wilson_r;
+    const int V = g->g.V, L = g->g.L;
+    const size_t fb = (size_t)2 * V * sizeof(double);
+    SMG_CUDA(ctx, cudaMalloc(&h.pi, fb));
+    SMG_CUDA(ctx, cudaMalloc(&h.gf, fb));
+    SMG_CUDA(ctx, cudaMalloc(&h.ff, fb));
+    SMG_CUDA(ctx, cudaMalloc(&h.scal, 64));
+    SMG_CUDA(ctx, cudaMalloc(&h.U_old, (size_t)2 * V * sizeof(cx<double>)));
+    SMG_CUDA(ctx, cudaMemcpyAsync(h.U_old, g->U64, (size_t)2 * V * sizeof(cx<double>), cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+    SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.phi));
+    SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.X));
+    SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.eta));
+    SMG_TRY(smg_dirac_create(g, mass, wilson_r, p->c_sw, p->mu_t, &h.d));
+    h.eo = p->use_eo != 0;
+    if (h.eo) {
+        SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.chi));
+        SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.psi));
+        SMG_CUDA(ctx, cudaMalloc(&h.W, (size_t)V * sizeof(double)));
+        SMG_CUDA(ctx, cudaMemsetAsync(h.phi->data, 0, h.phi->bytes, ctx->stream));
+        SMG_CUDA(ctx, cudaMemsetAsync(h.eta->data, 0, h.eta->bytes, ctx->stream));
+    }
+    return SMG_OK;
+}
+
+// momenta: MomentumField::randomise (hmc_forces.cpp:64-69), mu-major then site order
+smg_status hmc_draw_momenta(Hmc& h, smg_rng* rng) {
+    smg_context* ctx = h.ctx;
+    std::vector<double> pi_h((size_t)h.n2());
+    std::normal_distribution<double> dist(0.0, 1.0);
+    for (auto& v : pi_h) v = dist(rng->gen);
+    SMG_CUDA(ctx, cudaMemcpyAsync(h.pi, pi_h.data(), pi_h.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SMG_OK;
+}
+
+smg_status hmc_draw_pseudofermion(Hmc& h, smg_rng* rng) {
+    smg_context* ctx = h.ctx;
+    const int V = h.g->g.V;
+    if (h.eo) {
+        // phi_o = M^dag eta_o, eta_o = random_vec(V, rng) on the odd sites
+        // (generate_pseudofermion_eo, src/dirac.h:491-497); the odd half of a field is the
+        // reference's half vector in order
+        std::vector<double> eta_h((size_t)2 * V);
+        std::normal_distribution<double> dist(0.0, 1.0);
+        for (size_t i = 0; i < (size_t)V; ++i) {
+            const double im = dist(rng->gen);
+            const double re = dist(rng->gen);
+            eta_h[2 * i] = re;
+            eta_h[2 * i + 1] = im;
+        }
+        SMG_CUDA(ctx, cudaMemcpyAsync((char*)h.eta->data + h.eta->bytes / 2, eta_h.data(), h.eta->bytes / 2,
+                                      cudaMemcpyHostToDevice, ctx->stream));
+        SMG_TRY(smg_eo_schur_internal(h.d, true, h.eta, h.phi, h.chi, nullptr));
+        SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        return SMG_OK;
+    }
+    // pseudofermion phi = D^dag eta, eta = random_vec(n, rng) (hmc_trajectory.cpp:32-36); the
+    // reference's random_vec draws each entry's imaginary part first (GCC argument order)
+    std::vector<double> eta_h((size_t)4 * V);
+    std::normal_distribution<double> dist(0.0, 1.0);
+    for (size_t i = 0; i < (size_t)2 * V; ++i) {
+        const double im = dist(rng->gen);
+        const double re = dist(rng->gen);
+        eta_h[2 * i] = re;
+        eta_h[2 * i + 1] = im;
+    }
+    SMG_TRY(smg_field_upload(h.eta, eta_h.data()));
+    return smg_dirac_apply(h.d, SMG_OP_DDAG, h.eta, h.phi);
+}
+
 }  // namespace
 
 // gauge_force into a device array (defined next to the kernel in gauge.cu)
@@ -307,91 +413,18 @@ SMG_API smg_status smg_hmc_trajectory(smg_gauge* g, double mass, double wilson_r
                                       smg_rng* rng, smg_hmc_result* res) {
     if (!g || !p || !rng) return SMG_BAD_ARG;
     smg_context* ctx = g->ctx;
-    if (p->n_steps < 1 || p->n_inner < 0 || !(p->tau > 0) || p->cg_maxiter < 1 || !(p->cg_tol > 0))
-        return smg_fail(ctx, SMG_BAD_ARG, "hmc: n_steps >= 1, n_inner >= 0, tau > 0, cg_maxiter >= 1, cg_tol > 0");
-    if (p->use_eo && (p->mixed_precision || g->g.L % 2))
-        return smg_fail(ctx, SMG_UNSUPPORTED, "hmc: the even-odd path runs FP64 solves on an even L");
+    SMG_TRY(hmc_check(g, p));
+    const int V = g->g.V;
     Hmc h;
-    h.ctx = ctx;
-    h.g = g;
-    h.p = *p;
-    h.mass = mass;
-    h.r = wilson_r;
-    const int V = g->g.V, L = g->g.L;
-    const size_t fb = (size_t)2 * V * sizeof(double);
-    SMG_CUDA(ctx, cudaMalloc(&h.pi, fb));
-    SMG_CUDA(ctx, cudaMalloc(&h.gf, fb));
-    SMG_CUDA(ctx, cudaMalloc(&h.ff, fb));
-    SMG_CUDA(ctx, cudaMalloc(&h.scal, 64));
-    SMG_CUDA(ctx, cudaMalloc(&h.U_old, (size_t)2 * V * sizeof(cx<double>)));
-    SMG_CUDA(ctx, cudaMemcpyAsync(h.U_old, g->U64, (size_t)2 * V * sizeof(cx<double>), cudaMemcpyDeviceToDevice,
-                                  ctx->stream));
-    SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.phi));
-    SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.X));
-    SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.eta));
-    SMG_TRY(smg_dirac_create(g, mass, wilson_r, p->c_sw, p->mu_t, &h.d));
-    h.eo = p->use_eo != 0;
-    if (h.eo) {
-        SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.chi));
-        SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.psi));
-        SMG_CUDA(ctx, cudaMalloc(&h.W, (size_t)V * sizeof(double)));
-        SMG_CUDA(ctx, cudaMemsetAsync(h.phi->data, 0, h.phi->bytes, ctx->stream));
-        SMG_CUDA(ctx, cudaMemsetAsync(h.eta->data, 0, h.eta->bytes, ctx->stream));
-    }
-
-    // momenta: MomentumField::randomise (hmc_forces.cpp:64-69), mu-major then site order
-    {
-        std::vector<double> pi_h((size_t)2 * V);
-        std::normal_distribution<double> dist(0.0, 1.0);
-        for (auto& v : pi_h) v = dist(rng->gen);
-        SMG_CUDA(ctx, cudaMemcpyAsync(h.pi, pi_h.data(), fb, cudaMemcpyHostToDevice, ctx->stream));
-        SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    }
-    if (h.eo) {
-        // phi_o = M^dag eta_o, eta_o = random_vec(V, rng) on the odd sites
-        // (generate_pseudofermion_eo, src/dirac.h:491-497); the odd half of a field is the
-        // reference's half vector in order
-        std::vector<double> eta_h((size_t)2 * V);
-        std::normal_distribution<double> dist(0.0, 1.0);
-        for (size_t i = 0; i < (size_t)V; ++i) {
-            const double im = dist(rng->gen);
-            const double re = dist(rng->gen);
-            eta_h[2 * i] = re;
-            eta_h[2 * i + 1] = im;
-        }
-        SMG_CUDA(ctx, cudaMemcpyAsync((char*)h.eta->data + h.eta->bytes / 2, eta_h.data(), h.eta->bytes / 2,
-                                      cudaMemcpyHostToDevice, ctx->stream));
-        SMG_TRY(smg_eo_schur_internal(h.d, true, h.eta, h.phi, h.chi, nullptr));
-        SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    } else {
-        // pseudofermion phi = D^dag eta, eta = random_vec(n, rng) (hmc_trajectory.cpp:32-36); the
-        // reference's random_vec draws each entry's imaginary part first (GCC argument order)
-        std::vector<double> eta_h((size_t)4 * V);
-        std::normal_distribution<double> dist(0.0, 1.0);
-        for (size_t i = 0; i < (size_t)2 * V; ++i) {
-            const double im = dist(rng->gen);
-            const double re = dist(rng->gen);
-            eta_h[2 * i] = re;
-            eta_h[2 * i + 1] = im;
-        }
-        SMG_TRY(smg_field_upload(h.eta, eta_h.data()));
-        SMG_TRY(smg_dirac_apply(h.d, SMG_OP_DDAG, h.eta, h.phi));
-    }
+    SMG_TRY(hmc_setup(h, g, mass, wilson_r, p));
+    SMG_TRY(hmc_draw_momenta(h, rng));
+    SMG_TRY(hmc_draw_pseudofermion(h, rng));
 
     double KE0 = 0, SG0 = 0, SF0 = 0, LD0 = 0;
-    SMG_TRY(h.kinetic(&KE0));
-    SMG_TRY(smg_gauge_action(g, p->beta, &SG0));
-    SMG_TRY(h.fermion_action(&SF0));
-    SMG_TRY(h.log_det_term(&LD0));
-
-    SMG_TRY(p->n_inner > 0 ? h.evolve_nested() : h.evolve_plain());
-
+    SMG_TRY(h.hamiltonian(&KE0, &SG0, &SF0, &LD0));
+    SMG_TRY(h.evolve());
     double KE1 = 0, SG1 = 0, SF1 = 0, LD1 = 0;
-    SMG_TRY(h.refresh());
-    SMG_TRY(h.kinetic(&KE1));
-    SMG_TRY(smg_gauge_action(g, p->beta, &SG1));
-    SMG_TRY(h.fermion_action(&SF1));
-    SMG_TRY(h.log_det_term(&LD1));
+    SMG_TRY(h.hamiltonian(&KE1, &SG1, &SF1, &LD1));
     const double dH = (KE1 + SG1 + SF1 + LD1) - (KE0 + SG0 + SF0 + LD0);
     // Metropolis (hmc_trajectory.cpp:226-228): the uniform draw happens only when needed
     bool accept = p->force_accept != 0 || dH < 0;
@@ -417,6 +450,61 @@ SMG_API smg_status smg_hmc_trajectory(smg_gauge* g, double mass, double wilson_r
         res->plaquette = plaq;
         res->dLD = LD1 - LD0;
     }
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_hmc_reversibility(smg_gauge* g, double mass, double wilson_r, const smg_hmc_params* p,
+                                         smg_rng* rng, smg_reversibility_result* res) {
+    if (!g || !p || !rng || !res) return SMG_BAD_ARG;
+    smg_context* ctx = g->ctx;
+    SMG_TRY(hmc_check(g, p));
+    const int n2 = 2 * g->g.V;
+    Hmc h;
+    SMG_TRY(hmc_setup(h, g, mass, wilson_r, p));
+    // the reference draws the pseudofermion before the momenta here (hmc_trajectory.cpp:428-433)
+    SMG_TRY(hmc_draw_pseudofermion(h, rng));
+    SMG_TRY(hmc_draw_momenta(h, rng));
+    std::vector<double> pi0((size_t)n2), pi1((size_t)n2);
+    SMG_CUDA(ctx, cudaMemcpyAsync(pi0.data(), h.pi, (size_t)n2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+
+    double KE0 = 0, SG0 = 0, SF0 = 0, LD0 = 0, KE1 = 0, SG1 = 0, SF1 = 0, LD1 = 0, KE2 = 0, SG2 = 0, SF2 = 0, LD2 = 0;
+    SMG_TRY(h.hamiltonian(&KE0, &SG0, &SF0, &LD0));
+    SMG_TRY(h.evolve());
+    SMG_TRY(h.hamiltonian(&KE1, &SG1, &SF1, &LD1));
+    k_negate<<<(n2 + 255) / 256, 256, 0, ctx->stream>>>(h.pi, n2);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    SMG_TRY(h.evolve());
+    SMG_TRY(h.hamiltonian(&KE2, &SG2, &SF2, &LD2));
+
+    // relative differences of the links and of the flipped momenta (hmc_trajectory.cpp:484-503)
+    std::vector<cx<double>> u0((size_t)n2), u1((size_t)n2);
+    SMG_CUDA(ctx, cudaMemcpyAsync(u0.data(), h.U_old, (size_t)n2 * sizeof(cx<double>), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    SMG_CUDA(ctx, cudaMemcpyAsync(u1.data(), g->U64, (size_t)n2 * sizeof(cx<double>), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    SMG_CUDA(ctx, cudaMemcpyAsync(pi1.data(), h.pi, (size_t)n2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double un = 0, ud = 0, pn = 0, pd = 0;
+    for (int i = 0; i < n2; ++i) {
+        const double dr = u1[i].re - u0[i].re, di = u1[i].im - u0[i].im;
+        un += u0[i].re * u0[i].re + u0[i].im * u0[i].im;
+        ud += dr * dr + di * di;
+        const double dp = -pi1[i] - pi0[i];
+        pn += pi0[i] * pi0[i];
+        pd += dp * dp;
+    }
+    // the links at entry are restored
+    SMG_CUDA(ctx, cudaMemcpyAsync(g->U64, h.U_old, (size_t)n2 * sizeof(cx<double>), cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+    SMG_TRY(smg_gauge_ensure_f32(g));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    res->gauge_delta = std::sqrt(ud / std::max(un, 1e-30));
+    res->mom_delta = std::sqrt(pd / std::max(pn, 1e-30));
+    res->dH_forward = (KE1 + SG1 + SF1 + LD1) - (KE0 + SG0 + SF0 + LD0);
+    res->dH_backward = (KE2 + SG2 + SF2 + LD2) - (KE1 + SG1 + SF1 + LD1);
+    res->total_cg_iters = h.cg_iters;
+    res->solves = h.solves;
     return SMG_OK;
 }
 

@@ -2142,6 +2142,45 @@ smg_status build(smg_mg* mg, const double* warm) {
     return SMG_OK;
 }
 
+// The Galerkin operators of every level recomputed from the current links with the existing
+// prolongators (MGHierarchy::rebuild_deeper_levels with the level-0 rebuild it assumes,
+// src/multigrid.cpp:158-193); the FP32 and tensor-core copies are refreshed in place, so a captured
+// cycle stays valid.
+smg_status rebuild_operators(smg_mg* mg) {
+    smg_context* ctx = mg->ctx;
+    const Geom g = mg->dirac->gauge->g;
+    const int nlev = (int)mg->lv.size();
+    {
+        Level& L = mg->lv[0];
+        const int nc = L.nc_next, nagg = L.nagg_x * L.nagg_y;
+        const int nh = (L.ax + 2) * (L.ay + 2);
+        cx<double>* W = nullptr;
+        SMG_CUDA(ctx, cudaMallocAsync(&W, (size_t)nagg * nc * nh * 2 * sizeof(cx<double>), ctx->stream));
+        smg_dirac* d = mg->dirac;
+        k_W0<<<nagg, 256, 0, ctx->stream>>>(L.V64, d->gauge->U64, d->C64, g, L.ax, L.ay, nc, 2.0 * d->r + d->mass,
+                                           d->mu_t, d->r, W);
+        k_galerkin0<<<dim3(nagg, 9), 256, 0, ctx->stream>>>(W, L.nagg_x, L.nagg_y, L.ax, L.ay, nc, mg->lv[1].A64);
+        count_launch(ctx, 2);
+        SMG_CHECK_LAUNCH(ctx);
+        SMG_CUDA(ctx, cudaFreeAsync(W, ctx->stream));
+    }
+    for (int l = 1; l < nlev - 1; ++l) {
+        Level& L = mg->lv[l];
+        const int nc = L.nc_next, nagg = L.nagg_x * L.nagg_y;
+        const size_t sm2 = (size_t)L.ndof * nc * sizeof(cx<double>);
+        int threads = 256;
+        while (threads * 4 < nc * nc) threads *= 2;
+        SMG_CUDA(ctx, cudaFuncSetAttribute(k_galerkin_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
+        k_galerkin_c<<<nagg, threads, sm2, ctx->stream>>>(L.A64, L.V64, L.nx, L.ny, L.ax, L.ay, L.ndof, nc,
+                                                          mg->lv[l + 1].A64);
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+    }
+    SMG_TRY(make_f32_copies(mg));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SMG_OK;
+}
+
 void destroy_levels(smg_mg* mg) {
     for (auto& L : mg->lv) {
         for (void* p : {(void*)L.V64, (void*)L.V32, (void*)L.A64, (void*)L.A32, L.Atc})
@@ -2594,6 +2633,11 @@ SMG_API smg_status smg_mg_set_symmetric(smg_mg* mg, double damping, double* omeg
     if (omega)
         for (int l = 0; l + 1 < nl; ++l) omega[l] = om[l];
     return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_rebuild(smg_mg* mg) {
+    if (!mg) return SMG_BAD_ARG;
+    return rebuild_operators(mg);
 }
 
 }  // extern "C"

@@ -88,6 +88,15 @@ def hmc_case(ref, name, L, beta, m, r, csw, gseed, seed, n_steps, omelyan, n_tra
     print("wrote", name, out[:, :2].tolist())
 
 
+def reversibility_case(ref, name, L, beta, m, r, csw, gseed, seed, n_steps, omelyan, tau=1.0):
+    """The reference's reversibility_test_plain (forward, momentum flip, backward)."""
+    U = gauge_normal(L, beta, gseed).reshape(-1)
+    out = ref.hmc_reversibility(U, m, r, beta, tau, n_steps, omelyan, 10000, 1e-12, csw, 0.0, seed)
+    np.savez_compressed(OUT / f"{name}.npz", L=L, beta=beta, m=m, r=r, csw=csw, gseed=gseed, seed=seed,
+                        n_steps=n_steps, omelyan=omelyan, tau=tau, cg_tol=1e-12, U=U, result=out)
+    print("wrote", name, out.tolist())
+
+
 def solvers_case(ref, name, L, beta, m, r, csw, gseed, seed, null_iters=5):
     """PCG (plain with a start vector, and with the symmetric MG), FGMRES (with MG and
     unpreconditioned, Ritz harvesting on), the Richardson/MR smoothers, lambda_max,
@@ -182,6 +191,8 @@ CASES = {
     "gauge_L8": lambda ref: gauge_files_case(ref, "gauge_L8", 8, 3.0, 0.05, 81),
     "eo_L16_clover_twist": lambda ref: eo_case(ref, "eo_L16_clover_twist", 16, 2.0, 0.1, 1.0, 1.0, 0.2, 91, 92),
     "eo_L16_wilson": lambda ref: eo_case(ref, "eo_L16_wilson", 16, 4.0, 0.2, 1.0, 0.0, 0.0, 93, 94),
+    "reversibility_L8_omelyan": lambda ref: reversibility_case(ref, "reversibility_L8_omelyan", 8, 4.0, 0.1, 1.0,
+                                                               1.0, 71, 72, 5, 1),
     "hmc_eo_L8": lambda ref: hmc_eo_case(ref, "hmc_eo_L8", 8, 4.0, 0.1, 1.0, 1.0, 95, 96, 6, 3),
     "delta_L16": lambda ref: delta_case(ref, "delta_L16", 16, 3.0, 0.1, 1.0, 1.0, 0.1, 97, 98, 0.05),
 }

@@ -35,6 +35,39 @@ def test_trajectories_match_reference(smg_gpu, name):
     assert np.max(np.abs(g.U.reshape(-1) - d["U_out"])) < 1e-10
 
 
+def test_reversibility_matches_reference(smg_gpu):
+    """reversibility_test_plain (src/hmc_trajectory.cpp:416-509): the reference's dH of the forward
+    half, dH_backward = -dH_forward, and links and momenta back to rounding after the flip."""
+    d = golden("reversibility_L8_omelyan")
+    L = int(d["L"])
+    lat = smg_gpu.Lattice(L)
+    g = smg_gpu.GaugeField(lat, d["U"])
+    p = smg_gpu.hmc_params(float(d["beta"]), tau=float(d["tau"]), n_steps=int(d["n_steps"]),
+                           omelyan=bool(d["omelyan"]), cg_tol=float(d["cg_tol"]), c_sw=float(d["csw"]))
+    res = smg_gpu.hmc_reversibility(g, float(d["m"]), float(d["r"]), p, smg_gpu.Rng(int(d["seed"])))
+    gauge_delta, mom_delta, dH_f, dH_b, _ = d["result"]
+    assert abs(res.dH_forward - dH_f) < 1e-8 * max(1.0, abs(dH_f))
+    assert abs(res.dH_backward - dH_b) < 1e-8 * max(1.0, abs(dH_b))
+    # the reference reaches 6e-14 / 2e-13 with CG to 1e-12; the residual of the solves bounds both
+    assert res.gauge_delta < 1e-10 and mom_delta < 1e-10 and res.mom_delta < 1e-10
+    assert abs(res.dH_forward + res.dH_backward) < 1e-8
+    # the links at entry are restored
+    assert np.max(np.abs(g.U.reshape(-1) - d["U"])) == 0.0
+
+
+@pytest.mark.parametrize("n_inner,use_eo", [(4, False), (0, True)])
+def test_reversibility_nested_and_even_odd(smg_gpu, n_inner, use_eo):
+    """The nested integrator and the even-odd path are reversible to the solver tolerance."""
+    L = 16
+    lat = smg_gpu.Lattice(L)
+    g = smg_gpu.GaugeField(lat, smg_gpu.gauge_normal(L, 4.0, 81))
+    p = smg_gpu.hmc_params(4.0, tau=0.5, n_steps=4, omelyan=True, n_inner=n_inner, cg_tol=1e-12, c_sw=1.0,
+                           use_eo=use_eo)
+    res = smg_gpu.hmc_reversibility(g, 0.1, 1.0, p, smg_gpu.Rng(82))
+    assert res.gauge_delta < 1e-10 and res.mom_delta < 1e-9
+    assert abs(res.dH_forward + res.dH_backward) < 1e-7 * max(1.0, abs(res.dH_forward))
+
+
 def _nested_restatement(port, rng, U, m, r, csw, beta, tau, n_outer, n_inner, tol):
     """The nested Omelyan integrator (fermion force outside, leapfrog on the gauge force inside)
     restated with the oracle's forces and solver; momenta, eta and the links in the reference's

@@ -148,3 +148,59 @@ def test_three_level_cycle_matches_oracle(smg_gpu, port, chiral, k):
     got = mg.precondition(b)
     want = port.mgN_precondition(po, U, b)
     assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-9
+
+
+def test_rebuild_after_gauge_change(smg_gpu):
+    """rebuild_deeper_levels: after new links, every coarse operator is the Galerkin product of the
+    new operator with the existing prolongators (2 levels: equal to a fresh build on the same null
+    vectors; level 2: A2 = P1^dag A1 P1 through the host transfer entry points)."""
+    L = 32
+    U1 = smg_gpu.gauge_normal(L, 3.0, 301)
+    U2 = smg_gpu.gauge_normal(L, 3.0, 302)
+    lat = smg_gpu.Lattice(L)
+    g = smg_gpu.GaugeField(lat, U1)
+    D = smg_gpu.DiracOp(lat, g, 0.1, 1.0, 1.0, 0.0)
+    p = smg_gpu.mg_params(3, 4, 4, blocks=[(4, 4), (2, 2)], null_iters=3, coarse_tol=1e-13, coarse_max_iter=2000,
+                          seed=3)
+    mg = smg_gpu.MGHierarchy(D, p)
+    nv = mg.null_vecs_l0.copy()
+    g.set_links(U2)
+    D.refresh()
+    mg.rebuild()
+    # level 1: the fresh hierarchy on U2 with the same null vectors has the same prolongator
+    g2 = smg_gpu.GaugeField(lat, U2)
+    D2 = smg_gpu.DiracOp(lat, g2, 0.1, 1.0, 1.0, 0.0)
+    fresh = smg_gpu.MGHierarchy(D2, smg_gpu.mg_params(2, 4, 4, null_iters=0, coarse_tol=1e-13, seed=3),
+                                warm_start=nv)
+    assert np.max(np.abs(mg.coarse_op(1) - fresh.coarse_op(1))) / np.max(np.abs(fresh.coarse_op(1))) < 1e-12
+    # level 2 is the Galerkin product of the rebuilt level-1 operator
+    nx, ny, nd = mg.level_dims(2)
+    rng = np.random.default_rng(5)
+    xc = rng.standard_normal(nx * ny * nd) + 1j * rng.standard_normal(nx * ny * nd)
+    want = mg.restrict_vec(1, mg.coarse_apply(1, mg.prolong(1, xc)))
+    got = mg.coarse_apply(2, xc)
+    assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-12
+
+
+def test_rebuild_f32_cycle_matches_fresh_hierarchy(smg_gpu):
+    """An F32 hierarchy rebuilt after new links applies the same cycle as one built on the new links
+    from the same null vectors (its FP32 copies and captured cycle are refreshed in place)."""
+    L = 32
+    lat = smg_gpu.Lattice(L)
+    g = smg_gpu.GaugeField(lat, smg_gpu.gauge_normal(L, 3.0, 303))
+    D = smg_gpu.DiracOp(lat, g, 0.1, 1.0, 1.0, 0.0)
+    p = smg_gpu.mg_params(2, 4, 4, null_iters=3, coarse_tol=1e-10, coarse_max_iter=500, precision="f32", seed=7)
+    mg = smg_gpu.MGHierarchy(D, p)
+    src = smg_gpu.random_vec(lat.ndof, 11)
+    mg.precondition(src)  # one cycle on the old links before the rebuild
+    U2 = smg_gpu.gauge_normal(L, 3.0, 304)
+    g.set_links(U2)
+    D.refresh()
+    mg.rebuild()
+    g2 = smg_gpu.GaugeField(lat, U2)
+    D2 = smg_gpu.DiracOp(lat, g2, 0.1, 1.0, 1.0, 0.0)
+    fresh = smg_gpu.MGHierarchy(
+        D2, smg_gpu.mg_params(2, 4, 4, null_iters=0, coarse_tol=1e-10, coarse_max_iter=500, precision="f32", seed=7),
+        warm_start=mg.null_vecs_l0)
+    a, b = mg.precondition(src), fresh.precondition(src)
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-4
