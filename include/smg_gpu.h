@@ -328,6 +328,47 @@ SMG_API smg_status smg_mg_params_default(smg_mg_params* p);
 SMG_API smg_status smg_mg_create(smg_dirac* d, const smg_mg_params* p, const double* warm_start,
                                  smg_mg** out);
 SMG_API smg_status smg_mg_destroy(smg_mg* mg);
+/* ------------------------------------------------------ coarse deflation */
+
+/* Outcome of the thick-restart Lanczos run of smg_mg_setup_deflation
+ * (TRLMResult, reference src/eigensolver.h). */
+typedef struct {
+    int converged;
+    int restarts;
+    int iterations; /* Lanczos steps */
+    int n_kr;       /* Krylov space size used */
+} smg_deflation_info;
+
+/* SparseCoarseOp::setup_deflation with the default TRLM solver (reference
+ * src/coarse_op.cpp:10-54, trlm_eigensolver src/eigensolver_core.cpp:691):
+ * the n_ev lowest eigenpairs of the level-1 operator A_c = P^dag D^dag D P,
+ * held by the hierarchy.  n_kr <= 0 selects min(2 n_ev + 10, dim); the
+ * reference's setup_sparse_coarse passes max_restarts = 100, tol = 1e-10.
+ * With eigenpairs held and level 1 the coarsest level, the coarsest CG starts
+ * from the deflated guess x0 = sum_i v_i (v_i^dag b) / lambda_i
+ * (SparseCoarseOp::solve, src/coarse_op.h:492-547).  n_ev = 0 clears the
+ * space.  Returns SMG_NOT_CONVERGED (pairs still stored) when Lanczos did not
+ * converge within max_restarts. */
+SMG_API smg_status smg_mg_setup_deflation(smg_mg* mg, int n_ev, int n_kr, int max_restarts, double tol,
+                                          smg_deflation_info* info);
+/* Replaces the eigenpairs (defl_vecs / defl_vals): n vectors of the level-1
+ * dimension, interleaved complex128, in the reference's coarse layout
+ * c[b * k + kv] with b the lexicographic coarse site. */
+SMG_API smg_status smg_mg_set_deflation(smg_mg* mg, int n, const double* vals, const double* vecs);
+/* Copies out the eigenpair count and (when the pointers are non-null) the
+ * values and vectors in the layout of smg_mg_set_deflation. */
+SMG_API smg_status smg_mg_get_deflation(smg_mg* mg, int* n, double* vals, double* vecs);
+/* rr_evolve on the current level-1 operator (reference
+ * src/eigen_evolve.cpp:48-105, as evolve_coarse_deflation applies it after
+ * the coarse operator was rebuilt, src/hmc_multiscale.cpp:278-331 without
+ * forecasting): Rayleigh-Ritz of the held vectors; max_residual (optional)
+ * receives max_i ||A v_i - lambda_i v_i|| / ||A v_i||. */
+SMG_API smg_status smg_mg_deflation_rr(smg_mg* mg, double* max_residual);
+/* CoarseDeflState::lowmode_solution (reference src/hmc.h:312-323):
+ * x = P sum_i v_i (v_i^dag P^dag phi) / lambda_i for single-RHS F64 fields
+ * (terms with lambda_i <= 1e-14 skipped). */
+SMG_API smg_status smg_mg_lowmode_solution(smg_mg* mg, const smg_field* phi, smg_field* x);
+
 /* MGHierarchy::rebuild_deeper_levels with the level-0 Galerkin rebuild it
  * assumes (reference src/multigrid.cpp:158-193): after the gauge field of the
  * hierarchy's Dirac handle changed (smg_gauge_set + smg_dirac_refresh), every
@@ -541,6 +582,77 @@ typedef struct {
  * reference's test covers n_inner = 0, use_eo = 0). */
 SMG_API smg_status smg_hmc_reversibility(smg_gauge* g, double mass, double wilson_r, const smg_hmc_params* p,
                                          smg_rng* rng, smg_reversibility_result* res);
+
+/* Outer integrators of hmc_trajectory_mg_multiscale (OuterIntegrator,
+ * reference src/hmc.h:327-336). */
+typedef enum {
+    SMG_OUTER_LEAPFROG = 0,
+    SMG_OUTER_OMELYAN = 1,  /* 2MN, lambda = 0.1932 */
+    SMG_OUTER_FGI = 2,      /* force-gradient PQPQP, lambda = 1/6, xi = 1/72 */
+    SMG_OUTER_FGI_QPQPQ = 3 /* force-gradient QPQPQ */
+} smg_outer_integrator;
+
+/* MGMultiScaleParams (reference src/hmc.h:338-357) without the research
+ * options (deflation refresh, perturbative MG refresh, eigenspace tracking,
+ * even-odd), which stay at their defaults (off). */
+typedef struct {
+    double beta;
+    double tau;
+    int n_outer;
+    int n_inner;
+    int cg_maxiter;
+    double cg_tol;
+    int inner_smooth;  /* MR steps before and after the low-mode projection (0 = raw projection) */
+    int outer_type;    /* smg_outer_integrator */
+    double c_sw;
+    double mu_t;
+} smg_ms_params;
+
+/* MGMultiScaleResult (reference src/hmc.h:359-367) without the wall-clock
+ * split, plus the plaquette after the trajectory and the number of solves. */
+typedef struct {
+    int accepted;
+    double dH, dKE, dSG, dSF;
+    int highmode_cg_iters; /* every MG-preconditioned CG iteration of the trajectory */
+    int lowmode_force_evals;
+    int solves;
+    double plaquette;
+} smg_ms_result;
+
+/* coarse_lowmode_force (reference src/hmc_multiscale.cpp:237-276): with
+ * smooth_iters > 0, x = MR(D^dag D, phi, from 0), x += lowmode_solution of
+ * phi - D^dag D x, x = MR(D^dag D, phi, from x); with smooth_iters = 0 the
+ * low-mode solution of phi itself; force = fermion_force(D, x) as host
+ * [mu][s] doubles.  The low-mode solution uses mg's level-0 prolongator and
+ * deflation space. */
+SMG_API smg_status smg_coarse_lowmode_force(smg_dirac* d, smg_mg* mg, const smg_field* phi, int smooth_iters,
+                                            double* force);
+
+/* n_outer = 4, n_inner = 5, cg_maxiter = 500, cg_tol = 1e-10,
+ * inner_smooth = 3, leapfrog, c_sw = mu_t = 0, beta = 4, tau = 1. */
+SMG_API smg_status smg_ms_params_default(smg_ms_params* p);
+
+/* hmc_trajectory_mg_multiscale (reference src/hmc_multiscale.cpp:340-886,
+ * without tracking, forecasting or refreshes): the outer integrator kicks with
+ * the gauge force plus the fermion force (MG-preconditioned CG with the
+ * hierarchy mg) minus the low-mode force, the inner leapfrog (n_inner steps)
+ * with the low-mode force alone; the low-mode force is the fermion force of
+ * coarse_lowmode_force (src/hmc_multiscale.cpp:237-276) built from mg's
+ * level-0 prolongator and deflation space.  mg must have been built on a
+ * Dirac operator over the gauge handle g; its coarse operators are not
+ * rebuilt during the trajectory (smg_mg_rebuild and smg_mg_deflation_rr
+ * between trajectories do what the reference's MG-HMC driver does).  As in the
+ * reference the momenta are drawn first and the pseudofermion is drawn twice,
+ * the second draw used. */
+SMG_API smg_status smg_hmc_mg_multiscale(smg_gauge* g, double mass, double wilson_r, const smg_ms_params* p,
+                                         smg_mg* mg, smg_rng* rng, smg_ms_result* res);
+/* reversibility_test_mg_multiscale (reference src/hmc_multiscale.cpp:963-
+ * 1000): momenta then one pseudofermion from rng, forward molecular dynamics,
+ * momentum flip, backward; the links at entry are restored.  As in the
+ * reference the forces use mu_t = 0 and FGI_QPQPQ runs as FGI. */
+SMG_API smg_status smg_hmc_mg_multiscale_reversibility(smg_gauge* g, double mass, double wilson_r,
+                                                       const smg_ms_params* p, smg_mg* mg, smg_rng* rng,
+                                                       smg_reversibility_result* res);
 
 /* ------------------------------------------------------------ gauge files */
 

@@ -15,6 +15,9 @@
 //   estimate_lambda_max                     src/smoother.h
 //   MGHierarchy::set_symmetric              src/multigrid.h:62
 //   MGHierarchy::rebuild                    src/multigrid.cpp:158-193 (rebuild_deeper_levels)
+//   MGHierarchy::setup_deflation / deflation / deflation_rr / lowmode_solution
+//                                           src/coarse_op.cpp:10-54, src/eigen_evolve.cpp:48, src/hmc.h:307
+//   coarse_lowmode_force                    src/hmc_multiscale.cpp:237-276
 //   fermion_action(_precond) + fermion_force as a forward/backward pair
 //                                           src/hmc.h (FermionActionResult)
 // Host vectors keep the reference layout (Vec v[2*s + spin]); each call copies
@@ -251,6 +254,43 @@ class MGHierarchy {
     }
     // MGHierarchy::rebuild_deeper_levels (src/multigrid.cpp:158-193) after the links changed
     void rebuild() { check(smg_mg_rebuild(h_.get()), default_context(), "smg_mg_rebuild"); }
+    // the deflation part of setup_sparse_coarse (src/multigrid.cpp:754-794): TRLM eigenpairs of the
+    // level-1 operator, the coarsest CG of a two-level hierarchy starting from the deflated guess
+    smg_deflation_info setup_deflation(int n_defl, int n_kr = 0, int max_restarts = 100, double tol = 1e-10) {
+        smg_deflation_info info{};
+        const smg_status s = smg_mg_setup_deflation(h_.get(), n_defl, n_kr, max_restarts, tol, &info);
+        if (s != SMG_NOT_CONVERGED) check(s, default_context(), "smg_mg_setup_deflation");
+        return info;
+    }
+    // sparse_Ac.defl_vals / defl_vecs
+    void deflation(std::vector<double>& vals, std::vector<Vec>& vecs) const {
+        int n = 0;
+        check(smg_mg_get_deflation(h_.get(), &n, nullptr, nullptr), default_context(), "smg_mg_get_deflation");
+        int nx = 0, ny = 0, nd = 0;
+        check(smg_mg_level_dims(h_.get(), 1, &nx, &ny, &nd), default_context(), "smg_mg_level_dims");
+        const size_t dim = (size_t)nx * ny * nd;
+        std::vector<cx> flat((size_t)n * dim);
+        vals.resize(n);
+        check(smg_mg_get_deflation(h_.get(), &n, vals.data(), reinterpret_cast<double*>(flat.data())),
+              default_context(), "smg_mg_get_deflation");
+        vecs.assign(n, Vec());
+        for (int i = 0; i < n; ++i) vecs[i].assign(flat.begin() + i * dim, flat.begin() + (i + 1) * dim);
+    }
+    // evolve_coarse_deflation without forecasting (src/hmc_multiscale.cpp:278-331) after rebuild()
+    double deflation_rr() {
+        double r = 0;
+        check(smg_mg_deflation_rr(h_.get(), &r), default_context(), "smg_mg_deflation_rr");
+        return r;
+    }
+    // CoarseDeflState::lowmode_solution (src/hmc.h:312-323)
+    Vec lowmode_solution(const Vec& phi) {
+        DeviceField fb(D_.lat.L, 1), fx(D_.lat.L, 1);
+        fb.upload(phi);
+        check(smg_mg_lowmode_solution(h_.get(), fb.get(), fx.get()), default_context(), "smg_mg_lowmode_solution");
+        Vec x(phi.size());
+        fx.download(x);
+        return x;
+    }
     smg_mg* handle() const { return h_.get(); }
 
    private:
@@ -383,6 +423,18 @@ inline void fermion_force(const DiracOp& D, const Vec& X, std::array<RVec, 2>& f
     fx.upload(X);
     RVec flat(2 * (size_t)D.lat.V);
     check(smg_fermion_force(D.handle(), fx.get(), flat.data()), default_context(), "smg_fermion_force");
+    force[0].assign(flat.begin(), flat.begin() + D.lat.V);
+    force[1].assign(flat.begin() + D.lat.V, flat.end());
+}
+
+// coarse_lowmode_force (src/hmc_multiscale.cpp:237-276) with mg's prolongator and deflation space
+inline void coarse_lowmode_force(const DiracOp& D, MGHierarchy& mg, const Vec& phi, std::array<RVec, 2>& force,
+                                 int smooth_iters = 0) {
+    DeviceField fp(D.lat.L, 1);
+    fp.upload(phi);
+    RVec flat(2 * (size_t)D.lat.V);
+    check(smg_coarse_lowmode_force(D.handle(), mg.handle(), fp.get(), smooth_iters, flat.data()), default_context(),
+          "smg_coarse_lowmode_force");
     force[0].assign(flat.begin(), flat.begin() + D.lat.V);
     force[1].assign(flat.begin() + D.lat.V, flat.end());
 }

@@ -54,6 +54,12 @@ class RefMGParams(C.Structure):
                                          "pre_smooth", "post_smooth", "n_defl")]
 
 
+class RefMSParams(C.Structure):
+    _fields_ = [("beta", C.c_double), ("tau", C.c_double), ("n_outer", C.c_int), ("n_inner", C.c_int),
+                ("cg_maxiter", C.c_int), ("cg_tol", C.c_double), ("inner_smooth", C.c_int), ("outer_type", C.c_int),
+                ("c_sw", C.c_double), ("mu_t", C.c_double)]
+
+
 class OrcMG2Params(C.Structure):
     _fields_ = [("L", C.c_int), ("bs", C.c_int), ("k", C.c_int), ("m", C.c_double), ("r", C.c_double),
                 ("csw", C.c_double), ("mu", C.c_double), ("pre_smooth", C.c_int), ("post_smooth", C.c_int),
@@ -374,6 +380,42 @@ class Ref(_Lib):
                                       C.c_double(cg_tol), C.c_double(csw), C.c_double(mu), C.c_int(force_accept),
                                       C.c_uint(seed), C.c_int(n_traj), _p(out), C.c_int(int(use_eo)))
         return U, out.reshape(n_traj, 8)[:, :8 if use_eo else 7]
+
+    def ms_setup(self, U, m, r, csw, mu, params: RefMGParams, seed, phi, smooth, cdim):
+        """A reference hierarchy with TRLM coarse deflation: (null vectors, deflation values,
+        deflation vectors, low-mode solution of phi, coarse_lowmode_force(phi, smooth))."""
+        U, phi = _c(U), _c(phi)
+        L = self._L(U)
+        n = 2 * L * L
+        nv = np.zeros((params.k_null, n), dtype=np.complex128)
+        vals = np.zeros(params.n_defl)
+        vecs = np.zeros((params.n_defl, cdim), dtype=np.complex128)
+        low = np.zeros(n, dtype=np.complex128)
+        force = np.zeros(2 * L * L)
+        self.lib.ref_ms_setup(C.c_int(L), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw), C.c_double(mu),
+                              C.byref(params), C.c_uint(seed), _p(phi), C.c_int(smooth), _p(nv),
+                              vals.ctypes.data_as(C.POINTER(C.c_double)), _p(vecs), _p(low),
+                              force.ctypes.data_as(C.POINTER(C.c_double)))
+        return nv, vals, vecs, low, force
+
+    def ms_trajectories(self, U, m, r, params: RefMGParams, mg_seed, ms: RefMSParams, seed, n_traj):
+        """hmc_trajectory_mg_multiscale n_traj times (deflation evolved between accepted
+        trajectories); returns the final links and per trajectory (accepted, dH, dKE, dSG, dSF,
+        CG iterations, low-mode evaluations, plaquette)."""
+        U = _c(U).copy()
+        out = np.zeros(9 * n_traj)
+        self.lib.ref_ms_trajectories(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.byref(params),
+                                     C.c_uint(mg_seed), C.byref(ms), C.c_uint(seed), C.c_int(n_traj),
+                                     out.ctypes.data_as(C.POINTER(C.c_double)))
+        return U, out.reshape(n_traj, 9)[:, :8]
+
+    def ms_reversibility(self, U, m, r, params: RefMGParams, mg_seed, ms: RefMSParams, seed):
+        U = _c(U)
+        out = np.zeros(5)
+        self.lib.ref_ms_reversibility(C.c_int(self._L(U)), _p(U), C.c_double(m), C.c_double(r), C.byref(params),
+                                      C.c_uint(mg_seed), C.byref(ms), C.c_uint(seed),
+                                      out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
 
     def hmc_reversibility(self, U, m, r, beta, tau, n_steps, omelyan, cg_maxiter, cg_tol, csw, mu, seed):
         """The reference's reversibility_test_plain with std::mt19937(seed): (gauge_delta,

@@ -311,6 +311,121 @@ void ref_pseudofermion(int L, const double* U, double m, double r, double csw, d
 }
 
 
+struct RefMSParams {
+    double beta, tau;
+    int n_outer, n_inner, cg_maxiter;
+    double cg_tol;
+    int inner_smooth, outer_type;
+    double c_sw, mu_t;
+};
+
+static MGMultiScaleParams ms_params(const RefMSParams* q) {
+    MGMultiScaleParams mp;
+    mp.beta = q->beta;
+    mp.tau = q->tau;
+    mp.n_outer = q->n_outer;
+    mp.n_inner = q->n_inner;
+    mp.cg_maxiter = q->cg_maxiter;
+    mp.cg_tol = q->cg_tol;
+    mp.inner_smooth = q->inner_smooth;
+    mp.outer_type = static_cast<OuterIntegrator>(q->outer_type);
+    mp.c_sw = q->c_sw;
+    mp.mu_t = q->mu_t;
+    return mp;
+}
+
+// A hierarchy with coarse deflation (build_mg_hierarchy + setup_sparse_coarse with TRLM,
+// src/multigrid.cpp:754-794): its level-0 null vectors (k_null x ndof), the deflation pairs
+// (n_defl values, n_defl x coarse-dim vectors), CoarseDeflState::lowmode_solution of phi and
+// coarse_lowmode_force(D, cdefl, P, phi, smooth) (src/hmc_multiscale.cpp:237-276).
+void ref_ms_setup(int L, const double* U, double m, double r, double csw, double mu, const RefMGParams* p,
+                  unsigned seed, const double* phi, int smooth, double* null_out, double* vals_out, double* vecs_out,
+                  double* lowmode_out, double* force_out) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    MGHierarchy mg = ref_build(D, *p, seed, nullptr);
+    for (int i = 0; i < p->k_null; ++i) from_vec(mg.null_vecs_l0[i], null_out + (size_t)2 * w.lat.ndof * i);
+    CoarseDeflState cdefl;
+    cdefl.eigvecs = mg.sparse_Ac.defl_vecs;
+    cdefl.eigvals = mg.sparse_Ac.defl_vals;
+    const int cdim = mg.sparse_Ac.dim;
+    for (size_t i = 0; i < cdefl.eigvals.size(); ++i) {
+        vals_out[i] = cdefl.eigvals[i];
+        from_vec(cdefl.eigvecs[i], vecs_out + (size_t)2 * cdim * i);
+    }
+    const Vec ph = to_vec(phi, w.lat.ndof);
+    from_vec(cdefl.lowmode_solution(ph, mg.geo_prolongators[0]), lowmode_out);
+    std::array<RVec, 2> f;
+    coarse_lowmode_force(D, cdefl, mg.geo_prolongators[0], ph, f, smooth);
+    for (int mu2 = 0; mu2 < 2; ++mu2)
+        for (int s = 0; s < w.lat.V; ++s) force_out[mu2 * w.lat.V + s] = f[mu2][s];
+}
+
+// hmc_trajectory_mg_multiscale (src/hmc_multiscale.cpp:340-886) n_traj times from one
+// std::mt19937(seed) with the hierarchy of ref_ms_setup as preconditioner, prolongator and
+// deflation space; after an accepted trajectory the sparse coarse operator is rebuilt for the new
+// links and the deflation pairs follow by evolve_coarse_deflation, as the MG-HMC driver does
+// (src/mode_mg_hmc.cpp:280-288).  U is updated in place; per trajectory out[9 t + {0..8}] =
+// accepted, dH, dKE, dSG, dSF, CG iterations, low-mode force evaluations, plaquette, max |dH| 0.
+void ref_ms_trajectories(int L, double* U, double m, double r, const RefMGParams* p, unsigned mg_seed,
+                         const RefMSParams* q, unsigned seed, int n_traj, double* out) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, q->c_sw, q->mu_t);
+    MGHierarchy mg = ref_build(D, *p, mg_seed, nullptr);
+    CoarseDeflState cdefl;
+    cdefl.eigvecs = mg.sparse_Ac.defl_vecs;
+    cdefl.eigvals = mg.sparse_Ac.defl_vals;
+    auto& P = mg.geo_prolongators[0];
+    std::function<Vec(const Vec&)> pre = [&mg](const Vec& b) -> Vec { return mg.precondition(b); };
+    const MGMultiScaleParams mp = ms_params(q);
+    std::mt19937 rng(seed);
+    for (int t = 0; t < n_traj; ++t) {
+        MGMultiScaleResult res = hmc_trajectory_mg_multiscale(w.g, w.lat, m, r, mp, cdefl, P, pre, rng);
+        double* o = out + 9 * t;
+        o[0] = res.accepted ? 1.0 : 0.0;
+        o[1] = res.dH;
+        o[2] = res.dKE;
+        o[3] = res.dSG;
+        o[4] = res.dSF;
+        o[5] = res.highmode_cg_iters;
+        o[6] = res.lowmode_force_evals;
+        o[7] = w.g.avg_plaq();
+        o[8] = 0.0;
+        if (res.accepted) {
+            DiracOp Dn(w.lat, w.g, m, r, q->c_sw, q->mu_t);
+            OpApply An = [&Dn](const Vec& s, Vec& d) { Dn.apply_DdagD(s, d); };
+            mg.sparse_Ac.build(P, An, w.lat.ndof);
+            evolve_coarse_deflation(cdefl, mg.sparse_Ac, nullptr);
+        }
+    }
+    for (int mu2 = 0; mu2 < 2; ++mu2)
+        for (int s = 0; s < w.lat.V; ++s) {
+            U[2 * (mu2 * w.lat.V + s)] = w.g.U[mu2][s].real();
+            U[2 * (mu2 * w.lat.V + s) + 1] = w.g.U[mu2][s].imag();
+        }
+}
+
+// reversibility_test_mg_multiscale (src/hmc_multiscale.cpp:963-1000) with the hierarchy of
+// ref_ms_setup; out = {gauge_delta, mom_delta, dH_forward, dH_backward, total CG}
+void ref_ms_reversibility(int L, const double* U, double m, double r, const RefMGParams* p, unsigned mg_seed,
+                          const RefMSParams* q, unsigned seed, double* out) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, q->c_sw, q->mu_t);
+    MGHierarchy mg = ref_build(D, *p, mg_seed, nullptr);
+    CoarseDeflState cdefl;
+    cdefl.eigvecs = mg.sparse_Ac.defl_vecs;
+    cdefl.eigvals = mg.sparse_Ac.defl_vals;
+    std::function<Vec(const Vec&)> pre = [&mg](const Vec& b) -> Vec { return mg.precondition(b); };
+    std::mt19937 rng(seed);
+    ReversibilityResult res =
+        reversibility_test_mg_multiscale(w.g, w.lat, m, r, ms_params(q), cdefl, mg.geo_prolongators[0], pre, rng);
+    out[0] = res.gauge_delta;
+    out[1] = res.mom_delta;
+    out[2] = res.dH_forward;
+    out[3] = res.dH_backward;
+    out[4] = res.total_cg;
+}
+
 // reversibility_test_plain (src/hmc_trajectory.cpp:416-509) with one std::mt19937(seed) and no
 // preconditioner; out = {gauge_delta, mom_delta, dH_forward, dH_backward, total_cg}.  The links
 // are restored by the reference itself.

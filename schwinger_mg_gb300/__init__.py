@@ -23,6 +23,11 @@ from .api import (  # noqa: F401
     cg_solve_mixed,
     hmc_params,
     hmc_reversibility,
+    hmc_mg_multiscale,
+    hmc_mg_multiscale_reversibility,
+    ms_params,
+    MSResult,
+    coarse_lowmode_force,
     hmc_trajectory,
     MGHierarchy,
     build_full_mg,

@@ -63,6 +63,25 @@ class ReversibilityResult(C.Structure):
                 ("dH_backward", C.c_double), ("total_cg_iters", C.c_int), ("solves", C.c_int)]
 
 
+class DeflationInfo(C.Structure):
+    """smg_deflation_info (include/smg_gpu.h)."""
+    _fields_ = [("converged", C.c_int), ("restarts", C.c_int), ("iterations", C.c_int), ("n_kr", C.c_int)]
+
+
+class MSParams(C.Structure):
+    """smg_ms_params (include/smg_gpu.h)."""
+    _fields_ = [("beta", C.c_double), ("tau", C.c_double), ("n_outer", C.c_int), ("n_inner", C.c_int),
+                ("cg_maxiter", C.c_int), ("cg_tol", C.c_double), ("inner_smooth", C.c_int), ("outer_type", C.c_int),
+                ("c_sw", C.c_double), ("mu_t", C.c_double)]
+
+
+class MSResult(C.Structure):
+    """smg_ms_result (include/smg_gpu.h)."""
+    _fields_ = [("accepted", C.c_int), ("dH", C.c_double), ("dKE", C.c_double), ("dSG", C.c_double),
+                ("dSF", C.c_double), ("highmode_cg_iters", C.c_int), ("lowmode_force_evals", C.c_int),
+                ("solves", C.c_int), ("plaquette", C.c_double)]
+
+
 class MGParams(C.Structure):
     """smg_mg_params (include/smg_gpu.h)."""
     _fields_ = [("n_levels", C.c_int), ("block", (C.c_int * 2) * (MAX_LEVELS - 1)),
@@ -150,6 +169,17 @@ _SIGS = {
     "smg_richardson_smooth": (_st, [_vp, _vp, _vp, C.c_int, C.c_double]),
     "smg_estimate_lambda_max": (_st, [_vp, C.c_int, _dp]),
     "smg_mg_rebuild": (_st, [_vp]),
+    "smg_mg_setup_deflation": (_st, [_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(DeflationInfo)]),
+    "smg_mg_set_deflation": (_st, [_vp, C.c_int, _dp, _dp]),
+    "smg_mg_get_deflation": (_st, [_vp, C.POINTER(C.c_int), _dp, _dp]),
+    "smg_mg_deflation_rr": (_st, [_vp, _dp]),
+    "smg_mg_lowmode_solution": (_st, [_vp, _vp, _vp]),
+    "smg_coarse_lowmode_force": (_st, [_vp, _vp, _vp, C.c_int, _dp]),
+    "smg_ms_params_default": (_st, [C.POINTER(MSParams)]),
+    "smg_hmc_mg_multiscale": (_st, [_vp, C.c_double, C.c_double, C.POINTER(MSParams), _vp, _vp,
+                                    C.POINTER(MSResult)]),
+    "smg_hmc_mg_multiscale_reversibility": (_st, [_vp, C.c_double, C.c_double, C.POINTER(MSParams), _vp, _vp,
+                                                  C.POINTER(ReversibilityResult)]),
     "smg_mg_estimate_lambda_max": (_st, [_vp, C.c_int, C.c_int, _dp]),
     "smg_mg_set_symmetric": (_st, [_vp, C.c_double, _dp]),
     "smg_fgmres_solve": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(SolveResult),

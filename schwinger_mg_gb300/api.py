@@ -586,6 +586,65 @@ def hmc_reversibility(g: GaugeField, mass: float, wilson_r: float, params: _L.HM
     return ReversibilityResult(r.gauge_delta, r.mom_delta, r.dH_forward, r.dH_backward, r.total_cg_iters, r.solves)
 
 
+def coarse_lowmode_force(D: DiracOp, mg: MGHierarchy, phi, smooth_iters: int = 0) -> np.ndarray:
+    """coarse_lowmode_force (reference src/hmc_multiscale.cpp:237-276); returns F[mu][s]."""
+    f = Field(D.lat, 1, "f64", D.ctx, data=phi)
+    out = np.empty(2 * D.lat.V)
+    _L.check(_L.lib().smg_coarse_lowmode_force(D.h, mg.h, f.h, smooth_iters, _ptr(out)), "smg_coarse_lowmode_force",
+             D.ctx.h)
+    return out.reshape(2, D.lat.V)
+
+
+OUTER_INTEGRATORS = {"leapfrog": 0, "omelyan": 1, "fgi": 2, "fgi_qpqpq": 3}
+
+
+def ms_params(beta: float, tau: float = 1.0, n_outer: int = 4, n_inner: int = 5, cg_maxiter: int = 500,
+              cg_tol: float = 1e-10, inner_smooth: int = 3, outer="leapfrog", c_sw: float = 0.0,
+              mu_t: float = 0.0) -> _L.MSParams:
+    """smg_ms_params from MGMultiScaleParams (reference src/hmc.h:338-357)."""
+    p = _L.MSParams()
+    _L.check(_L.lib().smg_ms_params_default(C.byref(p)), "smg_ms_params_default")
+    p.beta, p.tau, p.n_outer, p.n_inner = beta, tau, n_outer, n_inner
+    p.cg_maxiter, p.cg_tol, p.inner_smooth = cg_maxiter, cg_tol, inner_smooth
+    p.outer_type = OUTER_INTEGRATORS[outer] if isinstance(outer, str) else int(outer)
+    p.c_sw, p.mu_t = c_sw, mu_t
+    return p
+
+
+@dataclass
+class MSResult:
+    """MGMultiScaleResult (reference src/hmc.h:359-367) plus the plaquette and the number of solves."""
+    accepted: bool
+    dH: float
+    dKE: float
+    dSG: float
+    dSF: float
+    highmode_cg_iters: int
+    lowmode_force_evals: int
+    solves: int
+    plaquette: float
+
+
+def hmc_mg_multiscale(g: GaugeField, mass: float, wilson_r: float, params: _L.MSParams, mg: MGHierarchy,
+                      rng: Rng) -> MSResult:
+    """hmc_trajectory_mg_multiscale (reference src/hmc_multiscale.cpp:340-886) on the device."""
+    r = _L.MSResult()
+    _L.check(_L.lib().smg_hmc_mg_multiscale(g.h, mass, wilson_r, C.byref(params), mg.h, rng.h, C.byref(r)),
+             "smg_hmc_mg_multiscale", g.ctx.h)
+    return MSResult(bool(r.accepted), r.dH, r.dKE, r.dSG, r.dSF, r.highmode_cg_iters, r.lowmode_force_evals, r.solves,
+                    r.plaquette)
+
+
+def hmc_mg_multiscale_reversibility(g: GaugeField, mass: float, wilson_r: float, params: _L.MSParams,
+                                    mg: MGHierarchy, rng: Rng) -> ReversibilityResult:
+    """reversibility_test_mg_multiscale (reference src/hmc_multiscale.cpp:963-1000)."""
+    r = _L.ReversibilityResult()
+    _L.check(_L.lib().smg_hmc_mg_multiscale_reversibility(g.h, mass, wilson_r, C.byref(params), mg.h, rng.h,
+                                                          C.byref(r)),
+             "smg_hmc_mg_multiscale_reversibility", g.ctx.h)
+    return ReversibilityResult(r.gauge_delta, r.mom_delta, r.dH_forward, r.dH_backward, r.total_cg_iters, r.solves)
+
+
 # ---------------------------------------------------------------- host inputs
 def save_gauge(g: "GaugeField | np.ndarray", beta: float, mass: float, path, avg_plaq: float | None = None) -> None:
     """save_gauge (reference src/hmc_forces.cpp:18-35): the "SWNG" file.  `g` is a
@@ -788,6 +847,51 @@ class MGHierarchy(_Handle):
         _L.check(_L.lib().smg_mg_precondition(self.h, fb.h, fx.h), "smg_mg_precondition", self.ctx.h)
         return fx.download().reshape(a.shape)
 
+
+    def setup_deflation(self, n_ev: int, n_kr: int = 0, max_restarts: int = 100, tol: float = 1e-10,
+                        allow_unconverged: bool = False) -> _L.DeflationInfo:
+        """SparseCoarseOp::setup_deflation (src/coarse_op.cpp:10-54, TRLM): the n_ev lowest
+        eigenpairs of the level-1 operator; the coarsest CG of a two-level hierarchy then starts
+        from the deflated guess."""
+        info = _L.DeflationInfo()
+        st = _L.lib().smg_mg_setup_deflation(self.h, n_ev, n_kr, max_restarts, tol, C.byref(info))
+        if not (allow_unconverged and st == _L.NOT_CONVERGED):
+            _L.check(st, "smg_mg_setup_deflation", self.ctx.h)
+        return info
+
+    def set_deflation(self, vals, vecs) -> None:
+        """Installs eigenpairs (vectors in the reference's coarse layout, one per row)."""
+        vals = np.ascontiguousarray(vals, dtype=np.float64).reshape(-1)
+        vecs = _as_c128(vecs).reshape(len(vals), -1)
+        _L.check(_L.lib().smg_mg_set_deflation(self.h, len(vals), _ptr(vals), _ptr(vecs.view(np.float64))),
+                 "smg_mg_set_deflation", self.ctx.h)
+
+    @property
+    def deflation(self):
+        """(eigenvalues, eigenvectors [n][level-1 dim]) of the deflation space."""
+        n = C.c_int()
+        _L.check(_L.lib().smg_mg_get_deflation(self.h, C.byref(n), None, None), "smg_mg_get_deflation", self.ctx.h)
+        vals = np.empty(n.value)
+        vecs = np.empty((n.value, self.level_dim(1)), dtype=np.complex128)
+        if n.value:
+            _L.check(_L.lib().smg_mg_get_deflation(self.h, C.byref(n), _ptr(vals), _ptr(vecs.view(np.float64))),
+                     "smg_mg_get_deflation", self.ctx.h)
+        return vals, vecs
+
+    def deflation_rr(self) -> float:
+        """rr_evolve (src/eigen_evolve.cpp:48-105) of the deflation space on the current level-1
+        operator; returns the largest relative eigen-residual."""
+        out = C.c_double()
+        _L.check(_L.lib().smg_mg_deflation_rr(self.h, C.byref(out)), "smg_mg_deflation_rr", self.ctx.h)
+        return out.value
+
+    def lowmode_solution(self, phi) -> np.ndarray:
+        """CoarseDeflState::lowmode_solution (src/hmc.h:312-323): P sum_i v_i v_i^dag / lambda_i P^dag phi."""
+        lat = self.D.lat
+        f = Field(lat, 1, "f64", self.ctx, data=phi)
+        x = Field(lat, 1, "f64", self.ctx)
+        _L.check(_L.lib().smg_mg_lowmode_solution(self.h, f.h, x.h), "smg_mg_lowmode_solution", self.ctx.h)
+        return x.download()
 
     def rebuild(self) -> None:
         """rebuild_deeper_levels (src/multigrid.cpp:158-193): the coarse operators from the current

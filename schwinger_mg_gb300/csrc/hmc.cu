@@ -11,6 +11,7 @@
 #include <random>
 #include <vector>
 
+#include "mg_internal.h"
 #include "reduce.cuh"
 #include "smg_internal.h"
 
@@ -57,12 +58,54 @@ __global__ void k_negate(double* __restrict__ pi, int n) {
     if (i < n) pi[i] = -pi[i];
 }
 
+// F = gf + ff - fl (the outer force of hmc_trajectory_mg_multiscale, src/hmc_multiscale.cpp:498-503)
+__global__ void k_outer_combine(double* __restrict__ F, const double* __restrict__ gf, const double* __restrict__ ff,
+                                const double* __restrict__ fl, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) F[i] = gf[i] + ff[i] - fl[i];
+}
+
+// r = a - b, or x += b (a == nullptr) over n complex entries
+__global__ void k_sub_add(cx<double>* __restrict__ out, const cx<double>* __restrict__ a,
+                          const cx<double>* __restrict__ b, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = a ? a[i] - b[i] : out[i] + b[i];
+}
+
 // sum of squares of n doubles (MomentumField::kinetic_energy without the 1/2)
 __global__ void __launch_bounds__(256) k_sumsq(const double* __restrict__ a, int n, double* partials,
                                                unsigned int* ticket, double* out) {
     double v[1] = {0.0};
     for (int i = blockIdx.x * blockDim.y + threadIdx.y; i < n; i += gridDim.x * blockDim.y) v[0] += a[i] * a[i];
     block_reduce_finalise<1>(v, partials, ticket, 1, FinStore{out, 1});
+}
+
+// coarse_lowmode_force (src/hmc_multiscale.cpp:237-276): MR on D^dag D x = phi from x = 0, the
+// low-mode solution of the residual added, MR again (smooth > 0; otherwise x is the low-mode
+// solution of phi), then the fermion force of x into F (device [mu][s]); xl, rl, tl are
+// single-RHS F64 scratch fields
+smg_status lowmode_force_fields(smg_dirac* d, smg_mg* mg, const smg_field* phi, int smooth, smg_field* xl,
+                                smg_field* rl, smg_field* tl, double* F) {
+    smg_context* ctx = d->ctx;
+    if (smooth <= 0) {
+        SMG_TRY(smg_mg_lowmode_internal(mg, phi, xl));
+        return smg_fermion_force_dev(d, xl, F);
+    }
+    const int64_t n = 2 * (int64_t)phi->g.V;
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    SMG_CUDA(ctx, cudaMemsetAsync(xl->data, 0, xl->bytes, ctx->stream));
+    SMG_TRY(smg_mr_smooth(d, phi, xl, smooth));
+    SMG_TRY(smg_dirac_apply(d, SMG_OP_DDAGD, xl, tl));
+    k_sub_add<<<blocks, 256, 0, ctx->stream>>>((cx<double>*)rl->data, (const cx<double>*)phi->data,
+                                               (const cx<double>*)tl->data, n);
+    count_launch(ctx);
+    SMG_TRY(smg_mg_lowmode_internal(mg, rl, tl));
+    k_sub_add<<<blocks, 256, 0, ctx->stream>>>((cx<double>*)xl->data, nullptr, (const cx<double>*)tl->data, n);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    SMG_TRY(smg_mr_smooth(d, phi, xl, smooth));
+    return smg_fermion_force_dev(d, xl, F);
 }
 
 struct Hmc {
@@ -86,11 +129,23 @@ struct Hmc {
     bool stale = false;  // links changed since the clover field and the FP32 links were formed
     int cg_iters = 0, solves = 0;
     smg_status warn = SMG_OK;
+    // multi-timescale MG HMC: the hierarchy (preconditioner, prolongator, deflation space) and the
+    // low-mode force's fields and forces
+    smg_mg* mg = nullptr;
+    bool mg_stale = false;  // links changed since the hierarchy's own Dirac operator was refreshed
+    int inner_smooth = 0, n_inner = 1, lowmode_evals = 0;
+    double *fl = nullptr, *fo = nullptr, *pi_save = nullptr;
+    cx<double>* U_save = nullptr;
+    smg_field *xl = nullptr, *rl = nullptr, *tl = nullptr;
 
     ~Hmc() {
         if (ctx) cudaStreamSynchronize(ctx->stream);
-        for (void* q : {(void*)pi, (void*)gf, (void*)ff, (void*)scal, (void*)U_old, (void*)W})
+        for (void* q : {(void*)pi, (void*)gf, (void*)ff, (void*)scal, (void*)U_old, (void*)W, (void*)fl, (void*)fo,
+                        (void*)pi_save, (void*)U_save})
             if (q) cudaFree(q);
+        smg_field_destroy(xl);
+        smg_field_destroy(rl);
+        smg_field_destroy(tl);
         smg_field_destroy(phi);
         smg_field_destroy(X);
         smg_field_destroy(eta);
@@ -109,11 +164,18 @@ struct Hmc {
         return SMG_OK;
     }
 
-    // X = (D^dag D)^-1 phi with the current links
+    // X = (D^dag D)^-1 phi with the current links; with a hierarchy, CG preconditioned by its cycle
+    // (cg_solve_precond, src/hmc_multiscale.cpp:479-484)
     smg_status solve() {
         SMG_TRY(refresh());
+        if (mg && mg_stale) {
+            smg_dirac* md = smg_mg_dirac(mg);
+            if (md != d) SMG_TRY(smg_dirac_refresh(md));
+            mg_stale = false;
+        }
         smg_solve_result res{};
-        const smg_status st = eo                  ? smg_eo_cg_solve(d, phi, X, p.cg_maxiter, p.cg_tol, &res)
+        const smg_status st = mg                  ? smg_cg_solve_precond(d, mg, phi, X, 0, p.cg_maxiter, p.cg_tol, &res)
+                              : eo                ? smg_eo_cg_solve(d, phi, X, p.cg_maxiter, p.cg_tol, &res)
                               : p.mixed_precision ? smg_cg_solve_mixed(d, phi, X, p.cg_maxiter, p.cg_tol, &res)
                                                   : smg_cg_solve(d, phi, X, p.cg_maxiter, p.cg_tol, &res);
         cg_iters += res.iterations;
@@ -162,6 +224,108 @@ struct Hmc {
         count_launch(ctx);
         SMG_CHECK_LAUNCH(ctx);
         stale = true;
+        mg_stale = true;
+        return SMG_OK;
+    }
+
+    smg_status lowmode_force(double* F) {
+        SMG_TRY(refresh());
+        return lowmode_force_fields(d, mg, phi, inner_smooth, xl, rl, tl, F);
+    }
+
+    // compute_outer_force (src/hmc_multiscale.cpp:424-504): gauge + fermion - low-mode force
+    smg_status outer_force(double* F) {
+        SMG_TRY(gauge_force());
+        SMG_TRY(solve());
+        SMG_TRY(smg_fermion_force_dev(d, X, ff));
+        SMG_TRY(lowmode_force(fl));
+        k_outer_combine<<<(n2() + 255) / 256, 256, 0, ctx->stream>>>(F, gf, ff, fl, n2());
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+        return SMG_OK;
+    }
+
+    // inner_integrator (src/hmc_multiscale.cpp:638-658): leapfrog on the low-mode force
+    smg_status inner_lowmode(double dt_total) {
+        const double dti = dt_total / n_inner;
+        SMG_TRY(lowmode_force(fl));
+        ++lowmode_evals;
+        SMG_TRY(kick(fl, nullptr, 0.5 * dti));
+        for (int i = 0; i < n_inner; ++i) {
+            SMG_TRY(update_gauge(dti));
+            SMG_TRY(lowmode_force(fl));
+            ++lowmode_evals;
+            SMG_TRY(kick(fl, nullptr, i < n_inner - 1 ? dti : 0.5 * dti));
+        }
+        return SMG_OK;
+    }
+
+    // fg_step (src/hmc_multiscale.cpp:737-779): force-gradient update of the expensive force by a
+    // displaced gauge field, lambda = 1/6, xi = 1/72
+    smg_status fg_step(double h) {
+        const double om = 1.0 - 2.0 / 6.0, xi_h3 = 2.0 / 72.0 * h * h * h;
+        const size_t ub = (size_t)n2() * sizeof(cx<double>), pb = (size_t)n2() * sizeof(double);
+        SMG_CUDA(ctx, cudaMemcpyAsync(U_save, g->U64, ub, cudaMemcpyDeviceToDevice, ctx->stream));
+        SMG_CUDA(ctx, cudaMemcpyAsync(pi_save, pi, pb, cudaMemcpyDeviceToDevice, ctx->stream));
+        SMG_CUDA(ctx, cudaMemsetAsync(pi, 0, pb, ctx->stream));
+        SMG_TRY(outer_force(fo));
+        SMG_TRY(kick(fo, nullptr, xi_h3 / (om * h)));
+        SMG_TRY(update_gauge(1.0));
+        SMG_CUDA(ctx, cudaMemcpyAsync(pi, pi_save, pb, cudaMemcpyDeviceToDevice, ctx->stream));
+        SMG_TRY(outer_force(fo));
+        SMG_TRY(kick(fo, nullptr, om * h));
+        SMG_CUDA(ctx, cudaMemcpyAsync(g->U64, U_save, ub, cudaMemcpyDeviceToDevice, ctx->stream));
+        stale = true;
+        mg_stale = true;
+        return SMG_OK;
+    }
+
+    // the outer integrators of hmc_trajectory_mg_multiscale (src/hmc_multiscale.cpp:712-836)
+    smg_status evolve_multiscale(int outer_type, int n_outer, double tau) {
+        const double h = tau / n_outer;
+        if (outer_type == SMG_OUTER_LEAPFROG) {
+            SMG_TRY(outer_force(fo));
+            SMG_TRY(kick(fo, nullptr, 0.5 * h));
+            for (int o = 0; o < n_outer; ++o) {
+                SMG_TRY(inner_lowmode(h));
+                SMG_TRY(outer_force(fo));
+                SMG_TRY(kick(fo, nullptr, o < n_outer - 1 ? h : 0.5 * h));
+            }
+        } else if (outer_type == SMG_OUTER_OMELYAN) {
+            const double lam = kOmelyanLambda;
+            SMG_TRY(outer_force(fo));
+            SMG_TRY(kick(fo, nullptr, lam * h));
+            for (int o = 0; o < n_outer; ++o) {
+                SMG_TRY(inner_lowmode(0.5 * h));
+                SMG_TRY(outer_force(fo));
+                SMG_TRY(kick(fo, nullptr, (1.0 - 2.0 * lam) * h));
+                SMG_TRY(inner_lowmode(0.5 * h));
+                SMG_TRY(outer_force(fo));
+                SMG_TRY(kick(fo, nullptr, o < n_outer - 1 ? 2.0 * lam * h : lam * h));
+            }
+        } else if (outer_type == SMG_OUTER_FGI) {
+            const double lam = 1.0 / 6.0;
+            SMG_TRY(outer_force(fo));
+            SMG_TRY(kick(fo, nullptr, lam * h));
+            for (int o = 0; o < n_outer; ++o) {
+                SMG_TRY(inner_lowmode(0.5 * h));
+                SMG_TRY(fg_step(h));
+                SMG_TRY(inner_lowmode(0.5 * h));
+                SMG_TRY(outer_force(fo));
+                SMG_TRY(kick(fo, nullptr, o < n_outer - 1 ? 2.0 * lam * h : lam * h));
+            }
+        } else {  // FGI_QPQPQ
+            const double lam = 1.0 / 6.0;
+            SMG_TRY(inner_lowmode(lam * h));
+            for (int o = 0; o < n_outer; ++o) {
+                SMG_TRY(outer_force(fo));
+                SMG_TRY(kick(fo, nullptr, 0.5 * h));
+                SMG_TRY(fg_step(h));
+                SMG_TRY(outer_force(fo));
+                SMG_TRY(kick(fo, nullptr, 0.5 * h));
+                SMG_TRY(inner_lowmode(o < n_outer - 1 ? 2.0 * lam * h : lam * h));
+            }
+        }
         return SMG_OK;
     }
 
@@ -361,6 +525,48 @@ smg_status hmc_draw_pseudofermion(Hmc& h, smg_rng* rng) {
     return smg_dirac_apply(h.d, SMG_OP_DDAG, h.eta, h.phi);
 }
 
+smg_status ms_check(smg_gauge* g, const smg_ms_params* p, smg_mg* mg) {
+    smg_context* ctx = g->ctx;
+    if (p->n_outer < 1 || p->n_inner < 1 || !(p->tau > 0) || p->cg_maxiter < 1 || !(p->cg_tol > 0) ||
+        p->inner_smooth < 0 || p->outer_type < SMG_OUTER_LEAPFROG || p->outer_type > SMG_OUTER_FGI_QPQPQ)
+        return smg_fail(ctx, SMG_BAD_ARG,
+                        "multiscale hmc: n_outer, n_inner >= 1, tau > 0, cg_maxiter >= 1, cg_tol > 0, "
+                        "inner_smooth >= 0, outer_type in [0, 3]");
+    if (smg_mg_dirac(mg)->gauge != g)
+        return smg_fail(ctx, SMG_BAD_ARG, "multiscale hmc: the hierarchy must be built on the trajectory's gauge field");
+    return SMG_OK;
+}
+
+// the device state of a multi-timescale trajectory; mu_t as given (the reversibility test passes 0)
+smg_status ms_setup(Hmc& h, smg_gauge* g, double mass, double wilson_r, const smg_ms_params* p, double mu_t,
+                    smg_mg* mg) {
+    smg_hmc_params hp{};
+    smg_hmc_params_default(&hp);
+    hp.beta = p->beta;
+    hp.tau = p->tau;
+    hp.n_steps = p->n_outer;
+    hp.cg_maxiter = p->cg_maxiter;
+    hp.cg_tol = p->cg_tol;
+    hp.c_sw = p->c_sw;
+    hp.mu_t = mu_t;
+    SMG_TRY(hmc_setup(h, g, mass, wilson_r, &hp));
+    smg_context* ctx = g->ctx;
+    const int L = g->g.L;
+    const size_t fb = (size_t)h.n2() * sizeof(double);
+    h.mg = mg;
+    h.mg_stale = true;
+    h.inner_smooth = p->inner_smooth;
+    h.n_inner = p->n_inner;
+    SMG_CUDA(ctx, cudaMalloc(&h.fl, fb));
+    SMG_CUDA(ctx, cudaMalloc(&h.fo, fb));
+    SMG_CUDA(ctx, cudaMalloc(&h.pi_save, fb));
+    SMG_CUDA(ctx, cudaMalloc(&h.U_save, (size_t)h.n2() * sizeof(cx<double>)));
+    SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.xl));
+    SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.rl));
+    SMG_TRY(smg_field_create(ctx, L, 1, SMG_F64, &h.tl));
+    return SMG_OK;
+}
+
 }  // namespace
 
 // gauge_force into a device array (defined next to the kernel in gauge.cu)
@@ -450,6 +656,148 @@ SMG_API smg_status smg_hmc_trajectory(smg_gauge* g, double mass, double wilson_r
         res->plaquette = plaq;
         res->dLD = LD1 - LD0;
     }
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_coarse_lowmode_force(smg_dirac* d, smg_mg* mg, const smg_field* phi, int smooth_iters,
+                                            double* force) {
+    if (!d || !mg || !phi || !force || smooth_iters < 0) return SMG_BAD_ARG;
+    smg_context* ctx = d->ctx;
+    if (phi->prec != SMG_F64 || phi->nrhs != 1 || phi->g.L != d->gauge->g.L ||
+        smg_mg_dirac(mg)->gauge->g.L != d->gauge->g.L)
+        return smg_fail(ctx, SMG_BAD_ARG, "coarse_lowmode_force: single-RHS F64 phi on the hierarchy's lattice");
+    const int L = phi->g.L;
+    smg_field *xl = nullptr, *rl = nullptr, *tl = nullptr;
+    double* F = nullptr;
+    const size_t fb = (size_t)2 * phi->g.V * sizeof(double);
+    smg_status st = smg_field_create(ctx, L, 1, SMG_F64, &xl);
+    if (st == SMG_OK) st = smg_field_create(ctx, L, 1, SMG_F64, &rl);
+    if (st == SMG_OK) st = smg_field_create(ctx, L, 1, SMG_F64, &tl);
+    if (st == SMG_OK && cudaMalloc(&F, fb) != cudaSuccess) st = smg_fail(ctx, SMG_NO_MEMORY, "force buffer");
+    if (st == SMG_OK) st = lowmode_force_fields(d, mg, phi, smooth_iters, xl, rl, tl, F);
+    if (st == SMG_OK && cudaMemcpyAsync(force, F, fb, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess)
+        st = smg_fail(ctx, SMG_DEVICE_ERROR, "force copy");
+    cudaStreamSynchronize(ctx->stream);
+    if (F) cudaFree(F);
+    smg_field_destroy(xl);
+    smg_field_destroy(rl);
+    smg_field_destroy(tl);
+    return st;
+}
+
+SMG_API smg_status smg_ms_params_default(smg_ms_params* p) {
+    if (!p) return SMG_BAD_ARG;
+    *p = smg_ms_params{};
+    p->beta = 4.0;
+    p->tau = 1.0;
+    p->n_outer = 4;
+    p->n_inner = 5;
+    p->cg_maxiter = 500;
+    p->cg_tol = 1e-10;
+    p->inner_smooth = 3;
+    p->outer_type = SMG_OUTER_LEAPFROG;
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_hmc_mg_multiscale(smg_gauge* g, double mass, double wilson_r, const smg_ms_params* p,
+                                         smg_mg* mg, smg_rng* rng, smg_ms_result* res) {
+    if (!g || !p || !mg || !rng) return SMG_BAD_ARG;
+    smg_context* ctx = g->ctx;
+    SMG_TRY(ms_check(g, p, mg));
+    Hmc h;
+    SMG_TRY(ms_setup(h, g, mass, wilson_r, p, p->mu_t, mg));
+    // momenta, then the pseudofermion twice (the first draw is overwritten,
+    // src/hmc_multiscale.cpp:360-384)
+    SMG_TRY(hmc_draw_momenta(h, rng));
+    SMG_TRY(hmc_draw_pseudofermion(h, rng));
+    SMG_TRY(hmc_draw_pseudofermion(h, rng));
+    double KE0 = 0, SG0 = 0, SF0 = 0, LD0 = 0;
+    SMG_TRY(h.hamiltonian(&KE0, &SG0, &SF0, &LD0));
+    SMG_TRY(h.evolve_multiscale(p->outer_type, p->n_outer, p->tau));
+    double KE1 = 0, SG1 = 0, SF1 = 0, LD1 = 0;
+    SMG_TRY(h.hamiltonian(&KE1, &SG1, &SF1, &LD1));
+    const double dH = (KE1 + SG1 + SF1) - (KE0 + SG0 + SF0);
+    // Metropolis (src/hmc_multiscale.cpp:874-876)
+    bool accept = dH < 0;
+    if (!accept) {
+        std::uniform_real_distribution<double> uniform(0.0, 1.0);
+        accept = uniform(rng->gen) < std::exp(-dH);
+    }
+    if (!accept) {
+        SMG_CUDA(ctx, cudaMemcpyAsync(g->U64, h.U_old, (size_t)h.n2() * sizeof(cx<double>), cudaMemcpyDeviceToDevice,
+                                      ctx->stream));
+        SMG_TRY(smg_gauge_ensure_f32(g));
+    }
+    // the hierarchy's Dirac operator follows the links the trajectory leaves
+    if (smg_mg_dirac(mg) != h.d) SMG_TRY(smg_dirac_refresh(smg_mg_dirac(mg)));
+    double plaq = 0;
+    SMG_TRY(smg_gauge_avg_plaq(g, &plaq));
+    if (res) {
+        res->accepted = accept ? 1 : 0;
+        res->dH = dH;
+        res->dKE = KE1 - KE0;
+        res->dSG = SG1 - SG0;
+        res->dSF = SF1 - SF0;
+        res->highmode_cg_iters = h.cg_iters;
+        res->lowmode_force_evals = h.lowmode_evals;
+        res->solves = h.solves;
+        res->plaquette = plaq;
+    }
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_hmc_mg_multiscale_reversibility(smg_gauge* g, double mass, double wilson_r,
+                                                       const smg_ms_params* p, smg_mg* mg, smg_rng* rng,
+                                                       smg_reversibility_result* res) {
+    if (!g || !p || !mg || !rng || !res) return SMG_BAD_ARG;
+    smg_context* ctx = g->ctx;
+    SMG_TRY(ms_check(g, p, mg));
+    Hmc h;
+    // DiracOp(lat, gauge, mass, wilson_r, c_sw) of mg_ms_md_evolve: mu_t = 0 (src/hmc_multiscale.cpp:904)
+    SMG_TRY(ms_setup(h, g, mass, wilson_r, p, 0.0, mg));
+    SMG_TRY(hmc_draw_momenta(h, rng));
+    SMG_TRY(hmc_draw_pseudofermion(h, rng));
+    const int n2 = h.n2();
+    // mg_ms_md_evolve runs FGI_QPQPQ as FGI (src/hmc_multiscale.cpp:933)
+    const int outer = p->outer_type == SMG_OUTER_FGI_QPQPQ ? SMG_OUTER_FGI : p->outer_type;
+    std::vector<double> pi0((size_t)n2), pi1((size_t)n2);
+    SMG_CUDA(ctx, cudaMemcpyAsync(pi0.data(), h.pi, (size_t)n2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    double KE0 = 0, SG0 = 0, SF0 = 0, LD0 = 0, KE1 = 0, SG1 = 0, SF1 = 0, LD1 = 0, KE2 = 0, SG2 = 0, SF2 = 0, LD2 = 0;
+    SMG_TRY(h.hamiltonian(&KE0, &SG0, &SF0, &LD0));
+    SMG_TRY(h.evolve_multiscale(outer, p->n_outer, p->tau));
+    SMG_TRY(h.hamiltonian(&KE1, &SG1, &SF1, &LD1));
+    k_negate<<<(n2 + 255) / 256, 256, 0, ctx->stream>>>(h.pi, n2);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    SMG_TRY(h.evolve_multiscale(outer, p->n_outer, p->tau));
+    SMG_TRY(h.hamiltonian(&KE2, &SG2, &SF2, &LD2));
+    std::vector<cx<double>> u0((size_t)n2), u1((size_t)n2);
+    SMG_CUDA(ctx, cudaMemcpyAsync(u0.data(), h.U_old, (size_t)n2 * sizeof(cx<double>), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    SMG_CUDA(ctx, cudaMemcpyAsync(u1.data(), g->U64, (size_t)n2 * sizeof(cx<double>), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    SMG_CUDA(ctx, cudaMemcpyAsync(pi1.data(), h.pi, (size_t)n2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double un = 0, ud = 0, pn = 0, pd = 0;
+    for (int i = 0; i < n2; ++i) {
+        const double dr = u1[i].re - u0[i].re, di = u1[i].im - u0[i].im;
+        un += u0[i].re * u0[i].re + u0[i].im * u0[i].im;
+        ud += dr * dr + di * di;
+        const double dp = pi1[i] + pi0[i];
+        pn += pi0[i] * pi0[i];
+        pd += dp * dp;
+    }
+    SMG_CUDA(ctx, cudaMemcpyAsync(g->U64, h.U_old, (size_t)n2 * sizeof(cx<double>), cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+    SMG_TRY(smg_gauge_ensure_f32(g));
+    if (smg_mg_dirac(mg) != h.d) SMG_TRY(smg_dirac_refresh(smg_mg_dirac(mg)));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    res->gauge_delta = std::sqrt(ud / std::max(un, 1e-30));
+    res->mom_delta = std::sqrt(pd / std::max(pn, 1e-30));
+    res->dH_forward = (KE1 + SG1 + SF1) - (KE0 + SG0 + SF0);
+    res->dH_backward = (KE2 + SG2 + SF2) - (KE1 + SG1 + SF1);
+    res->total_cg_iters = h.cg_iters;
+    res->solves = h.solves;
     return SMG_OK;
 }
 

@@ -21,6 +21,7 @@
 #include "smg_internal.h"
 #include "vec.cuh"
 #include "half.cuh"
+#include "mg_internal.h"
 
 #include <algorithm>
 #include <cmath>
@@ -903,13 +904,16 @@ struct CcgState {
     double tol2 = 0;
 };
 
-__global__ void k_ccg_init(CcgState s, int nrhs) {
+// bnorm2 = ||b||^2: taken from rr = ||r0||^2 = ||b||^2 for a zero start, or already in place
+// (have_bnorm) for a deflated start
+__global__ void k_ccg_init(CcgState s, int nrhs, int have_bnorm) {
     if (threadIdx.x == 0) *s.n_active = 0;
     __syncthreads();
     for (int j = threadIdx.x; j < nrhs; j += blockDim.x) {
-        s.bnorm2[j] = s.rr[j];
+        if (!have_bnorm) s.bnorm2[j] = s.rr[j];
         s.beta[j] = 0.0;
-        int act = (s.rr[j] >= 1e-60 && isfinite(s.rr[j])) ? 1 : 0;
+        int act = (s.rr[j] >= 1e-60 && isfinite(s.rr[j]) && s.bnorm2[j] >= 1e-60) ? 1 : 0;
+        if (act && s.rr[j] < s.tol2 * s.bnorm2[j]) act = 0;  // the initial guess already converged
         s.active[j] = act;
         if (act) atomicAdd(s.n_active, 1);
     }
@@ -1024,6 +1028,9 @@ struct smg_mg {
     // persistent coarsest CG: barrier words, error flag, iteration count, partials
     bool persistent = true;
     void* cg_state = nullptr;  // [0..1] barrier, [2] err, [3] iters (ints), doubles from byte 256
+    // eigenpairs of the level-1 operator: the deflated initial guess of the coarsest CG when level 1
+    // is the coarsest level, and the low-mode projector of the multi-timescale HMC
+    MgDeflation defl;
 };
 
 namespace {
@@ -1655,7 +1662,7 @@ template <typename T>
 smg_status coarse_cg(smg_mg* mg, int l, void* x, const void* b) {
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[l];
-    if (mg->persistent && mg->work_nrhs == 1) {
+    if (mg->persistent && mg->work_nrhs == 1 && !(l == 1 && mg->defl.n > 0)) {
         if (L.ndof == 8) return coarse_cg_persistent<T, 8>(mg, l, x, b);
         if (L.ndof == 16) return coarse_cg_persistent<T, 16>(mg, l, x, b);
         if (L.ndof == 32) return coarse_cg_persistent<T, 32>(mg, l, x, b);
@@ -1664,6 +1671,7 @@ smg_status coarse_cg(smg_mg* mg, int l, void* x, const void* b) {
     const int nrhs = mg->work_nrhs;
     VecView<T> xv = cview<T>(x, L, nrhs), pv = cview<T>(w.p, L, nrhs), rv = cview<T>(w.r, L, nrhs);
     const size_t bytes = (size_t)xv.n() * sizeof(cx<T>);
+    const bool deflated = l == 1 && mg->defl.n > 0;
     double* sc = lvl_scal(mg, l);
     CcgState s;
     s.rr = sc;
@@ -1673,11 +1681,24 @@ smg_status coarse_cg(smg_mg* mg, int l, void* x, const void* b) {
     s.active = (int*)(sc + 6 * nrhs);
     s.n_active = (int*)(sc + 7 * nrhs);
     s.tol2 = mg->p.coarse_tol * mg->p.coarse_tol;
-    SMG_CUDA(ctx, cudaMemsetAsync(x, 0, bytes, ctx->stream));
-    SMG_CUDA(ctx, cudaMemcpyAsync(w.r, b, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-    SMG_CUDA(ctx, cudaMemcpyAsync(w.p, b, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (deflated) {
+        // SparseCoarseOp::solve (src/coarse_op.h:492-520): CG from x0 = sum_i v_i (v_i^dag b) / lambda_i
+        SMG_TRY(smg_defl_guess<T>(ctx, mg->defl, cview<T>((void*)b, L, nrhs), xv));
+        SMG_TRY(coarse_apply<T>(mg, l, xv, (cx<T>*)w.Ar, 0, nullptr, nullptr));
+        k_vsub<T><<<blocks_for(xv.n()), 256, 0, ctx->stream>>>((cx<T>*)w.r, (const cx<T>*)b, (const cx<T>*)w.Ar,
+                                                             xv.n());
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+        SMG_CUDA(ctx, cudaMemcpyAsync(w.p, w.r, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+        // the stopping test is relative to ||b|| as in the reference
+        SMG_TRY(vreduce<T>(ctx, flat(cview<T>((void*)b, L, nrhs)), nullptr, VR_NORM, s.bnorm2));
+    } else {
+        SMG_CUDA(ctx, cudaMemsetAsync(x, 0, bytes, ctx->stream));
+        SMG_CUDA(ctx, cudaMemcpyAsync(w.r, b, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+        SMG_CUDA(ctx, cudaMemcpyAsync(w.p, b, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
     SMG_TRY(vreduce<T>(ctx, flat(rv), nullptr, VR_NORM, s.rr));
-    k_ccg_init<<<1, 256, 0, ctx->stream>>>(s, nrhs);
+    k_ccg_init<<<1, 256, 0, ctx->stream>>>(s, nrhs, deflated ? 1 : 0);
     count_launch(ctx);
     const VecView<T> xf = flat(xv), pf = flat(pv);
     ReduceLaunch rl = reduce_launch(xf.nsites, nrhs);
@@ -2359,6 +2380,44 @@ smg_status smg_mg_check_device_error(smg_mg* mg) {
     return SMG_OK;
 }
 
+// ------------------------------------------------------------ level-1 helpers for deflation.cu
+
+MgDeflation& smg_mg_defl(smg_mg* mg) { return mg->defl; }
+smg_context* smg_mg_ctx(smg_mg* mg) { return mg->ctx; }
+smg_dirac* smg_mg_dirac(smg_mg* mg) { return mg->dirac; }
+int smg_mg_nlevels(const smg_mg* mg) { return (int)mg->lv.size(); }
+int64_t smg_mg_level1_dim(const smg_mg* mg) { return (int64_t)mg->lv[1].nsites * mg->lv[1].ndof; }
+void smg_mg_drop_cycle_graph(smg_mg* mg) {
+    cudaStreamSynchronize(mg->ctx->stream);
+    drop_graph(mg);
+}
+
+smg_status smg_mg_apply1_f64(smg_mg* mg, const cx<double>* x, cx<double>* y) {
+    return coarse_apply<double>(mg, 1, cview<double>((void*)x, mg->lv[1], 1), y, 0, nullptr, nullptr);
+}
+
+smg_status smg_mg_restrict0_f64(smg_mg* mg, const smg_field* fine, cx<double>* coarse) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[0];
+    const int64_t total = (int64_t)mg->lv[1].nsites * L.nc_next;
+    k_restrict0<double><<<blocks_for(total), 256, 0, ctx->stream>>>(L.V64, (const cx<double>*)fine->data, coarse,
+                                                                   mg->null0[0]->g, L.ax, L.ay, L.nc_next, 1);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+smg_status smg_mg_prolong0_f64(smg_mg* mg, const cx<double>* coarse, smg_field* fine) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[0];
+    const Geom g = mg->null0[0]->g;
+    k_prolong0<double><<<blocks_for((int64_t)g.V), 256, 0, ctx->stream>>>(L.V64, coarse, (cx<double>*)fine->data, g,
+                                                                         L.ax, L.ay, L.nc_next, 1, 0);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
 extern "C" {
 
 SMG_API smg_status smg_mg_params_default(smg_mg_params* p) {
@@ -2413,6 +2472,7 @@ SMG_API smg_status smg_mg_destroy(smg_mg* mg) {
     drop_graph(mg);
     free_work(mg);
     destroy_levels(mg);
+    smg_defl_free(mg->defl);
     delete mg;
     return SMG_OK;
 }

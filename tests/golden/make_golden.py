@@ -97,6 +97,37 @@ def reversibility_case(ref, name, L, beta, m, r, csw, gseed, seed, n_steps, omel
     print("wrote", name, out.tolist())
 
 
+def ms_case(ref, name, L, beta, m, r, csw, gseed, seed, bs=4, k=4, n_defl=6, null_iters=5, smooth=3):
+    """Coarse deflation (TRLM on the level-1 operator), the low-mode solution and force, and the
+    MG multi-timescale HMC (trajectories for each outer integrator, reversibility) of the
+    reference, on one hierarchy built from mt19937(seed)."""
+    U = gauge_normal(L, beta, gseed).reshape(-1)
+    n = 2 * L * L
+    cdim = (L // bs) ** 2 * k
+    params = O.RefMGParams(2, bs, k, 0, null_iters, 1, 3, 3, n_defl)
+    phi = ref.random_vecs(1, n, seed + 1)
+    nv, vals, vecs, low, force = ref.ms_setup(U, m, r, csw, 0.0, params, seed, phi, smooth, cdim)
+    # one cycle whose coarsest solve is the deflated CG (setup_sparse_coarse wires it, src/multigrid.cpp:780-790)
+    pre = ref.mg_precondition(U, m, r, csw, 0.0, O.RefMGParams(2, bs, k, 0, 0, 1, 3, 3, n_defl), seed, phi, warm=nv)
+    out = dict(L=L, beta=beta, m=m, r=r, csw=csw, gseed=gseed, seed=seed, bs=bs, k=k, n_defl=n_defl, smooth=smooth,
+               U=U, null_vecs=nv, defl_vals=vals, defl_vecs=vecs, phi=phi, lowmode=low, lowmode_force=force,
+               precondition_deflated=pre)
+    ms = dict(beta=beta, tau=0.2, n_outer=4, n_inner=3, cg_maxiter=500, cg_tol=1e-12, inner_smooth=smooth, c_sw=csw,
+              mu_t=0.0)
+    for t, n_traj in ((0, 2), (1, 2), (2, 1), (3, 1)):
+        q = O.RefMSParams(ms["beta"], ms["tau"], ms["n_outer"], ms["n_inner"], ms["cg_maxiter"], ms["cg_tol"],
+                          ms["inner_smooth"], t, ms["c_sw"], ms["mu_t"])
+        U_out, traj = ref.ms_trajectories(U, m, r, params, seed, q, seed + 10 + t, n_traj)
+        out[f"traj_{t}"] = traj
+        out[f"U_out_{t}"] = U_out
+        if t < 3:
+            out[f"rev_{t}"] = ref.ms_reversibility(U, m, r, params, seed, q, seed + 20 + t)
+        print(name, "outer", t, traj[:, :2].tolist(), out.get(f"rev_{t}", np.zeros(5))[:4].tolist())
+    out.update({f"ms_{key}": v for key, v in ms.items()})
+    np.savez_compressed(OUT / f"{name}.npz", **out)
+    print("wrote", name, "defl vals", vals.tolist())
+
+
 def solvers_case(ref, name, L, beta, m, r, csw, gseed, seed, null_iters=5):
     """PCG (plain with a start vector, and with the symmetric MG), FGMRES (with MG and
     unpreconditioned, Ritz harvesting on), the Richardson/MR smoothers, lambda_max,
@@ -193,6 +224,7 @@ CASES = {
     "eo_L16_wilson": lambda ref: eo_case(ref, "eo_L16_wilson", 16, 4.0, 0.2, 1.0, 0.0, 0.0, 93, 94),
     "reversibility_L8_omelyan": lambda ref: reversibility_case(ref, "reversibility_L8_omelyan", 8, 4.0, 0.1, 1.0,
                                                                1.0, 71, 72, 5, 1),
+    "ms_L16": lambda ref: ms_case(ref, "ms_L16", 16, 4.0, 0.1, 1.0, 1.0, 111, 112),
     "hmc_eo_L8": lambda ref: hmc_eo_case(ref, "hmc_eo_L8", 8, 4.0, 0.1, 1.0, 1.0, 95, 96, 6, 3),
     "delta_L16": lambda ref: delta_case(ref, "delta_L16", 16, 3.0, 0.1, 1.0, 1.0, 0.1, 97, 98, 0.05),
 }
