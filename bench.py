@@ -201,21 +201,22 @@ def kernel_trace(step, ctx, path: str, what: str) -> None:
     kt.smg_ktrace_stop(raw.encode())
     lines = Path(raw).read_text().splitlines()
     span = float(lines[0].split()[2])
-    rows = [l.split(" ", 2) for l in lines[1:]]
-    names = [r[2] for r in rows]
+    rows = [l.split(" ", 3) for l in lines[1:]]
+    names = [r[3] for r in rows]
     if shutil.which("c++filt"):
         names = subprocess.run(["c++filt"], input="\n".join(names), capture_output=True, text=True).stdout.splitlines()
     agg = {}
     for r, nm in zip(rows, names):
         nm = nm.replace("(anonymous namespace)::", "")
         key = nm.split("(")[0] if "<" not in nm.split("(")[0] else nm[: nm.find(">(") + 1] if ">(" in nm else nm
+        key = (key, r[2])
         n, t = agg.get(key, (0, 0.0))
         agg[key] = (n + int(r[0]), t + float(r[1]))
     tot = sum(t for _, t in agg.values())
     out = [f"# CUPTI kernel trace: {what}", f"# kernel time {tot / 1e6:.2f} ms, span {span / 1e6:.2f} ms", "",
-           "| launches | total ms | avg us | share | kernel |", "|---:|---:|---:|---:|---|"]
-    for k, (n, t) in sorted(agg.items(), key=lambda kv: -kv[1][1]):
-        out.append(f"| {n} | {t / 1e6:.2f} | {t / n / 1e3:.1f} | {100 * t / tot:.1f}% | `{k}` |")
+           "| launches | total ms | avg us | share | kernel | grid |", "|---:|---:|---:|---:|---|---|"]
+    for (k, grid), (n, t) in sorted(agg.items(), key=lambda kv: -kv[1][1]):
+        out.append(f"| {n} | {t / 1e6:.2f} | {t / n / 1e3:.1f} | {100 * t / tot:.1f}% | `{k}` | {grid} |")
     Path(path).write_text("\n".join(out) + "\n")
 
 

@@ -39,14 +39,20 @@
 //     FP32 vector [site][dof][rhs] layout into BF16 A tiles by four stager
 //     warps and kept in a ring of four rows (output row y reads source rows
 //     y-1, y, y+1);
-//   * warp 0 issues the link copies, warp 1 the MMAs, warps 4 and 5 read the
-//     accumulators (TMEM lanes 0..63, one 256-column slot per output row, two
-//     slots) and write y, with the fused per-rhs reductions ||y||^2 and
-//     <y, w> of the FP32 kernels.
+//   * warp 0 issues the link copies, warp 1 the MMAs, warps 4, 5 and 8, 9
+//     read the accumulators (TMEM lanes 0..63, one 256-column slot per output
+//     row, two slots; the two pairs share the lane groups and split a row's
+//     sites) and write y, with the fused per-rhs reductions ||y||^2 and
+//     <y, w> of the FP32 kernels; warps 10 and 11 only join the final barrier.
 // Every mbarrier wait is bounded (about one second of SM clock); on timeout
 // the CTA raises *err = 2, waits (bounded) for its own bulk copies and MMAs,
 // frees its tensor memory and returns.
 #include <cuda_bf16.h>
+
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
 
 #include "smg_internal.h"
 
@@ -80,8 +86,11 @@ constexpr int kBarFinal = kBarAccEmpty + 2;
 constexpr int kNumBars = kBarFinal + 1;
 constexpr int kBarOffset = kRingBytes + kLinkBytes;           // A-tile over-read (M = 128) lands in the link ring
 constexpr int kMiscOffset = kBarOffset + kNumBars * 8;
-constexpr int kRedOffset = (kMiscOffset + 16 + 15) / 16 * 16;  // 32 rhs x 3 doubles
-constexpr int kSmemBytes = kRedOffset + kRhsTile * 3 * 8;
+constexpr int kThreads = 384;                                 // 12 warps (roles below)
+constexpr int kEpiHalves = 2;                                 // epilogue warp pairs, each half a row
+constexpr int kEpiSites = kW / kEpiHalves;                    // output sites per pair and row
+constexpr int kRedOffset = (kMiscOffset + 16 + 15) / 16 * 16;  // [half][32 rhs][3] doubles
+constexpr int kSmemBytes = kRedOffset + kEpiHalves * kRhsTile * 3 * 8;
 static_assert(kSmemBytes + 1024 <= 227 * 1024, "shared memory budget");
 static_assert(kTileA % 16 == 0 && kRowBytes % 16 == 0 && kUnitBytes % 16 == 0, "16-byte alignment");
 static_assert(2 * kAccCols <= kTmemCols, "tensor memory budget");
@@ -231,7 +240,7 @@ struct TcArgs {
 };
 
 template <int EPI>
-__global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
+__global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
     if (a.gate && *a.gate == 0) return;  // every right-hand side of the solve has converged
     constexpr int K = EPI == 2 ? 3 : 1;
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -257,7 +266,7 @@ __global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
         }
         for (int i = 0; i < 2; ++i) {
             mbar_init(bar(kBarAccFull + i), 1);
-            mbar_init(bar(kBarAccEmpty + i), 64);
+            mbar_init(bar(kBarAccEmpty + i), 32 * 2 * kEpiHalves);
         }
         mbar_init(bar(kBarFinal), 1);
         misc[1] = 0;
@@ -341,9 +350,11 @@ __global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
             drain_bar(bar(kBarFinal), 0);
         }
         __syncwarp();
-    } else if (warp == 4 || warp == 5) {
-        // ---------------- epilogue: TMEM lanes 0..63 hold the 64 useful rows
-        const int sub = warp - 4;
+    } else if (warp == 4 || warp == 5 || warp == 8 || warp == 9) {
+        // ---------------- epilogue: TMEM lanes 0..63 hold the 64 useful rows; warps 4, 5 take the
+        // first kEpiSites sites of a row and warps 8, 9 (the same lane groups) the others
+        const int half = warp >= 8 ? 1 : 0;
+        const int sub = warp - (half ? 8 : 4);
         const int m = 32 * sub + lane;
         const int rhs = m >> 1, c = m & 1;
         double v[K];
@@ -353,14 +364,15 @@ __global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
         const float* __restrict__ wbase = reinterpret_cast<const float*>(a.w);
         float* __restrict__ ybase = reinterpret_cast<float*>(a.y);
         for (int r = 0; r < H; ++r) {
-            const int64_t row0 = ((int64_t)x0 + (int64_t)nx * (y0 + r)) * kNc * nrhs + rhs0 + rhs;  // site x0
-            // EPI 2: w of the first kPre sites is requested before the accumulators are ready and
-            // each later site's w kPre sites ahead, so the L2 latency overlaps the epilogue work
-            constexpr int kPre = 4;
-            float wb[kPre][kNc];
+            // site x0 + half * kEpiSites
+            const int64_t row0 =
+                ((int64_t)x0 + half * kEpiSites + (int64_t)nx * (y0 + r)) * kNc * nrhs + rhs0 + rhs;
+            // EPI 2: w of this thread's sites is requested before the accumulators are ready, so the
+            // L2 latency overlaps the wait
+            float wb[kEpiSites][kNc];
             if (EPI == 2) {
 #pragma unroll
-                for (int q = 0; q < kPre; ++q)
+                for (int q = 0; q < kEpiSites; ++q)
 #pragma unroll
                     for (int k = 0; k < kNc; ++k)
                         wb[q][k] = __ldcg(wbase + (row0 + (int64_t)q * kNc * nrhs) * 2 + c + k * rstride);
@@ -369,10 +381,11 @@ __global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
             if (!__all_sync(0xffffffffu, ok)) break;
             tc_fence_after();
 #pragma unroll
-            for (int i = 0; i < kW; ++i) {
+            for (int q = 0; q < kEpiSites; ++q) {
+                const int i = half * kEpiSites + q;
                 float d[32];
                 tmem_ld32(tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)((r & 1) * kAccCols + 32 * i), d);
-                const int64_t base = (row0 + (int64_t)i * kNc * nrhs) * 2 + c;
+                const int64_t base = (row0 + (int64_t)q * kNc * nrhs) * 2 + c;
                 float o[kNc];
 #pragma unroll
                 for (int k = 0; k < kNc; ++k) {
@@ -385,17 +398,12 @@ __global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
                     if (EPI == 1) {
                         s0 += o[k] * o[k];
                     } else if (EPI == 2) {
-                        const float wc = wb[i % kPre][k];
+                        const float wc = wb[q][k];
                         const float wo = __shfl_xor_sync(0xffffffffu, wc, 1);
                         s0 += o[k] * wc;                     // Re <y, w>: yr wr + yi wi
                         s1 += c == 0 ? o[k] * wo : -o[k] * wo;  // Im <y, w>: yr wi - yi wr
                         s2 += o[k] * o[k];
                     }
-                }
-                if (EPI == 2 && i + kPre < kW) {
-#pragma unroll
-                    for (int k = 0; k < kNc; ++k)
-                        wb[i % kPre][k] = __ldcg(wbase + base + (int64_t)kPre * kNc * nrhs * 2 + k * rstride);
                 }
 #pragma unroll
                 for (int k = 0; k < kNc; ++k) ybase[base + k * rstride] = o[k];
@@ -415,9 +423,9 @@ __global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
             for (int k = 0; k < K; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], 1);
             if (c == 0)
 #pragma unroll
-                for (int k = 0; k < K; ++k) red[rhs * K + k] = v[k];
+                for (int k = 0; k < K; ++k) red[(half * kRhsTile + rhs) * K + k] = v[k];
         }
-    } else {
+    } else if (warp == 2 || warp == 3 || warp == 6 || warp == 7) {
         // ---------------- stagers (warps 2, 3, 6, 7): FP32 source rows -> BF16 A tiles
         const int st = (warp < 4 ? warp - 2 : warp - 4) * 32 + lane;  // 0..127
         for (int lr = 0; lr < H + 2; ++lr) {
@@ -471,7 +479,8 @@ __global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
         if (tid < kRhsTile) {
 #pragma unroll
             for (int k = 0; k < K; ++k)
-                a.partials[((int64_t)(rhs0 + tid) * K + k) * nblk + blin] = aborted ? 0.0 : red[tid * K + k];
+                a.partials[((int64_t)(rhs0 + tid) * K + k) * nblk + blin] =
+                    aborted ? 0.0 : red[tid * K + k] + red[(kRhsTile + tid) * K + k];
         }
         __threadfence();
         __syncthreads();
@@ -482,7 +491,7 @@ __global__ void __launch_bounds__(256, 1) k_coarse_apply_tc(TcArgs a) {
             // independent loads are in flight; the order is fixed (deterministic)
             __threadfence();
             constexpr int kPairs = kRhsTile * K;
-            for (int p0 = warp * 4; p0 < kPairs; p0 += 4 * 8) {
+            for (int p0 = warp * 4; p0 < kPairs; p0 += 4 * (kThreads / 32)) {
                 double acc[4] = {0.0, 0.0, 0.0, 0.0};
                 const double* src[4];
 #pragma unroll
@@ -541,10 +550,24 @@ __global__ void k_tile_links(const cx<double>* __restrict__ A, int nx, int64_t n
     *reinterpret_cast<uint4*>(out + block * kLinkDir + (n >> 3) * 256 + g * 128 + (n & 7) * 16) = v;
 }
 
-int rows_per_cta(int nx, int ny, int nz) {
+int rows_per_cta_rule(int nx, int ny, int nz) {
     int H = ny;
     while (H % 2 == 0 && H > 4 && (nx / kW) * (ny / H) * nz < 120) H /= 2;
     return H;
+}
+
+// Rows per CTA chosen by timing for a lattice and right-hand-side count (smg_coarse_tc_tune); the
+// rule above until then.  Shared by every context of the process.
+smg_status launch_tc(smg_context* ctx, const void* links, int nx, int ny, int nrhs, int H, const cx<float>* x,
+                     cx<float>* y, int epi, const cx<float>* w, double* out, const int* gate, int* err);
+
+std::mutex g_rows_mu;
+std::map<std::tuple<int, int, int>, int> g_rows;
+
+int rows_per_cta(int nx, int ny, int nz) {
+    std::lock_guard<std::mutex> lock(g_rows_mu);
+    auto it = g_rows.find(std::make_tuple(nx, ny, nz));
+    return it != g_rows.end() ? it->second : rows_per_cta_rule(nx, ny, nz);
 }
 
 }  // namespace
@@ -572,7 +595,69 @@ smg_status smg_coarse_tc_apply(smg_context* ctx, const void* links, int nx, int 
     if (!smg_coarse_tc_shape_ok(nx, ny, kNc) || nrhs % kRhsTile != 0 || nrhs / kRhsTile > kMaxTickets)
         return smg_fail(ctx, SMG_UNSUPPORTED, "tensor-core coarse apply: shape not supported");
     const int nz = nrhs / kRhsTile;
-    const int H = rows_per_cta(nx, ny, nz);
+    return launch_tc(ctx, links, nx, ny, nrhs, rows_per_cta(nx, ny, nz), x, y, epi, w, out, gate, err);
+}
+
+// Times every rows-per-CTA choice H (the divisors ny, ny / 2, ... of the lattice height) for this
+// lattice and right-hand-side count and keeps the fastest for later applies; x and y are scratch
+// vectors of the shape.  Skipped inside stream capture and when the shape is already tuned.
+smg_status smg_coarse_tc_tune(smg_context* ctx, const void* links, int nx, int ny, int nrhs, const cx<float>* x,
+                              cx<float>* y) {
+    if (!smg_coarse_tc_shape_ok(nx, ny, kNc) || nrhs % kRhsTile != 0 || nrhs / kRhsTile > kMaxTickets)
+        return SMG_OK;
+    const int nz = nrhs / kRhsTile;
+    const auto key = std::make_tuple(nx, ny, nz);
+    {
+        std::lock_guard<std::mutex> lock(g_rows_mu);
+        if (g_rows.count(key)) return SMG_OK;
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    SMG_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return SMG_OK;
+    std::vector<int> cand;
+    for (int H = ny;; H /= 2) {
+        cand.push_back(H);
+        if (H % 2) break;
+    }
+    cudaEvent_t e0, e1;
+    SMG_CUDA(ctx, cudaEventCreate(&e0));
+    SMG_CUDA(ctx, cudaEventCreate(&e1));
+    int best = rows_per_cta_rule(nx, ny, nz);
+    float best_ms = 1e30f;
+    smg_status st = SMG_OK;
+    for (int H : cand) {
+        st = launch_tc(ctx, links, nx, ny, nrhs, H, x, y, 0, nullptr, nullptr, nullptr, nullptr);  // warm-up
+        if (st != SMG_OK) break;
+        cudaEventRecord(e0, ctx->stream);
+        for (int rep = 0; rep < 3 && st == SMG_OK; ++rep)
+            st = launch_tc(ctx, links, nx, ny, nrhs, H, x, y, 0, nullptr, nullptr, nullptr, nullptr);
+        cudaEventRecord(e1, ctx->stream);
+        if (st != SMG_OK || cudaEventSynchronize(e1) != cudaSuccess) break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = H;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    SMG_TRY(st);
+    SMG_CHECK_LAUNCH(ctx);
+    // reduction scratch for the fused-epilogue applies of this shape, reserved outside any capture
+    SMG_TRY(smg_reduce_reserve(ctx, (size_t)(nx / kW) * (ny / best) * nrhs * 3));
+    std::lock_guard<std::mutex> lock(g_rows_mu);
+    g_rows[key] = best;
+    return SMG_OK;
+}
+
+int smg_coarse_tc_rows(int nx, int ny, int nrhs) { return rows_per_cta(nx, ny, nrhs / kRhsTile); }
+
+namespace {
+
+smg_status launch_tc(smg_context* ctx, const void* links, int nx, int ny, int nrhs, int H, const cx<float>* x,
+                     cx<float>* y, int epi, const cx<float>* w, double* out, const int* gate, int* err) {
+    const int nz = nrhs / kRhsTile;
     const dim3 grid(nx / kW, ny / H, nz);
     TcArgs a;
     a.links = static_cast<const uint8_t*>(links);
@@ -592,12 +677,14 @@ smg_status smg_coarse_tc_apply(smg_context* ctx, const void* links, int nx, int 
         a.out = out;
     }
     if (epi == 0)
-        k_coarse_apply_tc<0><<<grid, 256, kSmemBytes, ctx->stream>>>(a);
+        k_coarse_apply_tc<0><<<grid, kThreads, kSmemBytes, ctx->stream>>>(a);
     else if (epi == 1)
-        k_coarse_apply_tc<1><<<grid, 256, kSmemBytes, ctx->stream>>>(a);
+        k_coarse_apply_tc<1><<<grid, kThreads, kSmemBytes, ctx->stream>>>(a);
     else
-        k_coarse_apply_tc<2><<<grid, 256, kSmemBytes, ctx->stream>>>(a);
+        k_coarse_apply_tc<2><<<grid, kThreads, kSmemBytes, ctx->stream>>>(a);
     count_launch(ctx);
     SMG_CHECK_LAUNCH(ctx);
     return SMG_OK;
 }
+
+}  // namespace

@@ -374,12 +374,43 @@ __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
     }
 }
 
-// out[j] = sum over blocks of part[block][j] (j = rhs * 3 + k), in FP64 and a fixed order
-__global__ void k_dots_finish(const float* __restrict__ part, int nblocks, int ncol, double* __restrict__ out) {
+// Sums of the stencil blocks' partials part[block][j] (j = rhs * 3 + k < ncol <= 96) in FP64 and a
+// fixed order, in two passes: block g of the first sums the contiguous rows [g R, g R + R) with
+// threads (row group, column j) and kDotsRows independent loads per thread; the second pass sums
+// the per-block results of one column per block.
+constexpr int kDotsRows = 8;  // rows per thread in the first pass
+__global__ void __launch_bounds__(256) k_dots_stage(const float* __restrict__ part, int nblocks, int ncol, int R,
+                                                    double* __restrict__ mid) {
+    __shared__ double s[256];
+    const int groups = blockDim.x / ncol;
+    const int r = threadIdx.x / ncol, j = threadIdx.x - r * ncol;
+    double acc = 0.0;
+    if (r < groups) {
+        const int b0 = blockIdx.x * R;
+        const int b1 = b0 + R < nblocks ? b0 + R : nblocks;
+        float v[kDotsRows];
+#pragma unroll
+        for (int u = 0; u < kDotsRows; ++u) {
+            const int b = b0 + r + u * groups;
+            v[u] = b < b1 ? part[(int64_t)b * ncol + j] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < kDotsRows; ++u) acc += (double)v[u];
+    }
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x < ncol) {
+        double t = 0.0;
+        for (int q = 0; q < groups; ++q) t += s[q * ncol + threadIdx.x];
+        mid[(int64_t)threadIdx.x * gridDim.x + blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_dots_finish(const double* __restrict__ mid, int G, double* __restrict__ out) {
     __shared__ double s[256];
     const int j = blockIdx.x;
-    double acc = 0;
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc += (double)part[(int64_t)b * ncol + j];
+    double acc = 0.0;
+    for (int g = threadIdx.x; g < G; g += blockDim.x) acc += mid[(int64_t)j * G + g];
     s[threadIdx.x] = acc;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
@@ -476,8 +507,13 @@ smg_status launch_dslash_h_dots(smg_dirac* d, const smg_field* src, smg_field* d
         k_dslash_h<true, true, true, true, true><<<grid, block, 0, ctx->stream>>>(a);
     else
         k_dslash_h<true, true, true, false, true><<<grid, block, 0, ctx->stream>>>(a);
-    k_dots_finish<<<nrhs * 3, 256, 0, ctx->stream>>>(part, (int)(grid.x * grid.y), nrhs * 3, out3);
-    count_launch(ctx, 2);
+    const int ncol = nrhs * 3, nblocks = (int)(grid.x * grid.y);
+    const int groups = 256 / ncol, R = groups * kDotsRows;  // rows per first-pass block
+    const int G = (nblocks + R - 1) / R;
+    SMG_TRY(smg_reduce_reserve(ctx, (size_t)G * ncol));
+    k_dots_stage<<<G, groups * ncol, 0, ctx->stream>>>(part, nblocks, ncol, R, ctx->red.partials);
+    k_dots_finish<<<ncol, 256, 0, ctx->stream>>>(ctx->red.partials, G, out3);
+    count_launch(ctx, 3);
     SMG_CHECK_LAUNCH(ctx);
     return SMG_OK;
 }
@@ -834,6 +870,11 @@ smg_status smg_dslash_h_dots(smg_dirac* d, const smg_field* src, smg_field* dst,
     return launch_dslash_h_dots(d, src, dst, w, part, out3_dev);
 }
 int smg_dslash_h_blocks(int L, int nrhs) { return dslash_h_blocks(L, nrhs); }
+// reduction scratch (doubles) the fused FP16 stencil reductions use for a lattice and nrhs
+size_t smg_dslash_h_dots_scratch(int L, int nrhs) {
+    const int ncol = nrhs * 3, R = (256 / ncol) * kDotsRows;
+    return (size_t)((dslash_h_blocks(L, nrhs) + R - 1) / R) * ncol;
+}
 
 smg_status smg_dirac_apply_internal(smg_dirac* d, smg_operator op, const smg_field* src, smg_field* dst,
                                     double* norm2_out_dev) {

@@ -28,6 +28,7 @@
 #include <complex>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <random>
 #include <type_traits>
 #include <vector>
@@ -38,12 +39,15 @@ smg_status smg_dslash_mr(smg_dirac* d, bool dag, const smg_field* src, smg_field
 smg_status smg_dslash_h_dots(smg_dirac* d, const smg_field* src, smg_field* dst, const smg_field* w, float* part,
                              double* out3_dev);
 int smg_dslash_h_blocks(int L, int nrhs);
+size_t smg_dslash_h_dots_scratch(int L, int nrhs);
 // tensor-core coarse apply (coarse_tc.cu)
 bool smg_coarse_tc_shape_ok(int nx, int ny, int ndof);
 size_t smg_coarse_tc_link_bytes(int64_t nsites);
 smg_status smg_coarse_tc_tile_links(smg_context* ctx, const cx<double>* A64, int nx, int64_t nsites, void* out);
 smg_status smg_coarse_tc_apply(smg_context* ctx, const void* links, int nx, int ny, int nrhs, const cx<float>* x,
                                cx<float>* y, int epi, const cx<float>* w, double* out, const int* gate, int* err);
+smg_status smg_coarse_tc_tune(smg_context* ctx, const void* links, int nx, int ny, int nrhs, const cx<float>* x,
+                              cx<float>* y);
 
 namespace {
 
@@ -302,7 +306,6 @@ __device__ __forceinline__ int64_t transfer_site(const TransferGeom& t, int B, i
 __device__ __forceinline__ int64_t transfer_idx(const TransferGeom& t, int64_t s, int j, int rhs) {
     return t.level0 ? (s * t.nrhs + rhs) * 2 + j : (s * t.ndof + j) * t.nrhs + rhs;
 }
-constexpr int kTransferChunk = 4;  // outputs reduced across rows per shared-memory pass
 
 // fine/coarse vector readers for the restriction: plain, or FP16 with per-site scales
 template <typename T>
@@ -320,61 +323,63 @@ struct InHalf {
     }
 };
 
+// One block per (aggregate, tile of `lanes` right-hand sides) stages the aggregate's ne = ax ay
+// ndof input values of its right-hand sides and its block vectors in shared memory (every global
+// load issued before any arithmetic), then each thread (rhs lane, row) forms whole outputs from
+// shared memory: no cross-thread reduction, one barrier.
 template <typename T, int NC, typename In = InPlain<T>>
 __global__ void __launch_bounds__(256) k_restrict_agg(const cx<T>* __restrict__ V, In in,
                                                       cx<T>* __restrict__ out, TransferGeom t) {
     extern __shared__ unsigned char s_raw[];
-    cx<T>* s_acc = reinterpret_cast<cx<T>*>(s_raw);  // [rows][kTransferChunk][lanes]
     const int lanes = blockDim.x, rows = blockDim.y;
-    const int B = blockIdx.x, m = t.ax * t.ay, nd = t.ndof, nrhs = t.nrhs;
+    const int B = blockIdx.x, m = t.ax * t.ay, nd = t.ndof, nrhs = t.nrhs, ne = m * nd;
+    cx<T>* s_f = reinterpret_cast<cx<T>*>(s_raw);  // [ne][lanes]
+    cx<T>* s_v = s_f + (int64_t)ne * lanes;        // [ne][NC]
     const int rhs = blockIdx.y * lanes + threadIdx.x;
     const bool live = rhs < nrhs;
-    cx<T> acc[NC];
-#pragma unroll
-    for (int i = 0; i < NC; ++i) acc[i] = mk<T>(0, 0);
-    for (int e = threadIdx.y; e < m * nd; e += rows) {
+#pragma unroll 4
+    for (int e = threadIdx.y; e < ne; e += rows) {
         const int loc = e / nd, j = e - loc * nd;
         const int64_t s = transfer_site(t, B, loc);
-        const cx<T> f = live ? in(transfer_idx(t, s, j, rhs), s) : mk<T>(0, 0);
-        const cx<T>* v = V + (((int64_t)B * m + loc) * nd + j) * NC;
-#pragma unroll
-        for (int i = 0; i < NC; ++i) acc[i] = acc[i] + cmulc(v[i], f);
+        s_f[e * lanes + threadIdx.x] = live ? in(transfer_idx(t, s, j, rhs), s) : mk<T>(0, 0);
     }
-    // rows summed in a fixed order, kTransferChunk outputs per pass
-#pragma unroll
-    for (int i0 = 0; i0 < NC; i0 += kTransferChunk) {
-#pragma unroll
-        for (int ii = 0; ii < kTransferChunk; ++ii)
-            s_acc[(threadIdx.y * kTransferChunk + ii) * lanes + threadIdx.x] = acc[i0 + ii];
-        __syncthreads();
-        if (live && threadIdx.y < kTransferChunk) {
-            cx<T> sum = mk<T>(0, 0);
-            for (int r = 0; r < rows; ++r) sum = sum + s_acc[(r * kTransferChunk + threadIdx.y) * lanes + threadIdx.x];
-            out[((int64_t)B * NC + i0 + threadIdx.y) * nrhs + rhs] = sum;
-        }
-        __syncthreads();
+    const cx<T>* __restrict__ Vb = V + (int64_t)B * ne * NC;
+    for (int k = threadIdx.y * lanes + threadIdx.x; k < ne * NC; k += lanes * rows) s_v[k] = Vb[k];
+    __syncthreads();
+    if (!live) return;
+    for (int i = threadIdx.y; i < NC; i += rows) {
+        cx<T> acc = mk<T>(0, 0);
+#pragma unroll 8
+        for (int e = 0; e < ne; ++e) acc = acc + cmulc(s_v[e * NC + i], s_f[e * lanes + threadIdx.x]);
+        out[((int64_t)B * NC + i) * nrhs + rhs] = acc;
     }
 }
 
 template <typename T, int NC>
 __global__ void __launch_bounds__(256) k_prolong_agg(const cx<T>* __restrict__ V, const cx<T>* __restrict__ cin,
                                                      cx<T>* __restrict__ out, TransferGeom t, int accumulate) {
+    extern __shared__ unsigned char s_raw[];
     const int lanes = blockDim.x, rows = blockDim.y;
-    const int B = blockIdx.x, m = t.ax * t.ay, nd = t.ndof, nrhs = t.nrhs;
+    const int B = blockIdx.x, m = t.ax * t.ay, nd = t.ndof, nrhs = t.nrhs, ne = m * nd;
+    cx<T>* s_c = reinterpret_cast<cx<T>*>(s_raw);  // [NC][lanes]
+    cx<T>* s_v = s_c + NC * lanes;                 // [ne][NC]
     const int rhs = blockIdx.y * lanes + threadIdx.x;
-    if (rhs >= nrhs) return;
-    cx<T> c[NC];
-#pragma unroll
-    for (int i = 0; i < NC; ++i) c[i] = cin[((int64_t)B * NC + i) * nrhs + rhs];
-    for (int e = threadIdx.y; e < m * nd; e += rows) {
+    const bool live = rhs < nrhs;
+    for (int i = threadIdx.y; i < NC; i += rows)
+        s_c[i * lanes + threadIdx.x] = live ? cin[((int64_t)B * NC + i) * nrhs + rhs] : mk<T>(0, 0);
+    const cx<T>* __restrict__ Vb = V + (int64_t)B * ne * NC;
+    for (int k = threadIdx.y * lanes + threadIdx.x; k < ne * NC; k += lanes * rows) s_v[k] = Vb[k];
+    __syncthreads();
+    if (!live) return;
+#pragma unroll 2
+    for (int e = threadIdx.y; e < ne; e += rows) {
         const int loc = e / nd, j = e - loc * nd;
-        const int64_t s = transfer_site(t, B, loc);
-        const cx<T>* v = V + (((int64_t)B * m + loc) * nd + j) * NC;
+        const int64_t o = transfer_idx(t, transfer_site(t, B, loc), j, rhs);
+        const cx<T> prev = accumulate ? out[o] : mk<T>(0, 0);
         cx<T> acc = mk<T>(0, 0);
 #pragma unroll
-        for (int i = 0; i < NC; ++i) acc = acc + v[i] * c[i];
-        const int64_t o = transfer_idx(t, s, j, rhs);
-        out[o] = accumulate ? out[o] + acc : acc;
+        for (int i = 0; i < NC; ++i) acc = acc + s_v[e * NC + i] * s_c[i * lanes + threadIdx.x];
+        out[o] = accumulate ? prev + acc : acc;
     }
 }
 
@@ -961,17 +966,31 @@ __global__ void __launch_bounds__(256) k_ccg_update(CcgState s, VecView<T> x, cx
     T v[1] = {T(0)};
     cx<T>* __restrict__ xp = x.p;
     if (rhs < nrhs) {
-        const int ds = x.dstride();
-#pragma unroll 2
-        for (int st = blockIdx.x * blockDim.y + threadIdx.y; st < x.nsites; st += gridDim.x * blockDim.y) {
-            const int64_t base = x.idx(st, rhs, 0);
-            for (int d = 0; d < x.ndof; ++d) {
-                const int64_t e = base + (int64_t)d * ds;
-                const cx<T> ri = r[e] - al * Ap[e];
-                xp[e] = xp[e] + al * p[e];
-                r[e] = ri;
-                v[0] += norm2(ri);
-            }
+        // coarse vectors [site][dof][rhs]: entry (e = site * ndof + dof, rhs) at e * nrhs + rhs; four
+        // entries per thread and pass with every load issued first
+        constexpr int U = 4;
+        const int64_t nel = (int64_t)x.nsites * x.ndof;
+        for (int64_t e0 = ((int64_t)blockIdx.x * blockDim.y + threadIdx.y) * U; e0 < nel;
+             e0 += (int64_t)gridDim.x * blockDim.y * U) {
+            cx<T> rv[U], av[U], xv[U], pv[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (e0 + u < nel) {
+                    const int64_t e = (e0 + u) * nrhs + rhs;
+                    rv[u] = r[e];
+                    av[u] = Ap[e];
+                    xv[u] = xp[e];
+                    pv[u] = p[e];
+                }
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+                if (e0 + u < nel) {
+                    const int64_t e = (e0 + u) * nrhs + rhs;
+                    const cx<T> ri = rv[u] - al * av[u];
+                    xp[e] = xv[u] + al * pv[u];
+                    r[e] = ri;
+                    v[0] += norm2(ri);
+                }
         }
     }
     block_reduce_finalise<1>(v, partials, ticket, nrhs, FinCcg{s});
@@ -1308,8 +1327,10 @@ smg_status ensure_work(smg_mg* mg, int nrhs, smg_precision prec) {
     SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &mg->f_r));
     SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &mg->f_Ar));
     SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &mg->f_t));
-    if (wp == SMG_F16)
+    if (wp == SMG_F16) {
         SMG_CUDA(ctx, cudaMalloc(&mg->hdots, (size_t)smg_dslash_h_blocks(L, nrhs) * nrhs * 3 * sizeof(float)));
+        SMG_TRY(smg_reduce_reserve(ctx, smg_dslash_h_dots_scratch(L, nrhs)));  // before any capture
+    }
     size_t es = prec == SMG_F64 ? sizeof(cx<double>) : sizeof(cx<float>);
     mg->cw.resize(mg->lv.size());
     for (size_t l = 1; l < mg->lv.size(); ++l) {
@@ -1330,6 +1351,12 @@ smg_status ensure_work(smg_mg* mg, int nrhs, smg_precision prec) {
     mg->work_nrhs = nrhs;
     mg->work_prec = prec;
     mg->work_gen++;
+    // launch shape of the tensor-core coarse applies, timed once per lattice and nrhs
+    if (prec == SMG_F32)
+        for (size_t l = 1; l < mg->lv.size(); ++l)
+            if (tc_path(mg, (int)l, nrhs))
+                SMG_TRY(smg_coarse_tc_tune(ctx, mg->lv[l].Atc, mg->lv[l].nx, mg->lv[l].ny, nrhs,
+                                           (const cx<float>*)mg->cw[l].x, (cx<float>*)mg->cw[l].Ar));
     return SMG_OK;
 }
 
@@ -1512,6 +1539,22 @@ smg_status smooth_fine_half(smg_mg* mg, smg_field* x, const smg_field* b, int ni
 TransferGeom transfer_geom(const smg_mg* mg, int l, int nrhs);
 dim3 transfer_block(int nrhs);
 
+// dynamic shared memory of the aggregate transfer kernels: staged inputs (restriction: ne x lanes,
+// prolongation: NC x lanes) and the aggregate's block vectors (ne x NC)
+template <typename T>
+size_t transfer_smem(const Level& L, int lanes, bool restrict_in) {
+    const int64_t ne = (int64_t)L.ax * L.ay * L.ndof;
+    return (size_t)(((restrict_in ? ne : L.nc_next) * lanes + ne * L.nc_next) * sizeof(cx<T>));
+}
+// above the default 48 KB the kernel instance must opt in (once per instance)
+template <typename K>
+void transfer_smem_attr(K kernel, size_t bytes, std::once_flag& once) {
+    if (bytes > 48 * 1024)
+        std::call_once(once, [kernel] {
+            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        });
+}
+
 // restriction of the FP16 fine residual (k_restrict_agg with an FP16 reader)
 smg_status restrict_half(smg_mg* mg, const smg_field* r, void* out) {
     smg_context* ctx = mg->ctx;
@@ -1522,7 +1565,7 @@ smg_status restrict_half(smg_mg* mg, const smg_field* r, void* out) {
     TransferGeom t = transfer_geom(mg, 0, nrhs);
     const dim3 block = transfer_block(nrhs);
     const dim3 grid(N.nsites, (nrhs + block.x - 1) / block.x);
-    const size_t sm = (size_t)block.x * block.y * kTransferChunk * sizeof(cx<float>);
+    const size_t sm = transfer_smem<float>(L, (int)block.x, true);
     const InHalf in{(const __half2*)r->data, r->scale};
     if (nc == 8)
         k_restrict_agg<float, 8, InHalf><<<grid, block, sm, ctx->stream>>>(L.V32, in, (cx<float>*)out, t);
@@ -1702,6 +1745,7 @@ smg_status coarse_cg(smg_mg* mg, int l, void* x, const void* b) {
     count_launch(ctx);
     const VecView<T> xf = flat(xv), pf = flat(pv);
     ReduceLaunch rl = reduce_launch(xf.nsites, nrhs);
+    if (rl.grid.x > 148) rl.grid.x = 148;  // fewer partials for the finishing block (k_ccg_update strides)
     SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * nrhs * 3));
     SMG_TRY(smg_host_stage_reserve(ctx, 64));
     int* h_act = (int*)ctx->host_stage;
@@ -1757,8 +1801,14 @@ smg_status restrict_to(smg_mg* mg, int l, const void* fine_or_coarse, void* out)
         TransferGeom t = transfer_geom(mg, l, nrhs);
         const dim3 block = transfer_block(nrhs);
         const dim3 grid(N.nsites, (nrhs + block.x - 1) / block.x);
-        const size_t sm = (size_t)block.x * block.y * kTransferChunk * sizeof(cx<T>);
-#define SMG_RA(NC) k_restrict_agg<T, NC><<<grid, block, sm, ctx->stream>>>(Vp<T>(L), InPlain<T>{(const cx<T>*)fine_or_coarse}, (cx<T>*)out, t)
+        const size_t sm = transfer_smem<T>(L, (int)block.x, true);
+#define SMG_RA(NC)                                                                                         \
+    do {                                                                                                   \
+        static std::once_flag once;                                                                        \
+        transfer_smem_attr(k_restrict_agg<T, NC>, sm, once);                                               \
+        k_restrict_agg<T, NC><<<grid, block, sm, ctx->stream>>>(Vp<T>(L), InPlain<T>{(const cx<T>*)fine_or_coarse}, \
+                                                               (cx<T>*)out, t);                            \
+    } while (0)
         if (nc == 8) SMG_RA(8);
         else if (nc == 16) SMG_RA(16);
         else SMG_RA(32);
@@ -1790,7 +1840,14 @@ smg_status prolong_to(smg_mg* mg, int l, const void* coarse, void* out, int accu
         TransferGeom t = transfer_geom(mg, l, nrhs);
         const dim3 block = transfer_block(nrhs);
         const dim3 grid(N.nsites, (nrhs + block.x - 1) / block.x);
-#define SMG_PA(NC) k_prolong_agg<T, NC><<<grid, block, 0, ctx->stream>>>(Vp<T>(L), (const cx<T>*)coarse, (cx<T>*)out, t, accumulate)
+        const size_t sm = transfer_smem<T>(L, (int)block.x, false);
+#define SMG_PA(NC)                                                                                         \
+    do {                                                                                                   \
+        static std::once_flag once;                                                                        \
+        transfer_smem_attr(k_prolong_agg<T, NC>, sm, once);                                                \
+        k_prolong_agg<T, NC><<<grid, block, sm, ctx->stream>>>(Vp<T>(L), (const cx<T>*)coarse, (cx<T>*)out, t, \
+                                                              accumulate);                                 \
+    } while (0)
         if (nc == 8) SMG_PA(8);
         else if (nc == 16) SMG_PA(16);
         else SMG_PA(32);

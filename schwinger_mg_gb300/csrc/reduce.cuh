@@ -57,8 +57,8 @@ __device__ __forceinline__ void block_reduce_finalise(double (&v)[K], double* __
             for (int w = 0; w < nwarps; ++w) a += s_rows[k][w][t];
             partials[((size_t)(rhs0 + t) * K + k) * gridDim.x + blockIdx.x] = a;
         }
+        __threadfence();  // this thread's partials are visible before the block takes its ticket
     }
-    __threadfence();
     __syncthreads();
     if (t == 0) {
         unsigned int prev = atomicAdd(ticket + blockIdx.y, 1u);
@@ -67,29 +67,43 @@ __device__ __forceinline__ void block_reduce_finalise(double (&v)[K], double* __
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    // last block: one warp per (lane, k) pair, strided sums in a fixed order
+    // last block: each warp sums four (lane, k) pairs at once, lanes striding over the blocks with
+    // four blocks per pair in flight (16 independent loads per lane); fixed order, deterministic
     const int npairs = lanes * K;
-    for (int p = warp; p < npairs; p += nwarps) {
-        const int l = p / K, k = p - l * K;
-        const int r = rhs0 + l;
-        double a = 0.0;
-        if (r < nrhs) {
-            // eight independent accumulators keep eight loads in flight; fixed order, deterministic
-            const double* src = partials + ((size_t)r * K + k) * gridDim.x;
-            const int nb = (int)gridDim.x;
-            double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-            int b = lane_id;
-            for (; b + 7 * 32 < nb; b += 8 * 32) {
+    const int nb = (int)gridDim.x;
+    for (int p0 = warp * 4; p0 < npairs; p0 += nwarps * 4) {
+        const double* src[4];
+        bool live[4];
+        double acc[4][4];
 #pragma unroll
-                for (int u = 0; u < 8; ++u) acc[u] += __ldcg(src + b + u * 32);
-            }
+        for (int q = 0; q < 4; ++q) {
+            const int p = p0 + q < npairs ? p0 + q : npairs - 1;
+            const int l = p / K, k = p - l * K;
+            live[q] = p0 + q < npairs && rhs0 + l < nrhs;
+            src[q] = partials + ((size_t)(rhs0 + l) * K + k) * nb;
 #pragma unroll
-            for (int u = 0; u < 8; ++u)
-                if (b + u * 32 < nb) acc[u] += __ldcg(src + b + u * 32);
-            a = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+            for (int u = 0; u < 4; ++u) acc[q][u] = 0.0;
         }
-        for (int off = 16; off >= 1; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
-        if (lane_id == 0) s_fin[k][l] = a;
+        int b = lane_id;
+        for (; b + 3 * 32 < nb; b += 4 * 32) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (live[q]) acc[q][u] += __ldcg(src[q] + b + u * 32);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (live[q] && b + u * 32 < nb) acc[q][u] += __ldcg(src[q] + b + u * 32);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            double a = (acc[q][0] + acc[q][1]) + (acc[q][2] + acc[q][3]);
+            for (int off = 16; off >= 1; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+            const int p = p0 + q, l = p / K, k = p - l * K;
+            if (lane_id == 0 && p < npairs) s_fin[k][l] = live[q] ? a : 0.0;
+        }
     }
     __syncthreads();
     if (t < lanes && rhs0 + t < nrhs) {

@@ -4,7 +4,8 @@
 // to its kernels without serialising them.
 //
 //   int smg_ktrace_start(void);              0 on success
-//   int smg_ktrace_stop(const char* path);   writes "launches total_ns name" lines
+//   int smg_ktrace_stop(const char* path);   writes "launches total_ns gridXxYxZ name" lines
+//                                            (one line per kernel and grid shape)
 #include <cupti.h>
 
 #include <cstdio>
@@ -34,7 +35,9 @@ void CUPTIAPI buffer_completed(CUcontext, uint32_t, uint8_t* buf, size_t, size_t
     while (cuptiActivityGetNextRecord(buf, valid, &rec) == CUPTI_SUCCESS) {
         if (rec->kind != CUPTI_ACTIVITY_KIND_CONCURRENT_KERNEL) continue;
         const auto* k = reinterpret_cast<const CUpti_ActivityKernel10*>(rec);
-        Agg& a = g_agg[k->name ? k->name : "?"];
+        char grid[64];
+        std::snprintf(grid, sizeof grid, "%dx%dx%d ", k->gridX, k->gridY, k->gridZ);
+        Agg& a = g_agg[std::string(grid) + (k->name ? k->name : "?")];
         a.n += 1;
         a.ns += k->end - k->start;
         if (k->start < g_first) g_first = k->start;
