@@ -175,6 +175,12 @@ def dslash_bytes_f32(L, nrhs):
     return L * L * (32 * nrhs + 20)
 
 
+def dslash_bytes_f16(L, nrhs):
+    """Compulsory HBM bytes of one FP16-field D application: spinor in + out (2 x 8 B per site per
+    rhs) plus the two per-site scales (8 B), 2 complex64 links (16 B), the clover shift (4 B)."""
+    return L * L * (16 * nrhs + 28)
+
+
 def dslash_bytes_f64_single(L):
     """13 x 8 B per site for one FP64 single-RHS application (in 32, out 32, links 32, clover 8)."""
     return L * L * 104
@@ -286,6 +292,10 @@ def run_ours(args, ws, rank, local):
         D = smg.DiracOp(lat, g, c["m"], c["r"], c["csw"], c["mu"])
         t0 = time.perf_counter()
         mg32 = smg.MGHierarchy(D, mg_params(smg, c, "f32"))
+        defl_info = None
+        if args.coarse_defl:
+            defl_info = mg32.setup_deflation(args.coarse_defl, level=c["levels"] - 1, tol=1e-6,
+                                             allow_unconverged=True)
         ctx.synchronize()
         setup_s = time.perf_counter() - t0
         B = np.stack([smg.random_vec(lat.ndof, c["seed"] + 1 + j) for j in range(nrhs)])
@@ -351,6 +361,9 @@ def run_ours(args, ws, rank, local):
                        "L": L, "nrhs": nrhs, "levels": c["levels"], "gcr_iterations": iters,
                        "smoother_work_vectors": "FP16, per-site scales" if c["smoother_half"] else "FP32",
                        "gcr_truncation": c["trunc"],
+                       "coarsest_deflation": ({"eigenvectors": args.coarse_defl, "converged": bool(defl_info.converged),
+                                               "restarts": defl_info.restarts, "lanczos_steps": defl_info.iterations}
+                                              if defl_info is not None else None),
                        "launches_before_timed": int(l0),
                        "true_residual": true_res, "setup_s": setup_s,
                        "plain_fp64_mg_solves_per_s": 1e3 / ms64, "plain_fp64_mg_iterations": it64,
@@ -375,9 +388,10 @@ def run_ours(args, ws, rank, local):
         g = smg.GaugeField(lat, U, ctx)
         D = smg.DiracOp(lat, g, c["m"], c["r"], c["csw"], c["mu"])
         srcs = np.stack([smg.random_vec(lat.ndof, c["seed"] + 1 + j) for j in range(nrhs)])
-        fs = smg.Field(lat, nrhs, "f32", ctx, data=srcs)
-        fd = smg.Field(lat, nrhs, "f32", ctx)
-        bytes_step = dslash_bytes_f32(L, nrhs)
+        prec = args.dslash_prec
+        fs = smg.Field(lat, nrhs, prec, ctx, data=srcs)
+        fd = smg.Field(lat, nrhs, prec, ctx)
+        bytes_step = dslash_bytes_f32(L, nrhs) if prec == "f32" else dslash_bytes_f16(L, nrhs)
 
         def step():
             smg._lib.check(lib.smg_dirac_apply(D.h, 0, fs.h, fd.h), "dirac_apply", ctx.h)
@@ -404,17 +418,21 @@ def run_ours(args, ws, rank, local):
         e2e_ms = timed(e2e_step, args.steps)
         hb = srcs.size * 16
         out.update({
-            "value": value, "unit": "GB/s", "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
-            "config": {"workload": f"FP32 Wilson-clover D on {nrhs} RHS, L={L} (beta=6, m=-0.05, c_sw=1)",
+            "value": value, "unit": "GB/s", "ms_per_step": ms, "higher_is_better": True, "dtype": prec,
+            "config": {"workload": (f"FP32 Wilson-clover D on {nrhs} RHS, L={L} (beta=6, m=-0.05, c_sw=1)" if prec == "f32"
+                                    else f"Wilson-clover D on FP16 fields (per-site scales, FP32 arithmetic), {nrhs} RHS, "
+                                         f"L={L} (beta=6, m=-0.05, c_sw=1)"),
                        "L": L, "nrhs": nrhs, "bytes_per_step": bytes_step,
-                       "l2": "inputs and outputs (268 MB) exceed the 129 MB L2; no flush",
+                       "l2": f"inputs and outputs ({bytes_step / 1e6:.0f} MB) exceed the 129 MB L2; no flush",
                        "timed_steps": max(args.steps, 500)},
             "e2e": {"value": ws * bytes_step / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
                     "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb, "ms_per_step": e2e_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": (140.034048e6 + 98.370048e6) if (L, nrhs) == (512, 32) else None,
+                         "traffic": (140.034048e6 + 98.370048e6) if (L, nrhs, prec) == (512, 32, "f32") else None,
                          "traffic_unit": "bytes per launch (ncu, profiles/dslash_f32_L512_32rhs.md)",
-                         "kernel": "k_dslash<float,false,0,r=1> (autotuned row kernel)", "peak_source": peak_kind},
+                         "kernel": ("k_dslash<float,false,0,r=1> (autotuned row kernel)" if prec == "f32"
+                                    else "k_dslash_h<false,true,true,r=1> (FP16 fields)"),
+                         "peak_source": peak_kind},
             "gpu_launches": int(launches), "clocks": clk.summary(),
         })
     elif args.workload == "hmc":
@@ -790,6 +808,10 @@ def main():
                     help="mg workload: precision of the fine smoother's work vectors (f16: per-site scaled FP16)")
     ap.add_argument("--trunc", type=int, default=0, help="mg / batch workloads: GCR truncation override")
     ap.add_argument("--coarse-iters", type=int, default=0, help="mg / batch workloads: coarsest-CG iteration cap override")
+    ap.add_argument("--dslash-prec", default="f32", choices=["f32", "f16"],
+                    help="dslash workload: field precision (f16 = FP16 storage with per-site scales)")
+    ap.add_argument("--coarse-defl", type=int, default=0,
+                    help="mg workload: eigenvectors of the coarsest operator for the coarsest CG's deflated start")
     ap.add_argument("--kernel-trace", default="", help="mg and batch workloads: write a CUPTI per-kernel summary of "
                                                          "one extra (untimed) step to this path")
     args = ap.parse_args()

@@ -351,6 +351,12 @@ typedef struct {
  * converge within max_restarts. */
 SMG_API smg_status smg_mg_setup_deflation(smg_mg* mg, int n_ev, int n_kr, int max_restarts, double tol,
                                           smg_deflation_info* info);
+/* smg_mg_setup_deflation on the operator of coarse level `level` (1 = the
+ * reference's choice).  With level the coarsest level, the coarsest CG of
+ * every cycle starts from the deflated guess; the low-mode solution needs
+ * level 1. */
+SMG_API smg_status smg_mg_setup_deflation_level(smg_mg* mg, int level, int n_ev, int n_kr, int max_restarts,
+                                                double tol, smg_deflation_info* info);
 /* Replaces the eigenpairs (defl_vecs / defl_vals): n vectors of the level-1
  * dimension, interleaved complex128, in the reference's coarse layout
  * c[b * k + kv] with b the lexicographic coarse site. */

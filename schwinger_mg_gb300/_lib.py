@@ -170,6 +170,8 @@ _SIGS = {
     "smg_estimate_lambda_max": (_st, [_vp, C.c_int, _dp]),
     "smg_mg_rebuild": (_st, [_vp]),
     "smg_mg_setup_deflation": (_st, [_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(DeflationInfo)]),
+    "smg_mg_setup_deflation_level": (_st, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
+                                           C.POINTER(DeflationInfo)]),
     "smg_mg_set_deflation": (_st, [_vp, C.c_int, _dp, _dp]),
     "smg_mg_get_deflation": (_st, [_vp, C.POINTER(C.c_int), _dp, _dp]),
     "smg_mg_deflation_rr": (_st, [_vp, _dp]),

@@ -849,12 +849,13 @@ class MGHierarchy(_Handle):
 
 
     def setup_deflation(self, n_ev: int, n_kr: int = 0, max_restarts: int = 100, tol: float = 1e-10,
-                        allow_unconverged: bool = False) -> _L.DeflationInfo:
+                        allow_unconverged: bool = False, level: int = 1) -> _L.DeflationInfo:
         """SparseCoarseOp::setup_deflation (src/coarse_op.cpp:10-54, TRLM): the n_ev lowest
-        eigenpairs of the level-1 operator; the coarsest CG of a two-level hierarchy then starts
-        from the deflated guess."""
+        eigenpairs of the level-1 operator (or of `level`); when that level is the coarsest, the
+        coarsest CG of every cycle starts from the deflated guess."""
         info = _L.DeflationInfo()
-        st = _L.lib().smg_mg_setup_deflation(self.h, n_ev, n_kr, max_restarts, tol, C.byref(info))
+        self._defl_level = level
+        st = _L.lib().smg_mg_setup_deflation_level(self.h, level, n_ev, n_kr, max_restarts, tol, C.byref(info))
         if not (allow_unconverged and st == _L.NOT_CONVERGED):
             _L.check(st, "smg_mg_setup_deflation", self.ctx.h)
         return info
@@ -863,6 +864,7 @@ class MGHierarchy(_Handle):
         """Installs eigenpairs (vectors in the reference's coarse layout, one per row)."""
         vals = np.ascontiguousarray(vals, dtype=np.float64).reshape(-1)
         vecs = _as_c128(vecs).reshape(len(vals), -1)
+        self._defl_level = 1
         _L.check(_L.lib().smg_mg_set_deflation(self.h, len(vals), _ptr(vals), _ptr(vecs.view(np.float64))),
                  "smg_mg_set_deflation", self.ctx.h)
 
@@ -872,7 +874,7 @@ class MGHierarchy(_Handle):
         n = C.c_int()
         _L.check(_L.lib().smg_mg_get_deflation(self.h, C.byref(n), None, None), "smg_mg_get_deflation", self.ctx.h)
         vals = np.empty(n.value)
-        vecs = np.empty((n.value, self.level_dim(1)), dtype=np.complex128)
+        vecs = np.empty((n.value, self.level_dim(getattr(self, "_defl_level", 1))), dtype=np.complex128)
         if n.value:
             _L.check(_L.lib().smg_mg_get_deflation(self.h, C.byref(n), _ptr(vals), _ptr(vecs.view(np.float64))),
                      "smg_mg_get_deflation", self.ctx.h)

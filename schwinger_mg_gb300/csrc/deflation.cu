@@ -3,7 +3,8 @@
 // src/hmc.h:307-324).
 //
 // The deflation space is the n lowest eigenpairs of the level-1 operator
-// A_c = P^dag (D^dag D) P.  They are found by thick-restart Lanczos
+// A_c = P^dag (D^dag D) P (or, on request, of a deeper coarse level's
+// operator).  They are found by thick-restart Lanczos
 // (Wu & Simon, SIAM J. Matrix Anal. Appl. 22 (2000) 602), the method of the
 // reference's trlm_eigensolver without Chebyshev acceleration, with the same
 // schedule: Krylov space n_kr, restart keeping
@@ -270,10 +271,10 @@ smg_status commit(smg_context* ctx, MgDeflation& d) {
 }
 
 // trlm_eigensolver (src/eigensolver_core.cpp:691-1057, poly_deg = 0) on A_1 of the hierarchy
-smg_status trlm(smg_mg* mg, int n_ev, int n_kr, int max_restarts, double tol, cx<double>* vecs_out,
+smg_status trlm(smg_mg* mg, int level, int n_ev, int n_kr, int max_restarts, double tol, cx<double>* vecs_out,
                 std::vector<double>& vals_out, smg_deflation_info* info) {
     smg_context* ctx = smg_mg_ctx(mg);
-    const int64_t n = smg_mg_level1_dim(mg);
+    const int64_t n = smg_mg_level_dim(mg, level);
     Workspace ws;
     ws.ctx = ctx;
     cx<double>* K = nullptr;  // n_kr + 1 Krylov vectors
@@ -318,7 +319,7 @@ smg_status trlm(smg_mg* mg, int n_ev, int n_kr, int max_restarts, double tol, cx
         // Krylov extension from num_keep to n_kr (lanczosStep, src/eigensolver_core.cpp:816-851)
         for (int j = num_keep; j < n_kr; ++j) {
             cx<double>* vj = K + (int64_t)j * n;
-            SMG_TRY(smg_mg_apply1_f64(mg, vj, r));
+            SMG_TRY(smg_mg_apply_f64(mg, level, vj, r));
             for (int pass = 0; pass < 2; ++pass) {
                 SMG_TRY(multi_dot(ctx, K, n, j + 1, r, n, part, c));
                 // alpha_j = Re <v_j, A v_j> before any orthogonalisation
@@ -477,6 +478,8 @@ template smg_status smg_defl_guess<double>(smg_context*, MgDeflation&, VecView<d
 smg_status smg_mg_lowmode_internal(smg_mg* mg, const smg_field* phi, smg_field* x) {
     smg_context* ctx = smg_mg_ctx(mg);
     MgDeflation& d = smg_mg_defl(mg);
+    if (d.n > 0 && d.level != 1)
+        return smg_fail(ctx, SMG_UNSUPPORTED, "low-mode solution: the deflation space is not on level 1");
     if (d.n == 0) {
         SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
         return SMG_OK;
@@ -494,12 +497,13 @@ smg_status smg_mg_lowmode_internal(smg_mg* mg, const smg_field* phi, smg_field* 
 
 extern "C" {
 
-SMG_API smg_status smg_mg_setup_deflation(smg_mg* mg, int n_ev, int n_kr, int max_restarts, double tol,
-                                          smg_deflation_info* info) {
+SMG_API smg_status smg_mg_setup_deflation_level(smg_mg* mg, int level, int n_ev, int n_kr, int max_restarts,
+                                                double tol, smg_deflation_info* info) {
     if (!mg || n_ev < 0 || max_restarts < 0 || !(tol > 0)) return SMG_BAD_ARG;
     smg_context* ctx = smg_mg_ctx(mg);
-    if (smg_mg_nlevels(mg) < 2) return smg_fail(ctx, SMG_BAD_ARG, "deflation needs a coarse level");
-    const int64_t dim = smg_mg_level1_dim(mg);
+    if (level < 1 || level >= smg_mg_nlevels(mg))
+        return smg_fail(ctx, SMG_BAD_ARG, "deflation: level must be a coarse level of the hierarchy");
+    const int64_t dim = smg_mg_level_dim(mg, level);
     MgDeflation& d = smg_mg_defl(mg);
     smg_mg_drop_cycle_graph(mg);
     if (n_ev == 0) {
@@ -516,8 +520,9 @@ SMG_API smg_status smg_mg_setup_deflation(smg_mg* mg, int n_ev, int n_kr, int ma
     if (n_ev > n_kr || n_kr > 120) return smg_fail(ctx, SMG_UNSUPPORTED, "deflation: n_ev <= n_kr <= 120 required");
     SMG_TRY(ensure_storage(ctx, d, n_ev, dim));
     d.n = 0;
+    d.level = level;
     std::vector<double> vals;
-    SMG_TRY(trlm(mg, n_ev, n_kr, max_restarts, tol, d.V64, vals, info));
+    SMG_TRY(trlm(mg, level, n_ev, n_kr, max_restarts, tol, d.V64, vals, info));
     d.n = n_ev;
     d.vals = vals;
     SMG_TRY(commit(ctx, d));
@@ -525,13 +530,19 @@ SMG_API smg_status smg_mg_setup_deflation(smg_mg* mg, int n_ev, int n_kr, int ma
     return SMG_OK;
 }
 
+SMG_API smg_status smg_mg_setup_deflation(smg_mg* mg, int n_ev, int n_kr, int max_restarts, double tol,
+                                          smg_deflation_info* info) {
+    return smg_mg_setup_deflation_level(mg, 1, n_ev, n_kr, max_restarts, tol, info);
+}
+
 SMG_API smg_status smg_mg_set_deflation(smg_mg* mg, int n, const double* vals, const double* vecs) {
     if (!mg || n < 0 || (n > 0 && (!vals || !vecs))) return SMG_BAD_ARG;
     smg_context* ctx = smg_mg_ctx(mg);
     if (smg_mg_nlevels(mg) < 2) return smg_fail(ctx, SMG_BAD_ARG, "deflation needs a coarse level");
-    const int64_t dim = smg_mg_level1_dim(mg);
+    const int64_t dim = smg_mg_level_dim(mg, 1);
     MgDeflation& d = smg_mg_defl(mg);
     smg_mg_drop_cycle_graph(mg);
+    d.level = 1;
     if (n > 0) {
         SMG_TRY(ensure_storage(ctx, d, n, dim));
         SMG_CUDA(ctx, cudaMemcpyAsync(d.V64, vecs, (size_t)n * dim * sizeof(cx<double>), cudaMemcpyHostToDevice,
@@ -579,7 +590,7 @@ SMG_API smg_status smg_mg_deflation_rr(smg_mg* mg, double* max_residual) {
     SMG_TRY(ws.alloc(&out, (size_t)2 * k * n));
     SMG_TRY(ws.alloc(&part, part_doubles(k)));
     // rr_evolve (src/eigen_evolve.cpp:48-105): M_ij = v_i^dag A v_j, eigenpairs of M, rotated vectors
-    for (int j = 0; j < k; ++j) SMG_TRY(smg_mg_apply1_f64(mg, d.V64 + (int64_t)j * n, AV + (int64_t)j * n));
+    for (int j = 0; j < k; ++j) SMG_TRY(smg_mg_apply_f64(mg, d.level, d.V64 + (int64_t)j * n, AV + (int64_t)j * n));
     for (int j = 0; j < k; ++j) SMG_TRY(multi_dot(ctx, d.V64, n, k, AV + (int64_t)j * n, n, part, M + (int64_t)j * k));
     std::vector<cx<double>> mh((size_t)k * k);
     SMG_CUDA(ctx, cudaMemcpyAsync(mh.data(), M, mh.size() * sizeof(cx<double>), cudaMemcpyDeviceToHost, ctx->stream));

@@ -310,12 +310,24 @@ __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
         const int yp = y + 1 == g.L ? 0 : y + 1, ym = y == 0 ? g.L - 1 : y - 1;
         const int q_xp = op + ((xp + g.L * y) >> 1), q_xm = op + ((xm + g.L * y) >> 1);
         const int q_yp = op + ((x + g.L * yp) >> 1), q_ym = op + ((x + g.L * ym) >> 1);
+        // FP16 input: the stored values are read unscaled and each neighbour's site scale is folded
+        // into its link (and the centre's into the diagonal), the operator being linear in each
         auto ld = [&](int qq, int rr) {
-            return IN_H ? ld_spinor_h(a.src16, a.src_scale, qq, rr, nrhs) : ld_spinor(a.src32, qq, rr, nrhs);
+            return IN_H ? ld_spinor_h_raw(a.src16, qq, rr, nrhs) : ld_spinor(a.src32, qq, rr, nrhs);
         };
-        const cx<float> u0f = a.U[q], u0b = a.U[q_xm], u1f = a.U[g.V + q], u1b = a.U[g.V + q_ym];
+        cx<float> u0f = a.U[q], u0b = a.U[q_xm], u1f = a.U[g.V + q], u1b = a.U[g.V + q_ym];
         const float Cq = a.C ? a.C[q] : 0.f;
-        const cx<float> dg0 = mk(a.diag + Cq, a.mu_eff), dg1 = mk(a.diag - Cq, -a.mu_eff);
+        cx<float> dg0 = mk(a.diag + Cq, a.mu_eff), dg1 = mk(a.diag - Cq, -a.mu_eff);
+        if (IN_H) {
+            const float sq = a.src_scale[q], sxp = a.src_scale[q_xp], sxm = a.src_scale[q_xm];
+            const float syp = a.src_scale[q_yp], sym = a.src_scale[q_ym];
+            u0f = mk(u0f.re * sxp, u0f.im * sxp);
+            u0b = mk(u0b.re * sxm, u0b.im * sxm);
+            u1f = mk(u1f.re * syp, u1f.im * syp);
+            u1b = mk(u1b.re * sym, u1b.im * sym);
+            dg0 = mk(dg0.re * sq, dg0.im * sq);
+            dg1 = mk(dg1.re * sq, dg1.im * sq);
+        }
         Spinor<float> ps[2], pxp[2], pxm[2], pyp[2], pym[2];
 #pragma unroll
         for (int k = 0; k < 2; ++k) {

@@ -31,6 +31,17 @@ __device__ __forceinline__ Spinor<float> ld_spinor_h(const __half2* __restrict__
     return o;
 }
 
+// The stored values of one two-spinor without the site scale (the caller folds the scale into a
+// factor it multiplies by anyway)
+__device__ __forceinline__ Spinor<float> ld_spinor_h_raw(const __half2* __restrict__ f, int64_t q, int rhs, int nrhs) {
+    const Spinor16 h = reinterpret_cast<const Spinor16*>(f)[q * nrhs + rhs];
+    const float2 a = __half22float2(h.s0), b = __half22float2(h.s1);
+    Spinor<float> o;
+    o.s0 = mk(a.x, a.y);
+    o.s1 = mk(b.x, b.y);
+    return o;
+}
+
 // Stores one two-spinor per thread.  The `lanes` threads of a site group (consecutive lanes of one
 // warp with blockDim.x == lanes) cooperate on the site's scale; every thread of the warp must call
 // this (the shuffles span the warp), and `valid` (uniform within a group) says whether to store.

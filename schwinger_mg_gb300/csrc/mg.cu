@@ -1705,7 +1705,7 @@ template <typename T>
 smg_status coarse_cg(smg_mg* mg, int l, void* x, const void* b) {
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[l];
-    if (mg->persistent && mg->work_nrhs == 1 && !(l == 1 && mg->defl.n > 0)) {
+    if (mg->persistent && mg->work_nrhs == 1 && !(l == mg->defl.level && mg->defl.n > 0)) {
         if (L.ndof == 8) return coarse_cg_persistent<T, 8>(mg, l, x, b);
         if (L.ndof == 16) return coarse_cg_persistent<T, 16>(mg, l, x, b);
         if (L.ndof == 32) return coarse_cg_persistent<T, 32>(mg, l, x, b);
@@ -1714,7 +1714,7 @@ smg_status coarse_cg(smg_mg* mg, int l, void* x, const void* b) {
     const int nrhs = mg->work_nrhs;
     VecView<T> xv = cview<T>(x, L, nrhs), pv = cview<T>(w.p, L, nrhs), rv = cview<T>(w.r, L, nrhs);
     const size_t bytes = (size_t)xv.n() * sizeof(cx<T>);
-    const bool deflated = l == 1 && mg->defl.n > 0;
+    const bool deflated = l == mg->defl.level && mg->defl.n > 0;
     double* sc = lvl_scal(mg, l);
     CcgState s;
     s.rr = sc;
@@ -2443,14 +2443,14 @@ MgDeflation& smg_mg_defl(smg_mg* mg) { return mg->defl; }
 smg_context* smg_mg_ctx(smg_mg* mg) { return mg->ctx; }
 smg_dirac* smg_mg_dirac(smg_mg* mg) { return mg->dirac; }
 int smg_mg_nlevels(const smg_mg* mg) { return (int)mg->lv.size(); }
-int64_t smg_mg_level1_dim(const smg_mg* mg) { return (int64_t)mg->lv[1].nsites * mg->lv[1].ndof; }
+int64_t smg_mg_level_dim(const smg_mg* mg, int l) { return (int64_t)mg->lv[l].nsites * mg->lv[l].ndof; }
 void smg_mg_drop_cycle_graph(smg_mg* mg) {
     cudaStreamSynchronize(mg->ctx->stream);
     drop_graph(mg);
 }
 
-smg_status smg_mg_apply1_f64(smg_mg* mg, const cx<double>* x, cx<double>* y) {
-    return coarse_apply<double>(mg, 1, cview<double>((void*)x, mg->lv[1], 1), y, 0, nullptr, nullptr);
+smg_status smg_mg_apply_f64(smg_mg* mg, int l, const cx<double>* x, cx<double>* y) {
+    return coarse_apply<double>(mg, l, cview<double>((void*)x, mg->lv[l], 1), y, 0, nullptr, nullptr);
 }
 
 smg_status smg_mg_restrict0_f64(smg_mg* mg, const smg_field* fine, cx<double>* coarse) {

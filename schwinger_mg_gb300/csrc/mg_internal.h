@@ -6,11 +6,12 @@
 #include "smg_internal.h"
 #include "vec.cuh"
 
-// Eigenpairs of the level-1 operator A_c = P^dag (D^dag D) P (SparseCoarseOp::defl_vecs /
+// Eigenpairs of a coarse operator, by default the level-1 A_c = P^dag (D^dag D) P (SparseCoarseOp::defl_vecs /
 // defl_vals, reference src/coarse_op.h:168-200; CoarseDeflState, src/hmc.h:307-324).  Vectors
 // are level-1 coarse vectors of one right-hand side ([site][dof], sites lexicographic on the
 // coarse lattice, the reference's c[b * k + kv]), stored contiguously one after the other.
 struct MgDeflation {
+    int level = 1;     // the level whose operator the pairs belong to
     int n = 0;         // number of eigenpairs held
     int cap = 0;       // vectors allocated
     int64_t dim = 0;   // complex entries per vector
@@ -40,8 +41,8 @@ MgDeflation& smg_mg_defl(smg_mg* mg);
 smg_context* smg_mg_ctx(smg_mg* mg);
 smg_dirac* smg_mg_dirac(smg_mg* mg);
 int smg_mg_nlevels(const smg_mg* mg);
-int64_t smg_mg_level1_dim(const smg_mg* mg);      // complex entries of a level-1 vector
-smg_status smg_mg_apply1_f64(smg_mg* mg, const cx<double>* x, cx<double>* y);                // A_1 x
+int64_t smg_mg_level_dim(const smg_mg* mg, int l);  // complex entries of a level-l vector (l >= 1)
+smg_status smg_mg_apply_f64(smg_mg* mg, int l, const cx<double>* x, cx<double>* y);          // A_l x
 smg_status smg_mg_restrict0_f64(smg_mg* mg, const smg_field* fine, cx<double>* coarse);      // P^dag f
 smg_status smg_mg_prolong0_f64(smg_mg* mg, const cx<double>* coarse, smg_field* fine);       // P c
 void smg_mg_drop_cycle_graph(smg_mg* mg);  // the captured cycle is re-captured on its next use
