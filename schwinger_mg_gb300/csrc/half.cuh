@@ -50,7 +50,7 @@ __device__ __forceinline__ void st_spinor_h(__half2* __restrict__ f, float* __re
     float m = valid ? fmaxf(fmaxf(fabsf(v.s0.re), fabsf(v.s0.im)), fmaxf(fabsf(v.s1.re), fabsf(v.s1.im))) : 0.f;
     for (int o = lanes >> 1; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o, lanes));
     if (!valid) return;
-    const float inv = m > 0.f ? 1.0f / m : 0.f;
+    const float inv = m > 0.f ? __fdividef(1.0f, m) : 0.f;  // fast reciprocal: FP16 rounding dominates
     Spinor16 h;
     h.s0 = __floats2half2_rn(v.s0.re * inv, v.s0.im * inv);
     h.s1 = __floats2half2_rn(v.s1.re * inv, v.s1.im * inv);
@@ -68,7 +68,7 @@ __device__ __forceinline__ void st_spinor2_h(__half2* __restrict__ f, float* __r
     }
     for (int o = lanes >> 1; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o, lanes));
     if (!valid) return;
-    const float inv = m > 0.f ? 1.0f / m : 0.f;
+    const float inv = m > 0.f ? __fdividef(1.0f, m) : 0.f;  // fast reciprocal: FP16 rounding dominates
     Spinor16 h;
     h.s0 = __floats2half2_rn(v.s0.re * inv, v.s0.im * inv);
     h.s1 = __floats2half2_rn(v.s1.re * inv, v.s1.im * inv);

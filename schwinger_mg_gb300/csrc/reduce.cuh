@@ -67,10 +67,42 @@ __device__ __forceinline__ void block_reduce_finalise(double (&v)[K], double* __
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    // last block: each warp sums four (lane, k) pairs at once, lanes striding over the blocks with
-    // four blocks per pair in flight (16 independent loads per lane); fixed order, deterministic
+    // last block: with at most one (lane, k) pair per warp, one warp per pair with eight loads per
+    // lane in flight (the short tail of few right-hand sides); otherwise each warp sums four pairs
+    // at once with four blocks per pair in flight (16 independent loads per lane); fixed order,
+    // deterministic
     const int npairs = lanes * K;
     const int nb = (int)gridDim.x;
+    if (npairs <= nwarps) {
+        if (warp < npairs) {
+            const int l = warp / K, k = warp - l * K;
+            double a = 0.0;
+            if (rhs0 + l < nrhs) {
+                const double* src = partials + ((size_t)(rhs0 + l) * K + k) * nb;
+                double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+                int b = lane_id;
+                for (; b + 7 * 32 < nb; b += 8 * 32) {
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) acc[u] += __ldcg(src + b + u * 32);
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u)
+                    if (b + u * 32 < nb) acc[u] += __ldcg(src + b + u * 32);
+                a = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+            }
+            for (int off = 16; off >= 1; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+            if (lane_id == 0) s_fin[k][l] = a;
+        }
+        __syncthreads();
+        if (t < lanes && rhs0 + t < nrhs) {
+            double sums[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) sums[k] = s_fin[k][t];
+            fin(rhs0 + t, sums);
+        }
+        if (t == 0) ticket[blockIdx.y] = 0u;
+        return;
+    }
     for (int p0 = warp * 4; p0 < npairs; p0 += nwarps * 4) {
         const double* src[4];
         bool live[4];
