@@ -308,10 +308,12 @@ __device__ __forceinline__ int64_t transfer_idx(const TransferGeom& t, int64_t s
 }
 
 // fine/coarse vector readers for the restriction: plain, or FP16 with per-site scales
+// (spinor() reads both spin components of a level-0 site and right-hand side in one access)
 template <typename T>
 struct InPlain {
     const cx<T>* __restrict__ p;
     __device__ __forceinline__ cx<T> operator()(int64_t idx, int64_t) const { return p[idx]; }
+    __device__ __forceinline__ Spinor<T> spinor(int64_t q, int rhs, int nrhs) const { return ld_spinor(p, q, rhs, nrhs); }
 };
 struct InHalf {
     const __half2* __restrict__ p;
@@ -320,6 +322,9 @@ struct InHalf {
         const float2 v = __half22float2(p[idx]);
         const float s = scale[site];
         return mk(v.x * s, v.y * s);
+    }
+    __device__ __forceinline__ Spinor<float> spinor(int64_t q, int rhs, int nrhs) const {
+        return ld_spinor_h(p, scale, q, rhs, nrhs);
     }
 };
 
@@ -337,11 +342,22 @@ __global__ void __launch_bounds__(256) k_restrict_agg(const cx<T>* __restrict__ 
     cx<T>* s_v = s_f + (int64_t)ne * lanes;        // [ne][NC]
     const int rhs = blockIdx.y * lanes + threadIdx.x;
     const bool live = rhs < nrhs;
+    if (t.level0) {  // both spins of a site in one access
+#pragma unroll 2
+        for (int loc = threadIdx.y; loc < m; loc += rows) {
+            Spinor<T> f;
+            f.s0 = f.s1 = mk<T>(0, 0);
+            if (live) f = in.spinor(transfer_site(t, B, loc), rhs, nrhs);
+            s_f[(2 * loc) * lanes + threadIdx.x] = f.s0;
+            s_f[(2 * loc + 1) * lanes + threadIdx.x] = f.s1;
+        }
+    } else {
 #pragma unroll 4
-    for (int e = threadIdx.y; e < ne; e += rows) {
-        const int loc = e / nd, j = e - loc * nd;
-        const int64_t s = transfer_site(t, B, loc);
-        s_f[e * lanes + threadIdx.x] = live ? in(transfer_idx(t, s, j, rhs), s) : mk<T>(0, 0);
+        for (int e = threadIdx.y; e < ne; e += rows) {
+            const int loc = e / nd, j = e - loc * nd;
+            const int64_t s = transfer_site(t, B, loc);
+            s_f[e * lanes + threadIdx.x] = live ? in(transfer_idx(t, s, j, rhs), s) : mk<T>(0, 0);
+        }
     }
     const cx<T>* __restrict__ Vb = V + (int64_t)B * ne * NC;
     for (int k = threadIdx.y * lanes + threadIdx.x; k < ne * NC; k += lanes * rows) s_v[k] = Vb[k];
@@ -361,13 +377,51 @@ __global__ void __launch_bounds__(256) k_prolong_agg(const cx<T>* __restrict__ V
     extern __shared__ unsigned char s_raw[];
     const int lanes = blockDim.x, rows = blockDim.y;
     const int B = blockIdx.x, m = t.ax * t.ay, nd = t.ndof, nrhs = t.nrhs, ne = m * nd;
-    cx<T>* s_c = reinterpret_cast<cx<T>*>(s_raw);  // [NC][lanes]
+    cx<T>* s_c = reinterpret_cast<cx<T>*>(s_raw);  // [NC][lanes] (coarse levels)
     cx<T>* s_v = s_c + NC * lanes;                 // [ne][NC]
     const int rhs = blockIdx.y * lanes + threadIdx.x;
     const bool live = rhs < nrhs;
+    const cx<T>* __restrict__ Vb = V + (int64_t)B * ne * NC;
+    if (t.level0) {
+        // the NC coarse values of this thread's rhs in registers, the block vectors in shared memory;
+        // one fine site (both spins, one 2-spinor access) per step, two sites' previous values
+        // requested before any arithmetic
+        cx<T> c[NC];
+#pragma unroll
+        for (int i = 0; i < NC; ++i) c[i] = live ? cin[((int64_t)B * NC + i) * nrhs + rhs] : mk<T>(0, 0);
+        for (int k = threadIdx.y * lanes + threadIdx.x; k < ne * NC; k += lanes * rows) s_v[k] = Vb[k];
+        __syncthreads();
+        if (!live) return;
+        for (int l0 = threadIdx.y; l0 < m; l0 += 2 * rows) {
+            const int l1 = l0 + rows;
+            const int64_t q0 = transfer_site(t, B, l0), q1 = l1 < m ? transfer_site(t, B, l1) : 0;
+            Spinor<T> p0, p1;
+            p0.s0 = p0.s1 = p1.s0 = p1.s1 = mk<T>(0, 0);
+            if (accumulate) {
+                p0 = ld_spinor(out, q0, rhs, nrhs);
+                if (l1 < m) p1 = ld_spinor(out, q1, rhs, nrhs);
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int loc = h ? l1 : l0;
+                if (loc >= m) break;
+                cx<T> a0 = mk<T>(0, 0), a1 = mk<T>(0, 0);
+#pragma unroll
+                for (int i = 0; i < NC; ++i) {
+                    a0 = a0 + s_v[(2 * loc) * NC + i] * c[i];
+                    a1 = a1 + s_v[(2 * loc + 1) * NC + i] * c[i];
+                }
+                const Spinor<T>& pv = h ? p1 : p0;
+                Spinor<T> o;
+                o.s0 = accumulate ? pv.s0 + a0 : a0;
+                o.s1 = accumulate ? pv.s1 + a1 : a1;
+                st_spinor(out, h ? q1 : q0, rhs, nrhs, o);
+            }
+        }
+        return;
+    }
     for (int i = threadIdx.y; i < NC; i += rows)
         s_c[i * lanes + threadIdx.x] = live ? cin[((int64_t)B * NC + i) * nrhs + rhs] : mk<T>(0, 0);
-    const cx<T>* __restrict__ Vb = V + (int64_t)B * ne * NC;
     for (int k = threadIdx.y * lanes + threadIdx.x; k < ne * NC; k += lanes * rows) s_v[k] = Vb[k];
     __syncthreads();
     if (!live) return;

@@ -140,3 +140,27 @@ def test_multiscale_bad_arguments(smg_gpu, ms):
     p.n_inner = 0
     with pytest.raises(smg_gpu.SmgError):
         smg_gpu.hmc_mg_multiscale(g, 0.1, 1.0, p, mg, smg_gpu.Rng(1))
+
+
+def test_deflation_of_the_coarsest_level(smg_gpu):
+    """Eigenpairs of a deeper level's operator (level 2 of three), and the cycle with the coarsest CG
+    started from their deflated guess equals the undeflated cycle when the coarsest CG converges."""
+    L = 32
+    lat = smg_gpu.Lattice(L)
+    g = smg_gpu.GaugeField(lat, smg_gpu.gauge_normal(L, 3.0, 401))
+    D = smg_gpu.DiracOp(lat, g, 0.1, 1.0, 1.0, 0.0)
+    p = smg_gpu.mg_params(3, 4, 4, blocks=[(4, 4), (2, 2)], null_iters=3, coarse_tol=1e-13, coarse_max_iter=2000,
+                          seed=9)
+    mg = smg_gpu.MGHierarchy(D, p)
+    src = smg_gpu.random_vec(lat.ndof, 17)
+    plain = mg.precondition(src)
+    info = mg.setup_deflation(6, level=2)
+    assert info.converged
+    vals, vecs = mg.deflation
+    assert vecs.shape == (6, mg.level_dim(2))
+    for v, lam in zip(vecs, vals):
+        assert np.linalg.norm(mg.coarse_apply(2, v) - lam * v) < 1e-8 * lam
+    defl = mg.precondition(src)
+    assert np.linalg.norm(defl - plain) / np.linalg.norm(plain) < 1e-9
+    with pytest.raises(smg_gpu.SmgError):  # the low-mode solution needs a level-1 space
+        mg.lowmode_solution(src)
