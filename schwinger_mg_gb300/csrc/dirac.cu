@@ -285,8 +285,10 @@ struct DslashH {
     float* __restrict__ part = nullptr;
 };
 
-// thread = right-hand sides rhs and rhs + lanes (lanes = nrhs / 2) of one site
-template <bool DAG, bool IN_H, bool OUT_H, bool R1, bool DOTS = false>
+// thread = right-hand sides rhs + k * lanes (k < NR, lanes = nrhs / NR) of one site: the site's
+// index arithmetic, link, clover and scale loads and the scale folding are shared by its NR
+// right-hand sides, which are processed two at a time
+template <bool DAG, bool IN_H, bool OUT_H, bool R1, bool DOTS = false, int NR = 2>
 __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
     const Geom g = a.g;
     const int nrhs = a.nrhs, lanes = blockDim.x;
@@ -297,9 +299,9 @@ __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
     const int p = rem >= g.Lh ? 1 : 0;
     const int xh = rem - p * g.Lh;
     const int q = p * g.Vh + y * g.Lh + xh;
-    Spinor<float> out[2];
+    Spinor<float> out[NR];
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < NR; ++k) {
         out[k].s0 = mk(0.f, 0.f);
         out[k].s1 = mk(0.f, 0.f);
     }
@@ -328,31 +330,36 @@ __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
             dg0 = mk(dg0.re * sq, dg0.im * sq);
             dg1 = mk(dg1.re * sq, dg1.im * sq);
         }
-        Spinor<float> ps[2], pxp[2], pxm[2], pyp[2], pym[2];
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
-            const int rr = rhs + k * lanes;
-            ps[k] = ld(q, rr);
-            pxp[k] = ld(q_xp, rr);
-            pxm[k] = ld(q_xm, rr);
-            pyp[k] = ld(q_yp, rr);
-            pym[k] = ld(q_ym, rr);
-        }
+        for (int k0 = 0; k0 < NR; k0 += 2) {
+            Spinor<float> ps[2], pxp[2], pxm[2], pyp[2], pym[2];
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
-            cx<float> S0, S1;
-            hop_sum<float, DAG, R1>(u0f, u0b, u1f, u1b, pxp[k], pxm[k], pyp[k], pym[k], a.r, S0, S1);
-            out[k].s0 = dg0 * ps[k].s0 - 0.5f * S0;
-            out[k].s1 = dg1 * ps[k].s1 - 0.5f * S1;
+            for (int k = 0; k < 2; ++k) {
+                const int rr = rhs + (k0 + k) * lanes;
+                ps[k] = ld(q, rr);
+                pxp[k] = ld(q_xp, rr);
+                pxm[k] = ld(q_xm, rr);
+                pyp[k] = ld(q_yp, rr);
+                pym[k] = ld(q_ym, rr);
+            }
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                cx<float> S0, S1;
+                hop_sum<float, DAG, R1>(u0f, u0b, u1f, u1b, pxp[k], pxm[k], pyp[k], pym[k], a.r, S0, S1);
+                out[k0 + k].s0 = dg0 * ps[k].s0 - 0.5f * S0;
+                out[k0 + k].s1 = dg1 * ps[k].s1 - 0.5f * S1;
+            }
         }
     }
     if (DOTS) {
         // <out, w> and ||out||^2 of this block's sites, per rhs, summed over the block's rows in a fixed order
-        __shared__ float s_d[256 * 6];
-        float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        __shared__ float s_d[256 * 3 * NR];
+        float v[3 * NR];
+#pragma unroll
+        for (int k = 0; k < 3 * NR; ++k) v[k] = 0.f;
         if (valid) {
 #pragma unroll
-            for (int k = 0; k < 2; ++k) {
+            for (int k = 0; k < NR; ++k) {
                 const Spinor<float> wv = ld_spinor_h(a.w16, a.w_scale, q, rhs + k * lanes, nrhs);
                 const cx<float> c = cmulc(out[k].s0, wv.s0) + cmulc(out[k].s1, wv.s1);
                 v[3 * k] = c.re;
@@ -362,29 +369,36 @@ __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
         }
         const int t = threadIdx.y * lanes + rhs;
 #pragma unroll
-        for (int k = 0; k < 6; ++k) s_d[k * 256 + t] = v[k];
+        for (int k = 0; k < 3 * NR; ++k) s_d[k * 256 + t] = v[k];
         __syncthreads();
         if (threadIdx.y == 0) {
-            float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            float acc[3 * NR];
+#pragma unroll
+            for (int k = 0; k < 3 * NR; ++k) acc[k] = 0.f;
             for (int row = 0; row < (int)blockDim.y; ++row)
 #pragma unroll
-                for (int k = 0; k < 6; ++k) acc[k] += s_d[k * 256 + row * lanes + rhs];
-            float* p = a.part + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * nrhs * 3;
+                for (int k = 0; k < 3 * NR; ++k) acc[k] += s_d[k * 256 + row * lanes + rhs];
+            float* pp = a.part + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * nrhs * 3;
 #pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                p[3 * (rhs + k * lanes)] = acc[3 * k];
-                p[3 * (rhs + k * lanes) + 1] = acc[3 * k + 1];
-                p[3 * (rhs + k * lanes) + 2] = acc[3 * k + 2];
+            for (int k = 0; k < NR; ++k) {
+                pp[3 * (rhs + k * lanes)] = acc[3 * k];
+                pp[3 * (rhs + k * lanes) + 1] = acc[3 * k + 1];
+                pp[3 * (rhs + k * lanes) + 2] = acc[3 * k + 2];
             }
         }
     }
     if (OUT_H) {
-        st_spinor2_h(a.dst16, a.dst_scale, q, rhs, nrhs, lanes, out[0], out[1], valid);
+        st_spinorN_h<NR>(a.dst16, a.dst_scale, q, rhs, nrhs, lanes, out, valid);
     } else if (valid) {
-        st_spinor(a.dst32, q, rhs, nrhs, out[0]);
-        st_spinor(a.dst32, q, rhs + lanes, nrhs, out[1]);
+#pragma unroll
+        for (int k = 0; k < NR; ++k) st_spinor(a.dst32, q, rhs + k * lanes, nrhs, out[k]);
     }
 }
+
+// right-hand sides per thread of the FP16 stencil launches: two.  Four per thread (NR = 4) were
+// measured at L = 512, 32 RHS: the plain stencil unchanged (57.0 against 57.2 us), the one with the
+// fused MR reductions slower (95 against 81 us, more registers and shared memory per block).
+int dslash_h_nr(int) { return 2; }
 
 // Sums of the stencil blocks' partials part[block][j] (j = rhs * 3 + k < ncol <= 96) in FP64 and a
 // fixed order, in two passes: block g of the first sums the contiguous rows [g R, g R + R) with
@@ -461,12 +475,12 @@ smg_status launch_dslash_h(smg_dirac* d, bool dag, const smg_field* src, smg_fie
     a.diag = (float)(2.0 * d->r + d->mass);
     a.mu_eff = (float)(dag ? -d->mu_t : d->mu_t);
     a.r = (float)d->r;
-    const int lanes = nrhs / 2, rows = 256 / lanes;
+    const int nr = dslash_h_nr(nrhs), lanes = nrhs / nr, rows = 256 / lanes;
     const dim3 block(lanes, rows), grid((a.g.L + rows - 1) / rows, a.g.L);
-#define SMG_DH(DG, I, O)                                                          \
-    do {                                                                          \
-        if (d->r == 1.0) k_dslash_h<DG, I, O, true><<<grid, block, 0, ctx->stream>>>(a);  \
-        else k_dslash_h<DG, I, O, false><<<grid, block, 0, ctx->stream>>>(a);            \
+#define SMG_DH(DG, I, O)                                                                     \
+    do {                                                                                     \
+        if (d->r == 1.0) k_dslash_h<DG, I, O, true><<<grid, block, 0, ctx->stream>>>(a);   \
+        else k_dslash_h<DG, I, O, false><<<grid, block, 0, ctx->stream>>>(a);             \
     } while (0)
     if (dag) {
         if (ih && oh) SMG_DH(true, true, true);
@@ -485,7 +499,7 @@ smg_status launch_dslash_h(smg_dirac* d, bool dag, const smg_field* src, smg_fie
 
 // blocks of the FP16 stencil's grid (the size of the partial-sum buffer of the fused dot/norm)
 int dslash_h_blocks(int L, int nrhs) {
-    const int rows = 256 / (nrhs / 2);
+    const int rows = 256 / (nrhs / dslash_h_nr(nrhs));
     return ((L + rows - 1) / rows) * L;
 }
 
@@ -513,7 +527,7 @@ smg_status launch_dslash_h_dots(smg_dirac* d, const smg_field* src, smg_field* d
     a.diag = (float)(2.0 * d->r + d->mass);
     a.mu_eff = (float)(-d->mu_t);
     a.r = (float)d->r;
-    const int lanes = nrhs / 2, rows = 256 / lanes;
+    const int nr = dslash_h_nr(nrhs), lanes = nrhs / nr, rows = 256 / lanes;
     const dim3 block(lanes, rows), grid((a.g.L + rows - 1) / rows, a.g.L);
     if (d->r == 1.0)
         k_dslash_h<true, true, true, true, true><<<grid, block, 0, ctx->stream>>>(a);

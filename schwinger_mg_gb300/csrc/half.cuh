@@ -79,5 +79,28 @@ __device__ __forceinline__ void st_spinor2_h(__half2* __restrict__ f, float* __r
     if ((threadIdx.x & (lanes - 1)) == 0) scale[q] = m;
 }
 
+// NR spinors per thread (right-hand sides rhs + k * lanes, k < NR), same contract as above.
+template <int NR>
+__device__ __forceinline__ void st_spinorN_h(__half2* __restrict__ f, float* __restrict__ scale, int64_t q, int rhs,
+                                             int nrhs, int lanes, const Spinor<float> (&v)[NR], bool valid) {
+    float m = 0.f;
+    if (valid) {
+#pragma unroll
+        for (int k = 0; k < NR; ++k)
+            m = fmaxf(m, fmaxf(fmaxf(fabsf(v[k].s0.re), fabsf(v[k].s0.im)), fmaxf(fabsf(v[k].s1.re), fabsf(v[k].s1.im))));
+    }
+    for (int o = lanes >> 1; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o, lanes));
+    if (!valid) return;
+    const float inv = m > 0.f ? __fdividef(1.0f, m) : 0.f;  // fast reciprocal: FP16 rounding dominates
+#pragma unroll
+    for (int k = 0; k < NR; ++k) {
+        Spinor16 h;
+        h.s0 = __floats2half2_rn(v[k].s0.re * inv, v[k].s0.im * inv);
+        h.s1 = __floats2half2_rn(v[k].s1.re * inv, v[k].s1.im * inv);
+        reinterpret_cast<Spinor16*>(f)[q * nrhs + rhs + k * lanes] = h;
+    }
+    if ((threadIdx.x & (lanes - 1)) == 0) scale[q] = m;
+}
+
 // nrhs values whose sites can be written as F16 (one site per power-of-two lane group)
 inline bool f16_nrhs_ok(int nrhs) { return nrhs >= 1 && nrhs <= 32 && (nrhs & (nrhs - 1)) == 0; }
