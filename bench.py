@@ -490,6 +490,8 @@ def run_ours(args, ws, rank, local):
             c["nrhs"] = args.nrhs
         if args.L:
             c["n_lat"] = args.L  # --L N: the first N lattices of the batch (a small case)
+        if args.workers:
+            c["workers"] = args.workers
         lats_all = batch_lattices(c)
         lats = shard(lats_all, rank, ws)  # several GPUs: the 64 lattices are split across the ranks
         nrhs = c["nrhs"]
@@ -808,6 +810,7 @@ def main():
                     help="mg workload: precision of the fine smoother's work vectors (f16: per-site scaled FP16)")
     ap.add_argument("--trunc", type=int, default=0, help="mg / batch workloads: GCR truncation override")
     ap.add_argument("--coarse-iters", type=int, default=0, help="mg / batch workloads: coarsest-CG iteration cap override")
+    ap.add_argument("--workers", type=int, default=0, help="batch workload: host worker threads override")
     ap.add_argument("--dslash-prec", default="f32", choices=["f32", "f16"],
                     help="dslash workload: field precision (f16 = FP16 storage with per-site scales)")
     ap.add_argument("--coarse-defl", type=int, default=0,

@@ -49,6 +49,7 @@
 // frees its tensor memory and returns.
 #include <cuda_bf16.h>
 
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -610,6 +611,17 @@ smg_status smg_coarse_tc_tune(smg_context* ctx, const void* links, int nx, int n
     {
         std::lock_guard<std::mutex> lock(g_rows_mu);
         if (g_rows.count(key)) return SMG_OK;
+    }
+    // SMG_TC_ROWS=<H> fixes the rows per CTA for every shape it divides (for measurements, e.g. under a
+    // profiler whose replay distorts the timing)
+    if (const char* e = std::getenv("SMG_TC_ROWS")) {
+        const int H = std::atoi(e);
+        if (H > 0 && ny % H == 0) {
+            SMG_TRY(smg_reduce_reserve(ctx, (size_t)(nx / kW) * (ny / H) * nrhs * 3));
+            std::lock_guard<std::mutex> lock(g_rows_mu);
+            g_rows[key] = H;
+            return SMG_OK;
+        }
     }
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     SMG_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cs));
