@@ -18,6 +18,8 @@
 //   MGHierarchy::setup_deflation / deflation / deflation_rr / lowmode_solution
 //                                           src/coarse_op.cpp:10-54, src/eigen_evolve.cpp:48, src/hmc.h:307
 //   coarse_lowmode_force                    src/hmc_multiscale.cpp:237-276
+//   hmc_trajectory, reversibility_test_plain, hmc_trajectory_mg_multiscale,
+//   reversibility_test_mg_multiscale        src/hmc_trajectory.cpp:38-509, src/hmc_multiscale.cpp:340-1000
 //   fermion_action(_precond) + fermion_force as a forward/backward pair
 //                                           src/hmc.h (FermionActionResult)
 // Host vectors keep the reference layout (Vec v[2*s + spin]); each call copies
@@ -106,6 +108,14 @@ class GaugeField {
         double v = 0;
         check(smg_gauge_avg_plaq(handle(), &v), default_context(), "smg_gauge_avg_plaq");
         return v;
+    }
+    // Copies the device links into the host copy U (after a device-side update such as an HMC step).
+    void pull() {
+        std::vector<double> flat(4 * (size_t)lat.V);
+        check(smg_gauge_get(handle(), flat.data()), default_context(), "smg_gauge_get");
+        for (int mu = 0; mu < 2; ++mu)
+            for (int s = 0; s < lat.V; ++s)
+                U[mu][s] = cx(flat[2 * ((size_t)mu * lat.V + s)], flat[2 * ((size_t)mu * lat.V + s) + 1]);
     }
 
    private:
@@ -450,6 +460,58 @@ inline double gauge_action(const GaugeField& g, double beta) {
     double v = 0;
     check(smg_gauge_action(g.handle(), beta, &v), default_context(), "smg_gauge_action");
     return v;
+}
+
+// std::mt19937 with the reference's distributions, owned by the library (momenta, eta, Metropolis)
+class Rng {
+   public:
+    explicit Rng(uint32_t seed) {
+        smg_rng* r = nullptr;
+        check(smg_rng_create(seed, &r), default_context(), "smg_rng_create");
+        h_.reset(r);
+    }
+    smg_rng* get() const { return h_.get(); }
+
+   private:
+    std::unique_ptr<smg_rng, smg_status (*)(smg_rng*)> h_{nullptr, &smg_rng_destroy};
+};
+
+// hmc_trajectory (src/hmc_trajectory.cpp:38-235) on the device; g.U follows the device links
+inline smg_hmc_result hmc_trajectory(GaugeField& g, double mass, double wilson_r, const smg_hmc_params& p, Rng& rng) {
+    smg_hmc_result res{};
+    check(smg_hmc_trajectory(g.handle(), mass, wilson_r, &p, rng.get(), &res), default_context(),
+          "smg_hmc_trajectory");
+    g.pull();
+    return res;
+}
+
+// reversibility_test_plain (src/hmc_trajectory.cpp:416-509); the links are restored
+inline smg_reversibility_result reversibility_test_plain(GaugeField& g, double mass, double wilson_r,
+                                                         const smg_hmc_params& p, Rng& rng) {
+    smg_reversibility_result res{};
+    check(smg_hmc_reversibility(g.handle(), mass, wilson_r, &p, rng.get(), &res), default_context(),
+          "smg_hmc_reversibility");
+    return res;
+}
+
+// hmc_trajectory_mg_multiscale (src/hmc_multiscale.cpp:340-886): mg supplies the preconditioner, the
+// prolongator and the deflation space and must be built on a DiracOp over g
+inline smg_ms_result hmc_trajectory_mg_multiscale(GaugeField& g, double mass, double wilson_r,
+                                                  const smg_ms_params& p, MGHierarchy& mg, Rng& rng) {
+    smg_ms_result res{};
+    check(smg_hmc_mg_multiscale(g.handle(), mass, wilson_r, &p, mg.handle(), rng.get(), &res), default_context(),
+          "smg_hmc_mg_multiscale");
+    g.pull();
+    return res;
+}
+
+// reversibility_test_mg_multiscale (src/hmc_multiscale.cpp:963-1000); the links are restored
+inline smg_reversibility_result reversibility_test_mg_multiscale(GaugeField& g, double mass, double wilson_r,
+                                                                 const smg_ms_params& p, MGHierarchy& mg, Rng& rng) {
+    smg_reversibility_result res{};
+    check(smg_hmc_mg_multiscale_reversibility(g.handle(), mass, wilson_r, &p, mg.handle(), rng.get(), &res),
+          default_context(), "smg_hmc_mg_multiscale_reversibility");
+    return res;
 }
 
 }  // namespace smg
