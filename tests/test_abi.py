@@ -105,6 +105,19 @@ def test_cpp_dropin_header_compiles(tmp_path):
         "    std::array<smg::RVec, 2> F;\n"
         "    act.backward(F);\n"
         "    return S + c.final_residual + f.final_residual + F[0][0];\n"
+        "}\n"
+        "double use_hmc(smg::GaugeField& g, smg::DiracOp& D, smg::MGHierarchy& mg, const smg::Vec& phi) {\n"
+        "    smg_hmc_params hp; smg_hmc_params_default(&hp);\n"
+        "    smg_ms_params mp; smg_ms_params_default(&mp);\n"
+        "    smg::Rng rng(1);\n"
+        "    auto t = smg::hmc_trajectory(g, 0.1, 1.0, hp, rng);\n"
+        "    auto r = smg::reversibility_test_plain(g, 0.1, 1.0, hp, rng);\n"
+        "    D.refresh(); mg.rebuild(); mg.setup_deflation(4); double rr = mg.deflation_rr();\n"
+        "    smg::Vec low = mg.lowmode_solution(phi);\n"
+        "    std::array<smg::RVec, 2> F; smg::coarse_lowmode_force(D, mg, phi, F, 3);\n"
+        "    auto m = smg::hmc_trajectory_mg_multiscale(g, 0.1, 1.0, mp, mg, rng);\n"
+        "    auto mr = smg::reversibility_test_mg_multiscale(g, 0.1, 1.0, mp, mg, rng);\n"
+        "    return t.dH + r.dH_forward + rr + low[0].real() + F[0][0] + m.dH + mr.dH_forward;\n"
         "}\n")
     r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-I", str(ROOT / "include"), str(src)],
                        capture_output=True, text=True)
