@@ -660,6 +660,33 @@ SMG_API smg_status smg_hmc_mg_multiscale_reversibility(smg_gauge* g, double mass
                                                        const smg_ms_params* p, smg_mg* mg, smg_rng* rng,
                                                        smg_reversibility_result* res);
 
+/* --------------------------------------------------- force verification */
+
+#define SMG_VERIFY_LINKS 20
+
+/* Outcome of smg_verify_forces: per tested link (mu, site) the analytic and
+ * finite-difference gauge and fermion forces, and the maxima the reference
+ * prints (max |ana - num| and that over max |ana|). */
+typedef struct {
+    int passed, gauge_passed, fermion_passed;
+    double gauge_max_err, gauge_rel, fermion_max_err, fermion_rel;
+    int n_links;
+    int mu[SMG_VERIFY_LINKS], site[SMG_VERIFY_LINKS];
+    double gf_ana[SMG_VERIFY_LINKS], gf_num[SMG_VERIFY_LINKS];
+    double ff_ana[SMG_VERIFY_LINKS], ff_num[SMG_VERIFY_LINKS];
+} smg_force_check;
+
+/* verify_forces (reference src/hmc_forces.cpp:869-981): the device's gauge
+ * force and pseudofermion force (full D^dag D or, with use_eo, the Schur
+ * complement with -2 log det D_ee) against central differences (eps = 1e-5)
+ * of the actions at the reference's 20 links (mu = t % 2,
+ * s = (7 t + 13 (t / 2)) % V), with its pseudofermion (random_vec from
+ * std::mt19937(12345)); passes when both relative errors are below
+ * err_threshold (the reference's callers use 1e-4). */
+SMG_API smg_status smg_verify_forces(smg_gauge* g, double beta, double mass, double wilson_r, int max_iter,
+                                     double tol, double c_sw, int use_eo, double err_threshold, double mu_t,
+                                     smg_force_check* out);
+
 /* ------------------------------------------------------------ gauge files */
 
 /* GaugeHeader (reference src/hmc.h:19-25): the 32-byte header of the "SWNG"

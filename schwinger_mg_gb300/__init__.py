@@ -28,6 +28,7 @@ from .api import (  # noqa: F401
     ms_params,
     MSResult,
     coarse_lowmode_force,
+    verify_forces,
     hmc_trajectory,
     MGHierarchy,
     build_full_mg,

@@ -82,6 +82,15 @@ class MSResult(C.Structure):
                 ("solves", C.c_int), ("plaquette", C.c_double)]
 
 
+class ForceCheck(C.Structure):
+    """smg_force_check (include/smg_gpu.h)."""
+    _fields_ = [("passed", C.c_int), ("gauge_passed", C.c_int), ("fermion_passed", C.c_int),
+                ("gauge_max_err", C.c_double), ("gauge_rel", C.c_double), ("fermion_max_err", C.c_double),
+                ("fermion_rel", C.c_double), ("n_links", C.c_int), ("mu", C.c_int * 20), ("site", C.c_int * 20),
+                ("gf_ana", C.c_double * 20), ("gf_num", C.c_double * 20), ("ff_ana", C.c_double * 20),
+                ("ff_num", C.c_double * 20)]
+
+
 class MGParams(C.Structure):
     """smg_mg_params (include/smg_gpu.h)."""
     _fields_ = [("n_levels", C.c_int), ("block", (C.c_int * 2) * (MAX_LEVELS - 1)),
@@ -169,6 +178,8 @@ _SIGS = {
     "smg_richardson_smooth": (_st, [_vp, _vp, _vp, C.c_int, C.c_double]),
     "smg_estimate_lambda_max": (_st, [_vp, C.c_int, _dp]),
     "smg_mg_rebuild": (_st, [_vp]),
+    "smg_verify_forces": (_st, [_vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double, C.c_int,
+                                C.c_double, C.c_double, C.POINTER(ForceCheck)]),
     "smg_mg_setup_deflation": (_st, [_vp, C.c_int, C.c_int, C.c_int, C.c_double, C.POINTER(DeflationInfo)]),
     "smg_mg_setup_deflation_level": (_st, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double,
                                            C.POINTER(DeflationInfo)]),

@@ -595,6 +595,18 @@ def coarse_lowmode_force(D: DiracOp, mg: MGHierarchy, phi, smooth_iters: int = 0
     return out.reshape(2, D.lat.V)
 
 
+def verify_forces(g: GaugeField, beta: float, mass: float, wilson_r: float = 1.0, max_iter: int = 10000,
+                  tol: float = 1e-12, c_sw: float = 0.0, use_eo: bool = False, err_threshold: float = 1e-4,
+                  mu_t: float = 0.0) -> _L.ForceCheck:
+    """verify_forces (reference src/hmc_forces.cpp:869-981) on the device: analytic gauge and
+    fermion forces against central differences at the reference's 20 links; `.passed` is its
+    return value, the per-link values are in gf_ana/gf_num/ff_ana/ff_num."""
+    out = _L.ForceCheck()
+    _L.check(_L.lib().smg_verify_forces(g.h, beta, mass, wilson_r, max_iter, tol, c_sw, int(use_eo), err_threshold,
+                                        mu_t, C.byref(out)), "smg_verify_forces", g.ctx.h)
+    return out
+
+
 OUTER_INTEGRATORS = {"leapfrog": 0, "omelyan": 1, "fgi": 2, "fgi_qpqpq": 3}
 
 

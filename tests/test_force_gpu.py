@@ -111,3 +111,23 @@ def test_force_finite_differences_L128_64_links(smg_gpu):
         fd = -(delta_S(Up) - delta_S(Um)) / (2 * eps)
         rel.append(abs(F[mu, s] - fd) / abs(F[mu, s]))
     assert max(rel) < 1e-7, f"force vs finite differences at L=128: max rel {max(rel):.3e}"
+
+
+@pytest.mark.parametrize("L,csw,use_eo,mu", [(8, 1.0, False, 0.0), (16, 1.0, True, 0.0), (16, 1.0, False, 0.1)])
+def test_verify_forces_passes(smg_gpu, L, csw, use_eo, mu):
+    """verify_forces (src/hmc_forces.cpp:869-981): the device forces against central differences at the
+    reference's 20 links; the analytic values are the device force at those links."""
+    lat = smg_gpu.Lattice(L)
+    U = smg_gpu.gauge_normal(L, 4.0, 31 + L)
+    g = smg_gpu.GaugeField(lat, U)
+    chk = smg_gpu.verify_forces(g, 4.0, 0.1, 1.0, c_sw=csw, use_eo=use_eo, mu_t=mu)
+    assert chk.passed and chk.n_links == 20
+    assert chk.fermion_rel < 1e-4 and chk.gauge_rel < 1e-6
+    V = L * L
+    for t in range(20):
+        assert chk.mu[t] == t % 2 and chk.site[t] == (7 * t + 13 * (t // 2)) % V
+    gf = smg_gpu.gauge_force(g, 4.0)
+    assert all(abs(chk.gf_ana[t] - gf[chk.mu[t], chk.site[t]]) < 1e-14 * max(1.0, abs(gf[chk.mu[t], chk.site[t]]))
+               for t in range(20))
+    # the links are untouched
+    assert np.max(np.abs(g.U.reshape(-1) - U.reshape(-1))) == 0.0
