@@ -18,6 +18,7 @@
 //   MGHierarchy::setup_deflation / deflation / deflation_rr / lowmode_solution
 //                                           src/coarse_op.cpp:10-54, src/eigen_evolve.cpp:48, src/hmc.h:307
 //   coarse_lowmode_force                    src/hmc_multiscale.cpp:237-276
+//   verify_forces                           src/hmc_forces.cpp:869-981
 //   hmc_trajectory, reversibility_test_plain, hmc_trajectory_mg_multiscale,
 //   reversibility_test_mg_multiscale        src/hmc_trajectory.cpp:38-509, src/hmc_multiscale.cpp:340-1000
 //   fermion_action(_precond) + fermion_force as a forward/backward pair
@@ -460,6 +461,18 @@ inline double gauge_action(const GaugeField& g, double beta) {
     double v = 0;
     check(smg_gauge_action(g.handle(), beta, &v), default_context(), "smg_gauge_action");
     return v;
+}
+
+// verify_forces (src/hmc_forces.cpp:869-981): true when both forces pass; details in *check
+inline bool verify_forces(const GaugeField& g, double beta, double mass, double wilson_r, int max_iter, double tol,
+                          double c_sw = 0.0, bool use_eo = false, double err_threshold = 1e-4, double mu_t = 0.0,
+                          smg_force_check* check_out = nullptr) {
+    smg_force_check c{};
+    check(smg_verify_forces(g.handle(), beta, mass, wilson_r, max_iter, tol, c_sw, use_eo ? 1 : 0, err_threshold,
+                            mu_t, &c),
+          default_context(), "smg_verify_forces");
+    if (check_out) *check_out = c;
+    return c.passed != 0;
 }
 
 // std::mt19937 with the reference's distributions, owned by the library (momenta, eta, Metropolis)

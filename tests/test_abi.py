@@ -117,7 +117,8 @@ def test_cpp_dropin_header_compiles(tmp_path):
         "    std::array<smg::RVec, 2> F; smg::coarse_lowmode_force(D, mg, phi, F, 3);\n"
         "    auto m = smg::hmc_trajectory_mg_multiscale(g, 0.1, 1.0, mp, mg, rng);\n"
         "    auto mr = smg::reversibility_test_mg_multiscale(g, 0.1, 1.0, mp, mg, rng);\n"
-        "    return t.dH + r.dH_forward + rr + low[0].real() + F[0][0] + m.dH + mr.dH_forward;\n"
+        "    bool ok = smg::verify_forces(g, 4.0, 0.1, 1.0, 1000, 1e-12, 1.0, true);\n"
+        "    return t.dH + r.dH_forward + rr + low[0].real() + F[0][0] + m.dH + mr.dH_forward + (ok ? 1 : 0);\n"
         "}\n")
     r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-I", str(ROOT / "include"), str(src)],
                        capture_output=True, text=True)
