@@ -663,8 +663,6 @@ smg_status smg_coarse_tc_tune(smg_context* ctx, const void* links, int nx, int n
     return SMG_OK;
 }
 
-int smg_coarse_tc_rows(int nx, int ny, int nrhs) { return rows_per_cta(nx, ny, nrhs / kRhsTile); }
-
 namespace {
 
 smg_status launch_tc(smg_context* ctx, const void* links, int nx, int ny, int nrhs, int H, const cx<float>* x,
