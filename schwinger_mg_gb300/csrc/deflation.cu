@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(256) k_mdot(const cx<double>* __restrict__ K, 
     }
 }
 
-// out[k] = sum over blocks; scale > 0 multiplies (used for nothing but 1 here)
+// out[k] = the sum of the per-block partials of <K_k, r> (fixed order)
 __global__ void k_mdot_finish(const double* __restrict__ part, int G, int m, cx<double>* __restrict__ out) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 2 * m) return;
