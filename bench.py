@@ -1,7 +1,7 @@
 """Benchmark of the Wilson-clover Dirac operator and its MG solve path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload mg|dslash|cg|coarse|hmc|batch]
-                    [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W]
+                    [--workload mg|mg2|dslash|smoother|cg|coarse|hmc|batch] [--impl ours|reference]
 
 Prints ONE JSON line (rank 0).  A step is one pass of the hot path over one
 batch of seeded synthetic input (links U = exp(i theta), theta ~ N(0, 1/beta);
@@ -14,17 +14,26 @@ is reported.  Workloads:
   vectors per level = 16 coarse dofs, V-cycle); 32 right-hand sides solved
   together to a true FP64 residual of 1e-10 by an FP32 GCR (truncation 10)
   preconditioned with the FP32 hierarchy, whose fine smoother keeps its work
-  vectors in FP16 with per-site scales, inside FP64 defect correction.  The hierarchy is built
-  once before timing.  value = solves/s.  The plain FP64 single-RHS MG on the
-  same inputs is measured beside it (config.plain_fp64_mg_solves_per_s).
+  vectors in FP16 with per-site scales, inside FP64 defect correction.  The
+  hierarchy is built once before timing.  value = solves/s.  The plain FP64
+  single-RHS MG on the same inputs is measured beside it
+  (detail.plain_fp64_mg_solves_per_s).
+* mg2 — two-level MG-GCR at L = 256, beta = 6, m = -0.05, c_sw = 1; 4 x 4
+  aggregates with 8 null vectors split by chirality (16 coarse dofs), 2
+  inverse iterations, 4 MR steps; one source; the FP32 hierarchy inside FP64
+  defect correction against the plain FP64 MG on the same inputs.
 * dslash — FP32 D on 32 right-hand sides at L = 512; value = algorithmic GB/s.
+* smoother — the fine smoother's three kernels of one MR step on the FP16
+  work vectors of the mg workload's hierarchy (L = 512, 32 RHS); value =
+  algorithmic GB/s of the stencil with the fused MR reductions.  A small
+  process for kernel profiles.
 * coarse — the level-1 coarse operator of the mg workload alone (128 x 128
   sites, 16 dofs, 32 RHS); value = algorithmic GB/s.  A small case for
   kernel profiles.
 * hmc — differentiated HMC at L = 128 (beta = 4, m = 0.1, c_sw = 1): nested
   Omelyan with 10 fermion-force steps and 4 gauge-force substeps per inner
   integration, mixed-precision solves to 1e-10, 20 trajectories;
-  value = trajectories/s, with dH, acceptance and plaquette in config.
+  value = trajectories/s, with dH, acceptance and plaquette in detail.
 * batch — 64 independent lattices, L drawn from {64, 96, 128, 192, 256, 384},
   beta ~ U[2, 8], m ~ U[-0.05, 0.2], c_sw = 1, 8 Gaussian RHS each; every
   lattice runs a 2-level MG (4 x 4, 8 null vectors) mixed GCR to a true FP64
@@ -34,8 +43,12 @@ is reported.  Workloads:
   value = solves/s.
 
 `--impl reference` times the reference's CPU implementation of the same
-workload on this machine's host cores: the C restatement in oracle/ (the
-reference tree is not present where the benchmark runs), with every host core.
+workload on this machine's host cores, with every core: the C restatement in
+oracle/ (the reference tree is not present where the benchmark runs), which
+makes its own inputs and builds its own hierarchy on the CPU; nothing of the
+GPU library is loaded.  The same code gives the GPU arm's cpu_baseline.
+`--gpus N` without a torchrun environment relaunches itself under
+torch.distributed.run with N ranks.
 """
 from __future__ import annotations
 
@@ -147,6 +160,9 @@ def shard(items: list, rank: int, ws: int) -> list:
 MG = dict(L=512, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20240, nrhs=32, levels=3, blocks=[(4, 4), (2, 2)],
           n_vec=16, chiral=False, w_cycle=False, null_iters=6, pre=4, post=4, coarse_max_iter=20, coarse_tol=5e-2,
           tol=1e-10, max_iter=500, trunc=10)
+MG2 = dict(L=256, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=2025, nrhs=1, levels=2, blocks=[(4, 4)], n_vec=8,
+           chiral=True, w_cycle=False, null_iters=2, pre=4, post=4, coarse_max_iter=50, coarse_tol=5e-2, tol=1e-10,
+           max_iter=1000, trunc=20)
 DSLASH = dict(L=512, nrhs=32, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20240)
 CG = dict(L=32, beta=2.0, m=0.1, r=1.0, csw=1.0, mu=0.0, seed=31, tol=1e-10, max_iter=10000)
 HMC = dict(L=128, beta=4.0, m=0.1, r=1.0, csw=1.0, seed=2024, rng_seed=4048, tau=1.0, n_outer=10, n_inner=4,
@@ -184,6 +200,84 @@ def dslash_bytes_f16(L, nrhs):
 def dslash_bytes_f64_single(L):
     """13 x 8 B per site for one FP64 single-RHS application (in 32, out 32, links 32, clover 8)."""
     return L * L * 104
+
+
+def sized(base: dict, args) -> dict:
+    """A workload's configuration with the --L / --nrhs overrides (smaller cases for profiles)."""
+    c = dict(base)
+    if args.L:
+        c["L"] = args.L
+    if args.nrhs:
+        c["nrhs"] = args.nrhs
+    return c
+
+
+def workload_config(workload: str, args) -> tuple[dict, dict]:
+    """(parameters, the `config` object of the JSON line): the same for both arms of the benchmark."""
+    if workload in ("mg", "mg2", "smoother", "coarse"):
+        c = sized(MG2 if workload == "mg2" else MG, args)
+        if args.trunc:
+            c["trunc"] = args.trunc
+        if args.coarse_iters:
+            c["coarse_max_iter"] = args.coarse_iters
+        c["smoother_half"] = args.smoother == "f16" and workload != "mg2"
+        L, nrhs = c["L"], c["nrhs"]
+        blk = ", ".join(f"{a}x{b}" for a, b in c["blocks"])
+        vecs = f"{c['n_vec']} null vectors{' split by chirality' if c['chiral'] else ''}"
+        name = (f"MG-GCR, L={L} (beta={c['beta']:g}, m={c['m']:g}, c_sw={c['csw']:g}), {nrhs} RHS, {c['levels']} levels "
+                f"({blk}; {vecs}, {c['null_iters']} inverse iterations), {'W' if c['w_cycle'] else 'V'}-cycle, "
+                f"{c['pre']}+{c['post']} MR steps, coarsest CG <= {c['coarse_max_iter']} iterations to "
+                f"{c['coarse_tol']:g}, GCR truncation {c['trunc']}, true FP64 residual {c['tol']:g}")
+        if workload == "smoother":
+            name = f"fine smoother kernels of one MR step on FP16 work vectors, L={L}, {nrhs} RHS"
+        if workload == "coarse":
+            name = (f"level-1 coarse operator apply, {L // 4}x{L // 4} sites x {c['n_vec']} dof, {nrhs} RHS "
+                    f"(L={L} fine, 4x4 aggregates)")
+        cfg = {"workload": name, "L": L, "nrhs": nrhs, "levels": c["levels"], "aggregates": [list(b) for b in c["blocks"]],
+               "null_vectors": c["n_vec"], "chiral_split": c["chiral"], "null_iters": c["null_iters"],
+               "mr_steps": [c["pre"], c["post"]], "coarse_cg": [c["coarse_max_iter"], c["coarse_tol"]],
+               "gcr_truncation": c["trunc"], "tol": c["tol"]}
+        return c, cfg
+    if workload == "dslash":
+        c = sized(DSLASH, args)
+        prec = args.dslash_prec
+        name = (f"FP32 Wilson-clover D on {c['nrhs']} RHS, L={c['L']} (beta=6, m=-0.05, c_sw=1)" if prec == "f32"
+                else f"Wilson-clover D on FP16 fields (per-site scales, FP32 arithmetic), {c['nrhs']} RHS, "
+                     f"L={c['L']} (beta=6, m=-0.05, c_sw=1)")
+        return c, {"workload": name, "L": c["L"], "nrhs": c["nrhs"], "precision": prec}
+    if workload == "hmc":
+        c = sized(HMC, args)
+        name = (f"HMC, L={c['L']} (beta={c['beta']}, m={c['m']}, c_sw={c['csw']}), two flavours, tau={c['tau']}, "
+                f"nested Omelyan: {c['n_outer']} fermion-force steps, {c['n_inner']} gauge-force substeps per inner "
+                "integration, mixed-precision CG to a true FP64 residual of 1e-10")
+        return c, {"workload": name, "L": c["L"], "trajectories": c["n_traj"]}
+    if workload == "batch":
+        c = dict(BATCH)
+        c["smoother_half"] = args.smoother == "f16"
+        if args.trunc:
+            c["trunc"] = args.trunc
+        if args.coarse_iters:
+            c["coarse_max_iter"] = args.coarse_iters
+        if args.nrhs:
+            c["nrhs"] = args.nrhs
+        if args.L:
+            c["n_lat"] = args.L  # --L N: the first N lattices of the batch (a small case)
+        if args.workers:
+            c["workers"] = args.workers
+        name = (f"uneven batch of {c['n_lat']} lattices (L in {c['sizes']}, beta~U[2,8], m~U[-0.05,0.2], c_sw=1), "
+                f"{c['nrhs']} RHS each, 2-level MG (4x4, 8 null vectors), mixed FP32/FP64 GCR to a true FP64 "
+                "residual of 1e-10, plus each lattice's pseudofermion force")
+        return c, {"workload": name, "lattices": c["n_lat"], "rhs_per_lattice": c["nrhs"]}
+    c = dict(CG)
+    return c, {"workload": f"FP64 CG on D^dag D, L={c['L']} (beta={c['beta']:g}, m={c['m']:g}, c_sw={c['csw']:g}) "
+                           f"to {c['tol']:g}", "L": c["L"]}
+
+
+def mg_params(smg, c, precision):
+    return smg.mg_params(c["levels"], c["blocks"][0][0], c["n_vec"], blocks=c["blocks"], chiral_split=c["chiral"],
+                         null_iters=c["null_iters"], pre_smooth=c["pre"], post_smooth=c["post"], w_cycle=c["w_cycle"],
+                         coarse_max_iter=c["coarse_max_iter"], coarse_tol=c["coarse_tol"], precision=precision,
+                         seed=c["seed"], smoother_half=c.get("smoother_half", False) and precision == "f32")
 
 
 def kernel_trace(step, ctx, path: str, what: str) -> None:
@@ -226,19 +320,12 @@ def kernel_trace(step, ctx, path: str, what: str) -> None:
     Path(path).write_text("\n".join(out) + "\n")
 
 
-# DRAM read + write bytes of one level-1 tensor-core coarse apply at L = 512, 32 RHS, from one ncu capture
-# (profiles/coarse_apply_tc_L512_level1_32rhs.md)
+# DRAM read + write bytes per launch at L = 512, 32 RHS, from one ncu capture each
+# (profiles/coarse_apply_tc_L512_level1_32rhs.md, profiles/dslash_f32_L512_32rhs.md,
+# profiles/smoother_f16_L512_32rhs.md)
 TC_LEVEL1_L512_DRAM_BYTES = 226.540288e6 + 42.035968e6
-
-
-def sized(base: dict, args) -> dict:
-    """A workload's configuration with the --L / --nrhs overrides (smaller cases for profiles)."""
-    c = dict(base)
-    if args.L:
-        c["L"] = args.L
-    if args.nrhs:
-        c["nrhs"] = args.nrhs
-    return c
+DSLASH_F32_L512_DRAM_BYTES = 140.034048e6 + 98.370048e6
+SMOOTHER_DOTS_L512_DRAM_BYTES = None
 
 
 def coarse_kernel_name(c, L, nrhs):
@@ -248,11 +335,15 @@ def coarse_kernel_name(c, L, nrhs):
     return f"k_coarse_apply_tiled<float,0,16> (level 1, {lc}x{lc}x16, {nrhs} RHS)"
 
 
-def mg_params(smg, c, precision):
-    return smg.mg_params(c["levels"], c["blocks"][0][0], c["n_vec"], blocks=c["blocks"], chiral_split=c["chiral"],
-                         null_iters=c["null_iters"], pre_smooth=c["pre"], post_smooth=c["post"], w_cycle=c["w_cycle"],
-                         coarse_max_iter=c["coarse_max_iter"], coarse_tol=c["coarse_tol"], precision=precision,
-                         seed=c["seed"], smoother_half=c.get("smoother_half", False) and precision == "f32")
+def smoother_times(smg, lib, ctx, mg32, lat, B, reps=20):
+    """The fine smoother's three kernels on the hierarchy's FP16 work vectors (smg_mg_time_smoother)."""
+    f32 = smg.Field(lat, B.shape[0], "f32", ctx, data=B)
+    ms, by = (Cc.c_double * 3)(), (Cc.c_double * 3)()
+    smg._lib.check(lib.smg_mg_time_smoother(mg32.h, f32.h, reps, ms, by), "smg_mg_time_smoother", ctx.h)
+    names = ["k_dslash_h<D, FP16 in/out>", "k_dslash_h<D^dag, FP16, fused <Ar,r>, ||Ar||^2> (+ 2 reduction kernels)",
+             "k_smooth_update_h (x FP32, r FP16)"]
+    return [{"kernel": n, "ms_per_launch": ms[k], "bytes_per_launch": by[k],
+             "achieved_gbs": by[k] / (ms[k] * 1e-3) / 1e9} for k, n in enumerate(names)]
 
 
 def run_ours(args, ws, rank, local):
@@ -264,8 +355,10 @@ def run_ours(args, ws, rank, local):
     ctx = smg.Context(local)
     lib = smg.lib()
     peak, peak_kind = peaks()
+    c, cfg = workload_config(args.workload, args)
     out = {"metric": METRIC, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "scaling": "weak",
-           "vs_baseline": None, "data": "synthetic (seeded theta ~ N(0,1/beta) links, Gaussian complex sources)"}
+           "vs_baseline": None, "data": "synthetic (seeded theta ~ N(0,1/beta) links, Gaussian complex sources)",
+           "config": cfg}
 
     def timed(step, n):
         """Device milliseconds per step on the library's stream, max over ranks."""
@@ -278,13 +371,13 @@ def run_ours(args, ws, rank, local):
         ms = ctx.timer_end() / n
         return max_over_ranks(ms, ws)
 
-    if args.workload == "mg":
-        c = sized(MG, args)
-        c["smoother_half"] = args.smoother == "f16"
-        if args.trunc:
-            c["trunc"] = args.trunc
-        if args.coarse_iters:
-            c["coarse_max_iter"] = args.coarse_iters
+    def pinned_io(B):
+        host_in = torch.empty(B.size * 2, dtype=torch.float64).pin_memory()
+        host_in.numpy()[:] = B.reshape(-1).view(np.float64)
+        host_out = torch.empty_like(host_in).pin_memory()
+        return host_in, host_out, Cc.cast(host_in.data_ptr(), DP), Cc.cast(host_out.data_ptr(), DP)
+
+    if args.workload in ("mg", "mg2"):
         L, nrhs = c["L"], c["nrhs"]
         U = smg.gauge_normal(L, c["beta"], c["seed"])
         lat = smg.Lattice(L)
@@ -292,10 +385,6 @@ def run_ours(args, ws, rank, local):
         D = smg.DiracOp(lat, g, c["m"], c["r"], c["csw"], c["mu"])
         t0 = time.perf_counter()
         mg32 = smg.MGHierarchy(D, mg_params(smg, c, "f32"))
-        defl_info = None
-        if args.coarse_defl:
-            defl_info = mg32.setup_deflation(args.coarse_defl, level=c["levels"] - 1, tol=1e-6,
-                                             allow_unconverged=True)
         ctx.synchronize()
         setup_s = time.perf_counter() - t0
         B = np.stack([smg.random_vec(lat.ndof, c["seed"] + 1 + j) for j in range(nrhs)])
@@ -313,18 +402,15 @@ def run_ours(args, ws, rank, local):
         l0 = ctx.kernel_launches
         with Clocks(local) as clk:
             ms = timed(step, args.steps)
-        launches = ctx.kernel_launches - l0
+        launches = (ctx.kernel_launches - l0) // args.steps
         iters, true_res = res.iterations, res.true_residual
         if args.kernel_trace and rank == 0:
-            kernel_trace(step, ctx, args.kernel_trace, f"one step of the mg workload (L={L}, {nrhs} RHS, "
+            kernel_trace(step, ctx, args.kernel_trace, f"one step of the {args.workload} workload (L={L}, {nrhs} RHS, "
                                                        f"{iters} GCR iterations)")
         value = ws * nrhs / (ms * 1e-3)
 
-        # end to end through the C ABI: pinned host rhs in, solve, solutions out
-        host_in = torch.empty(B.size * 2, dtype=torch.float64).pin_memory()
-        host_in.numpy()[:] = B.reshape(-1).view(np.float64)
-        host_out = torch.empty_like(host_in).pin_memory()
-        pin, pout = Cc.cast(host_in.data_ptr(), DP), Cc.cast(host_out.data_ptr(), DP)
+        # end to end through the C ABI: pinned host rhs in, solve, solutions out, every timed step
+        host_in, host_out, pin, pout = pinned_io(B)
 
         def e2e_step():
             smg._lib.check(lib.smg_field_upload_async(fb.h, pin), "upload", ctx.h)
@@ -332,7 +418,7 @@ def run_ours(args, ws, rank, local):
             smg._lib.check(lib.smg_field_download_async(fx.h, pout), "download", ctx.h)
 
         e2e_step()
-        e2e_ms = timed(e2e_step, max(1, min(args.steps, 3)))
+        e2e_ms = timed(e2e_step, args.steps)
         sol = host_out.numpy().view(np.complex128).reshape(nrhs, -1)
         hb = B.size * 16
 
@@ -342,46 +428,82 @@ def run_ours(args, ws, rank, local):
         x1 = smg.Field(lat, 1, "f64", ctx)
         solve(mg64, b1, x1)
         ms64 = timed(lambda: solve(mg64, b1, x1), 2)
-        it64 = res.iterations
-
-        # dominant kernel: the coarse-operator apply at level 1 on 32 RHS, timed alone
+        it64, res64 = res.iterations, res.true_residual
+        detail = {"gcr_iterations": iters, "true_residual": true_res, "setup_s": setup_s,
+                  "smoother_work_vectors": "FP16, per-site scales" if c["smoother_half"] and nrhs >= 8 else "FP32",
+                  "plain_fp64_mg_solves_per_s": 1e3 / ms64, "plain_fp64_mg_iterations": it64,
+                  "plain_fp64_mg_true_residual": res64, "mixed_batched_over_plain_fp64": value / ws / (1e3 / ms64),
+                  "launches_before_timed": int(l0)}
+        kernels = []
+        # the coarse-operator apply at level 1, timed alone
         cms, cbytes = Cc.c_double(), Cc.c_double()
         smg._lib.check(lib.smg_mg_time_coarse_apply(mg32.h, 1, nrhs, 20, Cc.byref(cms), Cc.byref(cbytes)),
                        "smg_mg_time_coarse_apply", ctx.h)
-        achieved = cbytes.value / (cms.value * 1e-3) / 1e9
-        # fine operator: FP32 D on 32 RHS
+        kernels.append({"kernel": coarse_kernel_name(c, L, nrhs), "ms_per_launch": cms.value,
+                        "bytes_per_launch": cbytes.value, "achieved_gbs": cbytes.value / (cms.value * 1e-3) / 1e9,
+                        "traffic": TC_LEVEL1_L512_DRAM_BYTES if (L, nrhs) == (512, 32) else None})
+        # fine operator: FP32 D on the workload's right-hand sides
         f32s = smg.Field(lat, nrhs, "f32", ctx, data=B)
         f32d = smg.Field(lat, nrhs, "f32", ctx)
         dms = timed(lambda: smg._lib.check(lib.smg_dirac_apply(D.h, 0, f32s.h, f32d.h), "dirac", ctx.h), 20)
         dgbs = dslash_bytes_f32(L, nrhs) / (dms * 1e-3) / 1e9
+        kernels.append({"kernel": f"k_dslash<float> (FP32 D, {nrhs} RHS)", "ms_per_launch": dms,
+                        "bytes_per_launch": dslash_bytes_f32(L, nrhs), "achieved_gbs": dgbs,
+                        "traffic": DSLASH_F32_L512_DRAM_BYTES if (L, nrhs) == (512, 32) else None})
+        detail["fine_dslash_f32_gbs"] = dgbs
+        detail["fine_dslash_frac_of_hbm"] = dgbs / peak
+        if c["smoother_half"] and nrhs >= 8:
+            sm = smoother_times(smg, lib, ctx, mg32, lat, B)
+            sm[1]["traffic"] = SMOOTHER_DOTS_L512_DRAM_BYTES if (L, nrhs) == (512, 32) else None
+            kernels = sm + kernels
+        # the step's largest kernel (profiles/mg_gcr_L512_32rhs_kernel_shares.md): the FP16 stencil with the
+        # fused MR reductions when the smoother runs on FP16 work vectors, else the level-1 coarse apply
+        top = next((k for k in kernels if "fused" in k["kernel"]), kernels[0])
+        for k in kernels:
+            k["frac_of_hbm"] = k["achieved_gbs"] / peak
+        detail["kernels"] = kernels
+        detail["l2"] = (f"fine fields of {nrhs} RHS ({16 * L * L * nrhs / 1e6:.0f} MB FP32) "
+                        f"{'exceed' if 16 * L * L * nrhs > 129e6 else 'fit in'} the 129 MB L2; no flush")
         out.update({
-            "value": value, "unit": "solves/s", "ms_per_step": ms, "higher_is_better": True, "dtype": "f32+f64",
-            "config": {"workload": f"MG-GCR, L={L} (beta=6, m=-0.05, c_sw=1), {nrhs} RHS, 3 levels (4x4, 2x2; 16 null vectors), V-cycle, "
-                                   "FP32 GCR + FP32 hierarchy inside FP64 defect correction, true FP64 residual 1e-10",
-                       "L": L, "nrhs": nrhs, "levels": c["levels"], "gcr_iterations": iters,
-                       "smoother_work_vectors": "FP16, per-site scales" if c["smoother_half"] else "FP32",
-                       "gcr_truncation": c["trunc"],
-                       "coarsest_deflation": ({"eigenvectors": args.coarse_defl, "converged": bool(defl_info.converged),
-                                               "restarts": defl_info.restarts, "lanczos_steps": defl_info.iterations}
-                                              if defl_info is not None else None),
-                       "launches_before_timed": int(l0),
-                       "true_residual": true_res, "setup_s": setup_s,
-                       "plain_fp64_mg_solves_per_s": 1e3 / ms64, "plain_fp64_mg_iterations": it64,
-                       "mixed_batched_over_plain_fp64": value / ws / (1e3 / ms64),
-                       "fine_dslash_f32_32rhs_gbs": dgbs, "fine_dslash_frac_of_hbm": dgbs / peak,
-                       "l2": f"fine fields of {nrhs} RHS ({16 * L * L * nrhs / 1e6:.0f} MB FP32) "
-                                 f"{'exceed' if 16 * L * L * nrhs > 129e6 else 'fit in'} the 129 MB L2; no flush"},
+            "value": value, "unit": "solves/s", "ms_per_step": ms, "higher_is_better": True, "dtype": "f32+f16+f64",
+            "detail": detail,
             "e2e": {"value": ws * nrhs / (e2e_ms * 1e-3), "unit": "solves/s", "h2d_bytes_per_step": hb,
-                    "d2h_bytes_per_step": hb, "ms_per_step": e2e_ms, "finite": bool(np.isfinite(sol).all())},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": TC_LEVEL1_L512_DRAM_BYTES if (L, nrhs) == (512, 32) else None,
-                         "traffic_unit": "bytes per launch (ncu)", "kernel": coarse_kernel_name(c, L, nrhs),
-                         "bytes_per_launch": cbytes.value, "ms_per_launch": cms.value, "peak_source": peak_kind},
+                    "d2h_bytes_per_step": hb, "ms_per_step": e2e_ms, "timed_steps": args.steps,
+                    "finite": bool(np.isfinite(sol).all())},
+            "roofline": {"bound": "hbm", "achieved": top["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                         "frac": top["achieved_gbs"] / peak, "traffic": top.get("traffic"),
+                         "traffic_unit": "bytes per launch (ncu dram read + write)", "kernel": top["kernel"],
+                         "bytes_per_launch": top["bytes_per_launch"], "ms_per_launch": top["ms_per_launch"],
+                         "peak_source": peak_kind},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
         })
+    elif args.workload == "smoother":
+        L, nrhs = c["L"], c["nrhs"]
+        U = smg.gauge_normal(L, c["beta"], c["seed"])
+        lat = smg.Lattice(L)
+        D = smg.DiracOp(lat, smg.GaugeField(lat, U, ctx), c["m"], c["r"], c["csw"], c["mu"])
+        mg32 = smg.MGHierarchy(D, mg_params(smg, c, "f32"))
+        B = np.stack([smg.random_vec(lat.ndof, c["seed"] + 1 + j) for j in range(nrhs)])
+        l0 = ctx.kernel_launches
+        with Clocks(local) as clk:
+            ks = smoother_times(smg, lib, ctx, mg32, lat, B, reps=max(args.steps, 50))
+        launches = ctx.kernel_launches - l0
+        top = ks[1]
+        top["traffic"] = SMOOTHER_DOTS_L512_DRAM_BYTES if (L, nrhs) == (512, 32) else None
+        for k in ks:
+            k["frac_of_hbm"] = k["achieved_gbs"] / peak
+        out.update({
+            "value": ws * top["achieved_gbs"], "unit": "GB/s", "ms_per_step": top["ms_per_launch"],
+            "higher_is_better": True, "dtype": "f16 storage, f32 arithmetic",
+            "detail": {"kernels": ks, "l2": "FP16 fields of 32 RHS (67 MB each) with their neighbours exceed L2"},
+            "e2e": None,
+            "roofline": {"bound": "hbm", "achieved": top["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                         "frac": top["achieved_gbs"] / peak, "traffic": top["traffic"], "kernel": top["kernel"],
+                         "bytes_per_launch": top["bytes_per_launch"], "peak_source": peak_kind},
+            "gpu_launches": int(launches), "clocks": clk.summary(),
+        })
     elif args.workload == "dslash":
-        c = sized(DSLASH, args)
         L, nrhs = c["L"], c["nrhs"]
         U = smg.gauge_normal(L, c["beta"], c["seed"])
         lat = smg.Lattice(L)
@@ -398,16 +520,14 @@ def run_ours(args, ws, rank, local):
 
         for _ in range(args.warmup):
             step()
+        n_timed = max(args.steps, 500)
         l0 = ctx.kernel_launches
         with Clocks(local) as clk:
-            ms = timed(step, max(args.steps, 500))
-        launches = (ctx.kernel_launches - l0) * args.steps // max(args.steps, 500)
+            ms = timed(step, n_timed)
+        launches = (ctx.kernel_launches - l0) // n_timed
         value = ws * bytes_step / (ms * 1e-3) / 1e9
         achieved = bytes_step / (ms * 1e-3) / 1e9
-        host_in = torch.empty(srcs.size * 2, dtype=torch.float64).pin_memory()
-        host_in.numpy()[:] = srcs.reshape(-1).view(np.float64)
-        host_out = torch.empty_like(host_in).pin_memory()
-        pin, pout = Cc.cast(host_in.data_ptr(), DP), Cc.cast(host_out.data_ptr(), DP)
+        host_in, host_out, pin, pout = pinned_io(srcs)
 
         def e2e_step():
             smg._lib.check(lib.smg_field_upload_async(fs.h, pin), "upload", ctx.h)
@@ -419,16 +539,12 @@ def run_ours(args, ws, rank, local):
         hb = srcs.size * 16
         out.update({
             "value": value, "unit": "GB/s", "ms_per_step": ms, "higher_is_better": True, "dtype": prec,
-            "config": {"workload": (f"FP32 Wilson-clover D on {nrhs} RHS, L={L} (beta=6, m=-0.05, c_sw=1)" if prec == "f32"
-                                    else f"Wilson-clover D on FP16 fields (per-site scales, FP32 arithmetic), {nrhs} RHS, "
-                                         f"L={L} (beta=6, m=-0.05, c_sw=1)"),
-                       "L": L, "nrhs": nrhs, "bytes_per_step": bytes_step,
-                       "l2": f"inputs and outputs ({bytes_step / 1e6:.0f} MB) exceed the 129 MB L2; no flush",
-                       "timed_steps": max(args.steps, 500)},
+            "detail": {"bytes_per_step": bytes_step, "timed_steps": n_timed,
+                       "l2": f"inputs and outputs ({bytes_step / 1e6:.0f} MB) exceed the 129 MB L2; no flush"},
             "e2e": {"value": ws * bytes_step / (e2e_ms * 1e-3) / 1e9, "unit": "GB/s",
                     "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb, "ms_per_step": e2e_ms},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": (140.034048e6 + 98.370048e6) if (L, nrhs, prec) == (512, 32, "f32") else None,
+                         "traffic": DSLASH_F32_L512_DRAM_BYTES if (L, nrhs, prec) == (512, 32, "f32") else None,
                          "traffic_unit": "bytes per launch (ncu, profiles/dslash_f32_L512_32rhs.md)",
                          "kernel": ("k_dslash<float,false,0,r=1> (autotuned row kernel)" if prec == "f32"
                                     else "k_dslash_h<false,true,true,r=1> (FP16 fields)"),
@@ -437,7 +553,6 @@ def run_ours(args, ws, rank, local):
         })
     elif args.workload == "hmc":
         # differentiated HMC: nested Omelyan (fermion force outside, gauge force inside), mixed solves
-        c = sized(HMC, args)
         L = c["L"]
         U = smg.gauge_normal(L, c["beta"], c["seed"])
         lat = smg.Lattice(L)
@@ -456,16 +571,12 @@ def run_ours(args, ws, rank, local):
         l0 = ctx.kernel_launches
         with Clocks(local) as clk:
             ms = timed(step, n_timed)
-        launches = (ctx.kernel_launches - l0) * args.steps // n_timed
+        launches = (ctx.kernel_launches - l0) // n_timed
         acc = [r.accepted for r in results]
         out.update({
             "value": ws * 1e3 / ms, "unit": "trajectories/s", "ms_per_step": ms, "higher_is_better": True,
             "dtype": "f64+f32",
-            "config": {"workload": f"HMC, L={L} (beta={c['beta']}, m={c['m']}, c_sw={c['csw']}), two flavours, "
-                                   f"tau={c['tau']}, nested Omelyan: {c['n_outer']} fermion-force steps, "
-                                   f"{c['n_inner']} gauge-force substeps per inner integration, "
-                                   "mixed-precision CG to a true FP64 residual of 1e-10",
-                       "trajectories": len(results), "timed_trajectories": n_timed,
+            "detail": {"trajectories": len(results), "timed_trajectories": n_timed,
                        "acceptance": float(np.mean(acc)),
                        "dH": [round(r.dH, 6) for r in results],
                        "mean_exp_minus_dH": float(np.mean([np.exp(-r.dH) for r in results])),
@@ -479,19 +590,7 @@ def run_ours(args, ws, rank, local):
             "gpu_launches": int(launches), "clocks": clk.summary(),
         })
     elif args.workload == "batch":
-        # uneven multi-lattice batch: every lattice's 8 RHS by mixed MG-GCR to 1e-10 plus its pseudofermion force
-        c = dict(BATCH)
-        c["smoother_half"] = args.smoother == "f16"
-        if args.trunc:
-            c["trunc"] = args.trunc
-        if args.coarse_iters:
-            c["coarse_max_iter"] = args.coarse_iters
-        if args.nrhs:
-            c["nrhs"] = args.nrhs
-        if args.L:
-            c["n_lat"] = args.L  # --L N: the first N lattices of the batch (a small case)
-        if args.workers:
-            c["workers"] = args.workers
+        # uneven multi-lattice batch: every lattice's RHS by mixed MG-GCR to 1e-10 plus its pseudofermion force
         lats_all = batch_lattices(c)
         lats = shard(lats_all, rank, ws)  # several GPUs: the 64 lattices are split across the ranks
         nrhs = c["nrhs"]
@@ -545,7 +644,7 @@ def run_ours(args, ws, rank, local):
         st, _ = batch.solve(c["max_iter"], c["tol"], c["trunc"], with_force=True, host_io=True)
         smg._lib.check(st, "batch e2e")
         e2e_secs = []
-        for _ in range(max(1, min(args.steps, 3))):
+        for _ in range(args.steps):
             torch.cuda.synchronize()
             st, sec = batch.solve(c["max_iter"], c["tol"], c["trunc"], with_force=True, host_io=True)
             smg._lib.check(st, "batch e2e")
@@ -580,15 +679,11 @@ def run_ours(args, ws, rank, local):
             sizes[L] = sizes.get(L, 0) + 1
         out.update({
             "value": n_solves / (ms * 1e-3), "unit": "solves/s", "ms_per_step": ms, "higher_is_better": True,
-            "dtype": "f32+f64", "scaling": "strong",
-            "config": {"workload": f"uneven batch of {len(lats_all)} lattices (L in {c['sizes']}, beta~U[2,8], "
-                                   f"m~U[-0.05,0.2], c_sw=1), {nrhs} RHS each, 2-level MG (4x4, 8 null vectors), "
-                                   "mixed FP32/FP64 GCR to a true FP64 residual of 1e-10, plus each lattice's "
-                                   "pseudofermion force", "lattices": len(lats_all), "lattices_rank0": len(lats),
-                       "sizes_rank0": sizes,
+            "dtype": "f32+f16+f64", "scaling": "strong",
+            "detail": {"lattices_rank0": len(lats), "sizes_rank0": sizes,
                        "smoother_work_vectors": "FP16, per-site scales" if c["smoother_half"] else "FP32",
-                       "gcr_truncation": c["trunc"], "coarsest_cg_iterations": c["coarse_max_iter"],
-                       "sites_total": int(sum(L * L for (L, _, _, _) in lats)), "rhs_per_lattice": nrhs,
+                       "coarsest_cg_iterations": c["coarse_max_iter"],
+                       "sites_total": int(sum(L * L for (L, _, _, _) in lats)),
                        "worst_true_residual": max_over_ranks(worst_res, ws),
                        "gcr_iterations_min_max": [min(iters), max(iters)],
                        "host_workers": c["workers"], "setup_s": setup_s,
@@ -606,7 +701,6 @@ def run_ours(args, ws, rank, local):
         batch.close()
     elif args.workload == "coarse":
         # the level-1 coarse operator alone: (L/4)^2 sites, 16 dofs, 32 RHS, 9-point stencil
-        c = sized(MG, args)
         L, nrhs = c["L"], c["nrhs"]
         U = smg.gauge_normal(L, c["beta"], c["seed"])
         lat = smg.Lattice(L)
@@ -623,9 +717,7 @@ def run_ours(args, ws, rank, local):
         gbs = cbytes.value / (cms.value * 1e-3) / 1e9
         out.update({
             "value": gbs * ws, "unit": "GB/s", "ms_per_step": cms.value, "higher_is_better": True, "dtype": "f32",
-            "config": {"workload": f"level-1 coarse operator apply, {L // 4}x{L // 4} sites x 16 dof, {nrhs} RHS "
-                                   f"(L={L} fine, 4x4 aggregates, 16 null vectors)",
-                       "bytes_per_launch": cbytes.value, "timed_launches": reps,
+            "detail": {"bytes_per_launch": cbytes.value, "timed_launches": reps,
                        "l2": "links and vectors exceed the 129 MB L2 at L=512; no flush"},
             "e2e": None,
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
@@ -635,7 +727,6 @@ def run_ours(args, ws, rank, local):
             "gpu_launches": int(launches), "clocks": clk.summary(),
         })
     else:
-        c = CG
         L = c["L"]
         U = smg.gauge_normal(L, c["beta"], c["seed"])
         lat = smg.Lattice(L)
@@ -654,7 +745,7 @@ def run_ours(args, ws, rank, local):
         l0 = ctx.kernel_launches
         with Clocks(local) as clk:
             ms = timed(step, args.steps)
-        launches = ctx.kernel_launches - l0
+        launches = (ctx.kernel_launches - l0) // args.steps
         bh = b.copy()
         xh = np.empty_like(bh)
         pb, px = bh.view(np.float64).ctypes.data_as(DP), xh.view(np.float64).ctypes.data_as(DP)
@@ -667,133 +758,160 @@ def run_ours(args, ws, rank, local):
         e2e_ms = timed(e2e_step, args.steps)
         out.update({"value": ws * 1e3 / ms, "unit": "solves/s", "ms_per_step": ms, "higher_is_better": True,
                     "dtype": "f64",
-                    "config": {"workload": "FP64 CG on D^dag D, L=32 (beta=2, m=0.1, c_sw=1) to 1e-10",
-                               "iterations": res.iterations, "true_residual": res.true_residual,
+                    "detail": {"iterations": res.iterations, "true_residual": res.true_residual,
                                "l2": "working set is L2-resident within a solve"},
                     "e2e": {"value": ws * 1e3 / e2e_ms, "unit": "solves/s", "h2d_bytes_per_step": bh.nbytes,
                             "d2h_bytes_per_step": xh.nbytes, "ms_per_step": e2e_ms},
                     "gpu_launches": int(launches), "clocks": clk.summary()})
-    if rank == 0 and not args.no_cpu_baseline and args.workload != "coarse":
-        out["cpu_baseline"] = cpu_baseline(args.workload, ctx_objects=locals())
+    if rank == 0 and not args.no_cpu_baseline and args.workload not in ("coarse", "smoother"):
+        base = cpu_reference(args.workload, c, steps=1, warmup=0)
+        out["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample", "seconds")}
     return out
 
 
-def cpu_baseline(workload: str, threads: int | None = None, ctx_objects=None):
-    """The oracle (C restatement of the reference's CPU path) on this host's cores, bounded sample."""
+# ------------------------------------------------------------------ the reference's CPU path
+def cpu_reference(workload: str, c: dict, steps: int, warmup: int, threads: int | None = None) -> dict:
+    """The reference's CPU path for `workload` on this host's cores: the oracle's C restatement
+    (oracle/smg_oracle.c), which makes its own seeded inputs (oracle/inputs.cpp) and builds its own
+    hierarchy on the CPU; nothing of the GPU library is used.  Times `steps` bounded samples after
+    `warmup` untimed ones; returns value, unit, ms_per_step and a description of the sample."""
     from oracle import oracle as O
-
-    import schwinger_mg_gb300 as smg
 
     port = O.port()
     n_threads = threads or os.cpu_count() or 1
     port.set_threads(n_threads)
-    if workload == "mg":
-        c = ctx_objects.get("c", MG) if ctx_objects else MG
+    if workload in ("mg", "mg2"):
         L = c["L"]
-        mg32 = ctx_objects["mg32"] if ctx_objects else None
-        U = smg.gauge_normal(L, c["beta"], c["seed"])
-        if mg32 is None:
-            raise RuntimeError("the MG CPU baseline needs the hierarchy")
-        ncs = [mg32.level_dims(l + 1)[2] for l in range(c["levels"] - 1)]
-        bvs = [mg32.prolongator(l) for l in range(c["levels"] - 1)]
-        links = [None] + [mg32.coarse_op(l) for l in range(1, c["levels"])]
-        p = port.mgN_params(L, c["m"], c["r"], c["csw"], c["mu"], c["blocks"], ncs, bvs, links, c["pre"], c["post"],
-                            c["w_cycle"], c["coarse_max_iter"], c["coarse_tol"])
-        b = smg.random_vec(2 * L * L, c["seed"] + 1)
-        _, it, res, sec = port.mgN_gcr(p, U, b, c["max_iter"], c["tol"], c["trunc"])
-        return {"value": 1.0 / sec, "unit": "solves/s", "cores": n_threads, "kind": "port",
-                "sample": f"one full solve of 1 RHS with the same 3-level hierarchy (the reference solves one "
-                          f"right-hand side at a time): {it} GCR iterations to {res:.1e}, {sec:.1f} s",
-                "seconds": sec}
-    if workload == "dslash":
-        c = DSLASH
-        L, nrhs = c["L"], 8
-        U = smg.gauge_normal(L, c["beta"], c["seed"])
-        srcs = np.stack([smg.random_vec(2 * L * L, c["seed"] + 1 + j) for j in range(nrhs)])
-        t1, _ = port.time_dirac(U, c["m"], c["r"], c["csw"], c["mu"], 0, srcs[:1], 1)
-        reps = max(2, int(10.0 / max(t1 * nrhs, 1e-6)))  # about 10 s of CPU work
-        t, _ = port.time_dirac(U, c["m"], c["r"], c["csw"], c["mu"], 0, srcs, reps)
+        U = port.gauge_normal(L, c["beta"], c["seed"])
+        nl = c["levels"] - 1
+        t0 = time.perf_counter()
+        bvs, links, _ = port.mgN_setup(L, U, c["m"], c["r"], c["csw"], c["mu"], c["blocks"][:nl], [c["n_vec"]] * nl,
+                                       c["null_iters"], c["seed"], chiral_split=c["chiral"])
+        setup_s = time.perf_counter() - t0
+        ncs = [2 * c["n_vec"] if c["chiral"] else c["n_vec"]] * nl
+        p = port.mgN_params(L, c["m"], c["r"], c["csw"], c["mu"], c["blocks"][:nl], ncs, bvs, links, c["pre"],
+                            c["post"], c["w_cycle"], c["coarse_max_iter"], c["coarse_tol"])
+        secs, its, ress = [], [], []
+        for i in range(warmup + steps):
+            b = port.random_vec(2 * L * L, c["seed"] + 1 + (i % c["nrhs"]))
+            _, it, res, sec = port.mgN_gcr(p, U, b, c["max_iter"], c["tol"], c["trunc"])
+            if i >= warmup:
+                secs.append(sec)
+                its.append(it)
+                ress.append(res)
+        sec = float(np.mean(secs))
+        return {"value": 1.0 / sec, "unit": "solves/s", "ms_per_step": 1e3 * sec, "cores": n_threads, "kind": "port",
+                "sample": f"{len(secs)} one-RHS FP64 solve(s) of the workload's right-hand sides (the reference "
+                          f"solves one at a time) on a hierarchy built on the CPU in {setup_s:.1f} s: GCR iterations "
+                          f"{its}, final residuals {max(ress):.1e}, {sec:.2f} s per solve",
+                "seconds": float(np.sum(secs)), "iterations": its, "setup_s": setup_s}
+    if workload in ("dslash", "smoother", "coarse"):
+        cc = DSLASH
+        L, nrhs = cc["L"], 8
+        U = port.gauge_normal(L, cc["beta"], cc["seed"])
+        srcs = np.stack([port.random_vec(2 * L * L, cc["seed"] + 1 + j) for j in range(nrhs)])
+        t1, _ = port.time_dirac(U, cc["m"], cc["r"], cc["csw"], cc["mu"], 0, srcs[:1], 1)
+        reps = max(2, int(10.0 / max(t1 * nrhs, 1e-6)))  # about 10 s of CPU work per step
+        ts = []
+        for i in range(warmup + steps):
+            t, _ = port.time_dirac(U, cc["m"], cc["r"], cc["csw"], cc["mu"], 0, srcs, reps)
+            if i >= warmup:
+                ts.append(t)
+        t = float(np.mean(ts))
         gbs = reps * nrhs * dslash_bytes_f64_single(L) / t / 1e9
-        return {"value": gbs, "unit": "GB/s", "cores": n_threads, "kind": "port",
-                "sample": f"FP64 D on {nrhs} RHS x {reps} reps at L={L} (the reference computes one RHS at a time "
-                          "in FP64; 104 B/site per application)", "seconds": t}
+        return {"value": gbs, "unit": "GB/s", "ms_per_step": 1e3 * t, "cores": n_threads, "kind": "port",
+                "sample": f"FP64 D on {nrhs} RHS x {reps} reps at L={L} per step (the reference computes one RHS at "
+                          "a time in FP64; 104 B/site per application)", "seconds": float(np.sum(ts))}
     if workload == "batch":
-        # one right-hand side of one sampled lattice (L = 128) through the port's MG-GCR with a hierarchy of
-        # the batch's parameters, scaled to the whole batch by site count
-        import schwinger_mg_gb300 as smg2
-
-        c = BATCH
+        # one right-hand side of one sampled lattice (L = 128) through a 2-level hierarchy of the batch's
+        # parameters built on the CPU, scaled to the whole batch by site count
         lats = batch_lattices(c)
         L, beta, m, gseed = next(t for t in lats if t[0] == 128)
-        U = smg2.gauge_normal(L, beta, gseed)
-        lat = smg2.Lattice(L)
-        D = smg2.DiracOp(lat, smg2.GaugeField(lat, U), m, c["r"], c["csw"], 0.0)
-        mgh = smg2.MGHierarchy(D, mg_params(smg2, c, "f64"))
-        ncs = [mgh.level_dims(1)[2]]
-        p = port.mgN_params(L, m, c["r"], c["csw"], 0.0, c["blocks"], ncs, [mgh.prolongator(0)],
-                            [None, mgh.coarse_op(1)], c["pre"], c["post"], c["w_cycle"], c["coarse_max_iter"],
-                            c["coarse_tol"])
-        b = smg2.random_vec(2 * L * L, gseed * 100)
-        _, it, res, sec = port.mgN_gcr(p, U, b, c["max_iter"], c["tol"], c["trunc"])
+        U = port.gauge_normal(L, beta, gseed)
+        bvs, links, _ = port.mgN_setup(L, U, m, c["r"], c["csw"], 0.0, c["blocks"], [c["n_vec"]], c["null_iters"],
+                                       c["seed"])
+        p = port.mgN_params(L, m, c["r"], c["csw"], 0.0, c["blocks"], [c["n_vec"]], bvs, links, c["pre"], c["post"],
+                            c["w_cycle"], c["coarse_max_iter"], c["coarse_tol"])
+        secs, its = [], []
+        for i in range(warmup + steps):
+            b = port.random_vec(2 * L * L, gseed * 100 + (i % c["nrhs"]))
+            _, it, res, sec = port.mgN_gcr(p, U, b, c["max_iter"], c["tol"], c["trunc"])
+            if i >= warmup:
+                secs.append(sec)
+                its.append(it)
+        sec = float(np.mean(secs))
         total_sites = sum(t[0] ** 2 for t in lats)
         est = sec * c["nrhs"] * total_sites / (L * L)
-        return {"value": c["n_lat"] * c["nrhs"] / est, "unit": "solves/s", "cores": n_threads, "kind": "port",
-                "sample": f"one 1-RHS solve of an L={L} lattice of the batch ({it} GCR iterations to {res:.1e}, "
-                          f"{sec:.2f} s), scaled by site count to the {c['n_lat']} x {c['nrhs']} solves "
-                          "(forces excluded)", "seconds": sec}
+        return {"value": c["n_lat"] * c["nrhs"] / est, "unit": "solves/s", "ms_per_step": 1e3 * est, "cores": n_threads,
+                "kind": "port",
+                "sample": f"one-RHS solves of an L={L} lattice of the batch (GCR iterations {its}, {sec:.2f} s each), "
+                          f"scaled by site count to the {c['n_lat']} x {c['nrhs']} solves (forces excluded)",
+                "seconds": float(np.sum(secs))}
     if workload == "hmc":
         # one fermion-force evaluation (CG to 1e-10 + force) and one gauge force on the CPU; a nested
         # Omelyan trajectory makes 2 n_outer + 1 of them plus the two Hamiltonian solves
-        c = HMC
         L = c["L"]
-        U = smg.gauge_normal(L, c["beta"], c["seed"]).reshape(-1)
-        phi = smg.random_vec(2 * L * L, c["seed"] + 7)
-        t0 = time.perf_counter()
-        X, it, _ = port.cg(U, c["m"], c["r"], c["csw"], 0.0, phi, 100000, c["tol"])
-        port.fermion_force(U, c["m"], c["r"], c["csw"], 0.0, X)
-        port.gauge_force(U, c["beta"])
-        t_force = time.perf_counter() - t0
+        U = port.gauge_normal(L, c["beta"], c["seed"]).reshape(-1)
+        phi = port.random_vec(2 * L * L, c["seed"] + 7)
+        ts = []
+        for i in range(warmup + steps):
+            t0 = time.perf_counter()
+            X, it, _ = port.cg(U, c["m"], c["r"], c["csw"], 0.0, phi, 100000, c["tol"])
+            port.fermion_force(U, c["m"], c["r"], c["csw"], 0.0, X)
+            port.gauge_force(U, c["beta"])
+            if i >= warmup:
+                ts.append(time.perf_counter() - t0)
+        t_force = float(np.mean(ts))
         n_solves = 2 * c["n_outer"] + 3
-        return {"value": 1.0 / (n_solves * t_force), "unit": "trajectories/s", "cores": n_threads, "kind": "port",
-                "sample": f"one force evaluation at L={L} (FP64 CG, {it} iterations, to 1e-10, fermion + gauge "
-                          f"force) in {t_force:.2f} s, times the {n_solves} solves of one trajectory",
-                "seconds": t_force}
-    c = CG
-    U = smg.gauge_normal(c["L"], c["beta"], c["seed"])
-    b = smg.random_vec(2 * c["L"] ** 2, c["seed"] + 1)
-    reps, tot, it = 0, 0.0, 0
-    while tot < 5.0 and reps < 200:
-        t, _, it = port.time_cg(U, c["m"], c["r"], c["csw"], c["mu"], b, c["max_iter"], c["tol"])
-        tot += t
-        reps += 1
-    return {"value": reps / tot, "unit": "solves/s", "cores": n_threads, "kind": "port",
-            "sample": f"{reps} FP64 CG solves at L={c['L']} ({it} iterations each)", "seconds": tot}
+        return {"value": 1.0 / (n_solves * t_force), "unit": "trajectories/s", "ms_per_step": 1e3 * n_solves * t_force,
+                "cores": n_threads, "kind": "port",
+                "sample": f"force evaluations at L={L} (FP64 CG, {it} iterations, to 1e-10, fermion + gauge force) "
+                          f"in {t_force:.2f} s each, times the {n_solves} solves of one trajectory",
+                "seconds": float(np.sum(ts))}
+    U = port.gauge_normal(c["L"], c["beta"], c["seed"])
+    b = port.random_vec(2 * c["L"] ** 2, c["seed"] + 1)
+    ts, it = [], 0
+    for i in range(warmup + steps):
+        reps, tot = 0, 0.0
+        while tot < 2.0 and reps < 100:
+            t, _, it = port.time_cg(U, c["m"], c["r"], c["csw"], c["mu"], b, c["max_iter"], c["tol"])
+            tot += t
+            reps += 1
+        if i >= warmup:
+            ts.append(tot / reps)
+    t = float(np.mean(ts))
+    return {"value": 1.0 / t, "unit": "solves/s", "ms_per_step": 1e3 * t, "cores": n_threads, "kind": "port",
+            "sample": f"FP64 CG solves at L={c['L']} ({it} iterations each), about 2 s of repeats per step",
+            "seconds": float(np.sum(ts))}
 
 
 def run_reference(args, ws, rank):
-    """The reference's CPU path (C restatement) on every host core, same workload and metric."""
+    """The reference's CPU path on every host core, same workload, metric and config as the GPU arm.
+    Bounded: at most 5 timed steps after at most 1 warm-up (each MG step is one full solve)."""
     if rank != 0:
         return None
-    if args.workload == "mg":
-        # the hierarchy is built on the GPU (the reference's own build cannot run at this size: its deeper
-        # levels are dense), then every timed step runs on the CPU
-        import schwinger_mg_gb300 as smg
-
-        c = MG
-        ctx = smg.Context(0)
-        U = smg.gauge_normal(c["L"], c["beta"], c["seed"])
-        lat = smg.Lattice(c["L"])
-        D = smg.DiracOp(lat, smg.GaugeField(lat, U, ctx), c["m"], c["r"], c["csw"], c["mu"])
-        mg32 = smg.MGHierarchy(D, mg_params(smg, c, "f64"))
-        base = cpu_baseline("mg", ctx_objects={"mg32": mg32})
-    else:
-        base = cpu_baseline(args.workload)
+    c, cfg = workload_config(args.workload, args)
+    steps, warmup = max(1, min(args.steps, 5)), min(args.warmup, 1)
+    base = cpu_reference(args.workload, c, steps=steps, warmup=warmup)
     val = base["value"]
     return {"metric": METRIC, "impl": "reference", "value": val, "unit": base["unit"], "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": {"workload": args.workload},
+            "steps": steps, "warmup": warmup, "ms_per_step": base["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": cfg,
             "cpu_baseline": {"kind": base["kind"], "cores": base["cores"], "sample": base["sample"], "value": val},
-            "e2e": {"value": val, "unit": base["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": val, "unit": base["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+
+
+def relaunch_distributed(n: int) -> int:
+    """`--gpus N` outside torchrun: run this script under torch.distributed.run with N ranks on this node."""
+    import socket
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr=127.0.0.1", f"--master-port={port}", str(Path(__file__).resolve()), *sys.argv[1:]]
+    return subprocess.call(cmd)
 
 
 def main():
@@ -801,7 +919,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--workload", default="mg", choices=["mg", "dslash", "cg", "coarse", "hmc", "batch"])
+    ap.add_argument("--workload", default="mg",
+                    choices=["mg", "mg2", "dslash", "smoother", "cg", "coarse", "hmc", "batch"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--L", type=int, default=0, help="lattice size override (smaller cases for profiles)")
@@ -813,13 +932,15 @@ def main():
     ap.add_argument("--workers", type=int, default=0, help="batch workload: host worker threads override")
     ap.add_argument("--dslash-prec", default="f32", choices=["f32", "f16"],
                     help="dslash workload: field precision (f16 = FP16 storage with per-site scales)")
-    ap.add_argument("--coarse-defl", type=int, default=0,
-                    help="mg workload: eigenvectors of the coarsest operator for the coarsest CG's deflated start")
     ap.add_argument("--kernel-trace", default="", help="mg and batch workloads: write a CUPTI per-kernel summary of "
                                                          "one extra (untimed) step to this path")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if "WORLD_SIZE" not in os.environ and args.gpus > 1:
+        sys.exit(relaunch_distributed(args.gpus))
     ws, rank, local = dist_env()
+    if ws != args.gpus:
+        raise SystemExit(f"--gpus {args.gpus} but WORLD_SIZE={ws}: launch one rank per GPU")
     if args.impl == "reference":
         line = run_reference(args, ws, rank)
         if line is not None:

@@ -431,6 +431,14 @@ SMG_API smg_status smg_mg_coarse_apply_host(smg_mg* mg, int level, const double*
 SMG_API smg_status smg_mg_coarse_apply_batch(smg_mg* mg, int level, int nrhs, int engine, const float* in,
                                              const float* w, float* out, double* dots);
 SMG_API smg_status smg_mg_time_coarse_apply(smg_mg* mg, int level, int nrhs, int reps, double* ms, double* bytes);
+/* Timing of the fine smoother's kernels of one MR step (mr_smooth_op,
+ * src/smoother.cpp:26-40) on the hierarchy's FP16 work vectors (F32
+ * hierarchy with smoother_half): ms[0] t = D r, ms[1] A r = D^dag t with
+ * <A r, r> and ||A r||^2 fused, ms[2] the x / r update; each the average of
+ * `reps` launches timed with CUDA events on the context's stream after one
+ * warm-up pass.  r is formed from b (F32, nrhs a power of two >= 8).
+ * bytes[k] (optional): each kernel's compulsory HBM bytes. */
+SMG_API smg_status smg_mg_time_smoother(smg_mg* mg, const smg_field* b, int reps, double* ms, double* bytes);
 
 /* fcg_solve / fcg_solve_mg: truncated GCR on A = D^dag D from x = 0
  * (reference src/solvers.cpp:223-300, 803-811), preconditioned by one MG

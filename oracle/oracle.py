@@ -26,7 +26,8 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 PORT_SO = HERE / "_build" / "libsmg_oracle.so"
 REF_SO = HERE / "_ref" / "libsmg_ref.so"
-REF_SRC = Path(os.environ.get("SMG_REFERENCE_SRC", "/root/reference/src"))
+# the reference's src/ directory, only from the environment (the reference shim is built only when it is set)
+REF_SRC = Path(os.environ["SMG_REFERENCE_SRC"]) if os.environ.get("SMG_REFERENCE_SRC") else None
 
 _dp = C.POINTER(C.c_double)
 
@@ -35,10 +36,11 @@ def build(ref: bool | None = None) -> None:
     """Compiles the C restatement and, when the reference tree exists, the reference shim."""
     targets = ["oracle"]
     if ref is None:
-        ref = (REF_SRC / "dirac.h").exists()
+        ref = REF_SRC is not None and (REF_SRC / "dirac.h").exists()
     if ref:
         targets.append("ref")
-    subprocess.run(["make", "-s", "-j8", "-C", str(HERE), f"REF={REF_SRC}", *targets], check=True)
+    args = [f"REF={REF_SRC}"] if REF_SRC is not None else []
+    subprocess.run(["make", "-s", "-j8", "-C", str(HERE), *args, *targets], check=True)
 
 
 def _p(a: np.ndarray):
@@ -75,6 +77,12 @@ class OrcMGNParams(C.Structure):
                 ("block_vecs", C.POINTER(C.c_double) * (MAXL - 1)), ("links", C.POINTER(C.c_double) * MAXL),
                 ("pre_smooth", C.c_int), ("post_smooth", C.c_int), ("w_cycle", C.c_int),
                 ("coarse_max_iter", C.c_int), ("coarse_tol", C.c_double)]
+
+
+class OrcMGNSetupParams(C.Structure):
+    _fields_ = [("n_levels", C.c_int), ("L", C.c_int), ("m", C.c_double), ("r", C.c_double), ("csw", C.c_double),
+                ("mu", C.c_double), ("block", (C.c_int * 2) * (MAXL - 1)), ("nvec", C.c_int * (MAXL - 1)),
+                ("chiral_split", C.c_int), ("null_iters", C.c_int), ("null_mr_steps", C.c_int), ("seed", C.c_uint32)]
 
 
 class _Lib:
@@ -270,6 +278,46 @@ class Port(_Lib):
                                   C.c_int(trunc), C.byref(res), C.byref(sec))
         return x, it, res.value, sec.value
 
+    def random_vec(self, n: int, seed: int) -> np.ndarray:
+        """random_vec(n, std::mt19937(seed)) (oracle/inputs.cpp)."""
+        v = np.empty(n, dtype=np.complex128)
+        self.lib.orc_random_vec(C.c_long(n), C.c_uint32(seed), _p(v))
+        return v
+
+    def gauge_normal(self, L: int, beta: float, seed: int) -> np.ndarray:
+        """Links U[mu][s] = exp(i theta), theta ~ N(0, 1/beta) from std::mt19937(seed) (oracle/inputs.cpp)."""
+        U = np.empty(2 * L * L, dtype=np.complex128)
+        self.lib.orc_gauge_normal(C.c_int(L), C.c_double(beta), C.c_uint32(seed), _p(U))
+        return U.reshape(2, L * L)
+
+    def mgN_setup(self, L, U, m, r, csw, mu, blocks, nvecs, null_iters, seed, chiral_split=False, null_mr_steps=5):
+        """The hierarchy built on the CPU (orc_mgN_setup): (block_vecs per transfer, links per level with
+        links[0] = None, level-0 null vectors), in the layouts orc_mgN_params takes."""
+        n_levels = len(blocks) + 1
+        p = OrcMGNSetupParams()
+        p.n_levels, p.L, p.m, p.r, p.csw, p.mu = n_levels, L, m, r, csw, mu
+        for l, (b, k) in enumerate(zip(blocks, nvecs)):
+            p.block[l][0], p.block[l][1] = b
+            p.nvec[l] = k
+        p.chiral_split, p.null_iters, p.null_mr_steps, p.seed = int(chiral_split), null_iters, null_mr_steps, seed
+        nx = ny = L
+        nd = 2
+        bvs, links = [], [None]
+        for (ax, ay), k in zip(blocks, nvecs):
+            nc = 2 * k if chiral_split else k
+            bvs.append(np.empty(nx * ny * nd * nc, dtype=np.complex128))
+            nx, ny, nd = nx // ax, ny // ay, nc
+            links.append(np.empty(nx * ny * 9 * nd * nd, dtype=np.complex128))
+        null0 = np.empty(nvecs[0] * 2 * L * L, dtype=np.complex128)
+        bv_arr = (_dp * (MAXL - 1))(*[_p(b) for b in bvs])
+        lk_arr = (_dp * MAXL)(None, *[_p(a) for a in links[1:]])
+        U = _c(U)
+        self.lib.orc_mgN_setup.restype = C.c_int
+        rc = self.lib.orc_mgN_setup(C.byref(p), _p(U), bv_arr, lk_arr, _p(null0))
+        if rc != 0:
+            raise ValueError(f"orc_mgN_setup: bad geometry ({rc})")
+        return bvs, links, null0.reshape(nvecs[0], -1)
+
     def set_threads(self, n: int) -> None:
         self.lib.orc_set_threads(C.c_int(n))
 
@@ -339,6 +387,23 @@ class Ref(_Lib):
         self.lib.ref_dense_coarse_build(C.c_int(L), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw),
                                         C.c_double(mu), C.c_int(bs), C.c_int(k), _p(bv), _p(mat))
         return mat.reshape(dim, dim).T  # stored column-major
+
+    def mg3_export(self, U, m, r, csw, mu, params: RefMGParams, seed):
+        """The reference's three-level hierarchy: (level-0 null vectors, level-1 CoarseProlongator block vectors
+        [block][k][block_k], dense level-1 operator, dense level-2 operator), the dense matrices as [row][col]."""
+        U = _c(U)
+        L = self._L(U)
+        k = params.k_null
+        dim1 = (L // params.block_size) ** 2 * k
+        cb = params.coarse_block if params.coarse_block > 0 else 4 * k
+        dim2 = dim1 // cb * k
+        null0 = np.empty(k * 2 * L * L, dtype=np.complex128)
+        bv1 = np.empty(dim1 // cb * k * cb, dtype=np.complex128)
+        A1 = np.empty(dim1 * dim1, dtype=np.complex128)
+        A2 = np.empty(dim2 * dim2, dtype=np.complex128)
+        self.lib.ref_mg3_export(C.c_int(L), _p(U), C.c_double(m), C.c_double(r), C.c_double(csw), C.c_double(mu),
+                                C.byref(params), C.c_uint(seed), _p(null0), _p(bv1), _p(A1), _p(A2))
+        return null0.reshape(k, -1), bv1, A1.reshape(dim1, dim1).T.copy(), A2.reshape(dim2, dim2).T.copy()
 
     def verify_forces(self, U, beta, m, r, csw, mu, max_iter, tol, use_eo=False):
         U = _c(U)

@@ -299,6 +299,27 @@ void ref_mg_null_vectors(int L, const double* U, double m, double r, double csw,
     for (int i = 0; i < p->k_null; ++i) from_vec(mg.null_vecs_l0[i], out + (size_t)2 * w.lat.ndof * i);
 }
 
+// The three-level hierarchy of build_mg_hierarchy (src/multigrid.cpp:595-687):
+// level-0 null vectors (k x 2V), the level-1 CoarseProlongator block vectors
+// (src/prolongator.h:149-228; [block][k][block_k]), the level-1 operator
+// (levels[0].Ac, dense columns) and the level-2 operator (intermediate_Ac,
+// dense columns).  Sizes: dim1 = (L/bs)^2 k, dim2 = dim1 / block_k * k.
+void ref_mg3_export(int L, const double* U, double m, double r, double csw, double mu, const RefMGParams* p,
+                    unsigned seed, double* null0, double* bv1, double* Ac1, double* Ac2) {
+    World w(L, U);
+    DiracOp D(w.lat, w.g, m, r, csw, mu);
+    MGHierarchy mg = ref_build(D, *p, seed, nullptr);
+    for (int i = 0; i < p->k_null; ++i) from_vec(mg.null_vecs_l0[i], null0 + (size_t)2 * w.lat.ndof * i);
+    const CoarseProlongator& Pc = mg.coarse_prolongators.at(0);
+    for (int b = 0; b < Pc.nblocks; ++b)
+        for (int k = 0; k < Pc.k_vec; ++k)
+            from_vec(Pc.block_vecs[b][k], bv1 + (size_t)2 * ((size_t)b * Pc.k_vec + k) * Pc.block_k);
+    const CoarseOp& A1 = mg.levels[0].Ac;
+    for (int j = 0; j < A1.dim; ++j) from_vec(A1.mat[j], Ac1 + (size_t)2 * A1.dim * j);
+    const CoarseOp& A2 = mg.intermediate_Ac.at(0);
+    for (int j = 0; j < A2.dim; ++j) from_vec(A2.mat[j], Ac2 + (size_t)2 * A2.dim * j);
+}
+
 // generate_pseudofermion (src/hmc_trajectory.cpp:32-36) with mt19937(seed)
 void ref_pseudofermion(int L, const double* U, double m, double r, double csw, double mu, unsigned seed,
                        double* phi) {

@@ -735,6 +735,7 @@ static int c_cg(const Coarse* A, const cxd* b, cxd* x, int max_iter, double cg_t
         cxd pAp = v_dot(p, Ap, dim);
         if (cabs(pAp) < 1e-30) break;
         cxd alpha = rr_val / pAp;
+#pragma omp parallel for schedule(static) if (dim > 4096)
         for (int i = 0; i < dim; ++i) {
             x[i] += alpha * p[i];
             r[i] -= alpha * Ap[i];
@@ -746,6 +747,7 @@ static int c_cg(const Coarse* A, const cxd* b, cxd* x, int max_iter, double cg_t
         cxd rr_new = v_dot(r, r, dim);
         cxd beta = rr_new / rr_val;
         rr_val = rr_new;
+#pragma omp parallel for schedule(static) if (dim > 4096)
         for (int i = 0; i < dim; ++i) p[i] = r[i] + beta * p[i];
     }
     free(Ax);
@@ -1060,6 +1062,7 @@ static void n_mr(const MGN* g, int l, cxd* x, const cxd* b, int niter) {
     cxd* Ar = (cxd*)malloc(sizeof(cxd) * (size_t)n);
     for (int it = 0; it < niter; ++it) {
         n_apply(g, l, x, r);
+#pragma omp parallel for schedule(static) if (n > 4096)
         for (long i = 0; i < n; ++i) r[i] = b[i] - r[i];
         n_apply(g, l, r, Ar);
         cxd rAr = v_dot(Ar, r, n), ArAr = v_dot(Ar, Ar, n);
@@ -1081,6 +1084,7 @@ static void n_cycle(const MGN* g, int l, const cxd* b, cxd* x) {
     n_mr(g, l, x, b, g->p->pre_smooth);
     cxd* r = (cxd*)malloc(sizeof(cxd) * (size_t)n);
     n_apply(g, l, x, r);
+#pragma omp parallel for schedule(static) if (n > 4096)
     for (long i = 0; i < n; ++i) r[i] = b[i] - r[i];
     long nc = n_dim(g, l + 1);
     cxd* rc = (cxd*)malloc(sizeof(cxd) * (size_t)nc);
@@ -1187,9 +1191,12 @@ int orc_mgN_gcr(const orc_mgN_params* p, const double* U, const double* bh, doub
         memcpy(Ap, Az, sizeof(cxd) * (size_t)n);
         for (int i = 0; i < nd; ++i) {
             cxd beta = v_dot(APd[i], Az, n) / ApAp[i];
+            const cxd* Pi = Pd[i];
+            const cxd* APi = APd[i];
+#pragma omp parallel for schedule(static) if (n > 4096)
             for (long j = 0; j < n; ++j) {
-                pp[j] -= beta * Pd[i][j];
-                Ap[j] -= beta * APd[i][j];
+                pp[j] -= beta * Pi[j];
+                Ap[j] -= beta * APi[j];
             }
         }
         double ApAp_val = creal(v_dot(Ap, Ap, n));
@@ -1204,6 +1211,7 @@ int orc_mgN_gcr(const orc_mgN_params* p, const double* U, const double* bh, doub
             continue;
         }
         cxd alpha = v_dot(Ap, r, n) / ApAp_val;
+#pragma omp parallel for schedule(static) if (n > 4096)
         for (long j = 0; j < n; ++j) {
             x[j] += alpha * pp[j];
             r[j] -= alpha * Ap[j];
@@ -1243,4 +1251,314 @@ int orc_mgN_gcr(const orc_mgN_params* p, const double* U, const double* bh, doub
     free(rhs);
     n_free(&g);
     return iter;
+}
+
+/* ------------------------------------------------------ CPU hierarchy set-up */
+/* The reference's hierarchy build (build_mg_hierarchy, src/multigrid.cpp:595-687)
+ * restated on the CPU with a geometric ax x ay aggregate at every level (the
+ * reference's CoarseProlongator linear blocking of 4k consecutive coarse dofs,
+ * src/prolongator.h:149-228, is the 4 x 1 aggregate of coarse sites):
+ *   - one std::mt19937(seed) draws every start vector, level by level, in
+ *     random_vec order (compute_near_null_space / _generic draw from the rng
+ *     they are given, src/multigrid.cpp:435-484, 545-587);
+ *   - near-null vectors: per vector `iters` x (mr_smooth_op from x = 0 with
+ *     the vector as right-hand side, Gram-Schmidt against the earlier ones,
+ *     normalise), then a final Gram-Schmidt pass;
+ *   - block vectors: the null vectors cut to aggregates and orthonormalised
+ *     by modified Gram-Schmidt (orthonormalise_block, src/prolongator.h:111-130);
+ *   - Galerkin operators formed directly instead of by probing
+ *     (SparseCoarseOp::build, src/coarse_op.h:241-279):
+ *       level 1:     A[b][d](i, j) = <D P e_{b,i}, D P e_{nb(b,d),j}>  (A = D^dag D)
+ *       level l + 1: A[b][d](i, j) = <P e_{b,i}, A_l P e_{nb(b,d),j}>
+ *     in the link layout [site][dir][i * nc + j] of SparseCoarseOp.
+ * With chiral_split each null vector gives two block vectors, its upper and
+ * lower chirality halves (spin 0 / 1 at level 0, the first / second half of
+ * the coarse dofs deeper), ordered i = c * nvec + k. */
+
+void* orc_rng_create(uint32_t seed);
+void orc_rng_random_vec(void* h, long n, double* v);
+void orc_rng_destroy(void* h);
+
+typedef void (*op_fn)(const void* ctx, const cxd* x, cxd* y);
+
+static void op_ddagd(const void* c, const cxd* x, cxd* y) { d_apply_DdagD((const Dirac*)c, x, y); }
+static void op_coarse(const void* c, const cxd* x, cxd* y) { c_apply((const Coarse*)c, x, y); }
+
+/* mr_smooth_op (reference src/smoother.cpp:26-40) */
+static void mr_op(op_fn A, const void* ac, long n, cxd* x, const cxd* b, int niter, cxd* r, cxd* Ar) {
+    for (int it = 0; it < niter; ++it) {
+        A(ac, x, r);
+#pragma omp parallel for schedule(static) if (n > 4096)
+        for (long i = 0; i < n; ++i) r[i] = b[i] - r[i];
+        A(ac, r, Ar);
+        cxd rAr = v_dot(Ar, r, n), ArAr = v_dot(Ar, Ar, n);
+        if (cabs(ArAr) < 1e-30) break;
+        v_axpy(rAr / ArAr, r, x, n);
+    }
+}
+
+/* compute_near_null_space_generic (reference src/multigrid.cpp:545-587) on
+ * start vectors nv[0..k) that are overwritten with the result */
+static void null_space_op(op_fn A, const void* ac, long n, int k, int iters, int mr_steps, cxd** nv) {
+    cxd* x_new = (cxd*)malloc(sizeof(cxd) * (size_t)n);
+    cxd* r = (cxd*)malloc(sizeof(cxd) * (size_t)n);
+    cxd* Ar = (cxd*)malloc(sizeof(cxd) * (size_t)n);
+    for (int i = 0; i < k; ++i) {
+        v_scale(nv[i], 1.0 / v_norm(nv[i], n), n);
+        for (int it = 0; it < iters; ++it) {
+            memset(x_new, 0, sizeof(cxd) * (size_t)n);
+            mr_op(A, ac, n, x_new, nv[i], mr_steps, r, Ar);
+            for (int j = 0; j < i; ++j) v_axpy(-v_dot(nv[j], x_new, n), nv[j], x_new, n);
+            double nrm = v_norm(x_new, n);
+            if (!(nrm > 1e-14)) break;
+            v_scale(x_new, 1.0 / nrm, n);
+            memcpy(nv[i], x_new, sizeof(cxd) * (size_t)n);
+        }
+    }
+    for (int i = 0; i < k; ++i) {
+        for (int j = 0; j < i; ++j) v_axpy(-v_dot(nv[j], nv[i], n), nv[j], nv[i], n);
+        double nrm = v_norm(nv[i], n);
+        if (nrm > 1e-14) v_scale(nv[i], 1.0 / nrm, n);
+    }
+    free(x_new);
+    free(r);
+    free(Ar);
+}
+
+/* block vectors [agg][i][loc * nd + j] of ax x ay aggregates on an nx x ny
+ * level with nd dofs per site (loc = (x % ax) + ax * (y % ay), agg =
+ * (x / ax) + (nx / ax) * (y / ay)), orthonormalised per aggregate */
+static cxd* block_vectors(int nx, int ny, int nd, int ax, int ay, int nvec, int split, cxd* const* nv) {
+    const int nax = nx / ax, nagg = nax * (ny / ay), m = ax * ay, len = m * nd;
+    const int nc = split ? 2 * nvec : nvec;
+    cxd* bv = (cxd*)calloc((size_t)nagg * nc * len, sizeof(cxd));
+#pragma omp parallel for schedule(static)
+    for (int B = 0; B < nagg; ++B) {
+        const int x0 = (B % nax) * ax, y0 = (B / nax) * ay;
+        for (int k = 0; k < nvec; ++k)
+            for (int loc = 0; loc < m; ++loc) {
+                const long s = (x0 + loc % ax) + (long)nx * (y0 + loc / ax);
+                for (int j = 0; j < nd; ++j) {
+                    const cxd v = nv[k][s * nd + j];
+                    if (split) {
+                        const int chi = nd == 2 ? j : (j < nd / 2 ? 0 : 1);
+                        bv[((long)B * nc + chi * nvec + k) * len + loc * nd + j] = v;
+                    } else {
+                        bv[((long)B * nc + k) * len + loc * nd + j] = v;
+                    }
+                }
+            }
+        for (int k = 0; k < nc; ++k) {
+            cxd* v = bv + ((long)B * nc + k) * len;
+            for (int j = 0; j < k; ++j) {
+                const cxd* u = bv + ((long)B * nc + j) * len;
+                cxd proj = 0;
+                for (int e = 0; e < len; ++e) proj += conj(u[e]) * v[e];
+                for (int e = 0; e < len; ++e) v[e] -= proj * u[e];
+            }
+            double nn = 0;
+            for (int e = 0; e < len; ++e) nn += creal(v[e]) * creal(v[e]) + cimag(v[e]) * cimag(v[e]);
+            nn = sqrt(nn);
+            if (nn > 1e-14)
+                for (int e = 0; e < len; ++e) v[e] /= nn;
+        }
+    }
+    return bv;
+}
+
+/* one site of D applied to a field given by its values at the site and its
+ * four neighbours (the arithmetic of apply_impl + accumulate_hops,
+ * reference src/dirac.h:58-113) */
+static void d_site(const Dirac* D, int s, const cxd* c, const cxd* xp, const cxd* xm, const cxd* yp,
+                   const cxd* ym, cxd* out) {
+    const int L = D->g.L;
+    const double r = D->r;
+    const double diag = 2.0 * D->r + D->mass;
+    const double C = D->F ? 0.5 * D->csw * D->F[s] : 0.0;
+    cxd d0 = ((diag + C) + I * D->mu) * c[0];
+    cxd d1 = ((diag - C) - I * D->mu) * c[1];
+    {
+        cxd u = D->g.U0[s];
+        cxd a0 = u * xp[0], a1 = u * xp[1];
+        d0 -= 0.5 * (r * a0 - a1);
+        d1 -= 0.5 * (-a0 + r * a1);
+    }
+    {
+        cxd u = conj(D->g.U0[l_xm(L, s)]);
+        cxd a0 = u * xm[0], a1 = u * xm[1];
+        d0 -= 0.5 * (r * a0 + a1);
+        d1 -= 0.5 * (a0 + r * a1);
+    }
+    {
+        cxd u = D->g.U1[s];
+        cxd a0 = u * yp[0], a1 = u * yp[1];
+        d0 -= 0.5 * (r * a0 + I * a1);
+        d1 -= 0.5 * (-I * a0 + r * a1);
+    }
+    {
+        cxd u = conj(D->g.U1[l_ym(L, s)]);
+        cxd a0 = u * ym[0], a1 = u * ym[1];
+        d0 -= 0.5 * (r * a0 - I * a1);
+        d1 -= 0.5 * (I * a0 + r * a1);
+    }
+    out[0] = d0;
+    out[1] = d1;
+}
+
+static const int kDirOf[3][3] = {{8, 2, 7}, {4, 0, 3}, {6, 1, 5}}; /* [dx + 1][dy + 1] -> direction */
+
+/* level-1 Galerkin operator from W_{B,i} = D P e_{B,i} on the (ax+2) x (ay+2)
+ * frame around each aggregate; links [B][d][i * nc + j] */
+static void galerkin0(const Dirac* D, int ax, int ay, int nc, const cxd* bv, cxd* lk) {
+    const int L = D->g.L, nax = L / ax, nay = L / ay, nagg = nax * nay, m = ax * ay;
+    const int fx = ax + 2, fy = ay + 2, nh = fx * fy;
+    cxd* W = (cxd*)malloc(sizeof(cxd) * (size_t)nagg * nc * nh * 2);
+    const cxd zero2[2] = {0, 0};
+#pragma omp parallel for schedule(static)
+    for (int B = 0; B < nagg; ++B) {
+        const int x0 = (B % nax) * ax, y0 = (B / nax) * ay;
+        for (int i = 0; i < nc; ++i) {
+            const cxd* v = bv + ((long)B * nc + i) * m * 2;
+            for (int h = 0; h < nh; ++h) {
+                const int lx = h % fx - 1, ly = h / fx - 1;
+                const int s = l_idx(L, x0 + lx, y0 + ly);
+#define PV(X, Y) (((X) >= 0 && (X) < ax && (Y) >= 0 && (Y) < ay) ? v + 2 * ((X) + ax * (Y)) : zero2)
+                d_site(D, s, PV(lx, ly), PV(lx + 1, ly), PV(lx - 1, ly), PV(lx, ly + 1), PV(lx, ly - 1),
+                       W + (((long)B * nc + i) * nh + h) * 2);
+#undef PV
+            }
+        }
+    }
+#pragma omp parallel for schedule(static)
+    for (int B = 0; B < nagg; ++B) {
+        const int Bx = B % nax, By = B / nax;
+        for (int d = 0; d < 9; ++d) {
+            const int dx = kDx[d], dy = kDy[d];
+            const int B2 = (Bx + dx + nax) % nax + nax * ((By + dy + nay) % nay);
+            const int hx0 = dx > 0 ? ax : 0, hx1 = dx < 0 ? 2 : fx;
+            const int hy0 = dy > 0 ? ay : 0, hy1 = dy < 0 ? 2 : fy;
+            for (int i = 0; i < nc; ++i) {
+                const cxd* w1 = W + ((long)B * nc + i) * nh * 2;
+                for (int j = 0; j < nc; ++j) {
+                    const cxd* w2 = W + ((long)B2 * nc + j) * nh * 2;
+                    cxd acc = 0;
+                    for (int hy = hy0; hy < hy1; ++hy)
+                        for (int hx = hx0; hx < hx1; ++hx) {
+                            const int h1 = hx + fx * hy, h2 = (hx - dx * ax) + fx * (hy - dy * ay);
+                            acc += conj(w1[2 * h1]) * w2[2 * h2] + conj(w1[2 * h1 + 1]) * w2[2 * h2 + 1];
+                        }
+                    lk[(((long)B * 9 + d) * nc + i) * nc + j] = acc;
+                }
+            }
+        }
+    }
+    free(W);
+}
+
+/* Galerkin operator of a coarse level: A'[B][d'](i, j) = sum over the sites s
+ * of B and directions d of V_B(s)^dag L[s][d] V_B2(nb(s, d)) */
+static void galerkin_c(int nx, int ny, int nd, const cxd* lk, int ax, int ay, int nc, const cxd* bv, cxd* out) {
+    const int nax = nx / ax, nay = ny / ay, nagg = nax * nay, m = ax * ay, len = m * nd;
+    memset(out, 0, sizeof(cxd) * (size_t)nagg * 9 * nc * nc);
+#pragma omp parallel
+    {
+        cxd* T = (cxd*)malloc(sizeof(cxd) * (size_t)nd * nc); /* T[ki][j] = sum_kj L(ki, kj) V_B2[j](loc2, kj) */
+#pragma omp for schedule(static)
+        for (int B = 0; B < nagg; ++B) {
+            const int Bx = B % nax, By = B / nax;
+            for (int loc = 0; loc < m; ++loc) {
+                const int x = Bx * ax + loc % ax, y = By * ay + loc / ax;
+                const long s = x + (long)nx * y;
+                for (int d = 0; d < 9; ++d) {
+                    const int x2 = (x + kDx[d] + nx) % nx, y2 = (y + kDy[d] + ny) % ny;
+                    const int B2x = x2 / ax, B2y = y2 / ay;
+                    int ddx = B2x - Bx, ddy = B2y - By;
+                    if (ddx > 1) ddx -= nax;
+                    if (ddx < -1) ddx += nax;
+                    if (ddy > 1) ddy -= nay;
+                    if (ddy < -1) ddy += nay;
+                    const int dp = kDirOf[ddx + 1][ddy + 1];
+                    const int B2 = B2x + nax * B2y, loc2 = (x2 % ax) + ax * (y2 % ay);
+                    const cxd* Lm = lk + (s * 9 + d) * nd * nd;
+                    for (int ki = 0; ki < nd; ++ki)
+                        for (int j = 0; j < nc; ++j) {
+                            const cxd* v2 = bv + ((long)B2 * nc + j) * len + loc2 * nd;
+                            cxd acc = 0;
+                            for (int kj = 0; kj < nd; ++kj) acc += Lm[ki * nd + kj] * v2[kj];
+                            T[ki * nc + j] = acc;
+                        }
+                    cxd* Ao = out + ((long)B * 9 + dp) * nc * nc;
+                    for (int i = 0; i < nc; ++i) {
+                        const cxd* v1 = bv + ((long)B * nc + i) * len + loc * nd;
+                        for (int j = 0; j < nc; ++j) {
+                            cxd acc = 0;
+                            for (int ki = 0; ki < nd; ++ki) acc += conj(v1[ki]) * T[ki * nc + j];
+                            Ao[i * nc + j] += acc;
+                        }
+                    }
+                }
+            }
+        }
+        free(T);
+    }
+}
+
+int orc_mgN_setup(const orc_mgN_setup_params* p, const double* U, double* const* block_vecs, double* const* links,
+                  double* null0) {
+    if (p->n_levels < 2 || p->n_levels > ORC_MAX_LEVELS) return -1;
+    Dirac D = d_make(p->L, U, p->m, p->r, p->csw, p->mu);
+    void* rng = orc_rng_create(p->seed);
+    int nx = p->L, ny = p->L, nd = 2;
+    cxd* lk_prev = NULL; /* operator of the current level l >= 1 */
+    int rc = 0;
+    for (int l = 0; l < p->n_levels - 1 && rc == 0; ++l) {
+        const int ax = p->block[l][0], ay = p->block[l][1], k = p->nvec[l];
+        const int nc = p->chiral_split ? 2 * k : k;
+        const long n = (long)nx * ny * nd;
+        if (ax < 1 || ay < 1 || nx % ax || ny % ay || nx / ax < 3 || ny / ay < 3) {
+            rc = -2;
+            break;
+        }
+        cxd** nv = (cxd**)malloc(sizeof(cxd*) * (size_t)k);
+        double* h = (double*)malloc(sizeof(double) * 2 * (size_t)n);
+        for (int i = 0; i < k; ++i) {
+            orc_rng_random_vec(rng, n, h);
+            nv[i] = to_cx(h, n);
+        }
+        free(h);
+        Coarse A;
+        if (l == 0) {
+            null_space_op(op_ddagd, &D, n, k, p->null_iters, p->null_mr_steps, nv);
+            if (null0)
+                for (int i = 0; i < k; ++i) from_cx(nv[i], n, null0 + 2 * n * i);
+        } else {
+            A.nbx = nx;
+            A.nby = ny;
+            A.k = nd;
+            A.dim = (int)n;
+            A.lk = lk_prev;
+            null_space_op(op_coarse, &A, n, k, p->null_iters, p->null_mr_steps, nv);
+        }
+        cxd* bv = block_vectors(nx, ny, nd, ax, ay, k, p->chiral_split, nv);
+        for (int i = 0; i < k; ++i) free(nv[i]);
+        free(nv);
+        const int cx_ = nx / ax, cy_ = ny / ay;
+        cxd* lk = (cxd*)malloc(sizeof(cxd) * (size_t)cx_ * cy_ * 9 * nc * nc);
+        if (l == 0)
+            galerkin0(&D, ax, ay, nc, bv, lk);
+        else
+            galerkin_c(nx, ny, nd, lk_prev, ax, ay, nc, bv, lk);
+        from_cx(bv, n * nc, block_vecs[l]);
+        from_cx(lk, (long)cx_ * cy_ * 9 * nc * nc, links[l + 1]);
+        free(bv);
+        free(lk_prev);
+        lk_prev = lk;
+        nx = cx_;
+        ny = cy_;
+        nd = nc;
+    }
+    free(lk_prev);
+    orc_rng_destroy(rng);
+    d_free(&D);
+    return rc;
 }

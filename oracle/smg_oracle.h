@@ -89,6 +89,30 @@ void orc_mgN_precondition(const orc_mgN_params* p, const double* U, const double
 int orc_mgN_gcr(const orc_mgN_params* p, const double* U, const double* b, double* x, int max_iter, double tol,
                 int trunc, double* final_res, double* seconds);
 
+/* Hierarchy set-up on the CPU (the reference's build_mg_hierarchy with a
+ * geometric aggregate at every level and direct Galerkin products; see
+ * smg_oracle.c).  block_vecs[l] receives level l's block vectors
+ * [agg][i][loc * ndof_l + j], links[l + 1] level l + 1's operator in the
+ * SparseCoarseOp layout [site][dir][i * nc + j], null0 (optional) the level-0
+ * null vectors; the caller sizes every array.  Returns 0, or < 0 for a bad
+ * geometry. */
+typedef struct {
+    int n_levels, L;
+    double m, r, csw, mu;
+    int block[ORC_MAX_LEVELS - 1][2];
+    int nvec[ORC_MAX_LEVELS - 1];
+    int chiral_split, null_iters, null_mr_steps;
+    uint32_t seed;
+} orc_mgN_setup_params;
+
+int orc_mgN_setup(const orc_mgN_setup_params* p, const double* U, double* const* block_vecs, double* const* links,
+                  double* null0);
+
+/* Seeded inputs (oracle/inputs.cpp): random_vec(n, std::mt19937(seed)) and
+ * links U = exp(i theta), theta ~ N(0, 1/beta). */
+void orc_random_vec(long n, uint32_t seed, double* v);
+void orc_gauge_normal(int L, double beta, uint32_t seed, double* U);
+
 /* CPU timing of the restatement (bench.py's CPU baseline): seconds for `reps`
  * applications of D (op 0) or D^dag D (op 2) to nrhs spinors, and for one CG
  * solve; the operator is set up outside the timed region. */

@@ -171,6 +171,7 @@ _SIGS = {
     "smg_mg_restrict_host": (_st, [_vp, C.c_int, _dp, _dp]),
     "smg_mg_coarse_apply_host": (_st, [_vp, C.c_int, _dp, _dp]),
     "smg_mg_time_coarse_apply": (_st, [_vp, C.c_int, C.c_int, C.c_int, _dp, _dp]),
+    "smg_mg_time_smoother": (_st, [_vp, _vp, C.c_int, _dp, _dp]),
     "smg_mg_coarse_apply_batch": (_st, [_vp, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _dp]),
     "smg_gcr_solve": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(SolveResult)]),
     "smg_cg_solve_precond": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_double, C.POINTER(SolveResult)]),

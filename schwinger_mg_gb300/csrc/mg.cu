@@ -2728,6 +2728,66 @@ SMG_API smg_status smg_mg_time_coarse_apply(smg_mg* mg, int level, int nrhs, int
     return SMG_OK;
 }
 
+// The fine smoother's three kernels of one MR step on FP16 work vectors, each launched `reps`
+// times on the context's stream and timed with CUDA events: [0] t = D r (FP16 -> FP16),
+// [1] Ar = D^dag t with <Ar, r> and ||Ar||^2 fused, [2] x += omega r, r -= omega Ar.  r is
+// made from b (F32, the hierarchy's nrhs); bytes[] are each kernel's compulsory HBM bytes.
+SMG_API smg_status smg_mg_time_smoother(smg_mg* mg, const smg_field* b, int reps, double* ms, double* bytes) {
+    if (!mg || !b || !ms || reps < 1) return SMG_BAD_ARG;
+    smg_context* ctx = mg->ctx;
+    if (b->prec != SMG_F32 || b->g.L != mg->lv[0].nx)
+        return smg_fail(ctx, SMG_BAD_ARG, "smoother timing: b must be an F32 field of the hierarchy's lattice");
+    const int V = b->g.V, nrhs = b->nrhs;
+    if (!half_smoother(mg, nrhs, SMG_F32))
+        return smg_fail(ctx, SMG_UNSUPPORTED, "smoother timing: the hierarchy has no FP16 smoother for this nrhs");
+    SMG_TRY(ensure_work(mg, nrhs, SMG_F32));
+    if (!mg->hdots) return smg_fail(ctx, SMG_UNSUPPORTED, "smoother timing: no fused stencil reductions");
+    smg_field *r = mg->f_r, *Ar = mg->f_Ar, *t = mg->f_t;
+    const dim3 blk(nrhs / 2, 512 / nrhs), grd((V + blk.y - 1) / blk.y);
+    double* sc = lvl_scal(mg, 0);
+    smg_field* x = nullptr;
+    SMG_TRY(smg_field_create(ctx, b->g.L, nrhs, SMG_F32, &x));
+    SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
+    k_sub_h<<<grd, blk, 0, ctx->stream>>>((const cx<float>*)b->data, nullptr, nullptr, (__half2*)r->data, r->scale, V,
+                                          nrhs);
+    count_launch(ctx);
+    cudaEvent_t ev[4];
+    for (auto& e : ev) SMG_CUDA(ctx, cudaEventCreate(&e));
+    smg_status st = SMG_OK;
+    for (int pass = 0; pass < 2 && st == SMG_OK; ++pass) {  // pass 0 warms up
+        SMG_CUDA(ctx, cudaEventRecord(ev[0], ctx->stream));
+        for (int i = 0; i < reps && st == SMG_OK; ++i) st = smg_dslash(mg->dirac, false, r, t, nullptr);
+        SMG_CUDA(ctx, cudaEventRecord(ev[1], ctx->stream));
+        for (int i = 0; i < reps && st == SMG_OK; ++i) st = smg_dslash_h_dots(mg->dirac, t, Ar, r, mg->hdots, sc);
+        SMG_CUDA(ctx, cudaEventRecord(ev[2], ctx->stream));
+        for (int i = 0; i < reps && st == SMG_OK; ++i) {
+            // omega from the last reductions, applied to a copy-free update: r and x drift but stay finite
+            k_smooth_update_h<<<grd, blk, 0, ctx->stream>>>((cx<float>*)x->data, (__half2*)r->data, r->scale,
+                                                            (const __half2*)Ar->data, Ar->scale, sc, 0.f, V, nrhs);
+            count_launch(ctx);
+        }
+        SMG_CUDA(ctx, cudaEventRecord(ev[3], ctx->stream));
+    }
+    SMG_CUDA(ctx, cudaEventSynchronize(ev[3]));
+    for (int k = 0; k < 3; ++k) {
+        float f = 0;
+        SMG_CUDA(ctx, cudaEventElapsedTime(&f, ev[k], ev[k + 1]));
+        ms[k] = (double)f / reps;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    smg_field_destroy(x);
+    SMG_TRY(st);
+    SMG_CHECK_LAUNCH(ctx);
+    if (bytes) {
+        // per site: FP16 two-spinor 8 B per rhs plus a 4 B scale per field; links 2 x 8 B; clover 4 B
+        const double n = (double)V;
+        bytes[0] = n * (16.0 * nrhs + 8 + 16 + 4);            // r in, t out, links, clover
+        bytes[1] = n * (24.0 * nrhs + 12 + 16 + 4);           // t and r (= w) in, Ar out
+        bytes[2] = n * (32.0 * nrhs + 24.0 * nrhs + 12);      // x in and out (FP32); r, Ar in, r out (FP16)
+    }
+    return SMG_OK;
+}
+
 SMG_API smg_status smg_mg_coarse_apply_batch(smg_mg* mg, int level, int nrhs, int engine, const float* in,
                                              const float* w, float* out, double* dots) {
     if (!mg || !in || !out || level < 1 || level >= (int)mg->lv.size() || nrhs < 1 || engine < 0 || engine > 1)

@@ -207,6 +207,42 @@ def gauge_files_case(ref, name, L, beta, mass, gseed):
     print("wrote", name)
 
 
+def sparse_from_dense(A, nx, ny, k):
+    """SparseCoarseOp links [site][dir][i * k + j] of a dense 9-point coarse operator (checked exact)."""
+    dx = [0, 1, -1, 0, 0, 1, 1, -1, -1]
+    dy = [0, 0, 0, 1, -1, 1, -1, 1, -1]
+    lk = np.zeros((nx * ny, 9, k, k), complex)
+    back = np.zeros_like(A)
+    for b in range(nx * ny):
+        bx, by = b % nx, b // nx
+        for d in range(9):
+            nb = (bx + dx[d]) % nx + nx * ((by + dy[d]) % ny)
+            lk[b, d] = A[b * k:(b + 1) * k, nb * k:(nb + 1) * k]
+            back[b * k:(b + 1) * k, nb * k:(nb + 1) * k] += lk[b, d]
+    assert np.max(np.abs(back - A)) <= 1e-14 * np.max(np.abs(A)), "not a 9-point operator"
+    return lk.reshape(-1)
+
+
+def mg3_case(ref, name, L, beta, m, r, csw, mu, gseed, bs, k, null_iters, seed):
+    """Three levels with the reference's default coarse blocking (4k consecutive coarse dofs,
+    CoarseProlongator, src/prolongator.h:149-228) and its dense intermediate operator
+    (src/multigrid.cpp:640-687); W-cycle, 3 + 3 MR steps, dense LU on the coarsest level."""
+    U = gauge_normal(L, beta, gseed).reshape(-1)
+    n = 2 * L * L
+    params = O.RefMGParams(3, bs, k, 0, null_iters, 1, 3, 3, 0)
+    nv, bv1, A1, A2 = ref.mg3_export(U, m, r, csw, mu, params, seed)
+    n1 = L // bs
+    # 4k consecutive dofs of the lexicographic level-1 vector = 4 x 1 aggregates of level-1 sites
+    links2 = sparse_from_dense(A2, n1 // 4, n1, k)
+    fsrc = ref.random_vecs(1, n, seed + 2)
+    pre = ref.mg_precondition(U, m, r, csw, mu, params, seed, fsrc)
+    x, it, res = ref.mg_gcr(U, m, r, csw, mu, params, seed, fsrc, 200, 1e-10, 20)
+    np.savez_compressed(OUT / f"{name}.npz", L=L, beta=beta, m=m, r=r, csw=csw, mu=mu, gseed=gseed, bs=bs, k=k,
+                        null_iters=null_iters, seed=seed, U=U, null_vecs=nv, block_vecs1=bv1, links2=links2,
+                        fine_src=fsrc, mg_precondition=pre, gcr_iters=it, gcr_res=res)
+    print("wrote", name, "gcr iters", it, "res", res)
+
+
 CASES = {
     "dirac_L8_wilson": lambda ref: dirac_case(ref, "dirac_L8_wilson", 8, 2.0, 0.3, 1.0, 0.0, 0.0, 11, 12),
     "dirac_L16_clover_twist": lambda ref: dirac_case(ref, "dirac_L16_clover_twist", 16, 2.0, -0.05, 1.0, 1.0, 0.2,
@@ -227,6 +263,7 @@ CASES = {
     "ms_L16": lambda ref: ms_case(ref, "ms_L16", 16, 4.0, 0.1, 1.0, 1.0, 111, 112),
     "hmc_eo_L8": lambda ref: hmc_eo_case(ref, "hmc_eo_L8", 8, 4.0, 0.1, 1.0, 1.0, 95, 96, 6, 3),
     "delta_L16": lambda ref: delta_case(ref, "delta_L16", 16, 3.0, 0.1, 1.0, 1.0, 0.1, 97, 98, 0.05),
+    "mg3_L48_k4": lambda ref: mg3_case(ref, "mg3_L48_k4", 48, 6.0, -0.05, 1.0, 1.0, 0.0, 121, 4, 4, 5, 122),
 }
 
 

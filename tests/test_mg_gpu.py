@@ -204,3 +204,97 @@ def test_rebuild_f32_cycle_matches_fresh_hierarchy(smg_gpu):
         warm_start=mg.null_vecs_l0)
     a, b = mg.precondition(src), fresh.precondition(src)
     assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-4
+
+
+def test_three_level_reference_blocking_matches_reference(smg_gpu):
+    """The reference's three-level hierarchy (golden mg3_L48_k4): level 2 blocks 4k consecutive level-1
+    dofs (CoarseProlongator, src/prolongator.h:149-228), which is the 4 x 1 aggregate of level-1 sites,
+    with the dense intermediate operator P^dag A_1 P (src/multigrid.cpp:640-687).  The GPU hierarchy is
+    built from the same seed: null vectors, level-1 block vectors, level-2 operator, W-cycle and the
+    reference-coefficient GCR are compared."""
+    d = golden("mg3_L48_k4")
+    lat, g, D = _setup(smg_gpu, d)
+    k = int(d["k"])
+    p = smg_gpu.mg_params(3, int(d["bs"]), k, blocks=[(int(d["bs"]), int(d["bs"])), (4, 1)],
+                          null_iters=int(d["null_iters"]), seed=int(d["seed"]), w_cycle=True, pre_smooth=3,
+                          post_smooth=3, coarse_tol=1e-14, coarse_max_iter=5000)
+    mg = smg_gpu.MGHierarchy(D, p)
+    n1 = int(d["L"]) // int(d["bs"])
+    assert mg.level_dims(2) == (n1 // 4, n1, k)
+    assert _relmax(mg.null_vecs_l0.reshape(-1), d["null_vecs"].reshape(-1)) < 1e-9
+    assert _relmax(mg.prolongator(1), d["block_vecs1"]) < 1e-8
+    assert _relmax(mg.coarse_op(2), d["links2"]) < 1e-8
+    out = mg.precondition(d["fine_src"])
+    ref = d["mg_precondition"]
+    assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < 1e-8
+    r = smg_gpu.fcg_solve_mg(D, lat.ndof, d["fine_src"], mg, 200, 1e-10, 20, reference_coefficient=True)
+    assert r.iterations == int(d["gcr_iters"])
+    assert r.final_residual == pytest.approx(float(d["gcr_res"]), rel=0.05)
+
+
+def test_chiral_coarse_links_match_oracle(smg_gpu, port):
+    """Nc = 16 (8 null vectors split by chirality): the GPU's direct Galerkin links against the oracle's
+    probing build (SparseCoarseOp::build, src/coarse_op.h:241-279) on the GPU's own block vectors, and the
+    whole three-level hierarchy against the oracle's CPU set-up from the same seed."""
+    L = 32
+    U = smg_gpu.gauge_normal(L, 6.0, 4242)
+    lat = smg_gpu.Lattice(L)
+    args = (-0.05, 1.0, 1.0, 0.0)
+    D = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, U), *args)
+    p = smg_gpu.mg_params(3, 4, 8, blocks=[(4, 4), (2, 2)], chiral_split=True, null_iters=2, seed=7)
+    mg = smg_gpu.MGHierarchy(D, p)
+    assert mg.level_dims(1) == (8, 8, 16)
+    bv = mg.prolongator(0)
+    assert _relmax(mg.coarse_op(1), port.sparse_coarse_build(U, *args, 4, 16, bv)) < 1e-12
+    bvs, links, null0 = port.mgN_setup(L, U, *args, [(4, 4), (2, 2)], [8, 8], 2, 7, chiral_split=True)
+    assert _relmax(mg.null_vecs_l0.reshape(-1), null0.reshape(-1)) < 1e-10
+    assert _relmax(bv, bvs[0]) < 1e-10
+    assert _relmax(mg.coarse_op(1), links[1]) < 1e-10
+    assert _relmax(mg.coarse_op(2), links[2]) < 1e-8
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_config2_two_level_chiral_L256(smg_gpu, prec):
+    """The two-level configuration at L = 256 (beta = 6, m = -0.05, c_sw = 1): 4 x 4 aggregates, 8 null
+    vectors split by chirality (16 coarse dofs), 2 inverse iterations, 4 MR steps, coarsest CG <= 50
+    iterations to 5e-2.  Plain FP64 and the FP32 hierarchy inside FP64 defect correction both reach a
+    true FP64 residual of 1e-10; the mixed solve takes at most 15 % more GCR iterations."""
+    L = 256
+    U = smg_gpu.gauge_normal(L, 6.0, 2025)
+    lat = smg_gpu.Lattice(L)
+    D = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, U), -0.05, 1.0, 1.0, 0.0)
+    b = smg_gpu.random_vec(lat.ndof, 2026)
+    its = {}
+    for pr in ("f64", prec):
+        p = smg_gpu.mg_params(2, 4, 8, chiral_split=True, null_iters=2, pre_smooth=4, post_smooth=4, w_cycle=False,
+                              coarse_max_iter=50, coarse_tol=5e-2, precision=pr, seed=2025)
+        mg = smg_gpu.MGHierarchy(D, p)
+        assert mg.level_dims(1) == (64, 64, 16)
+        r = smg_gpu.fcg_solve_mg(D, lat.ndof, b, mg, 1000, 1e-10, 20)
+        assert r.status == 0, r
+        assert r.true_residual < 1e-10
+        its[pr] = r.iterations
+    Ax = D.apply_DdagD(r.solution)
+    assert np.linalg.norm(b - Ax) / np.linalg.norm(b) < 1e-10
+    assert its[prec] <= 1.15 * its["f64"] + 1
+
+
+def test_config2_settings_match_oracle_iterations(smg_gpu, port):
+    """The same settings at L = 64: the GPU's FP64 hierarchy and GCR against the oracle's CPU set-up and
+    GCR from the same seeds (the oracle's GCR stops on the recursive residual)."""
+    L = 64
+    U = smg_gpu.gauge_normal(L, 6.0, 2025)
+    lat = smg_gpu.Lattice(L)
+    args = (-0.05, 1.0, 1.0, 0.0)
+    D = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, U), *args)
+    p = smg_gpu.mg_params(2, 4, 8, chiral_split=True, null_iters=2, pre_smooth=4, post_smooth=4, w_cycle=False,
+                          coarse_max_iter=50, coarse_tol=5e-2, precision="f64", seed=2025)
+    mg = smg_gpu.MGHierarchy(D, p)
+    b = smg_gpu.random_vec(lat.ndof, 2026)
+    r = smg_gpu.fcg_solve_mg(D, lat.ndof, b, mg, 1000, 1e-10, 20)
+    bvs, links, _ = port.mgN_setup(L, U, *args, [(4, 4)], [8], 2, 2025, chiral_split=True)
+    assert _relmax(mg.coarse_op(1), links[1]) < 1e-9
+    po = port.mgN_params(L, *args, [(4, 4)], [16], bvs, links, 4, 4, False, 50, 5e-2)
+    _, it_o, res_o, _ = port.mgN_gcr(po, U, b, 1000, 1e-10, 20)
+    assert r.status == 0 and r.true_residual < 1e-10
+    assert abs(r.iterations - it_o) <= 2

@@ -52,3 +52,30 @@ def test_two_gloo_ranks_reduce_and_shard():
     assert not seeds0 & seeds1
     assert len(seeds0) + len(seeds1) == res[0][3] == 64
     assert abs(len(seeds0) - len(seeds1)) <= 1
+
+
+def test_gpus_flag_starts_ranks_under_torchrun():
+    """`bench.py --gpus 2` outside torchrun relaunches itself with two ranks (127.0.0.1 rendezvous); the
+    reference arm runs on rank 0 alone, which prints the one line with n_gpus = 2."""
+    pytest.importorskip("torch")
+    import json
+    import subprocess
+
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--gpus", "2", "--impl", "reference", "--workload",
+                        "cg", "--steps", "1", "--warmup", "0"], capture_output=True, text=True, timeout=600, env=env,
+                       cwd=str(ROOT))
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["n_gpus"] == 2
+
+
+def test_gpus_flag_refuses_a_mismatched_world():
+    import subprocess
+
+    env = dict(os.environ, WORLD_SIZE="1", RANK="0", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--gpus", "2", "--impl", "reference", "--workload",
+                        "cg", "--steps", "1"], capture_output=True, text=True, timeout=120, env=env, cwd=str(ROOT))
+    assert r.returncode != 0 and "WORLD_SIZE" in (r.stderr + r.stdout)
