@@ -86,6 +86,8 @@ typedef struct smg_dirac smg_dirac;
 typedef struct smg_field smg_field;
 typedef struct smg_mg smg_mg;
 typedef struct smg_batch smg_batch;
+typedef struct smg_prolongator smg_prolongator;
+typedef struct smg_coarse_op smg_coarse_op;
 
 /* Result of a Krylov solve; mirrors CGResult / FCGResult
  * (reference src/solvers.h:25-35).  final_residual is the solver's own
@@ -215,7 +217,11 @@ SMG_API smg_status smg_blas_scale(const double* alpha, smg_field* v);
  * the GPU (different streams, or different host threads on one device) race
  * and must be serialised by the caller.  The first call on each device looks
  * the array's device address up; make that first call before any stream
- * capture. */
+ * capture.  The address is kept for the life of the process: after
+ * cudaDeviceReset (or anything else that re-creates the device's primary
+ * context) it is stale, so do not call this function again in that process.
+ * A launch error that the caller's own earlier work left pending is not
+ * cleared: the call returns SMG_DEVICE_ERROR without launching. */
 SMG_API smg_status smg_blas_dot_noalloc(const double* a, const double* b, int64_t n, int nrhs, double* out,
                                         void* stream);
 
@@ -327,6 +333,14 @@ SMG_API smg_status smg_mg_params_default(smg_mg_params* p);
  * warm_start argument.  Every coarse lattice must be at least 3 x 3. */
 SMG_API smg_status smg_mg_create(smg_dirac* d, const smg_mg_params* p, const double* warm_start,
                                  smg_mg** out);
+/* build_mg_hierarchy with the caller's generator (src/multigrid.cpp:595-687,
+ * src/mg_builder.cpp:3-31): start_vecs[l], l < n_levels - 1, holds the
+ * n_vec[l] start vectors of level l (random_vec draws, each nsites_l *
+ * ndof_l complex: 2V at level 0) in the order the reference draws them from
+ * its std::mt19937, so the hierarchy equals the reference's for the same
+ * generator state; null_iters inverse iterations follow as in smg_mg_create. */
+SMG_API smg_status smg_mg_create_from_starts(smg_dirac* d, const smg_mg_params* p, const double* const* start_vecs,
+                                             smg_mg** out);
 SMG_API smg_status smg_mg_destroy(smg_mg* mg);
 /* ------------------------------------------------------ coarse deflation */
 
@@ -386,6 +400,14 @@ SMG_API smg_status smg_mg_rebuild(smg_mg* mg);
 SMG_API smg_status smg_mg_level_dims(smg_mg* mg, int level, int* nx, int* ny, int* ndof);
 /* MGHierarchy::null_vecs_l0: n_vec[0] vectors of 2V complex. */
 SMG_API smg_status smg_mg_null_vectors(smg_mg* mg, double* out);
+SMG_API smg_status smg_mg_n_null_vectors(smg_mg* mg, int* k);
+/* Failure-path testing, no reference counterpart: the number of polls a
+ * grid-barrier wait of the coarsest-level CG kernel makes before it gives up
+ * (spins >= 0; 0 gives up at the first poll; < 0 restores the default of
+ * about one second).  A wait that gives up ends the kernel and the next call
+ * returns SMG_TIMEOUT (smg_mg_precondition and the solvers check the flag);
+ * the hierarchy stays usable.  Drops the captured cycle graph. */
+SMG_API smg_status smg_mg_set_wait_limit(smg_mg* mg, long long spins);
 /* Block vectors of the prolongator from level `level` to level+1 in the
  * reference layout [block][k][local dof] (src/prolongator.h:23) where a local
  * dof of level 0 is 2*(lx + bx*ly) + spin and of level l >= 1 is
@@ -415,6 +437,38 @@ SMG_API smg_status smg_mg_set_symmetric(smg_mg* mg, double damping, double* omeg
 SMG_API smg_status smg_mg_prolong_host(smg_mg* mg, int level, const double* coarse, double* fine);
 SMG_API smg_status smg_mg_restrict_host(smg_mg* mg, int level, const double* fine, double* coarse);
 SMG_API smg_status smg_mg_coarse_apply_host(smg_mg* mg, int level, const double* in, double* out);
+/* ----------------------------------- prolongator and sparse coarse operator */
+
+/* Prolongator(lat, bx, by, k) + build_from_vectors (src/prolongator.h:14-142):
+ * k null vectors (each 2V complex, reference layout) cut to bx x by blocks and
+ * orthonormalised per block on the device.  L / bx and L / by >= 3. */
+SMG_API smg_status smg_prolongator_create(smg_context* ctx, int L, int bx, int by, int k, const double* null_vecs,
+                                          smg_prolongator** out);
+SMG_API smg_status smg_prolongator_destroy(smg_prolongator* P);
+/* Prolongator::block_vecs in the layout [block][k][2 * (lx + bx * ly) + spin]. */
+SMG_API smg_status smg_prolongator_get_block_vecs(smg_prolongator* P, double* block_vecs);
+/* Prolongator::prolong / restrict_vec (src/prolongator.h:77-108) on host
+ * arrays: fine 2V complex, coarse (L/bx)(L/by) k complex [block][k]. */
+SMG_API smg_status smg_prolongator_prolong(smg_prolongator* P, const double* coarse, double* fine);
+SMG_API smg_status smg_prolongator_restrict(smg_prolongator* P, const double* fine, double* coarse);
+/* SparseCoarseOp::build(P, A = D^dag D) (src/coarse_op.h:241-279): the
+ * 9-point Galerkin operator P^dag D^dag D P, formed directly from D P. */
+SMG_API smg_status smg_coarse_op_create(const smg_prolongator* P, smg_dirac* d, smg_coarse_op** out);
+SMG_API smg_status smg_coarse_op_destroy(smg_coarse_op* A);
+SMG_API smg_status smg_coarse_op_dims(smg_coarse_op* A, int* nbx, int* nby, int* k);
+/* SparseCoarseOp::link, [block][dir][ki * k + kj] (src/coarse_op.h:159-166). */
+SMG_API smg_status smg_coarse_op_get_links(smg_coarse_op* A, double* links);
+/* SparseCoarseOp::apply_to (src/coarse_op.h:282-297) on host arrays. */
+SMG_API smg_status smg_coarse_op_apply(smg_coarse_op* A, const double* in, double* out);
+/* SparseCoarseOp::solve (src/coarse_op.h:492-547): CG to ||r|| / ||b|| < tol
+ * or max_iter iterations, from the deflated guess when deflation pairs are
+ * held (smg_coarse_op_setup_deflation). */
+SMG_API smg_status smg_coarse_op_solve(smg_coarse_op* A, const double* b, double* x, int max_iter, double tol);
+/* SparseCoarseOp::setup_deflation (src/coarse_op.cpp:10-54): TRLM eigenpairs
+ * of the operator (see smg_mg_setup_deflation). */
+SMG_API smg_status smg_coarse_op_setup_deflation(smg_coarse_op* A, int n_ev, int n_kr, int max_restarts, double tol,
+                                                 smg_deflation_info* info);
+
 /* Benchmark support, no reference counterpart: device milliseconds of one
  * application of the level-`level` coarse operator to nrhs right-hand sides
  * in the hierarchy's precision, averaged over `reps` back-to-back
@@ -431,13 +485,14 @@ SMG_API smg_status smg_mg_coarse_apply_host(smg_mg* mg, int level, const double*
 SMG_API smg_status smg_mg_coarse_apply_batch(smg_mg* mg, int level, int nrhs, int engine, const float* in,
                                              const float* w, float* out, double* dots);
 SMG_API smg_status smg_mg_time_coarse_apply(smg_mg* mg, int level, int nrhs, int reps, double* ms, double* bytes);
-/* Timing of the fine smoother's kernels of one MR step (mr_smooth_op,
- * src/smoother.cpp:26-40) on the hierarchy's FP16 work vectors (F32
- * hierarchy with smoother_half): ms[0] t = D r, ms[1] A r = D^dag t with
- * <A r, r> and ||A r||^2 fused, ms[2] the x / r update; each the average of
- * `reps` launches timed with CUDA events on the context's stream after one
- * warm-up pass.  r is formed from b (F32, nrhs a power of two >= 8).
- * bytes[k] (optional): each kernel's compulsory HBM bytes. */
+/* Timing of the fine smoother's kernels (mr_smooth_op, src/smoother.cpp:26-40)
+ * on the hierarchy's FP16 work vectors (F32 hierarchy with smoother_half):
+ * ms[0] t = D r with ||t||^2 fused, ms[1] A r = D^dag t with ||A r||^2 fused
+ * and the MR scalars finished, ms[2] the residual update r' = r - omega A r,
+ * ms[3] the pass that adds omega_k r_k of one smoothing into x; each the
+ * average of `reps` launches timed with CUDA events on the context's stream
+ * after one warm-up pass.  r is formed from b (F32, nrhs a power of two
+ * >= 8).  bytes[k] (optional): each kernel's compulsory HBM bytes. */
 SMG_API smg_status smg_mg_time_smoother(smg_mg* mg, const smg_field* b, int reps, double* ms, double* bytes);
 
 /* fcg_solve / fcg_solve_mg: truncated GCR on A = D^dag D from x = 0
@@ -713,7 +768,9 @@ SMG_API smg_status smg_host_gauge_write_swng(const char* path, int L, const doub
                                              double avg_plaq);
 /* load_gauge: reads the header (SMG_BAD_ARG on a wrong magic, or on an L other
  * than L_expected when L_expected > 0) and, when U != NULL, the links divided
- * by their modulus as the reference does after reading. */
+ * by their modulus as the reference does after reading.  Reading the links
+ * needs L_expected > 0 (U must hold 4 * L_expected^2 doubles); to learn L from
+ * a file, call first with U == NULL and read hdr->L. */
 SMG_API smg_status smg_host_gauge_read_swng(const char* path, int L_expected, smg_gauge_header* hdr, double* U);
 /* GaugeField::save / load (src/gauge.h:38-57): int32 V, then the links. */
 SMG_API smg_status smg_host_gauge_write_raw(const char* path, int L, const double* U);

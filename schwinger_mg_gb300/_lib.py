@@ -172,6 +172,21 @@ _SIGS = {
     "smg_mg_coarse_apply_host": (_st, [_vp, C.c_int, _dp, _dp]),
     "smg_mg_time_coarse_apply": (_st, [_vp, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     "smg_mg_time_smoother": (_st, [_vp, _vp, C.c_int, _dp, _dp]),
+    "smg_mg_create_from_starts": (_st, [_vp, _vp, C.POINTER(_dp), C.POINTER(_vp)]),
+    "smg_mg_n_null_vectors": (_st, [_vp, C.POINTER(C.c_int)]),
+    "smg_mg_set_wait_limit": (_st, [_vp, C.c_longlong]),
+    "smg_prolongator_create": (_st, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, _dp, C.POINTER(_vp)]),
+    "smg_prolongator_destroy": (_st, [_vp]),
+    "smg_prolongator_get_block_vecs": (_st, [_vp, _dp]),
+    "smg_prolongator_prolong": (_st, [_vp, _dp, _dp]),
+    "smg_prolongator_restrict": (_st, [_vp, _dp, _dp]),
+    "smg_coarse_op_create": (_st, [_vp, _vp, C.POINTER(_vp)]),
+    "smg_coarse_op_destroy": (_st, [_vp]),
+    "smg_coarse_op_dims": (_st, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "smg_coarse_op_get_links": (_st, [_vp, _dp]),
+    "smg_coarse_op_apply": (_st, [_vp, _dp, _dp]),
+    "smg_coarse_op_solve": (_st, [_vp, _dp, _dp, C.c_int, C.c_double]),
+    "smg_coarse_op_setup_deflation": (_st, [_vp, C.c_int, C.c_int, C.c_int, C.c_double, _vp]),
     "smg_mg_coarse_apply_batch": (_st, [_vp, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp, _dp]),
     "smg_gcr_solve": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(SolveResult)]),
     "smg_cg_solve_precond": (_st, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_double, C.POINTER(SolveResult)]),

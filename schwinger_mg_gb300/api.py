@@ -680,7 +680,7 @@ def load_gauge(path, L: int = 0):
     _L.check(_L.lib().smg_host_gauge_read_swng(p, L, C.byref(hdr), None), "smg_host_gauge_read_swng")
     n = int(hdr.L)
     U = np.empty(2 * n * n, dtype=np.complex128)
-    _L.check(_L.lib().smg_host_gauge_read_swng(p, L, C.byref(hdr), _ptr(U.view(np.float64))),
+    _L.check(_L.lib().smg_host_gauge_read_swng(p, n, C.byref(hdr), _ptr(U.view(np.float64))),
              "smg_host_gauge_read_swng")
     return U.reshape(2, n * n), dict(L=n, beta=hdr.beta, mass=hdr.mass, avg_plaq=hdr.avg_plaq)
 

@@ -93,6 +93,8 @@ SMG_API smg_status smg_context_destroy(smg_context* ctx) {
     if (!ctx) return SMG_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    for (smg_field* f : ctx->field_pool) smg_field_destroy(f);
+    for (auto& b : ctx->buf_pool) cudaFree(b.second);
     if (ctx->red.partials) cudaFree(ctx->red.partials);
     for (double* p : ctx->retired) cudaFree(p);
     if (ctx->red.tickets) cudaFree(ctx->red.tickets);

@@ -265,8 +265,11 @@ size_t tile_smem(int TY, int nrhs) {
 // ---------------------------------------------------------------- FP16 storage
 //
 // The row kernel with FP16 (per-site scaled) input and/or output fields and FP32
-// arithmetic and links: the MG smoother's work vectors.  A warp holds 32/nrhs
-// sites of nrhs lanes each, so an output site's scale is a shuffle reduction.
+// arithmetic and links: the MG smoother's work vectors.  A thread owns NP pairs of
+// adjacent right-hand sides of one site (2 NP consecutive two-spinors: one 16-byte
+// load per pair and neighbour in FP16), a warp holds 32 / lanes sites of
+// lanes = nrhs / (2 NP) threads, so an output site's scale is a shuffle reduction
+// over its lane group.
 struct DslashH {
     const cx<float>* __restrict__ src32 = nullptr;
     const __half2* __restrict__ src16 = nullptr;
@@ -279,20 +282,17 @@ struct DslashH {
     Geom g{};
     int nrhs = 1;
     float diag = 0, mu_eff = 0, r = 0;
-    // DOTS: <out, w> and ||out||^2 per block and rhs into part[block][rhs][3] (w FP16)
-    const __half2* __restrict__ w16 = nullptr;
-    const float* __restrict__ w_scale = nullptr;
+    // NORM: ||out||^2 per block and rhs into part[(block * nrhs + rhs) * 2 + part_col]
     float* __restrict__ part = nullptr;
+    int part_col = 0;
 };
 
-// thread = right-hand sides rhs + k * lanes (k < NR, lanes = nrhs / NR) of one site: the site's
-// index arithmetic, link, clover and scale loads and the scale folding are shared by its NR
-// right-hand sides, which are processed two at a time
-template <bool DAG, bool IN_H, bool OUT_H, bool R1, bool DOTS = false, int NR = 2>
+template <bool DAG, bool IN_H, bool OUT_H, bool R1, bool NORM, int NP>
 __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
+    constexpr int NR = 2 * NP;
     const Geom g = a.g;
     const int nrhs = a.nrhs, lanes = blockDim.x;
-    const int rhs = threadIdx.x;
+    const int rhs0 = threadIdx.x * NR;
     const int rem = blockIdx.x * blockDim.y + threadIdx.y;
     const int y = blockIdx.y;
     const bool valid = rem < g.L;
@@ -312,98 +312,104 @@ __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
         const int yp = y + 1 == g.L ? 0 : y + 1, ym = y == 0 ? g.L - 1 : y - 1;
         const int q_xp = op + ((xp + g.L * y) >> 1), q_xm = op + ((xm + g.L * y) >> 1);
         const int q_yp = op + ((x + g.L * yp) >> 1), q_ym = op + ((x + g.L * ym) >> 1);
+        Spinor<float> ps[NR], pxp[NR], pxm[NR], pyp[NR], pym[NR];
+        if (IN_H) {
+            ld_pairs_h<NP>(a.src16, q, rhs0, nrhs, ps);
+            ld_pairs_h<NP>(a.src16, q_xp, rhs0, nrhs, pxp);
+            ld_pairs_h<NP>(a.src16, q_xm, rhs0, nrhs, pxm);
+            ld_pairs_h<NP>(a.src16, q_yp, rhs0, nrhs, pyp);
+            ld_pairs_h<NP>(a.src16, q_ym, rhs0, nrhs, pym);
+        } else {
+            ld_pairs_f<NP>(a.src32, q, rhs0, nrhs, ps);
+            ld_pairs_f<NP>(a.src32, q_xp, rhs0, nrhs, pxp);
+            ld_pairs_f<NP>(a.src32, q_xm, rhs0, nrhs, pxm);
+            ld_pairs_f<NP>(a.src32, q_yp, rhs0, nrhs, pyp);
+            ld_pairs_f<NP>(a.src32, q_ym, rhs0, nrhs, pym);
+        }
         // FP16 input: the stored values are read unscaled and each neighbour's site scale is folded
-        // into its link (and the centre's into the diagonal), the operator being linear in each
-        auto ld = [&](int qq, int rr) {
-            return IN_H ? ld_spinor_h_raw(a.src16, qq, rr, nrhs) : ld_spinor(a.src32, qq, rr, nrhs);
-        };
+        // into its link (and the centre's into the diagonal), the operator being linear in each; the
+        // hopping term's 1/2 is folded into the links as well
         cx<float> u0f = a.U[q], u0b = a.U[q_xm], u1f = a.U[g.V + q], u1b = a.U[g.V + q_ym];
         const float Cq = a.C ? a.C[q] : 0.f;
         cx<float> dg0 = mk(a.diag + Cq, a.mu_eff), dg1 = mk(a.diag - Cq, -a.mu_eff);
+        float hxp = 0.5f, hxm = 0.5f, hyp = 0.5f, hym = 0.5f;
         if (IN_H) {
-            const float sq = a.src_scale[q], sxp = a.src_scale[q_xp], sxm = a.src_scale[q_xm];
-            const float syp = a.src_scale[q_yp], sym = a.src_scale[q_ym];
-            u0f = mk(u0f.re * sxp, u0f.im * sxp);
-            u0b = mk(u0b.re * sxm, u0b.im * sxm);
-            u1f = mk(u1f.re * syp, u1f.im * syp);
-            u1b = mk(u1b.re * sym, u1b.im * sym);
+            const float sq = a.src_scale[q];
+            hxp *= a.src_scale[q_xp];
+            hxm *= a.src_scale[q_xm];
+            hyp *= a.src_scale[q_yp];
+            hym *= a.src_scale[q_ym];
             dg0 = mk(dg0.re * sq, dg0.im * sq);
             dg1 = mk(dg1.re * sq, dg1.im * sq);
         }
+        u0f = mk(u0f.re * hxp, u0f.im * hxp);
+        u0b = mk(u0b.re * hxm, u0b.im * hxm);
+        u1f = mk(u1f.re * hyp, u1f.im * hyp);
+        u1b = mk(u1b.re * hym, u1b.im * hym);
 #pragma unroll
-        for (int k0 = 0; k0 < NR; k0 += 2) {
-            Spinor<float> ps[2], pxp[2], pxm[2], pyp[2], pym[2];
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const int rr = rhs + (k0 + k) * lanes;
-                ps[k] = ld(q, rr);
-                pxp[k] = ld(q_xp, rr);
-                pxm[k] = ld(q_xm, rr);
-                pyp[k] = ld(q_yp, rr);
-                pym[k] = ld(q_ym, rr);
-            }
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                cx<float> S0, S1;
-                hop_sum<float, DAG, R1>(u0f, u0b, u1f, u1b, pxp[k], pxm[k], pyp[k], pym[k], a.r, S0, S1);
-                out[k0 + k].s0 = dg0 * ps[k].s0 - 0.5f * S0;
-                out[k0 + k].s1 = dg1 * ps[k].s1 - 0.5f * S1;
-            }
+        for (int k = 0; k < NR; ++k) {
+            cx<float> S0, S1;
+            hop_sum<float, DAG, R1>(u0f, u0b, u1f, u1b, pxp[k], pxm[k], pyp[k], pym[k], a.r, S0, S1);
+            out[k].s0 = dg0 * ps[k].s0 - S0;
+            out[k].s1 = dg1 * ps[k].s1 - S1;
         }
     }
-    if (DOTS) {
-        // <out, w> and ||out||^2 of this block's sites, per rhs, summed over the block's rows in a fixed order
-        __shared__ float s_d[256 * 3 * NR];
-        float v[3 * NR];
+    if (NORM) {
+        // ||out||^2 of this block's sites per rhs: the rows of a warp by shuffles, the warps in shared memory
+        __shared__ float s_n[8][32];
+        float v[NR];
 #pragma unroll
-        for (int k = 0; k < 3 * NR; ++k) v[k] = 0.f;
-        if (valid) {
+        for (int k = 0; k < NR; ++k) v[k] = valid ? norm2(out[k].s0) + norm2(out[k].s1) : 0.f;
 #pragma unroll
-            for (int k = 0; k < NR; ++k) {
-                const Spinor<float> wv = ld_spinor_h(a.w16, a.w_scale, q, rhs + k * lanes, nrhs);
-                const cx<float> c = cmulc(out[k].s0, wv.s0) + cmulc(out[k].s1, wv.s1);
-                v[3 * k] = c.re;
-                v[3 * k + 1] = c.im;
-                v[3 * k + 2] = norm2(out[k].s0) + norm2(out[k].s1);
-            }
+        for (int k = 0; k < NR; ++k)
+            for (int o = lanes; o < 32; o <<= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+        const int warp = (threadIdx.y * lanes + threadIdx.x) >> 5, nw = (blockDim.y * lanes) >> 5;
+        if (((threadIdx.y * lanes) & 31) == 0) {  // the first row of each warp
+#pragma unroll
+            for (int k = 0; k < NR; ++k) s_n[warp][rhs0 + k] = v[k];
         }
-        const int t = threadIdx.y * lanes + rhs;
-#pragma unroll
-        for (int k = 0; k < 3 * NR; ++k) s_d[k * 256 + t] = v[k];
         __syncthreads();
         if (threadIdx.y == 0) {
-            float acc[3 * NR];
-#pragma unroll
-            for (int k = 0; k < 3 * NR; ++k) acc[k] = 0.f;
-            for (int row = 0; row < (int)blockDim.y; ++row)
-#pragma unroll
-                for (int k = 0; k < 3 * NR; ++k) acc[k] += s_d[k * 256 + row * lanes + rhs];
-            float* pp = a.part + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * nrhs * 3;
+            float* pp = a.part + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * nrhs * 2 + a.part_col;
 #pragma unroll
             for (int k = 0; k < NR; ++k) {
-                pp[3 * (rhs + k * lanes)] = acc[3 * k];
-                pp[3 * (rhs + k * lanes) + 1] = acc[3 * k + 1];
-                pp[3 * (rhs + k * lanes) + 2] = acc[3 * k + 2];
+                float t = 0.f;
+                for (int w = 0; w < nw; ++w) t += s_n[w][rhs0 + k];
+                pp[2 * (rhs0 + k)] = t;
             }
         }
     }
     if (OUT_H) {
-        st_spinorN_h<NR>(a.dst16, a.dst_scale, q, rhs, nrhs, lanes, out, valid);
+        st_pairs_h<NP>(a.dst16, a.dst_scale, q, rhs0, nrhs, lanes, out, valid);
     } else if (valid) {
+        float4* pd = reinterpret_cast<float4*>(a.dst32) + ((int64_t)q * nrhs + rhs0);
 #pragma unroll
-        for (int k = 0; k < NR; ++k) st_spinor(a.dst32, q, rhs + k * lanes, nrhs, out[k]);
+        for (int k = 0; k < NR; ++k) pd[k] = make_float4(out[k].s0.re, out[k].s0.im, out[k].s1.re, out[k].s1.im);
     }
 }
 
-// right-hand sides per thread of the FP16 stencil launches: two.  Four per thread (NR = 4) were
-// measured at L = 512, 32 RHS: the plain stencil unchanged (57.0 against 57.2 us), the one with the
-// fused MR reductions slower (95 against 81 us, more registers and shared memory per block).
-int dslash_h_nr(int) { return 2; }
+// right-hand-side pairs per thread of the FP16 stencil launches
+int dslash_h_np(int nrhs) {
+    static const int env = [] {
+        const char* e = std::getenv("SMG_DSLASH_H_NP");
+        return e ? std::atoi(e) : 0;
+    }();
+    const int np = env == 1 || env == 2 ? env : 1;
+    return nrhs >= 4 * np ? np : 1;
+}
 
-// Sums of the stencil blocks' partials part[block][j] (j = rhs * 3 + k < ncol <= 96) in FP64 and a
-// fixed order, in two passes: block g of the first sums the contiguous rows [g R, g R + R) with
-// threads (row group, column j) and kDotsRows independent loads per thread; the second pass sums
-// the per-block results of one column per block.
+struct HLaunch {
+    dim3 grid, block;
+};
+HLaunch dslash_h_launch(int L, int nrhs) {
+    const int np = dslash_h_np(nrhs), lanes = nrhs / (2 * np), rows = 256 / lanes;
+    return {dim3((L + rows - 1) / rows, L), dim3(lanes, rows)};
+}
+
+// Sums of the stencil blocks' partials part[block][j] (j < ncol <= 96) in FP64 and a fixed order, in
+// two passes: block g of the first sums the contiguous rows [g R, g R + R) with threads (row group,
+// column j) and kDotsRows independent loads per thread; the second pass sums the per-block results
+// of one column per block.
 constexpr int kDotsRows = 8;  // rows per thread in the first pass
 __global__ void __launch_bounds__(256) k_dots_stage(const float* __restrict__ part, int nblocks, int ncol, int R,
                                                     double* __restrict__ mid) {
@@ -432,9 +438,12 @@ __global__ void __launch_bounds__(256) k_dots_stage(const float* __restrict__ pa
     }
 }
 
-__global__ void __launch_bounds__(256) k_dots_finish(const double* __restrict__ mid, int G, double* __restrict__ out) {
+// the MR step's reductions per rhs from the two norm columns: out[3 rhs] = ||D r||^2 (= <A r, r> for
+// A = D^dag D), out[3 rhs + 1] = 0, out[3 rhs + 2] = ||A r||^2
+__global__ void __launch_bounds__(256) k_mr_norms_finish(const double* __restrict__ mid, int G,
+                                                         double* __restrict__ out) {
     __shared__ double s[256];
-    const int j = blockIdx.x;
+    const int j = blockIdx.x;  // column: rhs * 2 + which
     double acc = 0.0;
     for (int g = threadIdx.x; g < G; g += blockDim.x) acc += mid[(int64_t)j * G + g];
     s[threadIdx.x] = acc;
@@ -443,10 +452,18 @@ __global__ void __launch_bounds__(256) k_dots_finish(const double* __restrict__ 
         if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[j] = s[0];
+    if (threadIdx.x == 0) {
+        const int rhs = j >> 1;
+        if (j & 1) {
+            out[3 * rhs + 2] = s[0];
+        } else {
+            out[3 * rhs] = s[0];
+            out[3 * rhs + 1] = 0.0;
+        }
+    }
 }
 
-smg_status launch_dslash_h(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst) {
+smg_status launch_dslash_h(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, float* part, int part_col) {
     smg_context* ctx = src->ctx;
     const int nrhs = src->nrhs;
     if (!f16_nrhs_ok(nrhs) || nrhs < 2)
@@ -475,21 +492,33 @@ smg_status launch_dslash_h(smg_dirac* d, bool dag, const smg_field* src, smg_fie
     a.diag = (float)(2.0 * d->r + d->mass);
     a.mu_eff = (float)(dag ? -d->mu_t : d->mu_t);
     a.r = (float)d->r;
-    const int nr = dslash_h_nr(nrhs), lanes = nrhs / nr, rows = 256 / lanes;
-    const dim3 block(lanes, rows), grid((a.g.L + rows - 1) / rows, a.g.L);
-#define SMG_DH(DG, I, O)                                                                     \
-    do {                                                                                     \
-        if (d->r == 1.0) k_dslash_h<DG, I, O, true><<<grid, block, 0, ctx->stream>>>(a);   \
-        else k_dslash_h<DG, I, O, false><<<grid, block, 0, ctx->stream>>>(a);             \
+    a.part = part;
+    a.part_col = part_col;
+    const bool norm = part != nullptr;
+    if (norm && !(ih && oh)) return smg_fail(ctx, SMG_UNSUPPORTED, "fused FP16 stencil norm: F16 fields");
+    const HLaunch hl = dslash_h_launch(a.g.L, nrhs);
+    const int np = dslash_h_np(nrhs);
+#define SMG_DH(DG, I, O, N)                                                                                         \
+    do {                                                                                                            \
+        if (np == 2) {                                                                                              \
+            if (d->r == 1.0) k_dslash_h<DG, I, O, true, N, 2><<<hl.grid, hl.block, 0, ctx->stream>>>(a);           \
+            else k_dslash_h<DG, I, O, false, N, 2><<<hl.grid, hl.block, 0, ctx->stream>>>(a);                     \
+        } else {                                                                                                    \
+            if (d->r == 1.0) k_dslash_h<DG, I, O, true, N, 1><<<hl.grid, hl.block, 0, ctx->stream>>>(a);           \
+            else k_dslash_h<DG, I, O, false, N, 1><<<hl.grid, hl.block, 0, ctx->stream>>>(a);                     \
+        }                                                                                                           \
     } while (0)
-    if (dag) {
-        if (ih && oh) SMG_DH(true, true, true);
-        else if (ih) SMG_DH(true, true, false);
-        else SMG_DH(true, false, true);
+    if (norm) {
+        if (dag) SMG_DH(true, true, true, true);
+        else SMG_DH(false, true, true, true);
+    } else if (dag) {
+        if (ih && oh) SMG_DH(true, true, true, false);
+        else if (ih) SMG_DH(true, true, false, false);
+        else SMG_DH(true, false, true, false);
     } else {
-        if (ih && oh) SMG_DH(false, true, true);
-        else if (ih) SMG_DH(false, true, false);
-        else SMG_DH(false, false, true);
+        if (ih && oh) SMG_DH(false, true, true, false);
+        else if (ih) SMG_DH(false, true, false, false);
+        else SMG_DH(false, false, true, false);
     }
 #undef SMG_DH
     count_launch(ctx);
@@ -497,49 +526,22 @@ smg_status launch_dslash_h(smg_dirac* d, bool dag, const smg_field* src, smg_fie
     return SMG_OK;
 }
 
-// blocks of the FP16 stencil's grid (the size of the partial-sum buffer of the fused dot/norm)
+// blocks of the FP16 stencil's grid (the size of the partial-sum buffer of the fused norms)
 int dslash_h_blocks(int L, int nrhs) {
-    const int rows = 256 / (nrhs / dslash_h_nr(nrhs));
-    return ((L + rows - 1) / rows) * L;
+    const HLaunch hl = dslash_h_launch(L, nrhs);
+    return (int)(hl.grid.x * hl.grid.y);
 }
 
-// Ar = D^dag t on FP16 fields with <Ar, w>, ||Ar||^2 per rhs into out3 [rhs][3] (the MR step's
-// reductions fused into the stencil; part holds dslash_h_blocks * nrhs * 3 floats)
-smg_status launch_dslash_h_dots(smg_dirac* d, const smg_field* src, smg_field* dst, const smg_field* w, float* part,
-                                double* out3) {
-    smg_context* ctx = src->ctx;
-    const int nrhs = src->nrhs;
-    if (src->prec != SMG_F16 || dst->prec != SMG_F16 || w->prec != SMG_F16 || !f16_nrhs_ok(nrhs) || nrhs < 2)
-        return smg_fail(ctx, SMG_UNSUPPORTED, "fused FP16 stencil reductions: F16 fields, nrhs a power of two");
-    if (!d->gauge->U32) return smg_fail(ctx, SMG_DEVICE_ERROR, "FP32 links missing");
-    DslashH a;
-    a.src16 = (const __half2*)src->data;
-    a.src_scale = src->scale;
-    a.dst16 = (__half2*)dst->data;
-    a.dst_scale = dst->scale;
-    a.w16 = (const __half2*)w->data;
-    a.w_scale = w->scale;
-    a.part = part;
-    a.U = d->gauge->U32;
-    a.C = d->C32;
-    a.g = src->g;
-    a.nrhs = nrhs;
-    a.diag = (float)(2.0 * d->r + d->mass);
-    a.mu_eff = (float)(-d->mu_t);
-    a.r = (float)d->r;
-    const int nr = dslash_h_nr(nrhs), lanes = nrhs / nr, rows = 256 / lanes;
-    const dim3 block(lanes, rows), grid((a.g.L + rows - 1) / rows, a.g.L);
-    if (d->r == 1.0)
-        k_dslash_h<true, true, true, true, true><<<grid, block, 0, ctx->stream>>>(a);
-    else
-        k_dslash_h<true, true, true, false, true><<<grid, block, 0, ctx->stream>>>(a);
-    const int ncol = nrhs * 3, nblocks = (int)(grid.x * grid.y);
+// the MR step's scalars from the norm partials of its two stencils (columns 0 and 1 of part):
+// out3[rhs][3] = (||D r||^2, 0, ||D^dag D r||^2)
+smg_status launch_mr_norms_finish(smg_context* ctx, int L, int nrhs, const float* part, double* out3) {
+    const int ncol = nrhs * 2, nblocks = dslash_h_blocks(L, nrhs);
     const int groups = 256 / ncol, R = groups * kDotsRows;  // rows per first-pass block
     const int G = (nblocks + R - 1) / R;
     SMG_TRY(smg_reduce_reserve(ctx, (size_t)G * ncol));
     k_dots_stage<<<G, groups * ncol, 0, ctx->stream>>>(part, nblocks, ncol, R, ctx->red.partials);
-    k_dots_finish<<<ncol, 256, 0, ctx->stream>>>(ctx->red.partials, G, out3);
-    count_launch(ctx, 3);
+    k_mr_norms_finish<<<ncol, 256, 0, ctx->stream>>>(ctx->red.partials, G, out3);
+    count_launch(ctx, 2);
     SMG_CHECK_LAUNCH(ctx);
     return SMG_OK;
 }
@@ -849,7 +851,7 @@ smg_status dslash_dispatch(smg_dirac* d, bool dag, int epi, const smg_field* src
                            double* out_dev) {
     if (src->prec == SMG_F16 || dst->prec == SMG_F16) {
         if (epi != EPI_NONE) return smg_fail(src->ctx, SMG_UNSUPPORTED, "fused reductions on F16 fields");
-        return launch_dslash_h(d, dag, src, dst);
+        return launch_dslash_h(d, dag, src, dst, nullptr, 0);
     }
     if (src->prec != dst->prec) return smg_fail(src->ctx, SMG_BAD_ARG, "dslash between F32 and F64 fields");
     if (src->prec == SMG_F64) return launch_dslash<double>(d, dag, epi, src, dst, w, out_dev);
@@ -891,14 +893,18 @@ smg_status smg_dslash_mr(smg_dirac* d, bool dag, const smg_field* src, smg_field
                          double* out3_dev) {
     return dslash_dispatch(d, dag, EPI_MR, src, dst, w, out3_dev);
 }
-smg_status smg_dslash_h_dots(smg_dirac* d, const smg_field* src, smg_field* dst, const smg_field* w, float* part,
-                             double* out3_dev) {
-    return launch_dslash_h_dots(d, src, dst, w, part, out3_dev);
+// FP16 stencil with ||out||^2 per block and rhs into part column part_col (see k_dslash_h)
+smg_status smg_dslash_h_norm(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, float* part,
+                             int part_col) {
+    return launch_dslash_h(d, dag, src, dst, part, part_col);
+}
+smg_status smg_mr_norms_finish(smg_context* ctx, int L, int nrhs, const float* part, double* out3_dev) {
+    return launch_mr_norms_finish(ctx, L, nrhs, part, out3_dev);
 }
 int smg_dslash_h_blocks(int L, int nrhs) { return dslash_h_blocks(L, nrhs); }
-// reduction scratch (doubles) the fused FP16 stencil reductions use for a lattice and nrhs
+// reduction scratch (doubles) the fused FP16 stencil norms use for a lattice and nrhs
 size_t smg_dslash_h_dots_scratch(int L, int nrhs) {
-    const int ncol = nrhs * 3, R = (256 / ncol) * kDotsRows;
+    const int ncol = nrhs * 2, R = (256 / ncol) * kDotsRows;
     return (size_t)((dslash_h_blocks(L, nrhs) + R - 1) / R) * ncol;
 }
 

@@ -208,6 +208,41 @@ smg_status smg_field_alloc_like(const smg_field* proto, smg_precision prec, smg_
     return smg_field_create(proto->ctx, proto->g.L, proto->nrhs, prec, out);
 }
 
+smg_status smg_field_take(const smg_field* proto, smg_precision prec, smg_field** out) {
+    smg_context* ctx = proto->ctx;
+    auto& pool = ctx->field_pool;
+    for (size_t i = 0; i < pool.size(); ++i) {
+        smg_field* f = pool[i];
+        if (f->g.L == proto->g.L && f->nrhs == proto->nrhs && f->prec == prec) {
+            pool.erase(pool.begin() + (std::ptrdiff_t)i);
+            *out = f;
+            return SMG_OK;
+        }
+    }
+    return smg_field_create(ctx, proto->g.L, proto->nrhs, prec, out);
+}
+
+void smg_field_give(smg_field* f) {
+    if (f) f->ctx->field_pool.push_back(f);
+}
+
+smg_status smg_buf_take(smg_context* ctx, size_t bytes, void** out) {
+    auto& pool = ctx->buf_pool;
+    for (size_t i = 0; i < pool.size(); ++i) {
+        if (pool[i].first == bytes) {
+            *out = pool[i].second;
+            pool.erase(pool.begin() + (std::ptrdiff_t)i);
+            return SMG_OK;
+        }
+    }
+    SMG_CUDA(ctx, cudaMalloc(out, bytes));
+    return SMG_OK;
+}
+
+void smg_buf_give(smg_context* ctx, size_t bytes, void* p) {
+    if (p) ctx->buf_pool.emplace_back(bytes, p);
+}
+
 // Reduction helpers used by the solvers (results stay on the device).
 smg_status smg_dot_dev(const smg_field* a, const smg_field* b, double* out_dev) {
     SMG_TRY(smg_field_check_pair(a, b));

@@ -103,6 +103,9 @@ SMG_API smg_status smg_host_gauge_read_swng(const char* path, int L_expected, sm
     if (hdr->magic != kMagic) return SMG_BAD_ARG;              // "Bad magic number"
     if (L_expected > 0 && (int)hdr->L != L_expected) return SMG_BAD_ARG;  // "Lattice size mismatch"
     if (!U) return SMG_OK;
+    // the links are written only when the caller stated the size its buffer was made for: an L taken
+    // from the file alone could overrun it
+    if (L_expected <= 0) return SMG_BAD_ARG;
     if (hdr->L < 2 || hdr->L > 65536) return SMG_BAD_ARG;
     const int64_t n = (int64_t)4 * hdr->L * hdr->L;
     if (read_links(fl.f, n, U) != SMG_OK) return SMG_IO_ERROR;

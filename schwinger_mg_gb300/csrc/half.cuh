@@ -102,5 +102,71 @@ __device__ __forceinline__ void st_spinorN_h(__half2* __restrict__ f, float* __r
     if ((threadIdx.x & (lanes - 1)) == 0) scale[q] = m;
 }
 
+// ---- pairs of adjacent right-hand sides: one 16-byte access per pair (2 two-spinors) and site.
+// 2 NP two-spinors of right-hand sides rhs0 .. rhs0 + 2 NP - 1 of site q
+template <int NP>
+__device__ __forceinline__ void ld_pairs_h(const __half2* __restrict__ f, int64_t q, int rhs0, int nrhs,
+                                           Spinor<float> (&o)[2 * NP]) {
+    const uint4* p = reinterpret_cast<const uint4*>(f) + ((q * nrhs + rhs0) >> 1);
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        const uint4 v = __ldg(p + k);
+        const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&v.x));
+        const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&v.y));
+        const float2 c = __half22float2(*reinterpret_cast<const __half2*>(&v.z));
+        const float2 d = __half22float2(*reinterpret_cast<const __half2*>(&v.w));
+        o[2 * k].s0 = mk(a.x, a.y);
+        o[2 * k].s1 = mk(b.x, b.y);
+        o[2 * k + 1].s0 = mk(c.x, c.y);
+        o[2 * k + 1].s1 = mk(d.x, d.y);
+    }
+}
+
+template <int NP>
+__device__ __forceinline__ void ld_pairs_f(const cx<float>* __restrict__ f, int64_t q, int rhs0, int nrhs,
+                                           Spinor<float> (&o)[2 * NP]) {
+    const float4* p = reinterpret_cast<const float4*>(f) + (q * nrhs + rhs0);
+#pragma unroll
+    for (int k = 0; k < 2 * NP; ++k) {
+        const float4 v = __ldg(p + k);
+        o[k].s0 = mk(v.x, v.y);
+        o[k].s1 = mk(v.z, v.w);
+    }
+}
+
+__device__ __forceinline__ unsigned pack_h2(float a, float b) {
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const unsigned*>(&h);
+}
+
+// Stores 2 NP two-spinors of one site as FP16 with the site's scale (largest |re| or |im| over all
+// its right-hand sides, reduced over the site's `lanes` threads); every thread of the warp calls it.
+template <int NP>
+__device__ __forceinline__ void st_pairs_h(__half2* __restrict__ f, float* __restrict__ scale, int64_t q, int rhs0,
+                                           int nrhs, int lanes, const Spinor<float> (&v)[2 * NP], bool valid) {
+    float m = 0.f;
+    if (valid) {
+#pragma unroll
+        for (int k = 0; k < 2 * NP; ++k)
+            m = fmaxf(m, fmaxf(fmaxf(fabsf(v[k].s0.re), fabsf(v[k].s0.im)), fmaxf(fabsf(v[k].s1.re), fabsf(v[k].s1.im))));
+    }
+    for (int o = lanes >> 1; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o, lanes));
+    if (!valid) return;
+    const float inv = m > 0.f ? __fdividef(1.0f, m) : 0.f;  // fast reciprocal: FP16 rounding dominates
+    uint4* p = reinterpret_cast<uint4*>(f) + ((q * nrhs + rhs0) >> 1);
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        const Spinor<float>& a = v[2 * k];
+        const Spinor<float>& b = v[2 * k + 1];
+        uint4 h;
+        h.x = pack_h2(a.s0.re * inv, a.s0.im * inv);
+        h.y = pack_h2(a.s1.re * inv, a.s1.im * inv);
+        h.z = pack_h2(b.s0.re * inv, b.s0.im * inv);
+        h.w = pack_h2(b.s1.re * inv, b.s1.im * inv);
+        p[k] = h;
+    }
+    if ((threadIdx.x & (lanes - 1)) == 0) scale[q] = m;
+}
+
 // nrhs values whose sites can be written as F16 (one site per power-of-two lane group)
 inline bool f16_nrhs_ok(int nrhs) { return nrhs >= 1 && nrhs <= 32 && (nrhs & (nrhs - 1)) == 0; }

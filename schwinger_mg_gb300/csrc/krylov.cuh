@@ -20,15 +20,32 @@ __global__ void k_residual(const cx<T>* __restrict__ b, const cx<T>* __restrict_
     if (i < n) r[i] = b[i] - Ax[i];
 }
 
+// a solver's work fields, taken from the context's pool and given back when the solver returns
 struct FieldSet {
     std::vector<smg_field*> f;
     ~FieldSet() {
-        for (auto* p : f) smg_field_destroy(p);
+        for (auto* p : f) smg_field_give(p);
     }
-    smg_status add(const smg_field* proto, smg_field** out) {
-        SMG_TRY(smg_field_alloc_like(proto, proto->prec, out));
+    smg_status add(const smg_field* proto, smg_field** out) { return add(proto, proto->prec, out); }
+    smg_status add(const smg_field* proto, smg_precision prec, smg_field** out) {
+        SMG_TRY(smg_field_take(proto, prec, out));
         f.push_back(*out);
         return SMG_OK;
+    }
+};
+
+// a device buffer from the context's pool for the life of a solve
+struct PoolBuf {
+    smg_context* ctx = nullptr;
+    size_t bytes = 0;
+    void* p = nullptr;
+    ~PoolBuf() {
+        if (ctx) smg_buf_give(ctx, bytes, p);
+    }
+    smg_status take(smg_context* c, size_t b) {
+        ctx = c;
+        bytes = b;
+        return smg_buf_take(c, b, &p);
     }
 };
 

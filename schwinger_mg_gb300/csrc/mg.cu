@@ -36,8 +36,9 @@
 smg_status smg_dslash(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, double* norm2_dev);
 smg_status smg_dslash_mr(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, const smg_field* w,
                          double* out3_dev);
-smg_status smg_dslash_h_dots(smg_dirac* d, const smg_field* src, smg_field* dst, const smg_field* w, float* part,
-                             double* out3_dev);
+smg_status smg_dslash_h_norm(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, float* part,
+                             int part_col);
+smg_status smg_mr_norms_finish(smg_context* ctx, int L, int nrhs, const float* part, double* out3_dev);
 int smg_dslash_h_blocks(int L, int nrhs);
 size_t smg_dslash_h_dots_scratch(int L, int nrhs);
 // tensor-core coarse apply (coarse_tc.cu)
@@ -794,11 +795,14 @@ struct CoarseCgArgs {
     unsigned int* bar = nullptr;   // [0] arrivals, [1] generation
     int* err = nullptr;            // 0 ok, 1 barrier timeout
     int* iters = nullptr;          // iterations done (written by block 0)
+    long long spin_limit = 0;      // polls of a barrier wait before it gives up and raises err
 };
 
 constexpr long long kBarrierSpinLimit = 1ll << 22;  // x 256 ns sleep ~ 1 s
 
-__device__ __forceinline__ bool grid_barrier(unsigned int* bar, int* err) {
+// a grid-wide barrier of a co-resident (cooperative) grid; a wait polls at most spin_limit times
+// (spin_limit 0: it gives up at the first poll), then raises *err and the block returns false
+__device__ __forceinline__ bool grid_barrier(unsigned int* bar, int* err, long long spin_limit) {
     __syncthreads();
     __shared__ int s_ok;
     if (threadIdx.x == 0) {
@@ -818,7 +822,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* bar, int* err) {
             } else {
                 long long k = 0;
                 while (*vgen == gen) {
-                    if (*verr || ++k > kBarrierSpinLimit) {
+                    if (*verr || ++k > spin_limit) {
                         atomicExch(err, 1);
                         ok = 0;
                         break;
@@ -893,7 +897,7 @@ __global__ void __launch_bounds__(256) k_coarse_cg1(CoarseCgArgs a) {
     }
     double loc = block_sum256((double)loc_t);
     if (threadIdx.x == 0) part1[blockIdx.x] = loc;
-    if (!grid_barrier(a.bar, a.err)) return;
+    if (!grid_barrier(a.bar, a.err, a.spin_limit)) return;
     double rr = sum_partials(part1);
     const double bnorm2 = rr;
     int it = 0;
@@ -920,7 +924,7 @@ __global__ void __launch_bounds__(256) k_coarse_cg1(CoarseCgArgs a) {
         }
         double pap = block_sum256((double)pap_t);
         if (threadIdx.x == 0) part0[blockIdx.x] = pap;
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!grid_barrier(a.bar, a.err, a.spin_limit)) return;
         pap = sum_partials(part0);
         if (!(fabs(pap) >= 1e-30) || !isfinite(pap)) break;  // coarse_op.h:522
         const T al = (T)(rr / pap);
@@ -933,14 +937,14 @@ __global__ void __launch_bounds__(256) k_coarse_cg1(CoarseCgArgs a) {
         }
         double rloc = block_sum256((double)rloc_t);
         if (threadIdx.x == 0) part1[blockIdx.x] = rloc;
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!grid_barrier(a.bar, a.err, a.spin_limit)) return;
         const double rr_new = sum_partials(part1);
         ++it;
         if (!isfinite(rr_new) || rr_new < a.tol2 * bnorm2) break;  // coarse_op.h:531-536
         const T be = (T)(rr_new / rr);
         rr = rr_new;
         for (int e = t0; e < n; e += stride) p[e] = r[e] + be * p[e];
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!grid_barrier(a.bar, a.err, a.spin_limit)) return;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) *a.iters = it;
 }
@@ -1085,7 +1089,13 @@ struct smg_mg {
     int work_nrhs = 0;
     smg_precision work_prec = SMG_F64;
     smg_field *f_r = nullptr, *f_Ar = nullptr, *f_t = nullptr;  // fine MR temps
-    float* hdots = nullptr;  // per-block partial sums of the FP16 smoother's fused reductions
+    // FP16 smoother: residuals r_0 .. r_n of one smoothing (f_r aliases f_rs[0]), the field that
+    // holds the last smoothing's final residual, the norm partials of its stencils and every step's
+    // MR scalars [step][rhs][3]
+    std::vector<smg_field*> f_rs;
+    smg_field* f_res = nullptr;
+    float* hdots = nullptr;
+    double* mr_om = nullptr;
     std::vector<CoarseWork> cw;
     double* scal = nullptr;  // per-level scalar area
     size_t scal_doubles = 0;
@@ -1100,10 +1110,13 @@ struct smg_mg {
     uint64_t g_work_gen = 0; // workspace generation the graph was captured with
     // persistent coarsest CG: barrier words, error flag, iteration count, partials
     bool persistent = true;
+    long long spin_limit = kBarrierSpinLimit;  // the grid barrier's wait bound (smg_mg_set_wait_limit)
     void* cg_state = nullptr;  // [0..1] barrier, [2] err, [3] iters (ints), doubles from byte 256
     // eigenpairs of the level-1 operator: the deflated initial guess of the coarsest CG when level 1
     // is the coarsest level, and the low-mode projector of the multi-timescale HMC
     MgDeflation defl;
+    // during set-up only: caller-drawn start vectors per level (smg_mg_create_from_starts)
+    const double* const* starts = nullptr;
 };
 
 namespace {
@@ -1301,12 +1314,17 @@ smg_status level_apply_fine(smg_mg* mg, smg_field* x, smg_field* y, const smg_fi
 double* lvl_scal(smg_mg* mg, int l) { return mg->scal + (size_t)l * 16 * mg->work_nrhs + 64; }
 
 smg_status free_work(smg_mg* mg) {
-    smg_field_destroy(mg->f_r);
+    if (mg->f_rs.empty()) smg_field_destroy(mg->f_r);  // else f_r is f_rs[0]
+    for (smg_field* f : mg->f_rs) smg_field_destroy(f);
+    mg->f_rs.clear();
+    mg->f_res = nullptr;
     smg_field_destroy(mg->f_Ar);
     smg_field_destroy(mg->f_t);
     mg->f_r = mg->f_Ar = mg->f_t = nullptr;
     if (mg->hdots) cudaFree(mg->hdots);
     mg->hdots = nullptr;
+    if (mg->mr_om) cudaFree(mg->mr_om);
+    mg->mr_om = nullptr;
     for (auto& w : mg->cw) {
         for (void* p : {w.b, w.x, w.r, w.Ar, w.e, w.p})
             if (p) cudaFree(p);
@@ -1354,6 +1372,7 @@ smg_status coarse_cg_persistent(smg_mg* mg, int l, void* x, const void* b) {
     a.err = reinterpret_cast<int*>(st) + 2;
     a.iters = reinterpret_cast<int*>(st) + 3;
     a.part = reinterpret_cast<double*>(st + 256);
+    a.spin_limit = mg->spin_limit;
     // barrier words back to zero; a raised error flag stays raised until read
     SMG_CUDA(ctx, cudaMemsetAsync(st, 0, 2 * sizeof(unsigned int), ctx->stream));
     void* args[] = {&a};
@@ -1378,13 +1397,20 @@ smg_status ensure_work(smg_mg* mg, int nrhs, smg_precision prec) {
     free_work(mg);
     const int L = mg->lv[0].nx;
     const smg_precision wp = half_smoother(mg, nrhs, prec) ? SMG_F16 : prec;
-    SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &mg->f_r));
+    if (wp == SMG_F16) {
+        const int nsteps = std::max(1, std::max(mg->p.pre_smooth, mg->p.post_smooth));
+        mg->f_rs.assign(nsteps + 1, nullptr);
+        for (auto& f : mg->f_rs) SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &f));
+        mg->f_r = mg->f_rs[0];
+        SMG_CUDA(ctx, cudaMalloc(&mg->hdots, (size_t)smg_dslash_h_blocks(L, nrhs) * nrhs * 2 * sizeof(float)));
+        SMG_CUDA(ctx, cudaMalloc(&mg->mr_om, (size_t)nsteps * 3 * nrhs * sizeof(double)));
+        SMG_CUDA(ctx, cudaMemsetAsync(mg->mr_om, 0, (size_t)nsteps * 3 * nrhs * sizeof(double), ctx->stream));
+        SMG_TRY(smg_reduce_reserve(ctx, smg_dslash_h_dots_scratch(L, nrhs)));  // before any capture
+    } else {
+        SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &mg->f_r));
+    }
     SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &mg->f_Ar));
     SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &mg->f_t));
-    if (wp == SMG_F16) {
-        SMG_CUDA(ctx, cudaMalloc(&mg->hdots, (size_t)smg_dslash_h_blocks(L, nrhs) * nrhs * 3 * sizeof(float)));
-        SMG_TRY(smg_reduce_reserve(ctx, smg_dslash_h_dots_scratch(L, nrhs)));  // before any capture
-    }
     size_t es = prec == SMG_F64 ? sizeof(cx<double>) : sizeof(cx<float>);
     mg->cw.resize(mg->lv.size());
     for (size_t l = 1; l < mg->lv.size(); ++l) {
@@ -1446,147 +1472,167 @@ __global__ void __launch_bounds__(256) k_sub_h(const cx<float>* __restrict__ b, 
     st_spinor2_h(r, rs, s, rhs, nrhs, lanes, v[0], v[1], valid);
 }
 
-// MR (sc = [rhs][3] <Ar, r>, ||Ar||^2) or Richardson (fixed omega) step:
-// x += omega r (x FP32), r -= omega Ar (r, Ar FP16); omega formed once per block
-__global__ void __launch_bounds__(256) k_smooth_update_h(cx<float>* __restrict__ x, __half2* __restrict__ r,
-                                                         float* __restrict__ rs, const __half2* __restrict__ ar,
-                                                         const float* __restrict__ ars, const double* __restrict__ sc,
-                                                         float omega, int nsites, int nrhs) {
-    __shared__ cx<float> s_om[64];
-    const int lanes = blockDim.x, rhs = threadIdx.x;
-    if (threadIdx.y < 2) {
-        const int rr = rhs + threadIdx.y * lanes;
-        cx<float> om = mk(omega, 0.f);
-        if (sc) {
-            const double den = sc[3 * rr + 2];
-            om = (fabs(den) >= 1e-30 && isfinite(den)) ? mk((float)(sc[3 * rr] / den), (float)(sc[3 * rr + 1] / den))
-                                                       : mk(0.f, 0.f);
-        }
-        s_om[rr] = om;
-    }
+// The MR steps of the FP16 smoother keep every residual r_0 .. r_n (a ring of FP16 fields) and
+// leave x alone until the end, where one pass adds sum_k omega_k r_k: the FP32 x is read and
+// written once per smoothing instead of once per step.  omega_k per rhs comes from sc_k[rhs][3]
+// (MR: (re, im) of <A r, r> and ||A r||^2) or is a fixed Richardson omega.
+constexpr int kMaxMrSteps = 16;  // residuals one x pass combines
+
+__device__ __forceinline__ cx<float> mr_omega(const double* __restrict__ sc, int rr) {
+    const double den = sc[3 * rr + 2];
+    return (fabs(den) >= 1e-30 && isfinite(den)) ? mk((float)(sc[3 * rr] / den), (float)(sc[3 * rr + 1] / den))
+                                                 : mk(0.f, 0.f);
+}
+
+// r_out = r_in - omega A r (FP16 fields); a thread owns one pair of adjacent right-hand sides
+__global__ void __launch_bounds__(256) k_mr_rupdate_h(const __half2* __restrict__ r, const float* __restrict__ rs,
+                                                      const __half2* __restrict__ ar, const float* __restrict__ ars,
+                                                      __half2* __restrict__ ro, float* __restrict__ ros,
+                                                      const double* __restrict__ sc, float omega, int nsites,
+                                                      int nrhs) {
+    __shared__ cx<float> s_om[32];
+    const int lanes = blockDim.x, rhs0 = 2 * threadIdx.x;
+    const int tid = threadIdx.y * lanes + threadIdx.x;
+    if (tid < nrhs) s_om[tid] = sc ? mr_omega(sc, tid) : mk(omega, 0.f);
     __syncthreads();
     const int s = blockIdx.x * blockDim.y + threadIdx.y;
     const bool valid = s < nsites;
     Spinor<float> rn[2];
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        rn[k].s0 = mk(0.f, 0.f);
-        rn[k].s1 = mk(0.f, 0.f);
-    }
+    rn[0].s0 = rn[0].s1 = rn[1].s0 = rn[1].s1 = mk(0.f, 0.f);
     if (valid) {
-        Spinor<float> rv[2], av[2], xv[2];
+        Spinor<float> rv[2], av[2];
+        ld_pairs_h<1>(r, s, rhs0, nrhs, rv);
+        ld_pairs_h<1>(ar, s, rhs0, nrhs, av);
+        const float sr = rs[s], sa = ars[s];
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
-            const int rr = rhs + k * lanes;
-            rv[k] = ld_spinor_h(r, rs, s, rr, nrhs);
-            av[k] = ld_spinor_h(ar, ars, s, rr, nrhs);
-            xv[k] = ld_spinor(x, s, rr, nrhs);
-        }
-#pragma unroll
-        for (int k = 0; k < 2; ++k) {
-            const int rr = rhs + k * lanes;
-            const cx<float> om = s_om[rr];
-            xv[k].s0 = xv[k].s0 + om * rv[k].s0;
-            xv[k].s1 = xv[k].s1 + om * rv[k].s1;
-            st_spinor(x, s, rr, nrhs, xv[k]);
-            rn[k].s0 = rv[k].s0 - om * av[k].s0;
-            rn[k].s1 = rv[k].s1 - om * av[k].s1;
+            const cx<float> om = s_om[rhs0 + k];
+            const cx<float> oa = mk(om.re * sa, om.im * sa);
+            rn[k].s0 = sr * rv[k].s0 - oa * av[k].s0;
+            rn[k].s1 = sr * rv[k].s1 - oa * av[k].s1;
         }
     }
-    st_spinor2_h(r, rs, s, rhs, nrhs, lanes, rn[0], rn[1], valid);
+    st_pairs_h<1>(ro, ros, s, rhs0, nrhs, lanes, rn, valid);
 }
 
-// <Ar, r> (re, im) and ||Ar||^2 per rhs from FP16 fields, FP32 partials; a reducing lane owns
-// right-hand sides lane and lane + nlanes (nlanes = nrhs / 2)
-struct FinPairs3 {
-    double* out;
-    int nlanes;
-    __device__ void operator()(int lane, const double* s) const {
-        for (int k = 0; k < 3; ++k) {
-            out[3 * lane + k] = s[k];
-            out[3 * (lane + nlanes) + k] = s[3 + k];
-        }
-    }
+struct ResidualRing {
+    const __half2* r[kMaxMrSteps];
+    const float* s[kMaxMrSteps];
 };
 
-__global__ void __launch_bounds__(256) k_dotnorm_h(const __half2* __restrict__ ar, const float* __restrict__ ars,
-                                                   const __half2* __restrict__ r, const float* __restrict__ rs,
-                                                   int nsites, int nrhs, double* partials, unsigned int* ticket,
-                                                   double* out) {
-    const int nl = nrhs / 2;
-    const int lane = blockIdx.y * blockDim.x + threadIdx.x;
-    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (lane < nl) {
-        // two sites per pass with every load of the pass issued first
-        const int stride = gridDim.x * blockDim.y;
-        for (int s0 = blockIdx.x * blockDim.y + threadIdx.y; s0 < nsites; s0 += 2 * stride) {
-            Spinor<float> A[2][2], Bv[2][2];
+// x = (x_zero ? 0 : x) + sum_{k < n} omega_k r_k, omega_k from sc + k * 3 nrhs or fixed
+__global__ void __launch_bounds__(256) k_mr_xupdate_h(cx<float>* __restrict__ x, ResidualRing ring, int n,
+                                                      const double* __restrict__ sc, float omega, int x_zero,
+                                                      int nsites, int nrhs) {
+    __shared__ cx<float> s_om[kMaxMrSteps * 32];
+    const int lanes = blockDim.x, rhs0 = 2 * threadIdx.x;
+    const int tid = threadIdx.y * lanes + threadIdx.x;
+    for (int i = tid; i < n * nrhs; i += blockDim.x * blockDim.y)
+        s_om[i] = sc ? mr_omega(sc + (size_t)(i / nrhs) * 3 * nrhs, i % nrhs) : mk(omega, 0.f);
+    __syncthreads();
+    const int s = blockIdx.x * blockDim.y + threadIdx.y;
+    if (s >= nsites) return;
+    Spinor<float> xv[2];
+    if (x_zero) {
+        xv[0].s0 = xv[0].s1 = xv[1].s0 = xv[1].s1 = mk(0.f, 0.f);
+    } else {
+        ld_pairs_f<1>(x, s, rhs0, nrhs, xv);
+    }
+    for (int k = 0; k < n; ++k) {
+        Spinor<float> rv[2];
+        ld_pairs_h<1>(ring.r[k], s, rhs0, nrhs, rv);
+        const float sr = ring.s[k][s];
 #pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                const int s = s0 + u * stride;
-#pragma unroll
-                for (int k = 0; k < 2; ++k) {
-                    if (s < nsites) {
-                        A[u][k] = ld_spinor_h(ar, ars, s, lane + k * nl, nrhs);
-                        Bv[u][k] = ld_spinor_h(r, rs, s, lane + k * nl, nrhs);
-                    } else {
-                        A[u][k].s0 = A[u][k].s1 = Bv[u][k].s0 = Bv[u][k].s1 = mk(0.f, 0.f);
-                    }
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < 2; ++u)
-#pragma unroll
-                for (int k = 0; k < 2; ++k) {
-                    const cx<float> c = cmulc(A[u][k].s0, Bv[u][k].s0) + cmulc(A[u][k].s1, Bv[u][k].s1);
-                    v[3 * k] += c.re;
-                    v[3 * k + 1] += c.im;
-                    v[3 * k + 2] += norm2(A[u][k].s0) + norm2(A[u][k].s1);
-                }
+        for (int j = 0; j < 2; ++j) {
+            const cx<float> om = s_om[k * nrhs + rhs0 + j];
+            const cx<float> os = mk(om.re * sr, om.im * sr);
+            xv[j].s0 = xv[j].s0 + os * rv[j].s0;
+            xv[j].s1 = xv[j].s1 + os * rv[j].s1;
         }
     }
-    block_reduce_finalise<6>(v, partials, ticket, nl, FinPairs3{out, nl});
+    float4* px = reinterpret_cast<float4*>(x) + ((int64_t)s * nrhs + rhs0);
+    px[0] = make_float4(xv[0].s0.re, xv[0].s0.im, xv[0].s1.re, xv[0].s1.im);
+    px[1] = make_float4(xv[1].s0.re, xv[1].s0.im, xv[1].s1.re, xv[1].s1.im);
 }
 
-// mr_fine / smooth_fine with FP16 r, A r and D r (x and b FP32)
-smg_status smooth_fine_half(smg_mg* mg, smg_field* x, const smg_field* b, int niter, bool x_is_zero, double omega) {
+// launch shape of the pair kernels: (nrhs / 2 lanes, 256 / lanes sites)
+dim3 pair_block(int nrhs) { return dim3(nrhs / 2, 512 / nrhs); }
+dim3 pair_grid(int nsites, int nrhs) { return dim3((nsites + 512 / nrhs - 1) / (512 / nrhs)); }
+
+smg_status mr_xupdate_h(smg_mg* mg, smg_field* x, int first, int n, bool x_zero, double omega) {
     smg_context* ctx = mg->ctx;
-    smg_field *r = mg->f_r, *Ar = mg->f_Ar, *t = mg->f_t;
+    const int V = x->g.V, nrhs = x->nrhs;
+    if (n == 0) {
+        if (x_zero) SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
+        return SMG_OK;
+    }
+    ResidualRing ring{};
+    for (int k = 0; k < n; ++k) {
+        ring.r[k] = (const __half2*)mg->f_rs[first + k]->data;
+        ring.s[k] = mg->f_rs[first + k]->scale;
+    }
+    const double* sc = omega > 0 ? nullptr : mg->mr_om + (size_t)first * 3 * nrhs;
+    k_mr_xupdate_h<<<pair_grid(V, nrhs), pair_block(nrhs), 0, ctx->stream>>>((cx<float>*)x->data, ring, n, sc,
+                                                                             (float)omega, x_zero ? 1 : 0, V, nrhs);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+// One MR (omega <= 0) or Richardson (fixed omega) step of the FP16 smoother on r_it = f_rs[it]:
+// t = D r (||t||^2 fused), A r = D^dag t (||A r||^2 fused), the step's omega, and r_{it+1} when
+// write_next.  For A = D^dag D, <A r, r> = ||D r||^2, so MR's omega = ||D r||^2 / ||A r||^2.
+smg_status mr_step_h(smg_mg* mg, int it, double omega, bool write_next) {
+    smg_context* ctx = mg->ctx;
+    smg_field *r = mg->f_rs[it], *Ar = mg->f_Ar, *t = mg->f_t;
+    const int V = r->g.V, nrhs = r->nrhs;
+    const bool mr = !(omega > 0);
+    double* sc = mg->mr_om + (size_t)it * 3 * nrhs;
+    SMG_TRY(smg_dslash_h_norm(mg->dirac, false, r, t, mr ? mg->hdots : nullptr, 0));
+    SMG_TRY(smg_dslash_h_norm(mg->dirac, true, t, Ar, mr ? mg->hdots : nullptr, 1));
+    if (mr) SMG_TRY(smg_mr_norms_finish(ctx, r->g.L, nrhs, mg->hdots, sc));
+    if (write_next) {
+        smg_field* rn = mg->f_rs[it + 1];
+        k_mr_rupdate_h<<<pair_grid(V, nrhs), pair_block(nrhs), 0, ctx->stream>>>(
+            (const __half2*)r->data, r->scale, (const __half2*)Ar->data, Ar->scale, (__half2*)rn->data, rn->scale,
+            mr ? sc : nullptr, (float)omega, V, nrhs);
+        count_launch(ctx);
+    }
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+// mr_fine / smooth_fine with FP16 residuals, A r and D r (x and b FP32).  keep_residual: the last
+// step also writes r_n = b - A x (the residual the cycle restricts after pre-smoothing).
+smg_status smooth_fine_half(smg_mg* mg, smg_field* x, const smg_field* b, int niter, bool x_is_zero, double omega,
+                            bool keep_residual) {
+    smg_context* ctx = mg->ctx;
+    smg_field *r0 = mg->f_rs[0], *Ar = mg->f_Ar, *t = mg->f_t;
     const int V = b->g.V, nrhs = b->nrhs;
+    if ((int)mg->f_rs.size() < niter + 1) return smg_fail(ctx, SMG_BAD_ARG, "FP16 smoother: too few residual fields");
     const dim3 blk(nrhs / 2, 512 / nrhs), grd((V + blk.y - 1) / blk.y);
     if (x_is_zero) {
-        SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
-        k_sub_h<<<grd, blk, 0, ctx->stream>>>((const cx<float>*)b->data, nullptr, nullptr, (__half2*)r->data,
-                                              r->scale, V, nrhs);
+        k_sub_h<<<grd, blk, 0, ctx->stream>>>((const cx<float>*)b->data, nullptr, nullptr, (__half2*)r0->data,
+                                              r0->scale, V, nrhs);
     } else {
         SMG_TRY(smg_dslash(mg->dirac, false, x, t, nullptr));
         SMG_TRY(smg_dslash(mg->dirac, true, t, Ar, nullptr));
         k_sub_h<<<grd, blk, 0, ctx->stream>>>((const cx<float>*)b->data, (const __half2*)Ar->data, Ar->scale,
-                                              (__half2*)r->data, r->scale, V, nrhs);
+                                              (__half2*)r0->data, r0->scale, V, nrhs);
     }
     count_launch(ctx);
-    double* sc = lvl_scal(mg, 0);
-    const ReduceLaunch rl = reduce_launch(V, nrhs / 2);
-    SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * nrhs * 3));
+    int first = 0;  // first residual not yet added into x
+    bool zero = x_is_zero;
     for (int it = 0; it < niter; ++it) {
-        SMG_TRY(smg_dslash(mg->dirac, false, r, t, nullptr));
-        if (!(omega > 0) && mg->hdots) {
-            SMG_TRY(smg_dslash_h_dots(mg->dirac, t, Ar, r, mg->hdots, sc));  // MR: <Ar, r>, ||Ar||^2 fused
-        } else {
-            SMG_TRY(smg_dslash(mg->dirac, true, t, Ar, nullptr));
-            if (!(omega > 0)) {
-                k_dotnorm_h<<<rl.grid, rl.block, 0, ctx->stream>>>((const __half2*)Ar->data, Ar->scale,
-                                                                  (const __half2*)r->data, r->scale, V, nrhs,
-                                                                  ctx->red.partials, ctx->red.tickets, sc);
-                count_launch(ctx);
-            }
+        SMG_TRY(mr_step_h(mg, it, omega, it + 1 < niter || keep_residual));
+        if (it + 1 - first == kMaxMrSteps) {
+            SMG_TRY(mr_xupdate_h(mg, x, first, it + 1 - first, zero, omega));
+            first = it + 1;
+            zero = false;
         }
-        k_smooth_update_h<<<grd, blk, 0, ctx->stream>>>((cx<float>*)x->data, (__half2*)r->data, r->scale,
-                                                        (const __half2*)Ar->data, Ar->scale,
-                                                        omega > 0 ? nullptr : sc, (float)omega, V, nrhs);
-        count_launch(ctx);
-        SMG_CHECK_LAUNCH(ctx);
     }
+    SMG_TRY(mr_xupdate_h(mg, x, first, niter - first, zero, omega));
+    mg->f_res = mg->f_rs[niter];
     return SMG_OK;
 }
 
@@ -1696,9 +1742,10 @@ smg_status mr_coarse(smg_mg* mg, int l, void* x, const void* b, int niter, bool 
 // smoothers above, so the cycle picks either per level (mg_cycle,
 // src/multigrid.cpp:57-61, 95-98).
 template <typename T>
-smg_status smooth_fine(smg_mg* mg, smg_field* x, const smg_field* b, int niter, bool x_is_zero) {
+smg_status smooth_fine(smg_mg* mg, smg_field* x, const smg_field* b, int niter, bool x_is_zero,
+                       bool keep_residual = true) {
     const double om = mg->lv[0].rich_omega;
-    if (mg->f_r->prec == SMG_F16) return smooth_fine_half(mg, x, b, niter, x_is_zero, om);
+    if (mg->f_r->prec == SMG_F16) return smooth_fine_half(mg, x, b, niter, x_is_zero, om, keep_residual);
     if (!(om > 0)) return mr_fine<T>(mg, x, b, niter, x_is_zero);
     smg_context* ctx = mg->ctx;
     smg_field *r = mg->f_r, *Ar = mg->f_Ar;
@@ -1959,7 +2006,7 @@ smg_status cycle_fine(smg_mg* mg, smg_field* x, const smg_field* b) {
     SMG_TRY(smooth_fine<T>(mg, x, b, mg->p.pre_smooth, true));
     CoarseWork& nw = mg->cw[1];
     if (mg->f_r->prec == SMG_F16)
-        SMG_TRY(restrict_half(mg, mg->f_r, nw.b));
+        SMG_TRY(restrict_half(mg, mg->f_res, nw.b));
     else
         SMG_TRY(restrict_to<T>(mg, 0, mg->f_r->data, nw.b));
     SMG_TRY(cycle_coarse<T>(mg, 1, nw.x, nw.b));
@@ -1976,7 +2023,7 @@ smg_status cycle_fine(smg_mg* mg, smg_field* x, const smg_field* b) {
         count_launch(ctx);
     }
     SMG_TRY(prolong_to<T>(mg, 0, nw.x, x->data, 1));
-    return smooth_fine<T>(mg, x, b, mg->p.post_smooth, false);
+    return smooth_fine<T>(mg, x, b, mg->p.post_smooth, false, false);
 }
 
 // ------------------------------------------------------------ setup
@@ -2143,15 +2190,61 @@ smg_status validate(smg_context* ctx, int L, const smg_mg_params* p) {
     return SMG_OK;
 }
 
-smg_status build(smg_mg* mg, const double* warm) {
+// level-0 block vectors from the null vectors in mg->null0: cut to aggregates (with the chirality
+// split when asked) and orthonormalised per aggregate (Prolongator::build_from_vectors,
+// src/prolongator.h:133-141)
+smg_status block_vectors0(smg_mg* mg) {
     smg_context* ctx = mg->ctx;
+    const Geom g = mg->null0[0]->g;
+    Level& L = mg->lv[0];
+    if (!L.V64) SMG_CUDA(ctx, cudaMalloc(&L.V64, L.vsize() * sizeof(cx<double>)));
+    SMG_CUDA(ctx, cudaMemsetAsync(L.V64, 0, L.vsize() * sizeof(cx<double>), ctx->stream));
+    for (int k = 0; k < L.nvec; ++k) {
+        k_extract0<<<blocks_for(g.V), 256, 0, ctx->stream>>>((const cx<double>*)mg->null0[k]->data, k, g, L.ax, L.ay,
+                                                            L.nvec, L.nc_next, mg->p.chiral_split, L.V64);
+        count_launch(ctx);
+    }
+    const int len = L.ax * L.ay * 2, nc = L.nc_next;
+    const int nagg = L.nagg_x * L.nagg_y;
+    size_t smem = (size_t)len * nc * sizeof(cx<double>);
+    if (smem > 200 * 1024) return smg_fail(ctx, SMG_UNSUPPORTED, "aggregate too large for block Gram-Schmidt");
+    SMG_CUDA(ctx, cudaFuncSetAttribute(k_block_orth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_block_orth<<<nagg, 128, smem, ctx->stream>>>(L.V64, len, nc);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+// the level-1 Galerkin operator A_1 = P^dag D^dag D P from the level-0 block vectors: W = D P on
+// the block halos, then the 9 blocks of every coarse site
+smg_status galerkin0(smg_mg* mg) {
+    smg_context* ctx = mg->ctx;
+    smg_dirac* d = mg->dirac;
+    const Geom g = d->gauge->g;
+    const Level& L = mg->lv[0];
+    const int nc = L.nc_next, nagg = L.nagg_x * L.nagg_y;
+    const int nh = (L.ax + 2) * (L.ay + 2);
+    cx<double>* W = nullptr;
+    SMG_CUDA(ctx, cudaMallocAsync(&W, (size_t)nagg * nc * nh * 2 * sizeof(cx<double>), ctx->stream));
+    k_W0<<<nagg, 256, 0, ctx->stream>>>(L.V64, d->gauge->U64, d->C64, g, L.ax, L.ay, nc, 2.0 * d->r + d->mass,
+                                       d->mu_t, d->r, W);
+    count_launch(ctx);
+    Level& N = mg->lv[1];
+    if (!N.A64) SMG_CUDA(ctx, cudaMalloc(&N.A64, N.asize() * sizeof(cx<double>)));
+    k_galerkin0<<<dim3(nagg, 9), 256, 0, ctx->stream>>>(W, L.nagg_x, L.nagg_y, L.ax, L.ay, nc, N.A64);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    SMG_CUDA(ctx, cudaFreeAsync(W, ctx->stream));
+    return SMG_OK;
+}
+
+// level geometry of a hierarchy from its parameters and the fine lattice size
+void set_geometry(smg_mg* mg, int Lfine) {
     const smg_mg_params& P = mg->p;
-    const Geom g = mg->dirac->gauge->g;
     const int nlev = P.n_levels;
     mg->lv.resize(nlev);
-    // geometry
-    mg->lv[0].nx = mg->lv[0].ny = g.L;
-    mg->lv[0].nsites = g.V;
+    mg->lv[0].nx = mg->lv[0].ny = Lfine;
+    mg->lv[0].nsites = Lfine * Lfine;
     mg->lv[0].ndof = 2;
     for (int l = 0; l < nlev - 1; ++l) {
         Level& L = mg->lv[l];
@@ -2167,6 +2260,14 @@ smg_status build(smg_mg* mg, const double* warm) {
         N.nsites = N.nx * N.ny;
         N.ndof = L.nc_next;
     }
+}
+
+smg_status build(smg_mg* mg, const double* warm) {
+    smg_context* ctx = mg->ctx;
+    const smg_mg_params& P = mg->p;
+    const Geom g = mg->dirac->gauge->g;
+    const int nlev = P.n_levels;
+    set_geometry(mg, g.L);
     std::mt19937 rng(P.seed);
     std::normal_distribution<double> dist(0.0, 1.0);
     auto draw = [&](int64_t n, std::vector<double>& h) {  // random_vec order (linalg.cpp:44-48, GCC x86-64)
@@ -2188,6 +2289,8 @@ smg_status build(smg_mg* mg, const double* warm) {
         mg->null0.push_back(f);
         if (warm) {
             SMG_TRY(smg_field_upload(f, warm + (size_t)4 * g.V * i));
+        } else if (mg->starts && mg->starts[0]) {
+            SMG_TRY(smg_field_upload(f, mg->starts[0] + (size_t)4 * g.V * i));
         } else {
             draw((int64_t)2 * g.V, h);
             SMG_TRY(smg_field_upload(f, h.data()));
@@ -2195,38 +2298,8 @@ smg_status build(smg_mg* mg, const double* warm) {
     }
     SMG_TRY(null_space_fine(mg, mg->null0));
     // ---- level 0 prolongator and Galerkin operator
-    {
-        Level& L = mg->lv[0];
-        SMG_CUDA(ctx, cudaMalloc(&L.V64, L.vsize() * sizeof(cx<double>)));
-        SMG_CUDA(ctx, cudaMemsetAsync(L.V64, 0, L.vsize() * sizeof(cx<double>), ctx->stream));
-        for (int k = 0; k < k0; ++k) {
-            k_extract0<<<blocks_for(g.V), 256, 0, ctx->stream>>>((const cx<double>*)mg->null0[k]->data, k, g, L.ax,
-                                                                L.ay, L.nvec, L.nc_next, P.chiral_split, L.V64);
-            count_launch(ctx);
-        }
-        const int len = L.ax * L.ay * 2, nc = L.nc_next;
-        const int nagg = L.nagg_x * L.nagg_y;
-        size_t smem = (size_t)len * nc * sizeof(cx<double>);
-        if (smem > 200 * 1024) return smg_fail(ctx, SMG_UNSUPPORTED, "aggregate too large for block Gram-Schmidt");
-        SMG_CUDA(ctx, cudaFuncSetAttribute(k_block_orth, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_block_orth<<<nagg, 128, smem, ctx->stream>>>(L.V64, len, nc);
-        count_launch(ctx);
-        SMG_CHECK_LAUNCH(ctx);
-        // W = D P on block halos, then the 9 Galerkin blocks
-        const int nh = (L.ax + 2) * (L.ay + 2);
-        cx<double>* W = nullptr;
-        SMG_CUDA(ctx, cudaMallocAsync(&W, (size_t)nagg * nc * nh * 2 * sizeof(cx<double>), ctx->stream));
-        smg_dirac* d = mg->dirac;
-        k_W0<<<nagg, 256, 0, ctx->stream>>>(L.V64, d->gauge->U64, d->C64, g, L.ax, L.ay, nc, 2.0 * d->r + d->mass,
-                                           d->mu_t, d->r, W);
-        count_launch(ctx);
-        Level& N = mg->lv[1];
-        SMG_CUDA(ctx, cudaMalloc(&N.A64, N.asize() * sizeof(cx<double>)));
-        k_galerkin0<<<dim3(nagg, 9), 256, 0, ctx->stream>>>(W, L.nagg_x, L.nagg_y, L.ax, L.ay, nc, N.A64);
-        count_launch(ctx);
-        SMG_CHECK_LAUNCH(ctx);
-        SMG_CUDA(ctx, cudaFreeAsync(W, ctx->stream));
-    }
+    SMG_TRY(block_vectors0(mg));
+    SMG_TRY(galerkin0(mg));
     // ---- deeper levels
     for (int l = 1; l < nlev - 1; ++l) {
         Level& L = mg->lv[l];
@@ -2234,8 +2307,14 @@ smg_status build(smg_mg* mg, const double* warm) {
         std::vector<cx<double>*> vecs(L.nvec, nullptr);
         for (int i = 0; i < L.nvec; ++i) {
             SMG_CUDA(ctx, cudaMalloc(&vecs[i], (size_t)dim * sizeof(cx<double>)));
-            draw(dim, h);
-            SMG_CUDA(ctx, cudaMemcpy(vecs[i], h.data(), (size_t)dim * sizeof(cx<double>), cudaMemcpyHostToDevice));
+            const double* src = nullptr;
+            if (mg->starts && mg->starts[l]) {
+                src = mg->starts[l] + (size_t)2 * dim * i;
+            } else {
+                draw(dim, h);
+                src = h.data();
+            }
+            SMG_CUDA(ctx, cudaMemcpy(vecs[i], src, (size_t)dim * sizeof(cx<double>), cudaMemcpyHostToDevice));
         }
         smg_status st = null_space_coarse(mg, l, vecs);
         if (st == SMG_OK) {
@@ -2280,22 +2359,8 @@ smg_status build(smg_mg* mg, const double* warm) {
 // cycle stays valid.
 smg_status rebuild_operators(smg_mg* mg) {
     smg_context* ctx = mg->ctx;
-    const Geom g = mg->dirac->gauge->g;
     const int nlev = (int)mg->lv.size();
-    {
-        Level& L = mg->lv[0];
-        const int nc = L.nc_next, nagg = L.nagg_x * L.nagg_y;
-        const int nh = (L.ax + 2) * (L.ay + 2);
-        cx<double>* W = nullptr;
-        SMG_CUDA(ctx, cudaMallocAsync(&W, (size_t)nagg * nc * nh * 2 * sizeof(cx<double>), ctx->stream));
-        smg_dirac* d = mg->dirac;
-        k_W0<<<nagg, 256, 0, ctx->stream>>>(L.V64, d->gauge->U64, d->C64, g, L.ax, L.ay, nc, 2.0 * d->r + d->mass,
-                                           d->mu_t, d->r, W);
-        k_galerkin0<<<dim3(nagg, 9), 256, 0, ctx->stream>>>(W, L.nagg_x, L.nagg_y, L.ax, L.ay, nc, mg->lv[1].A64);
-        count_launch(ctx, 2);
-        SMG_CHECK_LAUNCH(ctx);
-        SMG_CUDA(ctx, cudaFreeAsync(W, ctx->stream));
-    }
+    SMG_TRY(galerkin0(mg));
     for (int l = 1; l < nlev - 1; ++l) {
         Level& L = mg->lv[l];
         const int nc = L.nc_next, nagg = L.nagg_x * L.nagg_y;
@@ -2577,6 +2642,188 @@ SMG_API smg_status smg_mg_create(smg_dirac* d, const smg_mg_params* p, const dou
     return SMG_OK;
 }
 
+SMG_API smg_status smg_mg_create_from_starts(smg_dirac* d, const smg_mg_params* p, const double* const* start_vecs,
+                                             smg_mg** out) {
+    if (!d || !p || !out || !start_vecs) return SMG_BAD_ARG;
+    *out = nullptr;
+    smg_context* ctx = d->ctx;
+    SMG_TRY(validate(ctx, d->gauge->g.L, p));
+    for (int l = 0; l < p->n_levels - 1; ++l)
+        if (!start_vecs[l]) return smg_fail(ctx, SMG_BAD_ARG, "start vectors missing for a level");
+    smg_mg* mg = new smg_mg();
+    mg->ctx = ctx;
+    mg->dirac = d;
+    mg->p = *p;
+    if (const char* e = std::getenv("SMG_CUDA_GRAPHS")) mg->use_graph = std::atoi(e) != 0;
+    mg->starts = start_vecs;
+    smg_status st = build(mg, nullptr);
+    mg->starts = nullptr;
+    if (st != SMG_OK) {
+        cudaStreamSynchronize(ctx->stream);
+        free_work(mg);
+        destroy_levels(mg);
+        delete mg;
+        return st;
+    }
+    *out = mg;
+    return SMG_OK;
+}
+
+// ---- standalone prolongator and coarse operator (Prolongator, src/prolongator.h:14-142, and
+// SparseCoarseOp, src/coarse_op.h:154-548): each holds a two-level hierarchy shell whose level 0
+// carries the block vectors (and, for the coarse operator, level 1 the Galerkin operator)
+struct smg_prolongator {
+    smg_mg* mg = nullptr;
+};
+struct smg_coarse_op {
+    smg_mg* mg = nullptr;
+};
+
+namespace {
+smg_mg* shell_mg(smg_context* ctx, smg_dirac* d, int L, int bx, int by, int k) {
+    smg_mg* mg = new smg_mg();
+    mg->ctx = ctx;
+    mg->dirac = d;
+    smg_mg_params_default(&mg->p);
+    mg->p.n_levels = 2;
+    mg->p.block[0][0] = bx;
+    mg->p.block[0][1] = by;
+    mg->p.n_vec[0] = k;
+    mg->p.null_iters = 0;
+    mg->p.w_cycle = 0;
+    mg->p.precision = SMG_F64;
+    mg->p.tensor_cores = 0;
+    mg->use_graph = false;
+    mg->persistent = false;
+    set_geometry(mg, L);
+    return mg;
+}
+}  // namespace
+
+SMG_API smg_status smg_prolongator_create(smg_context* ctx, int L, int bx, int by, int k, const double* null_vecs,
+                                          smg_prolongator** out) {
+    if (!ctx || !null_vecs || !out) return SMG_BAD_ARG;
+    *out = nullptr;
+    if (L < 2 || (L & 1) || bx < 2 || by < 2 || L % bx || L % by || L / bx < 3 || L / by < 3)
+        return smg_fail(ctx, SMG_BAD_ARG, "prolongator: blocks must divide L into at least 3 x 3 blocks");
+    if (k < 1 || k > 64 || k > 2 * bx * by) return smg_fail(ctx, SMG_BAD_ARG, "prolongator: k in [1, min(64, 2 bx by)]");
+    smg_mg* mg = shell_mg(ctx, nullptr, L, bx, by, k);
+    smg_status st = SMG_OK;
+    for (int i = 0; i < k && st == SMG_OK; ++i) {
+        smg_field* f = nullptr;
+        st = smg_field_create(ctx, L, 1, SMG_F64, &f);
+        if (st == SMG_OK) {
+            mg->null0.push_back(f);
+            st = smg_field_upload(f, null_vecs + (size_t)4 * L * L * i);
+        }
+    }
+    if (st == SMG_OK) st = block_vectors0(mg);
+    if (st == SMG_OK) st = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? SMG_OK : SMG_DEVICE_ERROR;
+    if (st != SMG_OK) {
+        smg_mg_destroy(mg);
+        return st;
+    }
+    *out = new smg_prolongator{mg};
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_prolongator_destroy(smg_prolongator* P) {
+    if (!P) return SMG_OK;
+    smg_mg_destroy(P->mg);
+    delete P;
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_prolongator_get_block_vecs(smg_prolongator* P, double* block_vecs) {
+    if (!P) return SMG_BAD_ARG;
+    return smg_mg_get_prolongator(P->mg, 0, block_vecs);
+}
+
+SMG_API smg_status smg_prolongator_prolong(smg_prolongator* P, const double* coarse, double* fine) {
+    if (!P) return SMG_BAD_ARG;
+    return smg_mg_prolong_host(P->mg, 0, coarse, fine);
+}
+
+SMG_API smg_status smg_prolongator_restrict(smg_prolongator* P, const double* fine, double* coarse) {
+    if (!P) return SMG_BAD_ARG;
+    return smg_mg_restrict_host(P->mg, 0, fine, coarse);
+}
+
+SMG_API smg_status smg_coarse_op_create(const smg_prolongator* P, smg_dirac* d, smg_coarse_op** out) {
+    if (!P || !d || !out) return SMG_BAD_ARG;
+    *out = nullptr;
+    const smg_mg* pm = P->mg;
+    smg_context* ctx = pm->ctx;
+    if (d->ctx != ctx) return smg_fail(ctx, SMG_BAD_ARG, "coarse operator: prolongator and operator contexts differ");
+    if (d->gauge->g.L != pm->lv[0].nx) return smg_fail(ctx, SMG_BAD_ARG, "coarse operator: lattice sizes differ");
+    const Level& L0 = pm->lv[0];
+    smg_mg* mg = shell_mg(ctx, d, L0.nx, L0.ax, L0.ay, L0.nvec);
+    smg_status st = SMG_OK;
+    Level& L = mg->lv[0];
+    const size_t vb = (size_t)L.vsize() * sizeof(cx<double>);
+    if (cudaMalloc(&L.V64, vb) != cudaSuccess) st = smg_fail(ctx, SMG_DEVICE_ERROR, "cudaMalloc");
+    if (st == SMG_OK && cudaMemcpyAsync(L.V64, L0.V64, vb, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess)
+        st = smg_fail(ctx, SMG_DEVICE_ERROR, "cudaMemcpyAsync");
+    if (st == SMG_OK) {  // transfers need a level-0 geometry field
+        smg_field* f = nullptr;
+        st = smg_field_create(ctx, L.nx, 1, SMG_F64, &f);
+        if (st == SMG_OK) mg->null0.push_back(f);
+    }
+    if (st == SMG_OK) st = galerkin0(mg);
+    if (st == SMG_OK) st = cudaStreamSynchronize(ctx->stream) == cudaSuccess ? SMG_OK : SMG_DEVICE_ERROR;
+    if (st != SMG_OK) {
+        smg_mg_destroy(mg);
+        return st;
+    }
+    *out = new smg_coarse_op{mg};
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_coarse_op_destroy(smg_coarse_op* A) {
+    if (!A) return SMG_OK;
+    smg_mg_destroy(A->mg);
+    delete A;
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_coarse_op_dims(smg_coarse_op* A, int* nbx, int* nby, int* k) {
+    if (!A) return SMG_BAD_ARG;
+    return smg_mg_level_dims(A->mg, 1, nbx, nby, k);
+}
+
+SMG_API smg_status smg_coarse_op_get_links(smg_coarse_op* A, double* links) {
+    if (!A) return SMG_BAD_ARG;
+    return smg_mg_get_coarse_op(A->mg, 1, links);
+}
+
+SMG_API smg_status smg_coarse_op_apply(smg_coarse_op* A, const double* in, double* out) {
+    if (!A) return SMG_BAD_ARG;
+    return smg_mg_coarse_apply_host(A->mg, 1, in, out);
+}
+
+SMG_API smg_status smg_coarse_op_solve(smg_coarse_op* A, const double* b, double* x, int max_iter, double tol) {
+    if (!A || !b || !x || max_iter < 0 || !(tol > 0)) return SMG_BAD_ARG;
+    smg_mg* mg = A->mg;
+    smg_context* ctx = mg->ctx;
+    SMG_TRY(ensure_work(mg, 1, SMG_F64));
+    const Level& L = mg->lv[1];
+    CoarseWork& w = mg->cw[1];
+    const size_t nb = (size_t)L.nsites * L.ndof * sizeof(cx<double>);
+    mg->p.coarse_max_iter = max_iter;
+    mg->p.coarse_tol = tol;
+    SMG_CUDA(ctx, cudaMemcpyAsync(w.b, b, nb, cudaMemcpyHostToDevice, ctx->stream));
+    SMG_TRY(coarse_cg<double>(mg, 1, w.x, w.b));
+    SMG_CUDA(ctx, cudaMemcpyAsync(x, w.x, nb, cudaMemcpyDeviceToHost, ctx->stream));
+    SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return smg_mg_check_device_error(mg);
+}
+
+SMG_API smg_status smg_coarse_op_setup_deflation(smg_coarse_op* A, int n_ev, int n_kr, int max_restarts, double tol,
+                                                 smg_deflation_info* info) {
+    if (!A) return SMG_BAD_ARG;
+    return smg_mg_setup_deflation(A->mg, n_ev, n_kr, max_restarts, tol, info);
+}
+
 SMG_API smg_status smg_mg_destroy(smg_mg* mg) {
     if (!mg) return SMG_OK;
     cudaStreamSynchronize(mg->ctx->stream);
@@ -2600,6 +2847,19 @@ SMG_API smg_status smg_mg_null_vectors(smg_mg* mg, double* out) {
     if (!mg || !out) return SMG_BAD_ARG;
     const size_t per = (size_t)4 * mg->lv[0].nsites;
     for (size_t i = 0; i < mg->null0.size(); ++i) SMG_TRY(smg_field_download(mg->null0[i], out + per * i));
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_set_wait_limit(smg_mg* mg, long long spins) {
+    if (!mg) return SMG_BAD_ARG;
+    mg->spin_limit = spins < 0 ? kBarrierSpinLimit : spins;
+    drop_graph(mg);  // a captured cycle holds the old bound in its kernel arguments
+    return SMG_OK;
+}
+
+SMG_API smg_status smg_mg_n_null_vectors(smg_mg* mg, int* k) {
+    if (!mg || !k) return SMG_BAD_ARG;
+    *k = (int)mg->null0.size();
     return SMG_OK;
 }
 
@@ -2728,10 +2988,12 @@ SMG_API smg_status smg_mg_time_coarse_apply(smg_mg* mg, int level, int nrhs, int
     return SMG_OK;
 }
 
-// The fine smoother's three kernels of one MR step on FP16 work vectors, each launched `reps`
-// times on the context's stream and timed with CUDA events: [0] t = D r (FP16 -> FP16),
-// [1] Ar = D^dag t with <Ar, r> and ||Ar||^2 fused, [2] x += omega r, r -= omega Ar.  r is
-// made from b (F32, the hierarchy's nrhs); bytes[] are each kernel's compulsory HBM bytes.
+// The fine smoother's kernels of one MR step on FP16 work vectors, each launched `reps` times on
+// the context's stream and timed with CUDA events: [0] t = D r with ||t||^2 fused (FP16 -> FP16),
+// [1] A r = D^dag t with ||A r||^2 fused plus the two small kernels that finish the MR scalars,
+// [2] r' = r - omega A r, [3] the x pass that adds omega_k r_k of a whole smoothing (pre_smooth
+// residuals).  r is made from b (F32, the hierarchy's nrhs); bytes[] are each kernel's compulsory
+// HBM bytes.
 SMG_API smg_status smg_mg_time_smoother(smg_mg* mg, const smg_field* b, int reps, double* ms, double* bytes) {
     if (!mg || !b || !ms || reps < 1) return SMG_BAD_ARG;
     smg_context* ctx = mg->ctx;
@@ -2741,35 +3003,38 @@ SMG_API smg_status smg_mg_time_smoother(smg_mg* mg, const smg_field* b, int reps
     if (!half_smoother(mg, nrhs, SMG_F32))
         return smg_fail(ctx, SMG_UNSUPPORTED, "smoother timing: the hierarchy has no FP16 smoother for this nrhs");
     SMG_TRY(ensure_work(mg, nrhs, SMG_F32));
-    if (!mg->hdots) return smg_fail(ctx, SMG_UNSUPPORTED, "smoother timing: no fused stencil reductions");
-    smg_field *r = mg->f_r, *Ar = mg->f_Ar, *t = mg->f_t;
-    const dim3 blk(nrhs / 2, 512 / nrhs), grd((V + blk.y - 1) / blk.y);
-    double* sc = lvl_scal(mg, 0);
+    const int nx = std::max(1, mg->p.pre_smooth);
     smg_field* x = nullptr;
     SMG_TRY(smg_field_create(ctx, b->g.L, nrhs, SMG_F32, &x));
     SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
-    k_sub_h<<<grd, blk, 0, ctx->stream>>>((const cx<float>*)b->data, nullptr, nullptr, (__half2*)r->data, r->scale, V,
-                                          nrhs);
-    count_launch(ctx);
-    cudaEvent_t ev[4];
+    // a smoothing's residuals from b, so every field the timed kernels read holds real data
+    SMG_TRY(smooth_fine_half(mg, x, b, nx, true, 0.0, true));
+    smg_field *r = mg->f_rs[0], *Ar = mg->f_Ar, *t = mg->f_t, *rn = mg->f_rs[1];
+    double* sc = mg->mr_om;
+    const dim3 blk = pair_block(nrhs), grd = pair_grid(V, nrhs);
+    cudaEvent_t ev[5];
     for (auto& e : ev) SMG_CUDA(ctx, cudaEventCreate(&e));
     smg_status st = SMG_OK;
     for (int pass = 0; pass < 2 && st == SMG_OK; ++pass) {  // pass 0 warms up
         SMG_CUDA(ctx, cudaEventRecord(ev[0], ctx->stream));
-        for (int i = 0; i < reps && st == SMG_OK; ++i) st = smg_dslash(mg->dirac, false, r, t, nullptr);
+        for (int i = 0; i < reps && st == SMG_OK; ++i) st = smg_dslash_h_norm(mg->dirac, false, r, t, mg->hdots, 0);
         SMG_CUDA(ctx, cudaEventRecord(ev[1], ctx->stream));
-        for (int i = 0; i < reps && st == SMG_OK; ++i) st = smg_dslash_h_dots(mg->dirac, t, Ar, r, mg->hdots, sc);
-        SMG_CUDA(ctx, cudaEventRecord(ev[2], ctx->stream));
         for (int i = 0; i < reps && st == SMG_OK; ++i) {
-            // omega from the last reductions, applied to a copy-free update: r and x drift but stay finite
-            k_smooth_update_h<<<grd, blk, 0, ctx->stream>>>((cx<float>*)x->data, (__half2*)r->data, r->scale,
-                                                            (const __half2*)Ar->data, Ar->scale, sc, 0.f, V, nrhs);
+            st = smg_dslash_h_norm(mg->dirac, true, t, Ar, mg->hdots, 1);
+            if (st == SMG_OK) st = smg_mr_norms_finish(ctx, b->g.L, nrhs, mg->hdots, sc);
+        }
+        SMG_CUDA(ctx, cudaEventRecord(ev[2], ctx->stream));
+        for (int i = 0; i < reps; ++i) {
+            k_mr_rupdate_h<<<grd, blk, 0, ctx->stream>>>((const __half2*)r->data, r->scale, (const __half2*)Ar->data,
+                                                         Ar->scale, (__half2*)rn->data, rn->scale, sc, 0.f, V, nrhs);
             count_launch(ctx);
         }
         SMG_CUDA(ctx, cudaEventRecord(ev[3], ctx->stream));
+        for (int i = 0; i < reps && st == SMG_OK; ++i) st = mr_xupdate_h(mg, x, 0, nx, false, 0.0);
+        SMG_CUDA(ctx, cudaEventRecord(ev[4], ctx->stream));
     }
-    SMG_CUDA(ctx, cudaEventSynchronize(ev[3]));
-    for (int k = 0; k < 3; ++k) {
+    SMG_CUDA(ctx, cudaEventSynchronize(ev[4]));
+    for (int k = 0; k < 4; ++k) {
         float f = 0;
         SMG_CUDA(ctx, cudaEventElapsedTime(&f, ev[k], ev[k + 1]));
         ms[k] = (double)f / reps;
@@ -2779,11 +3044,12 @@ SMG_API smg_status smg_mg_time_smoother(smg_mg* mg, const smg_field* b, int reps
     SMG_TRY(st);
     SMG_CHECK_LAUNCH(ctx);
     if (bytes) {
-        // per site: FP16 two-spinor 8 B per rhs plus a 4 B scale per field; links 2 x 8 B; clover 4 B
+        // per site: an FP16 two-spinor is 8 B per rhs plus a 4 B scale per field; links 2 x 8 B; clover 4 B
         const double n = (double)V;
-        bytes[0] = n * (16.0 * nrhs + 8 + 16 + 4);            // r in, t out, links, clover
-        bytes[1] = n * (24.0 * nrhs + 12 + 16 + 4);           // t and r (= w) in, Ar out
-        bytes[2] = n * (32.0 * nrhs + 24.0 * nrhs + 12);      // x in and out (FP32); r, Ar in, r out (FP16)
+        bytes[0] = n * (16.0 * nrhs + 8 + 16 + 4);              // r in, t out, links, clover
+        bytes[1] = n * (16.0 * nrhs + 8 + 16 + 4);              // t in, A r out, links, clover
+        bytes[2] = n * (24.0 * nrhs + 12);                      // r, A r in, r' out
+        bytes[3] = n * (32.0 * nrhs + nx * (8.0 * nrhs + 4));   // x in and out (FP32), the residuals in
     }
     return SMG_OK;
 }

@@ -67,6 +67,8 @@ SMG_API smg_status smg_blas_dot_noalloc(const double* a, const double* b, int64_
                                         void* stream) {
     if (!a || !b || !out || n < 0) return SMG_BAD_ARG;
     if (nrhs < 1 || nrhs > kNoAllocMaxRhs) return SMG_BAD_ARG;  // beyond the scratch: 16 vectors per call
+    // an error left by earlier work stays with its owner: report it without launching or clearing it
+    if (cudaPeekAtLastError() != cudaSuccess) return SMG_DEVICE_ERROR;
     int device = -1;
     if (cudaGetDevice(&device) != cudaSuccess) return SMG_DEVICE_ERROR;
     double* scratch = nullptr;

@@ -158,6 +158,10 @@ struct smg_context {
     std::vector<double*> retired;
     // stencil launch shape chosen by timing per (L, nrhs, precision): key -> variant
     std::vector<std::pair<uint64_t, int>> dslash_plans;
+    // device memory of finished solves, kept for the next solve on this context and freed with it:
+    // work fields by (L, nrhs, precision) and scalar buffers by size (stream order makes reuse safe)
+    std::vector<smg_field*> field_pool;
+    std::vector<std::pair<size_t, void*>> buf_pool;
 };
 
 struct smg_gauge {
@@ -217,4 +221,11 @@ smg_status smg_dirac_apply_internal(smg_dirac* d, smg_operator op, const smg_fie
                                     smg_field* dst, double* norm2_out_dev);
 smg_status smg_field_check_pair(const smg_field* a, const smg_field* b);
 smg_status smg_field_alloc_like(const smg_field* proto, smg_precision prec, smg_field** out);
+// a work field like proto in precision prec from the context's pool (allocated when none is free),
+// and its return to the pool
+smg_status smg_field_take(const smg_field* proto, smg_precision prec, smg_field** out);
+void smg_field_give(smg_field* f);
+// a device buffer of `bytes` from the context's pool, and its return
+smg_status smg_buf_take(smg_context* ctx, size_t bytes, void** out);
+void smg_buf_give(smg_context* ctx, size_t bytes, void* p);
 smg_status smg_gauge_ensure_f32(smg_gauge* g);

@@ -177,8 +177,9 @@ smg_status cg_run(smg_dirac* d, const smg_field* b, smg_field* x, int max_iter, 
 
     // device scalar block
     size_t nbytes = (size_t)nrhs * (5 * sizeof(double) + 3 * sizeof(int)) + 64;
-    char* blk = nullptr;
-    SMG_CUDA(ctx, cudaMallocAsync((void**)&blk, nbytes, ctx->stream));
+    PoolBuf blk_buf;
+    SMG_TRY(blk_buf.take(ctx, nbytes));
+    char* blk = static_cast<char*>(blk_buf.p);
     CgState s;
     s.rr = (double*)blk;
     s.pAp = s.rr + nrhs;
@@ -280,7 +281,6 @@ smg_status cg_run(smg_dirac* d, const smg_field* b, smg_field* x, int max_iter, 
     SMG_CUDA(ctx, cudaMemcpyAsync(h.data(), blk, (size_t)nrhs * 5 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     SMG_CUDA(ctx, cudaMemcpyAsync(hi.data(), s.active, (size_t)nrhs * 3 * sizeof(int), cudaMemcpyDeviceToHost,
                                   ctx->stream));
-    SMG_CUDA(ctx, cudaFreeAsync(blk, ctx->stream));
     SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
 
     smg_status st = SMG_OK;
@@ -523,10 +523,8 @@ struct GcrWs {
     double* dots = nullptr;
     double* apr = nullptr;
     int nrhs = 0, nbuf = 0;
+    PoolBuf blk_buf;
     double* apr_of(int buf) const { return apr + (size_t)buf * 3 * nrhs; }
-    ~GcrWs() {
-        if (blk) cudaFreeAsync(blk, ctx->stream);
-    }
     smg_status init(smg_context* c, const smg_field* proto, int trunc) {
         ctx = c;
         nrhs = proto->nrhs;
@@ -543,7 +541,8 @@ struct GcrWs {
         }
         const size_t nd_ = (size_t)nrhs * (3 + 5 * nbuf) + 64;
         const size_t bytes = nd_ * sizeof(double) + (size_t)nrhs * 2 * sizeof(int) + 64;
-        SMG_CUDA(ctx, cudaMallocAsync(&blk, bytes, ctx->stream));
+        SMG_TRY(blk_buf.take(ctx, bytes));
+        blk = static_cast<double*>(blk_buf.p);
         SMG_CUDA(ctx, cudaMemsetAsync(blk, 0, bytes, ctx->stream));
         sc.rr = blk;
         sc.bnorm2 = blk + nrhs;
@@ -783,14 +782,13 @@ smg_status gcr_mixed(smg_dirac* d, smg_mg* mg, const smg_field* b, smg_field* x,
     SMG_TRY(fs.add(b, &t64));
     SMG_TRY(fs.add(b, &Ax64));
     smg_field *r32 = nullptr, *e32 = nullptr;
-    SMG_TRY(smg_field_alloc_like(b, SMG_F32, &r32));
-    fs.f.push_back(r32);
-    SMG_TRY(smg_field_alloc_like(b, SMG_F32, &e32));
-    fs.f.push_back(e32);
+    SMG_TRY(fs.add(b, SMG_F32, &r32));
+    SMG_TRY(fs.add(b, SMG_F32, &e32));
     GcrWs<float> ws;
     SMG_TRY(ws.init(ctx, r32, trunc));
-    double* sc = nullptr;  // [0, nrhs) ||r||^2, [nrhs, 2 nrhs) multipliers
-    SMG_CUDA(ctx, cudaMallocAsync((void**)&sc, (size_t)2 * nrhs * sizeof(double), ctx->stream));
+    PoolBuf sc_buf;  // [0, nrhs) ||r||^2, [nrhs, 2 nrhs) multipliers
+    SMG_TRY(sc_buf.take(ctx, (size_t)2 * nrhs * sizeof(double)));
+    double* sc = static_cast<double*>(sc_buf.p);
     std::vector<double> b2(nrhs), rr(nrhs), mult(nrhs);
     // x = 0, r = b
     SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
@@ -849,7 +847,6 @@ smg_status gcr_mixed(smg_dirac* d, smg_mg* mg, const smg_field* b, smg_field* x,
             if (!std::isfinite(rr[j])) nonfinite = true;
         if (out.iterations == 0) break;  // no progress possible
     }
-    SMG_CUDA(ctx, cudaFreeAsync(sc, ctx->stream));
     double worst = 0;
     bool notconv = false;
     for (int j = 0; j < nrhs; ++j) {
@@ -884,13 +881,12 @@ smg_status cg_mixed(smg_dirac* d, const smg_field* b, smg_field* x, int max_iter
     SMG_TRY(fs.add(b, &t64));
     SMG_TRY(fs.add(b, &Ax64));
     smg_field *r32 = nullptr, *e32 = nullptr;
-    SMG_TRY(smg_field_alloc_like(b, SMG_F32, &r32));
-    fs.f.push_back(r32);
-    SMG_TRY(smg_field_alloc_like(b, SMG_F32, &e32));
-    fs.f.push_back(e32);
+    SMG_TRY(fs.add(b, SMG_F32, &r32));
+    SMG_TRY(fs.add(b, SMG_F32, &e32));
     SMG_TRY(smg_gauge_ensure_f32(d->gauge));
-    double* sc = nullptr;  // [0, nrhs) ||r||^2, [nrhs, 2 nrhs) multipliers
-    SMG_CUDA(ctx, cudaMallocAsync((void**)&sc, (size_t)2 * nrhs * sizeof(double), ctx->stream));
+    PoolBuf sc_buf;  // [0, nrhs) ||r||^2, [nrhs, 2 nrhs) multipliers
+    SMG_TRY(sc_buf.take(ctx, (size_t)2 * nrhs * sizeof(double)));
+    double* sc = static_cast<double*>(sc_buf.p);
     std::vector<double> b2(nrhs), rr(nrhs), mult(nrhs);
     SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
     SMG_CUDA(ctx, cudaMemcpyAsync(r64->data, b->data, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -945,7 +941,6 @@ smg_status cg_mixed(smg_dirac* d, const smg_field* b, smg_field* x, int max_iter
             if (!std::isfinite(rr[j])) nonfinite = true;
         if (ir.iterations == 0) break;  // no progress possible
     }
-    SMG_CUDA(ctx, cudaFreeAsync(sc, ctx->stream));
     double worst = 0;
     bool notconv = false;
     for (int j = 0; j < nrhs; ++j) {

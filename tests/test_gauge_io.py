@@ -72,3 +72,21 @@ def test_reference_reads_our_file(ref, tmp_path):
     U, hdr = ref.load_gauge(L, tmp_path / "o.swng")
     assert U is not None and list(hdr) == [BETA, MASS, 0.5]
     np.testing.assert_allclose(U.reshape(2, -1), _links(), rtol=0, atol=1e-15)
+
+
+def test_reading_links_needs_the_callers_size():
+    """The links are read only into a buffer whose lattice size the caller states: with L_expected <= 0
+    the header alone is returned, and asking for the links as well is a bad argument."""
+    import ctypes as C
+
+    import schwinger_mg_gb300 as smg
+    from schwinger_mg_gb300 import _lib
+
+    lib = smg.lib()
+    path = str(GOLDEN / "gauge_L8.swng").encode()
+    hdr = _lib.GaugeHeader()
+    assert lib.smg_host_gauge_read_swng(path, 0, C.byref(hdr), None) == 0 and hdr.L == L
+    U = np.empty(4 * L * L)
+    bad = lib.smg_host_gauge_read_swng(path, 0, C.byref(hdr), U.ctypes.data_as(C.POINTER(C.c_double)))
+    assert bad == _lib.BAD_ARG
+    assert lib.smg_host_gauge_read_swng(path, L, C.byref(hdr), U.ctypes.data_as(C.POINTER(C.c_double))) == 0
