@@ -12,7 +12,7 @@ is reported.  Workloads:
 * mg (default) — the multi-RHS MG-GCR solve on a 512 x 512 lattice, beta = 6,
   m = -0.05, c_sw = 1; three levels (4 x 4 then 2 x 2 aggregates, 16 null
   vectors per level = 16 coarse dofs, V-cycle); 32 right-hand sides solved
-  together to a true FP64 residual of 1e-10 by an FP32 GCR (truncation 10)
+  together to a true FP64 residual of 1e-10 by an FP32 GCR (truncation 6)
   preconditioned with the FP32 hierarchy, whose fine smoother keeps its work
   vectors in FP16 with per-site scales, inside FP64 defect correction.  The
   hierarchy is built once before timing.  value = solves/s.  The plain FP64
@@ -159,7 +159,7 @@ def shard(items: list, rank: int, ws: int) -> list:
 # ------------------------------------------------------------------ workloads
 MG = dict(L=512, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=20240, nrhs=32, levels=3, blocks=[(4, 4), (2, 2)],
           n_vec=16, chiral=False, w_cycle=False, null_iters=6, pre=4, post=4, coarse_max_iter=20, coarse_tol=5e-2,
-          tol=1e-10, max_iter=500, trunc=10)
+          tol=1e-10, max_iter=500, trunc=6)
 MG2 = dict(L=256, beta=6.0, m=-0.05, r=1.0, csw=1.0, mu=0.0, seed=2025, nrhs=1, levels=2, blocks=[(4, 4)], n_vec=8,
            chiral=True, w_cycle=False, null_iters=2, pre=4, post=4, coarse_max_iter=50, coarse_tol=5e-2, tol=1e-10,
            max_iter=1000, trunc=20)

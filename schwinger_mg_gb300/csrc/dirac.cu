@@ -388,13 +388,15 @@ __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
     }
 }
 
-// right-hand-side pairs per thread of the FP16 stencil launches
+// right-hand-side pairs per thread of the FP16 stencil launches: two (four right-hand sides share a
+// site's index, link and scale work) from 8 right-hand sides up (L = 512, 32 RHS: D 55.3 against
+// 57.4 us, D^dag with the fused norm 66.0 against 71.2 us); SMG_DSLASH_H_NP=1 or 2 fixes it
 int dslash_h_np(int nrhs) {
     static const int env = [] {
         const char* e = std::getenv("SMG_DSLASH_H_NP");
         return e ? std::atoi(e) : 0;
     }();
-    const int np = env == 1 || env == 2 ? env : 1;
+    const int np = env == 1 || env == 2 ? env : (nrhs >= 8 ? 2 : 1);
     return nrhs >= 4 * np ? np : 1;
 }
 
@@ -439,27 +441,33 @@ __global__ void __launch_bounds__(256) k_dots_stage(const float* __restrict__ pa
 }
 
 // the MR step's reductions per rhs from the two norm columns: out[3 rhs] = ||D r||^2 (= <A r, r> for
-// A = D^dag D), out[3 rhs + 1] = 0, out[3 rhs + 2] = ||A r||^2
+// A = D^dag D), out[3 rhs + 1] = 0, out[3 rhs + 2] = ||A r||^2, and the step's omega = out[3 rhs] /
+// out[3 rhs + 2] as a float pair (0 when the denominator is not a usable number); one block per rhs
 __global__ void __launch_bounds__(256) k_mr_norms_finish(const double* __restrict__ mid, int G,
-                                                         double* __restrict__ out) {
-    __shared__ double s[256];
-    const int j = blockIdx.x;  // column: rhs * 2 + which
-    double acc = 0.0;
-    for (int g = threadIdx.x; g < G; g += blockDim.x) acc += mid[(int64_t)j * G + g];
-    s[threadIdx.x] = acc;
+                                                         double* __restrict__ out, float2* __restrict__ omega) {
+    __shared__ double s[2][256];
+    const int rhs = blockIdx.x;
+    double a0 = 0.0, a1 = 0.0;
+    for (int g = threadIdx.x; g < G; g += blockDim.x) {
+        a0 += mid[(int64_t)(2 * rhs) * G + g];
+        a1 += mid[(int64_t)(2 * rhs + 1) * G + g];
+    }
+    s[0][threadIdx.x] = a0;
+    s[1][threadIdx.x] = a1;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+        if ((int)threadIdx.x < o) {
+            s[0][threadIdx.x] += s[0][threadIdx.x + o];
+            s[1][threadIdx.x] += s[1][threadIdx.x + o];
+        }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        const int rhs = j >> 1;
-        if (j & 1) {
-            out[3 * rhs + 2] = s[0];
-        } else {
-            out[3 * rhs] = s[0];
-            out[3 * rhs + 1] = 0.0;
-        }
+        const double num = s[0][0], den = s[1][0];
+        out[3 * rhs] = num;
+        out[3 * rhs + 1] = 0.0;
+        out[3 * rhs + 2] = den;
+        if (omega) omega[rhs] = make_float2((fabs(den) >= 1e-30 && isfinite(den)) ? (float)(num / den) : 0.f, 0.f);
     }
 }
 
@@ -534,13 +542,13 @@ int dslash_h_blocks(int L, int nrhs) {
 
 // the MR step's scalars from the norm partials of its two stencils (columns 0 and 1 of part):
 // out3[rhs][3] = (||D r||^2, 0, ||D^dag D r||^2)
-smg_status launch_mr_norms_finish(smg_context* ctx, int L, int nrhs, const float* part, double* out3) {
+smg_status launch_mr_norms_finish(smg_context* ctx, int L, int nrhs, const float* part, double* out3, float* omega) {
     const int ncol = nrhs * 2, nblocks = dslash_h_blocks(L, nrhs);
     const int groups = 256 / ncol, R = groups * kDotsRows;  // rows per first-pass block
     const int G = (nblocks + R - 1) / R;
     SMG_TRY(smg_reduce_reserve(ctx, (size_t)G * ncol));
     k_dots_stage<<<G, groups * ncol, 0, ctx->stream>>>(part, nblocks, ncol, R, ctx->red.partials);
-    k_mr_norms_finish<<<ncol, 256, 0, ctx->stream>>>(ctx->red.partials, G, out3);
+    k_mr_norms_finish<<<nrhs, 256, 0, ctx->stream>>>(ctx->red.partials, G, out3, reinterpret_cast<float2*>(omega));
     count_launch(ctx, 2);
     SMG_CHECK_LAUNCH(ctx);
     return SMG_OK;
@@ -898,8 +906,9 @@ smg_status smg_dslash_h_norm(smg_dirac* d, bool dag, const smg_field* src, smg_f
                              int part_col) {
     return launch_dslash_h(d, dag, src, dst, part, part_col);
 }
-smg_status smg_mr_norms_finish(smg_context* ctx, int L, int nrhs, const float* part, double* out3_dev) {
-    return launch_mr_norms_finish(ctx, L, nrhs, part, out3_dev);
+smg_status smg_mr_norms_finish(smg_context* ctx, int L, int nrhs, const float* part, double* out3_dev,
+                               float* omega_dev) {
+    return launch_mr_norms_finish(ctx, L, nrhs, part, out3_dev, omega_dev);
 }
 int smg_dslash_h_blocks(int L, int nrhs) { return dslash_h_blocks(L, nrhs); }
 // reduction scratch (doubles) the fused FP16 stencil norms use for a lattice and nrhs

@@ -38,7 +38,8 @@ smg_status smg_dslash_mr(smg_dirac* d, bool dag, const smg_field* src, smg_field
                          double* out3_dev);
 smg_status smg_dslash_h_norm(smg_dirac* d, bool dag, const smg_field* src, smg_field* dst, float* part,
                              int part_col);
-smg_status smg_mr_norms_finish(smg_context* ctx, int L, int nrhs, const float* part, double* out3_dev);
+smg_status smg_mr_norms_finish(smg_context* ctx, int L, int nrhs, const float* part, double* out3_dev,
+                               float* omega_dev);
 int smg_dslash_h_blocks(int L, int nrhs);
 size_t smg_dslash_h_dots_scratch(int L, int nrhs);
 // tensor-core coarse apply (coarse_tc.cu)
@@ -1096,6 +1097,7 @@ struct smg_mg {
     smg_field* f_res = nullptr;
     float* hdots = nullptr;
     double* mr_om = nullptr;
+    float2* mr_omf = nullptr;  // each step's omega per rhs, as the update kernels read it
     std::vector<CoarseWork> cw;
     double* scal = nullptr;  // per-level scalar area
     size_t scal_doubles = 0;
@@ -1325,6 +1327,8 @@ smg_status free_work(smg_mg* mg) {
     mg->hdots = nullptr;
     if (mg->mr_om) cudaFree(mg->mr_om);
     mg->mr_om = nullptr;
+    if (mg->mr_omf) cudaFree(mg->mr_omf);
+    mg->mr_omf = nullptr;
     for (auto& w : mg->cw) {
         for (void* p : {w.b, w.x, w.r, w.Ar, w.e, w.p})
             if (p) cudaFree(p);
@@ -1405,6 +1409,8 @@ smg_status ensure_work(smg_mg* mg, int nrhs, smg_precision prec) {
         SMG_CUDA(ctx, cudaMalloc(&mg->hdots, (size_t)smg_dslash_h_blocks(L, nrhs) * nrhs * 2 * sizeof(float)));
         SMG_CUDA(ctx, cudaMalloc(&mg->mr_om, (size_t)nsteps * 3 * nrhs * sizeof(double)));
         SMG_CUDA(ctx, cudaMemsetAsync(mg->mr_om, 0, (size_t)nsteps * 3 * nrhs * sizeof(double), ctx->stream));
+        SMG_CUDA(ctx, cudaMalloc(&mg->mr_omf, (size_t)nsteps * nrhs * sizeof(float2)));
+        SMG_CUDA(ctx, cudaMemsetAsync(mg->mr_omf, 0, (size_t)nsteps * nrhs * sizeof(float2), ctx->stream));
         SMG_TRY(smg_reduce_reserve(ctx, smg_dslash_h_dots_scratch(L, nrhs)));  // before any capture
     } else {
         SMG_TRY(smg_field_create(ctx, L, nrhs, wp, &mg->f_r));
@@ -1474,27 +1480,17 @@ __global__ void __launch_bounds__(256) k_sub_h(const cx<float>* __restrict__ b, 
 
 // The MR steps of the FP16 smoother keep every residual r_0 .. r_n (a ring of FP16 fields) and
 // leave x alone until the end, where one pass adds sum_k omega_k r_k: the FP32 x is read and
-// written once per smoothing instead of once per step.  omega_k per rhs comes from sc_k[rhs][3]
-// (MR: (re, im) of <A r, r> and ||A r||^2) or is a fixed Richardson omega.
+// written once per smoothing instead of once per step.  omega_k per rhs is the step's MR value,
+// ||D r||^2 / ||A r||^2 as the norm-finishing kernel stored it, or a fixed Richardson omega.
 constexpr int kMaxMrSteps = 16;  // residuals one x pass combines
-
-__device__ __forceinline__ cx<float> mr_omega(const double* __restrict__ sc, int rr) {
-    const double den = sc[3 * rr + 2];
-    return (fabs(den) >= 1e-30 && isfinite(den)) ? mk((float)(sc[3 * rr] / den), (float)(sc[3 * rr + 1] / den))
-                                                 : mk(0.f, 0.f);
-}
 
 // r_out = r_in - omega A r (FP16 fields); a thread owns one pair of adjacent right-hand sides
 __global__ void __launch_bounds__(256) k_mr_rupdate_h(const __half2* __restrict__ r, const float* __restrict__ rs,
                                                       const __half2* __restrict__ ar, const float* __restrict__ ars,
                                                       __half2* __restrict__ ro, float* __restrict__ ros,
-                                                      const double* __restrict__ sc, float omega, int nsites,
+                                                      const float2* __restrict__ om, float omega, int nsites,
                                                       int nrhs) {
-    __shared__ cx<float> s_om[32];
     const int lanes = blockDim.x, rhs0 = 2 * threadIdx.x;
-    const int tid = threadIdx.y * lanes + threadIdx.x;
-    if (tid < nrhs) s_om[tid] = sc ? mr_omega(sc, tid) : mk(omega, 0.f);
-    __syncthreads();
     const int s = blockIdx.x * blockDim.y + threadIdx.y;
     const bool valid = s < nsites;
     Spinor<float> rn[2];
@@ -1504,10 +1500,10 @@ __global__ void __launch_bounds__(256) k_mr_rupdate_h(const __half2* __restrict_
         ld_pairs_h<1>(r, s, rhs0, nrhs, rv);
         ld_pairs_h<1>(ar, s, rhs0, nrhs, av);
         const float sr = rs[s], sa = ars[s];
+        const float4 o = om ? __ldg(reinterpret_cast<const float4*>(om + rhs0)) : make_float4(omega, 0.f, omega, 0.f);
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
-            const cx<float> om = s_om[rhs0 + k];
-            const cx<float> oa = mk(om.re * sa, om.im * sa);
+            const cx<float> oa = k == 0 ? mk(o.x * sa, o.y * sa) : mk(o.z * sa, o.w * sa);
             rn[k].s0 = sr * rv[k].s0 - oa * av[k].s0;
             rn[k].s1 = sr * rv[k].s1 - oa * av[k].s1;
         }
@@ -1520,16 +1516,11 @@ struct ResidualRing {
     const float* s[kMaxMrSteps];
 };
 
-// x = (x_zero ? 0 : x) + sum_{k < n} omega_k r_k, omega_k from sc + k * 3 nrhs or fixed
+// x = (x_zero ? 0 : x) + sum_{k < n} omega_k r_k, omega_k = om[k * nrhs + rhs] or fixed
 __global__ void __launch_bounds__(256) k_mr_xupdate_h(cx<float>* __restrict__ x, ResidualRing ring, int n,
-                                                      const double* __restrict__ sc, float omega, int x_zero,
+                                                      const float2* __restrict__ om, float omega, int x_zero,
                                                       int nsites, int nrhs) {
-    __shared__ cx<float> s_om[kMaxMrSteps * 32];
-    const int lanes = blockDim.x, rhs0 = 2 * threadIdx.x;
-    const int tid = threadIdx.y * lanes + threadIdx.x;
-    for (int i = tid; i < n * nrhs; i += blockDim.x * blockDim.y)
-        s_om[i] = sc ? mr_omega(sc + (size_t)(i / nrhs) * 3 * nrhs, i % nrhs) : mk(omega, 0.f);
-    __syncthreads();
+    const int rhs0 = 2 * threadIdx.x;
     const int s = blockIdx.x * blockDim.y + threadIdx.y;
     if (s >= nsites) return;
     Spinor<float> xv[2];
@@ -1542,10 +1533,11 @@ __global__ void __launch_bounds__(256) k_mr_xupdate_h(cx<float>* __restrict__ x,
         Spinor<float> rv[2];
         ld_pairs_h<1>(ring.r[k], s, rhs0, nrhs, rv);
         const float sr = ring.s[k][s];
+        const float4 o =
+            om ? __ldg(reinterpret_cast<const float4*>(om + (size_t)k * nrhs + rhs0)) : make_float4(omega, 0.f, omega, 0.f);
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-            const cx<float> om = s_om[k * nrhs + rhs0 + j];
-            const cx<float> os = mk(om.re * sr, om.im * sr);
+            const cx<float> os = j == 0 ? mk(o.x * sr, o.y * sr) : mk(o.z * sr, o.w * sr);
             xv[j].s0 = xv[j].s0 + os * rv[j].s0;
             xv[j].s1 = xv[j].s1 + os * rv[j].s1;
         }
@@ -1571,8 +1563,8 @@ smg_status mr_xupdate_h(smg_mg* mg, smg_field* x, int first, int n, bool x_zero,
         ring.r[k] = (const __half2*)mg->f_rs[first + k]->data;
         ring.s[k] = mg->f_rs[first + k]->scale;
     }
-    const double* sc = omega > 0 ? nullptr : mg->mr_om + (size_t)first * 3 * nrhs;
-    k_mr_xupdate_h<<<pair_grid(V, nrhs), pair_block(nrhs), 0, ctx->stream>>>((cx<float>*)x->data, ring, n, sc,
+    const float2* om = omega > 0 ? nullptr : mg->mr_omf + (size_t)first * nrhs;
+    k_mr_xupdate_h<<<pair_grid(V, nrhs), pair_block(nrhs), 0, ctx->stream>>>((cx<float>*)x->data, ring, n, om,
                                                                              (float)omega, x_zero ? 1 : 0, V, nrhs);
     count_launch(ctx);
     SMG_CHECK_LAUNCH(ctx);
@@ -1588,14 +1580,15 @@ smg_status mr_step_h(smg_mg* mg, int it, double omega, bool write_next) {
     const int V = r->g.V, nrhs = r->nrhs;
     const bool mr = !(omega > 0);
     double* sc = mg->mr_om + (size_t)it * 3 * nrhs;
+    float2* om = mg->mr_omf + (size_t)it * nrhs;
     SMG_TRY(smg_dslash_h_norm(mg->dirac, false, r, t, mr ? mg->hdots : nullptr, 0));
     SMG_TRY(smg_dslash_h_norm(mg->dirac, true, t, Ar, mr ? mg->hdots : nullptr, 1));
-    if (mr) SMG_TRY(smg_mr_norms_finish(ctx, r->g.L, nrhs, mg->hdots, sc));
+    if (mr) SMG_TRY(smg_mr_norms_finish(ctx, r->g.L, nrhs, mg->hdots, sc, reinterpret_cast<float*>(om)));
     if (write_next) {
         smg_field* rn = mg->f_rs[it + 1];
         k_mr_rupdate_h<<<pair_grid(V, nrhs), pair_block(nrhs), 0, ctx->stream>>>(
             (const __half2*)r->data, r->scale, (const __half2*)Ar->data, Ar->scale, (__half2*)rn->data, rn->scale,
-            mr ? sc : nullptr, (float)omega, V, nrhs);
+            mr ? om : nullptr, (float)omega, V, nrhs);
         count_launch(ctx);
     }
     SMG_CHECK_LAUNCH(ctx);
@@ -3021,12 +3014,14 @@ SMG_API smg_status smg_mg_time_smoother(smg_mg* mg, const smg_field* b, int reps
         SMG_CUDA(ctx, cudaEventRecord(ev[1], ctx->stream));
         for (int i = 0; i < reps && st == SMG_OK; ++i) {
             st = smg_dslash_h_norm(mg->dirac, true, t, Ar, mg->hdots, 1);
-            if (st == SMG_OK) st = smg_mr_norms_finish(ctx, b->g.L, nrhs, mg->hdots, sc);
+            if (st == SMG_OK)
+                st = smg_mr_norms_finish(ctx, b->g.L, nrhs, mg->hdots, sc, reinterpret_cast<float*>(mg->mr_omf));
         }
         SMG_CUDA(ctx, cudaEventRecord(ev[2], ctx->stream));
         for (int i = 0; i < reps; ++i) {
             k_mr_rupdate_h<<<grd, blk, 0, ctx->stream>>>((const __half2*)r->data, r->scale, (const __half2*)Ar->data,
-                                                         Ar->scale, (__half2*)rn->data, rn->scale, sc, 0.f, V, nrhs);
+                                                         Ar->scale, (__half2*)rn->data, rn->scale, mg->mr_omf, 0.f, V,
+                                                         nrhs);
             count_launch(ctx);
         }
         SMG_CUDA(ctx, cudaEventRecord(ev[3], ctx->stream));
