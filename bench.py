@@ -13,8 +13,9 @@ is reported.  Workloads:
   m = -0.05, c_sw = 1; three levels (4 x 4 then 2 x 2 aggregates, 16 null
   vectors per level = 16 coarse dofs, V-cycle); 32 right-hand sides solved
   together to a true FP64 residual of 1e-10 by an FP32 GCR (truncation 6)
-  preconditioned with the FP32 hierarchy, whose fine smoother keeps its work
-  vectors in FP16 with per-site scales, inside FP64 defect correction.  The
+  preconditioned with the FP32 hierarchy, whose fine smoother and coarsest CG
+  keep their work vectors in FP16 with per-site scales, inside FP64 defect
+  correction.  The
   hierarchy is built once before timing.  value = solves/s.  The plain FP64
   single-RHS MG on the same inputs is measured beside it
   (detail.plain_fp64_mg_solves_per_s).
@@ -221,6 +222,7 @@ def workload_config(workload: str, args) -> tuple[dict, dict]:
         if args.coarse_iters:
             c["coarse_max_iter"] = args.coarse_iters
         c["smoother_half"] = args.smoother == "f16" and workload != "mg2"
+        c["coarse_half"] = args.coarse_prec == "f16" and workload != "mg2"
         L, nrhs = c["L"], c["nrhs"]
         blk = ", ".join(f"{a}x{b}" for a, b in c["blocks"])
         vecs = f"{c['n_vec']} null vectors{' split by chirality' if c['chiral'] else ''}"
@@ -277,7 +279,8 @@ def mg_params(smg, c, precision):
     return smg.mg_params(c["levels"], c["blocks"][0][0], c["n_vec"], blocks=c["blocks"], chiral_split=c["chiral"],
                          null_iters=c["null_iters"], pre_smooth=c["pre"], post_smooth=c["post"], w_cycle=c["w_cycle"],
                          coarse_max_iter=c["coarse_max_iter"], coarse_tol=c["coarse_tol"], precision=precision,
-                         seed=c["seed"], smoother_half=c.get("smoother_half", False) and precision == "f32")
+                         seed=c["seed"], smoother_half=c.get("smoother_half", False) and precision == "f32",
+                         coarse_half=c.get("coarse_half", False) and precision == "f32")
 
 
 def kernel_trace(step, ctx, path: str, what: str) -> None:
@@ -432,6 +435,7 @@ def run_ours(args, ws, rank, local):
         it64, res64 = res.iterations, res.true_residual
         detail = {"gcr_iterations": iters, "true_residual": true_res, "setup_s": setup_s,
                   "smoother_work_vectors": "FP16, per-site scales" if c["smoother_half"] and nrhs >= 8 else "FP32",
+                  "coarsest_cg_vectors": "FP16, per-site scales" if c["coarse_half"] and nrhs == 32 else "FP32",
                   "plain_fp64_mg_solves_per_s": 1e3 / ms64, "plain_fp64_mg_iterations": it64,
                   "plain_fp64_mg_true_residual": res64, "mixed_batched_over_plain_fp64": value / ws / (1e3 / ms64),
                   "launches_before_timed": int(l0)}
@@ -928,6 +932,9 @@ def main():
     ap.add_argument("--nrhs", type=int, default=0, help="right-hand-side count override")
     ap.add_argument("--smoother", default="f16", choices=["f32", "f16"],
                     help="mg workload: precision of the fine smoother's work vectors (f16: per-site scaled FP16)")
+    ap.add_argument("--coarse-prec", default="f16", choices=["f32", "f16"],
+                    help="mg workload: precision of the coarsest CG's residual and search direction (f16: per-site "
+                         "scaled FP16)")
     ap.add_argument("--trunc", type=int, default=0, help="mg / batch workloads: GCR truncation override")
     ap.add_argument("--coarse-iters", type=int, default=0, help="mg / batch workloads: coarsest-CG iteration cap override")
     ap.add_argument("--workers", type=int, default=0, help="batch workload: host worker threads override")

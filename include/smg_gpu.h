@@ -315,6 +315,10 @@ typedef struct {
                                           vectors (residual, A r, D r) in FP16 with one FP32 scale
                                           per site, arithmetic in FP32 (power-of-two nrhs from 8
                                           to 32); 0 (default): FP32 */
+    int coarse_half;                   /* 1: an F32 hierarchy keeps the coarsest-level CG's residual
+                                          and search direction in FP16 with one FP32 scale per coarse
+                                          site (the tensor-core path: 16 dofs, 32 right-hand sides),
+                                          arithmetic and accumulation in FP32; 0 (default): FP32 */
 } smg_mg_params;
 
 /* Fills p with the reference's defaults: 2 levels, 4 x 4 blocks, 4 null

@@ -97,7 +97,8 @@ class MGParams(C.Structure):
                 ("n_vec", C.c_int * (MAX_LEVELS - 1)), ("chiral_split", C.c_int), ("null_iters", C.c_int),
                 ("null_mr_steps", C.c_int), ("pre_smooth", C.c_int), ("post_smooth", C.c_int), ("w_cycle", C.c_int),
                 ("coarse_max_iter", C.c_int), ("coarse_tol", C.c_double), ("precision", C.c_int),
-                ("seed", C.c_uint32), ("tensor_cores", C.c_int), ("smoother_half", C.c_int)]
+                ("seed", C.c_uint32), ("tensor_cores", C.c_int), ("smoother_half", C.c_int),
+                ("coarse_half", C.c_int)]
 
 
 _vp = C.c_void_p

@@ -720,13 +720,14 @@ def mg_params(n_levels: int = 2, block_size: int = 4, k_null: int = 4, coarse_bl
               w_cycle: bool = True, pre_smooth: int = 3, post_smooth: int = 3, chiral_split: bool = False,
               blocks=None, n_vecs=None, null_mr_steps: int = 5, coarse_max_iter: int = 200,
               coarse_tol: float = 1e-12, precision: str = "f64", seed: int = 42,
-              tensor_cores: bool = True, smoother_half: bool = False) -> _L.MGParams:
+              tensor_cores: bool = True, smoother_half: bool = False, coarse_half: bool = False) -> _L.MGParams:
     """smg_mg_params from the reference's build_mg_hierarchy arguments
     (src/multigrid.cpp:595-602).  `blocks` / `n_vecs` override the per-level
     aggregate shapes and null-vector counts.  `tensor_cores` lets an F32
     hierarchy apply its batched coarse operators on the tensor cores;
     `smoother_half` keeps its fine smoother's work vectors in FP16 with
-    per-site scales."""
+    per-site scales; `coarse_half` does the same for the coarsest-level
+    CG's residual and search direction."""
     p = _L.MGParams()
     _L.check(_L.lib().smg_mg_params_default(C.byref(p)), "smg_mg_params_default")
     p.n_levels = n_levels
@@ -745,6 +746,7 @@ def mg_params(n_levels: int = 2, block_size: int = 4, k_null: int = 4, coarse_bl
     p.seed = seed
     p.tensor_cores = int(tensor_cores)
     p.smoother_half = int(smoother_half)
+    p.coarse_half = int(coarse_half)
     return p
 
 

@@ -48,6 +48,7 @@
 // the CTA raises *err = 2, waits (bounded) for its own bulk copies and MMAs,
 // frees its tensor memory and returns.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <cstdlib>
 #include <map>
@@ -232,6 +233,11 @@ struct TcArgs {
     const float2* x = nullptr;       // [site][dof][nrhs]
     float2* y = nullptr;
     const float2* w = nullptr;       // EPI 2
+    // HIN: x and w in FP16 with one FP32 scale per site (x = xh * xs[site], w = wh * ws[site])
+    const __half2* xh = nullptr;
+    const float* xs = nullptr;
+    const __half* wh = nullptr;
+    const float* ws = nullptr;
     double* partials = nullptr;
     unsigned int* tickets = nullptr;
     double* out = nullptr;
@@ -240,7 +246,7 @@ struct TcArgs {
     int nx = 0, ny = 0, nrhs = 0, H = 0;
 };
 
-template <int EPI>
+template <int EPI, bool HIN = false>
 __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
     if (a.gate && *a.gate == 0) return;  // every right-hand side of the solve has converged
     constexpr int K = EPI == 2 ? 3 : 1;
@@ -373,10 +379,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
             float wb[kEpiSites][kNc];
             if (EPI == 2) {
 #pragma unroll
-                for (int q = 0; q < kEpiSites; ++q)
+                for (int q = 0; q < kEpiSites; ++q) {
+                    const int64_t wi = (row0 + (int64_t)q * kNc * nrhs) * 2 + c;
+                    if (HIN) {
+                        const float sq = __ldcg(a.ws + (x0 + half * kEpiSites + q) + (int64_t)nx * (y0 + r));
 #pragma unroll
-                    for (int k = 0; k < kNc; ++k)
-                        wb[q][k] = __ldcg(wbase + (row0 + (int64_t)q * kNc * nrhs) * 2 + c + k * rstride);
+                        for (int k = 0; k < kNc; ++k) wb[q][k] = __half2float(__ldcg(a.wh + wi + k * rstride)) * sq;
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < kNc; ++k) wb[q][k] = __ldcg(wbase + wi + k * rstride);
+                    }
+                }
             }
             bool ok = wait_bar(bar(kBarAccFull + (r & 1)), (r >> 1) & 1, abort_flag);
             if (!__all_sync(0xffffffffu, ok)) break;
@@ -441,10 +454,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
                 const int item = st + it * 128;
                 const int r = item & 31, g = (item >> 5) & 1, t = item >> 6;
                 const int gx = wrapi(x0 - 1 + t, nx);
-                const float2* src = a.x + ((int64_t)(gx + (int64_t)nx * gy) * kNc + g * 8) * nrhs + rhs0 + r;
+                const int64_t off = ((int64_t)(gx + (int64_t)nx * gy) * kNc + g * 8) * nrhs + rhs0 + r;
                 float2 e[8];
+                if (HIN) {
+                    const float sc = __ldg(a.xs + gx + (int64_t)nx * gy);
 #pragma unroll
-                for (int j = 0; j < 8; ++j) e[j] = src[(int64_t)j * nrhs];
+                    for (int j = 0; j < 8; ++j) {
+                        const float2 h = __half22float2(a.xh[off + (int64_t)j * nrhs]);
+                        e[j] = make_float2(h.x * sc, h.y * sc);
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) e[j] = a.x[off + (int64_t)j * nrhs];
+                }
                 uint4 re, im;
                 re.x = pack_bf16(e[0].x, e[1].x);
                 re.y = pack_bf16(e[2].x, e[3].x);
@@ -560,7 +582,8 @@ int rows_per_cta_rule(int nx, int ny, int nz) {
 // Rows per CTA chosen by timing for a lattice and right-hand-side count (smg_coarse_tc_tune); the
 // rule above until then.  Shared by every context of the process.
 smg_status launch_tc(smg_context* ctx, const void* links, int nx, int ny, int nrhs, int H, const cx<float>* x,
-                     cx<float>* y, int epi, const cx<float>* w, double* out, const int* gate, int* err);
+                     cx<float>* y, int epi, const cx<float>* w, double* out, const int* gate, int* err,
+                     const TcArgs* half_in = nullptr);
 
 std::mutex g_rows_mu;
 std::map<std::tuple<int, int, int>, int> g_rows;
@@ -586,6 +609,8 @@ smg_status smg_coarse_tc_tile_links(smg_context* ctx, const cx<double>* A64, int
     SMG_CUDA(ctx, cudaFuncSetAttribute(k_coarse_apply_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     SMG_CUDA(ctx, cudaFuncSetAttribute(k_coarse_apply_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     SMG_CUDA(ctx, cudaFuncSetAttribute(k_coarse_apply_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
+    SMG_CUDA(ctx, cudaFuncSetAttribute(k_coarse_apply_tc<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       kSmemBytes));
     return SMG_OK;
 }
 
@@ -597,6 +622,23 @@ smg_status smg_coarse_tc_apply(smg_context* ctx, const void* links, int nx, int 
         return smg_fail(ctx, SMG_UNSUPPORTED, "tensor-core coarse apply: shape not supported");
     const int nz = nrhs / kRhsTile;
     return launch_tc(ctx, links, nx, ny, nrhs, rows_per_cta(nx, ny, nz), x, y, epi, w, out, gate, err);
+}
+
+// y = A x with x and w in FP16 with one FP32 scale per site ([site][dof][rhs] __half2, scales
+// [site]) and the fused <y, w>, ||y||^2 per rhs; y in FP32
+smg_status smg_coarse_tc_apply_h(smg_context* ctx, const void* links, int nx, int ny, int nrhs, const void* xh,
+                                 const float* xs, cx<float>* y, const void* wh, const float* ws, double* out,
+                                 const int* gate, int* err) {
+    if (!smg_coarse_tc_shape_ok(nx, ny, kNc) || nrhs % kRhsTile != 0 || nrhs / kRhsTile > kMaxTickets || !xh ||
+        !xs || !wh || !ws)
+        return smg_fail(ctx, SMG_UNSUPPORTED, "tensor-core coarse apply on FP16 vectors: shape not supported");
+    TcArgs h;
+    h.xh = static_cast<const __half2*>(xh);
+    h.xs = xs;
+    h.wh = static_cast<const __half*>(wh);
+    h.ws = ws;
+    const int nz = nrhs / kRhsTile;
+    return launch_tc(ctx, links, nx, ny, nrhs, rows_per_cta(nx, ny, nz), nullptr, y, 2, nullptr, out, gate, err, &h);
 }
 
 // Times every rows-per-CTA choice H (the divisors ny, ny / 2, ... of the lattice height) for this
@@ -666,10 +708,17 @@ smg_status smg_coarse_tc_tune(smg_context* ctx, const void* links, int nx, int n
 namespace {
 
 smg_status launch_tc(smg_context* ctx, const void* links, int nx, int ny, int nrhs, int H, const cx<float>* x,
-                     cx<float>* y, int epi, const cx<float>* w, double* out, const int* gate, int* err) {
+                     cx<float>* y, int epi, const cx<float>* w, double* out, const int* gate, int* err,
+                     const TcArgs* half_in) {
     const int nz = nrhs / kRhsTile;
     const dim3 grid(nx / kW, ny / H, nz);
     TcArgs a;
+    if (half_in) {  // FP16 x and w with per-site scales (EPI 2 only)
+        a.xh = half_in->xh;
+        a.xs = half_in->xs;
+        a.wh = half_in->wh;
+        a.ws = half_in->ws;
+    }
     a.links = static_cast<const uint8_t*>(links);
     a.x = reinterpret_cast<const float2*>(x);
     a.y = reinterpret_cast<float2*>(y);
@@ -686,7 +735,9 @@ smg_status launch_tc(smg_context* ctx, const void* links, int nx, int ny, int nr
         a.tickets = ctx->red.tickets;
         a.out = out;
     }
-    if (epi == 0)
+    if (half_in)
+        k_coarse_apply_tc<2, true><<<grid, kThreads, kSmemBytes, ctx->stream>>>(a);
+    else if (epi == 0)
         k_coarse_apply_tc<0><<<grid, kThreads, kSmemBytes, ctx->stream>>>(a);
     else if (epi == 1)
         k_coarse_apply_tc<1><<<grid, kThreads, kSmemBytes, ctx->stream>>>(a);

@@ -46,6 +46,9 @@ size_t smg_dslash_h_dots_scratch(int L, int nrhs);
 bool smg_coarse_tc_shape_ok(int nx, int ny, int ndof);
 size_t smg_coarse_tc_link_bytes(int64_t nsites);
 smg_status smg_coarse_tc_tile_links(smg_context* ctx, const cx<double>* A64, int nx, int64_t nsites, void* out);
+smg_status smg_coarse_tc_apply_h(smg_context* ctx, const void* links, int nx, int ny, int nrhs, const void* xh,
+                                 const float* xs, cx<float>* y, const void* wh, const float* ws, double* out,
+                                 const int* gate, int* err);
 smg_status smg_coarse_tc_apply(smg_context* ctx, const void* links, int nx, int ny, int nrhs, const cx<float>* x,
                                cx<float>* y, int epi, const cx<float>* w, double* out, const int* gate, int* err);
 smg_status smg_coarse_tc_tune(smg_context* ctx, const void* links, int nx, int ny, int nrhs, const cx<float>* x,
@@ -1067,6 +1070,114 @@ __global__ void k_ccg_p(CcgState s, VecView<T> p, const cx<T>* __restrict__ r) {
     for (int d = 0; d < p.ndof; ++d) p.p[base + (int64_t)d * ds] = r[base + (int64_t)d * ds] + be * p.p[base + (int64_t)d * ds];
 }
 
+// ---- the coarsest CG on FP16 vectors (coarse_half): r and p as __half2 [site][dof][rhs] with one
+// FP32 scale per coarse site (the largest |re| or |im| of all its dofs and right-hand sides), x and
+// A p in FP32, every arithmetic operation in FP32.  nrhs = 32, 16 dofs: a warp owns a site, lane =
+// right-hand side, looping over the 16 dofs (128-byte accesses per dof), so the site maximum is a
+// warp reduction; blocks of 8 warps walk the sites.
+constexpr int kCgHalfDofs = 16;
+
+__device__ __forceinline__ float warp_max(float m) {
+    for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    return m;
+}
+__device__ __forceinline__ float absmax2(cx<float> z) { return fmaxf(fabsf(z.re), fabsf(z.im)); }
+// the 16 dofs of (site, lane) in FP16 with the site maximum m (reduced over the warp)
+__device__ __forceinline__ void st_site16(__half2* f, float* sc, int64_t e0, int site, const cx<float> (&v)[kCgHalfDofs],
+                                          float m) {
+    const float inv = m > 0.f ? __fdividef(1.0f, m) : 0.f;
+#pragma unroll
+    for (int d = 0; d < kCgHalfDofs; ++d) f[e0 + d * 32] = __floats2half2_rn(v[d].re * inv, v[d].im * inv);
+    if (threadIdx.x == 0) sc[site] = m;
+}
+
+// r = p = b (FP16), x = 0, ||r||^2 per rhs into out
+__global__ void __launch_bounds__(256) k_ccgh_init(const cx<float>* __restrict__ b, cx<float>* __restrict__ x,
+                                                   __half2* __restrict__ r, float* __restrict__ rs,
+                                                   __half2* __restrict__ p, float* __restrict__ ps, int nsites,
+                                                   double* partials, unsigned int* ticket, double* out) {
+    float n2 = 0.f;
+    for (int site = blockIdx.x * blockDim.y + threadIdx.y; site < nsites; site += gridDim.x * blockDim.y) {
+        const int64_t e0 = (int64_t)site * kCgHalfDofs * 32 + threadIdx.x;
+        cx<float> v[kCgHalfDofs];
+        float m = 0.f;
+#pragma unroll
+        for (int d = 0; d < kCgHalfDofs; ++d) {
+            v[d] = b[e0 + d * 32];
+            x[e0 + d * 32] = mk(0.f, 0.f);
+            m = fmaxf(m, absmax2(v[d]));
+            n2 += norm2(v[d]);
+        }
+        m = warp_max(m);
+        st_site16(r, rs, e0, site, v, m);
+        st_site16(p, ps, e0, site, v, m);
+    }
+    double v[1] = {(double)n2};
+    block_reduce_finalise<1>(v, partials, ticket, 32, FinStore{out, 1});
+}
+
+// x += alpha p, r -= alpha A p with alpha = rr / <p, A p>; ||r||^2 -> finaliser
+__global__ void __launch_bounds__(256) k_ccgh_update(CcgState s, cx<float>* __restrict__ x, __half2* __restrict__ r,
+                                                     float* __restrict__ rs, const __half2* __restrict__ p,
+                                                     const float* __restrict__ ps, const cx<float>* __restrict__ Ap,
+                                                     int nsites, double* partials, unsigned int* ticket) {
+    if (*s.n_active == 0) return;  // read by every block before the finaliser can change it
+    const int rhs = threadIdx.x;
+    float al = 0.f;
+    if (s.active[rhs]) {
+        const double pap = s.pap3[3 * rhs];  // <Ap, p>, real for Hermitian positive A
+        if (fabs(pap) >= 1e-30 && isfinite(pap)) al = (float)(s.rr[rhs] / pap);
+    }
+    float n2 = 0.f;
+    for (int site = blockIdx.x * blockDim.y + threadIdx.y; site < nsites; site += gridDim.x * blockDim.y) {
+        const int64_t e0 = (int64_t)site * kCgHalfDofs * 32 + rhs;
+        const float sr = rs[site], sp = ps[site];
+        cx<float> rn[kCgHalfDofs];
+        float m = 0.f;
+#pragma unroll
+        for (int d = 0; d < kCgHalfDofs; ++d) {
+            const float2 rv = __half22float2(r[e0 + d * 32]);
+            const float2 pv = __half22float2(p[e0 + d * 32]);
+            const cx<float> av = Ap[e0 + d * 32];
+            cx<float> xv = x[e0 + d * 32];
+            xv.re += al * sp * pv.x;
+            xv.im += al * sp * pv.y;
+            x[e0 + d * 32] = xv;
+            rn[d] = mk(sr * rv.x - al * av.re, sr * rv.y - al * av.im);
+            m = fmaxf(m, absmax2(rn[d]));
+            n2 += norm2(rn[d]);
+        }
+        m = warp_max(m);
+        __syncwarp();  // every lane has read this site's scale before lane 0 replaces it
+        st_site16(r, rs, e0, site, rn, m);
+    }
+    double v[1] = {(double)n2};
+    block_reduce_finalise<1>(v, partials, ticket, 32, FinCcg{s});
+}
+
+// p = r + beta p
+__global__ void __launch_bounds__(256) k_ccgh_p(CcgState s, const __half2* __restrict__ r, const float* __restrict__ rs,
+                                                __half2* __restrict__ p, float* __restrict__ ps, int nsites) {
+    if (*s.n_active == 0) return;
+    const float be = (float)s.beta[threadIdx.x];
+    for (int site = blockIdx.x * blockDim.y + threadIdx.y; site < nsites; site += gridDim.x * blockDim.y) {
+        const int64_t e0 = (int64_t)site * kCgHalfDofs * 32 + threadIdx.x;
+        const float sr = rs[site], sp = ps[site] * be;
+        cx<float> pn[kCgHalfDofs];
+        float m = 0.f;
+#pragma unroll
+        for (int d = 0; d < kCgHalfDofs; ++d) {
+            const float2 rv = __half22float2(r[e0 + d * 32]);
+            const float2 pv = __half22float2(p[e0 + d * 32]);
+            pn[d] = mk(sr * rv.x + sp * pv.x, sr * rv.y + sp * pv.y);
+            m = fmaxf(m, absmax2(pn[d]));
+        }
+        m = warp_max(m);
+        __syncwarp();  // every lane has read this site's scale before lane 0 replaces it
+        st_site16(p, ps, e0, site, pn, m);
+    }
+}
+
 }  // namespace
 
 // ====================================================================== host
@@ -1078,6 +1189,12 @@ struct CoarseWork {  // per level l >= 1, per precision
     void* Ar = nullptr;
     void* e = nullptr;
     void* p = nullptr;
+    // coarsest level with coarse_half: the CG's residual and search direction in FP16 (__half2
+    // [site][dof][rhs]) with one FP32 scale per site
+    void* rh = nullptr;
+    void* ph = nullptr;
+    float* rs = nullptr;
+    float* ps = nullptr;
 };
 
 struct smg_mg {
@@ -1330,7 +1447,7 @@ smg_status free_work(smg_mg* mg) {
     if (mg->mr_omf) cudaFree(mg->mr_omf);
     mg->mr_omf = nullptr;
     for (auto& w : mg->cw) {
-        for (void* p : {w.b, w.x, w.r, w.Ar, w.e, w.p})
+        for (void* p : {w.b, w.x, w.r, w.Ar, w.e, w.p, w.rh, w.ph, (void*)w.rs, (void*)w.ps})
             if (p) cudaFree(p);
     }
     mg->cw.clear();
@@ -1388,6 +1505,13 @@ smg_status coarse_cg_persistent(smg_mg* mg, int l, void* x, const void* b) {
 
 // the fine smoother's work vectors are FP16 for F32 cycles of hierarchies that ask for it, when the
 // right-hand sides fit the FP16 writers (power-of-two lane groups) and the aggregate restriction
+// the coarsest level keeps its CG vectors in FP16 (coarse_half) on the tensor-core path with 32
+// right-hand sides (one site-block of 16 dofs x 16 right-hand-side pairs per CTA in the update kernels)
+bool coarse_half_level(const smg_mg* mg, int l, int nrhs, smg_precision prec) {
+    return mg->p.coarse_half && prec == SMG_F32 && l == (int)mg->lv.size() - 1 && nrhs == 32 &&
+           mg->lv[l].ndof == 16 && tc_path(mg, l, nrhs);
+}
+
 bool half_smoother(const smg_mg* mg, int nrhs, smg_precision prec) {
     const int nc = mg->lv[0].nc_next;
     return mg->p.smoother_half && prec == SMG_F32 && nrhs >= 8 && f16_nrhs_ok(nrhs) &&
@@ -1425,6 +1549,16 @@ smg_status ensure_work(smg_mg* mg, int nrhs, smg_precision prec) {
         for (void** p : {&w.b, &w.x, &w.r, &w.Ar, &w.e, &w.p}) {
             SMG_CUDA(ctx, cudaMalloc(p, bytes));
             SMG_CUDA(ctx, cudaMemsetAsync(*p, 0, bytes, ctx->stream));
+        }
+        if (coarse_half_level(mg, (int)l, nrhs, prec)) {
+            const size_t hb = (size_t)mg->lv[l].nsites * nrhs * mg->lv[l].ndof * sizeof(__half2);
+            const size_t sb = (size_t)mg->lv[l].nsites * sizeof(float);
+            SMG_CUDA(ctx, cudaMalloc(&w.rh, hb));
+            SMG_CUDA(ctx, cudaMalloc(&w.ph, hb));
+            SMG_CUDA(ctx, cudaMalloc((void**)&w.rs, sb));
+            SMG_CUDA(ctx, cudaMalloc((void**)&w.ps, sb));
+            SMG_CUDA(ctx, cudaMemsetAsync(w.rs, 0, sb, ctx->stream));
+            SMG_CUDA(ctx, cudaMemsetAsync(w.ps, 0, sb, ctx->stream));
         }
     }
     if (!mg->cg_state) {
@@ -1795,10 +1929,60 @@ smg_status smooth_coarse(smg_mg* mg, int l, void* x, const void* b, int niter, b
 
 // Coarsest solve: CG from x = 0 to coarse_tol (SparseCoarseOp::solve without
 // deflation, src/coarse_op.h:492-547); the host checks progress every 8 steps
+// coarse_cg with the residual and search direction in FP16 (coarse_half): the same iteration, stop
+// rule and per-rhs masks, the tensor-core apply reading p in FP16 for A p and <A p, p>
+smg_status coarse_cg_half(smg_mg* mg, int l, void* x, const void* b) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[l];
+    CoarseWork& w = mg->cw[l];
+    const int nrhs = mg->work_nrhs;
+    double* sc = lvl_scal(mg, l);
+    CcgState s;
+    s.rr = sc;
+    s.pap3 = sc + nrhs;
+    s.bnorm2 = sc + 4 * nrhs;
+    s.beta = sc + 5 * nrhs;
+    s.active = (int*)(sc + 6 * nrhs);
+    s.n_active = (int*)(sc + 7 * nrhs);
+    s.tol2 = mg->p.coarse_tol * mg->p.coarse_tol;
+    const dim3 blk(32, 8);  // lane = rhs, one site per warp
+    const int grid = std::min((L.nsites + 7) / 8, 4 * ctx->num_sms);
+    SMG_TRY(smg_reduce_reserve(ctx, (size_t)grid * nrhs));
+    __half2 *rh = (__half2*)w.rh, *ph = (__half2*)w.ph;
+    k_ccgh_init<<<grid, blk, 0, ctx->stream>>>((const cx<float>*)b, (cx<float>*)x, rh, w.rs, ph, w.ps, L.nsites,
+                                               ctx->red.partials, ctx->red.tickets, s.rr);
+    k_ccg_init<<<1, 256, 0, ctx->stream>>>(s, nrhs, 0);
+    count_launch(ctx, 2);
+    SMG_TRY(smg_host_stage_reserve(ctx, 64));
+    int* h_act = (int*)ctx->host_stage;
+    int it = 0;
+    while (it < mg->p.coarse_max_iter) {
+        int chunk = std::min(8, mg->p.coarse_max_iter - it);
+        for (int c = 0; c < chunk; ++c) {
+            SMG_TRY(smg_coarse_tc_apply_h(ctx, L.Atc, L.nx, L.ny, nrhs, ph, w.ps, (cx<float>*)w.Ar, ph, w.ps, s.pap3,
+                                          s.n_active, device_err(mg)));
+            k_ccgh_update<<<grid, blk, 0, ctx->stream>>>(s, (cx<float>*)x, rh, w.rs, ph, w.ps, (const cx<float>*)w.Ar,
+                                                         L.nsites, ctx->red.partials, ctx->red.tickets);
+            k_ccgh_p<<<grid, blk, 0, ctx->stream>>>(s, rh, w.rs, ph, w.ps, L.nsites);
+            count_launch(ctx, 2);
+            SMG_CHECK_LAUNCH(ctx);
+        }
+        it += chunk;
+        if (mg->capturing) continue;  // inside a graph: the gated kernels finish the budget as no-ops
+        SMG_CUDA(ctx, cudaMemcpyAsync(h_act, s.n_active, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (*h_act == 0) break;
+    }
+    return SMG_OK;
+}
+
 template <typename T>
 smg_status coarse_cg(smg_mg* mg, int l, void* x, const void* b) {
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[l];
+    if (std::is_same<T, float>::value && coarse_half_level(mg, l, mg->work_nrhs, SMG_F32) && mg->cw[l].rh &&
+        !(l == mg->defl.level && mg->defl.n > 0))
+        return coarse_cg_half(mg, l, x, b);
     if (mg->persistent && mg->work_nrhs == 1 && !(l == mg->defl.level && mg->defl.n > 0)) {
         if (L.ndof == 8) return coarse_cg_persistent<T, 8>(mg, l, x, b);
         if (L.ndof == 16) return coarse_cg_persistent<T, 16>(mg, l, x, b);

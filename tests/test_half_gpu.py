@@ -64,3 +64,30 @@ def test_half_smoother_cycle_and_solve(smg_gpu, nrhs, levels):
     assert r.status == 0 and r.true_residual < 1e-10
     for j in (0, nrhs - 1):
         assert np.linalg.norm(B[j] - D.apply_DdagD(r.solution[j])) / np.linalg.norm(B[j]) < 1e-10
+
+
+def test_half_coarsest_cg_cycle_and_solve(smg_gpu):
+    """The coarsest-level CG with its residual and search direction in FP16 with one FP32 scale per
+    coarse site (coarse_half; tensor-core apply on FP16 inputs): the cycle stays within the FP16
+    rounding of the FP32-vector cycle, and the mixed solve reaches a true FP64 residual of 1e-10 in at
+    most a few more iterations."""
+    L, nrhs = 64, 32
+    U = smg_gpu.gauge_normal(L, 6.0, 43)
+    lat = smg_gpu.Lattice(L)
+    D = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, U), -0.05, 1.0, 1.0, 0.0)
+    kw = dict(blocks=[(4, 4), (2, 2)], chiral_split=False, null_iters=4, pre_smooth=4, post_smooth=4,
+              w_cycle=False, coarse_max_iter=20, coarse_tol=5e-2, precision="f32", seed=11, smoother_half=True)
+    mg32 = smg_gpu.MGHierarchy(D, smg_gpu.mg_params(3, 4, 16, **kw))
+    mg16 = smg_gpu.MGHierarchy(D, smg_gpu.mg_params(3, 4, 16, coarse_half=True, **kw))
+    assert mg16.level_dims(2) == (8, 8, 16)
+    B = np.stack([smg_gpu.random_vec(lat.ndof, 70 + j) for j in range(nrhs)])
+    b32 = smg_gpu.Field(lat, nrhs, "f32", data=B)
+    c32 = mg32.precondition(b32).download()
+    c16 = mg16.precondition(b32).download()
+    assert np.linalg.norm(c16 - c32) / np.linalg.norm(c32) < 2e-2
+    r32 = smg_gpu.fcg_solve_mg(D, lat.ndof, B, mg32, 300, 1e-10, 20)
+    r16 = smg_gpu.fcg_solve_mg(D, lat.ndof, B, mg16, 300, 1e-10, 20)
+    assert r16.status == 0 and r16.true_residual < 1e-10
+    assert r16.iterations <= 1.1 * r32.iterations + 2
+    for j in (0, nrhs - 1):
+        assert np.linalg.norm(B[j] - D.apply_DdagD(r16.solution[j])) / np.linalg.norm(B[j]) < 1e-10
