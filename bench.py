@@ -328,7 +328,7 @@ def kernel_trace(step, ctx, path: str, what: str) -> None:
 # profiles/smoother_f16_L512_32rhs.md)
 TC_LEVEL1_L512_DRAM_BYTES = 226.540288e6 + 42.035968e6
 DSLASH_F32_L512_DRAM_BYTES = 140.034048e6 + 98.370048e6
-SMOOTHER_D_L512_DRAM_BYTES = None
+SMOOTHER_D_L512_DRAM_BYTES = 74.601984e6 + 31.954176e6
 
 
 def coarse_kernel_name(c, L, nrhs):
