@@ -370,27 +370,30 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
         const int64_t rstride = 2ll * nrhs;  // floats between consecutive dofs
         const float* __restrict__ wbase = reinterpret_cast<const float*>(a.w);
         float* __restrict__ ybase = reinterpret_cast<float*>(a.y);
-        for (int r = 0; r < H; ++r) {
-            // site x0 + half * kEpiSites
-            const int64_t row0 =
-                ((int64_t)x0 + half * kEpiSites + (int64_t)nx * (y0 + r)) * kNc * nrhs + rhs0 + rhs;
-            // EPI 2: w of this thread's sites is requested before the accumulators are ready, so the
-            // L2 latency overlaps the wait
-            float wb[kEpiSites][kNc];
-            if (EPI == 2) {
+        // first entry of this thread's (rhs, re/im) for site q of the pair's half of output row r
+        auto entry = [&](int r, int q) {
+            return (((int64_t)x0 + half * kEpiSites + q + (int64_t)nx * (y0 + r)) * kNc * nrhs + rhs0 + rhs) * 2 + c;
+        };
+        // EPI 2: w of site q of row r into wb[q].  Software-pipelined: row 0 is requested before the
+        // first accumulator wait, row r + 1's site q right after row r's site q has used wb[q], so the
+        // loads have a whole row of epilogue work to land instead of stalling every row
+        float wb[kEpiSites][kNc];
+        auto load_w = [&](int r, int q) {
+            const int64_t wi = entry(r, q);
+            if (HIN) {
+                const float sq = __ldcg(a.ws + (x0 + half * kEpiSites + q) + (int64_t)nx * (y0 + r));
 #pragma unroll
-                for (int q = 0; q < kEpiSites; ++q) {
-                    const int64_t wi = (row0 + (int64_t)q * kNc * nrhs) * 2 + c;
-                    if (HIN) {
-                        const float sq = __ldcg(a.ws + (x0 + half * kEpiSites + q) + (int64_t)nx * (y0 + r));
+                for (int k = 0; k < kNc; ++k) wb[q][k] = __half2float(__ldcg(a.wh + wi + k * rstride)) * sq;
+            } else {
 #pragma unroll
-                        for (int k = 0; k < kNc; ++k) wb[q][k] = __half2float(__ldcg(a.wh + wi + k * rstride)) * sq;
-                    } else {
-#pragma unroll
-                        for (int k = 0; k < kNc; ++k) wb[q][k] = __ldcg(wbase + wi + k * rstride);
-                    }
-                }
+                for (int k = 0; k < kNc; ++k) wb[q][k] = __ldcg(wbase + wi + k * rstride);
             }
+        };
+        if (EPI == 2) {
+#pragma unroll
+            for (int q = 0; q < kEpiSites; ++q) load_w(0, q);
+        }
+        for (int r = 0; r < H; ++r) {
             bool ok = wait_bar(bar(kBarAccFull + (r & 1)), (r >> 1) & 1, abort_flag);
             if (!__all_sync(0xffffffffu, ok)) break;
             tc_fence_after();
@@ -399,7 +402,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
                 const int i = half * kEpiSites + q;
                 float d[32];
                 tmem_ld32(tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)((r & 1) * kAccCols + 32 * i), d);
-                const int64_t base = (row0 + (int64_t)q * kNc * nrhs) * 2 + c;
+                const int64_t base = entry(r, q);
                 float o[kNc];
 #pragma unroll
                 for (int k = 0; k < kNc; ++k) {
@@ -419,6 +422,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
                         s2 += o[k] * o[k];
                     }
                 }
+                if (EPI == 2 && r + 1 < H) load_w(r + 1, q);
 #pragma unroll
                 for (int k = 0; k < kNc; ++k) ybase[base + k * rstride] = o[k];
                 if (EPI == 1) {

@@ -388,6 +388,123 @@ __global__ void __launch_bounds__(256) k_dslash_h(DslashH a) {
     }
 }
 
+// The MG smoother's FP16 -> FP16 stencil in its one production shape: 32 right-hand sides in two
+// pairs per thread (8 threads per site, compile-time lane groups), r = 1, no twisted mass.  The spin
+// projections of the four neighbours are formed on the packed FP16 pairs before conversion (one
+// packed add, or a half swap and a packed fma for the +-i sigma_2 hops, where the generic kernel
+// converts both spin components and adds in FP32); the extra rounding of that sum is of the size of
+// the fields' own FP16 storage error.  The diagonal is real (the centre's site scale folded in).
+__device__ __forceinline__ __half2 h2_of(unsigned u) { return *reinterpret_cast<const __half2*>(&u); }
+__device__ __forceinline__ cx<float> cx_of(__half2 h) {
+    const float2 f = __half22float2(h);
+    return mk(f.x, f.y);
+}
+// s0 + s1, s0 - s1, s0 + i s1, s0 - i s1 on (re, im) FP16 pairs
+__device__ __forceinline__ __half2 proj_add(__half2 s0, __half2 s1) { return __hadd2(s0, s1); }
+__device__ __forceinline__ __half2 proj_sub(__half2 s0, __half2 s1) { return __hsub2(s0, s1); }
+__device__ __forceinline__ __half2 proj_addi(__half2 s0, __half2 s1) {
+    return __hfma2(__lowhigh2highlow(s1), __floats2half2_rn(-1.f, 1.f), s0);
+}
+__device__ __forceinline__ __half2 proj_subi(__half2 s0, __half2 s1) {
+    return __hfma2(__lowhigh2highlow(s1), __floats2half2_rn(1.f, -1.f), s0);
+}
+
+template <bool DAG, bool NORM>
+__global__ void __launch_bounds__(256) k_dslash_h32(DslashH a) {
+    constexpr int NP = 2, NR = 4, LANES = 8, NRHS = 32;
+    const Geom g = a.g;
+    const int rhs0 = threadIdx.x * NR;
+    const int rem = blockIdx.x * blockDim.y + threadIdx.y;
+    const int y = blockIdx.y;
+    const bool valid = rem < g.L;
+    const int p = rem >= g.Lh ? 1 : 0;
+    const int xh = rem - p * g.Lh;
+    const int q = p * g.Vh + y * g.Lh + xh;
+    Spinor<float> out[NR];
+#pragma unroll
+    for (int k = 0; k < NR; ++k) {
+        out[k].s0 = mk(0.f, 0.f);
+        out[k].s1 = mk(0.f, 0.f);
+    }
+    if (valid) {
+        const int x = 2 * xh + ((y + p) & 1);
+        const int op = (1 - p) * g.Vh;
+        const int xp = x + 1 == g.L ? 0 : x + 1, xm = x == 0 ? g.L - 1 : x - 1;
+        const int yp = y + 1 == g.L ? 0 : y + 1, ym = y == 0 ? g.L - 1 : y - 1;
+        const int q_xp = op + ((xp + g.L * y) >> 1), q_xm = op + ((xm + g.L * y) >> 1);
+        const int q_yp = op + ((x + g.L * yp) >> 1), q_ym = op + ((x + g.L * ym) >> 1);
+        // a site's 32 two-spinors are 16 uint4 (one pair each); this thread's pairs 2 tx, 2 tx + 1
+        const uint4* __restrict__ f = reinterpret_cast<const uint4*>(a.src16) + 2 * threadIdx.x;
+        uint4 vc[NP], vxp[NP], vxm[NP], vyp[NP], vym[NP];
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+            vc[k] = __ldg(f + (int64_t)q * (NRHS / 2) + k);
+            vxp[k] = __ldg(f + (int64_t)q_xp * (NRHS / 2) + k);
+            vxm[k] = __ldg(f + (int64_t)q_xm * (NRHS / 2) + k);
+            vyp[k] = __ldg(f + (int64_t)q_yp * (NRHS / 2) + k);
+            vym[k] = __ldg(f + (int64_t)q_ym * (NRHS / 2) + k);
+        }
+        cx<float> u0f = a.U[q], u0b = a.U[q_xm], u1f = a.U[g.V + q], u1b = a.U[g.V + q_ym];
+        const float Cq = a.C ? a.C[q] : 0.f;
+        const float sq = a.src_scale[q];
+        const float dg0 = (a.diag + Cq) * sq, dg1 = (a.diag - Cq) * sq;
+        const float hxp = 0.5f * a.src_scale[q_xp], hxm = 0.5f * a.src_scale[q_xm];
+        const float hyp = 0.5f * a.src_scale[q_yp], hym = 0.5f * a.src_scale[q_ym];
+        u0f = mk(u0f.re * hxp, u0f.im * hxp);
+        u0b = mk(u0b.re * hxm, u0b.im * hxm);
+        u1f = mk(u1f.re * hyp, u1f.im * hyp);
+        u1b = mk(u1b.re * hym, u1b.im * hym);
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+            const int j = k >> 1;
+            const bool hi = k & 1;  // second right-hand side of the pair: words z (s0) and w (s1)
+            const unsigned c0 = hi ? vc[j].z : vc[j].x, c1 = hi ? vc[j].w : vc[j].y;
+            const __half2 xp0 = h2_of(hi ? vxp[j].z : vxp[j].x), xp1 = h2_of(hi ? vxp[j].w : vxp[j].y);
+            const __half2 xm0 = h2_of(hi ? vxm[j].z : vxm[j].x), xm1 = h2_of(hi ? vxm[j].w : vxm[j].y);
+            const __half2 yp0 = h2_of(hi ? vyp[j].z : vyp[j].x), yp1 = h2_of(hi ? vyp[j].w : vyp[j].y);
+            const __half2 ym0 = h2_of(hi ? vym[j].z : vym[j].x), ym1 = h2_of(hi ? vym[j].w : vym[j].y);
+            const cx<float> hxf = cx_of(DAG ? proj_add(xp0, xp1) : proj_sub(xp0, xp1));
+            const cx<float> hxb = cx_of(DAG ? proj_sub(xm0, xm1) : proj_add(xm0, xm1));
+            const cx<float> hyf = cx_of(DAG ? proj_subi(yp0, yp1) : proj_addi(yp0, yp1));
+            const cx<float> hyb = cx_of(DAG ? proj_addi(ym0, ym1) : proj_subi(ym0, ym1));
+            cx<float> S0, S1;
+            hop_recon<float, DAG>(u0f, u0b, u1f, u1b, hxf, hxb, hyf, hyb, S0, S1);
+            const cx<float> p0 = cx_of(h2_of(c0)), p1 = cx_of(h2_of(c1));
+            out[k].s0 = mk(fmaf(dg0, p0.re, -S0.re), fmaf(dg0, p0.im, -S0.im));
+            out[k].s1 = mk(fmaf(dg1, p1.re, -S1.re), fmaf(dg1, p1.im, -S1.im));
+        }
+    }
+    if (NORM) {
+        // ||out||^2 of this block's sites per rhs: the four sites of a warp by shuffles, the eight
+        // warps in shared memory
+        __shared__ float s_n[8][32];
+        float v[NR];
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+            v[k] = valid ? norm2(out[k].s0) + norm2(out[k].s1) : 0.f;
+            v[k] += __shfl_xor_sync(0xffffffffu, v[k], 8);
+            v[k] += __shfl_xor_sync(0xffffffffu, v[k], 16);
+        }
+        const int warp = threadIdx.y >> 2;
+        if ((threadIdx.y & 3) == 0) {
+#pragma unroll
+            for (int k = 0; k < NR; ++k) s_n[warp][rhs0 + k] = v[k];
+        }
+        __syncthreads();
+        if (threadIdx.y == 0) {
+            float* pp = a.part + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * NRHS * 2 + a.part_col;
+#pragma unroll
+            for (int k = 0; k < NR; ++k) {
+                float t = 0.f;
+#pragma unroll
+                for (int w = 0; w < 8; ++w) t += s_n[w][rhs0 + k];
+                pp[2 * (rhs0 + k)] = t;
+            }
+        }
+    }
+    st_pairs_h<NP>(a.dst16, a.dst_scale, q, rhs0, NRHS, LANES, out, valid);
+}
+
 // right-hand-side pairs per thread of the FP16 stencil launches: two (four right-hand sides share a
 // site's index, link and scale work) from 8 right-hand sides up (L = 512, 32 RHS: D 55.3 against
 // 57.4 us, D^dag with the fused norm 66.0 against 71.2 us); SMG_DSLASH_H_NP=1 or 2 fixes it
@@ -398,6 +515,16 @@ int dslash_h_np(int nrhs) {
     }();
     const int np = env == 1 || env == 2 ? env : (nrhs >= 8 ? 2 : 1);
     return nrhs >= 4 * np ? np : 1;
+}
+
+// the specialised 32-RHS FP16 stencil (k_dslash_h32) where it applies; SMG_DSLASH_H32=0 keeps the
+// generic kernel
+bool dslash_h32_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("SMG_DSLASH_H32");
+        return !(e && std::atoi(e) == 0);
+    }();
+    return on;
 }
 
 struct HLaunch {
@@ -506,6 +633,18 @@ smg_status launch_dslash_h(smg_dirac* d, bool dag, const smg_field* src, smg_fie
     if (norm && !(ih && oh)) return smg_fail(ctx, SMG_UNSUPPORTED, "fused FP16 stencil norm: F16 fields");
     const HLaunch hl = dslash_h_launch(a.g.L, nrhs);
     const int np = dslash_h_np(nrhs);
+    if (ih && oh && nrhs == 32 && np == 2 && d->r == 1.0 && a.mu_eff == 0.f && dslash_h32_enabled()) {
+        if (dag) {
+            if (norm) k_dslash_h32<true, true><<<hl.grid, hl.block, 0, ctx->stream>>>(a);
+            else k_dslash_h32<true, false><<<hl.grid, hl.block, 0, ctx->stream>>>(a);
+        } else {
+            if (norm) k_dslash_h32<false, true><<<hl.grid, hl.block, 0, ctx->stream>>>(a);
+            else k_dslash_h32<false, false><<<hl.grid, hl.block, 0, ctx->stream>>>(a);
+        }
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+        return SMG_OK;
+    }
 #define SMG_DH(DG, I, O, N)                                                                                         \
     do {                                                                                                            \
         if (np == 2) {                                                                                              \

@@ -14,6 +14,17 @@
 #pragma once
 #include "smg_internal.h"
 
+// r = 1: the projected half spinors h (one per hop) times their links, rebuilt into the two spin
+// components of the hopping sum
+template <typename T, bool DAG>
+__device__ __forceinline__ void hop_recon(cx<T> u0f, cx<T> u0b, cx<T> u1f, cx<T> u1b, cx<T> hxf, cx<T> hxb,
+                                          cx<T> hyf, cx<T> hyb, cx<T>& S0, cx<T>& S1) {
+    const cx<T> A_xf = u0f * hxf, B_xb = cmulc(u0b, hxb);
+    const cx<T> A_yf = u1f * hyf, B_yb = cmulc(u1b, hyb);
+    S0 = (A_xf + B_xb) + (A_yf + B_yb);
+    S1 = DAG ? (A_xf - B_xb) + times_i(A_yf - B_yb) : (B_xb - A_xf) + times_i(B_yb - A_yf);
+}
+
 template <typename T, bool DAG, bool R1>
 __device__ __forceinline__ void hop_sum(cx<T> u0f, cx<T> u0b, cx<T> u1f, cx<T> u1b, const Spinor<T>& pxp,
                                         const Spinor<T>& pxm, const Spinor<T>& pyp, const Spinor<T>& pym, T r,
@@ -23,10 +34,7 @@ __device__ __forceinline__ void hop_sum(cx<T> u0f, cx<T> u0b, cx<T> u1f, cx<T> u
         const cx<T> hxb = DAG ? pxm.s0 - pxm.s1 : pxm.s0 + pxm.s1;
         const cx<T> hyf = DAG ? pyp.s0 - times_i(pyp.s1) : pyp.s0 + times_i(pyp.s1);
         const cx<T> hyb = DAG ? pym.s0 + times_i(pym.s1) : pym.s0 - times_i(pym.s1);
-        const cx<T> A_xf = u0f * hxf, B_xb = cmulc(u0b, hxb);
-        const cx<T> A_yf = u1f * hyf, B_yb = cmulc(u1b, hyb);
-        S0 = (A_xf + B_xb) + (A_yf + B_yb);
-        S1 = DAG ? (A_xf - B_xb) + times_i(A_yf - B_yb) : (B_xb - A_xf) + times_i(B_yb - A_yf);
+        hop_recon<T, DAG>(u0f, u0b, u1f, u1b, hxf, hxb, hyf, hyb, S0, S1);
     } else {
         const T sgn = DAG ? T(-1) : T(1);
         const cx<T> a0x = u0f * pxp.s0, a1x = u0f * pxp.s1;

@@ -31,12 +31,14 @@ def test_f16_nrhs_must_be_a_power_of_two(smg_gpu):
         smg_gpu.Field(lat, 12, "f16")
 
 
-@pytest.mark.parametrize("nrhs", [8, 32])
-def test_operator_on_f16_fields(smg_gpu, nrhs):
+@pytest.mark.parametrize("nrhs,mu", [(8, 0.0), (32, 0.0), (32, 0.1)])
+def test_operator_on_f16_fields(smg_gpu, nrhs, mu):
+    """32 RHS without twist is the specialised smoother stencil (FP16 spin projections); with a twist,
+    and at 8 RHS, the generic FP16 stencil."""
     L = 64
     U = smg_gpu.gauge_normal(L, 6.0, 21)
     lat = smg_gpu.Lattice(L)
-    D = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, U), -0.05, 1.0, 1.0, 0.0)
+    D = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, U), -0.05, 1.0, 1.0, mu)
     B = np.stack([smg_gpu.random_vec(lat.ndof, 30 + j) for j in range(nrhs)])
     for op in (0, 1):
         want = D.apply_op(op, B)
