@@ -577,6 +577,594 @@ __global__ void k_tile_links(const cx<double>* __restrict__ A, int nx, int64_t n
     *reinterpret_cast<uint4*>(out + block * kLinkDir + (n >> 3) * 256 + g * 128 + (n & 7) * 16) = v;
 }
 
+// ------------------------------------------------------------ persistent coarsest CG
+// The whole coarsest-level CG of 32 right-hand sides (SparseCoarseOp::solve without deflation,
+// src/coarse_op.h:492-547) in one cooperative launch: every CTA owns the strip of kW x H sites of
+// the apply above and keeps the apply's pipeline (link ring, staged source rows, tensor memory)
+// across the iterations.  Per iteration k:
+//   apply   the stagers form p_k = r_k + beta_{k-1} p_{k-1} on the fly for the source rows (FP16 r
+//           and p_{k-1} of any CTA's sites, published before the last grid barrier) and stage it as
+//           BF16; warps 10, 11 write p_k of the CTA's own sites (FP16, site scales) into the other p
+//           buffer; the epilogue writes A p_k (FP32) of the own sites;
+//   <A p_k, p_k> over the own sites per rhs, grid barrier, alpha_k = rr_k / <p_k, A p_k> from the
+//           per-CTA partials summed in CTA order (identical, deterministic scalars in every CTA);
+//   update  own sites: x += alpha p_k, r_{k+1} = r_k - alpha A p_k (FP16, new site scales), and
+//           ||r_{k+1}||^2; grid barrier; beta_k, the per-rhs stop rule of the launched CG, and the
+//           exit once no rhs is active.
+// r and p are internal to the solve and stored dof-inner ([site][rhs][dof] __half2: the 16 dofs of a
+// site and rhs are four 16-byte words); b, x and A p keep the [site][dof][rhs] layout of the cycle.
+// Every phase issues its loads before its stores (the compiler may not move a load above a store
+// to global memory that it cannot prove disjoint), and values written by other CTAs during the
+// launch are read past L1 (ld.global.cg).  Every mbarrier and grid-barrier wait is bounded: a CTA
+// that gives up raises the error word, which ends every other CTA's barrier wait.
+struct CcgTcArgs {
+    const uint8_t* links = nullptr;
+    const float2* b = nullptr;           // [site][dof][32] right-hand side (FP32)
+    float2* x = nullptr;                 // solution (FP32, [site][dof][32])
+    __half2* r = nullptr;                // residual (FP16, dof-inner) and site scales
+    float* rs = nullptr;
+    __half2* p[2] = {nullptr, nullptr};  // search directions (FP16, dof-inner), p_k in p[k & 1]
+    float* ps[2] = {nullptr, nullptr};
+    float2* Ap = nullptr;                // A p_k (FP32, [site][dof][32])
+    double* part = nullptr;              // [2][32][nblk] per-CTA partial sums
+    unsigned int* bar = nullptr;         // grid barrier: [0] arrivals, [1] generation
+    int* err = nullptr;                  // 1 grid-barrier timeout, 2 mbarrier timeout
+    int* iters = nullptr;                // iterations done (CTA 0)
+    long long spin_limit = 0;
+    double tol2 = 0;
+    int nx = 0, ny = 0, H = 0, max_iter = 0;
+};
+
+constexpr int kCcgMaxCtas = 160;                    // partial sums: five loads per lane and rhs
+// extra shared memory of the persistent CG after the apply's: scalars and reduction rows
+constexpr int kCcgOffset = (kSmemBytes + 15) / 16 * 16;
+constexpr int kCcgRr = kCcgOffset;                  // double [32]
+constexpr int kCcgBn = kCcgRr + 32 * 8;             // double [32]
+constexpr int kCcgSum = kCcgBn + 32 * 8;            // double [32]: the last grid-wide sums
+constexpr int kCcgAlpha = kCcgSum + 32 * 8;         // float [32]
+constexpr int kCcgBeta = kCcgAlpha + 32 * 4;        // float [32]
+constexpr int kCcgAct = kCcgBeta + 32 * 4;          // int [32]
+constexpr int kCcgWred = kCcgAct + 32 * 4;          // float [12][32]
+constexpr int kCcgSmemBytes = kCcgWred + 12 * 32 * 4;
+static_assert(kCcgSmemBytes + 1024 <= 227 * 1024, "shared memory budget (persistent CG)");
+
+__device__ __forceinline__ float ccg_warp_max(float m) {
+    for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    return m;
+}
+__device__ __forceinline__ float2 h2f(unsigned u) { return __half22float2(*reinterpret_cast<const __half2*>(&u)); }
+__device__ __forceinline__ unsigned f2h(float re, float im) {
+    const __half2 h = __floats2half2_rn(re, im);
+    return *reinterpret_cast<const unsigned*>(&h);
+}
+__device__ __forceinline__ unsigned word_of(const uint4& w, int i) {
+    return i == 0 ? w.x : (i == 1 ? w.y : (i == 2 ? w.z : w.w));
+}
+// the four 16-byte words of (site, rhs) of a dof-inner FP16 vector
+__device__ __forceinline__ const uint4* h16_ptr(const __half2* v, int64_t site, int rhs) {
+    return reinterpret_cast<const uint4*>(v) + (site * kRhsTile + rhs) * (kNc / 4);
+}
+__device__ __forceinline__ uint4* h16_ptr(__half2* v, int64_t site, int rhs) {
+    return reinterpret_cast<uint4*>(v) + (site * kRhsTile + rhs) * (kNc / 4);
+}
+
+// grid-wide barrier of the co-resident grid; gives up after spin_limit polls or when *err is raised
+__device__ __forceinline__ bool ccg_grid_barrier(unsigned int* bar, int* err, long long spin_limit) {
+    __threadfence();
+    __syncthreads();
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        volatile unsigned int* vgen = bar + 1;
+        volatile int* verr = err;
+        if (*verr) {
+            ok = 0;
+        } else {
+            const unsigned int gen = *vgen;
+            __threadfence();
+            const unsigned int nblk = gridDim.x * gridDim.y;
+            if (atomicAdd(bar, 1u) == nblk - 1) {
+                bar[0] = 0u;
+                __threadfence();
+                atomicAdd(bar + 1, 1u);
+            } else {
+                long long k = 0;
+                while (*vgen == gen) {
+                    if (*verr || ++k > spin_limit) {
+                        atomicCAS(err, 0, 1);
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
+            __threadfence();
+        }
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// out32[j] = sum over the grid's CTAs of part[j][cta] for the 32 rhs: warp w takes rhs w, w + 12,
+// w + 24 with all its loads issued first, lanes stride the CTAs, then a fixed shuffle tree (the same
+// order in every CTA)
+__device__ __forceinline__ void ccg_sum_partials(const double* part, int nblk, double* out32) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double v[3][5];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const int j = warp + (kThreads / 32) * q;
+#pragma unroll
+        for (int u = 0; u < 5; ++u) {
+            const int c = lane + 32 * u;
+            v[q][u] = (j < 32 && c < nblk) ? __ldcg(part + (int64_t)j * nblk + c) : 0.0;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const int j = warp + (kThreads / 32) * q;
+        double s = ((v[q][0] + v[q][1]) + (v[q][2] + v[q][3])) + v[q][4];
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0 && j < 32) out32[j] = s;
+    }
+}
+
+// the per-rhs sums of the warps' lanes (s_wred[warp][lane]) as this CTA's partial part[rhs][blin]
+__device__ __forceinline__ void ccg_publish(float* s_wred, float v, double* part, int nblk, int blin) {
+    s_wred[threadIdx.x] = v;  // [warp][lane]
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) t += (double)s_wred[w * 32 + threadIdx.x];
+        part[(int64_t)threadIdx.x * nblk + blin] = t;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int H = a.H, nx = a.nx, ny = a.ny;
+    constexpr int nrhs = kRhsTile;
+    const int x0 = blockIdx.x * kW, y0 = blockIdx.y * H;
+    const int nblk = gridDim.x * gridDim.y, blin = blockIdx.x + gridDim.x * blockIdx.y;
+    const int nown = kW * H;
+    const uint32_t ring_a = smem_u32(smem);
+    const uint32_t link_a = ring_a + kRingBytes;
+    const uint32_t bar_a = ring_a + kBarOffset;
+    int* misc = reinterpret_cast<int*>(smem + kMiscOffset);  // [0] TMEM base, [1] abort flag
+    double* s_rr = reinterpret_cast<double*>(smem + kCcgRr);
+    double* s_bn = reinterpret_cast<double*>(smem + kCcgBn);
+    double* s_sum = reinterpret_cast<double*>(smem + kCcgSum);
+    float* s_alpha = reinterpret_cast<float*>(smem + kCcgAlpha);
+    float* s_beta = reinterpret_cast<float*>(smem + kCcgBeta);
+    int* s_act = reinterpret_cast<int*>(smem + kCcgAct);
+    float* s_wred = reinterpret_cast<float*>(smem + kCcgWred);
+    volatile int* abort_flag = misc + 1;
+    auto bar = [&](int i) { return bar_a + 8u * (uint32_t)i; };
+    double* part1 = a.part;                        // <A p, p> partials
+    double* part2 = a.part + (int64_t)32 * nblk;  // ||r||^2 partials
+    // own site s (0 .. kW H - 1) of this CTA
+    auto own_site = [&](int s) { return (int64_t)(x0 + s % kW) + (int64_t)nx * (y0 + s / kW); };
+
+    if (tid == 0) {
+        for (int i = 0; i < kRing; ++i) {
+            mbar_init(bar(kBarSrcFull + i), 128);
+            mbar_init(bar(kBarSrcEmpty + i), 1);
+        }
+        for (int i = 0; i < kUnits; ++i) {
+            mbar_init(bar(kBarUnitFull + i), 1);
+            mbar_init(bar(kBarUnitEmpty + i), 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(bar(kBarAccFull + i), 1);
+            mbar_init(bar(kBarAccEmpty + i), 32 * 2 * kEpiHalves);
+        }
+        mbar_init(bar(kBarFinal), 1);
+        misc[1] = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        fence_proxy_async();
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(misc)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(misc);
+
+    // ---- start: r = b (FP16), x = 0, p_{-1} = 0 in p[1], ||b||^2 per rhs (one warp per own site)
+    {
+        float n2 = 0.f;
+        for (int s = warp; s < nown; s += kThreads / 32) {
+            const int64_t site = own_site(s);
+            const int64_t e0 = site * kNc * nrhs + lane;
+            float2 v[kNc];
+#pragma unroll
+            for (int d = 0; d < kNc; ++d) v[d] = __ldcg(a.b + e0 + d * nrhs);
+            float m = 0.f;
+#pragma unroll
+            for (int d = 0; d < kNc; ++d) {
+                m = fmaxf(m, fmaxf(fabsf(v[d].x), fabsf(v[d].y)));
+                n2 += v[d].x * v[d].x + v[d].y * v[d].y;
+            }
+            m = ccg_warp_max(m);
+            const float inv = m > 0.f ? __fdividef(1.0f, m) : 0.f;
+            uint4* rp = h16_ptr(a.r, site, lane);
+            uint4* pp = h16_ptr(a.p[1], site, lane);
+#pragma unroll
+            for (int q = 0; q < kNc / 4; ++q) {
+                uint4 w;
+                w.x = f2h(v[4 * q].x * inv, v[4 * q].y * inv);
+                w.y = f2h(v[4 * q + 1].x * inv, v[4 * q + 1].y * inv);
+                w.z = f2h(v[4 * q + 2].x * inv, v[4 * q + 2].y * inv);
+                w.w = f2h(v[4 * q + 3].x * inv, v[4 * q + 3].y * inv);
+                __stcg(rp + q, w);
+                __stcg(pp + q, make_uint4(0u, 0u, 0u, 0u));
+            }
+#pragma unroll
+            for (int d = 0; d < kNc; ++d) __stcg(a.x + e0 + d * nrhs, make_float2(0.f, 0.f));
+            if (lane == 0) {
+                __stcg(a.rs + site, m);
+                __stcg(a.ps[1] + site, 0.f);
+            }
+        }
+        ccg_publish(s_wred, n2, part2, nblk, blin);
+    }
+    bool ok = ccg_grid_barrier(a.bar, a.err, a.spin_limit);
+    if (ok) {
+        ccg_sum_partials(part2, nblk, s_sum);
+        __syncthreads();
+        if (tid < 32) {
+            const double rr = s_sum[tid];
+            s_rr[tid] = rr;
+            s_bn[tid] = rr;
+            s_beta[tid] = 0.f;
+            int act = (rr >= 1e-60 && isfinite(rr)) ? 1 : 0;
+            if (act && rr < a.tol2 * rr) act = 0;
+            s_act[tid] = act;
+        }
+    }
+    int iter = 0;
+    int nact = ok ? __syncthreads_count(tid < 32 && s_act[tid]) : 0;
+    int issued = 0;  // link units issued by the producer (lane 0 of warp 0)
+    const int nunits = 3 * H;
+    for (int k = 0; ok && nact > 0 && k < a.max_iter; ++k) {
+        const __half2* __restrict__ pold = a.p[(k + 1) & 1];
+        const float* __restrict__ psold = a.ps[(k + 1) & 1];
+        __half2* __restrict__ pnew = a.p[k & 1];
+        float* __restrict__ psnew = a.ps[k & 1];
+        const int ub = k * nunits, sb = k * (H + 2), ab = k * H;  // unit, source-row and output-row bases
+        // ================= apply: A p_k with the apply kernel's warp roles
+        if (warp == 0) {
+            if (lane == 0) {
+                const int ring3 = 3 * nx;
+                for (int u = 0; u < nunits; ++u) {
+                    const int U = ub + u, slot = U % kUnits, use = U / kUnits;
+                    if (use > 0 && !wait_bar(bar(kBarUnitEmpty + slot), (use - 1) & 1, abort_flag)) break;
+                    const int r = u / 3, dyi = u - 3 * r;
+                    const uint8_t* row = a.links + ((int64_t)(y0 + r) * 3 + dyi) * ring3 * kLinkDir;
+                    const int p0 = (3 * x0 + 2) % ring3;
+                    const int n1 = ring3 - p0 < kRunBlocks ? ring3 - p0 : kRunBlocks;
+                    const uint32_t dst = link_a + (uint32_t)(slot * kUnitBytes);
+                    mbar_expect_tx(bar(kBarUnitFull + slot), kUnitBytes);
+                    bulk_g2s(dst, row + (int64_t)p0 * kLinkDir, (uint32_t)(n1 * kLinkDir), bar(kBarUnitFull + slot));
+                    if (n1 < kRunBlocks)
+                        bulk_g2s(dst + (uint32_t)(n1 * kLinkDir), row, (uint32_t)((kRunBlocks - n1) * kLinkDir),
+                                 bar(kBarUnitFull + slot));
+                    issued = U + 1;
+                }
+            }
+            __syncwarp();
+        } else if (warp == 1) {
+            if (lane == 0) {
+                bool mok = true;
+                for (int r = 0; r < H && mok; ++r) {
+                    const int R = ab + r;
+                    for (int lr = (r == 0 ? 0 : r + 2); lr <= r + 2 && mok; ++lr) {
+                        const int S = sb + lr;
+                        mok = wait_bar(bar(kBarSrcFull + S % kRing), (S / kRing) & 1, abort_flag);
+                    }
+                    if (mok && R >= 2) mok = wait_bar(bar(kBarAccEmpty + (R & 1)), ((R >> 1) - 1) & 1, abort_flag);
+                    if (!mok) break;
+                    const uint32_t acc = tmem + (uint32_t)((R & 1) * kAccCols);
+                    for (int dyi = 0; dyi < 3 && mok; ++dyi) {
+                        const int U = ub + 3 * r + dyi, slot = U % kUnits;
+                        mok = wait_bar(bar(kBarUnitFull + slot), (U / kUnits) & 1, abort_flag);
+                        if (!mok) break;
+                        tc_fence_after();
+                        const int S = sb + r + dyi;
+                        const uint32_t arow = ring_a + (uint32_t)((S % kRing) * kRowBytes);
+                        const uint32_t unit = link_a + (uint32_t)(slot * kUnitBytes);
+#pragma unroll
+                        for (int kk = 0; kk < kSrcSites; ++kk) {
+                            const int t = dyi == 0 ? (kk < 3 ? 2 + 3 * kk : (kk < 5 ? kk - 3 : (kk < 7 ? kk - 2 : (kk < 9 ? kk - 1 : 9)))) : kk;
+                            const SrcGroup g = src_group(t);
+                            const uint32_t accumulate = (dyi == 0 && kk < 3) ? 0u : 1u;
+                            mma_bf16(acc + (uint32_t)(32 * g.first), smem_desc(arow + (uint32_t)(t * kTileA), 128, kSboA),
+                                     smem_desc(unit + (uint32_t)g.run_off, 128, 256),
+                                     idesc_bf16(32u * (uint32_t)g.count), accumulate);
+                        }
+                        mma_commit(bar(kBarUnitEmpty + slot));
+                    }
+                    if (!mok) break;
+                    mma_commit(bar(kBarAccFull + (R & 1)));
+                    mma_commit(bar(kBarSrcEmpty + (sb + r) % kRing));
+                }
+                // the iteration's last two source rows are free once its MMAs complete
+                if (mok) {
+                    mma_commit(bar(kBarSrcEmpty + (sb + H) % kRing));
+                    mma_commit(bar(kBarSrcEmpty + (sb + H + 1) % kRing));
+                }
+            }
+            __syncwarp();
+        } else if (warp == 4 || warp == 5 || warp == 8 || warp == 9) {
+            // epilogue: A p_k of the own sites to global memory
+            const int half = warp >= 8 ? 1 : 0;
+            const int sub = warp - (half ? 8 : 4);
+            const int m = 32 * sub + lane;
+            const int rhs = m >> 1, c = m & 1;
+            const int64_t rstride = 2ll * nrhs;
+            float* __restrict__ ybase = reinterpret_cast<float*>(a.Ap);
+            for (int r = 0; r < H; ++r) {
+                const int R = ab + r;
+                const bool eok = wait_bar(bar(kBarAccFull + (R & 1)), (R >> 1) & 1, abort_flag);
+                if (!__all_sync(0xffffffffu, eok)) break;
+                tc_fence_after();
+#pragma unroll
+                for (int q = 0; q < kEpiSites; ++q) {
+                    const int i = half * kEpiSites + q;
+                    float d[32];
+                    tmem_ld32(tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)((R & 1) * kAccCols + 32 * i), d);
+                    const int64_t base =
+                        (((int64_t)x0 + i + (int64_t)nx * (y0 + r)) * kNc * nrhs + rhs) * 2 + c;
+#pragma unroll
+                    for (int kk = 0; kk < kNc; ++kk) {
+                        const float other = __shfl_xor_sync(0xffffffffu, d[16 + kk], 1);
+                        __stcg(ybase + base + kk * rstride, c == 0 ? d[kk] - other : d[kk] + other);
+                    }
+                }
+                tc_fence_before();
+                mbar_arrive(bar(kBarAccEmpty + (R & 1)));
+            }
+        } else if (warp == 2 || warp == 3 || warp == 6 || warp == 7) {
+            // stagers: p_k = r_k + beta p_{k-1} (FP16 inputs with site scales) -> BF16 A tiles
+            const int st = (warp < 4 ? warp - 2 : warp - 4) * 32 + lane;
+            for (int lr = 0; lr < H + 2; ++lr) {
+                const int S = sb + lr, slot = S % kRing, use = S / kRing;
+                if (use > 0 && !wait_bar(bar(kBarSrcEmpty + slot), (use - 1) & 1, abort_flag)) break;
+                const int gy = wrapi(y0 - 1 + lr, ny);
+                uint8_t* row = smem + slot * kRowBytes;
+                constexpr int kItems = kSrcSites * 2 * 32;  // (site, 8-dof group, rhs)
+                constexpr int kPer = kItems / 128;
+                uint4 rv[kPer][2], pv[kPer][2];
+                float sr[kPer], sp[kPer];
+#pragma unroll
+                for (int it = 0; it < kPer; ++it) {  // every load of the row first
+                    const int item = st + it * 128;
+                    const int r = item & 31, g = (item >> 5) & 1, t = item >> 6;
+                    const int64_t site = wrapi(x0 - 1 + t, nx) + (int64_t)nx * gy;
+                    const uint4* rp = h16_ptr(a.r, site, r) + 2 * g;
+                    const uint4* pp = h16_ptr(pold, site, r) + 2 * g;
+                    rv[it][0] = __ldcg(rp);
+                    rv[it][1] = __ldcg(rp + 1);
+                    pv[it][0] = __ldcg(pp);
+                    pv[it][1] = __ldcg(pp + 1);
+                    sr[it] = __ldcg(a.rs + site);
+                    sp[it] = __ldcg(psold + site) * s_beta[r];
+                }
+#pragma unroll
+                for (int it = 0; it < kPer; ++it) {
+                    const int item = st + it * 128;
+                    const int r = item & 31, g = (item >> 5) & 1, t = item >> 6;
+                    float2 e[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const float2 a2 = h2f(word_of(rv[it][j >> 2], j & 3));
+                        const float2 b2 = h2f(word_of(pv[it][j >> 2], j & 3));
+                        e[j] = make_float2(fmaf(sr[it], a2.x, sp[it] * b2.x), fmaf(sr[it], a2.y, sp[it] * b2.y));
+                    }
+                    uint4 re, im;
+                    re.x = pack_bf16(e[0].x, e[1].x);
+                    re.y = pack_bf16(e[2].x, e[3].x);
+                    re.z = pack_bf16(e[4].x, e[5].x);
+                    re.w = pack_bf16(e[6].x, e[7].x);
+                    im.x = pack_bf16(e[0].y, e[1].y);
+                    im.y = pack_bf16(e[2].y, e[3].y);
+                    im.z = pack_bf16(e[4].y, e[5].y);
+                    im.w = pack_bf16(e[6].y, e[7].y);
+                    uint8_t* tile = row + t * kTileA;
+                    const int mr = 2 * r, mi = 2 * r + 1;
+                    *reinterpret_cast<uint4*>(tile + (mr >> 3) * kSboA + g * 128 + (mr & 7) * 16) = re;
+                    *reinterpret_cast<uint4*>(tile + (mi >> 3) * kSboA + g * 128 + (mi & 7) * 16) = im;
+                }
+                fence_proxy_async();
+                mbar_arrive(bar(kBarSrcFull + slot));
+            }
+        } else if (warp == 10 || warp == 11) {
+            // own sites' p_k -> p[k & 1] (FP16, site scale = the site's largest |re| or |im|), two
+            // sites per step with both sites' loads first
+            for (int s0 = 2 * (warp - 10); s0 < nown; s0 += 4) {
+                uint4 rv[2][4], pv[2][4];
+                float sr[2], sp[2];
+                int64_t site[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    site[h] = own_site(s0 + h < nown ? s0 + h : s0);
+                    const uint4* rp = h16_ptr(a.r, site[h], lane);
+                    const uint4* pp = h16_ptr(pold, site[h], lane);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        rv[h][q] = __ldcg(rp + q);
+                        pv[h][q] = __ldcg(pp + q);
+                    }
+                    sr[h] = __ldcg(a.rs + site[h]);
+                    sp[h] = __ldcg(psold + site[h]) * s_beta[lane];
+                }
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (s0 + h >= nown) break;
+                    float2 v[kNc];
+                    float mx = 0.f;
+#pragma unroll
+                    for (int d = 0; d < kNc; ++d) {
+                        const float2 a2 = h2f(word_of(rv[h][d >> 2], d & 3));
+                        const float2 b2 = h2f(word_of(pv[h][d >> 2], d & 3));
+                        v[d] = make_float2(fmaf(sr[h], a2.x, sp[h] * b2.x), fmaf(sr[h], a2.y, sp[h] * b2.y));
+                        mx = fmaxf(mx, fmaxf(fabsf(v[d].x), fabsf(v[d].y)));
+                    }
+                    mx = ccg_warp_max(mx);
+                    const float inv = mx > 0.f ? __fdividef(1.0f, mx) : 0.f;
+                    uint4* op = h16_ptr(pnew, site[h], lane);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        uint4 w;
+                        w.x = f2h(v[4 * q].x * inv, v[4 * q].y * inv);
+                        w.y = f2h(v[4 * q + 1].x * inv, v[4 * q + 1].y * inv);
+                        w.z = f2h(v[4 * q + 2].x * inv, v[4 * q + 2].y * inv);
+                        w.w = f2h(v[4 * q + 3].x * inv, v[4 * q + 3].y * inv);
+                        __stcg(op + q, w);
+                    }
+                    if (lane == 0) __stcg(psnew + site[h], mx);
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (*abort_flag) {
+            if (tid == 0) atomicCAS(a.err, 0, 2);
+            break;
+        }
+        // ================= <A p_k, p_k> of the own sites per rhs (one warp per site, lane = rhs)
+        {
+            float dot = 0.f;
+            for (int s = warp; s < nown; s += kThreads / 32) {
+                const int64_t site = own_site(s);
+                const int64_t e0 = site * kNc * nrhs + lane;
+                float2 av[kNc];
+                uint4 pv[4];
+                const uint4* pp = h16_ptr(pnew, site, lane);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) pv[q] = __ldcg(pp + q);
+#pragma unroll
+                for (int d = 0; d < kNc; ++d) av[d] = __ldcg(a.Ap + e0 + d * nrhs);
+                const float sp = __ldcg(psnew + site);
+                float t = 0.f;
+#pragma unroll
+                for (int d = 0; d < kNc; ++d) {
+                    const float2 p2 = h2f(word_of(pv[d >> 2], d & 3));
+                    t += av[d].x * p2.x + av[d].y * p2.y;  // Re <A p, p>
+                }
+                dot += sp * t;
+            }
+            ccg_publish(s_wred, dot, part1, nblk, blin);
+        }
+        ok = ccg_grid_barrier(a.bar, a.err, a.spin_limit);
+        if (!ok) break;
+        ccg_sum_partials(part1, nblk, s_sum);
+        __syncthreads();
+        if (tid < 32) {
+            float al = 0.f;
+            const double pap = s_sum[tid];
+            if (s_act[tid] && fabs(pap) >= 1e-30 && isfinite(pap)) al = (float)(s_rr[tid] / pap);
+            s_alpha[tid] = al;
+        }
+        __syncthreads();
+        // ================= update of the own sites, one warp per site (lane = rhs), loads first
+        {
+            const float al = s_alpha[lane];
+            float n2 = 0.f;
+            for (int s = warp; s < nown; s += kThreads / 32) {
+                const int64_t site = own_site(s);
+                const int64_t e0 = site * kNc * nrhs + lane;
+                uint4 rv[4], pv[4];
+                float2 av[kNc], xv[kNc];
+                const uint4* rp = h16_ptr(a.r, site, lane);
+                const uint4* pp = h16_ptr(pnew, site, lane);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    rv[q] = __ldcg(rp + q);
+                    pv[q] = __ldcg(pp + q);
+                }
+#pragma unroll
+                for (int d = 0; d < kNc; ++d) {
+                    av[d] = __ldcg(a.Ap + e0 + d * nrhs);
+                    xv[d] = __ldcg(a.x + e0 + d * nrhs);
+                }
+                const float sr = __ldcg(a.rs + site), sp = __ldcg(psnew + site);
+                float2 rn[kNc];
+                float mx = 0.f;
+#pragma unroll
+                for (int d = 0; d < kNc; ++d) {
+                    const float2 r2 = h2f(word_of(rv[d >> 2], d & 3));
+                    const float2 p2 = h2f(word_of(pv[d >> 2], d & 3));
+                    xv[d].x += al * sp * p2.x;
+                    xv[d].y += al * sp * p2.y;
+                    rn[d] = make_float2(sr * r2.x - al * av[d].x, sr * r2.y - al * av[d].y);
+                    mx = fmaxf(mx, fmaxf(fabsf(rn[d].x), fabsf(rn[d].y)));
+                    n2 += rn[d].x * rn[d].x + rn[d].y * rn[d].y;
+                }
+                mx = ccg_warp_max(mx);  // also orders every lane's scale read before lane 0's write
+                const float inv = mx > 0.f ? __fdividef(1.0f, mx) : 0.f;
+#pragma unroll
+                for (int d = 0; d < kNc; ++d) __stcg(a.x + e0 + d * nrhs, xv[d]);
+                uint4* wp = h16_ptr(a.r, site, lane);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    uint4 w;
+                    w.x = f2h(rn[4 * q].x * inv, rn[4 * q].y * inv);
+                    w.y = f2h(rn[4 * q + 1].x * inv, rn[4 * q + 1].y * inv);
+                    w.z = f2h(rn[4 * q + 2].x * inv, rn[4 * q + 2].y * inv);
+                    w.w = f2h(rn[4 * q + 3].x * inv, rn[4 * q + 3].y * inv);
+                    __stcg(wp + q, w);
+                }
+                if (lane == 0) __stcg(a.rs + site, mx);
+            }
+            ccg_publish(s_wred, n2, part2, nblk, blin);
+        }
+        ok = ccg_grid_barrier(a.bar, a.err, a.spin_limit);
+        if (!ok) break;
+        // ================= beta_k and the stop rule (the launched CG's finaliser)
+        ccg_sum_partials(part2, nblk, s_sum);
+        __syncthreads();
+        if (tid < 32) {
+            const double rr_new = s_sum[tid];
+            float be = 0.f;
+            if (s_act[tid]) {
+                if (!isfinite(rr_new) || rr_new < a.tol2 * s_bn[tid]) {
+                    s_act[tid] = 0;
+                } else {
+                    be = (float)(rr_new / s_rr[tid]);
+                    s_rr[tid] = rr_new;
+                }
+            }
+            s_beta[tid] = be;
+        }
+        iter = k + 1;
+        nact = __syncthreads_count(tid < 32 && s_act[tid]);
+    }
+    if (blin == 0 && tid == 0 && a.iters) *a.iters = iter;
+
+    // ---- teardown: every issued bulk copy and MMA has completed before tensor memory is freed
+    if (warp == 0 && lane == 0)
+        for (int U = issued > kUnits ? issued - kUnits : 0; U < issued; ++U)
+            drain_bar(bar(kBarUnitFull + U % kUnits), (U / kUnits) & 1);
+    if (warp == 1 && lane == 0) {
+        mma_commit(bar(kBarFinal));
+        drain_bar(bar(kBarFinal), 0);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    if (*abort_flag && tid == 0 && a.err) atomicCAS(a.err, 0, 2);
+}
+
 int rows_per_cta_rule(int nx, int ny, int nz) {
     int H = ny;
     while (H % 2 == 0 && H > 4 && (nx / kW) * (ny / H) * nz < 120) H /= 2;
@@ -615,6 +1203,7 @@ smg_status smg_coarse_tc_tile_links(smg_context* ctx, const cx<double>* A64, int
     SMG_CUDA(ctx, cudaFuncSetAttribute(k_coarse_apply_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     SMG_CUDA(ctx, cudaFuncSetAttribute(k_coarse_apply_tc<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        kSmemBytes));
+    SMG_CUDA(ctx, cudaFuncSetAttribute(k_ccg_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kCcgSmemBytes));
     return SMG_OK;
 }
 
@@ -643,6 +1232,65 @@ smg_status smg_coarse_tc_apply_h(smg_context* ctx, const void* links, int nx, in
     h.ws = ws;
     const int nz = nrhs / kRhsTile;
     return launch_tc(ctx, links, nx, ny, nrhs, rows_per_cta(nx, ny, nz), nullptr, y, 2, nullptr, out, gate, err, &h);
+}
+
+// Rows per CTA of the persistent coarsest CG: the fewest (smallest power-of-two divisor of ny, or ny)
+// whose CTAs are all co-resident (one per SM); 0 when the shape does not fit.
+int smg_coarse_cg_tc_rows(smg_context* ctx, int nx, int ny) {
+    if (!smg_coarse_tc_shape_ok(nx, ny, kNc)) return 0;
+    static int per_sm = -1;
+    if (per_sm < 0) {
+        int nb = 0;
+        if (cudaFuncSetAttribute(k_ccg_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kCcgSmemBytes) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_ccg_tc, kThreads, kCcgSmemBytes) != cudaSuccess)
+            nb = 0;
+        per_sm = nb;
+    }
+    const int cap = per_sm * ctx->num_sms;
+    for (int H = 1; H <= ny; H *= 2) {
+        if (ny % H) break;
+        if ((nx / kW) * (ny / H) <= cap && (nx / kW) * (ny / H) <= kCcgMaxCtas) return H;
+    }
+    return 0;
+}
+
+// The coarsest CG of 32 right-hand sides from x = 0 in one cooperative launch (k_ccg_tc): b and x
+// FP32 [site][dof][32]; r, p0, p1 FP16 (__half2) with per-site scales rs, ps0, ps1; Ap FP32; part
+// 64 * (CTAs) doubles; state: the grid-barrier words [0..1], the error word [2] and the iteration
+// count [3] (ints).
+smg_status smg_coarse_cg_tc(smg_context* ctx, const void* links, int nx, int ny, const cx<float>* b, cx<float>* x,
+                            void* r, float* rs, void* p0, float* ps0, void* p1, float* ps1, cx<float>* Ap,
+                            double* part, int* state, int max_iter, double tol, long long spin_limit) {
+    const int H = smg_coarse_cg_tc_rows(ctx, nx, ny);
+    if (H == 0) return smg_fail(ctx, SMG_UNSUPPORTED, "persistent coarsest CG: CTAs cannot be co-resident");
+    CcgTcArgs a;
+    a.links = static_cast<const uint8_t*>(links);
+    a.b = reinterpret_cast<const float2*>(b);
+    a.x = reinterpret_cast<float2*>(x);
+    a.r = static_cast<__half2*>(r);
+    a.rs = rs;
+    a.p[0] = static_cast<__half2*>(p0);
+    a.p[1] = static_cast<__half2*>(p1);
+    a.ps[0] = ps0;
+    a.ps[1] = ps1;
+    a.Ap = reinterpret_cast<float2*>(Ap);
+    a.part = part;
+    a.bar = reinterpret_cast<unsigned int*>(state);
+    a.err = state + 2;
+    a.iters = state + 3;
+    a.spin_limit = spin_limit;
+    a.tol2 = tol * tol;
+    a.nx = nx;
+    a.ny = ny;
+    a.H = H;
+    a.max_iter = max_iter;
+    SMG_CUDA(ctx, cudaMemsetAsync(state, 0, 2 * sizeof(int), ctx->stream));  // barrier words; errors stay raised
+    void* args[] = {&a};
+    SMG_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_ccg_tc, dim3(nx / kW, ny / H), dim3(kThreads), args,
+                                              kCcgSmemBytes, ctx->stream));
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
 }
 
 // Times every rows-per-CTA choice H (the divisors ny, ny / 2, ... of the lattice height) for this

@@ -53,6 +53,10 @@ smg_status smg_coarse_tc_apply(smg_context* ctx, const void* links, int nx, int 
                                cx<float>* y, int epi, const cx<float>* w, double* out, const int* gate, int* err);
 smg_status smg_coarse_tc_tune(smg_context* ctx, const void* links, int nx, int ny, int nrhs, const cx<float>* x,
                               cx<float>* y);
+int smg_coarse_cg_tc_rows(smg_context* ctx, int nx, int ny);
+smg_status smg_coarse_cg_tc(smg_context* ctx, const void* links, int nx, int ny, const cx<float>* b, cx<float>* x,
+                            void* r, float* rs, void* p0, float* ps0, void* p1, float* ps1, cx<float>* Ap,
+                            double* part, int* state, int max_iter, double tol, long long spin_limit);
 
 namespace {
 
@@ -1195,6 +1199,11 @@ struct CoarseWork {  // per level l >= 1, per precision
     void* ph = nullptr;
     float* rs = nullptr;
     float* ps = nullptr;
+    // the persistent tensor-core CG (k_ccg_tc): the second search-direction buffer and the per-CTA
+    // partial sums
+    void* ph2 = nullptr;
+    float* ps2 = nullptr;
+    double* ccg_part = nullptr;
 };
 
 struct smg_mg {
@@ -1447,7 +1456,8 @@ smg_status free_work(smg_mg* mg) {
     if (mg->mr_omf) cudaFree(mg->mr_omf);
     mg->mr_omf = nullptr;
     for (auto& w : mg->cw) {
-        for (void* p : {w.b, w.x, w.r, w.Ar, w.e, w.p, w.rh, w.ph, (void*)w.rs, (void*)w.ps})
+        for (void* p : {w.b, w.x, w.r, w.Ar, w.e, w.p, w.rh, w.ph, (void*)w.rs, (void*)w.ps, w.ph2, (void*)w.ps2,
+                        (void*)w.ccg_part})
             if (p) cudaFree(p);
     }
     mg->cw.clear();
@@ -1512,6 +1522,18 @@ bool coarse_half_level(const smg_mg* mg, int l, int nrhs, smg_precision prec) {
            mg->lv[l].ndof == 16 && tc_path(mg, l, nrhs);
 }
 
+// the coarsest CG of a coarse_half level runs as one persistent cooperative launch (k_ccg_tc) when the
+// hierarchy is not batched next to other streams (its CTAs must be co-resident) and the launch shape
+// fits the GPU; SMG_CCG_PERSISTENT=0 keeps the per-iteration kernels
+bool ccg_tc_level(const smg_mg* mg, int l) {
+    static const bool on = [] {
+        const char* e = std::getenv("SMG_CCG_PERSISTENT");
+        return !(e && std::atoi(e) == 0);
+    }();
+    const Level& L = mg->lv[l];
+    return on && mg->persistent && smg_coarse_cg_tc_rows(mg->ctx, L.nx, L.ny) > 0;
+}
+
 bool half_smoother(const smg_mg* mg, int nrhs, smg_precision prec) {
     const int nc = mg->lv[0].nc_next;
     return mg->p.smoother_half && prec == SMG_F32 && nrhs >= 8 && f16_nrhs_ok(nrhs) &&
@@ -1559,6 +1581,13 @@ smg_status ensure_work(smg_mg* mg, int nrhs, smg_precision prec) {
             SMG_CUDA(ctx, cudaMalloc((void**)&w.ps, sb));
             SMG_CUDA(ctx, cudaMemsetAsync(w.rs, 0, sb, ctx->stream));
             SMG_CUDA(ctx, cudaMemsetAsync(w.ps, 0, sb, ctx->stream));
+            if (ccg_tc_level(mg, (int)l)) {
+                SMG_CUDA(ctx, cudaMalloc(&w.ph2, hb));
+                SMG_CUDA(ctx, cudaMalloc((void**)&w.ps2, sb));
+                const Level& Lc = mg->lv[l];
+                const size_t nblk = (size_t)(Lc.nx / 8) * (Lc.ny / smg_coarse_cg_tc_rows(ctx, Lc.nx, Lc.ny));
+                SMG_CUDA(ctx, cudaMalloc((void**)&w.ccg_part, 64 * nblk * sizeof(double)));
+            }
         }
     }
     if (!mg->cg_state) {
@@ -1981,8 +2010,14 @@ smg_status coarse_cg(smg_mg* mg, int l, void* x, const void* b) {
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[l];
     if (std::is_same<T, float>::value && coarse_half_level(mg, l, mg->work_nrhs, SMG_F32) && mg->cw[l].rh &&
-        !(l == mg->defl.level && mg->defl.n > 0))
+        !(l == mg->defl.level && mg->defl.n > 0)) {
+        CoarseWork& w = mg->cw[l];
+        if (w.ph2 && ccg_tc_level(mg, l))
+            return smg_coarse_cg_tc(mg->ctx, L.Atc, L.nx, L.ny, (const cx<float>*)b, (cx<float>*)x, w.rh, w.rs, w.ph,
+                                    w.ps, w.ph2, w.ps2, (cx<float>*)w.Ar, w.ccg_part, (int*)mg->cg_state,
+                                    mg->p.coarse_max_iter, mg->p.coarse_tol, mg->spin_limit);
         return coarse_cg_half(mg, l, x, b);
+    }
     if (mg->persistent && mg->work_nrhs == 1 && !(l == mg->defl.level && mg->defl.n > 0)) {
         if (L.ndof == 8) return coarse_cg_persistent<T, 8>(mg, l, x, b);
         if (L.ndof == 16) return coarse_cg_persistent<T, 16>(mg, l, x, b);

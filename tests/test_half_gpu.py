@@ -4,6 +4,11 @@ site scale, the operator on FP16 fields against FP64, and mixed MG-GCR
 solves that still reach a true FP64 residual of 1e-10."""
 from __future__ import annotations
 
+import os
+import subprocess
+import sys
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -93,3 +98,44 @@ def test_half_coarsest_cg_cycle_and_solve(smg_gpu):
     assert r16.iterations <= 1.1 * r32.iterations + 2
     for j in (0, nrhs - 1):
         assert np.linalg.norm(B[j] - D.apply_DdagD(r16.solution[j])) / np.linalg.norm(B[j]) < 1e-10
+
+
+_CCG_CHILD = r"""
+import sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import schwinger_mg_gb300 as smg
+L, nrhs = 64, 32
+lat = smg.Lattice(L)
+D = smg.DiracOp(lat, smg.GaugeField(lat, smg.gauge_normal(L, 6.0, 43)), -0.05, 1.0, 1.0, 0.0)
+mg = smg.MGHierarchy(D, smg.mg_params(3, 4, 16, blocks=[(4, 4), (2, 2)], chiral_split=False, null_iters=4,
+                                       pre_smooth=4, post_smooth=4, w_cycle=False, coarse_max_iter=20,
+                                       coarse_tol=5e-2, precision="f32", seed=11, smoother_half=True,
+                                       coarse_half=True))
+B = np.stack([smg.random_vec(lat.ndof, 70 + j) for j in range(nrhs)])
+c = mg.precondition(smg.Field(lat, nrhs, "f32", data=B)).download()
+r = smg.fcg_solve_mg(D, lat.ndof, B, mg, 300, 1e-10, 20)
+np.savez(sys.argv[2], c=c, iters=r.iterations, res=r.true_residual)
+"""
+
+
+def _ccg_run(tmp_path: Path, name: str, persistent: bool) -> dict:
+    root = Path(__file__).resolve().parents[1]
+    out = tmp_path / f"{name}.npz"
+    env = dict(os.environ, SMG_CCG_PERSISTENT="1" if persistent else "0")
+    subprocess.run([sys.executable, "-c", _CCG_CHILD, str(root), str(out)], env=env, check=True, timeout=600)
+    with np.load(out) as z:
+        return {k: z[k] for k in z.files}
+
+
+def test_persistent_coarsest_cg_matches_per_iteration_kernels(tmp_path):
+    """The coarsest CG as one cooperative launch (k_ccg_tc: p formed on the fly from the FP16 r and the
+    previous p, two grid barriers per iteration) against the per-iteration kernels (apply, update, p
+    update) on the same hierarchy and right-hand sides, each in its own process: the cycles agree to
+    the FP16 and BF16 rounding of the search direction, the solves reach 1e-10 in as many iterations
+    up to two."""
+    per = _ccg_run(tmp_path, "per_iteration", False)
+    pst = _ccg_run(tmp_path, "persistent", True)
+    assert np.linalg.norm(pst["c"] - per["c"]) / np.linalg.norm(per["c"]) < 1e-2
+    assert float(pst["res"]) < 1e-10 and float(per["res"]) < 1e-10
+    assert abs(int(pst["iters"]) - int(per["iters"])) <= 2
