@@ -328,7 +328,7 @@ def kernel_trace(step, ctx, path: str, what: str) -> None:
 # profiles/smoother_f16_L512_32rhs.md)
 TC_LEVEL1_L512_DRAM_BYTES = 226.540288e6 + 42.035968e6
 DSLASH_F32_L512_DRAM_BYTES = 140.034048e6 + 98.370048e6
-SMOOTHER_D_L512_DRAM_BYTES = 74.601984e6 + 31.954176e6
+SMOOTHER_D_L512_DRAM_BYTES = 74.627072e6 + 31.32672e6
 
 
 def coarse_kernel_name(c, L, nrhs):
@@ -343,8 +343,8 @@ def smoother_times(smg, lib, ctx, mg32, lat, B, reps=20):
     f32 = smg.Field(lat, B.shape[0], "f32", ctx, data=B)
     ms, by = (Cc.c_double * 4)(), (Cc.c_double * 4)()
     smg._lib.check(lib.smg_mg_time_smoother(mg32.h, f32.h, reps, ms, by), "smg_mg_time_smoother", ctx.h)
-    names = ["k_dslash_h<D, FP16 in/out, fused ||t||^2>",
-             "k_dslash_h<D^dag, FP16 in/out, fused ||Ar||^2> (+ 2 kernels finishing the MR scalars)",
+    names = ["k_dslash_h32<D, fused ||t||^2> (FP16 in/out, 32 RHS)",
+             "k_dslash_h32<D^dag, fused ||Ar||^2> (+ 2 kernels finishing the MR scalars)",
              "k_mr_rupdate_h (r' = r - omega Ar, FP16)", "k_mr_xupdate_h (x += sum_k omega_k r_k, one per smoothing)"]
     return [{"kernel": n, "ms_per_launch": ms[k], "bytes_per_launch": by[k],
              "achieved_gbs": by[k] / (ms[k] * 1e-3) / 1e9} for k, n in enumerate(names)]

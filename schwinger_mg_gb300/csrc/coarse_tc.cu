@@ -591,17 +591,21 @@ __global__ void k_tile_links(const cx<double>* __restrict__ A, int nx, int64_t n
 //   update  own sites: x += alpha p_k, r_{k+1} = r_k - alpha A p_k (FP16, new site scales), and
 //           ||r_{k+1}||^2; grid barrier; beta_k, the per-rhs stop rule of the launched CG, and the
 //           exit once no rhs is active.
-// r and p are internal to the solve and stored dof-inner ([site][rhs][dof] __half2: the 16 dofs of a
-// site and rhs are four 16-byte words); b, x and A p keep the [site][dof][rhs] layout of the cycle.
-// Every phase issues its loads before its stores (the compiler may not move a load above a store
-// to global memory that it cannot prove disjoint), and values written by other CTAs during the
-// launch are read past L1 (ld.global.cg).  Every mbarrier and grid-barrier wait is bounded: a CTA
+// r and p are internal to the solve: FP16 dof-inner ([site][rhs][dof] __half2, the 16 dofs of a site
+// and rhs are four 16-byte words) with one FP32 scale per site and half of the 32 rhs ([site][2]);
+// b, x and A p keep the [site][dof][rhs] layout of the cycle.  The vector phases work on (site,
+// half) units, one per warp: lane l takes rhs 16 h + l / 2 and dofs 8 (l & 1) .. 8 (l & 1) + 7, so
+// that a warp's 16-byte accesses to r and p are one contiguous 1 KB and its accesses to b, x and
+// A p two contiguous 128-byte runs per dof (whole 32-byte sectors: values other CTAs write are read
+// past L1, ld.global.cg, and a half-used sector would cost a second L2 transfer).  Every phase issues
+// its loads before its stores (the compiler may not move a load above a store to global memory that
+// it cannot prove disjoint).  Every mbarrier and grid-barrier wait is bounded: a CTA
 // that gives up raises the error word, which ends every other CTA's barrier wait.
 struct CcgTcArgs {
     const uint8_t* links = nullptr;
     const float2* b = nullptr;           // [site][dof][32] right-hand side (FP32)
     float2* x = nullptr;                 // solution (FP32, [site][dof][32])
-    __half2* r = nullptr;                // residual (FP16, dof-inner) and site scales
+    __half2* r = nullptr;                // residual (FP16, dof-inner) and its scales [site][2]
     float* rs = nullptr;
     __half2* p[2] = {nullptr, nullptr};  // search directions (FP16, dof-inner), p_k in p[k & 1]
     float* ps[2] = {nullptr, nullptr};
@@ -710,15 +714,40 @@ __device__ __forceinline__ void ccg_sum_partials(const double* part, int nblk, d
     }
 }
 
-// the per-rhs sums of the warps' lanes (s_wred[warp][lane]) as this CTA's partial part[rhs][blin]
-__device__ __forceinline__ void ccg_publish(float* s_wred, float v, double* part, int nblk, int blin) {
-    s_wred[threadIdx.x] = v;  // [warp][lane]
+// this CTA's per-rhs partial part[rhs][blin] from the lanes' unit sums acc[h] (rhs 16 h + lane / 2,
+// the two lanes of an rhs already combined; lanes with odd index hold copies)
+__device__ __forceinline__ void ccg_publish(float* s_wred, const float (&acc)[2], double* part, int nblk, int blin) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if ((lane & 1) == 0) {
+        s_wred[warp * 32 + (lane >> 1)] = acc[0];
+        s_wred[warp * 32 + 16 + (lane >> 1)] = acc[1];
+    }
     __syncthreads();
     if (threadIdx.x < 32) {
         double t = 0.0;
         for (int w = 0; w < kThreads / 32; ++w) t += (double)s_wred[w * 32 + threadIdx.x];
         part[(int64_t)threadIdx.x * nblk + blin] = t;
     }
+}
+
+// 8 dofs (two 16-byte words) of a dof-inner FP16 vector as complex floats times a scale
+__device__ __forceinline__ void h8_unpack(const uint4& w0, const uint4& w1, float s, float2 (&v)[8]) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float2 a = h2f(word_of(w0, j)), b = h2f(word_of(w1, j));
+        v[j] = make_float2(a.x * s, a.y * s);
+        v[4 + j] = make_float2(b.x * s, b.y * s);
+    }
+}
+__device__ __forceinline__ void h8_pack(const float2 (&v)[8], float inv, uint4& w0, uint4& w1) {
+    w0.x = f2h(v[0].x * inv, v[0].y * inv);
+    w0.y = f2h(v[1].x * inv, v[1].y * inv);
+    w0.z = f2h(v[2].x * inv, v[2].y * inv);
+    w0.w = f2h(v[3].x * inv, v[3].y * inv);
+    w1.x = f2h(v[4].x * inv, v[4].y * inv);
+    w1.y = f2h(v[5].x * inv, v[5].y * inv);
+    w1.z = f2h(v[6].x * inv, v[6].y * inv);
+    w1.w = f2h(v[7].x * inv, v[7].y * inv);
 }
 
 __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
@@ -728,7 +757,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
     constexpr int nrhs = kRhsTile;
     const int x0 = blockIdx.x * kW, y0 = blockIdx.y * H;
     const int nblk = gridDim.x * gridDim.y, blin = blockIdx.x + gridDim.x * blockIdx.y;
-    const int nown = kW * H;
+    const int nunit = 2 * kW * H;  // (own site, rhs half) units
     const uint32_t ring_a = smem_u32(smem);
     const uint32_t link_a = ring_a + kRingBytes;
     const uint32_t bar_a = ring_a + kBarOffset;
@@ -744,8 +773,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
     auto bar = [&](int i) { return bar_a + 8u * (uint32_t)i; };
     double* part1 = a.part;                        // <A p, p> partials
     double* part2 = a.part + (int64_t)32 * nblk;  // ||r||^2 partials
-    // own site s (0 .. kW H - 1) of this CTA
-    auto own_site = [&](int s) { return (int64_t)(x0 + s % kW) + (int64_t)nx * (y0 + s / kW); };
+    // unit u: own site u / 2 of the strip, rhs half u & 1; this lane's rhs and dof half
+    const int lrhs = lane >> 1, dh = lane & 1;
+    auto unit_site = [&](int u) {
+        const int s = u >> 1;
+        return (int64_t)(x0 + s % kW) + (int64_t)nx * (y0 + s / kW);
+    };
+    // [site][dof][rhs] index of (site, dof 8 dh, rhs) for b, x and A p
+    auto e_of = [&](int64_t site, int rhs) { return (site * kNc + 8 * dh) * nrhs + rhs; };
 
     if (tid == 0) {
         for (int i = 0; i < kRing; ++i) {
@@ -776,43 +811,42 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
     tc_fence_after();
     const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(misc);
 
-    // ---- start: r = b (FP16), x = 0, p_{-1} = 0 in p[1], ||b||^2 per rhs (one warp per own site)
+    // ---- start: r = b (FP16), x = 0, p_{-1} = 0 in p[1], ||b||^2 per rhs
     {
-        float n2 = 0.f;
-        for (int s = warp; s < nown; s += kThreads / 32) {
-            const int64_t site = own_site(s);
-            const int64_t e0 = site * kNc * nrhs + lane;
-            float2 v[kNc];
+        float acc[2] = {0.f, 0.f};
+        for (int u = warp; u < nunit; u += kThreads / 32) {
+            const int64_t site = unit_site(u);
+            const int h = u & 1, rhs = 16 * h + lrhs;
+            const int64_t e0 = e_of(site, rhs);
+            float2 v[8];
 #pragma unroll
-            for (int d = 0; d < kNc; ++d) v[d] = __ldcg(a.b + e0 + d * nrhs);
-            float m = 0.f;
+            for (int j = 0; j < 8; ++j) v[j] = __ldcg(a.b + e0 + j * nrhs);
+            float m = 0.f, n2 = 0.f;
 #pragma unroll
-            for (int d = 0; d < kNc; ++d) {
-                m = fmaxf(m, fmaxf(fabsf(v[d].x), fabsf(v[d].y)));
-                n2 += v[d].x * v[d].x + v[d].y * v[d].y;
+            for (int j = 0; j < 8; ++j) {
+                m = fmaxf(m, fmaxf(fabsf(v[j].x), fabsf(v[j].y)));
+                n2 += v[j].x * v[j].x + v[j].y * v[j].y;
             }
             m = ccg_warp_max(m);
-            const float inv = m > 0.f ? __fdividef(1.0f, m) : 0.f;
-            uint4* rp = h16_ptr(a.r, site, lane);
-            uint4* pp = h16_ptr(a.p[1], site, lane);
+            uint4 w0, w1;
+            h8_pack(v, m > 0.f ? __fdividef(1.0f, m) : 0.f, w0, w1);
+            uint4* rp = h16_ptr(a.r, site, rhs) + 2 * dh;
+            uint4* pp = h16_ptr(a.p[1], site, rhs) + 2 * dh;
+            __stcg(rp, w0);
+            __stcg(rp + 1, w1);
+            __stcg(pp, make_uint4(0u, 0u, 0u, 0u));
+            __stcg(pp + 1, make_uint4(0u, 0u, 0u, 0u));
 #pragma unroll
-            for (int q = 0; q < kNc / 4; ++q) {
-                uint4 w;
-                w.x = f2h(v[4 * q].x * inv, v[4 * q].y * inv);
-                w.y = f2h(v[4 * q + 1].x * inv, v[4 * q + 1].y * inv);
-                w.z = f2h(v[4 * q + 2].x * inv, v[4 * q + 2].y * inv);
-                w.w = f2h(v[4 * q + 3].x * inv, v[4 * q + 3].y * inv);
-                __stcg(rp + q, w);
-                __stcg(pp + q, make_uint4(0u, 0u, 0u, 0u));
-            }
-#pragma unroll
-            for (int d = 0; d < kNc; ++d) __stcg(a.x + e0 + d * nrhs, make_float2(0.f, 0.f));
+            for (int j = 0; j < 8; ++j) __stcg(a.x + e0 + j * nrhs, make_float2(0.f, 0.f));
             if (lane == 0) {
-                __stcg(a.rs + site, m);
-                __stcg(a.ps[1] + site, 0.f);
+                __stcg(a.rs + 2 * site + h, m);
+                __stcg(a.ps[1] + 2 * site + h, 0.f);
             }
+            const float n2r = n2 + __shfl_xor_sync(0xffffffffu, n2, 1);  // the rhs's two lanes
+            if (h) acc[1] += n2r;
+            else acc[0] += n2r;
         }
-        ccg_publish(s_wred, n2, part2, nblk, blin);
+        ccg_publish(s_wred, acc, part2, nblk, blin);
     }
     bool ok = ccg_grid_barrier(a.bar, a.err, a.spin_limit);
     if (ok) {
@@ -901,134 +935,128 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                 }
             }
             __syncwarp();
-        } else if (warp == 4 || warp == 5 || warp == 8 || warp == 9) {
-            // epilogue: A p_k of the own sites to global memory
-            const int half = warp >= 8 ? 1 : 0;
-            const int sub = warp - (half ? 8 : 4);
-            const int m = 32 * sub + lane;
-            const int rhs = m >> 1, c = m & 1;
-            const int64_t rstride = 2ll * nrhs;
-            float* __restrict__ ybase = reinterpret_cast<float*>(a.Ap);
-            for (int r = 0; r < H; ++r) {
-                const int R = ab + r;
-                const bool eok = wait_bar(bar(kBarAccFull + (R & 1)), (R >> 1) & 1, abort_flag);
-                if (!__all_sync(0xffffffffu, eok)) break;
-                tc_fence_after();
-#pragma unroll
-                for (int q = 0; q < kEpiSites; ++q) {
-                    const int i = half * kEpiSites + q;
-                    float d[32];
-                    tmem_ld32(tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)((R & 1) * kAccCols + 32 * i), d);
-                    const int64_t base =
-                        (((int64_t)x0 + i + (int64_t)nx * (y0 + r)) * kNc * nrhs + rhs) * 2 + c;
-#pragma unroll
-                    for (int kk = 0; kk < kNc; ++kk) {
-                        const float other = __shfl_xor_sync(0xffffffffu, d[16 + kk], 1);
-                        __stcg(ybase + base + kk * rstride, c == 0 ? d[kk] - other : d[kk] + other);
-                    }
-                }
-                tc_fence_before();
-                mbar_arrive(bar(kBarAccEmpty + (R & 1)));
-            }
         } else if (warp == 2 || warp == 3 || warp == 6 || warp == 7) {
-            // stagers: p_k = r_k + beta p_{k-1} (FP16 inputs with site scales) -> BF16 A tiles
+            // stagers: p_k = r_k + beta p_{k-1} (FP16 inputs with scales) -> BF16 A tiles.  Item i of a
+            // source row: site i / 128 of the row, rhs (i / 4) % 32, word i % 4 (dofs 4 (i % 4) ..
+            // + 3): a warp's items are 8 rhs x 4 words of one site, 512 contiguous bytes of r and p
             const int st = (warp < 4 ? warp - 2 : warp - 4) * 32 + lane;
+            constexpr int kItems = kSrcSites * 32 * 4;
+            constexpr int kPer = kItems / 128;  // 10
+            constexpr int kBatch = 5;
             for (int lr = 0; lr < H + 2; ++lr) {
                 const int S = sb + lr, slot = S % kRing, use = S / kRing;
                 if (use > 0 && !wait_bar(bar(kBarSrcEmpty + slot), (use - 1) & 1, abort_flag)) break;
                 const int gy = wrapi(y0 - 1 + lr, ny);
                 uint8_t* row = smem + slot * kRowBytes;
-                constexpr int kItems = kSrcSites * 2 * 32;  // (site, 8-dof group, rhs)
-                constexpr int kPer = kItems / 128;
-                uint4 rv[kPer][2], pv[kPer][2];
-                float sr[kPer], sp[kPer];
 #pragma unroll
-                for (int it = 0; it < kPer; ++it) {  // every load of the row first
-                    const int item = st + it * 128;
-                    const int r = item & 31, g = (item >> 5) & 1, t = item >> 6;
-                    const int64_t site = wrapi(x0 - 1 + t, nx) + (int64_t)nx * gy;
-                    const uint4* rp = h16_ptr(a.r, site, r) + 2 * g;
-                    const uint4* pp = h16_ptr(pold, site, r) + 2 * g;
-                    rv[it][0] = __ldcg(rp);
-                    rv[it][1] = __ldcg(rp + 1);
-                    pv[it][0] = __ldcg(pp);
-                    pv[it][1] = __ldcg(pp + 1);
-                    sr[it] = __ldcg(a.rs + site);
-                    sp[it] = __ldcg(psold + site) * s_beta[r];
-                }
+                for (int b0 = 0; b0 < kPer; b0 += kBatch) {
+                    uint4 rv[kBatch], pv[kBatch];
+                    float sr[kBatch], sp[kBatch];
 #pragma unroll
-                for (int it = 0; it < kPer; ++it) {
-                    const int item = st + it * 128;
-                    const int r = item & 31, g = (item >> 5) & 1, t = item >> 6;
-                    float2 e[8];
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        const float2 a2 = h2f(word_of(rv[it][j >> 2], j & 3));
-                        const float2 b2 = h2f(word_of(pv[it][j >> 2], j & 3));
-                        e[j] = make_float2(fmaf(sr[it], a2.x, sp[it] * b2.x), fmaf(sr[it], a2.y, sp[it] * b2.y));
+                    for (int q = 0; q < kBatch; ++q) {  // the batch's loads first
+                        const int i = st + 128 * (b0 + q);
+                        const int t = i >> 7, r = (i >> 2) & 31, wq = i & 3;
+                        const int64_t site = wrapi(x0 - 1 + t, nx) + (int64_t)nx * gy;
+                        rv[q] = __ldcg(h16_ptr(a.r, site, r) + wq);
+                        pv[q] = __ldcg(h16_ptr(pold, site, r) + wq);
+                        sr[q] = __ldcg(a.rs + 2 * site + (r >> 4));
+                        sp[q] = __ldcg(psold + 2 * site + (r >> 4)) * s_beta[r];
                     }
-                    uint4 re, im;
-                    re.x = pack_bf16(e[0].x, e[1].x);
-                    re.y = pack_bf16(e[2].x, e[3].x);
-                    re.z = pack_bf16(e[4].x, e[5].x);
-                    re.w = pack_bf16(e[6].x, e[7].x);
-                    im.x = pack_bf16(e[0].y, e[1].y);
-                    im.y = pack_bf16(e[2].y, e[3].y);
-                    im.z = pack_bf16(e[4].y, e[5].y);
-                    im.w = pack_bf16(e[6].y, e[7].y);
-                    uint8_t* tile = row + t * kTileA;
-                    const int mr = 2 * r, mi = 2 * r + 1;
-                    *reinterpret_cast<uint4*>(tile + (mr >> 3) * kSboA + g * 128 + (mr & 7) * 16) = re;
-                    *reinterpret_cast<uint4*>(tile + (mi >> 3) * kSboA + g * 128 + (mi & 7) * 16) = im;
+#pragma unroll
+                    for (int q = 0; q < kBatch; ++q) {
+                        const int i = st + 128 * (b0 + q);
+                        const int t = i >> 7, r = (i >> 2) & 31, wq = i & 3;
+                        float2 e[4];
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const float2 a2 = h2f(word_of(rv[q], j)), b2 = h2f(word_of(pv[q], j));
+                            e[j] = make_float2(fmaf(sr[q], a2.x, sp[q] * b2.x), fmaf(sr[q], a2.y, sp[q] * b2.y));
+                        }
+                        const uint2 re = make_uint2(pack_bf16(e[0].x, e[1].x), pack_bf16(e[2].x, e[3].x));
+                        const uint2 im = make_uint2(pack_bf16(e[0].y, e[1].y), pack_bf16(e[2].y, e[3].y));
+                        uint8_t* tile = row + t * kTileA + (wq >> 1) * 128 + (wq & 1) * 8;
+                        const int mr = 2 * r, mi = 2 * r + 1;
+                        *reinterpret_cast<uint2*>(tile + (mr >> 3) * kSboA + (mr & 7) * 16) = re;
+                        *reinterpret_cast<uint2*>(tile + (mi >> 3) * kSboA + (mi & 7) * 16) = im;
+                    }
                 }
                 fence_proxy_async();
                 mbar_arrive(bar(kBarSrcFull + slot));
             }
-        } else if (warp == 10 || warp == 11) {
-            // own sites' p_k -> p[k & 1] (FP16, site scale = the site's largest |re| or |im|), two
-            // sites per step with both sites' loads first
-            for (int s0 = 2 * (warp - 10); s0 < nown; s0 += 4) {
-                uint4 rv[2][4], pv[2][4];
-                float sr[2], sp[2];
-                int64_t site[2];
+        } else {
+            // warps 4, 5, 8, 9 (then the epilogue) and 10, 11: p_k of the own sites -> p[k & 1] (FP16,
+            // scale per unit = its largest |re| or |im|); warp pw takes units pw, pw + 6, ..., four
+            // per step with all four units' loads first
+            const int pw = warp <= 5 ? warp - 4 : warp - 6;  // 0 .. 5
+            constexpr int kPw = 6, kPq = 4;
+            for (int u0 = pw; u0 < nunit; u0 += kPq * kPw) {
+                uint4 rv[kPq][2], pv[kPq][2];
+                float sr[kPq], sp[kPq];
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    site[h] = own_site(s0 + h < nown ? s0 + h : s0);
-                    const uint4* rp = h16_ptr(a.r, site[h], lane);
-                    const uint4* pp = h16_ptr(pold, site[h], lane);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        rv[h][q] = __ldcg(rp + q);
-                        pv[h][q] = __ldcg(pp + q);
-                    }
-                    sr[h] = __ldcg(a.rs + site[h]);
-                    sp[h] = __ldcg(psold + site[h]) * s_beta[lane];
+                for (int q = 0; q < kPq; ++q) {
+                    const int u = u0 + q * kPw < nunit ? u0 + q * kPw : u0;
+                    const int64_t site = unit_site(u);
+                    const int h = u & 1, rhs = 16 * h + lrhs;
+                    const uint4* rp = h16_ptr(a.r, site, rhs) + 2 * dh;
+                    const uint4* pp = h16_ptr(pold, site, rhs) + 2 * dh;
+                    rv[q][0] = __ldcg(rp);
+                    rv[q][1] = __ldcg(rp + 1);
+                    pv[q][0] = __ldcg(pp);
+                    pv[q][1] = __ldcg(pp + 1);
+                    sr[q] = __ldcg(a.rs + 2 * site + h);
+                    sp[q] = __ldcg(psold + 2 * site + h) * s_beta[rhs];
                 }
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    if (s0 + h >= nown) break;
-                    float2 v[kNc];
+                for (int q = 0; q < kPq; ++q) {
+                    const int u = u0 + q * kPw;
+                    if (u >= nunit) break;
+                    const int64_t site = unit_site(u);
+                    const int h = u & 1, rhs = 16 * h + lrhs;
+                    float2 v[8], pr[8];
+                    h8_unpack(rv[q][0], rv[q][1], sr[q], v);
+                    h8_unpack(pv[q][0], pv[q][1], sp[q], pr);
                     float mx = 0.f;
 #pragma unroll
-                    for (int d = 0; d < kNc; ++d) {
-                        const float2 a2 = h2f(word_of(rv[h][d >> 2], d & 3));
-                        const float2 b2 = h2f(word_of(pv[h][d >> 2], d & 3));
-                        v[d] = make_float2(fmaf(sr[h], a2.x, sp[h] * b2.x), fmaf(sr[h], a2.y, sp[h] * b2.y));
-                        mx = fmaxf(mx, fmaxf(fabsf(v[d].x), fabsf(v[d].y)));
+                    for (int j = 0; j < 8; ++j) {
+                        v[j] = make_float2(v[j].x + pr[j].x, v[j].y + pr[j].y);
+                        mx = fmaxf(mx, fmaxf(fabsf(v[j].x), fabsf(v[j].y)));
                     }
                     mx = ccg_warp_max(mx);
-                    const float inv = mx > 0.f ? __fdividef(1.0f, mx) : 0.f;
-                    uint4* op = h16_ptr(pnew, site[h], lane);
+                    uint4 w0, w1;
+                    h8_pack(v, mx > 0.f ? __fdividef(1.0f, mx) : 0.f, w0, w1);
+                    uint4* op = h16_ptr(pnew, site, rhs) + 2 * dh;
+                    __stcg(op, w0);
+                    __stcg(op + 1, w1);
+                    if (lane == 0) __stcg(psnew + 2 * site + h, mx);
+                }
+            }
+            if (warp <= 9) {
+                // epilogue: A p_k of the own sites to global memory
+                const int half = warp >= 8 ? 1 : 0;
+                const int sub = warp - (half ? 8 : 4);
+                const int m = 32 * sub + lane;
+                const int rhs = m >> 1, c = m & 1;
+                const int64_t rstride = 2ll * nrhs;
+                float* __restrict__ ybase = reinterpret_cast<float*>(a.Ap);
+                for (int r = 0; r < H; ++r) {
+                    const int R = ab + r;
+                    const bool eok = wait_bar(bar(kBarAccFull + (R & 1)), (R >> 1) & 1, abort_flag);
+                    if (!__all_sync(0xffffffffu, eok)) break;
+                    tc_fence_after();
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        uint4 w;
-                        w.x = f2h(v[4 * q].x * inv, v[4 * q].y * inv);
-                        w.y = f2h(v[4 * q + 1].x * inv, v[4 * q + 1].y * inv);
-                        w.z = f2h(v[4 * q + 2].x * inv, v[4 * q + 2].y * inv);
-                        w.w = f2h(v[4 * q + 3].x * inv, v[4 * q + 3].y * inv);
-                        __stcg(op + q, w);
+                    for (int q = 0; q < kEpiSites; ++q) {
+                        const int i = half * kEpiSites + q;
+                        float d[32];
+                        tmem_ld32(tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)((R & 1) * kAccCols + 32 * i), d);
+                        const int64_t base = (((int64_t)x0 + i + (int64_t)nx * (y0 + r)) * kNc * nrhs + rhs) * 2 + c;
+#pragma unroll
+                        for (int kk = 0; kk < kNc; ++kk) {
+                            const float other = __shfl_xor_sync(0xffffffffu, d[16 + kk], 1);
+                            __stcg(ybase + base + kk * rstride, c == 0 ? d[kk] - other : d[kk] + other);
+                        }
                     }
-                    if (lane == 0) __stcg(psnew + site[h], mx);
+                    tc_fence_before();
+                    mbar_arrive(bar(kBarAccEmpty + (R & 1)));
                 }
             }
         }
@@ -1039,29 +1067,42 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
             if (tid == 0) atomicCAS(a.err, 0, 2);
             break;
         }
-        // ================= <A p_k, p_k> of the own sites per rhs (one warp per site, lane = rhs)
+        // ================= <A p_k, p_k> of the own sites per rhs: three units per step, loads first
         {
-            float dot = 0.f;
-            for (int s = warp; s < nown; s += kThreads / 32) {
-                const int64_t site = own_site(s);
-                const int64_t e0 = site * kNc * nrhs + lane;
-                float2 av[kNc];
-                uint4 pv[4];
-                const uint4* pp = h16_ptr(pnew, site, lane);
+            float acc[2] = {0.f, 0.f};
+            constexpr int kW32 = kThreads / 32;
+            for (int u0 = warp; u0 < nunit; u0 += 3 * kW32) {
+                uint4 pw[3][2];
+                float2 av[3][8];
+                float sp[3];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) pv[q] = __ldcg(pp + q);
+                for (int q = 0; q < 3; ++q) {
+                    const int u = u0 + q * kW32 < nunit ? u0 + q * kW32 : u0;
+                    const int64_t site = unit_site(u);
+                    const int h = u & 1, rhs = 16 * h + lrhs;
+                    const int64_t e0 = e_of(site, rhs);
+                    const uint4* pp = h16_ptr(pnew, site, rhs) + 2 * dh;
+                    pw[q][0] = __ldcg(pp);
+                    pw[q][1] = __ldcg(pp + 1);
 #pragma unroll
-                for (int d = 0; d < kNc; ++d) av[d] = __ldcg(a.Ap + e0 + d * nrhs);
-                const float sp = __ldcg(psnew + site);
-                float t = 0.f;
-#pragma unroll
-                for (int d = 0; d < kNc; ++d) {
-                    const float2 p2 = h2f(word_of(pv[d >> 2], d & 3));
-                    t += av[d].x * p2.x + av[d].y * p2.y;  // Re <A p, p>
+                    for (int j = 0; j < 8; ++j) av[q][j] = __ldcg(a.Ap + e0 + j * nrhs);
+                    sp[q] = __ldcg(psnew + 2 * site + h);
                 }
-                dot += sp * t;
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    const int u = u0 + q * kW32;
+                    if (u >= nunit) break;
+                    float2 pv[8];
+                    h8_unpack(pw[q][0], pw[q][1], sp[q], pv);
+                    float t = 0.f;
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) t += av[q][j].x * pv[j].x + av[q][j].y * pv[j].y;  // Re <A p, p>
+                    const float v = t + __shfl_xor_sync(0xffffffffu, t, 1);
+                    if (u & 1) acc[1] += v;
+                    else acc[0] += v;
+                }
             }
-            ccg_publish(s_wred, dot, part1, nblk, blin);
+            ccg_publish(s_wred, acc, part1, nblk, blin);
         }
         ok = ccg_grid_barrier(a.bar, a.err, a.spin_limit);
         if (!ok) break;
@@ -1074,57 +1115,69 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
             s_alpha[tid] = al;
         }
         __syncthreads();
-        // ================= update of the own sites, one warp per site (lane = rhs), loads first
+        // ================= update of the own sites: two units per step, both units' loads first
         {
-            const float al = s_alpha[lane];
-            float n2 = 0.f;
-            for (int s = warp; s < nown; s += kThreads / 32) {
-                const int64_t site = own_site(s);
-                const int64_t e0 = site * kNc * nrhs + lane;
-                uint4 rv[4], pv[4];
-                float2 av[kNc], xv[kNc];
-                const uint4* rp = h16_ptr(a.r, site, lane);
-                const uint4* pp = h16_ptr(pnew, site, lane);
+            float acc[2] = {0.f, 0.f};
+            constexpr int kW32 = kThreads / 32;
+            for (int u0 = warp; u0 < nunit; u0 += 2 * kW32) {
+                uint4 rw[2][2], pw[2][2];
+                float2 av[2][8], xv[2][8];
+                float sr[2], sp[2];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    rv[q] = __ldcg(rp + q);
-                    pv[q] = __ldcg(pp + q);
+                for (int q = 0; q < 2; ++q) {
+                    const int u = u0 + q * kW32 < nunit ? u0 + q * kW32 : u0;
+                    const int64_t site = unit_site(u);
+                    const int h = u & 1, rhs = 16 * h + lrhs;
+                    const int64_t e0 = e_of(site, rhs);
+                    const uint4* rp = h16_ptr(a.r, site, rhs) + 2 * dh;
+                    const uint4* pp = h16_ptr(pnew, site, rhs) + 2 * dh;
+                    rw[q][0] = __ldcg(rp);
+                    rw[q][1] = __ldcg(rp + 1);
+                    pw[q][0] = __ldcg(pp);
+                    pw[q][1] = __ldcg(pp + 1);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        av[q][j] = __ldcg(a.Ap + e0 + j * nrhs);
+                        xv[q][j] = __ldcg(a.x + e0 + j * nrhs);
+                    }
+                    sr[q] = __ldcg(a.rs + 2 * site + h);
+                    sp[q] = __ldcg(psnew + 2 * site + h);
                 }
 #pragma unroll
-                for (int d = 0; d < kNc; ++d) {
-                    av[d] = __ldcg(a.Ap + e0 + d * nrhs);
-                    xv[d] = __ldcg(a.x + e0 + d * nrhs);
-                }
-                const float sr = __ldcg(a.rs + site), sp = __ldcg(psnew + site);
-                float2 rn[kNc];
-                float mx = 0.f;
+                for (int q = 0; q < 2; ++q) {
+                    const int u = u0 + q * kW32;
+                    if (u >= nunit) break;
+                    const int64_t site = unit_site(u);
+                    const int h = u & 1, rhs = 16 * h + lrhs;
+                    const int64_t e0 = e_of(site, rhs);
+                    const float al = s_alpha[rhs];
+                    float2 rv[8], pv[8];
+                    h8_unpack(rw[q][0], rw[q][1], sr[q], rv);
+                    h8_unpack(pw[q][0], pw[q][1], al * sp[q], pv);
+                    float mx = 0.f, n2 = 0.f;
 #pragma unroll
-                for (int d = 0; d < kNc; ++d) {
-                    const float2 r2 = h2f(word_of(rv[d >> 2], d & 3));
-                    const float2 p2 = h2f(word_of(pv[d >> 2], d & 3));
-                    xv[d].x += al * sp * p2.x;
-                    xv[d].y += al * sp * p2.y;
-                    rn[d] = make_float2(sr * r2.x - al * av[d].x, sr * r2.y - al * av[d].y);
-                    mx = fmaxf(mx, fmaxf(fabsf(rn[d].x), fabsf(rn[d].y)));
-                    n2 += rn[d].x * rn[d].x + rn[d].y * rn[d].y;
-                }
-                mx = ccg_warp_max(mx);  // also orders every lane's scale read before lane 0's write
-                const float inv = mx > 0.f ? __fdividef(1.0f, mx) : 0.f;
+                    for (int j = 0; j < 8; ++j) {
+                        xv[q][j].x += pv[j].x;
+                        xv[q][j].y += pv[j].y;
+                        rv[j] = make_float2(rv[j].x - al * av[q][j].x, rv[j].y - al * av[q][j].y);
+                        mx = fmaxf(mx, fmaxf(fabsf(rv[j].x), fabsf(rv[j].y)));
+                        n2 += rv[j].x * rv[j].x + rv[j].y * rv[j].y;
+                    }
+                    mx = ccg_warp_max(mx);  // also orders every lane's scale read before lane 0's write
+                    uint4 w0, w1;
+                    h8_pack(rv, mx > 0.f ? __fdividef(1.0f, mx) : 0.f, w0, w1);
 #pragma unroll
-                for (int d = 0; d < kNc; ++d) __stcg(a.x + e0 + d * nrhs, xv[d]);
-                uint4* wp = h16_ptr(a.r, site, lane);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    uint4 w;
-                    w.x = f2h(rn[4 * q].x * inv, rn[4 * q].y * inv);
-                    w.y = f2h(rn[4 * q + 1].x * inv, rn[4 * q + 1].y * inv);
-                    w.z = f2h(rn[4 * q + 2].x * inv, rn[4 * q + 2].y * inv);
-                    w.w = f2h(rn[4 * q + 3].x * inv, rn[4 * q + 3].y * inv);
-                    __stcg(wp + q, w);
+                    for (int j = 0; j < 8; ++j) __stcg(a.x + e0 + j * nrhs, xv[q][j]);
+                    uint4* wp = h16_ptr(a.r, site, rhs) + 2 * dh;
+                    __stcg(wp, w0);
+                    __stcg(wp + 1, w1);
+                    if (lane == 0) __stcg(a.rs + 2 * site + h, mx);
+                    const float v = n2 + __shfl_xor_sync(0xffffffffu, n2, 1);  // the rhs's two lanes
+                    if (h) acc[1] += v;
+                    else acc[0] += v;
                 }
-                if (lane == 0) __stcg(a.rs + site, mx);
             }
-            ccg_publish(s_wred, n2, part2, nblk, blin);
+            ccg_publish(s_wred, acc, part2, nblk, blin);
         }
         ok = ccg_grid_barrier(a.bar, a.err, a.spin_limit);
         if (!ok) break;

@@ -1574,7 +1574,8 @@ smg_status ensure_work(smg_mg* mg, int nrhs, smg_precision prec) {
         }
         if (coarse_half_level(mg, (int)l, nrhs, prec)) {
             const size_t hb = (size_t)mg->lv[l].nsites * nrhs * mg->lv[l].ndof * sizeof(__half2);
-            const size_t sb = (size_t)mg->lv[l].nsites * sizeof(float);
+            // one scale per site (per-iteration kernels) or per site and half of the 32 rhs (k_ccg_tc)
+            const size_t sb = (size_t)mg->lv[l].nsites * 2 * sizeof(float);
             SMG_CUDA(ctx, cudaMalloc(&w.rh, hb));
             SMG_CUDA(ctx, cudaMalloc(&w.ph, hb));
             SMG_CUDA(ctx, cudaMalloc((void**)&w.rs, sb));

@@ -147,6 +147,55 @@ __device__ __forceinline__ void block_reduce_finalise(double (&v)[K], double* __
     if (t == 0) ticket[blockIdx.y] = 0u;
 }
 
+// First stage only: the block's partial per (rhs, k) into partials[(rhs * K + k) * gridDim.x + blockIdx.x],
+// for a separate kernel to sum (k_sum_partials below) when a single finishing block would be slow.
+template <int K, typename T>
+__device__ __forceinline__ void block_partials(const T (&vin)[K], double* __restrict__ partials, int nrhs) {
+    __shared__ double s_rows[K][kReduceMaxThreads / 32][32];
+    const int lanes = blockDim.x;
+    const int t = threadIdx.y * lanes + threadIdx.x;
+    const int lane_id = t & 31, warp = t >> 5;
+    const int nwarps = (blockDim.x * blockDim.y + 31) >> 5;
+    const int rhs0 = blockIdx.y * lanes;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double a = (double)vin[k];
+        for (int off = 16; off >= lanes; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+        if (lane_id < lanes) s_rows[k][warp][lane_id] = a;
+    }
+    __syncthreads();
+    if (t < lanes && rhs0 + t < nrhs) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double a = 0.0;
+            for (int w = 0; w < nwarps; ++w) a += s_rows[k][w][t];
+            partials[((size_t)(rhs0 + t) * K + k) * gridDim.x + blockIdx.x] = a;
+        }
+    }
+}
+
+// Second stage: one warp per (rhs, k < nk) sums the nb block partials of block_partials<K> (lanes stride
+// the blocks, eight loads in flight per lane, then a fixed shuffle tree: deterministic) into
+// out[rhs * stride + k].  Launch with nrhs * nk warps.
+static __global__ void __launch_bounds__(256) k_sum_partials(const double* __restrict__ partials, int nb, int nrhs, int K,
+                                                      int nk, double* __restrict__ out, int stride) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= nrhs * nk) return;
+    const int rhs = w / nk, k = w - rhs * nk;
+    const double* src = partials + ((size_t)rhs * K + k) * nb;
+    double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int b0 = 0; b0 < nb; b0 += 8 * 32) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int b = b0 + u * 32 + lane;
+            if (b < nb) acc[u] += __ldcg(src + b);
+        }
+    }
+    double a = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+    for (int off = 16; off >= 1; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+    if (lane == 0) out[rhs * stride + k] = a;
+}
+
 // FP32 per-thread partials: widened to FP64 once per thread, then reduced as above.
 template <int K, typename Fin>
 __device__ __forceinline__ void block_reduce_finalise(float (&v)[K], double* __restrict__ partials,

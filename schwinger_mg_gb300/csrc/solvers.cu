@@ -376,17 +376,9 @@ struct DotPtrs {
     const cx<T>* ap[kDotChunk];
 };
 
-struct FinDots {  // out[rhs * stride + k] = sums[k], k < nk
-    double* out;
-    int stride, nk;
-    __device__ void operator()(int rhs, const double* s) const {
-        for (int k = 0; k < nk; ++k) out[rhs * stride + k] = s[k];
-    }
-};
-
+// per-block partials of <AP_i, Az> (block_partials<2 kDotChunk>); k_sum_partials finishes them
 template <typename T>
-__global__ void __launch_bounds__(256) k_gcr_multidot(VecView<T> az, DotPtrs<T> ptr, int ns, double* partials,
-                                                      unsigned int* ticket, double* out, int stride) {
+__global__ void __launch_bounds__(256) k_gcr_multidot(VecView<T> az, DotPtrs<T> ptr, int ns, double* partials) {
     constexpr int K = 2 * kDotChunk;
     const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
     T v[K];  // per-thread partials in the field precision (FP64 is scarce on this part)
@@ -406,7 +398,7 @@ __global__ void __launch_bounds__(256) k_gcr_multidot(VecView<T> az, DotPtrs<T> 
             }
         }
     }
-    block_reduce_finalise<K>(v, partials, ticket, az.nrhs, FinDots{out, stride, 2 * ns});
+    block_partials<K>(v, partials, az.nrhs);
 }
 
 template <typename T>
@@ -615,12 +607,14 @@ smg_status gcr_core(smg_dirac* d, smg_mg* mg, GcrWs<T>& ws, const smg_field* b, 
             DotPtrs<T> dp{};
             const int ns = std::min(kDotChunk, nring - c0);
             for (int i = 0; i < ns; ++i) dp.ap[i] = (const cx<T>*)ws.AP[ring[c0 + i]]->data;
-            // 2 blocks per SM: the 2 ns partials per rhs and block stay few for the final sum
-            const dim3 mgrid(std::min(rl.grid.x, 304u), rl.grid.y);
-            k_gcr_multidot<T><<<mgrid, rl.block, 0, ctx->stream>>>(fv<T>(ws.Az), dp, ns, ctx->red.partials,
-                                                                    ctx->red.tickets, ws.dots + 2 * c0,
+            // every resident block streams Az and the AP_i; the 2 ns block partials per rhs are summed
+            // by one warp each in a second kernel (a single finishing block would serialise them)
+            k_gcr_multidot<T><<<rl.grid, rl.block, 0, ctx->stream>>>(fv<T>(ws.Az), dp, ns, ctx->red.partials);
+            const int nwarp = nrhs * 2 * ns;
+            k_sum_partials<<<(nwarp + 7) / 8, 256, 0, ctx->stream>>>(ctx->red.partials, (int)rl.grid.x, nrhs,
+                                                                    2 * kDotChunk, 2 * ns, ws.dots + 2 * c0,
                                                                     2 * ws.nbuf);
-            count_launch(ctx);
+            count_launch(ctx, 2);
             SMG_CHECK_LAUNCH(ctx);
         }
         // p and Ap in kOrthChunk passes; the last one also forms <Ap, r> and ||Ap||^2
