@@ -315,10 +315,13 @@ typedef struct {
                                           vectors (residual, A r, D r) in FP16 with one FP32 scale
                                           per site, arithmetic in FP32 (power-of-two nrhs from 8
                                           to 32); 0 (default): FP32 */
-    int coarse_half;                   /* 1: an F32 hierarchy keeps the coarsest-level CG's residual
-                                          and search direction in FP16 with one FP32 scale per coarse
-                                          site (the tensor-core path: 16 dofs, 32 right-hand sides),
-                                          arithmetic and accumulation in FP32; 0 (default): FP32 */
+    int coarse_half;                   /* 1: an F32 hierarchy keeps the coarse solves' work vectors
+                                          in FP16 with FP32 scales (per coarse site and half of the
+                                          32 right-hand sides): the coarsest-level CG's residual and
+                                          search directions, and the MR residuals and A r of the
+                                          intermediate levels (the tensor-core path: 16 dofs, 32
+                                          right-hand sides); solutions, arithmetic and accumulation
+                                          in FP32; 0 (default): FP32 */
 } smg_mg_params;
 
 /* Fills p with the reference's defaults: 2 levels, 4 x 4 blocks, 4 null

@@ -726,8 +726,9 @@ def mg_params(n_levels: int = 2, block_size: int = 4, k_null: int = 4, coarse_bl
     aggregate shapes and null-vector counts.  `tensor_cores` lets an F32
     hierarchy apply its batched coarse operators on the tensor cores;
     `smoother_half` keeps its fine smoother's work vectors in FP16 with
-    per-site scales; `coarse_half` does the same for the coarsest-level
-    CG's residual and search direction."""
+    per-site scales; `coarse_half` does the same (scales per coarse site and
+    half of the 32 right-hand sides) for the coarsest-level CG's residual and
+    search directions and the intermediate levels' MR residuals."""
     p = _L.MGParams()
     _L.check(_L.lib().smg_mg_params_default(C.byref(p)), "smg_mg_params_default")
     p.n_levels = n_levels

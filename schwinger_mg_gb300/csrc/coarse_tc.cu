@@ -56,6 +56,7 @@
 #include <tuple>
 #include <vector>
 
+#include "half.cuh"
 #include "smg_internal.h"
 
 namespace {
@@ -233,11 +234,19 @@ struct TcArgs {
     const float2* x = nullptr;       // [site][dof][nrhs]
     float2* y = nullptr;
     const float2* w = nullptr;       // EPI 2
-    // HIN: x and w in FP16 with one FP32 scale per site (x = xh * xs[site], w = wh * ws[site])
+    // HIN: x and w in FP16 with FP32 scales, x = xh * xs[site * ssite + (rhs / 16) * shalf] (one scale
+    // per site: ssite 1, shalf 0; one per site and half of the 32 rhs: ssite 2, shalf 1), w likewise
     const __half2* xh = nullptr;
     const float* xs = nullptr;
     const __half* wh = nullptr;
     const float* ws = nullptr;
+    // HOUT: y in FP16 with one scale per site and rhs half (ys[2 site + rhs / 16], the half's largest
+    // |re| or |im|)
+    __half* yh = nullptr;
+    float* ys = nullptr;
+    int ssite = 1, shalf = 0;
+    // EPI 2: omega[rhs] = <y, w> / ||y||^2 (0 when ||y||^2 < 1e-30 or not finite), the MR step size
+    float2* omega = nullptr;
     double* partials = nullptr;
     unsigned int* tickets = nullptr;
     double* out = nullptr;
@@ -246,7 +255,7 @@ struct TcArgs {
     int nx = 0, ny = 0, nrhs = 0, H = 0;
 };
 
-template <int EPI, bool HIN = false>
+template <int EPI, bool HIN = false, bool HOUT = false>
 __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
     if (a.gate && *a.gate == 0) return;  // every right-hand side of the solve has converged
     constexpr int K = EPI == 2 ? 3 : 1;
@@ -381,7 +390,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
         auto load_w = [&](int r, int q) {
             const int64_t wi = entry(r, q);
             if (HIN) {
-                const float sq = __ldcg(a.ws + (x0 + half * kEpiSites + q) + (int64_t)nx * (y0 + r));
+                const float sq = __ldcg(a.ws + ((x0 + half * kEpiSites + q) + (int64_t)nx * (y0 + r)) * a.ssite +
+                                        (rhs >> 4) * a.shalf);
 #pragma unroll
                 for (int k = 0; k < kNc; ++k) wb[q][k] = __half2float(__ldcg(a.wh + wi + k * rstride)) * sq;
             } else {
@@ -423,8 +433,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
                     }
                 }
                 if (EPI == 2 && r + 1 < H) load_w(r + 1, q);
+                if (HOUT) {
+                    // this warp holds the (site, rhs half sub) unit: its largest |re| or |im| is the scale
+                    float mx = 0.f;
 #pragma unroll
-                for (int k = 0; k < kNc; ++k) ybase[base + k * rstride] = o[k];
+                    for (int k = 0; k < kNc; ++k) mx = fmaxf(mx, fabsf(o[k]));
+                    mx = warp_max_nonneg(mx);
+                    const float inv = mx > 0.f ? __fdividef(1.0f, mx) : 0.f;
+#pragma unroll
+                    for (int k = 0; k < kNc; ++k) a.yh[base + k * rstride] = __float2half_rn(o[k] * inv);
+                    if (lane == 0) a.ys[2 * ((x0 + i) + (int64_t)nx * (y0 + r)) + sub] = mx;
+                } else {
+#pragma unroll
+                    for (int k = 0; k < kNc; ++k) ybase[base + k * rstride] = o[k];
+                }
                 if (EPI == 1) {
                     v[0] += (double)s0;
                 } else if (EPI == 2) {
@@ -461,7 +483,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
                 const int64_t off = ((int64_t)(gx + (int64_t)nx * gy) * kNc + g * 8) * nrhs + rhs0 + r;
                 float2 e[8];
                 if (HIN) {
-                    const float sc = __ldg(a.xs + gx + (int64_t)nx * gy);
+                    const float sc = __ldg(a.xs + (gx + (int64_t)nx * gy) * a.ssite + (r >> 4) * a.shalf);
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
                         const float2 h = __half22float2(a.xh[off + (int64_t)j * nrhs]);
@@ -537,6 +559,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
                     for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
                     if (lane == 0 && p0 + q < kPairs)
                         a.out[(rhs0 + (p0 + q) / K) * K + (p0 + q) % K] = v;
+                }
+            }
+            if (EPI == 2 && a.omega) {
+                __syncthreads();  // this block's sums are in a.out
+                if (tid < kRhsTile) {
+                    const double* o3 = a.out + (int64_t)(rhs0 + tid) * K;
+                    const double den = o3[K - 1];
+                    float2 om = make_float2(0.f, 0.f);
+                    if (fabs(den) >= 1e-30 && isfinite(den)) om = make_float2((float)(o3[0] / den), (float)(o3[1] / den));
+                    a.omega[rhs0 + tid] = om;
                 }
             }
             if (tid == 0) a.tickets[blockIdx.z] = 0u;
@@ -632,10 +664,7 @@ constexpr int kCcgWred = kCcgAct + 32 * 4;          // float [12][32]
 constexpr int kCcgSmemBytes = kCcgWred + 12 * 32 * 4;
 static_assert(kCcgSmemBytes + 1024 <= 227 * 1024, "shared memory budget (persistent CG)");
 
-__device__ __forceinline__ float ccg_warp_max(float m) {
-    for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    return m;
-}
+__device__ __forceinline__ float ccg_warp_max(float m) { return warp_max_nonneg(m); }
 __device__ __forceinline__ float2 h2f(unsigned u) { return __half22float2(*reinterpret_cast<const __half2*>(&u)); }
 __device__ __forceinline__ unsigned f2h(float re, float im) {
     const __half2 h = __floats2half2_rn(re, im);
@@ -1256,6 +1285,8 @@ smg_status smg_coarse_tc_tile_links(smg_context* ctx, const cx<double>* A64, int
     SMG_CUDA(ctx, cudaFuncSetAttribute(k_coarse_apply_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes));
     SMG_CUDA(ctx, cudaFuncSetAttribute(k_coarse_apply_tc<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        kSmemBytes));
+    SMG_CUDA(ctx, cudaFuncSetAttribute(k_coarse_apply_tc<2, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       kSmemBytes));
     SMG_CUDA(ctx, cudaFuncSetAttribute(k_ccg_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kCcgSmemBytes));
     return SMG_OK;
 }
@@ -1341,6 +1372,41 @@ smg_status smg_coarse_cg_tc(smg_context* ctx, const void* links, int nx, int ny,
     void* args[] = {&a};
     SMG_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_ccg_tc, dim3(nx / kW, ny / H), dim3(kThreads), args,
                                               kCcgSmemBytes, ctx->stream));
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+// The MR step of an intermediate level on FP16 vectors with one scale per site and rhs half
+// ([site][dof][rhs] __half2, scales [site][2]): y = A x in FP16 (same format), <y, x>, ||y||^2 per rhs
+// into out[rhs * 3 + k] and omega[rhs] = <y, x> / ||y||^2
+smg_status smg_coarse_tc_apply_mr16(smg_context* ctx, const void* links, int nx, int ny, int nrhs, const void* xh,
+                                    const float* xs, void* yh, float* ys, double* out, float* omega, int* err) {
+    if (!smg_coarse_tc_shape_ok(nx, ny, kNc) || nrhs != kRhsTile || !xh || !xs || !yh || !ys || !out || !omega)
+        return smg_fail(ctx, SMG_UNSUPPORTED, "tensor-core MR apply on FP16 vectors: shape not supported");
+    const int H = rows_per_cta(nx, ny, 1);
+    const dim3 grid(nx / kW, ny / H, 1);
+    TcArgs a;
+    a.links = static_cast<const uint8_t*>(links);
+    a.xh = static_cast<const __half2*>(xh);
+    a.xs = xs;
+    a.wh = static_cast<const __half*>(xh);
+    a.ws = xs;
+    a.yh = static_cast<__half*>(yh);
+    a.ys = ys;
+    a.ssite = 2;
+    a.shalf = 1;
+    a.omega = reinterpret_cast<float2*>(omega);
+    a.err = err;
+    a.nx = nx;
+    a.ny = ny;
+    a.nrhs = nrhs;
+    a.H = H;
+    SMG_TRY(smg_reduce_reserve(ctx, (size_t)grid.x * grid.y * nrhs * 3));
+    a.partials = ctx->red.partials;
+    a.tickets = ctx->red.tickets;
+    a.out = out;
+    k_coarse_apply_tc<2, true, true><<<grid, kThreads, kSmemBytes, ctx->stream>>>(a);
     count_launch(ctx);
     SMG_CHECK_LAUNCH(ctx);
     return SMG_OK;

@@ -58,6 +58,12 @@ __device__ __forceinline__ void st_spinor_h(__half2* __restrict__ f, float* __re
     if ((threadIdx.x & (lanes - 1)) == 0) scale[q] = m;
 }
 
+// Largest of the warp's non-negative floats v in one redux.sync (the IEEE bit patterns of non-negative
+// floats order as unsigned integers); a NaN among them gives NaN.
+__device__ __forceinline__ float warp_max_nonneg(float v) {
+    return __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(v)));
+}
+
 // Two spinors per thread (right-hand sides rhs and rhs + lanes of one site), same contract as above.
 __device__ __forceinline__ void st_spinor2_h(__half2* __restrict__ f, float* __restrict__ scale, int64_t q, int rhs,
                                              int nrhs, int lanes, Spinor<float> v, Spinor<float> w, bool valid) {

@@ -54,6 +54,8 @@ smg_status smg_coarse_tc_apply(smg_context* ctx, const void* links, int nx, int 
 smg_status smg_coarse_tc_tune(smg_context* ctx, const void* links, int nx, int ny, int nrhs, const cx<float>* x,
                               cx<float>* y);
 int smg_coarse_cg_tc_rows(smg_context* ctx, int nx, int ny);
+smg_status smg_coarse_tc_apply_mr16(smg_context* ctx, const void* links, int nx, int ny, int nrhs, const void* xh,
+                                    const float* xs, void* yh, float* ys, double* out, float* omega, int* err);
 smg_status smg_coarse_cg_tc(smg_context* ctx, const void* links, int nx, int ny, const cx<float>* b, cx<float>* x,
                             void* r, float* rs, void* p0, float* ps0, void* p1, float* ps1, cx<float>* Ap,
                             double* part, int* state, int max_iter, double tol, long long spin_limit);
@@ -335,6 +337,19 @@ struct InHalf {
     __device__ __forceinline__ Spinor<float> spinor(int64_t q, int rhs, int nrhs) const {
         return ld_spinor_h(p, scale, q, rhs, nrhs);
     }
+};
+
+// coarse vectors in FP16 with one scale per site and half of the 32 rhs ([site][dof][32] __half2,
+// scales [site][2]): the intermediate-level MR smoother's residuals
+struct InHalfC {
+    const __half2* __restrict__ p;
+    const float* __restrict__ scale;
+    __device__ __forceinline__ cx<float> operator()(int64_t idx, int64_t site) const {
+        const float2 v = __half22float2(p[idx]);
+        const float s = scale[2 * site + ((idx & 31) >> 4)];
+        return mk(v.x * s, v.y * s);
+    }
+    __device__ __forceinline__ Spinor<float> spinor(int64_t, int, int) const { return Spinor<float>{}; }
 };
 
 // One block per (aggregate, tile of `lanes` right-hand sides) stages the aggregate's ne = ax ay
@@ -1081,10 +1096,7 @@ __global__ void k_ccg_p(CcgState s, VecView<T> p, const cx<T>* __restrict__ r) {
 // warp reduction; blocks of 8 warps walk the sites.
 constexpr int kCgHalfDofs = 16;
 
-__device__ __forceinline__ float warp_max(float m) {
-    for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    return m;
-}
+__device__ __forceinline__ float warp_max(float m) { return warp_max_nonneg(m); }
 __device__ __forceinline__ float absmax2(cx<float> z) { return fmaxf(fabsf(z.re), fabsf(z.im)); }
 // the 16 dofs of (site, lane) in FP16 with the site maximum m (reduced over the warp)
 __device__ __forceinline__ void st_site16(__half2* f, float* sc, int64_t e0, int site, const cx<float> (&v)[kCgHalfDofs],
@@ -1184,6 +1196,115 @@ __global__ void __launch_bounds__(256) k_ccgh_p(CcgState s, const __half2* __res
 
 }  // namespace
 
+
+// ---- the intermediate-level MR smoother on FP16 vectors (coarse_half): [site][16 dofs][32 rhs]
+// __half2 with one FP32 scale per site and rhs half.  A warp owns a (site, half) unit: lane l takes
+// rhs 16 h + l % 16 and dofs 8 (l / 16) .. + 7, so that each access instruction covers two
+// contiguous 128-byte (FP32) or 64-byte (FP16) runs and the unit's scale is a warp maximum.
+constexpr int kC16Dofs = 16;
+constexpr int kC16MaxSteps = 8;  // MR steps one x pass combines
+struct C16Unit {
+    int64_t site;
+    int h, rhs, d0;
+};
+__device__ __forceinline__ C16Unit c16_unit(int64_t u) {
+    const int lane = threadIdx.x & 31;
+    C16Unit c;
+    c.site = u >> 1;
+    c.h = (int)(u & 1);
+    c.rhs = 16 * c.h + (lane & 15);
+    c.d0 = 8 * (lane >> 4);
+    return c;
+}
+__device__ __forceinline__ int64_t c16_idx(const C16Unit& c, int j) { return (c.site * kC16Dofs + c.d0 + j) * 32 + c.rhs; }
+// stores the unit's 8 values of this lane with the unit's scale (the warp's largest |re| or |im|)
+__device__ __forceinline__ void c16_store(const C16Unit& c, const cx<float> (&v)[8], __half2* __restrict__ out,
+                                          float* __restrict__ os) {
+    float m = 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) m = fmaxf(m, fmaxf(fabsf(v[j].re), fabsf(v[j].im)));
+    m = warp_max_nonneg(m);
+    const float inv = m > 0.f ? __fdividef(1.0f, m) : 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) out[c16_idx(c, j)] = __floats2half2_rn(v[j].re * inv, v[j].im * inv);
+    if ((threadIdx.x & 31) == 0) os[2 * c.site + c.h] = m;
+}
+
+// r = b - y (y may be null: r = b), FP32 in, FP16 out; one warp per unit
+__global__ void __launch_bounds__(256) k_c16_from(const cx<float>* __restrict__ b, const cx<float>* __restrict__ y,
+                                                  __half2* __restrict__ r, float* __restrict__ rs, int nsites) {
+    const int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (u >= 2ll * nsites) return;
+    const C16Unit c = c16_unit(u);
+    cx<float> v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = b[c16_idx(c, j)];
+    if (y) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = v[j] - y[c16_idx(c, j)];
+    }
+    c16_store(c, v, r, rs);
+}
+
+// r' = r - omega Ar (all FP16), omega per rhs
+__global__ void __launch_bounds__(256) k_c16_rupdate(const __half2* __restrict__ r, const float* __restrict__ rs,
+                                                     const __half2* __restrict__ ar, const float* __restrict__ ars,
+                                                     const float2* __restrict__ omega, __half2* __restrict__ ro,
+                                                     float* __restrict__ ros, int nsites) {
+    const int64_t u = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (u >= 2ll * nsites) return;
+    const C16Unit c = c16_unit(u);
+    const float2 om = omega[c.rhs];
+    const float sr = rs[2 * c.site + c.h], sa = ars[2 * c.site + c.h];
+    __half2 rv[8], av[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        rv[j] = r[c16_idx(c, j)];
+        av[j] = ar[c16_idx(c, j)];
+    }
+    cx<float> v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const float2 a = __half22float2(rv[j]), y = __half22float2(av[j]);
+        const float yr = sa * y.x, yi = sa * y.y;
+        v[j] = mk(sr * a.x - (om.x * yr - om.y * yi), sr * a.y - (om.x * yi + om.y * yr));
+    }
+    c16_store(c, v, ro, ros);
+}
+
+// the MR residuals of one smoothing as a list of FP16 vectors
+struct C16Ring {
+    const __half2* r[kC16MaxSteps];
+    const float* s[kC16MaxSteps];
+};
+// x (+)= sum_k omega_k r_k over n FP16 residuals (omega [k][32]); x FP32 [site][dof][32]; one warp per
+// (site, dof) row of 32 rhs (lane = rhs) with every load of the row issued first
+__global__ void __launch_bounds__(256) k_c16_xupdate(cx<float>* __restrict__ x, C16Ring ring, int n,
+                                                     const float2* __restrict__ omega, int nsites, int zero) {
+    const int lane = threadIdx.x & 31;
+    const int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (e >= (int64_t)nsites * kC16Dofs) return;
+    const int64_t i = e * 32 + lane, site = e / kC16Dofs;
+    __half2 rv[kC16MaxSteps];
+    float sc[kC16MaxSteps];
+    float2 om[kC16MaxSteps];
+#pragma unroll
+    for (int k = 0; k < kC16MaxSteps; ++k)
+        if (k < n) {
+            rv[k] = ring.r[k][i];
+            sc[k] = ring.s[k][2 * site + (lane >> 4)];
+            om[k] = omega[k * 32 + lane];
+        }
+    cx<float> acc = zero ? mk(0.f, 0.f) : x[i];
+#pragma unroll
+    for (int k = 0; k < kC16MaxSteps; ++k)
+        if (k < n) {
+            const float2 a = __half22float2(rv[k]);
+            const float ar = sc[k] * a.x, ai = sc[k] * a.y;
+            acc = mk(acc.re + om[k].x * ar - om[k].y * ai, acc.im + om[k].x * ai + om[k].y * ar);
+        }
+    x[i] = acc;
+}
 // ====================================================================== host
 
 struct CoarseWork {  // per level l >= 1, per precision
@@ -1204,6 +1325,16 @@ struct CoarseWork {  // per level l >= 1, per precision
     void* ph2 = nullptr;
     float* ps2 = nullptr;
     double* ccg_part = nullptr;
+    // intermediate level with coarse_half: the MR residuals r_0 .. r_n of one smoothing and A r in
+    // FP16 (scales per site and rhs half), the steps' MR scalars [step][rhs][3] and step sizes
+    // [step][rhs], and the ring slot of the last smoothing's final residual
+    std::vector<void*> r16;
+    std::vector<float*> r16s;
+    void* ar16 = nullptr;
+    float* ar16s = nullptr;
+    double* mr16_sc = nullptr;
+    float* mr16_om = nullptr;
+    int res16 = -1;
 };
 
 struct smg_mg {
@@ -1457,8 +1588,10 @@ smg_status free_work(smg_mg* mg) {
     mg->mr_omf = nullptr;
     for (auto& w : mg->cw) {
         for (void* p : {w.b, w.x, w.r, w.Ar, w.e, w.p, w.rh, w.ph, (void*)w.rs, (void*)w.ps, w.ph2, (void*)w.ps2,
-                        (void*)w.ccg_part})
+                        (void*)w.ccg_part, w.ar16, (void*)w.ar16s, (void*)w.mr16_sc, (void*)w.mr16_om})
             if (p) cudaFree(p);
+        for (void* p : w.r16) cudaFree(p);
+        for (float* p : w.r16s) cudaFree(p);
     }
     mg->cw.clear();
     if (mg->scal) cudaFree(mg->scal);
@@ -1520,6 +1653,14 @@ smg_status coarse_cg_persistent(smg_mg* mg, int l, void* x, const void* b) {
 bool coarse_half_level(const smg_mg* mg, int l, int nrhs, smg_precision prec) {
     return mg->p.coarse_half && prec == SMG_F32 && l == (int)mg->lv.size() - 1 && nrhs == 32 &&
            mg->lv[l].ndof == 16 && tc_path(mg, l, nrhs);
+}
+
+// an intermediate level of a coarse_half hierarchy smooths with MR on FP16 vectors (the tensor-core
+// apply reading and writing them) when its smoother is MR and the cycle has 32 right-hand sides
+bool mr16_level(const smg_mg* mg, int l, int nrhs, smg_precision prec) {
+    return mg->p.coarse_half && prec == SMG_F32 && l >= 1 && l < (int)mg->lv.size() - 1 && nrhs == 32 &&
+           mg->lv[l].ndof == 16 && tc_path(mg, l, nrhs) && !(mg->lv[l].rich_omega > 0) &&
+           std::max(mg->p.pre_smooth, mg->p.post_smooth) <= kC16MaxSteps;
 }
 
 // the coarsest CG of a coarse_half level runs as one persistent cooperative launch (k_ccg_tc) when the
@@ -1589,6 +1730,21 @@ smg_status ensure_work(smg_mg* mg, int nrhs, smg_precision prec) {
                 const size_t nblk = (size_t)(Lc.nx / 8) * (Lc.ny / smg_coarse_cg_tc_rows(ctx, Lc.nx, Lc.ny));
                 SMG_CUDA(ctx, cudaMalloc((void**)&w.ccg_part, 64 * nblk * sizeof(double)));
             }
+        }
+        if (mr16_level(mg, (int)l, nrhs, prec)) {
+            const size_t hb = (size_t)mg->lv[l].nsites * nrhs * mg->lv[l].ndof * sizeof(__half2);
+            const size_t sb = (size_t)mg->lv[l].nsites * 2 * sizeof(float);
+            const int nsteps = std::max(1, std::max(mg->p.pre_smooth, mg->p.post_smooth));
+            w.r16.assign(nsteps + 1, nullptr);
+            w.r16s.assign(nsteps + 1, nullptr);
+            for (int k = 0; k <= nsteps; ++k) {
+                SMG_CUDA(ctx, cudaMalloc(&w.r16[k], hb));
+                SMG_CUDA(ctx, cudaMalloc((void**)&w.r16s[k], sb));
+            }
+            SMG_CUDA(ctx, cudaMalloc(&w.ar16, hb));
+            SMG_CUDA(ctx, cudaMalloc((void**)&w.ar16s, sb));
+            SMG_CUDA(ctx, cudaMalloc((void**)&w.mr16_sc, (size_t)nsteps * nrhs * 3 * sizeof(double)));
+            SMG_CUDA(ctx, cudaMalloc((void**)&w.mr16_om, (size_t)nsteps * nrhs * sizeof(float2)));
         }
     }
     if (!mg->cg_state) {
@@ -1927,9 +2083,86 @@ smg_status smooth_fine(smg_mg* mg, smg_field* x, const smg_field* b, int niter, 
     return SMG_OK;
 }
 
+// Coarse MR (mr_smooth_op, src/smoother.cpp:26-40) on FP16 work vectors (mr16_level): r_0 = b - A x
+// (or b) in FP16, then per step A r_k in FP16 with <A r_k, r_k>, ||A r_k||^2 and omega_k from the
+// tensor-core apply, r_{k+1} = r_k - omega_k A r_k, and x += sum_k omega_k r_k once at the end (x and
+// all arithmetic FP32).  The final residual stays in the ring slot res16 for the restriction.
+smg_status mr_coarse_half(smg_mg* mg, int l, void* x, const void* b, int niter, bool x_is_zero) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[l];
+    CoarseWork& w = mg->cw[l];
+    const int nrhs = mg->work_nrhs;
+    const int ugrid = (int)((2ll * L.nsites + 7) / 8);  // one warp per (site, rhs half), 8 warps per block
+    const cx<float>* y = nullptr;
+    if (!x_is_zero) {
+        SMG_TRY(coarse_apply<float>(mg, l, cview<float>(x, L, nrhs), (cx<float>*)w.Ar, 0, nullptr, nullptr));
+        y = (const cx<float>*)w.Ar;
+    }
+    k_c16_from<<<ugrid, 256, 0, ctx->stream>>>((const cx<float>*)b, y, (__half2*)w.r16[0], w.r16s[0], L.nsites);
+    count_launch(ctx);
+    for (int it = 0; it < niter; ++it) {
+        double* sc = w.mr16_sc + (size_t)it * nrhs * 3;
+        float* om = w.mr16_om + (size_t)it * nrhs * 2;
+        SMG_TRY(smg_coarse_tc_apply_mr16(ctx, L.Atc, L.nx, L.ny, nrhs, w.r16[it], w.r16s[it], w.ar16, w.ar16s, sc, om,
+                                         device_err(mg)));
+        k_c16_rupdate<<<ugrid, 256, 0, ctx->stream>>>((const __half2*)w.r16[it], w.r16s[it], (const __half2*)w.ar16,
+                                                      w.ar16s, (const float2*)om, (__half2*)w.r16[it + 1],
+                                                      w.r16s[it + 1], L.nsites);
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+    }
+    if (niter > 0) {
+        C16Ring ring{};
+        for (int k = 0; k < niter; ++k) {
+            ring.r[k] = (const __half2*)w.r16[k];
+            ring.s[k] = w.r16s[k];
+        }
+        const int64_t rows = (int64_t)L.nsites * kC16Dofs;
+        k_c16_xupdate<<<(unsigned)((rows + 7) / 8), 256, 0, ctx->stream>>>((cx<float>*)x, ring, niter, (const float2*)w.mr16_om, L.nsites,
+                                                      x_is_zero ? 1 : 0);
+        count_launch(ctx);
+    } else if (x_is_zero) {
+        SMG_CUDA(ctx, cudaMemsetAsync(x, 0, (size_t)L.nsites * nrhs * L.ndof * sizeof(cx<float>), ctx->stream));
+    }
+    w.res16 = niter;
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+// restriction of an intermediate level's FP16 residual (k_restrict_agg with the InHalfC reader)
+smg_status restrict_c16(smg_mg* mg, int l, void* out) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[l];
+    const Level& N = mg->lv[l + 1];
+    CoarseWork& w = mg->cw[l];
+    const int nrhs = mg->work_nrhs;
+    const int nc = L.nc_next;
+    if (nc != 8 && nc != 16 && nc != 32) return smg_fail(ctx, SMG_UNSUPPORTED, "FP16 restriction: coarse dofs");
+    TransferGeom t = transfer_geom(mg, l, nrhs);
+    const dim3 block = transfer_block(nrhs);
+    const dim3 grid(N.nsites, (nrhs + block.x - 1) / block.x);
+    const size_t sm = transfer_smem<float>(L, (int)block.x, true);
+    const InHalfC in{(const __half2*)w.r16[w.res16], w.r16s[w.res16]};
+#define SMG_RC(NC)                                                                                           \
+    do {                                                                                                     \
+        static std::once_flag once;                                                                          \
+        transfer_smem_attr(k_restrict_agg<float, NC, InHalfC>, sm, once);                                    \
+        k_restrict_agg<float, NC, InHalfC><<<grid, block, sm, ctx->stream>>>(L.V32, in, (cx<float>*)out, t); \
+    } while (0)
+    if (nc == 8) SMG_RC(8);
+    else if (nc == 16) SMG_RC(16);
+    else SMG_RC(32);
+#undef SMG_RC
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
 template <typename T>
 smg_status smooth_coarse(smg_mg* mg, int l, void* x, const void* b, int niter, bool x_is_zero) {
     const double om = mg->lv[l].rich_omega;
+    if (std::is_same<T, float>::value && !mg->cw[l].r16.empty() && mr16_level(mg, l, mg->work_nrhs, SMG_F32))
+        return mr_coarse_half(mg, l, x, b, niter, x_is_zero);
     if (!(om > 0)) return mr_coarse<T>(mg, l, x, b, niter, x_is_zero);
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[l];
@@ -2190,9 +2423,12 @@ smg_status cycle_coarse(smg_mg* mg, int l, void* x, const void* b) {
     const Level& L = mg->lv[l];
     const int nrhs = mg->work_nrhs;
     SMG_TRY(smooth_coarse<T>(mg, l, x, b, mg->p.pre_smooth, true));
-    // residual of the smoothed x is in cw[l].r
+    // residual of the smoothed x is in cw[l].r (or, FP16, in the ring slot cw[l].res16)
     CoarseWork& nw = mg->cw[l + 1];
-    SMG_TRY(restrict_to<T>(mg, l, mg->cw[l].r, nw.b));
+    if (std::is_same<T, float>::value && !mg->cw[l].r16.empty() && mr16_level(mg, l, nrhs, SMG_F32))
+        SMG_TRY(restrict_c16(mg, l, nw.b));
+    else
+        SMG_TRY(restrict_to<T>(mg, l, mg->cw[l].r, nw.b));
     SMG_TRY(cycle_coarse<T>(mg, l + 1, nw.x, nw.b));
     if (mg->p.w_cycle && l + 1 < last) {
         const Level& N = mg->lv[l + 1];
