@@ -39,11 +39,13 @@
 //     FP32 vector [site][dof][rhs] layout into BF16 A tiles by four stager
 //     warps and kept in a ring of four rows (output row y reads source rows
 //     y-1, y, y+1);
-//   * warp 0 issues the link copies, warp 1 the MMAs, warps 4, 5 and 8, 9
-//     read the accumulators (TMEM lanes 0..63, one 256-column slot per output
-//     row, two slots; the two pairs share the lane groups and split a row's
-//     sites) and write y, with the fused per-rhs reductions ||y||^2 and
-//     <y, w> of the FP32 kernels; warps 10 and 11 only join the final barrier.
+//   * warp 10 issues the link copies, warp 11 the MMAs; the warp pairs (0, 1),
+//     (4, 5), (8, 9) read the accumulators (TMEM lanes 0..63, which only warps
+//     with warp % 4 = 0 or 1 may access; one 256-column slot per output row,
+//     two slots), each pair a third of a row's sites, and write y with the
+//     fused per-rhs reductions ||y||^2 and <y, w> of the FP32 kernels.  The
+//     epilogue bounds the row rate, and the accumulator lanes tie it to two of
+//     the SM's four schedulers, so it gets three warps on each of them.
 // Every mbarrier wait is bounded (about one second of SM clock); on timeout
 // the CTA raises *err = 2, waits (bounded) for its own bulk copies and MMAs,
 // frees its tensor memory and returns.
@@ -90,10 +92,15 @@ constexpr int kNumBars = kBarFinal + 1;
 constexpr int kBarOffset = kRingBytes + kLinkBytes;           // A-tile over-read (M = 128) lands in the link ring
 constexpr int kMiscOffset = kBarOffset + kNumBars * 8;
 constexpr int kThreads = 384;                                 // 12 warps (roles below)
-constexpr int kEpiHalves = 2;                                 // epilogue warp pairs, each half a row
-constexpr int kEpiSites = kW / kEpiHalves;                    // output sites per pair and row
+constexpr int kEpiHalves = 2;                                 // persistent CG: epilogue warp pairs
+constexpr int kEpiSites = kW / kEpiHalves;                    // persistent CG: output sites per pair and row
+// the apply: three epilogue warp pairs (0, 1), (4, 5), (8, 9) take output sites 0-2, 3-5, 6-7 of a row;
+// the link producer and the MMA issuer are warps 10 and 11
+constexpr int kApGroups = 3;
+constexpr int kApSitesMax = 3;
+constexpr int kProdWarp = 10, kMmaWarp = 11;
 constexpr int kRedOffset = (kMiscOffset + 16 + 15) / 16 * 16;  // [half][32 rhs][3] doubles
-constexpr int kSmemBytes = kRedOffset + kEpiHalves * kRhsTile * 3 * 8;
+constexpr int kSmemBytes = kRedOffset + kApGroups * kRhsTile * 3 * 8;
 static_assert(kSmemBytes + 1024 <= 227 * 1024, "shared memory budget");
 static_assert(kTileA % 16 == 0 && kRowBytes % 16 == 0 && kUnitBytes % 16 == 0, "16-byte alignment");
 static_assert(2 * kAccCols <= kTmemCols, "tensor memory budget");
@@ -282,7 +289,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
         }
         for (int i = 0; i < 2; ++i) {
             mbar_init(bar(kBarAccFull + i), 1);
-            mbar_init(bar(kBarAccEmpty + i), 32 * 2 * kEpiHalves);
+            mbar_init(bar(kBarAccEmpty + i), 32 * 2 * kApGroups);
         }
         mbar_init(bar(kBarFinal), 1);
         misc[1] = 0;
@@ -300,7 +307,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
     tc_fence_after();
     const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(misc);
 
-    if (warp == 0) {
+    if (warp == kProdWarp) {
         // ---------------- link producer: per output row and dy one run of kRunBlocks blocks
         if (lane == 0) {
             const int ring3 = 3 * nx;  // blocks per (output row, dy) on the lattice
@@ -326,7 +333,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
                 drain_bar(bar(kBarUnitFull + u % kUnits), (u / kUnits) & 1);
         }
         __syncwarp();
-    } else if (warp == 1) {
+    } else if (warp == kMmaWarp) {
         // ---------------- MMA issuer: per output row, 3 dy x 10 source groups
         if (lane == 0) {
             bool ok = true;
@@ -366,11 +373,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
             drain_bar(bar(kBarFinal), 0);
         }
         __syncwarp();
-    } else if (warp == 4 || warp == 5 || warp == 8 || warp == 9) {
-        // ---------------- epilogue: TMEM lanes 0..63 hold the 64 useful rows; warps 4, 5 take the
-        // first kEpiSites sites of a row and warps 8, 9 (the same lane groups) the others
-        const int half = warp >= 8 ? 1 : 0;
-        const int sub = warp - (half ? 8 : 4);
+    } else if ((warp & 3) < 2) {
+        // ---------------- epilogue: TMEM lanes 0..63 hold the 64 useful rows and only warps with
+        // warp % 4 = 0 (lanes 0-31) or 1 (lanes 32-63) may read them: the pairs (0, 1), (4, 5), (8, 9)
+        // take sites 0-2, 3-5 and 6-7 of every output row
+        const int half = warp >> 2;  // the pair's group
+        const int sub = warp & 1;
+        const int sbase = kApSitesMax * half, nsq = half < 2 ? kApSitesMax : kW - 2 * kApSitesMax;
         const int m = 32 * sub + lane;
         const int rhs = m >> 1, c = m & 1;
         double v[K];
@@ -381,16 +390,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
         float* __restrict__ ybase = reinterpret_cast<float*>(a.y);
         // first entry of this thread's (rhs, re/im) for site q of the pair's half of output row r
         auto entry = [&](int r, int q) {
-            return (((int64_t)x0 + half * kEpiSites + q + (int64_t)nx * (y0 + r)) * kNc * nrhs + rhs0 + rhs) * 2 + c;
+            return (((int64_t)x0 + sbase + q + (int64_t)nx * (y0 + r)) * kNc * nrhs + rhs0 + rhs) * 2 + c;
         };
         // EPI 2: w of site q of row r into wb[q].  Software-pipelined: row 0 is requested before the
         // first accumulator wait, row r + 1's site q right after row r's site q has used wb[q], so the
         // loads have a whole row of epilogue work to land instead of stalling every row
-        float wb[kEpiSites][kNc];
+        float wb[kApSitesMax][kNc];
         auto load_w = [&](int r, int q) {
             const int64_t wi = entry(r, q);
             if (HIN) {
-                const float sq = __ldcg(a.ws + ((x0 + half * kEpiSites + q) + (int64_t)nx * (y0 + r)) * a.ssite +
+                const float sq = __ldcg(a.ws + ((x0 + sbase + q) + (int64_t)nx * (y0 + r)) * a.ssite +
                                         (rhs >> 4) * a.shalf);
 #pragma unroll
                 for (int k = 0; k < kNc; ++k) wb[q][k] = __half2float(__ldcg(a.wh + wi + k * rstride)) * sq;
@@ -401,15 +410,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
         };
         if (EPI == 2) {
 #pragma unroll
-            for (int q = 0; q < kEpiSites; ++q) load_w(0, q);
+            for (int q = 0; q < kApSitesMax; ++q)
+                if (q < nsq) load_w(0, q);
         }
         for (int r = 0; r < H; ++r) {
             bool ok = wait_bar(bar(kBarAccFull + (r & 1)), (r >> 1) & 1, abort_flag);
             if (!__all_sync(0xffffffffu, ok)) break;
             tc_fence_after();
 #pragma unroll
-            for (int q = 0; q < kEpiSites; ++q) {
-                const int i = half * kEpiSites + q;
+            for (int q = 0; q < kApSitesMax; ++q) {
+                if (q >= nsq) break;
+                const int i = sbase + q;
                 float d[32];
                 tmem_ld32(tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)((r & 1) * kAccCols + 32 * i), d);
                 const int64_t base = entry(r, q);
@@ -465,7 +476,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
 #pragma unroll
                 for (int k = 0; k < K; ++k) red[(half * kRhsTile + rhs) * K + k] = v[k];
         }
-    } else if (warp == 2 || warp == 3 || warp == 6 || warp == 7) {
+    } else if (warp < kProdWarp) {
         // ---------------- stagers (warps 2, 3, 6, 7): FP32 source rows -> BF16 A tiles
         const int st = (warp < 4 ? warp - 2 : warp - 4) * 32 + lane;  // 0..127
         for (int lr = 0; lr < H + 2; ++lr) {
@@ -529,7 +540,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
 #pragma unroll
             for (int k = 0; k < K; ++k)
                 a.partials[((int64_t)(rhs0 + tid) * K + k) * nblk + blin] =
-                    aborted ? 0.0 : red[tid * K + k] + red[(kRhsTile + tid) * K + k];
+                    aborted ? 0.0
+                            : (red[tid * K + k] + red[(kRhsTile + tid) * K + k]) + red[(2 * kRhsTile + tid) * K + k];
         }
         __threadfence();
         __syncthreads();
