@@ -654,7 +654,7 @@ struct CcgTcArgs {
     __half2* p[2] = {nullptr, nullptr};  // search directions (FP16, dof-inner), p_k in p[k & 1]
     float* ps[2] = {nullptr, nullptr};
     float2* Ap = nullptr;                // A p_k (FP32, [site][dof][32])
-    double* part = nullptr;              // [2][32][nblk] per-CTA partial sums
+    double* part = nullptr;              // storage of the [2][32][nblk] FP32 per-CTA partial sums
     unsigned int* bar = nullptr;         // grid barrier: [0] arrivals, [1] generation
     int* err = nullptr;                  // 1 grid-barrier timeout, 2 mbarrier timeout
     int* iters = nullptr;                // iterations done (CTA 0)
@@ -666,10 +666,10 @@ struct CcgTcArgs {
 constexpr int kCcgMaxCtas = 160;                    // partial sums: five loads per lane and rhs
 // extra shared memory of the persistent CG after the apply's: scalars and reduction rows
 constexpr int kCcgOffset = (kSmemBytes + 15) / 16 * 16;
-constexpr int kCcgRr = kCcgOffset;                  // double [32]
-constexpr int kCcgBn = kCcgRr + 32 * 8;             // double [32]
-constexpr int kCcgSum = kCcgBn + 32 * 8;            // double [32]: the last grid-wide sums
-constexpr int kCcgAlpha = kCcgSum + 32 * 8;         // float [32]
+constexpr int kCcgRr = kCcgOffset;                  // float [32]
+constexpr int kCcgBn = kCcgRr + 32 * 4;             // float [32]
+constexpr int kCcgSum = kCcgBn + 32 * 4;            // float [32]: the last grid-wide sums
+constexpr int kCcgAlpha = kCcgSum + 32 * 4;         // float [32]
 constexpr int kCcgBeta = kCcgAlpha + 32 * 4;        // float [32]
 constexpr int kCcgAct = kCcgBeta + 32 * 4;          // int [32]
 constexpr int kCcgWred = kCcgAct + 32 * 4;          // float [12][32]
@@ -733,23 +733,24 @@ __device__ __forceinline__ bool ccg_grid_barrier(unsigned int* bar, int* err, lo
 
 // out32[j] = sum over the grid's CTAs of part[j][cta] for the 32 rhs: warp w takes rhs w, w + 12,
 // w + 24 with all its loads issued first, lanes stride the CTAs, then a fixed shuffle tree (the same
-// order in every CTA)
-__device__ __forceinline__ void ccg_sum_partials(const double* part, int nblk, double* out32) {
+// order in every CTA).  The CG's scalars are FP32: the coarsest solve runs to a tolerance of a few
+// per cent, and FP64 arithmetic, scarce on this part, put microseconds of latency on every sum.
+__device__ __forceinline__ void ccg_sum_partials(const float* part, int nblk, float* out32) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double v[3][5];
+    float v[3][5];
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
         const int j = warp + (kThreads / 32) * q;
 #pragma unroll
         for (int u = 0; u < 5; ++u) {
             const int c = lane + 32 * u;
-            v[q][u] = (j < 32 && c < nblk) ? __ldcg(part + (int64_t)j * nblk + c) : 0.0;
+            v[q][u] = (j < 32 && c < nblk) ? __ldcg(part + (int64_t)j * nblk + c) : 0.f;
         }
     }
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
         const int j = warp + (kThreads / 32) * q;
-        double s = ((v[q][0] + v[q][1]) + (v[q][2] + v[q][3])) + v[q][4];
+        float s = ((v[q][0] + v[q][1]) + (v[q][2] + v[q][3])) + v[q][4];
         for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (lane == 0 && j < 32) out32[j] = s;
     }
@@ -757,7 +758,7 @@ __device__ __forceinline__ void ccg_sum_partials(const double* part, int nblk, d
 
 // this CTA's per-rhs partial part[rhs][blin] from the lanes' unit sums acc[h] (rhs 16 h + lane / 2,
 // the two lanes of an rhs already combined; lanes with odd index hold copies)
-__device__ __forceinline__ void ccg_publish(float* s_wred, const float (&acc)[2], double* part, int nblk, int blin) {
+__device__ __forceinline__ void ccg_publish(float* s_wred, const float (&acc)[2], float* part, int nblk, int blin) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if ((lane & 1) == 0) {
         s_wred[warp * 32 + (lane >> 1)] = acc[0];
@@ -765,8 +766,9 @@ __device__ __forceinline__ void ccg_publish(float* s_wred, const float (&acc)[2]
     }
     __syncthreads();
     if (threadIdx.x < 32) {
-        double t = 0.0;
-        for (int w = 0; w < kThreads / 32; ++w) t += (double)s_wred[w * 32 + threadIdx.x];
+        float t = 0.f;
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; ++w) t += s_wred[w * 32 + threadIdx.x];
         part[(int64_t)threadIdx.x * nblk + blin] = t;
     }
 }
@@ -803,17 +805,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
     const uint32_t link_a = ring_a + kRingBytes;
     const uint32_t bar_a = ring_a + kBarOffset;
     int* misc = reinterpret_cast<int*>(smem + kMiscOffset);  // [0] TMEM base, [1] abort flag
-    double* s_rr = reinterpret_cast<double*>(smem + kCcgRr);
-    double* s_bn = reinterpret_cast<double*>(smem + kCcgBn);
-    double* s_sum = reinterpret_cast<double*>(smem + kCcgSum);
+    float* s_rr = reinterpret_cast<float*>(smem + kCcgRr);
+    float* s_bn = reinterpret_cast<float*>(smem + kCcgBn);
+    float* s_sum = reinterpret_cast<float*>(smem + kCcgSum);
     float* s_alpha = reinterpret_cast<float*>(smem + kCcgAlpha);
     float* s_beta = reinterpret_cast<float*>(smem + kCcgBeta);
     int* s_act = reinterpret_cast<int*>(smem + kCcgAct);
     float* s_wred = reinterpret_cast<float*>(smem + kCcgWred);
     volatile int* abort_flag = misc + 1;
     auto bar = [&](int i) { return bar_a + 8u * (uint32_t)i; };
-    double* part1 = a.part;                        // <A p, p> partials
-    double* part2 = a.part + (int64_t)32 * nblk;  // ||r||^2 partials
+    float* part1 = reinterpret_cast<float*>(a.part);  // <A p, p> partials
+    float* part2 = part1 + (int64_t)32 * nblk;         // ||r||^2 partials
     // unit u: own site u / 2 of the strip, rhs half u & 1; this lane's rhs and dof half
     const int lrhs = lane >> 1, dh = lane & 1;
     auto unit_site = [&](int u) {
@@ -894,12 +896,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
         ccg_sum_partials(part2, nblk, s_sum);
         __syncthreads();
         if (tid < 32) {
-            const double rr = s_sum[tid];
+            const float rr = s_sum[tid];
             s_rr[tid] = rr;
             s_bn[tid] = rr;
             s_beta[tid] = 0.f;
-            int act = (rr >= 1e-60 && isfinite(rr)) ? 1 : 0;
-            if (act && rr < a.tol2 * rr) act = 0;
+            int act = (rr >= 1e-30f && isfinite(rr)) ? 1 : 0;
+            if (act && rr < (float)a.tol2 * rr) act = 0;
             s_act[tid] = act;
         }
     }
@@ -983,7 +985,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
             const int st = (warp < 4 ? warp - 2 : warp - 4) * 32 + lane;
             constexpr int kItems = kSrcSites * 32 * 4;
             constexpr int kPer = kItems / 128;  // 10
-            constexpr int kBatch = 5;
+            constexpr int kBatch = 10;
             for (int lr = 0; lr < H + 2; ++lr) {
                 const int S = sb + lr, slot = S % kRing, use = S / kRing;
                 if (use > 0 && !wait_bar(bar(kBarSrcEmpty + slot), (use - 1) & 1, abort_flag)) break;
@@ -1151,8 +1153,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
         __syncthreads();
         if (tid < 32) {
             float al = 0.f;
-            const double pap = s_sum[tid];
-            if (s_act[tid] && fabs(pap) >= 1e-30 && isfinite(pap)) al = (float)(s_rr[tid] / pap);
+            const float pap = s_sum[tid];
+            if (s_act[tid] && fabsf(pap) >= 1e-30f && isfinite(pap)) al = s_rr[tid] / pap;
             s_alpha[tid] = al;
         }
         __syncthreads();
@@ -1226,13 +1228,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
         ccg_sum_partials(part2, nblk, s_sum);
         __syncthreads();
         if (tid < 32) {
-            const double rr_new = s_sum[tid];
+            const float rr_new = s_sum[tid];
             float be = 0.f;
             if (s_act[tid]) {
-                if (!isfinite(rr_new) || rr_new < a.tol2 * s_bn[tid]) {
+                if (!isfinite(rr_new) || rr_new < (float)a.tol2 * s_bn[tid]) {
                     s_act[tid] = 0;
                 } else {
-                    be = (float)(rr_new / s_rr[tid]);
+                    be = rr_new / s_rr[tid];
                     s_rr[tid] = rr_new;
                 }
             }
