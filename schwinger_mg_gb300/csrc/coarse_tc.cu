@@ -1073,16 +1073,34 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                     if (lane == 0) __stcg(psnew + 2 * site + h, mx);
                 }
             }
+            // the six warps' own p_k is complete before the epilogue reads it back (named barrier 1:
+            // warps 10, 11 arrive, the epilogue warps wait)
+            if (warp <= 9) asm volatile("bar.sync 1, 192;" ::: "memory");
+            else asm volatile("bar.arrive 1, 192;" ::: "memory");
             if (warp <= 9) {
-                // epilogue: A p_k of the own sites to global memory
+                // epilogue: A p_k of the own sites to global memory and <A p_k, p_k> per rhs (p_k of
+                // the row's sites requested before the row's accumulator wait)
                 const int half = warp >= 8 ? 1 : 0;
                 const int sub = warp - (half ? 8 : 4);
                 const int m = 32 * sub + lane;
                 const int rhs = m >> 1, c = m & 1;
                 const int64_t rstride = 2ll * nrhs;
                 float* __restrict__ ybase = reinterpret_cast<float*>(a.Ap);
+                float dot = 0.f;
+                // p_k of site q of row r (16 dofs of this lane's rhs: four 16-byte words) and its scale
+                auto load_p = [&](int r, int q, uint4 (&w)[4], float& sc) {
+                    const int64_t site = (int64_t)x0 + half * kEpiSites + q + (int64_t)nx * (y0 + r);
+                    const uint4* pp = h16_ptr(pnew, site, rhs);
+#pragma unroll
+                    for (int w4 = 0; w4 < 4; ++w4) w[w4] = __ldcg(pp + w4);
+                    sc = __ldcg(psnew + 2 * site + (rhs >> 4));
+                };
                 for (int r = 0; r < H; ++r) {
                     const int R = ab + r;
+                    uint4 pw[2][4];  // sites q and q + 1 in flight
+                    float psq[2];
+                    load_p(r, 0, pw[0], psq[0]);
+                    load_p(r, 1, pw[1], psq[1]);
                     const bool eok = wait_bar(bar(kBarAccFull + (R & 1)), (R >> 1) & 1, abort_flag);
                     if (!__all_sync(0xffffffffu, eok)) break;
                     tc_fence_after();
@@ -1092,15 +1110,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                         float d[32];
                         tmem_ld32(tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)((R & 1) * kAccCols + 32 * i), d);
                         const int64_t base = (((int64_t)x0 + i + (int64_t)nx * (y0 + r)) * kNc * nrhs + rhs) * 2 + c;
+                        float t = 0.f;
 #pragma unroll
                         for (int kk = 0; kk < kNc; ++kk) {
                             const float other = __shfl_xor_sync(0xffffffffu, d[16 + kk], 1);
-                            __stcg(ybase + base + kk * rstride, c == 0 ? d[kk] - other : d[kk] + other);
+                            const float y = c == 0 ? d[kk] - other : d[kk] + other;
+                            __stcg(ybase + base + kk * rstride, y);
+                            const float2 p2 = h2f(word_of(pw[q & 1][kk >> 2], kk & 3));
+                            t += y * (c == 0 ? p2.x : p2.y);
                         }
+                        dot += psq[q & 1] * t;
+                        if (q + 2 < kEpiSites) load_p(r, q + 2, pw[q & 1], psq[q & 1]);
                     }
                     tc_fence_before();
                     mbar_arrive(bar(kBarAccEmpty + (R & 1)));
                 }
+                // Re <A p, p> of this warp's 16 rhs: the two lanes of an rhs combined
+                dot += __shfl_xor_sync(0xffffffffu, dot, 1);
+                if (c == 0) reinterpret_cast<float*>(smem + kRedOffset)[half * kRhsTile + rhs] = dot;
             }
         }
         tc_fence_before();
@@ -1110,42 +1137,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
             if (tid == 0) atomicCAS(a.err, 0, 2);
             break;
         }
-        // ================= <A p_k, p_k> of the own sites per rhs: three units per step, loads first
-        {
-            float acc[2] = {0.f, 0.f};
-            constexpr int kW32 = kThreads / 32;
-            for (int u0 = warp; u0 < nunit; u0 += 3 * kW32) {
-                uint4 pw[3][2];
-                float2 av[3][8];
-                float sp[3];
-#pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    const int u = u0 + q * kW32 < nunit ? u0 + q * kW32 : u0;
-                    const int64_t site = unit_site(u);
-                    const int h = u & 1, rhs = 16 * h + lrhs;
-                    const int64_t e0 = e_of(site, rhs);
-                    const uint4* pp = h16_ptr(pnew, site, rhs) + 2 * dh;
-                    pw[q][0] = __ldcg(pp);
-                    pw[q][1] = __ldcg(pp + 1);
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) av[q][j] = __ldcg(a.Ap + e0 + j * nrhs);
-                    sp[q] = __ldcg(psnew + 2 * site + h);
-                }
-#pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    const int u = u0 + q * kW32;
-                    if (u >= nunit) break;
-                    float2 pv[8];
-                    h8_unpack(pw[q][0], pw[q][1], sp[q], pv);
-                    float t = 0.f;
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) t += av[q][j].x * pv[j].x + av[q][j].y * pv[j].y;  // Re <A p, p>
-                    const float v = t + __shfl_xor_sync(0xffffffffu, t, 1);
-                    if (u & 1) acc[1] += v;
-                    else acc[0] += v;
-                }
-            }
-            ccg_publish(s_wred, acc, part1, nblk, blin);
+        // ================= <A p_k, p_k>: the epilogue's per-warp sums as this CTA's partials
+        if (tid < 32) {
+            const float* ed = reinterpret_cast<const float*>(smem + kRedOffset);
+            part1[(int64_t)tid * nblk + blin] = ed[tid] + ed[kRhsTile + tid];
         }
         ok = ccg_grid_barrier(a.bar, a.err, a.spin_limit);
         if (!ok) break;
