@@ -387,6 +387,30 @@ __global__ void __launch_bounds__(256) k_restrict_agg(const cx<T>* __restrict__ 
     for (int k = threadIdx.y * lanes + threadIdx.x; k < ne * NC; k += lanes * rows) s_v[k] = Vb[k];
     __syncthreads();
     if (!live) return;
+    if (NC == 2 * rows) {
+        // two adjacent outputs per thread: one shared-memory read of the input per entry serves both,
+        // and the two block-vector values are one 2 x 8-byte read
+        const int i0 = 2 * threadIdx.y;
+        cx<T> a0 = mk<T>(0, 0), a1 = mk<T>(0, 0);
+#pragma unroll 8
+        for (int e = 0; e < ne; ++e) {
+            const cx<T> f = s_f[e * lanes + threadIdx.x];
+            cx<T> v0, v1;
+            if constexpr (std::is_same<T, float>::value) {  // s_v is 16-byte aligned, i0 even
+                const float4 w = *reinterpret_cast<const float4*>(s_v + e * NC + i0);
+                v0 = mk(w.x, w.y);
+                v1 = mk(w.z, w.w);
+            } else {
+                v0 = s_v[e * NC + i0];
+                v1 = s_v[e * NC + i0 + 1];
+            }
+            a0 = a0 + cmulc(v0, f);
+            a1 = a1 + cmulc(v1, f);
+        }
+        out[((int64_t)B * NC + i0) * nrhs + rhs] = a0;
+        out[((int64_t)B * NC + i0 + 1) * nrhs + rhs] = a1;
+        return;
+    }
     for (int i = threadIdx.y; i < NC; i += rows) {
         cx<T> acc = mk<T>(0, 0);
 #pragma unroll 8
