@@ -437,9 +437,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_coarse_apply_tc(TcArgs a) {
                         s0 += o[k] * o[k];
                     } else if (EPI == 2) {
                         const float wc = wb[q][k];
-                        const float wo = __shfl_xor_sync(0xffffffffu, wc, 1);
-                        s0 += o[k] * wc;                     // Re <y, w>: yr wr + yi wi
-                        s1 += c == 0 ? o[k] * wo : -o[k] * wo;  // Im <y, w>: yr wi - yi wr
+                        s0 += o[k] * wc;  // Re <y, w>: yr wr + yi wi
+                        if (!HOUT) {      // Im <y, w>: yr wi - yi wr (the FP16 MR step takes omega real:
+                                          // <A r, r> is real for the Hermitian coarse operator)
+                            const float wo = __shfl_xor_sync(0xffffffffu, wc, 1);
+                            s1 += c == 0 ? o[k] * wo : -o[k] * wo;
+                        }
                         s2 += o[k] * o[k];
                     }
                 }

@@ -1302,32 +1302,41 @@ struct C16Ring {
     const float* s[kC16MaxSteps];
 };
 // x (+)= sum_k omega_k r_k over n FP16 residuals (omega [k][32]); x FP32 [site][dof][32]; one warp per
-// (site, dof) row of 32 rhs (lane = rhs) with every load of the row issued first
+// four (site, dof) rows of 32 rhs (lane = rhs, the rows of one site share its scales), every load of
+// the four rows issued first: short-lived one-row warps left the kernel latency-bound
+constexpr int kC16XRows = 4;
 __global__ void __launch_bounds__(256) k_c16_xupdate(cx<float>* __restrict__ x, C16Ring ring, int n,
                                                      const float2* __restrict__ omega, int nsites, int zero) {
     const int lane = threadIdx.x & 31;
-    const int64_t e = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (e >= (int64_t)nsites * kC16Dofs) return;
-    const int64_t i = e * 32 + lane, site = e / kC16Dofs;
-    __half2 rv[kC16MaxSteps];
+    const int64_t e0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * kC16XRows;
+    if (e0 >= (int64_t)nsites * kC16Dofs) return;
+    const int64_t site = e0 / kC16Dofs;  // kC16Dofs is a multiple of kC16XRows
+    __half2 rv[kC16MaxSteps][kC16XRows];
     float sc[kC16MaxSteps];
     float2 om[kC16MaxSteps];
+    cx<float> acc[kC16XRows];
 #pragma unroll
     for (int k = 0; k < kC16MaxSteps; ++k)
         if (k < n) {
-            rv[k] = ring.r[k][i];
+#pragma unroll
+            for (int j = 0; j < kC16XRows; ++j) rv[k][j] = ring.r[k][(e0 + j) * 32 + lane];
             sc[k] = ring.s[k][2 * site + (lane >> 4)];
             om[k] = omega[k * 32 + lane];
         }
-    cx<float> acc = zero ? mk(0.f, 0.f) : x[i];
+#pragma unroll
+    for (int j = 0; j < kC16XRows; ++j) acc[j] = zero ? mk(0.f, 0.f) : x[(e0 + j) * 32 + lane];
 #pragma unroll
     for (int k = 0; k < kC16MaxSteps; ++k)
         if (k < n) {
-            const float2 a = __half22float2(rv[k]);
-            const float ar = sc[k] * a.x, ai = sc[k] * a.y;
-            acc = mk(acc.re + om[k].x * ar - om[k].y * ai, acc.im + om[k].x * ai + om[k].y * ar);
+            const float wr = om[k].x * sc[k], wi = om[k].y * sc[k];  // omega_k times the scale
+#pragma unroll
+            for (int j = 0; j < kC16XRows; ++j) {
+                const float2 a = __half22float2(rv[k][j]);
+                acc[j] = mk(acc[j].re + wr * a.x - wi * a.y, acc[j].im + wr * a.y + wi * a.x);
+            }
         }
-    x[i] = acc;
+#pragma unroll
+    for (int j = 0; j < kC16XRows; ++j) x[(e0 + j) * 32 + lane] = acc[j];
 }
 // ====================================================================== host
 
@@ -2142,7 +2151,8 @@ smg_status mr_coarse_half(smg_mg* mg, int l, void* x, const void* b, int niter, 
             ring.s[k] = w.r16s[k];
         }
         const int64_t rows = (int64_t)L.nsites * kC16Dofs;
-        k_c16_xupdate<<<(unsigned)((rows + 7) / 8), 256, 0, ctx->stream>>>((cx<float>*)x, ring, niter, (const float2*)w.mr16_om, L.nsites,
+        const int64_t warps = rows / kC16XRows;
+        k_c16_xupdate<<<(unsigned)((warps + 7) / 8), 256, 0, ctx->stream>>>((cx<float>*)x, ring, niter, (const float2*)w.mr16_om, L.nsites,
                                                       x_is_zero ? 1 : 0);
         count_launch(ctx);
     } else if (x_is_zero) {
