@@ -631,8 +631,8 @@ __global__ void k_tile_links(const cx<double>* __restrict__ A, int nx, int64_t n
 // across the iterations.  Per iteration k:
 //   apply   the stagers form p_k = r_k + beta_{k-1} p_{k-1} on the fly for the source rows (FP16 r
 //           and p_{k-1} of any CTA's sites, published before the last grid barrier) and stage it as
-//           BF16; warps 10, 11 write p_k of the CTA's own sites (FP16, site scales) into the other p
-//           buffer; the epilogue writes A p_k (FP32) of the own sites;
+//           BF16; warps 0, 1, 4, 5, 8, 9 write p_k of the CTA's own sites (FP16) into the other p buffer,
+//           then, as the apply's three epilogue pairs, A p_k (FP32) of the own sites with <A p_k, p_k>;
 //   <A p_k, p_k> over the own sites per rhs, grid barrier, alpha_k = rr_k / <p_k, A p_k> from the
 //           per-CTA partials summed in CTA order (identical, deterministic scalars in every CTA);
 //   update  own sites: x += alpha p_k, r_{k+1} = r_k - alpha A p_k (FP16, new site scales), and
@@ -839,7 +839,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
         }
         for (int i = 0; i < 2; ++i) {
             mbar_init(bar(kBarAccFull + i), 1);
-            mbar_init(bar(kBarAccEmpty + i), 32 * 2 * kEpiHalves);
+            mbar_init(bar(kBarAccEmpty + i), 32 * 2 * kApGroups);
         }
         mbar_init(bar(kBarFinal), 1);
         misc[1] = 0;
@@ -919,7 +919,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
         float* __restrict__ psnew = a.ps[k & 1];
         const int ub = k * nunits, sb = k * (H + 2), ab = k * H;  // unit, source-row and output-row bases
         // ================= apply: A p_k with the apply kernel's warp roles
-        if (warp == 0) {
+        if (warp == kProdWarp) {
             if (lane == 0) {
                 const int ring3 = 3 * nx;
                 for (int u = 0; u < nunits; ++u) {
@@ -939,7 +939,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                 }
             }
             __syncwarp();
-        } else if (warp == 1) {
+        } else if (warp == kMmaWarp) {
             if (lane == 0) {
                 bool mok = true;
                 for (int r = 0; r < H && mok; ++r) {
@@ -981,8 +981,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                 }
             }
             __syncwarp();
-        } else if (warp == 2 || warp == 3 || warp == 6 || warp == 7) {
-            // stagers: p_k = r_k + beta p_{k-1} (FP16 inputs with scales) -> BF16 A tiles.  Item i of a
+        } else if ((warp & 3) >= 2) {
+            // stagers (warps 2, 3, 6, 7): p_k = r_k + beta p_{k-1} (FP16 inputs with scales) -> BF16 A tiles.  Item i of a
             // source row: site i / 128 of the row, rhs (i / 4) % 32, word i % 4 (dofs 4 (i % 4) ..
             // + 3): a warp's items are 8 rhs x 4 words of one site, 512 contiguous bytes of r and p
             const int st = (warp < 4 ? warp - 2 : warp - 4) * 32 + lane;
@@ -1030,10 +1030,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                 mbar_arrive(bar(kBarSrcFull + slot));
             }
         } else {
-            // warps 4, 5, 8, 9 (then the epilogue) and 10, 11: p_k of the own sites -> p[k & 1] (FP16,
-            // scale per unit = its largest |re| or |im|); warp pw takes units pw, pw + 6, ..., four
-            // per step with all four units' loads first
-            const int pw = warp <= 5 ? warp - 4 : warp - 6;  // 0 .. 5
+            // warps 0, 1, 4, 5, 8, 9: p_k of the own sites -> p[k & 1] (FP16, scale per unit = its
+            // largest |re| or |im|), then the epilogue; warp pw takes units pw, pw + 6, ..., four per
+            // step with all four units' loads first
+            const int pw = 2 * (warp >> 2) + (warp & 1);  // 0 .. 5
             constexpr int kPw = 6, kPq = 4;
             for (int u0 = pw; u0 < nunit; u0 += kPq * kPw) {
                 uint4 rv[kPq][2], pv[kPq][2];
@@ -1076,15 +1076,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                     if (lane == 0) __stcg(psnew + 2 * site + h, mx);
                 }
             }
-            // the six warps' own p_k is complete before the epilogue reads it back (named barrier 1:
-            // warps 10, 11 arrive, the epilogue warps wait)
-            if (warp <= 9) asm volatile("bar.sync 1, 192;" ::: "memory");
-            else asm volatile("bar.arrive 1, 192;" ::: "memory");
-            if (warp <= 9) {
+            // the six warps' own p_k is complete before the epilogue reads it back (named barrier 1)
+            asm volatile("bar.sync 1, 192;" ::: "memory");
+            {
                 // epilogue: A p_k of the own sites to global memory and <A p_k, p_k> per rhs (p_k of
-                // the row's sites requested before the row's accumulator wait)
-                const int half = warp >= 8 ? 1 : 0;
-                const int sub = warp - (half ? 8 : 4);
+                // the row's sites requested before the row's accumulator wait); the pairs (0, 1),
+                // (4, 5), (8, 9) take sites 0-2, 3-5 and 6-7 of every row
+                const int half = warp >> 2;  // the pair's group
+                const int sub = warp & 1;
+                const int sbase = kApSitesMax * half, nsq = half < 2 ? kApSitesMax : kW - 2 * kApSitesMax;
                 const int m = 32 * sub + lane;
                 const int rhs = m >> 1, c = m & 1;
                 const int64_t rstride = 2ll * nrhs;
@@ -1092,7 +1092,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                 float dot = 0.f;
                 // p_k of site q of row r (16 dofs of this lane's rhs: four 16-byte words) and its scale
                 auto load_p = [&](int r, int q, uint4 (&w)[4], float& sc) {
-                    const int64_t site = (int64_t)x0 + half * kEpiSites + q + (int64_t)nx * (y0 + r);
+                    const int64_t site = (int64_t)x0 + sbase + (q < nsq ? q : 0) + (int64_t)nx * (y0 + r);
                     const uint4* pp = h16_ptr(pnew, site, rhs);
 #pragma unroll
                     for (int w4 = 0; w4 < 4; ++w4) w[w4] = __ldcg(pp + w4);
@@ -1108,8 +1108,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                     if (!__all_sync(0xffffffffu, eok)) break;
                     tc_fence_after();
 #pragma unroll
-                    for (int q = 0; q < kEpiSites; ++q) {
-                        const int i = half * kEpiSites + q;
+                    for (int q = 0; q < kApSitesMax; ++q) {
+                        if (q >= nsq) break;
+                        const int i = sbase + q;
                         float d[32];
                         tmem_ld32(tmem + ((uint32_t)(32 * sub) << 16) + (uint32_t)((R & 1) * kAccCols + 32 * i), d);
                         const int64_t base = (((int64_t)x0 + i + (int64_t)nx * (y0 + r)) * kNc * nrhs + rhs) * 2 + c;
@@ -1123,7 +1124,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                             t += y * (c == 0 ? p2.x : p2.y);
                         }
                         dot += psq[q & 1] * t;
-                        if (q + 2 < kEpiSites) load_p(r, q + 2, pw[q & 1], psq[q & 1]);
+                        if (q + 2 < nsq) load_p(r, q + 2, pw[q & 1], psq[q & 1]);
                     }
                     tc_fence_before();
                     mbar_arrive(bar(kBarAccEmpty + (R & 1)));
@@ -1143,7 +1144,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
         // ================= <A p_k, p_k>: the epilogue's per-warp sums as this CTA's partials
         if (tid < 32) {
             const float* ed = reinterpret_cast<const float*>(smem + kRedOffset);
-            part1[(int64_t)tid * nblk + blin] = ed[tid] + ed[kRhsTile + tid];
+            part1[(int64_t)tid * nblk + blin] = (ed[tid] + ed[kRhsTile + tid]) + ed[2 * kRhsTile + tid];
         }
         ok = ccg_grid_barrier(a.bar, a.err, a.spin_limit);
         if (!ok) break;
@@ -1244,10 +1245,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
     if (blin == 0 && tid == 0 && a.iters) *a.iters = iter;
 
     // ---- teardown: every issued bulk copy and MMA has completed before tensor memory is freed
-    if (warp == 0 && lane == 0)
+    if (warp == kProdWarp && lane == 0)
         for (int U = issued > kUnits ? issued - kUnits : 0; U < issued; ++U)
             drain_bar(bar(kBarUnitFull + U % kUnits), (U / kUnits) & 1);
-    if (warp == 1 && lane == 0) {
+    if (warp == kMmaWarp && lane == 0) {
         mma_commit(bar(kBarFinal));
         drain_bar(bar(kBarFinal), 0);
     }
