@@ -329,6 +329,10 @@ def kernel_trace(step, ctx, path: str, what: str) -> None:
 TC_LEVEL1_L512_DRAM_BYTES = 226.540288e6 + 42.035968e6
 DSLASH_F32_L512_DRAM_BYTES = 140.034048e6 + 98.370048e6
 SMOOTHER_D_L512_DRAM_BYTES = 74.627072e6 + 31.32672e6
+# the persistent coarsest CG of the same workload (one solve of 20 iterations): ncu dram read + write and
+# lts__t_bytes (profiles/coarsest_cg_tc_L512_64x64_32rhs.md)
+CCG_L512_DRAM_BYTES = 548.350976e6 + 466.022912e6
+CCG_L512_L2_BYTES = 6.19010224e9
 
 
 def coarse_kernel_name(c, L, nrhs):
@@ -435,7 +439,8 @@ def run_ours(args, ws, rank, local):
         it64, res64 = res.iterations, res.true_residual
         detail = {"gcr_iterations": iters, "true_residual": true_res, "setup_s": setup_s,
                   "smoother_work_vectors": "FP16, per-site scales" if c["smoother_half"] and nrhs >= 8 else "FP32",
-                  "coarsest_cg_vectors": "FP16, per-site scales" if c["coarse_half"] and nrhs == 32 else "FP32",
+                  "coarse_work_vectors": ("FP16, scales per coarse site and rhs half (coarsest CG, level-1 MR)"
+                                          if c["coarse_half"] and nrhs == 32 else "FP32"),
                   "plain_fp64_mg_solves_per_s": 1e3 / ms64, "plain_fp64_mg_iterations": it64,
                   "plain_fp64_mg_true_residual": res64, "mixed_batched_over_plain_fp64": value / ws / (1e3 / ms64),
                   "launches_before_timed": int(l0)}
@@ -461,6 +466,18 @@ def run_ours(args, ws, rank, local):
             sm = smoother_times(smg, lib, ctx, mg32, lat, B)
             sm[0]["traffic"] = SMOOTHER_D_L512_DRAM_BYTES if (L, nrhs) == (512, 32) else None
             kernels = sm + kernels
+        # the coarsest solve of a cycle: with FP16 coarse vectors at 32 RHS one cooperative launch
+        # (k_ccg_tc), L2-resident, so no HBM roofline applies; its DRAM and L2 traffic are from ncu
+        sms, sit = Cc.c_double(), Cc.c_int()
+        smg._lib.check(lib.smg_mg_time_coarse_solve(mg32.h, 10, Cc.byref(sms), Cc.byref(sit)),
+                       "smg_mg_time_coarse_solve", ctx.h)
+        ccg = {"kernel": "coarsest CG (k_ccg_tc: one cooperative launch per solve)" if sit.value >= 0
+               else "coarsest CG (per-iteration kernels)", "ms_per_solve": sms.value,
+               "iterations": sit.value if sit.value >= 0 else None, "bound": "L2 / latency"}
+        if (L, nrhs) == (512, 32) and sit.value >= 0:
+            ccg["dram_bytes_per_solve"] = CCG_L512_DRAM_BYTES
+            ccg["l2_bytes_per_solve"] = CCG_L512_L2_BYTES
+        detail["coarsest_solve"] = ccg
         # the step's largest kernel (profiles/mg_gcr_L512_32rhs_kernel_shares.md): the FP16 stencil with the
         # fused MR reductions when the smoother runs on FP16 work vectors, else the level-1 coarse apply
         top = next((k for k in kernels if "fused" in k["kernel"]), kernels[0])

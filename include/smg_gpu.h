@@ -501,6 +501,13 @@ SMG_API smg_status smg_mg_time_coarse_apply(smg_mg* mg, int level, int nrhs, int
  * after one warm-up pass.  r is formed from b (F32, nrhs a power of two
  * >= 8).  bytes[k] (optional): each kernel's compulsory HBM bytes. */
 SMG_API smg_status smg_mg_time_smoother(smg_mg* mg, const smg_field* b, int reps, double* ms, double* bytes);
+/* Timing of the coarsest-level solve of the last cycle (SparseCoarseOp::solve,
+ * src/coarse_op.h:492-547) on the hierarchy's coarsest work vectors for the
+ * cycle's right-hand-side count: ms = the average of `reps` solves timed with
+ * CUDA events on the context's stream after one warm-up solve; iters (optional)
+ * = the CG iterations of the last solve when it ran as one cooperative launch,
+ * else -1.  The hierarchy must have run a cycle (SMG_BAD_ARG otherwise). */
+SMG_API smg_status smg_mg_time_coarse_solve(smg_mg* mg, int reps, double* ms, int* iters);
 
 /* fcg_solve / fcg_solve_mg: truncated GCR on A = D^dag D from x = 0
  * (reference src/solvers.cpp:223-300, 803-811), preconditioned by one MG

@@ -173,6 +173,7 @@ _SIGS = {
     "smg_mg_coarse_apply_host": (_st, [_vp, C.c_int, _dp, _dp]),
     "smg_mg_time_coarse_apply": (_st, [_vp, C.c_int, C.c_int, C.c_int, _dp, _dp]),
     "smg_mg_time_smoother": (_st, [_vp, _vp, C.c_int, _dp, _dp]),
+    "smg_mg_time_coarse_solve": (_st, [_vp, C.c_int, _dp, C.POINTER(C.c_int)]),
     "smg_mg_create_from_starts": (_st, [_vp, _vp, C.POINTER(_dp), C.POINTER(_vp)]),
     "smg_mg_n_null_vectors": (_st, [_vp, C.POINTER(C.c_int)]),
     "smg_mg_set_wait_limit": (_st, [_vp, C.c_longlong]),

@@ -3431,6 +3431,37 @@ SMG_API smg_status smg_mg_restrict_host(smg_mg* mg, int level, const double* fin
     return SMG_OK;
 }
 
+SMG_API smg_status smg_mg_time_coarse_solve(smg_mg* mg, int reps, double* ms, int* iters) {
+    if (!mg || !ms || reps < 1 || mg->work_nrhs < 1 || mg->lv.size() < 2) return SMG_BAD_ARG;
+    smg_context* ctx = mg->ctx;
+    const int l = (int)mg->lv.size() - 1;
+    CoarseWork& w = mg->cw[l];
+    cudaEvent_t e0, e1;
+    SMG_CUDA(ctx, cudaEventCreate(&e0));
+    SMG_CUDA(ctx, cudaEventCreate(&e1));
+    smg_status st = SMG_OK;
+    for (int pass = 0; pass < 2 && st == SMG_OK; ++pass) {  // pass 0 warms up
+        SMG_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+        for (int i = 0; i < (pass ? reps : 1) && st == SMG_OK; ++i)
+            st = mg->work_prec == SMG_F64 ? coarse_cg<double>(mg, l, w.x, w.b) : coarse_cg<float>(mg, l, w.x, w.b);
+        SMG_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+    }
+    SMG_CUDA(ctx, cudaEventSynchronize(e1));
+    float f = 0;
+    SMG_CUDA(ctx, cudaEventElapsedTime(&f, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    SMG_TRY(st);
+    SMG_TRY(smg_mg_check_device_error(mg));
+    *ms = (double)f / reps;
+    if (iters) {
+        *iters = -1;
+        if (mg->work_prec == SMG_F32 && coarse_half_level(mg, l, mg->work_nrhs, SMG_F32) && w.ph2 && ccg_tc_level(mg, l))
+            SMG_CUDA(ctx, cudaMemcpy(iters, static_cast<int*>(mg->cg_state) + 3, sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    return SMG_OK;
+}
+
 SMG_API smg_status smg_mg_time_coarse_apply(smg_mg* mg, int level, int nrhs, int reps, double* ms, double* bytes) {
     if (!mg || !ms || level < 1 || level >= (int)mg->lv.size() || nrhs < 1 || reps < 1) return SMG_BAD_ARG;
     smg_context* ctx = mg->ctx;
