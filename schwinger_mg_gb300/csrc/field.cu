@@ -146,13 +146,16 @@ size_t elem_bytes(smg_precision p) {
     return 0;
 }
 
+// Host images go through a staging buffer from the context's pool (a DMA copy, then a layout kernel):
+// allocating it per call put a device allocation and free into every upload and download.
 smg_status transfer_in(smg_field* f, const double* host) {
     smg_context* ctx = f->ctx;
     SMG_CUDA(ctx, cudaSetDevice(ctx->device));
     const int64_t n = f->n_complex();
+    const size_t nb = (size_t)n * sizeof(cx<double>);
     cx<double>* tmp = nullptr;
-    SMG_CUDA(ctx, cudaMallocAsync(&tmp, n * sizeof(cx<double>), ctx->stream));
-    SMG_CUDA(ctx, cudaMemcpyAsync(tmp, host, n * sizeof(cx<double>), cudaMemcpyHostToDevice, ctx->stream));
+    SMG_TRY(smg_buf_take(ctx, nb, reinterpret_cast<void**>(&tmp)));
+    SMG_CUDA(ctx, cudaMemcpyAsync(tmp, host, nb, cudaMemcpyHostToDevice, ctx->stream));
     int64_t total = (int64_t)f->g.V * f->nrhs;
     int blocks = (int)((total + 255) / 256);
     if (f->prec == SMG_F16) {
@@ -165,7 +168,7 @@ smg_status transfer_in(smg_field* f, const double* host) {
         k_host_to_field<float><<<blocks, 256, 0, ctx->stream>>>(tmp, (cx<float>*)f->data, f->g, f->nrhs);
     count_launch(ctx);
     SMG_CHECK_LAUNCH(ctx);
-    SMG_CUDA(ctx, cudaFreeAsync(tmp, ctx->stream));
+    smg_buf_give(ctx, nb, tmp);  // later users are ordered after this work on the same stream
     return SMG_OK;
 }
 
@@ -173,8 +176,9 @@ smg_status transfer_out(const smg_field* f, double* host, bool sync) {
     smg_context* ctx = f->ctx;
     SMG_CUDA(ctx, cudaSetDevice(ctx->device));
     const int64_t n = f->n_complex();
+    const size_t nb = (size_t)n * sizeof(cx<double>);
     cx<double>* tmp = nullptr;
-    SMG_CUDA(ctx, cudaMallocAsync(&tmp, n * sizeof(cx<double>), ctx->stream));
+    SMG_TRY(smg_buf_take(ctx, nb, reinterpret_cast<void**>(&tmp)));
     int64_t total = (int64_t)f->g.V * f->nrhs;
     int blocks = (int)((total + 255) / 256);
     if (f->prec == SMG_F16) {
@@ -187,8 +191,8 @@ smg_status transfer_out(const smg_field* f, double* host, bool sync) {
         k_field_to_host<float><<<blocks, 256, 0, ctx->stream>>>((const cx<float>*)f->data, tmp, f->g, f->nrhs);
     count_launch(ctx);
     SMG_CHECK_LAUNCH(ctx);
-    SMG_CUDA(ctx, cudaMemcpyAsync(host, tmp, n * sizeof(cx<double>), cudaMemcpyDeviceToHost, ctx->stream));
-    SMG_CUDA(ctx, cudaFreeAsync(tmp, ctx->stream));
+    SMG_CUDA(ctx, cudaMemcpyAsync(host, tmp, nb, cudaMemcpyDeviceToHost, ctx->stream));
+    smg_buf_give(ctx, nb, tmp);
     if (sync) SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return SMG_OK;
 }

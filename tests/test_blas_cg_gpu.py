@@ -91,3 +91,30 @@ def test_cg_nonfinite_rhs(smg_gpu):
     with pytest.raises(smg_gpu.SmgError) as e:
         smg_gpu.cg_solve(D, lat.ndof, b, 100, 1e-10)
     assert e.value.status == 3
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32", "f16"])
+def test_pinned_host_transfers_match_pageable(smg_gpu, prec):
+    """Uploads and downloads with page-locked host buffers (read and written by the layout kernels in
+    place) give the same fields and host images as with pageable numpy buffers (staged on the device)."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+
+    from schwinger_mg_gb300 import _lib
+
+    lat = smg_gpu.Lattice(32)
+    nrhs = 8
+    B = np.stack([smg_gpu.random_vec(lat.ndof, 900 + j) for j in range(nrhs)])
+    ref = smg_gpu.Field(lat, nrhs, prec, data=B)
+    pin_in = torch.empty(B.size * 2, dtype=torch.float64).pin_memory()
+    pin_in.numpy()[:] = B.reshape(-1).view(np.float64)
+    pin_out = torch.zeros_like(pin_in).pin_memory()
+    dp = C.POINTER(C.c_double)
+    f = smg_gpu.Field(lat, nrhs, prec)
+    lib = smg_gpu.lib()
+    assert lib.smg_field_upload_async(f.h, C.cast(pin_in.data_ptr(), dp)) == _lib.OK
+    assert lib.smg_field_download_async(f.h, C.cast(pin_out.data_ptr(), dp)) == _lib.OK
+    f.ctx.synchronize()
+    want = ref.download()
+    assert np.array_equal(f.download(), want)
+    assert np.array_equal(pin_out.numpy().view(np.complex128).reshape(want.shape), want)
