@@ -79,6 +79,9 @@ struct Level {
     int ax = 0, ay = 0, nvec = 0, nc_next = 0, nagg_x = 0, nagg_y = 0;
     cx<double>* V64 = nullptr;  // [agg][loc][dof][i]
     cx<float>* V32 = nullptr;
+    // level 0 with the packed transfers: V in FP32 as pairs over the two spins of a site,
+    // [agg][loc][i] = (Re V[loc][0][i], Re V[loc][1][i], Im V[loc][0][i], Im V[loc][1][i])
+    float4* V32s = nullptr;
     // operator of this level (l >= 1): [site][dir][j][i] = block(i, j)
     cx<double>* A64 = nullptr;
     cx<float>* A32 = nullptr;
@@ -89,6 +92,22 @@ struct Level {
 };
 
 // ------------------------------------------------------------ level-0 kernels
+
+// the level-0 shape the packed transfers serve: 4 x 4 aggregates and 8, 16 or 32 coarse dofs
+inline bool packed_shape0(const Level& L) {
+    return L.ax == 4 && L.ay == 4 && (L.nc_next == 8 || L.nc_next == 16 || L.nc_next == 32);
+}
+
+// V32s[(agg, loc)][i] = (Re V[loc][0][i], Re V[loc][1][i], Im V[loc][0][i], Im V[loc][1][i]) in FP32
+// from V64 [agg][loc][spin][i]; np = aggregates x sites per aggregate x nc
+__global__ void k_pair_spins(const cx<double>* __restrict__ V, float4* __restrict__ out, int64_t np, int nc) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) return;
+    const int64_t sl = k / nc;
+    const int i = (int)(k - sl * nc);
+    const cx<double> a = V[(2 * sl) * nc + i], b = V[(2 * sl + 1) * nc + i];
+    out[k] = make_float4((float)a.re, (float)b.re, (float)a.im, (float)b.im);
+}
 
 // V[B][loc][sp][i] from null vector k: i = c * nvec + k with chirality c = sp
 // (split) or i = k (no split)
@@ -1388,6 +1407,11 @@ struct smg_mg {
     float* hdots = nullptr;
     double* mr_om = nullptr;
     float2* mr_omf = nullptr;  // each step's omega per rhs, as the update kernels read it
+    // pre-smoothing x update left to the level-0 prolongation: x = (xp_zero ? 0 : x) +
+    // sum_{k < xp_n} omega_k f_rs[xp_first + k]
+    int xp_first = 0, xp_n = 0;
+    bool xp_zero = false;
+    double xp_omega = 0;
     std::vector<CoarseWork> cw;
     double* scal = nullptr;  // per-level scalar area
     size_t scal_doubles = 0;
@@ -1900,6 +1924,209 @@ __global__ void __launch_bounds__(256) k_mr_xupdate_h(cx<float>* __restrict__ x,
     px[1] = make_float4(xv[1].s0.re, xv[1].s0.im, xv[1].s1.re, xv[1].s1.im);
 }
 
+// asynchronous global -> shared copies (no registers held while in flight)
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Packed FP32 pairs for the level-0 transfers: fma.rn.f32x2 does two independent FP32 FMAs in one
+// instruction, so a complex multiply-add costs two instructions instead of four.  A pair is a
+// 64-bit register (low half first).
+using f32x2 = unsigned long long;
+__device__ __forceinline__ f32x2 f2_pack(float lo, float hi) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float2 f2_unpack(f32x2 v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// The level-0 transfers of the FP16 smoother for aggregates of 4 x 4 sites and tiles of 32
+// right-hand sides (lane = rhs).  The block vectors of an aggregate are V[e][i], e = 2 loc + spin,
+// i < NC, as the generic transfer kernels read them.
+constexpr int kAggSites0 = 16;
+
+// Restriction out_i = sum_e conj(V[e][i]) r_e of an FP16 residual with per-site scales (the
+// generic kernel with the InHalf reader, k_restrict_agg): one warp per aggregate, the lane's 16
+// two-spinors in registers, the warp's block vectors staged in shared memory as output pairs
+// [e][i/2] = (Re V[e][i], Re V[e][i+1], Im V[e][i], Im V[e][i+1]) so that one broadcast 16-byte read
+// feeds four packed FMAs.
+template <int NC>
+__global__ void __launch_bounds__(128) k_restrict0_h(const cx<float>* __restrict__ V, const __half2* __restrict__ r,
+                                                     const float* __restrict__ rs, cx<float>* __restrict__ out,
+                                                     TransferGeom t, int nagg) {
+    constexpr int ne = 2 * kAggSites0, NP = NC / 2;
+    __shared__ float4 s_v[4][ne * NP];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int B = blockIdx.x * 4 + w;
+    if (B >= nagg) return;  // whole warps; the kernel has no block barrier
+    const int nrhs = t.nrhs, rhs = blockIdx.y * 32 + lane;
+    const int x0 = (B % t.nax) * 4, y0 = (B / t.nax) * 4;
+    const int myq = site_q(t.g, x0 + (lane & 3), y0 + ((lane >> 2) & 3));  // lanes 16..31 repeat 0..15
+    const float mys = __ldg(rs + myq);
+    uint2 raw[kAggSites0];
+#pragma unroll
+    for (int s = 0; s < kAggSites0; ++s) {
+        const int q = __shfl_sync(0xffffffffu, myq, s);
+        raw[s] = __ldg(reinterpret_cast<const uint2*>(r) + ((int64_t)q * nrhs + rhs));
+    }
+    // float4 k of the aggregate's block vectors holds V entries 2k, 2k+1 = (e, i), (e, i + 1), i even
+    const float4* __restrict__ Vb = reinterpret_cast<const float4*>(V + (int64_t)B * ne * NC);
+#pragma unroll
+    for (int k = lane; k < ne * NP; k += 32) {
+        const float4 a = __ldg(Vb + k);
+        s_v[w][k] = make_float4(a.x, a.z, a.y, a.w);
+    }
+    __syncwarp();
+    f32x2 accr[NP], acci[NP];  // (Re out_i, Re out_i+1), (Im out_i, Im out_i+1)
+#pragma unroll
+    for (int p = 0; p < NP; ++p) accr[p] = acci[p] = 0ull;
+#pragma unroll
+    for (int s = 0; s < kAggSites0; ++s) {
+        const float sc = __shfl_sync(0xffffffffu, mys, s);
+        const float2 f0 = __half22float2(*reinterpret_cast<const __half2*>(&raw[s].x));
+        const float2 f1 = __half22float2(*reinterpret_cast<const __half2*>(&raw[s].y));
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const float fr = (j ? f1.x : f0.x) * sc, fi = (j ? f1.y : f0.y) * sc;
+            const f32x2 FR = f2_pack(fr, fr), FI = f2_pack(fi, fi), FRn = f2_pack(-fr, -fr);
+            const float4* __restrict__ vrow = &s_v[w][(2 * s + j) * NP];
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                const float4 v = vrow[p];
+                const f32x2 VR = f2_pack(v.x, v.y), VI = f2_pack(v.z, v.w);
+                accr[p] = f2_fma(VR, FR, accr[p]);  // Re conj(v) f = Re v Re f + Im v Im f
+                accr[p] = f2_fma(VI, FI, accr[p]);
+                acci[p] = f2_fma(VR, FI, acci[p]);  // Im conj(v) f = Re v Im f - Im v Re f
+                acci[p] = f2_fma(VI, FRn, acci[p]);
+            }
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const float2 re = f2_unpack(accr[p]), im = f2_unpack(acci[p]);
+        out[((int64_t)B * NC + 2 * p) * nrhs + rhs] = mk(re.x, im.x);
+        out[((int64_t)B * NC + 2 * p + 1) * nrhs + rhs] = mk(re.y, im.y);
+    }
+}
+
+// Prolongation with the pre-smoothing update folded in:
+//   x(site, spin) = [x] + sum_{k < n} omega_k r_k + sum_i V[e][i] c_i
+// (the generic kernel k_prolong_agg after k_mr_xupdate_h).  One block of four warps per aggregate,
+// warp w on the aggregate's row w (four sites); the block vectors staged in shared memory as pairs
+// over the two spins of a site, [loc][i] = (Re V[2 loc][i], Re V[2 loc + 1][i], Im V[2 loc][i],
+// Im V[2 loc + 1][i]) (the level's V32s copy), the coarse values as [i][lane], and the lane's x
+// values held as (Re spin 0, Re spin 1), (Im spin 0, Im spin 1) pairs.  The residuals' loads go
+// out kRingChunk at a time.
+constexpr int kRingChunk = 4;
+
+template <int NC>
+__global__ void __launch_bounds__(128) k_prolong0_ring(const float4* __restrict__ Vs, const cx<float>* __restrict__ cin,
+                                                       cx<float>* __restrict__ x, TransferGeom t, ResidualRing ring,
+                                                       int n, const float2* __restrict__ om, float omega,
+                                                       int accumulate) {
+    constexpr int S = 4;
+    __shared__ float4 s_v[kAggSites0 * NC];
+    __shared__ float2 s_c[NC * 32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int B = blockIdx.x;
+    const int nrhs = t.nrhs, rhs = blockIdx.y * 32 + lane;
+    const int myq = site_q(t.g, (B % t.nax) * 4 + (lane & 3), (B / t.nax) * 4 + w);  // lanes repeat mod 4
+    // the aggregate's spin-paired block vectors and the tile's coarse values go to shared memory by
+    // asynchronous copies that hold no registers while the residuals' loads are in flight
+    const float4* __restrict__ vsrc = Vs + (int64_t)B * kAggSites0 * NC;
+#pragma unroll
+    for (int k = threadIdx.x; k < kAggSites0 * NC; k += 128) cp_async16(&s_v[k], vsrc + k);
+    const float2* __restrict__ c2 = reinterpret_cast<const float2*>(cin) + (int64_t)B * NC * nrhs + rhs;
+#pragma unroll
+    for (int i = w; i < NC; i += 4) cp_async8(&s_c[i * 32 + lane], c2 + (int64_t)i * nrhs);
+    int q[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) q[s] = __shfl_sync(0xffffffffu, myq, s);
+    f32x2 xr[S], xi[S];
+    float4* __restrict__ px = reinterpret_cast<float4*>(x);  // one float4 = both spins of (site, rhs)
+    if (accumulate) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            const float4 v = px[(int64_t)q[s] * nrhs + rhs];
+            xr[s] = f2_pack(v.x, v.z);
+            xi[s] = f2_pack(v.y, v.w);
+        }
+    } else {
+#pragma unroll
+        for (int s = 0; s < S; ++s) xr[s] = xi[s] = 0ull;
+    }
+    for (int k0 = 0; k0 < n; k0 += kRingChunk) {
+        uint2 raw[kRingChunk][S];
+        float scl[kRingChunk];
+        float2 o[kRingChunk];
+#pragma unroll
+        for (int j = 0; j < kRingChunk; ++j) {
+            if (k0 + j < n) {
+                const int k = k0 + j;
+                o[j] = om ? __ldg(om + (int64_t)k * nrhs + rhs) : make_float2(omega, 0.f);
+                scl[j] = __ldg(ring.s[k] + myq);
+                const uint2* __restrict__ rk = reinterpret_cast<const uint2*>(ring.r[k]);
+#pragma unroll
+                for (int s = 0; s < S; ++s) raw[j][s] = __ldg(rk + ((int64_t)q[s] * nrhs + rhs));
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kRingChunk; ++j) {
+            if (k0 + j < n) {
+#pragma unroll
+                for (int s = 0; s < S; ++s) {
+                    const float sc = __shfl_sync(0xffffffffu, scl[j], s);
+                    const float orr = o[j].x * sc, oi = o[j].y * sc;
+                    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&raw[j][s].x));
+                    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&raw[j][s].y));
+                    const f32x2 RR = f2_pack(a.x, b.x), RI = f2_pack(a.y, b.y);
+                    // (omega s) r: Re = o_r r_r - o_i r_i, Im = o_r r_i + o_i r_r
+                    xr[s] = f2_fma(f2_pack(orr, orr), RR, xr[s]);
+                    xr[s] = f2_fma(f2_pack(-oi, -oi), RI, xr[s]);
+                    xi[s] = f2_fma(f2_pack(orr, orr), RI, xi[s]);
+                    xi[s] = f2_fma(f2_pack(oi, oi), RR, xi[s]);
+                }
+            }
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NC; ++i) {
+        const float2 c = s_c[i * 32 + lane];
+        const f32x2 CR = f2_pack(c.x, c.x), CI = f2_pack(c.y, c.y), CIn = f2_pack(-c.y, -c.y);
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            const float4 v = s_v[(S * w + s) * NC + i];
+            const f32x2 VR = f2_pack(v.x, v.y), VI = f2_pack(v.z, v.w);
+            xr[s] = f2_fma(VR, CR, xr[s]);  // Re v c = Re v Re c - Im v Im c
+            xr[s] = f2_fma(VI, CIn, xr[s]);
+            xi[s] = f2_fma(VR, CI, xi[s]);  // Im v c = Re v Im c + Im v Re c
+            xi[s] = f2_fma(VI, CR, xi[s]);
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        const float2 re = f2_unpack(xr[s]), im = f2_unpack(xi[s]);
+        px[(int64_t)q[s] * nrhs + rhs] = make_float4(re.x, im.x, re.y, im.y);
+    }
+}
+
 // launch shape of the pair kernels: (nrhs / 2 lanes, 256 / lanes sites)
 dim3 pair_block(int nrhs) { return dim3(nrhs / 2, 512 / nrhs); }
 dim3 pair_grid(int nsites, int nrhs) { return dim3((nsites + 512 / nrhs - 1) / (512 / nrhs)); }
@@ -1949,9 +2176,10 @@ smg_status mr_step_h(smg_mg* mg, int it, double omega, bool write_next) {
 }
 
 // mr_fine / smooth_fine with FP16 residuals, A r and D r (x and b FP32).  keep_residual: the last
-// step also writes r_n = b - A x (the residual the cycle restricts after pre-smoothing).
+// step also writes r_n = b - A x (the residual the cycle restricts after pre-smoothing).  defer_x:
+// the last x pass is left to the caller (mg->xp_*), which folds it into the prolongation.
 smg_status smooth_fine_half(smg_mg* mg, smg_field* x, const smg_field* b, int niter, bool x_is_zero, double omega,
-                            bool keep_residual) {
+                            bool keep_residual, bool defer_x = false) {
     smg_context* ctx = mg->ctx;
     smg_field *r0 = mg->f_rs[0], *Ar = mg->f_Ar, *t = mg->f_t;
     const int V = b->g.V, nrhs = b->nrhs;
@@ -1977,13 +2205,82 @@ smg_status smooth_fine_half(smg_mg* mg, smg_field* x, const smg_field* b, int ni
             zero = false;
         }
     }
-    SMG_TRY(mr_xupdate_h(mg, x, first, niter - first, zero, omega));
+    if (defer_x) {
+        mg->xp_first = first;
+        mg->xp_n = niter - first;
+        mg->xp_zero = zero;
+        mg->xp_omega = omega;
+    } else {
+        SMG_TRY(mr_xupdate_h(mg, x, first, niter - first, zero, omega));
+    }
     mg->f_res = mg->f_rs[niter];
     return SMG_OK;
 }
 
 TransferGeom transfer_geom(const smg_mg* mg, int l, int nrhs);
 dim3 transfer_block(int nrhs);
+
+// the level-0 transfers with packed FMAs (k_restrict0_h, k_prolong0_ring) serve the FP16 smoother
+// with 4 x 4 aggregates, 8, 16 or 32 coarse dofs and whole tiles of 32 rhs; SMG_TRANSFER0_PACKED=0
+// keeps the generic kernels and a separate x pass
+bool transfer0_packed(const smg_mg* mg) {
+    static const bool on = [] {
+        const char* e = std::getenv("SMG_TRANSFER0_PACKED");
+        return !(e && std::atoi(e) == 0);
+    }();
+    const Level& L = mg->lv[0];
+    return on && mg->lv.size() > 1 && packed_shape0(L) && mg->work_nrhs % 32 == 0 && mg->f_r &&
+           mg->f_r->prec == SMG_F16 && L.V32 && L.V32s;
+}
+
+smg_status restrict0_packed(smg_mg* mg, const smg_field* r, void* out) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[0];
+    const int nagg = mg->lv[1].nsites, nrhs = mg->work_nrhs;
+    const TransferGeom t = transfer_geom(mg, 0, nrhs);
+    const dim3 grid((nagg + 3) / 4, nrhs / 32), block(128);
+    const __half2* rp = (const __half2*)r->data;
+    cx<float>* o = (cx<float>*)out;
+    if (L.nc_next == 8)
+        k_restrict0_h<8><<<grid, block, 0, ctx->stream>>>(L.V32, rp, r->scale, o, t, nagg);
+    else if (L.nc_next == 16)
+        k_restrict0_h<16><<<grid, block, 0, ctx->stream>>>(L.V32, rp, r->scale, o, t, nagg);
+    else
+        k_restrict0_h<32><<<grid, block, 0, ctx->stream>>>(L.V32, rp, r->scale, o, t, nagg);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+// x = (pending x pass) + P e, consuming mg->xp_*
+smg_status prolong0_packed(smg_mg* mg, const void* coarse, smg_field* x) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[0];
+    const int nagg = mg->lv[1].nsites, nrhs = mg->work_nrhs;
+    const TransferGeom t = transfer_geom(mg, 0, nrhs);
+    ResidualRing ring{};
+    for (int k = 0; k < mg->xp_n; ++k) {
+        ring.r[k] = (const __half2*)mg->f_rs[mg->xp_first + k]->data;
+        ring.s[k] = mg->f_rs[mg->xp_first + k]->scale;
+    }
+    const double omega = mg->xp_omega;
+    const float2* om = omega > 0 ? nullptr : mg->mr_omf + (size_t)mg->xp_first * nrhs;
+    const int acc = mg->xp_zero ? 0 : 1;
+    const dim3 grid(nagg, nrhs / 32), block(128);
+    const cx<float>* c = (const cx<float>*)coarse;
+    cx<float>* xp = (cx<float>*)x->data;
+#define SMG_P0(NC) \
+    k_prolong0_ring<NC><<<grid, block, 0, ctx->stream>>>(L.V32s, c, xp, t, ring, mg->xp_n, om, (float)omega, acc)
+    if (L.nc_next == 8) SMG_P0(8);
+    else if (L.nc_next == 16) SMG_P0(16);
+    else SMG_P0(32);
+#undef SMG_P0
+    mg->xp_n = 0;
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
 
 // dynamic shared memory of the aggregate transfer kernels: staged inputs (restriction: ne x lanes,
 // prolongation: NC x lanes) and the aggregate's block vectors (ne x NC)
@@ -2486,9 +2783,16 @@ template <typename T>
 smg_status cycle_fine(smg_mg* mg, smg_field* x, const smg_field* b) {
     smg_context* ctx = mg->ctx;
     const int last = (int)mg->lv.size() - 1;
-    SMG_TRY(smooth_fine<T>(mg, x, b, mg->p.pre_smooth, true));
+    // packed level-0 transfers: the pre-smoothing x pass is folded into the prolongation
+    const bool packed = std::is_same<T, float>::value && transfer0_packed(mg);
+    if (packed)
+        SMG_TRY(smooth_fine_half(mg, x, b, mg->p.pre_smooth, true, mg->lv[0].rich_omega, true, true));
+    else
+        SMG_TRY(smooth_fine<T>(mg, x, b, mg->p.pre_smooth, true));
     CoarseWork& nw = mg->cw[1];
-    if (mg->f_r->prec == SMG_F16)
+    if (packed)
+        SMG_TRY(restrict0_packed(mg, mg->f_res, nw.b));
+    else if (mg->f_r->prec == SMG_F16)
         SMG_TRY(restrict_half(mg, mg->f_res, nw.b));
     else
         SMG_TRY(restrict_to<T>(mg, 0, mg->f_r->data, nw.b));
@@ -2505,7 +2809,10 @@ smg_status cycle_fine(smg_mg* mg, smg_field* x, const smg_field* b) {
         k_vadd<T><<<blocks_for(nn), 256, 0, ctx->stream>>>((cx<T>*)nw.x, (const cx<T>*)nw.e, nn);
         count_launch(ctx);
     }
-    SMG_TRY(prolong_to<T>(mg, 0, nw.x, x->data, 1));
+    if (packed)
+        SMG_TRY(prolong0_packed(mg, nw.x, x));
+    else
+        SMG_TRY(prolong_to<T>(mg, 0, nw.x, x->data, 1));
     return smooth_fine<T>(mg, x, b, mg->p.post_smooth, false, false);
 }
 
@@ -2629,6 +2936,12 @@ smg_status make_f32_copies(smg_mg* mg) {
             if (!L.V32) SMG_CUDA(ctx, cudaMalloc(&L.V32, n * sizeof(cx<float>)));
             k_cvt_flat<float, double><<<blocks_for(n), 256, 0, ctx->stream>>>(L.V64, L.V32, n);
             count_launch(ctx);
+            if (l == 0 && mg->p.smoother_half && packed_shape0(L)) {
+                const int64_t np = n / 2;
+                if (!L.V32s) SMG_CUDA(ctx, cudaMalloc(&L.V32s, np * sizeof(float4)));
+                k_pair_spins<<<blocks_for(np), 256, 0, ctx->stream>>>(L.V64, L.V32s, np, L.nc_next);
+                count_launch(ctx);
+            }
         }
         if (L.A64) {
             int64_t n = L.asize();
@@ -2863,7 +3176,7 @@ smg_status rebuild_operators(smg_mg* mg) {
 
 void destroy_levels(smg_mg* mg) {
     for (auto& L : mg->lv) {
-        for (void* p : {(void*)L.V64, (void*)L.V32, (void*)L.A64, (void*)L.A32, L.Atc})
+        for (void* p : {(void*)L.V64, (void*)L.V32, (void*)L.V32s, (void*)L.A64, (void*)L.A32, L.Atc})
             if (p) cudaFree(p);
     }
     mg->lv.clear();

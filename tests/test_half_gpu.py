@@ -108,7 +108,9 @@ import schwinger_mg_gb300 as smg
 L, nrhs = 64, 32
 lat = smg.Lattice(L)
 D = smg.DiracOp(lat, smg.GaugeField(lat, smg.gauge_normal(L, 6.0, 43)), -0.05, 1.0, 1.0, 0.0)
-mg = smg.MGHierarchy(D, smg.mg_params(3, 4, 16, blocks=[(4, 4), (2, 2)], chiral_split=False, null_iters=4,
+nvec = int(sys.argv[3]) if len(sys.argv) > 3 else 16
+chiral = len(sys.argv) > 4 and sys.argv[4] == "1"
+mg = smg.MGHierarchy(D, smg.mg_params(3, 4, nvec, blocks=[(4, 4), (2, 2)], chiral_split=chiral, null_iters=4,
                                        pre_smooth=4, post_smooth=4, w_cycle=False, coarse_max_iter=20,
                                        coarse_tol=5e-2, precision="f32", seed=11, smoother_half=True,
                                        coarse_half=True))
@@ -119,11 +121,12 @@ np.savez(sys.argv[2], c=c, iters=r.iterations, res=r.true_residual)
 """
 
 
-def _ccg_run(tmp_path: Path, name: str, persistent: bool) -> dict:
+def _ccg_run(tmp_path: Path, name: str, persistent: bool, *args: str, **switches: str) -> dict:
     root = Path(__file__).resolve().parents[1]
     out = tmp_path / f"{name}.npz"
-    env = dict(os.environ, SMG_CCG_PERSISTENT="1" if persistent else "0")
-    subprocess.run([sys.executable, "-c", _CCG_CHILD, str(root), str(out)], env=env, check=True, timeout=600)
+    env = dict(os.environ, SMG_CCG_PERSISTENT="1" if persistent else "0", **switches)
+    subprocess.run([sys.executable, "-c", _CCG_CHILD, str(root), str(out), *args], env=env, check=True,
+                   timeout=600)
     with np.load(out) as z:
         return {k: z[k] for k in z.files}
 
@@ -139,3 +142,17 @@ def test_persistent_coarsest_cg_matches_per_iteration_kernels(tmp_path):
     assert np.linalg.norm(pst["c"] - per["c"]) / np.linalg.norm(per["c"]) < 1e-2
     assert float(pst["res"]) < 1e-10 and float(per["res"]) < 1e-10
     assert abs(int(pst["iters"]) - int(per["iters"])) <= 2
+
+
+@pytest.mark.parametrize("nvec,chiral", [(16, "0"), (8, "0"), (16, "1")])
+def test_packed_level0_transfers_match_generic_kernels(tmp_path, nvec, chiral):
+    """The level-0 transfers with packed FP32 FMAs (k_restrict0_h; k_prolong0_ring with the
+    pre-smoothing x pass folded in) against the generic aggregate kernels and a separate x pass, each
+    in its own process, for 8, 16 and (chirally split) 32 coarse dofs: the same arithmetic in FP32 up
+    to the order of the sums, so the cycles agree to the FP16 rounding downstream, and the solves
+    reach 1e-10 in as many iterations up to one."""
+    gen = _ccg_run(tmp_path, "generic", True, str(nvec), chiral, SMG_TRANSFER0_PACKED="0")
+    pk = _ccg_run(tmp_path, "packed", True, str(nvec), chiral, SMG_TRANSFER0_PACKED="1")
+    assert np.linalg.norm(pk["c"] - gen["c"]) / np.linalg.norm(gen["c"]) < 1e-2
+    assert float(pk["res"]) < 1e-10 and float(gen["res"]) < 1e-10
+    assert abs(int(pk["iters"]) - int(gen["iters"])) <= 1
