@@ -734,6 +734,55 @@ __device__ __forceinline__ bool ccg_grid_barrier(unsigned int* bar, int* err, lo
     return s_ok != 0;
 }
 
+// The same barrier in two halves, so that a CTA does work on its own data while the others arrive:
+// ccg_barrier_arrive publishes this CTA's writes and counts it in (thread 0 keeps the generation it
+// saw and whether it may wait); ccg_barrier_wait returns once every CTA has arrived, with the same
+// bound and error flag as ccg_grid_barrier.  Between the two a CTA reads and writes only data no
+// other CTA touches before the next barrier.
+__device__ __forceinline__ void ccg_barrier_arrive(unsigned int* bar, int* err, unsigned int* s_gen, int* s_ok) {
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        volatile unsigned int* vgen = bar + 1;
+        volatile int* verr = err;
+        if (*verr) {
+            ok = 0;
+        } else {
+            const unsigned int gen = *vgen;
+            __threadfence();
+            const unsigned int nblk = gridDim.x * gridDim.y;
+            if (atomicAdd(bar, 1u) == nblk - 1) {
+                bar[0] = 0u;
+                __threadfence();
+                atomicAdd(bar + 1, 1u);
+            }
+            *s_gen = gen;
+        }
+        *s_ok = ok;
+    }
+}
+__device__ __forceinline__ bool ccg_barrier_wait(unsigned int* bar, int* err, long long spin_limit,
+                                                 const unsigned int* s_gen, int* s_ok) {
+    if (threadIdx.x == 0 && *s_ok) {
+        volatile unsigned int* vgen = bar + 1;
+        volatile int* verr = err;
+        const unsigned int gen = *s_gen;
+        long long k = 0;
+        while (*vgen == gen) {
+            if (*verr || ++k > spin_limit) {
+                atomicCAS(err, 0, 1);
+                *s_ok = 0;
+                break;
+            }
+            __nanosleep(32);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
+
 // out32[j] = sum over the grid's CTAs of part[j][cta] for the 32 rhs: warp w takes rhs w, w + 12,
 // w + 24 with all its loads issued first, lanes stride the CTAs, then a fixed shuffle tree (the same
 // order in every CTA).  The CG's scalars are FP32: the coarsest solve runs to a tolerance of a few
@@ -816,6 +865,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
     int* s_act = reinterpret_cast<int*>(smem + kCcgAct);
     float* s_wred = reinterpret_cast<float*>(smem + kCcgWred);
     volatile int* abort_flag = misc + 1;
+    __shared__ unsigned int s_gen[1];  // the split barrier's generation and go flag (thread 0)
+    __shared__ int s_ok[1];
     auto bar = [&](int i) { return bar_a + 8u * (uint32_t)i; };
     float* part1 = reinterpret_cast<float*>(a.part);  // <A p, p> partials
     float* part2 = part1 + (int64_t)32 * nblk;         // ||r||^2 partials
@@ -1157,14 +1208,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
             s_alpha[tid] = al;
         }
         __syncthreads();
-        // ================= update of the own sites: two units per step, both units' loads first
+        // ================= r update of the own sites: two units per step, both units' loads first
+        // (x moves in the second barrier's wait, below)
         {
             float acc[2] = {0.f, 0.f};
             constexpr int kW32 = kThreads / 32;
             for (int u0 = warp; u0 < nunit; u0 += 2 * kW32) {
-                uint4 rw[2][2], pw[2][2];
-                float2 av[2][8], xv[2][8];
-                float sr[2], sp[2];
+                uint4 rw[2][2];
+                float2 av[2][8];
+                float sr[2];
 #pragma unroll
                 for (int q = 0; q < 2; ++q) {
                     const int u = u0 + q * kW32 < nunit ? u0 + q * kW32 : u0;
@@ -1172,18 +1224,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                     const int h = u & 1, rhs = 16 * h + lrhs;
                     const int64_t e0 = e_of(site, rhs);
                     const uint4* rp = h16_ptr(a.r, site, rhs) + 2 * dh;
-                    const uint4* pp = h16_ptr(pnew, site, rhs) + 2 * dh;
                     rw[q][0] = __ldcg(rp);
                     rw[q][1] = __ldcg(rp + 1);
-                    pw[q][0] = __ldcg(pp);
-                    pw[q][1] = __ldcg(pp + 1);
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        av[q][j] = __ldcg(a.Ap + e0 + j * nrhs);
-                        xv[q][j] = __ldcg(a.x + e0 + j * nrhs);
-                    }
+                    for (int j = 0; j < 8; ++j) av[q][j] = __ldcg(a.Ap + e0 + j * nrhs);
                     sr[q] = __ldcg(a.rs + 2 * site + h);
-                    sp[q] = __ldcg(psnew + 2 * site + h);
                 }
 #pragma unroll
                 for (int q = 0; q < 2; ++q) {
@@ -1191,16 +1236,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                     if (u >= nunit) break;
                     const int64_t site = unit_site(u);
                     const int h = u & 1, rhs = 16 * h + lrhs;
-                    const int64_t e0 = e_of(site, rhs);
                     const float al = s_alpha[rhs];
-                    float2 rv[8], pv[8];
+                    float2 rv[8];
                     h8_unpack(rw[q][0], rw[q][1], sr[q], rv);
-                    h8_unpack(pw[q][0], pw[q][1], al * sp[q], pv);
                     float mx = 0.f, n2 = 0.f;
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
-                        xv[q][j].x += pv[j].x;
-                        xv[q][j].y += pv[j].y;
                         rv[j] = make_float2(rv[j].x - al * av[q][j].x, rv[j].y - al * av[q][j].y);
                         mx = fmaxf(mx, fmaxf(fabsf(rv[j].x), fabsf(rv[j].y)));
                         n2 += rv[j].x * rv[j].x + rv[j].y * rv[j].y;
@@ -1208,8 +1249,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                     mx = ccg_warp_max(mx);  // also orders every lane's scale read before lane 0's write
                     uint4 w0, w1;
                     h8_pack(rv, mx > 0.f ? __fdividef(1.0f, mx) : 0.f, w0, w1);
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) __stcg(a.x + e0 + j * nrhs, xv[q][j]);
                     uint4* wp = h16_ptr(a.r, site, rhs) + 2 * dh;
                     __stcg(wp, w0);
                     __stcg(wp + 1, w1);
@@ -1221,7 +1260,44 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
             }
             ccg_publish(s_wred, acc, part2, nblk, blin);
         }
-        ok = ccg_grid_barrier(a.bar, a.err, a.spin_limit);
+        // ================= x += alpha_k p_k of the own sites while the other CTAs arrive: x and
+        // p_k's own-site entries are this CTA's alone until p_k's buffer is rewritten in iteration k + 2
+        ccg_barrier_arrive(a.bar, a.err, s_gen, s_ok);
+        {
+            constexpr int kW32 = kThreads / 32;
+            for (int u0 = warp; u0 < nunit; u0 += 2 * kW32) {
+                uint4 pw[2][2];
+                float2 xv[2][8];
+                float sp[2];
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const int u = u0 + q * kW32 < nunit ? u0 + q * kW32 : u0;
+                    const int64_t site = unit_site(u);
+                    const int h = u & 1, rhs = 16 * h + lrhs;
+                    const int64_t e0 = e_of(site, rhs);
+                    const uint4* pp = h16_ptr(pnew, site, rhs) + 2 * dh;
+                    pw[q][0] = __ldcg(pp);
+                    pw[q][1] = __ldcg(pp + 1);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) xv[q][j] = __ldcg(a.x + e0 + j * nrhs);
+                    sp[q] = __ldcg(psnew + 2 * site + h);
+                }
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const int u = u0 + q * kW32;
+                    if (u >= nunit) break;
+                    const int64_t site = unit_site(u);
+                    const int h = u & 1, rhs = 16 * h + lrhs;
+                    const int64_t e0 = e_of(site, rhs);
+                    float2 pv[8];
+                    h8_unpack(pw[q][0], pw[q][1], s_alpha[rhs] * sp[q], pv);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        __stcg(a.x + e0 + j * nrhs, make_float2(xv[q][j].x + pv[j].x, xv[q][j].y + pv[j].y));
+                }
+            }
+        }
+        ok = ccg_barrier_wait(a.bar, a.err, a.spin_limit, s_gen, s_ok);
         if (!ok) break;
         // ================= beta_k and the stop rule (the launched CG's finaliser)
         ccg_sum_partials(part2, nblk, s_sum);

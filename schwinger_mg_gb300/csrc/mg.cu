@@ -82,6 +82,10 @@ struct Level {
     // level 0 with the packed transfers: V in FP32 as pairs over the two spins of a site,
     // [agg][loc][i] = (Re V[loc][0][i], Re V[loc][1][i], Im V[loc][0][i], Im V[loc][1][i])
     float4* V32s = nullptr;
+    // intermediate FP16 levels with the packed transfers: V as output pairs,
+    // [agg][loc][dof][i/2] = (Re V[..][i], Re V[..][i+1], Im V[..][i], Im V[..][i+1]); V32s then pairs
+    // adjacent dofs (2d, 2d+1) of a site instead of the two spins
+    float4* V32o = nullptr;
     // operator of this level (l >= 1): [site][dir][j][i] = block(i, j)
     cx<double>* A64 = nullptr;
     cx<float>* A32 = nullptr;
@@ -98,8 +102,15 @@ inline bool packed_shape0(const Level& L) {
     return L.ax == 4 && L.ay == 4 && (L.nc_next == 8 || L.nc_next == 16 || L.nc_next == 32);
 }
 
-// V32s[(agg, loc)][i] = (Re V[loc][0][i], Re V[loc][1][i], Im V[loc][0][i], Im V[loc][1][i]) in FP32
-// from V64 [agg][loc][spin][i]; np = aggregates x sites per aggregate x nc
+// the intermediate-level shape the packed FP16 transfers serve: 2 x 2 aggregates of 16-dof sites
+// and 8, 16 or 32 coarse dofs
+inline bool packed_shape_c16(const Level& L) {
+    return L.ndof == 16 && L.ax == 2 && L.ay == 2 && (L.nc_next == 8 || L.nc_next == 16 || L.nc_next == 32);
+}
+
+// out[k] = (Re V[2k'][i], Re V[2k'+1][i], Im V[2k'][i], Im V[2k'+1][i]) in FP32 with k = k' nc + i:
+// pairs of adjacent nc-entry rows of V64 [agg][loc][dof][i] (the two spins of a level-0 site, dofs
+// (2d, 2d+1) of a coarse site), or of adjacent entries (nc = 1: output pairs); np = entries / 2
 __global__ void k_pair_spins(const cx<double>* __restrict__ V, float4* __restrict__ out, int64_t np, int nc) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= np) return;
@@ -1387,6 +1398,10 @@ struct CoarseWork {  // per level l >= 1, per precision
     double* mr16_sc = nullptr;
     float* mr16_om = nullptr;
     int res16 = -1;
+    // pre-smoothing x update left to the packed prolongation into this level:
+    // x = (xp_zero ? 0 : x) + sum_{k < xp_n} omega_k r16[k]
+    int xp_n = 0;
+    bool xp_zero = false;
 };
 
 struct smg_mg {
@@ -2127,6 +2142,163 @@ __global__ void __launch_bounds__(128) k_prolong0_ring(const float4* __restrict_
     }
 }
 
+// The transfers of an intermediate FP16 level (coarse_half MR smoother) for 2 x 2 aggregates of
+// 16-dof sites and 32 rhs (lane = rhs): vectors [site][dof][32], FP16 residuals with one scale per
+// site and rhs half, block vectors V[agg][loc][dof][i].
+constexpr int kAggSitesC = 4;
+
+// Restriction out_i = sum_e conj(V[e][i]) r_e of the FP16 residual (the generic kernel with the
+// InHalfC reader): one warp per aggregate, the lane's 64 FP16 inputs in registers, the block vectors
+// (the level's output-pair copy V32o) staged in shared memory by asynchronous copies.
+template <int NC>
+__global__ void __launch_bounds__(NC == 32 ? 64 : 128) k_restrict_c16p(const float4* __restrict__ Vo,
+                                                                       const __half2* __restrict__ r,
+                                                                       const float* __restrict__ rs,
+                                                                       cx<float>* __restrict__ out, TransferGeom t,
+                                                                       int nagg) {
+    constexpr int WPB = NC == 32 ? 2 : 4, NE = kAggSitesC * kC16Dofs, NP = NC / 2;
+    __shared__ float4 s_v[WPB][NE * NP];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int B = blockIdx.x * WPB + w;
+    if (B >= nagg) return;  // whole warps; the kernel has no block barrier
+    const float4* __restrict__ src = Vo + (int64_t)B * NE * NP;
+#pragma unroll 4
+    for (int k = lane; k < NE * NP; k += 32) cp_async16(&s_v[w][k], src + k);
+    const int bx = (B % t.nax) * 2, by = (B / t.nax) * 2;
+    __half2 raw[kAggSitesC][kC16Dofs];
+    float sc[kAggSitesC];
+#pragma unroll
+    for (int l = 0; l < kAggSitesC; ++l) {
+        const int64_t site = (int64_t)(bx + (l & 1)) + (int64_t)t.nx * (by + (l >> 1));
+        sc[l] = __ldg(rs + 2 * site + (lane >> 4));
+        const __half2* __restrict__ rp = r + site * kC16Dofs * 32 + lane;
+#pragma unroll
+        for (int d = 0; d < kC16Dofs; ++d) raw[l][d] = rp[d * 32];
+    }
+    cp_async_wait_all();
+    __syncwarp();
+    f32x2 accr[NP], acci[NP];  // (Re out_i, Re out_i+1), (Im out_i, Im out_i+1)
+#pragma unroll
+    for (int p = 0; p < NP; ++p) accr[p] = acci[p] = 0ull;
+#pragma unroll
+    for (int l = 0; l < kAggSitesC; ++l) {
+#pragma unroll
+        for (int d = 0; d < kC16Dofs; ++d) {
+            const float2 f = __half22float2(raw[l][d]);
+            const float fr = f.x * sc[l], fi = f.y * sc[l];
+            const f32x2 FR = f2_pack(fr, fr), FI = f2_pack(fi, fi), FRn = f2_pack(-fr, -fr);
+            const float4* __restrict__ vrow = &s_v[w][(l * kC16Dofs + d) * NP];
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                const float4 v = vrow[p];
+                const f32x2 VR = f2_pack(v.x, v.y), VI = f2_pack(v.z, v.w);
+                accr[p] = f2_fma(VR, FR, accr[p]);
+                accr[p] = f2_fma(VI, FI, accr[p]);
+                acci[p] = f2_fma(VR, FI, acci[p]);
+                acci[p] = f2_fma(VI, FRn, acci[p]);
+            }
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const float2 re = f2_unpack(accr[p]), im = f2_unpack(acci[p]);
+        out[((int64_t)B * NC + 2 * p) * 32 + lane] = mk(re.x, im.x);
+        out[((int64_t)B * NC + 2 * p + 1) * 32 + lane] = mk(re.y, im.y);
+    }
+}
+
+// Prolongation into an intermediate FP16 level with its pre-smoothing x pass folded in:
+//   x(site, dof) = [x] + sum_{k < n} omega_k r_k + sum_i V[loc][dof][i] c_i
+// (k_prolong_agg after k_c16_xupdate).  One block of eight warps per aggregate, warp w on site w / 2
+// and dofs 8 (w % 2) .. + 7; the block vectors (the level's dof-paired copy V32s) and the coarse
+// values staged by asynchronous copies; the lane's x values held as pairs over dofs (2d, 2d + 1).
+template <int NC>
+__global__ void __launch_bounds__(256) k_prolong_c16p(const float4* __restrict__ Vs, const cx<float>* __restrict__ cin,
+                                                      cx<float>* __restrict__ x, TransferGeom t, C16Ring ring, int n,
+                                                      const float2* __restrict__ om, int accumulate) {
+    constexpr int DP = 4;  // dof pairs per warp
+    __shared__ float4 s_v[kAggSitesC * (kC16Dofs / 2) * NC];
+    __shared__ float2 s_c[NC * 32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int B = blockIdx.x, loc = w >> 1, dh = w & 1;
+    const float4* __restrict__ vsrc = Vs + (int64_t)B * kAggSitesC * (kC16Dofs / 2) * NC;
+#pragma unroll
+    for (int k = threadIdx.x; k < kAggSitesC * (kC16Dofs / 2) * NC; k += 256) cp_async16(&s_v[k], vsrc + k);
+    const float2* __restrict__ c2 = reinterpret_cast<const float2*>(cin) + (int64_t)B * NC * 32;
+#pragma unroll
+    for (int k = threadIdx.x; k < NC * 32; k += 256) cp_async8(&s_c[k], c2 + k);
+    const int64_t site = (int64_t)((B % t.nax) * 2 + (loc & 1)) + (int64_t)t.nx * ((B / t.nax) * 2 + (loc >> 1));
+    const int64_t row0 = site * kC16Dofs + 8 * dh;  // first (site, dof) row of the warp
+    f32x2 xr[DP], xi[DP];
+    float2* __restrict__ px = reinterpret_cast<float2*>(x);
+    if (accumulate) {
+#pragma unroll
+        for (int p = 0; p < DP; ++p) {
+            const float2 a = px[(row0 + 2 * p) * 32 + lane], b = px[(row0 + 2 * p + 1) * 32 + lane];
+            xr[p] = f2_pack(a.x, b.x);
+            xi[p] = f2_pack(a.y, b.y);
+        }
+    } else {
+#pragma unroll
+        for (int p = 0; p < DP; ++p) xr[p] = xi[p] = 0ull;
+    }
+    for (int k0 = 0; k0 < n; k0 += kRingChunk) {
+        __half2 raw[kRingChunk][2 * DP];
+        float scl[kRingChunk];
+        float2 o[kRingChunk];
+#pragma unroll
+        for (int j = 0; j < kRingChunk; ++j) {
+            if (k0 + j < n) {
+                const int k = k0 + j;
+                o[j] = __ldg(om + k * 32 + lane);
+                scl[j] = __ldg(ring.s[k] + 2 * site + (lane >> 4));
+                const __half2* __restrict__ rk = ring.r[k] + row0 * 32 + lane;
+#pragma unroll
+                for (int d = 0; d < 2 * DP; ++d) raw[j][d] = rk[d * 32];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kRingChunk; ++j) {
+            if (k0 + j < n) {
+                const float wr = o[j].x * scl[j], wi = o[j].y * scl[j];
+                const f32x2 WR = f2_pack(wr, wr), WI = f2_pack(wi, wi), WIn = f2_pack(-wi, -wi);
+#pragma unroll
+                for (int p = 0; p < DP; ++p) {
+                    const float2 a = __half22float2(raw[j][2 * p]), b = __half22float2(raw[j][2 * p + 1]);
+                    const f32x2 RR = f2_pack(a.x, b.x), RI = f2_pack(a.y, b.y);
+                    xr[p] = f2_fma(WR, RR, xr[p]);  // Re (w r) = w_r r_r - w_i r_i
+                    xr[p] = f2_fma(WIn, RI, xr[p]);
+                    xi[p] = f2_fma(WR, RI, xi[p]);  // Im (w r) = w_r r_i + w_i r_r
+                    xi[p] = f2_fma(WI, RR, xi[p]);
+                }
+            }
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const float4* __restrict__ vw = s_v + (loc * (kC16Dofs / 2) + DP * dh) * NC;
+#pragma unroll
+    for (int i = 0; i < NC; ++i) {
+        const float2 c = s_c[i * 32 + lane];
+        const f32x2 CR = f2_pack(c.x, c.x), CI = f2_pack(c.y, c.y), CIn = f2_pack(-c.y, -c.y);
+#pragma unroll
+        for (int p = 0; p < DP; ++p) {
+            const float4 v = vw[p * NC + i];
+            const f32x2 VR = f2_pack(v.x, v.y), VI = f2_pack(v.z, v.w);
+            xr[p] = f2_fma(VR, CR, xr[p]);
+            xr[p] = f2_fma(VI, CIn, xr[p]);
+            xi[p] = f2_fma(VR, CI, xi[p]);
+            xi[p] = f2_fma(VI, CR, xi[p]);
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < DP; ++p) {
+        const float2 re = f2_unpack(xr[p]), im = f2_unpack(xi[p]);
+        px[(row0 + 2 * p) * 32 + lane] = make_float2(re.x, im.x);
+        px[(row0 + 2 * p + 1) * 32 + lane] = make_float2(re.y, im.y);
+    }
+}
+
 // launch shape of the pair kernels: (nrhs / 2 lanes, 256 / lanes sites)
 dim3 pair_block(int nrhs) { return dim3(nrhs / 2, 512 / nrhs); }
 dim3 pair_grid(int nsites, int nrhs) { return dim3((nsites + 512 / nrhs - 1) / (512 / nrhs)); }
@@ -2220,14 +2392,19 @@ smg_status smooth_fine_half(smg_mg* mg, smg_field* x, const smg_field* b, int ni
 TransferGeom transfer_geom(const smg_mg* mg, int l, int nrhs);
 dim3 transfer_block(int nrhs);
 
-// the level-0 transfers with packed FMAs (k_restrict0_h, k_prolong0_ring) serve the FP16 smoother
-// with 4 x 4 aggregates, 8, 16 or 32 coarse dofs and whole tiles of 32 rhs; SMG_TRANSFER0_PACKED=0
-// keeps the generic kernels and a separate x pass
-bool transfer0_packed(const smg_mg* mg) {
+// the transfers with packed FMAs: SMG_TRANSFER_PACKED=0 keeps the generic kernels and separate x passes
+bool transfer_packed_on() {
     static const bool on = [] {
-        const char* e = std::getenv("SMG_TRANSFER0_PACKED");
+        const char* e = std::getenv("SMG_TRANSFER_PACKED");
         return !(e && std::atoi(e) == 0);
     }();
+    return on;
+}
+
+// the level-0 transfers with packed FMAs (k_restrict0_h, k_prolong0_ring) serve the FP16 smoother
+// with 4 x 4 aggregates, 8, 16 or 32 coarse dofs and whole tiles of 32 rhs
+bool transfer0_packed(const smg_mg* mg) {
+    const bool on = transfer_packed_on();
     const Level& L = mg->lv[0];
     return on && mg->lv.size() > 1 && packed_shape0(L) && mg->work_nrhs % 32 == 0 && mg->f_r &&
            mg->f_r->prec == SMG_F16 && L.V32 && L.V32s;
@@ -2417,7 +2594,7 @@ smg_status smooth_fine(smg_mg* mg, smg_field* x, const smg_field* b, int niter, 
 // (or b) in FP16, then per step A r_k in FP16 with <A r_k, r_k>, ||A r_k||^2 and omega_k from the
 // tensor-core apply, r_{k+1} = r_k - omega_k A r_k, and x += sum_k omega_k r_k once at the end (x and
 // all arithmetic FP32).  The final residual stays in the ring slot res16 for the restriction.
-smg_status mr_coarse_half(smg_mg* mg, int l, void* x, const void* b, int niter, bool x_is_zero) {
+smg_status mr_coarse_half(smg_mg* mg, int l, void* x, const void* b, int niter, bool x_is_zero, bool defer_x = false) {
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[l];
     CoarseWork& w = mg->cw[l];
@@ -2441,7 +2618,10 @@ smg_status mr_coarse_half(smg_mg* mg, int l, void* x, const void* b, int niter, 
         count_launch(ctx);
         SMG_CHECK_LAUNCH(ctx);
     }
-    if (niter > 0) {
+    if (defer_x) {  // the packed prolongation into this level adds the steps (k_prolong_c16p)
+        w.xp_n = niter;
+        w.xp_zero = x_is_zero;
+    } else if (niter > 0) {
         C16Ring ring{};
         for (int k = 0; k < niter; ++k) {
             ring.r[k] = (const __half2*)w.r16[k];
@@ -2484,6 +2664,61 @@ smg_status restrict_c16(smg_mg* mg, int l, void* out) {
     else if (nc == 16) SMG_RC(16);
     else SMG_RC(32);
 #undef SMG_RC
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+// the packed transfers of an intermediate FP16 level (k_restrict_c16p, k_prolong_c16p)
+bool transfer_c16_packed(const smg_mg* mg, int l) {
+    const Level& L = mg->lv[l];
+    return transfer_packed_on() && l + 1 < (int)mg->lv.size() && packed_shape_c16(L) && L.V32s && L.V32o &&
+           !mg->cw[l].r16.empty() && mr16_level(mg, l, mg->work_nrhs, SMG_F32);
+}
+
+smg_status restrict_c16_packed(smg_mg* mg, int l, void* out) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[l];
+    CoarseWork& w = mg->cw[l];
+    const int nagg = mg->lv[l + 1].nsites;
+    const TransferGeom t = transfer_geom(mg, l, 32);
+    const __half2* r = (const __half2*)w.r16[w.res16];
+    const float* rs = w.r16s[w.res16];
+    cx<float>* o = (cx<float>*)out;
+    if (L.nc_next == 8)
+        k_restrict_c16p<8><<<(nagg + 3) / 4, 128, 0, ctx->stream>>>(L.V32o, r, rs, o, t, nagg);
+    else if (L.nc_next == 16)
+        k_restrict_c16p<16><<<(nagg + 3) / 4, 128, 0, ctx->stream>>>(L.V32o, r, rs, o, t, nagg);
+    else
+        k_restrict_c16p<32><<<(nagg + 1) / 2, 64, 0, ctx->stream>>>(L.V32o, r, rs, o, t, nagg);
+    count_launch(ctx);
+    SMG_CHECK_LAUNCH(ctx);
+    return SMG_OK;
+}
+
+// x = (pending x pass of level l) + P e, consuming cw[l].xp_*
+smg_status prolong_c16_packed(smg_mg* mg, int l, const void* coarse, void* x) {
+    smg_context* ctx = mg->ctx;
+    const Level& L = mg->lv[l];
+    CoarseWork& w = mg->cw[l];
+    const int nagg = mg->lv[l + 1].nsites;
+    const TransferGeom t = transfer_geom(mg, l, 32);
+    C16Ring ring{};
+    for (int k = 0; k < w.xp_n; ++k) {
+        ring.r[k] = (const __half2*)w.r16[k];
+        ring.s[k] = w.r16s[k];
+    }
+    const float2* om = (const float2*)w.mr16_om;
+    const int acc = w.xp_zero ? 0 : 1;
+    const cx<float>* c = (const cx<float>*)coarse;
+    cx<float>* xp = (cx<float>*)x;
+    if (L.nc_next == 8)
+        k_prolong_c16p<8><<<nagg, 256, 0, ctx->stream>>>(L.V32s, c, xp, t, ring, w.xp_n, om, acc);
+    else if (L.nc_next == 16)
+        k_prolong_c16p<16><<<nagg, 256, 0, ctx->stream>>>(L.V32s, c, xp, t, ring, w.xp_n, om, acc);
+    else
+        k_prolong_c16p<32><<<nagg, 256, 0, ctx->stream>>>(L.V32s, c, xp, t, ring, w.xp_n, om, acc);
+    w.xp_n = 0;
     count_launch(ctx);
     SMG_CHECK_LAUNCH(ctx);
     return SMG_OK;
@@ -2753,10 +2988,17 @@ smg_status cycle_coarse(smg_mg* mg, int l, void* x, const void* b) {
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[l];
     const int nrhs = mg->work_nrhs;
-    SMG_TRY(smooth_coarse<T>(mg, l, x, b, mg->p.pre_smooth, true));
+    // packed FP16-level transfers: the pre-smoothing x pass is folded into the prolongation
+    const bool packed = std::is_same<T, float>::value && transfer_c16_packed(mg, l);
+    if (packed)
+        SMG_TRY(mr_coarse_half(mg, l, x, b, mg->p.pre_smooth, true, true));
+    else
+        SMG_TRY(smooth_coarse<T>(mg, l, x, b, mg->p.pre_smooth, true));
     // residual of the smoothed x is in cw[l].r (or, FP16, in the ring slot cw[l].res16)
     CoarseWork& nw = mg->cw[l + 1];
-    if (std::is_same<T, float>::value && !mg->cw[l].r16.empty() && mr16_level(mg, l, nrhs, SMG_F32))
+    if (packed)
+        SMG_TRY(restrict_c16_packed(mg, l, nw.b));
+    else if (std::is_same<T, float>::value && !mg->cw[l].r16.empty() && mr16_level(mg, l, nrhs, SMG_F32))
         SMG_TRY(restrict_c16(mg, l, nw.b));
     else
         SMG_TRY(restrict_to<T>(mg, l, mg->cw[l].r, nw.b));
@@ -2773,7 +3015,10 @@ smg_status cycle_coarse(smg_mg* mg, int l, void* x, const void* b) {
         k_vadd<T><<<blocks_for(nn), 256, 0, ctx->stream>>>((cx<T>*)nw.x, (const cx<T>*)nw.e, nn);
         count_launch(ctx);
     }
-    SMG_TRY(prolong_to<T>(mg, l, nw.x, x, 1));
+    if (packed)
+        SMG_TRY(prolong_c16_packed(mg, l, nw.x, x));
+    else
+        SMG_TRY(prolong_to<T>(mg, l, nw.x, x, 1));
     (void)L;
     return smooth_coarse<T>(mg, l, x, b, mg->p.post_smooth, false);
 }
@@ -2936,10 +3181,16 @@ smg_status make_f32_copies(smg_mg* mg) {
             if (!L.V32) SMG_CUDA(ctx, cudaMalloc(&L.V32, n * sizeof(cx<float>)));
             k_cvt_flat<float, double><<<blocks_for(n), 256, 0, ctx->stream>>>(L.V64, L.V32, n);
             count_launch(ctx);
-            if (l == 0 && mg->p.smoother_half && packed_shape0(L)) {
-                const int64_t np = n / 2;
+            const int64_t np = n / 2;
+            if ((l == 0 && mg->p.smoother_half && packed_shape0(L)) ||
+                (l >= 1 && mg->p.coarse_half && packed_shape_c16(L))) {
                 if (!L.V32s) SMG_CUDA(ctx, cudaMalloc(&L.V32s, np * sizeof(float4)));
                 k_pair_spins<<<blocks_for(np), 256, 0, ctx->stream>>>(L.V64, L.V32s, np, L.nc_next);
+                count_launch(ctx);
+            }
+            if (l >= 1 && mg->p.coarse_half && packed_shape_c16(L)) {
+                if (!L.V32o) SMG_CUDA(ctx, cudaMalloc(&L.V32o, np * sizeof(float4)));
+                k_pair_spins<<<blocks_for(np), 256, 0, ctx->stream>>>(L.V64, L.V32o, np, 1);
                 count_launch(ctx);
             }
         }
@@ -3176,7 +3427,7 @@ smg_status rebuild_operators(smg_mg* mg) {
 
 void destroy_levels(smg_mg* mg) {
     for (auto& L : mg->lv) {
-        for (void* p : {(void*)L.V64, (void*)L.V32, (void*)L.V32s, (void*)L.A64, (void*)L.A32, L.Atc})
+        for (void* p : {(void*)L.V64, (void*)L.V32, (void*)L.V32s, (void*)L.V32o, (void*)L.A64, (void*)L.A32, L.Atc})
             if (p) cudaFree(p);
     }
     mg->lv.clear();

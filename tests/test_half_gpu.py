@@ -110,7 +110,9 @@ lat = smg.Lattice(L)
 D = smg.DiracOp(lat, smg.GaugeField(lat, smg.gauge_normal(L, 6.0, 43)), -0.05, 1.0, 1.0, 0.0)
 nvec = int(sys.argv[3]) if len(sys.argv) > 3 else 16
 chiral = len(sys.argv) > 4 and sys.argv[4] == "1"
-mg = smg.MGHierarchy(D, smg.mg_params(3, 4, nvec, blocks=[(4, 4), (2, 2)], chiral_split=chiral, null_iters=4,
+nvec1 = int(sys.argv[5]) if len(sys.argv) > 5 else nvec
+mg = smg.MGHierarchy(D, smg.mg_params(3, 4, nvec, blocks=[(4, 4), (2, 2)], n_vecs=[nvec, nvec1],
+                                       chiral_split=chiral, null_iters=4,
                                        pre_smooth=4, post_smooth=4, w_cycle=False, coarse_max_iter=20,
                                        coarse_tol=5e-2, precision="f32", seed=11, smoother_half=True,
                                        coarse_half=True))
@@ -144,15 +146,20 @@ def test_persistent_coarsest_cg_matches_per_iteration_kernels(tmp_path):
     assert abs(int(pst["iters"]) - int(per["iters"])) <= 2
 
 
-@pytest.mark.parametrize("nvec,chiral", [(16, "0"), (8, "0"), (16, "1")])
-def test_packed_level0_transfers_match_generic_kernels(tmp_path, nvec, chiral):
-    """The level-0 transfers with packed FP32 FMAs (k_restrict0_h; k_prolong0_ring with the
-    pre-smoothing x pass folded in) against the generic aggregate kernels and a separate x pass, each
-    in its own process, for 8, 16 and (chirally split) 32 coarse dofs: the same arithmetic in FP32 up
+@pytest.mark.parametrize("nvec,chiral,nvec1", [(16, "0", 16), (8, "0", 8), (16, "1", 16), (16, "0", 8),
+                                               (16, "0", 32)])
+def test_packed_transfers_match_generic_kernels(tmp_path, nvec, chiral, nvec1):
+    """The transfers with packed FP32 FMAs (level 0: k_restrict0_h, k_prolong0_ring; level 1:
+    k_restrict_c16p, k_prolong_c16p; the prolongations with the pre-smoothing x pass folded in)
+    against the generic aggregate kernels and separate x passes, each
+    in its own process, for 8, 16 and (chirally split) 32 coarse dofs at level 0 and 8, 16 and 32 at
+    level 1 (the level-1 kernels serve 16-dof sites, so with nvec 16 unsplit): the same arithmetic in FP32 up
     to the order of the sums, so the cycles agree to the FP16 rounding downstream, and the solves
-    reach 1e-10 in as many iterations up to one."""
-    gen = _ccg_run(tmp_path, "generic", True, str(nvec), chiral, SMG_TRANSFER0_PACKED="0")
-    pk = _ccg_run(tmp_path, "packed", True, str(nvec), chiral, SMG_TRANSFER0_PACKED="1")
-    assert np.linalg.norm(pk["c"] - gen["c"]) / np.linalg.norm(gen["c"]) < 1e-2
+    reach 1e-10 in as many iterations up to 3 % (a flexible solve with a preconditioner that differs
+    in its last bits: 110 against 112 iterations with 8 null vectors)."""
+    args = (str(nvec), chiral, str(nvec1))
+    gen = _ccg_run(tmp_path, "generic", True, *args, SMG_TRANSFER_PACKED="0")
+    pk = _ccg_run(tmp_path, "packed", True, *args, SMG_TRANSFER_PACKED="1")
+    assert np.linalg.norm(pk["c"] - gen["c"]) / np.linalg.norm(gen["c"]) < 3e-3  # measured <= 5.1e-4
     assert float(pk["res"]) < 1e-10 and float(gen["res"]) < 1e-10
-    assert abs(int(pk["iters"]) - int(gen["iters"])) <= 1
+    assert abs(int(pk["iters"]) - int(gen["iters"])) <= max(1, int(0.03 * int(gen["iters"])))
