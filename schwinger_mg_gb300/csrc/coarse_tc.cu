@@ -1208,17 +1208,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
             s_alpha[tid] = al;
         }
         __syncthreads();
-        // ================= r update of the own sites: two units per step, both units' loads first
-        // (x moves in the second barrier's wait, below)
+        // ================= r update of the own sites: kUq units per step, all their loads first (x
+        // moves in the second barrier's wait, below)
         {
             float acc[2] = {0.f, 0.f};
-            constexpr int kW32 = kThreads / 32;
-            for (int u0 = warp; u0 < nunit; u0 += 2 * kW32) {
-                uint4 rw[2][2];
-                float2 av[2][8];
-                float sr[2];
+            constexpr int kW32 = kThreads / 32, kUq = 3;
+            for (int u0 = warp; u0 < nunit; u0 += kUq * kW32) {
+                uint4 rw[kUq][2];
+                float2 av[kUq][8];
+                float sr[kUq];
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
+                for (int q = 0; q < kUq; ++q) {
                     const int u = u0 + q * kW32 < nunit ? u0 + q * kW32 : u0;
                     const int64_t site = unit_site(u);
                     const int h = u & 1, rhs = 16 * h + lrhs;
@@ -1231,7 +1231,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                     sr[q] = __ldcg(a.rs + 2 * site + h);
                 }
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
+                for (int q = 0; q < kUq; ++q) {
                     const int u = u0 + q * kW32;
                     if (u >= nunit) break;
                     const int64_t site = unit_site(u);
@@ -1264,13 +1264,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
         // p_k's own-site entries are this CTA's alone until p_k's buffer is rewritten in iteration k + 2
         ccg_barrier_arrive(a.bar, a.err, s_gen, s_ok);
         {
-            constexpr int kW32 = kThreads / 32;
-            for (int u0 = warp; u0 < nunit; u0 += 2 * kW32) {
-                uint4 pw[2][2];
-                float2 xv[2][8];
-                float sp[2];
+            constexpr int kW32 = kThreads / 32, kXq = 3;
+            for (int u0 = warp; u0 < nunit; u0 += kXq * kW32) {
+                uint4 pw[kXq][2];
+                float2 xv[kXq][8];
+                float sp[kXq];
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
+                for (int q = 0; q < kXq; ++q) {
                     const int u = u0 + q * kW32 < nunit ? u0 + q * kW32 : u0;
                     const int64_t site = unit_site(u);
                     const int h = u & 1, rhs = 16 * h + lrhs;
@@ -1283,7 +1283,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_ccg_tc(CcgTcArgs a) {
                     sp[q] = __ldcg(psnew + 2 * site + h);
                 }
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
+                for (int q = 0; q < kXq; ++q) {
                     const int u = u0 + q * kW32;
                     if (u >= nunit) break;
                     const int64_t site = unit_site(u);
