@@ -331,8 +331,8 @@ DSLASH_F32_L512_DRAM_BYTES = 140.034048e6 + 98.370048e6
 SMOOTHER_D_L512_DRAM_BYTES = 74.627072e6 + 31.32672e6
 # the persistent coarsest CG of the same workload (one solve of 20 iterations): ncu dram read + write and
 # lts__t_bytes (profiles/coarsest_cg_tc_L512_64x64_32rhs.md)
-CCG_L512_DRAM_BYTES = 548.350976e6 + 466.022912e6
-CCG_L512_L2_BYTES = 6.19010224e9
+CCG_L512_DRAM_BYTES = 338.875904e6 + 417.792768e6
+CCG_L512_L2_BYTES = 5.71516448e9
 
 
 def coarse_kernel_name(c, L, nrhs):
