@@ -3439,9 +3439,13 @@ void destroy_levels(smg_mg* mg) {
 
 namespace {
 
+// The captured cycle goes; its input and output fields stay (a solver may hold them as its own
+// residual and preconditioned vector, smg_mg_graph_io) until the hierarchy goes or the shape changes.
 void drop_graph(smg_mg* mg) {
     if (mg->g_exec) cudaGraphExecDestroy(mg->g_exec);
     mg->g_exec = nullptr;
+}
+void free_graph_io(smg_mg* mg) {
     smg_field_destroy(mg->g_in);
     smg_field_destroy(mg->g_out);
     mg->g_in = mg->g_out = nullptr;
@@ -3455,8 +3459,13 @@ smg_status capture_cycle(smg_mg* mg, const smg_field* proto) {
     smg_context* ctx = mg->ctx;
     drop_graph(mg);
     SMG_TRY(ensure_work(mg, proto->nrhs, proto->prec));
-    SMG_TRY(smg_field_alloc_like(proto, proto->prec, &mg->g_in));
-    SMG_TRY(smg_field_alloc_like(proto, proto->prec, &mg->g_out));
+    const bool keep_io = mg->g_in && mg->g_out && mg->g_in->g.L == proto->g.L && mg->g_in->nrhs == proto->nrhs &&
+                         mg->g_in->prec == proto->prec;
+    if (!keep_io) {
+        free_graph_io(mg);
+        SMG_TRY(smg_field_alloc_like(proto, proto->prec, &mg->g_in));
+        SMG_TRY(smg_field_alloc_like(proto, proto->prec, &mg->g_out));
+    }
     SMG_TRY(smg_reduce_reserve(ctx, (size_t)kMaxReduceBlocks * proto->nrhs * 3 + 1024));
     SMG_TRY(smg_host_stage_reserve(ctx, 64));
     SMG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -3491,16 +3500,45 @@ smg_status cycle_graph(smg_mg* mg, const smg_field* b, smg_field* x) {
     const bool stale = !mg->g_exec || !mg->g_in || mg->g_in->nrhs != b->nrhs || mg->g_in->prec != b->prec ||
                        mg->work_nrhs != b->nrhs || mg->work_prec != b->prec || mg->g_work_gen != mg->work_gen;
     if (stale) SMG_TRY(capture_cycle<T>(mg, b));
-    SMG_CUDA(ctx, cudaMemcpyAsync(mg->g_in->data, b->data, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    // a caller that holds the graph's own input and output fields (smg_mg_graph_io) needs no copies
+    if (b != mg->g_in)
+        SMG_CUDA(ctx, cudaMemcpyAsync(mg->g_in->data, b->data, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     SMG_CUDA(ctx, cudaGraphLaunch(mg->g_exec, ctx->stream));
     ctx->launches += mg->g_launches;
-    SMG_CUDA(ctx, cudaMemcpyAsync(x->data, mg->g_out->data, x->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (x != mg->g_out)
+        SMG_CUDA(ctx, cudaMemcpyAsync(x->data, mg->g_out->data, x->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     return SMG_OK;
 }
 
 }  // namespace
 
-// ---- internal entry used by the GCR solver
+// ---- internal entries used by the GCR solver
+// The captured cycle's input and output fields for right-hand sides shaped like proto (capturing the
+// cycle first if needed), or null when the hierarchy runs its cycle without a graph: a solver that
+// keeps its residual in *in and its preconditioned vector in *out saves two field copies per cycle.
+// They stay valid until the hierarchy is destroyed or runs a cycle of another shape or precision.
+smg_status smg_mg_graph_io(smg_mg* mg, const smg_field* proto, smg_field** in, smg_field** out) {
+    *in = *out = nullptr;
+    if (!mg->use_graph || (proto->prec != SMG_F64 && proto->prec != SMG_F32)) return SMG_OK;
+    const bool stale = !mg->g_exec || !mg->g_in || mg->g_in->nrhs != proto->nrhs || mg->g_in->prec != proto->prec ||
+                       mg->g_in->g.L != proto->g.L || mg->work_nrhs != proto->nrhs || mg->work_prec != proto->prec ||
+                       mg->g_work_gen != mg->work_gen;
+    if (stale) {
+        const smg_status st =
+            proto->prec == SMG_F64 ? capture_cycle<double>(mg, proto) : capture_cycle<float>(mg, proto);
+        if (st != SMG_OK) {
+            if (st != SMG_DEVICE_ERROR || mg->g_exec) return st;
+            cudaGetLastError();  // capture failed: the cycle runs kernel by kernel
+            drop_graph(mg);
+            mg->use_graph = false;
+            return SMG_OK;
+        }
+    }
+    *in = mg->g_in;
+    *out = mg->g_out;
+    return SMG_OK;
+}
+
 smg_status smg_mg_apply_internal(smg_mg* mg, const smg_field* b, smg_field* x) {
     if (b->prec != SMG_F64 && b->prec != SMG_F32)
         return smg_fail(mg->ctx, SMG_UNSUPPORTED, "MG cycle on F16 fields");
@@ -3875,6 +3913,7 @@ SMG_API smg_status smg_mg_destroy(smg_mg* mg) {
     if (!mg) return SMG_OK;
     cudaStreamSynchronize(mg->ctx->stream);
     drop_graph(mg);
+    free_graph_io(mg);
     free_work(mg);
     destroy_levels(mg);
     smg_defl_free(mg->defl);

@@ -349,6 +349,7 @@ SMG_API smg_status smg_cg_solve(smg_dirac* d, const smg_field* rhs, smg_field* x
 // per iteration to apply the stop rule.
 // =====================================================================
 smg_status smg_mg_apply_internal(smg_mg* mg, const smg_field* b, smg_field* x);
+smg_status smg_mg_graph_io(smg_mg* mg, const smg_field* proto, smg_field** in, smg_field** out);
 smg_precision smg_mg_precision(const smg_mg* mg);
 smg_status smg_mg_check_device_error(smg_mg* mg);
 
@@ -560,13 +561,30 @@ struct GcrOut {
 template <typename T>
 smg_status gcr_core(smg_dirac* d, smg_mg* mg, GcrWs<T>& ws, const smg_field* b, smg_field* x, int max_iter, double tol,
                     int trunc, int ref_coeff, GcrOut& out) {
+    // the residual and the preconditioned vector live in the captured cycle's own input and output
+    // fields when the hierarchy has one, so a cycle copies neither (two 134 MB copies per cycle at
+    // L = 512, 32 RHS in FP32)
+    smg_field* rf = ws.r;
+    smg_field* zf = ws.z;
+    static const bool graph_io = [] {
+        const char* e = std::getenv("SMG_GRAPH_IO");
+        return !(e && std::atoi(e) == 0);
+    }();
+    if (mg && graph_io) {
+        smg_field *gi = nullptr, *go = nullptr;
+        SMG_TRY(smg_mg_graph_io(mg, ws.r, &gi, &go));
+        if (gi && go) {
+            rf = gi;
+            zf = go;
+        }
+    }
     smg_context* ctx = d->ctx;
     const int nrhs = b->nrhs, V = b->g.V;
     GcrScalars& sc = ws.sc;
     sc.tol2 = tol * tol;
     SMG_CUDA(ctx, cudaMemsetAsync(x->data, 0, x->bytes, ctx->stream));
-    SMG_CUDA(ctx, cudaMemcpyAsync(ws.r->data, b->data, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-    SMG_TRY(reduce_into<T>(ctx, fv<T>(ws.r), nullptr, VR_NORM, sc.rr));
+    SMG_CUDA(ctx, cudaMemcpyAsync(rf->data, b->data, b->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    SMG_TRY(reduce_into<T>(ctx, fv<T>(rf), nullptr, VR_NORM, sc.rr));
     SMG_CUDA(ctx, cudaMemcpyAsync(sc.bnorm2, sc.rr, nrhs * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
     out.rr.assign(nrhs, 0.0);
     out.b2.assign(nrhs, 0.0);
@@ -594,13 +612,13 @@ smg_status gcr_core(smg_dirac* d, smg_mg* mg, GcrWs<T>& ws, const smg_field* b, 
                                       ctx->stream));
         // z = M^-1 r
         if (!mg)
-            SMG_CUDA(ctx, cudaMemcpyAsync(ws.z->data, ws.r->data, ws.r->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+            SMG_CUDA(ctx, cudaMemcpyAsync(zf->data, rf->data, rf->bytes, cudaMemcpyDeviceToDevice, ctx->stream));
         else
-            SMG_TRY(smg_mg_apply_internal(mg, ws.r, ws.z));
+            SMG_TRY(smg_mg_apply_internal(mg, rf, zf));
         // p = z, Ap = A z, orthogonalised against the stored directions
         smg_field* p = ws.P[work];
         smg_field* Ap = ws.AP[work];
-        SMG_TRY(apply_A<T>(d, ws.z, ws.tmp, ws.Az));
+        SMG_TRY(apply_A<T>(d, zf, ws.tmp, ws.Az));
         const int nring = (int)ring.size();
         // <AP_i, Az> for every stored direction, kDotChunk per pass over Az
         for (int c0 = 0; c0 < nring; c0 += kDotChunk) {
@@ -628,15 +646,15 @@ smg_status gcr_core(smg_dirac* d, smg_mg* mg, GcrWs<T>& ws, const smg_field* b, 
             }
             const bool first = c0 == 0, last = c0 + kOrthChunk >= nring;
             k_gcr_orth_all<T><<<rl.grid, rl.block, 0, ctx->stream>>>(
-                fv<T>(p), (cx<T>*)Ap->data, first ? (const cx<T>*)ws.z->data : (const cx<T>*)p->data,
-                first ? (const cx<T>*)ws.Az->data : (const cx<T>*)Ap->data, (const cx<T>*)ws.r->data, op, ns, c0,
+                fv<T>(p), (cx<T>*)Ap->data, first ? (const cx<T>*)zf->data : (const cx<T>*)p->data,
+                first ? (const cx<T>*)ws.Az->data : (const cx<T>*)Ap->data, (const cx<T>*)rf->data, op, ns, c0,
                 ws.dots, 2 * ws.nbuf, ref_coeff, last ? 1 : 0, ctx->red.partials, ctx->red.tickets,
                 ws.apr_of(work));
             count_launch(ctx);
             SMG_CHECK_LAUNCH(ctx);
         }
         sc.apr3 = ws.apr_of(work);
-        k_gcr_update<T><<<rl.grid, rl.block, 0, ctx->stream>>>(sc, fv<T>(x), (cx<T>*)ws.r->data,
+        k_gcr_update<T><<<rl.grid, rl.block, 0, ctx->stream>>>(sc, fv<T>(x), (cx<T>*)rf->data,
                                                                (const cx<T>*)p->data, (const cx<T>*)Ap->data,
                                                                ctx->red.partials, ctx->red.tickets);
         count_launch(ctx);
