@@ -97,7 +97,14 @@ class Clocks:
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
                  "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
-            time.sleep(0.25)  # first sample before the timed work starts
+            # the sampler's start-up (NVML initialisation) stays out of the timed region: wait for its
+            # first sample (up to 3 s), then a little more
+            t_end = time.monotonic() + 3.0
+            while time.monotonic() < t_end and self.proc.poll() is None:
+                if self.path.stat().st_size > 0:
+                    break
+                time.sleep(0.02)
+            time.sleep(0.25)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
