@@ -92,8 +92,6 @@ constexpr int kNumBars = kBarFinal + 1;
 constexpr int kBarOffset = kRingBytes + kLinkBytes;           // A-tile over-read (M = 128) lands in the link ring
 constexpr int kMiscOffset = kBarOffset + kNumBars * 8;
 constexpr int kThreads = 384;                                 // 12 warps (roles below)
-constexpr int kEpiHalves = 2;                                 // persistent CG: epilogue warp pairs
-constexpr int kEpiSites = kW / kEpiHalves;                    // persistent CG: output sites per pair and row
 // the apply: three epilogue warp pairs (0, 1), (4, 5), (8, 9) take output sites 0-2, 3-5, 6-7 of a row;
 // the link producer and the MMA issuer are warps 10 and 11
 constexpr int kApGroups = 3;
