@@ -2242,7 +2242,9 @@ __global__ void __launch_bounds__(256) k_prolong_c16p(const float4* __restrict__
 #pragma unroll
         for (int p = 0; p < DP; ++p) xr[p] = xi[p] = 0ull;
     }
-    for (int k0 = 0; k0 < n; k0 += kRingChunk) {
+#pragma unroll
+    for (int k0 = 0; k0 < kC16MaxSteps; k0 += kRingChunk) {  // compile-time ring indices
+        if (k0 >= n) break;
         __half2 raw[kRingChunk][2 * DP];
         float scl[kRingChunk];
         float2 o[kRingChunk];
