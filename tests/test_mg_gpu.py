@@ -303,3 +303,24 @@ def test_config2_settings_match_oracle_iterations(smg_gpu, port):
     _, it_o, res_o, _ = port.mgN_gcr(po, U, b, 1000, 1e-10, 20)
     assert r.status == 0 and r.true_residual < 1e-10
     assert abs(r.iterations - it_o) <= 2
+
+
+def test_gcr_in_the_cycle_graph_fields_across_rhs_counts(smg_gpu):
+    """The GCR keeps its residual and preconditioned vector in the captured cycle's own input and output
+    fields: solves of 8, then 32, then again 8 right-hand sides on one FP32 hierarchy recapture the cycle
+    for each count, each reaches a true residual of 1e-10, and the two 8-RHS solves agree bit for bit."""
+    L = 32
+    lat = smg_gpu.Lattice(L)
+    D = smg_gpu.DiracOp(lat, smg_gpu.GaugeField(lat, smg_gpu.gauge_normal(L, 6.0, 17)), -0.05, 1.0, 1.0, 0.0)
+    mg = smg_gpu.MGHierarchy(D, smg_gpu.mg_params(2, 4, 8, null_iters=3, pre_smooth=4, post_smooth=4,
+                                                  w_cycle=False, coarse_tol=1e-6, precision="f32", seed=3))
+    B32 = np.stack([smg_gpu.random_vec(lat.ndof, 200 + j) for j in range(32)])
+    r8a = smg_gpu.fcg_solve_mg(D, lat.ndof, B32[:8], mg, 300, 1e-10, 10)
+    r32 = smg_gpu.fcg_solve_mg(D, lat.ndof, B32, mg, 300, 1e-10, 10)
+    r8b = smg_gpu.fcg_solve_mg(D, lat.ndof, B32[:8], mg, 300, 1e-10, 10)
+    for r in (r8a, r32, r8b):
+        assert r.status == 0 and r.true_residual < 1e-10
+    assert r8a.iterations == r8b.iterations
+    assert np.array_equal(r8a.solution, r8b.solution)
+    j = 5
+    assert np.linalg.norm(B32[j] - D.apply_DdagD(r32.solution[j])) / np.linalg.norm(B32[j]) < 1e-10
