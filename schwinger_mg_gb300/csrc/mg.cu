@@ -850,6 +850,72 @@ __global__ void __launch_bounds__(256) k_coarse_apply_flat(const cx<T>* __restri
     if (EPI != 0) block_reduce_finalise<K>(v, partials, ticket, nrhs, FinStore{out, K});
 }
 
+// The same operator with one thread per (coarse site, rhs) forming all NC outputs of its site: each
+// neighbour value is loaded once for the NC outputs and the links of a (direction, j) as NC / 2
+// 16-byte loads shared by the site's rhs lanes, against two 8-byte loads per multiply-add when
+// every output entry has its own thread.
+template <typename T, int EPI, int NC>
+__global__ void __launch_bounds__(256) k_coarse_apply_site(const cx<T>* __restrict__ A, VecView<T> xin,
+                                                           cx<T>* __restrict__ y, int nx, int ny,
+                                                           const cx<T>* __restrict__ w, double* partials,
+                                                           unsigned int* ticket, double* out,
+                                                           const int* __restrict__ gate) {
+    if (gate && *gate == 0) return;  // every right-hand side of the solve has converged
+    constexpr int K = EPI == 2 ? 3 : 1;
+    const int nrhs = xin.nrhs;
+    const int rhs = blockIdx.y * blockDim.x + threadIdx.x;
+    T v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = T(0);
+    if (rhs < nrhs)
+        for (int s = blockIdx.x * blockDim.y + threadIdx.y; s < xin.nsites; s += gridDim.x * blockDim.y) {
+            const int x = s % nx, yy = s / nx;
+            cx<T> acc[NC];
+#pragma unroll
+            for (int i = 0; i < NC; ++i) acc[i] = mk<T>(0, 0);
+#pragma unroll 1
+            for (int d = 0; d < 9; ++d) {
+                const int xn = x + c_dx[d], yn = yy + c_dy[d];
+                const int sn = (xn < 0 ? xn + nx : (xn >= nx ? xn - nx : xn)) +
+                               nx * (yn < 0 ? yn + ny : (yn >= ny ? yn - ny : yn));
+                const cx<T>* __restrict__ Ad = A + ((int64_t)s * 9 + d) * NC * NC;  // [j][i]
+                const cx<T>* __restrict__ Xn = xin.p + (int64_t)sn * NC * nrhs + rhs;  // [dof][rhs]
+                cx<T> xj[NC];
+#pragma unroll
+                for (int j = 0; j < NC; ++j) xj[j] = Xn[(int64_t)j * nrhs];
+#pragma unroll
+                for (int j = 0; j < NC; ++j) {
+#pragma unroll
+                    for (int i = 0; i < NC; ++i) acc[i] = acc[i] + Ad[j * NC + i] * xj[j];
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < NC; ++i) {
+                const int64_t o = ((int64_t)s * NC + i) * nrhs + rhs;
+                y[o] = acc[i];
+                if (EPI == 1) {
+                    v[0] += norm2(acc[i]);
+                } else if (EPI == 2) {
+                    const cx<T> c = cmulc(acc[i], w[o]);
+                    v[0] += c.re;
+                    v[1] += c.im;
+                    v[2] += norm2(acc[i]);
+                }
+            }
+        }
+    if (EPI != 0) block_reduce_finalise<K>(v, partials, ticket, nrhs, FinStore{out, K});
+}
+
+// one thread per (site, rhs) for few right-hand sides (k_coarse_apply_site); SMG_COARSE_SITE=0 keeps
+// one thread per output entry (k_coarse_apply_flat)
+bool coarse_site_on() {
+    static const bool on = [] {
+        const char* e = std::getenv("SMG_COARSE_SITE");
+        return !(e && std::atoi(e) == 0);
+    }();
+    return on;
+}
+
 // ------------------------------------------------------------ persistent coarsest CG
 // The whole coarsest-level CG of one right-hand side in one cooperative
 // launch (SparseCoarseOp::solve without deflation, src/coarse_op.h:492-547).
@@ -1526,6 +1592,26 @@ smg_status vaxpy(smg_context* ctx, VecView<T> y, const cx<T>* x, const double* c
 template <typename T, int NC>
 smg_status coarse_apply_tiled(smg_context* ctx, const Level& L, const cx<T>* A, VecView<T> x, cx<T>* y, int epi,
                               const cx<T>* w, double* out, const int* gate) {
+    if constexpr (NC <= 16) {
+    if (x.nrhs < 32 && coarse_site_on()) {  // few right-hand sides: one thread per (site, rhs)
+        ReduceLaunch rl = reduce_launch(L.nsites, x.nrhs);
+        SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * x.nrhs * 3));
+        double* part = epi ? ctx->red.partials : nullptr;
+        unsigned int* tick = epi ? ctx->red.tickets : nullptr;
+        if (epi == 0)
+            k_coarse_apply_site<T, 0, NC><<<rl.grid, rl.block, 0, ctx->stream>>>(A, x, y, L.nx, L.ny, w, part, tick,
+                                                                                out, gate);
+        else if (epi == 1)
+            k_coarse_apply_site<T, 1, NC><<<rl.grid, rl.block, 0, ctx->stream>>>(A, x, y, L.nx, L.ny, w, part, tick,
+                                                                                out, gate);
+        else
+            k_coarse_apply_site<T, 2, NC><<<rl.grid, rl.block, 0, ctx->stream>>>(A, x, y, L.nx, L.ny, w, part, tick,
+                                                                                out, gate);
+        count_launch(ctx);
+        SMG_CHECK_LAUNCH(ctx);
+        return SMG_OK;
+    }
+    }
     if (x.nrhs < 32) {  // few right-hand sides: one thread per output entry
         ReduceLaunch rl = reduce_launch((int)((int64_t)L.nsites * NC), x.nrhs);
         SMG_TRY(smg_reduce_reserve(ctx, (size_t)rl.grid.x * x.nrhs * 3));
