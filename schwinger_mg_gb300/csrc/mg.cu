@@ -1493,6 +1493,10 @@ struct smg_mg {
     int xp_first = 0, xp_n = 0;
     bool xp_zero = false;
     double xp_omega = 0;
+    // the pre-smoother's last residual r - omega A r left to the packed level-0 restriction: the step
+    // (its r in f_rs[rn_step], A r in f_Ar, omega from mr_omf or rn_omega), or -1
+    int rn_step = -1;
+    double rn_omega = 0;
     std::vector<CoarseWork> cw;
     double* scal = nullptr;  // per-level scalar area
     size_t scal_doubles = 0;
@@ -2066,10 +2070,12 @@ constexpr int kAggSites0 = 16;
 // two-spinors in registers, the warp's block vectors staged in shared memory as output pairs
 // [e][i/2] = (Re V[e][i], Re V[e][i+1], Im V[e][i], Im V[e][i+1]) so that one broadcast 16-byte read
 // feeds four packed FMAs.
-template <int NC>
+template <int NC, bool FUSED>
 __global__ void __launch_bounds__(128) k_restrict0_h(const cx<float>* __restrict__ V, const __half2* __restrict__ r,
                                                      const float* __restrict__ rs, cx<float>* __restrict__ out,
-                                                     TransferGeom t, int nagg) {
+                                                     TransferGeom t, int nagg, const __half2* __restrict__ ar,
+                                                     const float* __restrict__ ars, const float2* __restrict__ om,
+                                                     float omega) {
     constexpr int ne = 2 * kAggSites0, NP = NC / 2;
     __shared__ float4 s_v[4][ne * NP];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -2079,11 +2085,16 @@ __global__ void __launch_bounds__(128) k_restrict0_h(const cx<float>* __restrict
     const int x0 = (B % t.nax) * 4, y0 = (B / t.nax) * 4;
     const int myq = site_q(t.g, x0 + (lane & 3), y0 + ((lane >> 2) & 3));  // lanes 16..31 repeat 0..15
     const float mys = __ldg(rs + myq);
-    uint2 raw[kAggSites0];
+    // FUSED: the input is the last MR step's r - omega A r, formed here from r and A r (the step's
+    // k_mr_rupdate_h, whose output only this restriction would read)
+    const float mya = FUSED ? __ldg(ars + myq) : 0.f;
+    const float2 o = FUSED ? (om ? __ldg(om + rhs) : make_float2(omega, 0.f)) : make_float2(0.f, 0.f);
+    uint2 raw[kAggSites0], rawa[FUSED ? kAggSites0 : 1];
 #pragma unroll
     for (int s = 0; s < kAggSites0; ++s) {
         const int q = __shfl_sync(0xffffffffu, myq, s);
         raw[s] = __ldg(reinterpret_cast<const uint2*>(r) + ((int64_t)q * nrhs + rhs));
+        if constexpr (FUSED) rawa[s] = __ldg(reinterpret_cast<const uint2*>(ar) + ((int64_t)q * nrhs + rhs));
     }
     // float4 k of the aggregate's block vectors holds V entries 2k, 2k+1 = (e, i), (e, i + 1), i even
     const float4* __restrict__ Vb = reinterpret_cast<const float4*>(V + (int64_t)B * ne * NC);
@@ -2101,9 +2112,23 @@ __global__ void __launch_bounds__(128) k_restrict0_h(const cx<float>* __restrict
         const float sc = __shfl_sync(0xffffffffu, mys, s);
         const float2 f0 = __half22float2(*reinterpret_cast<const __half2*>(&raw[s].x));
         const float2 f1 = __half22float2(*reinterpret_cast<const __half2*>(&raw[s].y));
+        float oar = 0.f, oai = 0.f;
+        float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+        if constexpr (FUSED) {
+            const float sa = __shfl_sync(0xffffffffu, mya, s);
+            oar = o.x * sa;
+            oai = o.y * sa;
+            a0 = __half22float2(*reinterpret_cast<const __half2*>(&rawa[s].x));
+            a1 = __half22float2(*reinterpret_cast<const __half2*>(&rawa[s].y));
+        }
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-            const float fr = (j ? f1.x : f0.x) * sc, fi = (j ? f1.y : f0.y) * sc;
+            float fr = (j ? f1.x : f0.x) * sc, fi = (j ? f1.y : f0.y) * sc;
+            if constexpr (FUSED) {  // r - (omega s_a) A r, as k_mr_rupdate_h forms it
+                const float2 a = j ? a1 : a0;
+                fr -= oar * a.x - oai * a.y;
+                fi -= oar * a.y + oai * a.x;
+            }
             const f32x2 FR = f2_pack(fr, fr), FI = f2_pack(fi, fi), FRn = f2_pack(-fr, -fr);
             const float4* __restrict__ vrow = &s_v[w][(2 * s + j) * NP];
 #pragma unroll
@@ -2439,7 +2464,7 @@ smg_status mr_step_h(smg_mg* mg, int it, double omega, bool write_next) {
 // step also writes r_n = b - A x (the residual the cycle restricts after pre-smoothing).  defer_x:
 // the last x pass is left to the caller (mg->xp_*), which folds it into the prolongation.
 smg_status smooth_fine_half(smg_mg* mg, smg_field* x, const smg_field* b, int niter, bool x_is_zero, double omega,
-                            bool keep_residual, bool defer_x = false) {
+                            bool keep_residual, bool defer_x = false, bool defer_last_residual = false) {
     smg_context* ctx = mg->ctx;
     smg_field *r0 = mg->f_rs[0], *Ar = mg->f_Ar, *t = mg->f_t;
     const int V = b->g.V, nrhs = b->nrhs;
@@ -2457,8 +2482,9 @@ smg_status smooth_fine_half(smg_mg* mg, smg_field* x, const smg_field* b, int ni
     count_launch(ctx);
     int first = 0;  // first residual not yet added into x
     bool zero = x_is_zero;
+    const bool fuse_last = defer_last_residual && keep_residual && niter > 0;
     for (int it = 0; it < niter; ++it) {
-        SMG_TRY(mr_step_h(mg, it, omega, it + 1 < niter || keep_residual));
+        SMG_TRY(mr_step_h(mg, it, omega, it + 1 < niter || (keep_residual && !fuse_last)));
         if (it + 1 - first == kMaxMrSteps) {
             SMG_TRY(mr_xupdate_h(mg, x, first, it + 1 - first, zero, omega));
             first = it + 1;
@@ -2473,12 +2499,24 @@ smg_status smooth_fine_half(smg_mg* mg, smg_field* x, const smg_field* b, int ni
     } else {
         SMG_TRY(mr_xupdate_h(mg, x, first, niter - first, zero, omega));
     }
-    mg->f_res = mg->f_rs[niter];
+    mg->f_res = fuse_last ? nullptr : mg->f_rs[niter];
+    mg->rn_step = fuse_last ? niter - 1 : -1;
+    mg->rn_omega = omega;
     return SMG_OK;
 }
 
 TransferGeom transfer_geom(const smg_mg* mg, int l, int nrhs);
 dim3 transfer_block(int nrhs);
+
+// the pre-smoother's last residual update folded into the packed level-0 restriction;
+// SMG_FUSE_LAST_RESIDUAL=0 keeps it as its own kernel
+bool fuse_last_residual_on() {
+    static const bool on = [] {
+        const char* e = std::getenv("SMG_FUSE_LAST_RESIDUAL");
+        return !(e && std::atoi(e) == 0);
+    }();
+    return on;
+}
 
 // the transfers with packed FMAs: SMG_TRANSFER_PACKED=0 keeps the generic kernels and separate x passes
 bool transfer_packed_on() {
@@ -2498,20 +2536,36 @@ bool transfer0_packed(const smg_mg* mg) {
            mg->f_r->prec == SMG_F16 && L.V32 && L.V32s;
 }
 
-smg_status restrict0_packed(smg_mg* mg, const smg_field* r, void* out) {
+// the restriction of the pre-smoother's final residual: f_res, or, when the last MR step left it to
+// this kernel (mg->rn_step >= 0), r - omega A r of that step formed on the fly
+smg_status restrict0_packed(smg_mg* mg, void* out) {
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[0];
     const int nagg = mg->lv[1].nsites, nrhs = mg->work_nrhs;
     const TransferGeom t = transfer_geom(mg, 0, nrhs);
     const dim3 grid((nagg + 3) / 4, nrhs / 32), block(128);
-    const __half2* rp = (const __half2*)r->data;
     cx<float>* o = (cx<float>*)out;
-    if (L.nc_next == 8)
-        k_restrict0_h<8><<<grid, block, 0, ctx->stream>>>(L.V32, rp, r->scale, o, t, nagg);
-    else if (L.nc_next == 16)
-        k_restrict0_h<16><<<grid, block, 0, ctx->stream>>>(L.V32, rp, r->scale, o, t, nagg);
-    else
-        k_restrict0_h<32><<<grid, block, 0, ctx->stream>>>(L.V32, rp, r->scale, o, t, nagg);
+    const bool fused = mg->rn_step >= 0;
+    const smg_field* r = fused ? mg->f_rs[mg->rn_step] : mg->f_res;
+    const __half2* rp = (const __half2*)r->data;
+    const __half2* arp = fused ? (const __half2*)mg->f_Ar->data : nullptr;
+    const float* ars = fused ? mg->f_Ar->scale : nullptr;
+    const float2* om = fused && !(mg->rn_omega > 0) ? mg->mr_omf + (size_t)mg->rn_step * nrhs : nullptr;
+    const float omega = (float)mg->rn_omega;
+    mg->rn_step = -1;
+#define SMG_R0(NC)                                                                                                  \
+    do {                                                                                                            \
+        if (fused)                                                                                                  \
+            k_restrict0_h<NC, true><<<grid, block, 0, ctx->stream>>>(L.V32, rp, r->scale, o, t, nagg, arp, ars, om, \
+                                                                     omega);                                        \
+        else                                                                                                        \
+            k_restrict0_h<NC, false><<<grid, block, 0, ctx->stream>>>(L.V32, rp, r->scale, o, t, nagg, nullptr,     \
+                                                                      nullptr, nullptr, 0.f);                       \
+    } while (0)
+    if (L.nc_next == 8) SMG_R0(8);
+    else if (L.nc_next == 16) SMG_R0(16);
+    else SMG_R0(32);
+#undef SMG_R0
     count_launch(ctx);
     SMG_CHECK_LAUNCH(ctx);
     return SMG_OK;
@@ -3119,12 +3173,13 @@ smg_status cycle_fine(smg_mg* mg, smg_field* x, const smg_field* b) {
     // packed level-0 transfers: the pre-smoothing x pass is folded into the prolongation
     const bool packed = std::is_same<T, float>::value && transfer0_packed(mg);
     if (packed)
-        SMG_TRY(smooth_fine_half(mg, x, b, mg->p.pre_smooth, true, mg->lv[0].rich_omega, true, true));
+        SMG_TRY(smooth_fine_half(mg, x, b, mg->p.pre_smooth, true, mg->lv[0].rich_omega, true, true,
+                                 fuse_last_residual_on()));
     else
         SMG_TRY(smooth_fine<T>(mg, x, b, mg->p.pre_smooth, true));
     CoarseWork& nw = mg->cw[1];
     if (packed)
-        SMG_TRY(restrict0_packed(mg, mg->f_res, nw.b));
+        SMG_TRY(restrict0_packed(mg, nw.b));
     else if (mg->f_r->prec == SMG_F16)
         SMG_TRY(restrict_half(mg, mg->f_res, nw.b));
     else
