@@ -54,6 +54,7 @@ torch.distributed.run with N ranks.
 from __future__ import annotations
 
 import argparse
+import atexit
 import ctypes as Cc
 import json
 import os
@@ -80,36 +81,68 @@ def peaks():
     return 6800.0, "fallback"
 
 
-class Clocks:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+class ClockSampler:
+    """One nvidia-smi process per benchmark process sampling SM clocks, power and throttle reasons
+    every 200 ms with a timestamp, started before any timed work so that its start-up (NVML
+    initialisation) never falls inside a timed region."""
 
-    def __init__(self, device: int):
-        self.device = device
+    def __init__(self):
         self.proc = None
-        self.path = Path(tempfile.gettempdir()) / f"smg_clocks_{os.getpid()}.csv"
+        self.path = None
+        self.f = None
 
-    def __enter__(self):
+    def start(self, device: int):
+        if self.proc is not None:
+            return
+        self.path = Path(tempfile.gettempdir()) / f"smg_clocks_{os.getpid()}.csv"
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.device),
-                 "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                ["nvidia-smi", "-i", str(device),
+                 "--query-gpu=timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
-            # the sampler's start-up (NVML initialisation) stays out of the timed region: wait for its
-            # first sample (up to 3 s), then a little more
-            t_end = time.monotonic() + 3.0
-            while time.monotonic() < t_end and self.proc.poll() is None:
-                if self.path.stat().st_size > 0:
-                    break
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+            t_end = time.monotonic() + 5.0  # first sample before anything is timed
+            while time.monotonic() < t_end and self.proc.poll() is None and self.path.stat().st_size == 0:
                 time.sleep(0.02)
-            time.sleep(0.25)
         except (OSError, FileNotFoundError):
             self.proc = None
-        return self
 
-    def __exit__(self, *a):
+    def rows(self, t0: float, t1: float):
+        """Samples taken between the wall-clock times t0 and t1 (seconds since the epoch).  The sampler
+        stops here (nvidia-smi writes its samples out when it ends) and the next timed region starts
+        another one before its timing begins."""
+        if self.proc is None or self.path is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        self.proc = None
+        if not self.path.exists():
+            return None
+        text = self.path.read_text()
+        try:
+            self.path.unlink()
+        except OSError:
+            pass
+        out = []
+        for line in text.splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                ts = time.mktime(time.strptime(parts[0].split(".")[0], "%Y/%m/%d %H:%M:%S"))
+                ts += float("0." + parts[0].split(".")[1]) if "." in parts[0] else 0.0
+                out.append((ts, float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except (ValueError, IndexError):
+                continue
+        return [r for r in out if t0 <= r[0] <= t1]
+
+    def stop(self):
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -117,29 +150,44 @@ class Clocks:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
             self.f.close()
+            try:
+                self.path.unlink()
+            except OSError:
+                pass
+            self.proc = None
+
+
+SAMPLER = ClockSampler()
+atexit.register(SAMPLER.stop)
+
+
+class Clocks:
+    """The clock samples that fall inside one timed region (the process-wide sampler, started at the
+    first use if the workload did not start it earlier)."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.t0 = self.t1 = 0.0
+
+    def __enter__(self):
+        SAMPLER.start(self.device)
+        self.t0 = time.time()
+        return self
+
+    def __exit__(self, *a):
+        self.t1 = time.time()
+        time.sleep(0.25)  # the sample that covers the region's end
 
     def summary(self):
-        if self.proc is None or not self.path.exists():
+        rows = SAMPLER.rows(self.t0 - 0.1, self.t1 + 0.25)
+        if rows is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        rows = []
-        for line in self.path.read_text().splitlines():
-            parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
-            except ValueError:
-                continue
-        try:
-            self.path.unlink()
-        except OSError:
-            pass
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for _, _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
-        return {"sm_mhz": float(np.median([r[0] for r in rows])), "sm_max_mhz": max(r[1] for r in rows),
-                "power_w_max": max(r[2] for r in rows), "reasons": reasons, "samples": len(rows)}
+        reasons = sorted({names[i] for *_, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median([r[1] for r in rows])), "sm_max_mhz": max(r[2] for r in rows),
+                "power_w_max": max(r[3] for r in rows), "reasons": reasons, "samples": len(rows)}
 
 
 def dist_env():
@@ -369,6 +417,7 @@ def run_ours(args, ws, rank, local):
     torch.cuda.set_device(local)
     ctx = smg.Context(local)
     lib = smg.lib()
+    SAMPLER.start(local)  # clock sampling from before any set-up or timed work
     peak, peak_kind = peaks()
     c, cfg = workload_config(args.workload, args)
     out = {"metric": METRIC, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "scaling": "weak",
