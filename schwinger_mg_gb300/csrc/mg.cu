@@ -2069,7 +2069,8 @@ constexpr int kAggSites0 = 16;
 // generic kernel with the InHalf reader, k_restrict_agg): one warp per aggregate, the lane's 16
 // two-spinors in registers, the warp's block vectors staged in shared memory as output pairs
 // [e][i/2] = (Re V[e][i], Re V[e][i+1], Im V[e][i], Im V[e][i+1]) so that one broadcast 16-byte read
-// feeds four packed FMAs.
+// feeds four packed FMAs.  FUSED restricts r - omega A r of the last MR step, formed from that step's
+// FP16 r and A r (scales per site, omega per rhs) in place of the stored r_n.
 template <int NC, bool FUSED>
 __global__ void __launch_bounds__(128) k_restrict0_h(const cx<float>* __restrict__ V, const __half2* __restrict__ r,
                                                      const float* __restrict__ rs, cx<float>* __restrict__ out,
