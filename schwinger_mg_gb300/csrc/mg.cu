@@ -1468,6 +1468,8 @@ struct CoarseWork {  // per level l >= 1, per precision
     // x = (xp_zero ? 0 : x) + sum_{k < xp_n} omega_k r16[k]
     int xp_n = 0;
     bool xp_zero = false;
+    // the pre-smoother's last residual left to the packed restriction: that MR step, or -1
+    int rn_step = -1;
 };
 
 struct smg_mg {
@@ -2262,12 +2264,14 @@ constexpr int kAggSitesC = 4;
 // Restriction out_i = sum_e conj(V[e][i]) r_e of the FP16 residual (the generic kernel with the
 // InHalfC reader): one warp per aggregate, the lane's 64 FP16 inputs in registers, the block vectors
 // (the level's output-pair copy V32o) staged in shared memory by asynchronous copies.
-template <int NC>
+template <int NC, bool FUSED>
 __global__ void __launch_bounds__(NC == 32 ? 64 : 128) k_restrict_c16p(const float4* __restrict__ Vo,
                                                                        const __half2* __restrict__ r,
                                                                        const float* __restrict__ rs,
                                                                        cx<float>* __restrict__ out, TransferGeom t,
-                                                                       int nagg) {
+                                                                       int nagg, const __half2* __restrict__ ar,
+                                                                       const float* __restrict__ ars,
+                                                                       const float2* __restrict__ om) {
     constexpr int WPB = NC == 32 ? 2 : 4, NE = kAggSitesC * kC16Dofs, NP = NC / 2;
     __shared__ float4 s_v[WPB][NE * NP];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -2277,15 +2281,23 @@ __global__ void __launch_bounds__(NC == 32 ? 64 : 128) k_restrict_c16p(const flo
 #pragma unroll 4
     for (int k = lane; k < NE * NP; k += 32) cp_async16(&s_v[w][k], src + k);
     const int bx = (B % t.nax) * 2, by = (B / t.nax) * 2;
-    __half2 raw[kAggSitesC][kC16Dofs];
-    float sc[kAggSitesC];
+    // FUSED: the input is the last MR step's r - omega A r (k_c16_rupdate's arithmetic), formed here
+    __half2 raw[kAggSitesC][kC16Dofs], rawa[FUSED ? kAggSitesC : 1][FUSED ? kC16Dofs : 1];
+    float sc[kAggSitesC], sca[kAggSitesC];
+    const float2 o = FUSED ? __ldg(om + lane) : make_float2(0.f, 0.f);
 #pragma unroll
     for (int l = 0; l < kAggSitesC; ++l) {
         const int64_t site = (int64_t)(bx + (l & 1)) + (int64_t)t.nx * (by + (l >> 1));
         sc[l] = __ldg(rs + 2 * site + (lane >> 4));
+        sca[l] = FUSED ? __ldg(ars + 2 * site + (lane >> 4)) : 0.f;
         const __half2* __restrict__ rp = r + site * kC16Dofs * 32 + lane;
 #pragma unroll
         for (int d = 0; d < kC16Dofs; ++d) raw[l][d] = rp[d * 32];
+        if constexpr (FUSED) {
+            const __half2* __restrict__ ap = ar + site * kC16Dofs * 32 + lane;
+#pragma unroll
+            for (int d = 0; d < kC16Dofs; ++d) rawa[l][d] = ap[d * 32];
+        }
     }
     cp_async_wait_all();
     __syncwarp();
@@ -2297,7 +2309,13 @@ __global__ void __launch_bounds__(NC == 32 ? 64 : 128) k_restrict_c16p(const flo
 #pragma unroll
         for (int d = 0; d < kC16Dofs; ++d) {
             const float2 f = __half22float2(raw[l][d]);
-            const float fr = f.x * sc[l], fi = f.y * sc[l];
+            float fr = f.x * sc[l], fi = f.y * sc[l];
+            if constexpr (FUSED) {
+                const float2 y = __half22float2(rawa[l][d]);
+                const float yr = sca[l] * y.x, yi = sca[l] * y.y;
+                fr -= o.x * yr - o.y * yi;
+                fi -= o.x * yi + o.y * yr;
+            }
             const f32x2 FR = f2_pack(fr, fr), FI = f2_pack(fi, fi), FRn = f2_pack(-fr, -fr);
             const float4* __restrict__ vrow = &s_v[w][(l * kC16Dofs + d) * NP];
 #pragma unroll
@@ -2737,7 +2755,8 @@ smg_status smooth_fine(smg_mg* mg, smg_field* x, const smg_field* b, int niter, 
 // (or b) in FP16, then per step A r_k in FP16 with <A r_k, r_k>, ||A r_k||^2 and omega_k from the
 // tensor-core apply, r_{k+1} = r_k - omega_k A r_k, and x += sum_k omega_k r_k once at the end (x and
 // all arithmetic FP32).  The final residual stays in the ring slot res16 for the restriction.
-smg_status mr_coarse_half(smg_mg* mg, int l, void* x, const void* b, int niter, bool x_is_zero, bool defer_x = false) {
+smg_status mr_coarse_half(smg_mg* mg, int l, void* x, const void* b, int niter, bool x_is_zero, bool defer_x = false,
+                          bool defer_last_residual = false) {
     smg_context* ctx = mg->ctx;
     const Level& L = mg->lv[l];
     CoarseWork& w = mg->cw[l];
@@ -2755,12 +2774,14 @@ smg_status mr_coarse_half(smg_mg* mg, int l, void* x, const void* b, int niter, 
         float* om = w.mr16_om + (size_t)it * nrhs * 2;
         SMG_TRY(smg_coarse_tc_apply_mr16(ctx, L.Atc, L.nx, L.ny, nrhs, w.r16[it], w.r16s[it], w.ar16, w.ar16s, sc, om,
                                          device_err(mg)));
+        if (defer_last_residual && it + 1 == niter) break;  // the restriction forms r - omega A r itself
         k_c16_rupdate<<<ugrid, 256, 0, ctx->stream>>>((const __half2*)w.r16[it], w.r16s[it], (const __half2*)w.ar16,
                                                       w.ar16s, (const float2*)om, (__half2*)w.r16[it + 1],
                                                       w.r16s[it + 1], L.nsites);
         count_launch(ctx);
         SMG_CHECK_LAUNCH(ctx);
     }
+    w.rn_step = defer_last_residual && niter > 0 ? niter - 1 : -1;
     if (defer_x) {  // the packed prolongation into this level adds the steps (k_prolong_c16p)
         w.xp_n = niter;
         w.xp_zero = x_is_zero;
@@ -2825,15 +2846,28 @@ smg_status restrict_c16_packed(smg_mg* mg, int l, void* out) {
     CoarseWork& w = mg->cw[l];
     const int nagg = mg->lv[l + 1].nsites;
     const TransferGeom t = transfer_geom(mg, l, 32);
-    const __half2* r = (const __half2*)w.r16[w.res16];
-    const float* rs = w.r16s[w.res16];
+    // the last MR step's r - omega A r formed in the kernel when that step left it (rn_step >= 0)
+    const bool fused = w.rn_step >= 0;
+    const int slot = fused ? w.rn_step : w.res16;
+    const __half2* r = (const __half2*)w.r16[slot];
+    const float* rs = w.r16s[slot];
+    const __half2* ar = fused ? (const __half2*)w.ar16 : nullptr;
+    const float* ars = fused ? w.ar16s : nullptr;
+    const float2* om = fused ? (const float2*)w.mr16_om + (size_t)w.rn_step * 32 : nullptr;
+    w.rn_step = -1;
     cx<float>* o = (cx<float>*)out;
-    if (L.nc_next == 8)
-        k_restrict_c16p<8><<<(nagg + 3) / 4, 128, 0, ctx->stream>>>(L.V32o, r, rs, o, t, nagg);
-    else if (L.nc_next == 16)
-        k_restrict_c16p<16><<<(nagg + 3) / 4, 128, 0, ctx->stream>>>(L.V32o, r, rs, o, t, nagg);
-    else
-        k_restrict_c16p<32><<<(nagg + 1) / 2, 64, 0, ctx->stream>>>(L.V32o, r, rs, o, t, nagg);
+#define SMG_RC16(NC, G, B)                                                                                         \
+    do {                                                                                                           \
+        if (fused)                                                                                                 \
+            k_restrict_c16p<NC, true><<<G, B, 0, ctx->stream>>>(L.V32o, r, rs, o, t, nagg, ar, ars, om);          \
+        else                                                                                                       \
+            k_restrict_c16p<NC, false><<<G, B, 0, ctx->stream>>>(L.V32o, r, rs, o, t, nagg, nullptr, nullptr,      \
+                                                                 nullptr);                                         \
+    } while (0)
+    if (L.nc_next == 8) SMG_RC16(8, (nagg + 3) / 4, 128);
+    else if (L.nc_next == 16) SMG_RC16(16, (nagg + 3) / 4, 128);
+    else SMG_RC16(32, (nagg + 1) / 2, 64);
+#undef SMG_RC16
     count_launch(ctx);
     SMG_CHECK_LAUNCH(ctx);
     return SMG_OK;
@@ -3134,7 +3168,7 @@ smg_status cycle_coarse(smg_mg* mg, int l, void* x, const void* b) {
     // packed FP16-level transfers: the pre-smoothing x pass is folded into the prolongation
     const bool packed = std::is_same<T, float>::value && transfer_c16_packed(mg, l);
     if (packed)
-        SMG_TRY(mr_coarse_half(mg, l, x, b, mg->p.pre_smooth, true, true));
+        SMG_TRY(mr_coarse_half(mg, l, x, b, mg->p.pre_smooth, true, true, fuse_last_residual_on()));
     else
         SMG_TRY(smooth_coarse<T>(mg, l, x, b, mg->p.pre_smooth, true));
     // residual of the smoothed x is in cw[l].r (or, FP16, in the ring slot cw[l].res16)
